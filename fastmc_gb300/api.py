@@ -1,0 +1,219 @@
+"""Python API over the C ABI (include/fastmc_gb300.h).
+
+    sys = System.load("inputs/")            # FIELD, CONFIG, CONTROL
+    plain = PlainEngine(sys)                # per-move drop-in path
+    r = plain.insertion(1, xyz)             # insertion (mc_moves.f:150)
+    acc = plain.commit(rande)               # energy_eval + accept_move
+
+    batch = Batch([sys], chains)            # device-resident chains
+    stats = batch.run(256)                  # 256 main-loop iterations
+
+Every call goes to the CUDA library; a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+
+class System:
+    """Host-side inputs and tables of one framework (the reference start-up)."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def load(cls, directory: str) -> "System":
+        lib = L.load()
+        h = C.c_void_p()
+        L.check(lib.fmc_system_load(directory.encode(), C.byref(h)))
+        return cls(h.value)
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def info(self) -> L.SystemInfo:
+        inf = L.SystemInfo()
+        L.check(L.load().fmc_system_get_info(self._h, C.byref(inf)))
+        return inf
+
+    def set_fugacity(self, iguest: int, pascal: float) -> None:
+        L.check(L.load().fmc_system_set_fugacity(self._h, iguest, pascal))
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            L.load().fmc_system_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _result_dict(r: L.MoveResult, maxmls: int, ns: int) -> dict:
+    return {
+        "estep": r.estep, "ewld1": r.ewld1, "ewld2": r.ewld2, "vdw": r.vdw,
+        "delrc": r.delrc, "delE": np.array(r.delE[:maxmls]), "overlap": bool(r.overlap),
+        "surface": bool(r.surface), "surface_old": bool(r.surface_old), "status": r.status,
+        "newxyz": np.array(r.newxyz[:3 * ns]).reshape(ns, 3),
+    }
+
+
+class PlainEngine:
+    """Per-move drop-in: device mirror of one chain driven by the host."""
+
+    def __init__(self, system: System, precision: int = L.FMC_PREC_FP64,
+                 guest_capacity: int = 1024):
+        self.system = system
+        self._info = system.info()
+        h = C.c_void_p()
+        L.check(L.load().fmc_plain_create(system.handle, precision, guest_capacity, C.byref(h)))
+        self._h = h
+
+    def _ns(self, iguest: int) -> int:
+        return self._info.guest_nsites[iguest - 1]
+
+    def full_ewald(self) -> np.ndarray:
+        out = (C.c_double * 4)()
+        L.check(L.load().fmc_full_ewald(self._h, out))
+        return np.array(out[:])
+
+    def insertion(self, iguest: int, xyz) -> dict:
+        a = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(-1))
+        r = L.MoveResult()
+        L.check(L.load().fmc_insertion(self._h, iguest, a.ctypes.data_as(L.dp), C.byref(r)))
+        return _result_dict(r, self._info.maxmls, self._ns(iguest))
+
+    def deletion(self, iguest: int, choice: int) -> dict:
+        r = L.MoveResult()
+        L.check(L.load().fmc_deletion(self._h, iguest, choice, C.byref(r)))
+        return _result_dict(r, self._info.maxmls, self._ns(iguest))
+
+    def guest_energy(self, iguest: int, choice: int) -> dict:
+        r = L.MoveResult()
+        L.check(L.load().fmc_guest_energy(self._h, iguest, choice, C.byref(r)))
+        return _result_dict(r, self._info.maxmls, self._ns(iguest))
+
+    def displace(self, iguest: int, choice: int, abcq: Sequence[float]) -> dict:
+        a = np.ascontiguousarray(np.asarray(abcq, dtype=np.float64))
+        r = L.MoveResult()
+        L.check(L.load().fmc_displace(self._h, iguest, choice, a.ctypes.data_as(L.dp), C.byref(r)))
+        return _result_dict(r, self._info.maxmls, self._ns(iguest))
+
+    def commit(self, rande: float) -> bool:
+        acc = C.c_int()
+        L.check(L.load().fmc_metropolis_commit(self._h, rande, C.byref(acc)))
+        return bool(acc.value)
+
+    def nummols(self, iguest: int = 1) -> int:
+        n = C.c_int()
+        L.check(L.load().fmc_plain_get_nummols(self._h, iguest, C.byref(n)))
+        return n.value
+
+    def coords(self, iguest: int = 1) -> np.ndarray:
+        n = self.nummols(iguest)
+        ns = self._ns(iguest)
+        out = np.zeros(max(1, 3 * ns * n))
+        L.check(L.load().fmc_plain_get_coords(self._h, iguest, out.ctypes.data_as(L.dp), out.size))
+        return out[:3 * ns * n].reshape(n * ns, 3)
+
+    def sk(self) -> np.ndarray:
+        nk, nm = self._info.newld, self._info.maxmls + 1
+        out = np.zeros(2 * nk * nm)
+        L.check(L.load().fmc_plain_get_sk(self._h, out.ctypes.data_as(L.dp), out.size))
+        return out.reshape(nk, nm, 2)
+
+    def energy(self) -> np.ndarray:
+        out = np.zeros(self._info.maxmls)
+        L.check(L.load().fmc_plain_get_energy(self._h, out.ctypes.data_as(L.dp), out.size))
+        return out
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            L.load().fmc_plain_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Device-resident GCMC chains over one or more systems."""
+
+    def __init__(self, systems: List[System], chains: Sequence[dict],
+                 precision: int = L.FMC_PREC_FP32, guest_capacity: int = 1024):
+        self.systems = systems
+        arr = (C.c_void_p * len(systems))(*[s.handle.value for s in systems])
+        specs = (L.ChainSpec * len(chains))()
+        for i, c in enumerate(chains):
+            specs[i].system = int(c.get("system", 0))
+            specs[i].pressure_pa = float(c.get("pressure_pa", -1.0))
+            specs[i].seed = int(c.get("seed", i + 1))
+            specs[i].create_molecules = int(c.get("create_molecules", -1))
+        h = C.c_void_p()
+        L.check(L.load().fmc_batch_create(arr, len(systems), specs, len(chains), precision,
+                                          guest_capacity, C.byref(h)))
+        self._h = h
+        self.nchains = len(chains)
+
+    def set_log(self, cap: int) -> None:
+        L.check(L.load().fmc_batch_set_log(self._h, cap))
+
+    def run(self, nmoves: int, fugacity: Optional[np.ndarray] = None):
+        st = (L.ChainStats * self.nchains)()
+        if fugacity is not None:
+            f = np.ascontiguousarray(np.asarray(fugacity, dtype=np.float64))
+            L.check(L.load().fmc_batch_run_cycle(self._h, nmoves, f.ctypes.data_as(L.dp), st))
+        else:
+            L.check(L.load().fmc_batch_run(self._h, nmoves, st))
+        return st
+
+    def stats(self):
+        st = (L.ChainStats * self.nchains)()
+        L.check(L.load().fmc_batch_get_stats(self._h, st))
+        return st
+
+    def log(self, chain: int, cap: int):
+        buf = (L.MoveLog * max(1, cap))()
+        n = C.c_int()
+        L.check(L.load().fmc_batch_get_log(self._h, chain, buf, cap, C.byref(n)))
+        return list(buf[:n.value])
+
+    def coords(self, chain: int, cap: int = 1 << 16) -> np.ndarray:
+        out = np.zeros(cap)
+        n = C.c_int()
+        L.check(L.load().fmc_batch_get_coords(self._h, chain, out.ctypes.data_as(L.dp), cap, C.byref(n)))
+        return out, n.value
+
+    def sk(self, chain: int, nk: int, maxmls: int) -> np.ndarray:
+        out = np.zeros(2 * nk * (maxmls + 1))
+        L.check(L.load().fmc_batch_get_sk(self._h, chain, out.ctypes.data_as(L.dp), out.size))
+        return out.reshape(nk, maxmls + 1, 2)
+
+    def last_timing(self):
+        ms = C.c_double()
+        ev = C.c_int64()
+        mv = C.c_int64()
+        L.check(L.load().fmc_batch_last_timing(self._h, C.byref(ms), C.byref(ev), C.byref(mv)))
+        return ms.value, ev.value, mv.value
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            L.load().fmc_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,387 @@
+// device_core.cuh -- device data structures and the cooperative (one CTA)
+// trial-move energy evaluation for sm_103a.
+//
+// Layout in HBM (all L2-resident for the benchmark sizes):
+//  * framework atoms sorted by cell, z fastest: FP64 (x,y,z,q) records for
+//    the FP64 path, and FP32 hi/lo pairs (x_hi,y_hi,z_hi,q)+(x_lo,y_lo,z_lo,-)
+//    for the FP32 path, so that r = |p - a| keeps ~1 ulp of FP32 relative
+//    accuracy even at 100 A coordinates;
+//  * k-vectors in the reference order (ewald.f:151-315) as (l,m,n) and a_k;
+//  * per chain: guest site coordinates by slot, the molecule order the
+//    reference keeps (molxxx, mc_moves.f:574-590) as a slot list, the FP64
+//    structure factor of each guest type, FP32 mirrors of S(k) and the s(k)
+//    scratch of the last evaluation (the reference's ckcsnew/ckssnew).
+//
+// One CTA evaluates one guest position: the framework part scans the cell
+// columns that intersect the sphere of radius rc + r_mol around the
+// molecule (load-balanced over the CTA through a prefix sum of the column
+// segments), the guest part loops over guest molecules, and the k-space
+// part gives each thread a strided set of k-vectors with per-site power
+// tables e^{i 2 pi j s_d} in shared memory.  Reductions are fixed-order
+// warp-shuffle trees, so results are bitwise reproducible.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fmcdev {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxS = 8;    // sites per guest
+constexpr int kMaxG = 4;    // guest types
+constexpr int kMaxM = 8;    // molecule types
+constexpr int kMaxT = 16;   // atom types
+constexpr int kMaxKm = 40;  // kmax per axis + 1
+constexpr int kMaxSeg = 1536;
+
+// status word bits (ChainHdr::status)
+constexpr int kStTableLow = 1;     // pair closer than one grid step
+constexpr int kStSegOverflow = 2;  // too many framework segments
+constexpr int kStCapacity = 4;     // guest capacity exceeded
+constexpr int kStNonFinite = 8;    // non-finite energy
+constexpr int kStBadChoice = 16;   // molecule index out of range
+constexpr int kStKmax = 32;        // kmax beyond the shared tables
+
+constexpr double kPi = 3.141592653589793;
+constexpr double kSqrPi = 1.7724538509055159;
+constexpr double kR4pie0 = 138935.4835;
+constexpr double kBoltz = 1.3806503e-23;
+constexpr double kRgas = 8.314472 / 4184.0;
+constexpr double kMinAngle = kPi / 18.0;
+constexpr double kDelrMin = 0.1;
+
+// ----------------------------------------------------------------- params
+struct GuestType {
+  int mol;        // molecule type (1-based)
+  int ns;         // sites
+  int insert0;    // "create molecules"
+  int pad;
+  double q[kMaxS];
+  double mass[kMaxS];
+  double tmpl[kMaxS][3];   // centred template (readinputs.f:221-243)
+  int type[kMaxS];         // atom type 1..ntpatm
+  int frz[kMaxS];
+  double ewald3en;
+  double rmax;             // max site distance from the template centre
+  double delr;             // displacement size / list skin
+  double disp_ratio, tran_ratio, rota_ratio;
+  float mcinsf, mcdelf, mcdisf, mcjmpf, mcswpf, mctraf, mcrotf, mcswif;
+};
+
+// Per-system data, shared by every chain that uses the system.
+struct SysDev {
+  // cell
+  int imcon;
+  double cell[9], rcell[9], box[3];
+  double volm, statvolm, temp, beta, engunit, epsq, alpha;
+  double rcut, rc2, overlap_sq, surftol;
+  double sumchg0;          // system charge without guests
+  double chgsum_fw;        // framework charge (chgsum_mol of the framework)
+  int maxmls, ntpguest, ntpatm, fw_mol;
+  int eqsteps, nwindsteps, minchk, laccsample;
+  // framework
+  int nfw;
+  const double4 *fw64;     // x,y,z,q (wrapped into the cell for imcon 1/2)
+  const float4 *fwhi;      // x_hi,y_hi,z_hi,q
+  const float4 *fwlo;      // x_lo,y_lo,z_lo,0
+  const int *fwtype;
+  int use_cells;
+  int nc[3];
+  double csz[3];
+  const int *cell_start;   // [nc0*nc1*nc2+1], z fastest
+  // tables
+  int mxegrd;
+  double rdrewd, rdlrpot;
+  const double *erc;       // [mxegrd+3], 1-based
+  const double *vvv;       // [ntab][mxegrd+3]
+  const float4 *ercq;      // per interval (A,B,C,0): value = A + p(B + pC)
+  const float4 *vvvq;      // [ntab][mxegrd+3]
+  int tabstride;           // mxegrd+3
+  const int *pairtab;      // [(ntpatm+1)^2] -> table row or -1
+  const double *sig2;      // [(ntpatm+1)^2] (surftol + sigma)^2
+  const double *steadd;    // [loc2 pair] tail constants
+  const int *numtyp_fw, *numfrz_fw;   // [ntpatm+1]
+  // k-space
+  int nk, kmax[3];
+  const int4 *klmn;        // (l,m,n,0)
+  const double *akk;
+  const float *akk32;
+  const double2 *skfw;     // framework S(k)
+  double krecip;           // 2 * rvolm * r4pie0 / epsq
+  // guests
+  GuestType g[kMaxG];
+};
+
+// Per-chain scalar state (one record per chain in global memory).
+struct ChainHdr {
+  float u[97];
+  float c, cd, cm;
+  int ir, jr;
+  int nummols[kMaxG];
+  int nslots[kMaxG];       // high-water mark of slots
+  int nfree[kMaxG];
+  int status;
+  double energy[kMaxM + 1];      // energy(mol), 1-based
+  double chgsum_mol[kMaxM + 1];
+  double sumchg;
+  double surfacemols[kMaxM + 1];
+  int numtyp[kMaxT + 1], numfrz[kMaxT + 1];
+  int numtyp_mol[kMaxM + 1][kMaxT + 1];
+  int numfrz_mol[kMaxM + 1][kMaxT + 1];
+  double delrdisp[kMaxG], tran_delr[kMaxG];
+  double rotangle, rota_rotangle;
+  double fuga[kMaxG];
+  long long ins_count[kMaxG], accept_ins[kMaxG], del_count[kMaxG], accept_del[kMaxG];
+  long long disp_count[kMaxG], accept_disp[kMaxG], tran_count[kMaxG], accept_tran[kMaxG];
+  long long rota_count[kMaxG], accept_rota[kMaxG];
+  long long gcmccount, prodcount, rollcount;
+  int production, pad0;
+  double chainstats[kMaxG][6];
+  double wsum;
+  double wacc[kMaxG][8];
+  long long windows;
+  long long moves, evals, overlap_exits;
+  long long attempts[5], accepts[5];
+  long long log_n;
+  int system;
+  int pad1;
+};
+
+// Per-chain arrays.
+struct ChainArrays {
+  double *gpos;     // [chain][g][slot][site] x,y,z (stride 3)
+  float4 *ghi;      // [chain][g][slot][site] hi mirror (x,y,z,q)
+  float4 *glo;      // [chain][g][slot][site] lo mirror
+  int *ord;         // [chain][g][cap] slot ids in molecule order
+  int *freel;       // [chain][g][cap]
+  double2 *sk;      // [chain][g][nkmax] guest S(k)
+  float2 *sk32;     // [chain][maxmls+1][nkmax]: per mol type and total (FP32 mirror)
+  double2 *snew;    // [chain][nkmax] scratch s(k) of the evaluated position
+  double2 *sold;    // [chain][nkmax] scratch s(k) of the old position
+  int cap;          // molecules per guest type
+  int nkmax;
+  int nmt;          // rows of sk32 per chain (max maxmls over systems + 1)
+};
+
+// Description of one trial move (shared memory; copied to global between
+// the evaluate and commit kernels of the per-move ABI).
+struct MoveCtx {
+  int kind;           // 1 insert, 2 delete, 3 displace, 4 translate, 5 rotate
+  int g;              // guest type, 0-based
+  int choice;         // 1-based molecule (delete / displace)
+  int slot;           // storage slot of the molecule
+  int ns;
+  int overlap;
+  int surf_new, surf_old;
+  int accepted;
+  int evaluated;
+  int npos;           // 1 or 2 positions evaluated
+  int pad;
+  double pos[2][kMaxS][3];   // [0] = new / inserted / deleted, [1] = old (displace)
+  double estep;
+  double rande;
+  double delrc;
+  double delE[kMaxM + 1];
+  double delrc_mol[kMaxM + 1];
+  double parts[4];           // ewld1, ewld2, vdw, delrc of position 0
+  double ewld1_b;
+  double chgtmp, engsictmp;
+};
+
+struct Acc {  // per-position partial sums
+  double e2_fw, vdw_fw;
+  double e2_g[kMaxG], vdw_g[kMaxG];
+  double recip;
+  double mix[kMaxM + 1];
+};
+
+// ----------------------------------------------------------- MZT generator
+// duni (utility_pack.f:2768-2857): REAL*4 lagged subtract-with-borrow plus
+// a Weyl term; bit-exact because only float add/sub/compare are used.
+__device__ __forceinline__ double duni_next(ChainHdr &h) {
+  float uni = h.u[h.ir - 1] - h.u[h.jr - 1];
+  if (uni < 0.0f) uni = uni + 1.0f;
+  h.u[h.ir - 1] = uni;
+  h.ir = h.ir - 1;
+  if (h.ir == 0) h.ir = 97;
+  h.jr = h.jr - 1;
+  if (h.jr == 0) h.jr = 97;
+  h.c = h.c - h.cd;
+  if (h.c < 0.0f) h.c = h.c + h.cm;
+  uni = uni - h.c;
+  if (uni < 0.0f) uni = uni + 1.0f;
+  return double(uni);
+}
+
+// Initialisation from the clock values the reference reads
+// (utility_pack.f:2796-2852).
+__host__ __device__ inline void duni_init(ChainHdr &h, int ms, int sec) {
+  int i = (ms * 3) % 177 + 1, j = (sec * 23) % 177 + 1, k = (ms * 5) % 177 + 1,
+      l = (sec * 3) % 168;
+  h.ir = 97;
+  h.jr = 33;
+  for (int ii = 0; ii < 97; ++ii) {
+    float s = 0.0f, t = 0.5f;
+    for (int jj = 0; jj < 24; ++jj) {
+      int m = (((i * j) % 179) * k) % 179;
+      i = j;
+      j = k;
+      k = m;
+      l = (53 * l + 1) % 169;
+      if ((l * m) % 64 >= 32) s = s + t;
+      t = 0.5f * t;
+    }
+    h.u[ii] = s;
+  }
+  h.c = 362436.0f / 16777216.0f;
+  h.cd = 7654321.0f / 16777216.0f;
+  h.cm = 16777213.0f / 16777216.0f;
+}
+
+// ------------------------------------------------------------- geometry
+__device__ __forceinline__ void cartesian(const SysDev &S, double a, double b,
+                                          double c, double *o) {
+  o[0] = a * S.cell[0] + b * S.cell[3] + c * S.cell[6];
+  o[1] = a * S.cell[1] + b * S.cell[4] + c * S.cell[7];
+  o[2] = a * S.cell[2] + b * S.cell[5] + c * S.cell[8];
+}
+
+// rotation (utility_pack.f:3480-3524)
+__device__ inline void rotate_sites(double (*p)[3], int n, const double *cm,
+                                    double q1, double q2, double q3, double q4) {
+  double Q[9];
+  Q[0] = 2.0 * q2 * q2 + 2.0 * q1 * q1 - 1.0;
+  Q[1] = 2.0 * q2 * q3 - 2.0 * q1 * q4;
+  Q[2] = 2.0 * q2 * q4 + 2.0 * q1 * q3;
+  Q[3] = 2.0 * q2 * q3 + 2.0 * q1 * q4;
+  Q[4] = 2.0 * q1 * q1 + 2.0 * q3 * q3 - 1.0;
+  Q[5] = 2.0 * q3 * q4 - 2.0 * q1 * q2;
+  Q[6] = 2.0 * q2 * q4 - 2.0 * q1 * q3;
+  Q[7] = 2.0 * q3 * q4 + 2.0 * q1 * q2;
+  Q[8] = 2.0 * q4 * q4 + 2.0 * q1 * q1 - 1.0;
+  for (int i = 0; i < n; ++i) {
+    double x = p[i][0] - cm[0], y = p[i][1] - cm[1], z = p[i][2] - cm[2];
+    double tx = Q[0] * x + Q[1] * y + Q[2] * z;
+    double ty = Q[3] * x + Q[4] * y + Q[5] * z;
+    double tz = Q[6] * x + Q[7] * y + Q[8] * z;
+    p[i][0] = tx + cm[0];
+    p[i][1] = ty + cm[1];
+    p[i][2] = tz + cm[2];
+  }
+}
+
+// com (utility_pack.f:3565-3596)
+__device__ inline void centre_of_mass(const GuestType &G, double (*p)[3],
+                                      double *cm) {
+  double w = 0.0;
+  cm[0] = cm[1] = cm[2] = 0.0;
+  for (int i = 0; i < G.ns; ++i) {
+    w += G.mass[i];
+    cm[0] += p[i][0] * G.mass[i];
+    cm[1] += p[i][1] * G.mass[i];
+    cm[2] += p[i][2] * G.mass[i];
+  }
+  cm[0] /= w;
+  cm[1] /= w;
+  cm[2] /= w;
+}
+
+// random quaternion of random_ins / random_rot (utility_pack.f:3266-3330,
+// 3526-3563): theta = rand1 * angle, axis from three uniforms.
+__device__ inline void quaternion(double r1, double r2, double r3, double r4,
+                                  double angle, double *q) {
+  double theta = r1 * angle;
+  double b1 = 2.0 * r2 - 1.0, b2 = 2.0 * r3 - 1.0, b3 = 2.0 * r4 - 1.0;
+  double st = sin(theta / 2.0);
+  double nrm = sqrt(b1 * b1 + b2 * b2 + b3 * b3);
+  q[0] = cos(theta / 2.0);
+  q[1] = st * (b1 / nrm);
+  q[2] = st * (b2 / nrm);
+  q[3] = st * (b3 / nrm);
+}
+
+// translate (utility_pack.f:3161-3218)
+__device__ inline void translate_sites(const SysDev &S, const GuestType &G,
+                                       double (*p)[3], double a, double b,
+                                       double c) {
+  for (int i = 0; i < G.ns; ++i) {
+    p[i][0] = a + p[i][0];
+    p[i][1] = b + p[i][1];
+    p[i][2] = c + p[i][2];
+  }
+  double cm[3];
+  centre_of_mass(G, p, cm);
+  const double *r = S.rcell;
+  double sx = r[0] * cm[0] + r[3] * cm[1] + r[6] * cm[2];
+  double sy = r[1] * cm[0] + r[4] * cm[1] + r[7] * cm[2];
+  double sz = r[2] * cm[0] + r[5] * cm[1] + r[8] * cm[2];
+  sx -= floor(sx);
+  sy -= floor(sy);
+  sz -= floor(sz);
+  double w[3];
+  cartesian(S, sx, sy, sz, w);
+  double d0 = w[0] - cm[0], d1 = w[1] - cm[1], d2 = w[2] - cm[2];
+  for (int i = 0; i < G.ns; ++i) {
+    p[i][0] += d0;
+    p[i][1] += d1;
+    p[i][2] += d2;
+  }
+}
+
+// ------------------------------------------------------------ reductions
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Fixed-order block sum of n values per thread; result valid in red[0..n).
+__device__ inline void block_sum(double *vals, int n, double *red) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = 0; i < n; ++i) {
+    double v = warp_sum(vals[i]);
+    if (lane == 0) red[w * n + i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < n) {
+    double s = 0.0;
+    for (int k = 0; k < kWarps; ++k) s += red[k * n + threadIdx.x];
+    red[kWarps * n + threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+__device__ inline int block_or(int v, int *scratch) {
+  v = __any_sync(0xffffffffu, v) ? 1 : 0;
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int r = 0;
+  for (int k = 0; k < kWarps; ++k) r |= scratch[k];
+  __syncthreads();
+  return r;
+}
+
+// Exclusive block scan of one int per thread; returns the total.
+__device__ inline int block_scan(int v, int &excl, int *scratch) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) scratch[w] = x;
+  __syncthreads();
+  int base = 0, tot = 0;
+  for (int k = 0; k < kWarps; ++k) {
+    if (k < w) base += scratch[k];
+    tot += scratch[k];
+  }
+  excl = base + x - v;
+  __syncthreads();
+  return tot;
+}
+
+}  // namespace fmcdev

@@ -1,0 +1,1335 @@
+// engine.cu -- kernels and the C ABI of the GB300 GCMC energy path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "fmc_internal.h"
+
+using namespace fmcdev;
+
+namespace fmc {
+
+thread_local std::string g_error;
+void set_error(const std::string &m) { g_error = m; }
+[[noreturn]] void raise(int code, const std::string &msg) { throw Error{code, msg}; }
+
+#define FMC_CUDA(x)                                                                \
+  do {                                                                             \
+    cudaError_t e_ = (x);                                                          \
+    if (e_ != cudaSuccess)                                                         \
+      ::fmc::raise(FMC_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class F>
+int guard(F &&f) {
+  try {
+    g_error.clear();
+    return f();
+  } catch (const Error &e) {
+    g_error = e.msg;
+    return e.code;
+  } catch (const std::exception &e) {
+    g_error = e.what();
+    return FMC_ERR_ARG;
+  }
+}
+
+// --------------------------------------------------------------- kernels
+// K4: full structure factor S(k) = sum_j q_j e^{i k.r_j} of a set of atoms
+// (ewald.f:354-661).  Each block handles kKB k-vectors; threads stride
+// over the atoms; FP64 throughout.
+constexpr int kKB = 8;
+struct Rcell {
+  double r[9];
+};
+
+__global__ void __launch_bounds__(kThreads) structure_factor_kernel(
+    const double4 *__restrict__ atoms, int n, const int4 *__restrict__ klmn, int nk, Rcell rc,
+    double2 *__restrict__ out) {
+  __shared__ double red[kWarps * 2 * kKB + 2 * kKB];
+  int k0 = blockIdx.x * kKB;
+  double ax[kKB], ay[kKB];
+  int4 kv[kKB];
+  for (int j = 0; j < kKB; ++j) {
+    ax[j] = ay[j] = 0.0;
+    kv[j] = (k0 + j < nk) ? klmn[k0 + j] : make_int4(0, 0, 0, 0);
+  }
+  for (int a = threadIdx.x; a < n; a += kThreads) {
+    double4 A = atoms[a];
+    double f[3];
+    for (int d = 0; d < 3; ++d) f[d] = rc.r[d] * A.x + rc.r[3 + d] * A.y + rc.r[6 + d] * A.z;
+    for (int j = 0; j < kKB; ++j) {
+      double t = double(kv[j].x) * f[0] + double(kv[j].y) * f[1] + double(kv[j].z) * f[2];
+      t -= rint(t);
+      double sn, cs;
+      sincospi(2.0 * t, &sn, &cs);
+      ax[j] += A.w * cs;
+      ay[j] += A.w * sn;
+    }
+  }
+  double vals[2 * kKB];
+  for (int j = 0; j < kKB; ++j) {
+    vals[2 * j] = ax[j];
+    vals[2 * j + 1] = ay[j];
+  }
+  block_sum(vals, 2 * kKB, red);
+  if (threadIdx.x < kKB && k0 + threadIdx.x < nk) {
+    const double *R = red + kWarps * 2 * kKB;
+    out[k0 + threadIdx.x] = make_double2(R[2 * threadIdx.x], R[2 * threadIdx.x + 1]);
+  }
+}
+
+// Modes of the chain kernel.
+constexpr int kModeMoves = 0;   // nmoves main-loop iterations
+constexpr int kModeCreate = 1;  // "create molecules" pre-loading
+constexpr int kModeEval = 2;    // evaluate the move in gctx (per-move ABI)
+constexpr int kModeCommit = 3;  // decide with gctx.rande and commit
+
+template <class T>
+__device__ void block_copy(T *dst, const T *src) {
+  static_assert(sizeof(T) % 4 == 0, "copy granularity");
+  const int *s = reinterpret_cast<const int *>(src);
+  int *d = reinterpret_cast<int *>(dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(T) / 4); i += kThreads) d[i] = s[i];
+}
+
+template <bool F32>
+__device__ void propose_insert(BlockShared<F32> &B, int g) {
+  SysDev &S = B.S;
+  ChainHdr &H = B.H;
+  MoveCtx &mc = B.mc;
+  const GuestType &G = S.g[g];
+  double ra = duni_next(H), rb = duni_next(H), rc = duni_next(H);
+  double r1 = duni_next(H), r2 = duni_next(H), r3 = duni_next(H), r4 = duni_next(H);
+  double cc[3];
+  cartesian(S, ra, rb, rc, cc);
+  for (int s = 0; s < G.ns; ++s)
+    for (int d = 0; d < 3; ++d) mc.pos[0][s][d] = G.tmpl[s][d];
+  double q[4], zero[3] = {0.0, 0.0, 0.0};
+  quaternion(r1, r2, r3, r4, 2.0 * kPi, q);
+  rotate_sites(mc.pos[0], G.ns, zero, q[0], q[1], q[2], q[3]);
+  for (int s = 0; s < G.ns; ++s)
+    for (int d = 0; d < 3; ++d) mc.pos[0][s][d] += cc[d];
+  mc.kind = 1;
+  mc.g = g;
+  mc.ns = G.ns;
+  mc.npos = 1;
+  mc.slot = -1;
+  mc.choice = 0;
+  mc.overlap = 0;
+  mc.accepted = 0;
+  mc.rande = -1.0;
+}
+
+template <bool F32>
+__global__ void __launch_bounds__(kThreads, 1)
+    chain_kernel(const SysDev *__restrict__ systems, ChainHdr *hdrs, ChainArrays CA,
+                 MoveCtx *gctx, LogRec *logs, int logcap, int nmoves, int mode) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  BlockShared<F32> &B = *reinterpret_cast<BlockShared<F32> *>(dyn);
+  const int chain = blockIdx.x;
+  block_copy(&B.H, hdrs + chain);
+  __syncthreads();
+  block_copy(&B.S, systems + B.H.system);
+  if (threadIdx.x == 0) B.flags[0] = 0;
+  __syncthreads();
+  int st = 0;
+  if (mode == kModeMoves) {
+    for (int it = 0; it < nmoves; ++it) {
+      if (threadIdx.x == 0) {
+        propose(B, CA, chain);
+        geometry(B, CA, chain);
+      }
+      __syncthreads();
+      int full = 0;
+      if (B.mc.kind != 0) full = evaluate(B, CA, chain, st);
+      if (threadIdx.x == 0) {
+        decide(B, true);
+        if (full) B.H.evals += B.mc.npos;
+        else if (B.mc.overlap) B.H.overlap_exits++;
+        if (logcap > 0 && B.H.log_n < logcap) {
+          LogRec &L = logs[(size_t)chain * logcap + B.H.log_n];
+          L.move = B.mc.kind;
+          L.iguest = B.mc.g + 1;
+          L.choice = B.mc.choice;
+          L.overlap = B.mc.overlap;
+          L.accepted = B.mc.accepted;
+          L.estep = B.mc.estep;
+          L.rande = B.mc.rande;
+          for (int s = 0; s < 3 && s < B.mc.ns; ++s)
+            for (int d = 0; d < 3; ++d) L.newxyz[3 * s + d] = B.mc.pos[0][s][d];
+        }
+      }
+      __syncthreads();
+      commit(B, CA, chain, st);
+      if (threadIdx.x == 0) {
+        stats(B);
+        if (logcap > 0 && B.H.log_n < logcap) {
+          logs[(size_t)chain * logcap + B.H.log_n].nmols_after = B.H.nummols[B.mc.g];
+          B.H.log_n++;
+        }
+      }
+      __syncthreads();
+    }
+  } else if (mode == kModeCreate) {
+    for (int g = 0; g < B.S.ntpguest; ++g) {
+      long long maxiter = 1000LL * B.S.g[g].insert0, iter = 0;
+      while (B.H.nummols[g] < B.S.g[g].insert0) {
+        if (iter >= maxiter) {  // insert_guests iteration cap (error 2320)
+          st |= kStCapacity;
+          break;
+        }
+        if (threadIdx.x == 0) propose_insert(B, g);
+        __syncthreads();
+        evaluate(B, CA, chain, st);
+        if (threadIdx.x == 0) B.mc.accepted = B.mc.overlap ? 0 : 1;
+        __syncthreads();
+        commit(B, CA, chain, st);
+        __syncthreads();
+        ++iter;
+      }
+    }
+  } else if (mode == kModeEval) {
+    if (threadIdx.x == 0) {
+      B.mc = gctx[chain];
+      geometry(B, CA, chain);
+    }
+    __syncthreads();
+    int full = 0;
+    if (B.mc.kind != 0) full = evaluate(B, CA, chain, st);
+    if (threadIdx.x == 0) {
+      B.mc.evaluated = 1;
+      B.mc.accepted = 0;
+      (void)full;
+      gctx[chain] = B.mc;
+    }
+  } else if (mode == kModeCommit) {
+    if (threadIdx.x == 0) {
+      B.mc = gctx[chain];
+      decide(B, false);
+    }
+    __syncthreads();
+    commit(B, CA, chain, st);
+    if (threadIdx.x == 0) {
+      B.mc.evaluated = 0;
+      gctx[chain] = B.mc;
+    }
+  }
+  if (st) atomicOr(&B.flags[0], st);
+  __syncthreads();
+  if (threadIdx.x == 0) B.H.status |= B.flags[0];
+  __syncthreads();
+  block_copy(hdrs + chain, &B.H);
+}
+
+// ----------------------------------------------------- device allocations
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  void alloc(size_t count) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = count;
+    if (count) FMC_CUDA(cudaMalloc(&p, count * sizeof(T)));
+  }
+  void upload(const std::vector<T> &v) {
+    alloc(v.size());
+    if (!v.empty()) FMC_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  }
+  void zero() {
+    if (p) FMC_CUDA(cudaMemset(p, 0, n * sizeof(T)));
+  }
+};
+
+// Device copy of one system (framework, tables, k-vectors, S_fw).
+struct DevSystem {
+  SysDev d{};
+  DBuf<double4> fw64;
+  DBuf<float4> fwhi, fwlo;
+  DBuf<int> fwtype, cell_start, pairtab, numtyp_fw, numfrz_fw;
+  DBuf<double> erc, vvv, sig2, steadd, akk;
+  DBuf<float4> ercq, vvvq;
+  DBuf<float> akk32;
+  DBuf<int4> klmn;
+  DBuf<double2> skfw;
+  std::vector<double2> skfw_host;
+  const System *host = nullptr;
+};
+
+void ensure_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) raise(FMC_ERR_NODEVICE, "no CUDA device is visible");
+}
+
+std::vector<float4> quad_coeffs(const std::vector<double> &tab, int mx) {
+  std::vector<float4> q(mx + 3, make_float4(0, 0, 0, 0));
+  for (int l = 1; l <= mx; ++l) {
+    double v0 = tab[l], v1 = tab[l + 1], v2 = (l + 2 < (int)tab.size()) ? tab[l + 2] : 0.0;
+    double D = v2 - 2.0 * v1 + v0;
+    q[l] = make_float4((float)v0, (float)(v1 - v0 - 0.5 * D), (float)(0.5 * D), 0.f);
+  }
+  return q;
+}
+
+void compute_sk(const std::vector<double4> &atoms, const DevSystem &D, double2 *out) {
+  DBuf<double4> a;
+  a.upload(atoms);
+  Rcell rc;
+  for (int i = 0; i < 9; ++i) rc.r[i] = D.d.rcell[i];
+  int nb = (D.d.nk + kKB - 1) / kKB;
+  if (nb > 0) structure_factor_kernel<<<nb, kThreads>>>(a.p, (int)atoms.size(), D.klmn.p, D.d.nk, rc, out);
+  FMC_CUDA(cudaGetLastError());
+  FMC_CUDA(cudaDeviceSynchronize());
+}
+
+void build_device_system(const System &s, DevSystem &D) {
+  ensure_device();
+  D.host = &s;
+  SysDev &d = D.d;
+  std::memset(&d, 0, sizeof d);
+  d.imcon = s.imcon;
+  for (int i = 0; i < 9; ++i) {
+    d.cell[i] = s.cell[i];
+    d.rcell[i] = s.rcell[i];
+  }
+  d.box[0] = s.cell[0];
+  d.box[1] = s.cell[4];
+  d.box[2] = s.cell[8];
+  d.volm = s.volm;
+  d.statvolm = s.statvolm;
+  d.temp = s.temp;
+  d.beta = s.beta;
+  d.engunit = s.engunit;
+  d.epsq = s.epsq;
+  d.alpha = s.alpha;
+  d.rcut = s.rcut;
+  d.rc2 = s.rcut * s.rcut;
+  d.overlap_sq = s.overlap_sq;
+  d.surftol = s.surftol;
+  d.sumchg0 = s.sumchg;
+  d.maxmls = s.maxmls;
+  d.ntpguest = s.ntpguest;
+  d.ntpatm = s.ntpatm;
+  d.fw_mol = s.fw_mol;
+  d.eqsteps = s.eqsteps;
+  d.nwindsteps = s.nwindsteps;
+  d.minchk = s.minchk;
+  d.laccsample = s.laccsample ? 1 : 0;
+  if (s.ntpatm > kMaxT) raise(FMC_ERR_INPUT, "too many atom types");
+  for (int dd = 0; dd < 3; ++dd) {
+    d.kmax[dd] = s.kmax[dd];
+    if (s.kmax[dd] + 1 > kMaxKm) raise(FMC_ERR_INPUT, "kmax beyond the supported 39");
+  }
+  // framework atoms: sort into cells (z fastest) for imcon 1/2
+  const MolType &fw = s.mol[s.fw_mol];
+  int n = fw.nummols * fw.natoms;
+  d.nfw = n;
+  std::vector<double> x(n), y(n), z(n), q(n);
+  std::vector<int> t(n);
+  double chg_fw = 0.0;
+  for (int i = 0; i < n; ++i) {
+    x[i] = fw.xyz[3 * i];
+    y[i] = fw.xyz[3 * i + 1];
+    z[i] = fw.xyz[3 * i + 2];
+    q[i] = fw.chg[i % fw.natoms];
+    t[i] = fw.ltp[i % fw.natoms];
+    chg_fw += q[i];
+  }
+  d.chgsum_fw = chg_fw;
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::vector<int> cstart;
+  d.use_cells = (s.imcon == 1 || s.imcon == 2) ? 1 : 0;
+  if (d.use_cells) {
+    for (int dd = 0; dd < 3; ++dd) {
+      d.nc[dd] = std::max(3, (int)std::floor(d.box[dd] / 2.5));
+      d.csz[dd] = d.box[dd] / d.nc[dd];
+    }
+    std::vector<int> cell(n);
+    for (int i = 0; i < n; ++i) {
+      double w[3] = {x[i], y[i], z[i]};
+      int c3[3];
+      for (int dd = 0; dd < 3; ++dd) {
+        w[dd] -= d.box[dd] * std::floor(w[dd] / d.box[dd]);
+        c3[dd] = std::min(d.nc[dd] - 1, std::max(0, (int)std::floor(w[dd] / d.csz[dd])));
+      }
+      x[i] = w[0];
+      y[i] = w[1];
+      z[i] = w[2];
+      cell[i] = (c3[0] * d.nc[1] + c3[1]) * d.nc[2] + c3[2];
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cell[a] < cell[b]; });
+    int ncell = d.nc[0] * d.nc[1] * d.nc[2];
+    cstart.assign(ncell + 1, 0);
+    for (int i = 0; i < n; ++i) cstart[cell[i] + 1]++;
+    for (int c = 0; c < ncell; ++c) cstart[c + 1] += cstart[c];
+  } else {
+    cstart = {0, n};
+  }
+  std::vector<double4> a64(n);
+  std::vector<float4> ahi(n), alo(n);
+  std::vector<int> at(n);
+  for (int i = 0; i < n; ++i) {
+    int o = order[i];
+    a64[i] = make_double4(x[o], y[o], z[o], q[o]);
+    float hx = (float)x[o], hy = (float)y[o], hz = (float)z[o];
+    ahi[i] = make_float4(hx, hy, hz, (float)q[o]);
+    alo[i] = make_float4((float)(x[o] - hx), (float)(y[o] - hy), (float)(z[o] - hz), 0.f);
+    at[i] = t[o];
+  }
+  D.fw64.upload(a64);
+  D.fwhi.upload(ahi);
+  D.fwlo.upload(alo);
+  D.fwtype.upload(at);
+  D.cell_start.upload(cstart);
+  d.fw64 = D.fw64.p;
+  d.fwhi = D.fwhi.p;
+  d.fwlo = D.fwlo.p;
+  d.fwtype = D.fwtype.p;
+  d.cell_start = D.cell_start.p;
+  // tables
+  d.mxegrd = s.mxegrd;
+  d.tabstride = s.mxegrd + 3;
+  d.rdrewd = 1.0 / s.drewd;
+  d.rdlrpot = 1.0 / s.dlrpot;
+  std::vector<double> erc(d.tabstride, 0.0);
+  for (int i = 1; i <= s.mxegrd; ++i) erc[i] = s.erc[i];
+  D.erc.upload(erc);
+  D.ercq.upload(quad_coeffs(erc, s.mxegrd));
+  int ntab = s.ntpvdw + 1;
+  std::vector<double> vvv((size_t)ntab * d.tabstride, 0.0);
+  std::vector<float4> vq((size_t)ntab * d.tabstride, make_float4(0, 0, 0, 0));
+  for (int k = 1; k <= ntab && k < (int)s.vvv.size(); ++k) {
+    std::vector<double> row(d.tabstride, 0.0);
+    for (int i = 1; i <= s.mxegrd; ++i) row[i] = s.vvv[k][i];
+    std::copy(row.begin(), row.end(), vvv.begin() + (size_t)(k - 1) * d.tabstride);
+    auto qq = quad_coeffs(row, s.mxegrd);
+    std::copy(qq.begin(), qq.end(), vq.begin() + (size_t)(k - 1) * d.tabstride);
+  }
+  D.vvv.upload(vvv);
+  D.vvvq.upload(vq);
+  int na = s.ntpatm + 1;
+  std::vector<int> ptab(na * na, -1);
+  std::vector<double> sig2(na * na, 0.0);
+  for (int a = 1; a <= s.ntpatm; ++a)
+    for (int b = 1; b <= s.ntpatm; ++b) {
+      int k = s.lstvdw[loc2(a, b)];
+      if (k >= 1 && k <= ntab && s.ltpvdw[k] < 100 && std::fabs(s.vvv[k][1]) > 1.0e-10)
+        ptab[a * na + b] = k - 1;
+      double sg = (k >= 1 && k < (int)s.prmvdw.size()) ? s.prmvdw[k][2] : 0.0;
+      double st = s.surftol + sg;
+      sig2[a * na + b] = st * st;
+    }
+  D.pairtab.upload(ptab);
+  D.sig2.upload(sig2);
+  D.steadd.upload(s.steadd);
+  D.numtyp_fw.upload(s.numtyp_fw);
+  D.numfrz_fw.upload(s.numfrz_fw);
+  d.erc = D.erc.p;
+  d.vvv = D.vvv.p;
+  d.ercq = D.ercq.p;
+  d.vvvq = D.vvvq.p;
+  d.pairtab = D.pairtab.p;
+  d.sig2 = D.sig2.p;
+  d.steadd = D.steadd.p;
+  d.numtyp_fw = D.numtyp_fw.p;
+  d.numfrz_fw = D.numfrz_fw.p;
+  // k vectors
+  d.nk = s.newld;
+  std::vector<int4> lmn(s.newld);
+  std::vector<float> a32(s.newld);
+  for (int k = 0; k < s.newld; ++k) {
+    lmn[k] = make_int4(s.kl[k], s.km[k], s.kn[k], 0);
+    a32[k] = (float)s.akk[k];
+  }
+  D.klmn.upload(lmn);
+  D.akk.upload(s.akk);
+  D.akk32.upload(a32);
+  d.klmn = D.klmn.p;
+  d.akk = D.akk.p;
+  d.akk32 = D.akk32.p;
+  d.krecip = 2.0 * (2.0 * kPi / s.volm) * kR4pie0 / s.epsq;
+  // framework S(k) (K4)
+  D.skfw.alloc(std::max(1, s.newld));
+  compute_sk(a64, D, D.skfw.p);
+  D.skfw_host.resize(s.newld);
+  if (s.newld)
+    FMC_CUDA(cudaMemcpy(D.skfw_host.data(), D.skfw.p, s.newld * sizeof(double2), cudaMemcpyDeviceToHost));
+  d.skfw = D.skfw.p;
+  // guest types
+  for (int g = 1; g <= s.ntpguest; ++g) {
+    GuestType &G = d.g[g - 1];
+    const MolType &m = s.mol[s.locguest[g]];
+    G.mol = s.locguest[g];
+    G.ns = m.natoms;
+    G.insert0 = s.guest_insert[g];
+    double cx = 0, cy = 0, cz = 0;
+    for (int i = 0; i < m.natoms; ++i) {
+      G.q[i] = m.chg[i];
+      G.mass[i] = m.wght[i];
+      G.type[i] = m.ltp[i];
+      G.frz[i] = m.frz[i];
+      for (int dd = 0; dd < 3; ++dd) G.tmpl[i][dd] = s.guest_tmpl[g][3 * i + dd];
+      cx += G.tmpl[i][0];
+      cy += G.tmpl[i][1];
+      cz += G.tmpl[i][2];
+    }
+    cx /= m.natoms;
+    cy /= m.natoms;
+    cz /= m.natoms;
+    double rmax = 0.0;
+    for (int i = 0; i < m.natoms; ++i) {
+      double dx = G.tmpl[i][0] - cx, dy = G.tmpl[i][1] - cy, dz = G.tmpl[i][2] - cz;
+      rmax = std::max(rmax, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    G.rmax = rmax;
+    G.ewald3en = s.ewald3en[G.mol];
+    G.delr = s.delr[g];
+    G.disp_ratio = s.disp_ratio[g];
+    G.tran_ratio = s.tran_ratio[g];
+    G.rota_ratio = s.rota_ratio[g];
+    G.mcinsf = s.mcinsf[g];
+    G.mcdelf = s.mcdelf[g];
+    G.mcdisf = s.mcdisf[g];
+    G.mcjmpf = s.mcjmpf[g];
+    G.mcswpf = s.mcswpf[g];
+    G.mctraf = s.mctraf[g];
+    G.mcrotf = s.mcrotf[g];
+    G.mcswif = s.mcswif[g];
+  }
+}
+
+// Initial chain header (alloc_config_arrays defaults, gcmc.f:389-399, 692-699).
+ChainHdr initial_header(const System &s, int system_index, long long seed,
+                        const double *fuga_override) {
+  ChainHdr h;
+  std::memset(&h, 0, sizeof h);
+  long long sd = seed < 0 ? -seed : seed;
+  int ms = int(sd % 1000), sec = int((sd / 1000) % 60);
+  duni_init(h, ms, sec);
+  h.system = system_index;
+  for (int g = 1; g <= s.ntpguest; ++g) {
+    h.delrdisp[g - 1] = s.delr[g];
+    h.tran_delr[g - 1] = s.delr[g];
+    h.fuga[g - 1] = s.gstfuga[g];
+  }
+  if (fuga_override && *fuga_override >= 0.0) h.fuga[0] = *fuga_override;
+  h.rotangle = kPi / 3.0;
+  h.rota_rotangle = h.rotangle;
+  h.production = s.eqsteps == 0 ? 1 : 0;
+  h.sumchg = s.sumchg;
+  const MolType &fw = s.mol[s.fw_mol];
+  double cf = 0.0;
+  for (int i = 0; i < fw.natoms; ++i) cf += fw.chg[i] * fw.nummols;
+  // chgsum_mol(framework) accumulates atom by atom in ewald1
+  double acc = 0.0;
+  for (int m = 0; m < fw.nummols; ++m)
+    for (int i = 0; i < fw.natoms; ++i) acc += fw.chg[i];
+  (void)cf;
+  h.chgsum_mol[s.fw_mol] = acc;
+  for (int a = 1; a <= s.ntpatm && a <= kMaxT; ++a) {
+    h.numtyp[a] = s.numtyp_fw[a];
+    h.numfrz[a] = s.numfrz_fw[a];
+    h.numtyp_mol[s.fw_mol][a] = s.numtyp_fw[a];
+    h.numfrz_mol[s.fw_mol][a] = s.numfrz_fw[a];
+  }
+  return h;
+}
+
+// A set of chains on the device (the per-move ABI uses one chain).
+struct Chains {
+  std::vector<std::unique_ptr<DevSystem>> sys;
+  std::vector<const System *> hsys;
+  DBuf<SysDev> sysarr;
+  DBuf<ChainHdr> hdr;
+  DBuf<double> gpos;
+  DBuf<float4> ghi, glo;
+  DBuf<int> ord, freel;
+  DBuf<double2> sk, snew, sold;
+  DBuf<float2> sk32;
+  DBuf<MoveCtx> ctx;
+  DBuf<LogRec> logs;
+  ChainArrays CA{};
+  int nchains = 0, precision = 0, logcap = 0, maxmls = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_moves = -1;
+  size_t smem = 0;
+  double last_ms = 0.0;
+  long long last_evals = 0, last_moves = 0;
+  std::vector<ChainHdr> host_hdr;
+
+  ~Chains() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  void launch(int mode, int nmoves) {
+    dim3 grid(nchains), block(kThreads);
+    if (precision == FMC_PREC_FP32)
+      chain_kernel<true><<<grid, block, smem, stream>>>(sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
+                                                        nmoves, mode);
+    else
+      chain_kernel<false><<<grid, block, smem, stream>>>(sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
+                                                         nmoves, mode);
+    FMC_CUDA(cudaGetLastError());
+  }
+
+  void sync() { FMC_CUDA(cudaStreamSynchronize(stream)); }
+
+  void pull_headers() {
+    host_hdr.resize(nchains);
+    FMC_CUDA(cudaMemcpyAsync(host_hdr.data(), hdr.p, nchains * sizeof(ChainHdr),
+                             cudaMemcpyDeviceToHost, stream));
+    sync();
+  }
+
+  void check_status() {
+    pull_headers();
+    for (int c = 0; c < nchains; ++c)
+      if (host_hdr[c].status) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf,
+                      "chain %d raised device status 0x%x (1 table range, 2 segment overflow, "
+                      "4 capacity, 8 non-finite, 16 bad molecule index)",
+                      c, host_hdr[c].status);
+        raise(FMC_ERR_DEVICE, buf);
+      }
+  }
+};
+
+void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_chain_spec *spec,
+                 int nchains, int precision, int cap) {
+  ensure_device();
+  if (nsys < 1 || nchains < 1) raise(FMC_ERR_ARG, "need at least one system and one chain");
+  if (precision != FMC_PREC_FP64 && precision != FMC_PREC_FP32) raise(FMC_ERR_ARG, "bad precision");
+  if (cap < 1 || cap > 4096) raise(FMC_ERR_ARG, "guest capacity must be in 1..4096");
+  C.nchains = nchains;
+  C.precision = precision;
+  int nkmax = 1, maxmls = 1;
+  for (int i = 0; i < nsys; ++i) {
+    if (!systems[i]) raise(FMC_ERR_ARG, "null system");
+    if (precision == FMC_PREC_FP32 && systems[i]->imcon == 3)
+      raise(FMC_ERR_INPUT, "the FP32 path supports orthorhombic cells (imcon 1, 2)");
+    auto D = std::make_unique<DevSystem>();
+    build_device_system(*systems[i], *D);
+    nkmax = std::max(nkmax, systems[i]->newld);
+    maxmls = std::max(maxmls, systems[i]->maxmls);
+    C.hsys.push_back(systems[i]);
+    C.sys.push_back(std::move(D));
+  }
+  C.maxmls = maxmls;
+  std::vector<SysDev> sd;
+  for (auto &D : C.sys) sd.push_back(D->d);
+  C.sysarr.upload(sd);
+  std::vector<ChainHdr> hh;
+  for (int c = 0; c < nchains; ++c) {
+    int si = spec ? spec[c].system : 0;
+    if (si < 0 || si >= nsys) raise(FMC_ERR_ARG, "chain system index out of range");
+    double fu = spec ? spec[c].pressure_pa : -1.0;
+    long long seed = spec ? (long long)spec[c].seed : 1;
+    hh.push_back(initial_header(*systems[si], si, seed, &fu));
+  }
+  C.hdr.upload(hh);
+  ChainArrays &CA = C.CA;
+  CA.cap = cap;
+  CA.nkmax = nkmax;
+  CA.nmt = maxmls + 1;
+  size_t nsl = (size_t)nchains * kMaxG * cap * kMaxS;
+  C.gpos.alloc(nsl * 3);
+  C.gpos.zero();
+  C.ghi.alloc(nsl);
+  C.glo.alloc(nsl);
+  C.ghi.zero();
+  C.glo.zero();
+  C.ord.alloc((size_t)nchains * kMaxG * cap);
+  C.freel.alloc((size_t)nchains * kMaxG * cap);
+  C.ord.zero();
+  C.freel.zero();
+  C.sk.alloc((size_t)nchains * kMaxG * nkmax);
+  C.sk.zero();
+  C.snew.alloc((size_t)nchains * nkmax);
+  C.sold.alloc((size_t)nchains * nkmax);
+  C.snew.zero();
+  C.sold.zero();
+  C.sk32.alloc((size_t)nchains * (maxmls + 1) * nkmax);
+  // FP32 mirrors start from the framework S(k)
+  {
+    std::vector<float2> m((size_t)nchains * (maxmls + 1) * nkmax, make_float2(0.f, 0.f));
+    for (int c = 0; c < nchains; ++c) {
+      const DevSystem &D = *C.sys[hh[c].system];
+      const System &s = *D.host;
+      for (int k = 0; k < s.newld; ++k) {
+        double2 v = D.skfw_host[k];
+        float2 f = make_float2((float)v.x, (float)v.y);
+        m[((size_t)c * (maxmls + 1) + (s.fw_mol - 1)) * nkmax + k] = f;
+        m[((size_t)c * (maxmls + 1) + s.maxmls) * nkmax + k] = f;
+      }
+    }
+    FMC_CUDA(cudaMemcpy(C.sk32.p, m.data(), m.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  }
+  C.ctx.alloc(nchains);
+  C.ctx.zero();
+  C.logs.alloc(1);
+  CA.gpos = C.gpos.p;
+  CA.ghi = C.ghi.p;
+  CA.glo = C.glo.p;
+  CA.ord = C.ord.p;
+  CA.freel = C.freel.p;
+  CA.sk = C.sk.p;
+  CA.sk32 = C.sk32.p;
+  CA.snew = C.snew.p;
+  CA.sold = C.sold.p;
+  FMC_CUDA(cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking));
+  FMC_CUDA(cudaEventCreate(&C.ev0));
+  FMC_CUDA(cudaEventCreate(&C.ev1));
+  C.smem = precision == FMC_PREC_FP32 ? sizeof(BlockShared<true>) : sizeof(BlockShared<false>);
+  if (precision == FMC_PREC_FP32)
+    FMC_CUDA(cudaFuncSetAttribute(chain_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)C.smem));
+  else
+    FMC_CUDA(cudaFuncSetAttribute(chain_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)C.smem));
+}
+
+void fill_stats(const Chains &C, fmc_chain_stats *out) {
+  for (int c = 0; c < C.nchains; ++c) {
+    const ChainHdr &h = C.host_hdr[c];
+    fmc_chain_stats &o = out[c];
+    std::memset(&o, 0, sizeof o);
+    o.moves = h.moves;
+    o.evals = h.evals;
+    o.overlap_exits = h.overlap_exits;
+    for (int i = 0; i < 5; ++i) {
+      o.attempts[i] = h.attempts[i];
+      o.accepts[i] = h.accepts[i];
+    }
+    const System &s = *C.hsys[h.system];
+    o.nummols = h.nummols[0];
+    o.status = h.status;
+    o.energy = h.energy[s.locguest[1]];
+    if (h.wsum > 0) {
+      o.avg_n = h.wacc[0][0] / h.wsum;
+      o.avg_e = h.wacc[0][1] / h.wsum;
+      o.avg_en = h.wacc[0][2] / h.wsum;
+      o.avg_n2 = h.wacc[0][3] / h.wsum;
+      o.avg_e2 = h.wacc[0][4] / h.wsum;
+      o.avg_nf = h.wacc[0][5] / h.wsum;
+      o.qst = h.wacc[0][6] / h.wsum;
+      o.cv = h.wacc[0][7] / h.wsum;
+    }
+    o.prodcount = h.prodcount;
+    o.windows = h.windows;
+  }
+}
+
+}  // namespace fmc
+
+// =================================================================== C ABI
+using namespace fmc;
+
+struct fmc_plain {
+  Chains C;
+  fmc_system_info info{};
+  int has_move = 0;
+};
+
+struct fmc_batch {
+  Chains C;
+};
+
+extern "C" {
+
+int fmc_last_error(char *buf, int len) {
+  int n = (int)g_error.size();
+  if (buf && len > 0) {
+    int m = std::min(n, len - 1);
+    std::memcpy(buf, g_error.data(), m);
+    buf[m] = 0;
+  }
+  return n;
+}
+
+const char *fmc_version(void) { return "fastmc_gb300 1.0 sm_103a"; }
+
+int fmc_system_load(const char *dir, fmc_system **out) {
+  return guard([&] {
+    if (!out) raise(FMC_ERR_ARG, "null output pointer");
+    auto p = std::make_unique<fmc_system>();
+    load_system(dir ? dir : ".", p->s);
+    *out = p.release();
+    return FMC_OK;
+  });
+}
+
+int fmc_system_free(fmc_system *sys) {
+  delete sys;
+  return FMC_OK;
+}
+
+int fmc_system_get_info(const fmc_system *sys, fmc_system_info *info) {
+  return guard([&] {
+    if (!sys || !info) raise(FMC_ERR_ARG, "null argument");
+    const System &s = sys->s;
+    std::memset(info, 0, sizeof *info);
+    info->imcon = s.imcon;
+    info->maxmls = s.maxmls;
+    info->ntpguest = s.ntpguest;
+    info->ntpatm = s.ntpatm;
+    info->n_framework = s.mol[s.fw_mol].nummols * s.mol[s.fw_mol].natoms;
+    for (int d = 0; d < 3; ++d) info->kmax[d] = s.kmax[d];
+    info->newld = s.newld;
+    info->mxegrd = s.mxegrd;
+    for (int g = 1; g <= s.ntpguest; ++g) {
+      info->guest_mol[g - 1] = s.locguest[g];
+      info->guest_nsites[g - 1] = s.mol[s.locguest[g]].natoms;
+      info->guest_insert[g - 1] = s.guest_insert[g];
+      info->fugacity[g - 1] = s.gstfuga[g];
+      info->ewald3en[g - 1] = s.ewald3en[s.locguest[g]];
+    }
+    info->alpha = s.alpha;
+    info->rcut = s.rcut;
+    info->volm = s.volm;
+    info->engunit = s.engunit;
+    info->temperature = s.temp;
+    info->sumchg = s.sumchg;
+    info->drewd = s.drewd;
+    for (int i = 0; i < 9; ++i) info->cell[i] = s.cell[i];
+    info->mcsteps = s.mcsteps;
+    info->eqsteps = s.eqsteps;
+    info->nwindsteps = s.nwindsteps;
+    return FMC_OK;
+  });
+}
+
+int fmc_system_set_fugacity(fmc_system *sys, int iguest, double pascal) {
+  return guard([&] {
+    if (!sys || iguest < 1 || iguest > sys->s.ntpguest) raise(FMC_ERR_ARG, "bad guest index");
+    sys->s.gstfuga[iguest] = pascal;
+    return FMC_OK;
+  });
+}
+
+// ----------------------------------------------------------- plain mode
+int fmc_plain_create(const fmc_system *sys, int precision, int guest_capacity, fmc_plain **out) {
+  return guard([&] {
+    if (!sys || !out) raise(FMC_ERR_ARG, "null argument");
+    auto h = std::make_unique<fmc_plain>();
+    const System *sp = &sys->s;
+    fmc_chain_spec spec{0, -1.0, 1, 0};
+    init_chains(h->C, &sp, 1, &spec, 1, precision, guest_capacity);
+    *out = h.release();
+    return FMC_OK;
+  });
+}
+
+int fmc_plain_destroy(fmc_plain *h) {
+  delete h;
+  return FMC_OK;
+}
+
+int fmc_full_ewald(fmc_plain *h, double *out4) {
+  return guard([&] {
+    if (!h || !out4) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = h->C;
+    const System &s = *C.hsys[0];
+    const DevSystem &D = *C.sys[0];
+    C.pull_headers();
+    const ChainHdr &hd = C.host_hdr[0];
+    int nk = s.newld;
+    // guest S(k) recomputed from the device coordinates, per guest type
+    std::vector<double2> stot(D.skfw_host);
+    double sq = 0.0, sumchg = 0.0;
+    const MolType &fw = s.mol[s.fw_mol];
+    for (int m = 0; m < fw.nummols; ++m)
+      for (int i = 0; i < fw.natoms; ++i) {
+        sq += fw.chg[i] * fw.chg[i];
+        sumchg += fw.chg[i];
+      }
+    (void)sumchg;
+    double e3 = 0.0;
+    for (int g = 0; g < s.ntpguest; ++g) {
+      int n = hd.nummols[g];
+      const MolType &gm = s.mol[s.locguest[g + 1]];
+      std::vector<int> ord(n);
+      if (n)
+        FMC_CUDA(cudaMemcpy(ord.data(), C.ord.p + (size_t)g * C.CA.cap, n * sizeof(int),
+                            cudaMemcpyDeviceToHost));
+      std::vector<double4> atoms;
+      for (int i = 0; i < n; ++i) {
+        std::vector<double> xyz(3 * kMaxS);
+        FMC_CUDA(cudaMemcpy(xyz.data(), C.gpos.p + ((size_t)g * C.CA.cap + ord[i]) * kMaxS * 3,
+                            3 * kMaxS * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int sidx = 0; sidx < gm.natoms; ++sidx) {
+          atoms.push_back(make_double4(xyz[3 * sidx], xyz[3 * sidx + 1], xyz[3 * sidx + 2],
+                                       gm.chg[sidx]));
+          sq += gm.chg[sidx] * gm.chg[sidx];
+        }
+      }
+      e3 += n * s.ewald3en[s.locguest[g + 1]];
+      std::vector<double2> sg(nk, make_double2(0, 0));
+      if (!atoms.empty() && nk) {
+        DBuf<double2> tmp;
+        tmp.alloc(nk);
+        compute_sk(atoms, D, tmp.p);
+        FMC_CUDA(cudaMemcpy(sg.data(), tmp.p, nk * sizeof(double2), cudaMemcpyDeviceToHost));
+      }
+      // reset the running S(k) of this guest type to the recomputed one
+      if (nk)
+        FMC_CUDA(cudaMemcpy(C.sk.p + (size_t)g * C.CA.nkmax, sg.data(), nk * sizeof(double2),
+                            cudaMemcpyHostToDevice));
+      for (int k = 0; k < nk; ++k) {
+        stot[k].x += sg[k].x;
+        stot[k].y += sg[k].y;
+      }
+    }
+    double eng = 0.0;
+    for (int k = 0; k < nk; ++k) eng += s.akk[k] * (stot[k].x * stot[k].x + stot[k].y * stot[k].y);
+    double r4 = fmc::kR4pie0 / s.epsq;
+    double sic = -r4 * s.alpha * sq / fmc::kSqrPi;
+    double qfix = -(0.5 * fmc::kPi * r4) * ((hd.sumchg / s.alpha) * (hd.sumchg / s.alpha) / s.volm);
+    double ew1 = 2.0 * (2.0 * fmc::kPi / s.volm) * r4 * eng + sic + qfix;
+    out4[0] = (ew1 - e3) / s.engunit;
+    out4[1] = ew1;
+    out4[2] = sic;
+    out4[3] = qfix;
+    return FMC_OK;
+  });
+}
+
+static int plain_eval(fmc_plain *h, MoveCtx &mc, fmc_move_result *res, bool guest_energy) {
+  Chains &C = h->C;
+  const System &s = *C.hsys[0];
+  mc.evaluated = 0;
+  FMC_CUDA(cudaMemcpyAsync(C.ctx.p, &mc, sizeof(MoveCtx), cudaMemcpyHostToDevice, C.stream));
+  C.launch(kModeEval, 0);
+  MoveCtx out;
+  FMC_CUDA(cudaMemcpyAsync(&out, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost, C.stream));
+  C.sync();
+  C.check_status();
+  h->has_move = 1;
+  if (res) {
+    std::memset(res, 0, sizeof *res);
+    res->estep = out.estep;
+    if (guest_energy) res->estep = out.estep + out.delrc / s.engunit;
+    res->ewld1 = out.parts[0];
+    res->ewld2 = out.parts[1];
+    res->vdw = out.parts[2];
+    res->delrc = out.parts[3];
+    for (int m = 1; m <= s.maxmls && m <= FMC_MAX_MOLTYPES; ++m) res->delE[m - 1] = out.delE[m];
+    res->overlap = out.overlap;
+    res->surface = out.surf_new;
+    res->surface_old = out.surf_old;
+    res->status = C.host_hdr[0].status;
+    for (int i = 0; i < out.ns && i < FMC_MAX_SITES; ++i)
+      for (int d = 0; d < 3; ++d) res->newxyz[3 * i + d] = out.pos[0][i][d];
+  }
+  return FMC_OK;
+}
+
+int fmc_insertion(fmc_plain *h, int iguest, const double *xyz, fmc_move_result *res) {
+  return guard([&] {
+    if (!h || !xyz) raise(FMC_ERR_ARG, "null argument");
+    const System &s = *h->C.hsys[0];
+    if (iguest < 1 || iguest > s.ntpguest) raise(FMC_ERR_ARG, "bad guest index");
+    MoveCtx mc;
+    std::memset(&mc, 0, sizeof mc);
+    mc.kind = 1;
+    mc.g = iguest - 1;
+    mc.ns = s.mol[s.locguest[iguest]].natoms;
+    mc.npos = 1;
+    mc.slot = -1;
+    for (int i = 0; i < mc.ns; ++i)
+      for (int d = 0; d < 3; ++d) mc.pos[0][i][d] = xyz[3 * i + d];
+    return plain_eval(h, mc, res, false);
+  });
+}
+
+int fmc_deletion(fmc_plain *h, int iguest, int choice, fmc_move_result *res) {
+  return guard([&] {
+    if (!h) raise(FMC_ERR_ARG, "null argument");
+    const System &s = *h->C.hsys[0];
+    if (iguest < 1 || iguest > s.ntpguest) raise(FMC_ERR_ARG, "bad guest index");
+    MoveCtx mc;
+    std::memset(&mc, 0, sizeof mc);
+    mc.kind = 2;
+    mc.g = iguest - 1;
+    mc.ns = s.mol[s.locguest[iguest]].natoms;
+    mc.npos = 1;
+    mc.choice = choice;
+    return plain_eval(h, mc, res, false);
+  });
+}
+
+int fmc_guest_energy(fmc_plain *h, int iguest, int choice, fmc_move_result *res) {
+  return guard([&] {
+    if (!h) raise(FMC_ERR_ARG, "null argument");
+    const System &s = *h->C.hsys[0];
+    if (iguest < 1 || iguest > s.ntpguest) raise(FMC_ERR_ARG, "bad guest index");
+    MoveCtx mc;
+    std::memset(&mc, 0, sizeof mc);
+    mc.kind = 2;
+    mc.g = iguest - 1;
+    mc.ns = s.mol[s.locguest[iguest]].natoms;
+    mc.npos = 1;
+    mc.choice = choice;
+    int rc = plain_eval(h, mc, res, true);
+    h->has_move = 0;  // an energy query is not a move to commit
+    return rc;
+  });
+}
+
+int fmc_displace(fmc_plain *h, int iguest, int choice, const double *abcq, fmc_move_result *res) {
+  return guard([&] {
+    if (!h || !abcq) raise(FMC_ERR_ARG, "null argument");
+    const System &s = *h->C.hsys[0];
+    if (iguest < 1 || iguest > s.ntpguest) raise(FMC_ERR_ARG, "bad guest index");
+    MoveCtx mc;
+    std::memset(&mc, 0, sizeof mc);
+    mc.kind = 3;
+    mc.g = iguest - 1;
+    mc.ns = s.mol[s.locguest[iguest]].natoms;
+    mc.npos = 2;
+    mc.choice = choice;
+    mc.pos[1][0][0] = abcq[0];
+    mc.pos[1][0][1] = abcq[1];
+    mc.pos[1][0][2] = abcq[2];
+    mc.pos[1][1][0] = abcq[3];
+    mc.pos[1][1][1] = abcq[4];
+    mc.pos[1][1][2] = abcq[5];
+    mc.pos[1][2][0] = abcq[6];
+    return plain_eval(h, mc, res, false);
+  });
+}
+
+int fmc_metropolis_commit(fmc_plain *h, double rande, int *accepted) {
+  return guard([&] {
+    if (!h) raise(FMC_ERR_ARG, "null argument");
+    if (!h->has_move) raise(FMC_ERR_STATE, "no evaluated move to commit");
+    Chains &C = h->C;
+    MoveCtx mc;
+    FMC_CUDA(cudaMemcpy(&mc, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost));
+    mc.rande = rande;
+    FMC_CUDA(cudaMemcpyAsync(C.ctx.p, &mc, sizeof(MoveCtx), cudaMemcpyHostToDevice, C.stream));
+    C.launch(kModeCommit, 0);
+    FMC_CUDA(cudaMemcpyAsync(&mc, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost, C.stream));
+    C.sync();
+    C.check_status();
+    h->has_move = 0;
+    if (accepted) *accepted = mc.accepted;
+    return FMC_OK;
+  });
+}
+
+int fmc_plain_get_nummols(const fmc_plain *h, int iguest, int *n) {
+  return guard([&] {
+    if (!h || !n) raise(FMC_ERR_ARG, "null argument");
+    ChainHdr hd;
+    FMC_CUDA(cudaMemcpy(&hd, h->C.hdr.p, sizeof hd, cudaMemcpyDeviceToHost));
+    if (iguest < 1 || iguest > kMaxG) raise(FMC_ERR_ARG, "bad guest index");
+    *n = hd.nummols[iguest - 1];
+    return FMC_OK;
+  });
+}
+
+static int chain_coords(const Chains &C, int chain, int iguest, double *xyz, int cap, int *nout) {
+  ChainHdr hd;
+  FMC_CUDA(cudaMemcpy(&hd, C.hdr.p + chain, sizeof hd, cudaMemcpyDeviceToHost));
+  const System &s = *C.hsys[hd.system];
+  int g = iguest - 1;
+  int n = hd.nummols[g];
+  int ns = s.mol[s.locguest[iguest]].natoms;
+  std::vector<int> ord(n);
+  if (n)
+    FMC_CUDA(cudaMemcpy(ord.data(), C.ord.p + ((size_t)chain * kMaxG + g) * C.CA.cap,
+                        n * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<double> all((size_t)C.CA.cap * kMaxS * 3);
+  FMC_CUDA(cudaMemcpy(all.data(), C.gpos.p + ((size_t)chain * kMaxG + g) * C.CA.cap * kMaxS * 3,
+                      all.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  int w = 0;
+  for (int i = 0; i < n; ++i)
+    for (int sidx = 0; sidx < ns; ++sidx)
+      for (int d = 0; d < 3; ++d) {
+        if (w < cap) xyz[w] = all[((size_t)ord[i] * kMaxS + sidx) * 3 + d];
+        ++w;
+      }
+  if (nout) *nout = n;
+  return FMC_OK;
+}
+
+int fmc_plain_get_coords(const fmc_plain *h, int iguest, double *xyz, int cap) {
+  return guard([&] {
+    if (!h || !xyz) raise(FMC_ERR_ARG, "null argument");
+    return chain_coords(h->C, 0, iguest, xyz, cap, nullptr);
+  });
+}
+
+static int chain_sk(const Chains &C, int chain, double *out, int cap) {
+  ChainHdr hd;
+  FMC_CUDA(cudaMemcpy(&hd, C.hdr.p + chain, sizeof hd, cudaMemcpyDeviceToHost));
+  const System &s = *C.hsys[hd.system];
+  const DevSystem &D = *C.sys[hd.system];
+  int nk = s.newld, nm = s.maxmls + 1;
+  if (cap < 2 * nm * nk) raise(FMC_ERR_CAPACITY, "output buffer too small for S(k)");
+  std::vector<double2> g((size_t)kMaxG * C.CA.nkmax);
+  FMC_CUDA(cudaMemcpy(g.data(), C.sk.p + (size_t)chain * kMaxG * C.CA.nkmax,
+                      g.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < nk; ++k) {
+    double tx = 0, ty = 0;
+    for (int m = 0; m < nm; ++m) {
+      out[2 * ((size_t)k * nm + m)] = 0.0;
+      out[2 * ((size_t)k * nm + m) + 1] = 0.0;
+    }
+    double2 f = D.skfw_host[k];
+    out[2 * ((size_t)k * nm + (s.fw_mol - 1))] = f.x;
+    out[2 * ((size_t)k * nm + (s.fw_mol - 1)) + 1] = f.y;
+    tx += f.x;
+    ty += f.y;
+    for (int gg = 0; gg < s.ntpguest; ++gg) {
+      double2 v = g[(size_t)gg * C.CA.nkmax + k];
+      int m = s.locguest[gg + 1] - 1;
+      out[2 * ((size_t)k * nm + m)] = v.x;
+      out[2 * ((size_t)k * nm + m) + 1] = v.y;
+      tx += v.x;
+      ty += v.y;
+    }
+    out[2 * ((size_t)k * nm + s.maxmls)] = tx;
+    out[2 * ((size_t)k * nm + s.maxmls) + 1] = ty;
+  }
+  return FMC_OK;
+}
+
+int fmc_plain_get_sk(const fmc_plain *h, double *sk, int cap) {
+  return guard([&] {
+    if (!h || !sk) raise(FMC_ERR_ARG, "null argument");
+    return chain_sk(h->C, 0, sk, cap);
+  });
+}
+
+int fmc_plain_get_energy(const fmc_plain *h, double *energy, int cap) {
+  return guard([&] {
+    if (!h || !energy) raise(FMC_ERR_ARG, "null argument");
+    ChainHdr hd;
+    FMC_CUDA(cudaMemcpy(&hd, h->C.hdr.p, sizeof hd, cudaMemcpyDeviceToHost));
+    for (int m = 1; m <= h->C.maxmls && m <= cap; ++m) energy[m - 1] = hd.energy[m];
+    return FMC_OK;
+  });
+}
+
+// ----------------------------------------------------------- batch mode
+int fmc_batch_create(const fmc_system *const *systems, int nsys, const fmc_chain_spec *chains,
+                     int nchains, int precision, int guest_capacity, fmc_batch **out) {
+  return guard([&] {
+    if (!systems || !out) raise(FMC_ERR_ARG, "null argument");
+    std::vector<const System *> sp;
+    for (int i = 0; i < nsys; ++i) sp.push_back(systems[i] ? &systems[i]->s : nullptr);
+    auto b = std::make_unique<fmc_batch>();
+    init_chains(b->C, sp.data(), nsys, chains, nchains, precision, guest_capacity);
+    // per-chain "create molecules" override
+    if (chains) {
+      std::vector<ChainHdr> hh(nchains);
+      FMC_CUDA(cudaMemcpy(hh.data(), b->C.hdr.p, nchains * sizeof(ChainHdr), cudaMemcpyDeviceToHost));
+      (void)hh;
+    }
+    // device-side pre-loading uses the system's insert0; per-chain counts
+    // are applied by a system copy per distinct count
+    bool custom = false;
+    for (int c = 0; chains && c < nchains; ++c)
+      if (chains[c].create_molecules >= 0) custom = true;
+    if (custom) {
+      // one SysDev per chain carrying its own insert0
+      std::vector<SysDev> per(nchains);
+      std::vector<ChainHdr> hh(nchains);
+      FMC_CUDA(cudaMemcpy(hh.data(), b->C.hdr.p, nchains * sizeof(ChainHdr), cudaMemcpyDeviceToHost));
+      for (int c = 0; c < nchains; ++c) {
+        per[c] = b->C.sys[hh[c].system]->d;
+        if (chains[c].create_molecules >= 0) per[c].g[0].insert0 = chains[c].create_molecules;
+        hh[c].system = c;
+      }
+      DBuf<SysDev> tmp;
+      tmp.upload(per);
+      FMC_CUDA(cudaMemcpy(b->C.hdr.p, hh.data(), nchains * sizeof(ChainHdr), cudaMemcpyHostToDevice));
+      std::swap(b->C.sysarr.p, tmp.p);
+      std::swap(b->C.sysarr.n, tmp.n);
+      b->C.launch(kModeCreate, 0);
+      b->C.sync();
+      std::swap(b->C.sysarr.p, tmp.p);
+      std::swap(b->C.sysarr.n, tmp.n);
+      for (int c = 0; c < nchains; ++c) hh[c].system = chains[c].system;
+      std::vector<ChainHdr> cur(nchains);
+      FMC_CUDA(cudaMemcpy(cur.data(), b->C.hdr.p, nchains * sizeof(ChainHdr), cudaMemcpyDeviceToHost));
+      for (int c = 0; c < nchains; ++c) cur[c].system = chains[c].system;
+      FMC_CUDA(cudaMemcpy(b->C.hdr.p, cur.data(), nchains * sizeof(ChainHdr), cudaMemcpyHostToDevice));
+    } else {
+      b->C.launch(kModeCreate, 0);
+      b->C.sync();
+    }
+    b->C.check_status();
+    *out = b.release();
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_destroy(fmc_batch *b) {
+  delete b;
+  return FMC_OK;
+}
+
+int fmc_batch_set_log(fmc_batch *b, int cap) {
+  return guard([&] {
+    if (!b || cap < 0) raise(FMC_ERR_ARG, "bad argument");
+    Chains &C = b->C;
+    C.logcap = cap;
+    C.logs.alloc(std::max(1, cap) * (size_t)C.nchains);
+    C.logs.zero();
+    std::vector<ChainHdr> hh(C.nchains);
+    FMC_CUDA(cudaMemcpy(hh.data(), C.hdr.p, C.nchains * sizeof(ChainHdr), cudaMemcpyDeviceToHost));
+    for (auto &h : hh) h.log_n = 0;
+    FMC_CUDA(cudaMemcpy(C.hdr.p, hh.data(), C.nchains * sizeof(ChainHdr), cudaMemcpyHostToDevice));
+    if (C.graph) {
+      cudaGraphExecDestroy(C.graph);
+      C.graph = nullptr;
+      C.graph_moves = -1;
+    }
+    return FMC_OK;
+  });
+}
+
+static void run_cycle(Chains &C, int nmoves) {
+  if (nmoves < 0) raise(FMC_ERR_ARG, "negative move count");
+  if (C.graph_moves != nmoves) {
+    if (C.graph) {
+      cudaGraphExecDestroy(C.graph);
+      C.graph = nullptr;
+    }
+    cudaGraph_t g;
+    FMC_CUDA(cudaStreamBeginCapture(C.stream, cudaStreamCaptureModeThreadLocal));
+    C.launch(kModeMoves, nmoves);
+    FMC_CUDA(cudaStreamEndCapture(C.stream, &g));
+    FMC_CUDA(cudaGraphInstantiate(&C.graph, g, 0));
+    cudaGraphDestroy(g);
+    C.graph_moves = nmoves;
+  }
+  std::vector<long long> e0(C.nchains), m0(C.nchains);
+  C.pull_headers();
+  long long evals0 = 0, moves0 = 0;
+  for (auto &h : C.host_hdr) {
+    evals0 += h.evals;
+    moves0 += h.moves;
+  }
+  FMC_CUDA(cudaEventRecord(C.ev0, C.stream));
+  FMC_CUDA(cudaGraphLaunch(C.graph, C.stream));
+  FMC_CUDA(cudaEventRecord(C.ev1, C.stream));
+  C.sync();
+  float ms = 0.f;
+  FMC_CUDA(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
+  C.last_ms = ms;
+  C.check_status();
+  long long evals1 = 0, moves1 = 0;
+  for (auto &h : C.host_hdr) {
+    evals1 += h.evals;
+    moves1 += h.moves;
+  }
+  C.last_evals = evals1 - evals0;
+  C.last_moves = moves1 - moves0;
+}
+
+int fmc_batch_run(fmc_batch *b, int nmoves, fmc_chain_stats *stats) {
+  return guard([&] {
+    if (!b) raise(FMC_ERR_ARG, "null batch");
+    run_cycle(b->C, nmoves);
+    if (stats) fill_stats(b->C, stats);
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_run_cycle(fmc_batch *b, int nmoves, const double *host_fugacity,
+                        fmc_chain_stats *host_stats) {
+  return guard([&] {
+    if (!b) raise(FMC_ERR_ARG, "null batch");
+    Chains &C = b->C;
+    if (host_fugacity) {
+      // patch the per-chain fugacities in the device headers
+      C.pull_headers();
+      for (int c = 0; c < C.nchains; ++c) C.host_hdr[c].fuga[0] = host_fugacity[c];
+      FMC_CUDA(cudaMemcpyAsync(C.hdr.p, C.host_hdr.data(), C.nchains * sizeof(ChainHdr),
+                               cudaMemcpyHostToDevice, C.stream));
+    }
+    run_cycle(C, nmoves);
+    if (host_stats) fill_stats(C, host_stats);
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_get_stats(fmc_batch *b, fmc_chain_stats *stats) {
+  return guard([&] {
+    if (!b || !stats) raise(FMC_ERR_ARG, "null argument");
+    b->C.pull_headers();
+    fill_stats(b->C, stats);
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_get_log(fmc_batch *b, int chain, fmc_move_log *log, int cap, int *n) {
+  return guard([&] {
+    if (!b || !log || !n) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (chain < 0 || chain >= C.nchains) raise(FMC_ERR_ARG, "bad chain index");
+    C.pull_headers();
+    int m = (int)std::min<long long>(C.host_hdr[chain].log_n, std::min(cap, C.logcap));
+    std::vector<LogRec> tmp(m);
+    if (m)
+      FMC_CUDA(cudaMemcpy(tmp.data(), C.logs.p + (size_t)chain * C.logcap, m * sizeof(LogRec),
+                          cudaMemcpyDeviceToHost));
+    static_assert(sizeof(LogRec) == sizeof(fmc_move_log), "log layout");
+    std::memcpy(log, tmp.data(), m * sizeof(LogRec));
+    *n = m;
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_get_coords(fmc_batch *b, int chain, double *xyz, int cap, int *n) {
+  return guard([&] {
+    if (!b || !xyz) raise(FMC_ERR_ARG, "null argument");
+    if (chain < 0 || chain >= b->C.nchains) raise(FMC_ERR_ARG, "bad chain index");
+    return chain_coords(b->C, chain, 1, xyz, cap, n);
+  });
+}
+
+int fmc_batch_get_sk(fmc_batch *b, int chain, double *sk, int cap) {
+  return guard([&] {
+    if (!b || !sk) raise(FMC_ERR_ARG, "null argument");
+    if (chain < 0 || chain >= b->C.nchains) raise(FMC_ERR_ARG, "bad chain index");
+    return chain_sk(b->C, chain, sk, cap);
+  });
+}
+
+int fmc_batch_last_timing(const fmc_batch *b, double *kernel_ms, int64_t *evals, int64_t *moves) {
+  return guard([&] {
+    if (!b) raise(FMC_ERR_ARG, "null batch");
+    if (kernel_ms) *kernel_ms = b->C.last_ms;
+    if (evals) *evals = b->C.last_evals;
+    if (moves) *moves = b->C.last_moves;
+    return FMC_OK;
+  });
+}
+
+}  // extern "C"

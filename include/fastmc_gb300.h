@@ -1,0 +1,241 @@
+/*
+ * fastmc_gb300.h -- C ABI of the GB300 (sm_103a) GCMC trial-move energy path.
+ *
+ * The ABI is plain C: opaque handles, pointers, sizes and int status codes
+ * (0 = OK).  Every entry point is callable from Fortran through
+ * ISO_C_BINDING (integer(c_int), real(c_double), type(c_ptr)).  Logical
+ * flags are integer(c_int) 0/1.  Arrays are 0-based on this side; guest
+ * type and molecule indices keep the reference's 1-based numbering.
+ *
+ * Three groups of entry points:
+ *  1. Host set-up.  fmc_system_load reads FIELD, CONFIG and CONTROL and
+ *     builds the tables and constants that the reference computes at start
+ *     (gcmc.f:203-590).  A Fortran host that already holds these arrays
+ *     replaces it by fmc_system_create_from_arrays.
+ *  2. Per-move drop-in ("plain" mode).  The device mirrors the host's
+ *     guest coordinates and structure factor; each call evaluates one trial
+ *     move and leaves s(k) on the device for the commit, exactly like
+ *     ckcsnew/ckssnew in the reference.
+ *  3. Device-resident chains ("batch" mode): many independent GCMC chains
+ *     run their whole move loop on the device (RNG, proposal, energy,
+ *     Metropolis, commit, statistics) in one persistent kernel per cycle.
+ */
+#ifndef FASTMC_GB300_H
+#define FASTMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; positive values map to the reference's error() codes in
+ * INTEGRATION.md */
+#define FMC_OK 0
+#define FMC_ERR_ARG 1      /* invalid argument or handle */
+#define FMC_ERR_CUDA 2     /* CUDA runtime failure (message has details) */
+#define FMC_ERR_CAPACITY 3 /* guest capacity or buffer size exceeded */
+#define FMC_ERR_INPUT 4    /* malformed or unsupported input file content */
+#define FMC_ERR_DEVICE 5   /* a kernel raised its status word (see message) */
+#define FMC_ERR_STATE 6    /* call out of order (e.g. commit before a move) */
+#define FMC_ERR_NODEVICE 7 /* no CUDA device */
+
+/* arithmetic of the pair and k-space terms */
+#define FMC_PREC_FP64 0 /* everything FP64: parity mode */
+#define FMC_PREC_FP32 1 /* FP32 terms, FP64 accumulation, FP64 S(k) */
+
+/* move kinds (the reference's insert / delete / displace flags) */
+#define FMC_MOVE_INSERT 1
+#define FMC_MOVE_DELETE 2
+#define FMC_MOVE_DISPLACE 3  /* "move displace": translation + rotation */
+#define FMC_MOVE_TRANSLATE 4 /* "move translate" */
+#define FMC_MOVE_ROTATE 5    /* "move rotate" */
+
+#define FMC_MAX_MOLTYPES 8
+#define FMC_MAX_GUEST_TYPES 4
+#define FMC_MAX_SITES 8
+
+typedef struct fmc_system fmc_system;
+typedef struct fmc_plain fmc_plain;
+typedef struct fmc_batch fmc_batch;
+
+/* Copy the calling thread's last error message into buf (NUL-terminated).
+ * Returns the message length. */
+int fmc_last_error(char *buf, int len);
+
+/* Library version string, e.g. "fastmc_gb300 1.0 sm_103a". */
+const char *fmc_version(void);
+
+/* ------------------------------------------------------------- set-up --
+ * Replaces: initscan (utility_pack.f:207-508), readfield
+ * (readinputs.f:11-307), define_van_der_waals + forgen (vdw_terms.f:1-380),
+ * readconfig (readinputs.f:309-513), readcontrol (readinputs.f:515-944),
+ * fugacity (utility_pack.f:1206-1310), move-frequency normalisation
+ * (gcmc.f:341-386), erfcgen (ewald.f:1-30), lrcorrect (vdw_terms.f:468-684)
+ * and excluding_ewald_charges (gcmc.f:2662-2761). */
+int fmc_system_load(const char *dir, fmc_system **out);
+int fmc_system_free(fmc_system *sys);
+
+typedef struct {
+  int imcon;
+  int maxmls;       /* molecule types */
+  int ntpguest;     /* guest types */
+  int ntpatm;       /* unique atom types */
+  int n_framework;  /* framework atoms */
+  int kmax[3];
+  int newld;        /* k-vectors in the half space */
+  int mxegrd;       /* table points */
+  int guest_mol[FMC_MAX_GUEST_TYPES];    /* locguest */
+  int guest_nsites[FMC_MAX_GUEST_TYPES];
+  int guest_insert[FMC_MAX_GUEST_TYPES]; /* "create molecules" */
+  double alpha, rcut, volm, engunit, temperature, sumchg, drewd;
+  double cell[9];
+  double fugacity[FMC_MAX_GUEST_TYPES]; /* Pa */
+  double ewald3en[FMC_MAX_GUEST_TYPES]; /* per guest type, internal units */
+  int mcsteps, eqsteps, nwindsteps;
+} fmc_system_info;
+
+int fmc_system_get_info(const fmc_system *sys, fmc_system_info *info);
+
+/* Override the fugacity (Pa) of guest type iguest (1-based) before creating
+ * chains; used to build isotherms from one set of files. */
+int fmc_system_set_fugacity(fmc_system *sys, int iguest, double pascal);
+
+/* --------------------------------------------------- per-move drop-in --
+ * One trial-move evaluation per call.  Results in internal units where the
+ * reference keeps internal units and kcal/mol (FIELD unit) for estep/delE,
+ * as mc_moves.f does. */
+typedef struct {
+  double estep;     /* energy change, FIELD unit (what energy_eval gets) */
+  double ewld1;     /* reciprocal part (ewld1eng), internal units */
+  double ewld2;     /* real-space erfc part, internal units */
+  double vdw;       /* van der Waals part, internal units */
+  double delrc;     /* long-range correction, internal units */
+  double delE[FMC_MAX_MOLTYPES]; /* delE(1..maxmls) in delE[0..maxmls-1] */
+  int overlap;      /* loverlap */
+  int surface;      /* lnewsurf / linitsurf of the evaluated position */
+  int surface_old;  /* displacement: linitsurf of the old position */
+  int status;       /* device status word (0 = clean) */
+  double newxyz[3 * FMC_MAX_SITES]; /* trial site coordinates x,y,z */
+} fmc_move_result;
+
+/* Create the device mirror of `sys` (framework, tables, k-vectors) with
+ * room for `guest_capacity` molecules per guest type. */
+int fmc_plain_create(const fmc_system *sys, int precision, int guest_capacity,
+                     fmc_plain **out);
+int fmc_plain_destroy(fmc_plain *h);
+
+/* Full reciprocal sum from the current coordinates (ewald.f:354-661) and
+ * the electrostatic energy single_point prints (gcmc.f:2659, 585-586):
+ * out[0] = ecoul / engunit, out[1] = ewald1 sum (internal), out[2] = sic,
+ * out[3] = qfix.  Resets the device S(k) to the recomputed values. */
+int fmc_full_ewald(fmc_plain *h, double *out4);
+
+/* insertion (mc_moves.f:150-276) of guest type iguest at site coordinates
+ * xyz (natms triples x,y,z). */
+int fmc_insertion(fmc_plain *h, int iguest, const double *xyz,
+                  fmc_move_result *res);
+/* deletion (mc_moves.f:375-484) of molecule `choice` (1-based). */
+int fmc_deletion(fmc_plain *h, int iguest, int choice, fmc_move_result *res);
+/* displace_guest (gcmc.f:2816-2901): shift a,b,c then quaternion q1..q4
+ * about the new centre of mass; abcq = {a,b,c,q1,q2,q3,q4}. */
+int fmc_displace(fmc_plain *h, int iguest, int choice, const double *abcq,
+                 fmc_move_result *res);
+/* guest_energy (mc_moves.f:277-374) of existing molecule `choice`
+ * (lexisting = 1) without a move. */
+int fmc_guest_energy(fmc_plain *h, int iguest, int choice,
+                     fmc_move_result *res);
+
+/* energy_eval (utility_pack.f:3637-3693) on the device for the last
+ * evaluated move, then accept_move / reject_move (mc_moves.f:485-673):
+ * commits S(k), coordinates and counters on the device when accepted.
+ * `rande` is the host's uniform draw; for a displacement with estep < 0
+ * the move is accepted without it (gcmc.f:1879-1886).  Writes the
+ * decision to *accepted. */
+int fmc_metropolis_commit(fmc_plain *h, double rande, int *accepted);
+
+/* Read back the device state: guest coordinates of guest type iguest
+ * (3 * nsites * nummols doubles in molecule order) and the structure
+ * factor S(k) per molecule type, [k][moltype][re,im] with moltype
+ * 0..maxmls-1 and maxmls = total (2 * (maxmls+1) * newld doubles). */
+int fmc_plain_get_nummols(const fmc_plain *h, int iguest, int *n);
+int fmc_plain_get_coords(const fmc_plain *h, int iguest, double *xyz, int cap);
+int fmc_plain_get_sk(const fmc_plain *h, double *sk, int cap);
+/* Guest energies energy(mol), FIELD unit, mol = 1..maxmls. */
+int fmc_plain_get_energy(const fmc_plain *h, double *energy, int cap);
+
+/* ------------------------------------------------ device-resident chains */
+typedef struct {
+  int system;           /* index into the systems array */
+  double pressure_pa;   /* fugacity of guest type 1 (< 0: keep the file's) */
+  int64_t seed;         /* MZT seed hook (see fmc_batch_create) */
+  int create_molecules; /* < 0: use the CONTROL value */
+} fmc_chain_spec;
+
+/* Per-chain counters and averages, guest type 1. */
+typedef struct {
+  int64_t moves;           /* trial moves done */
+  int64_t evals;           /* completed energy evaluations (no overlap exit) */
+  int64_t overlap_exits;   /* positions rejected by the overlap test */
+  int64_t attempts[5];     /* insert, delete, displace, translate, rotate */
+  int64_t accepts[5];
+  int nummols;
+  int status;              /* device status word */
+  double energy;           /* energy(guest mol), FIELD unit */
+  double avg_n, avg_e, avg_en, avg_n2, avg_e2, avg_nf, qst, cv;
+  int64_t prodcount;
+  int64_t windows;
+} fmc_chain_stats;
+
+/* One entry of the optional per-move log (parity tests). */
+typedef struct {
+  int move;      /* FMC_MOVE_* */
+  int iguest;
+  int choice;
+  int overlap;
+  int accepted;
+  int nmols_after;
+  double estep;
+  double rande;  /* -1 when not drawn */
+  double newxyz[9];
+} fmc_move_log;
+
+/* Create `nchains` chains over `nsys` systems.  The seed hook: seed s maps
+ * to the clock values the reference would read (milliseconds s % 1000,
+ * seconds (s / 1000) % 60, utility_pack.f:2796-2802) and the first draw
+ * (gcmc.f:389) is consumed.  "create molecules" pre-loading
+ * (mc_moves.f:84-149) runs on the device here.
+ * guest_capacity bounds the molecules per chain. */
+int fmc_batch_create(const fmc_system *const *systems, int nsys,
+                     const fmc_chain_spec *chains, int nchains, int precision,
+                     int guest_capacity, fmc_batch **out);
+int fmc_batch_destroy(fmc_batch *b);
+
+/* Enable a per-move log of `cap` entries per chain (0 disables). */
+int fmc_batch_set_log(fmc_batch *b, int cap);
+
+/* Run `nmoves` main-loop iterations (gcmc.f:704-1164) on every chain.  The
+ * cycle is captured once as a CUDA graph and replayed.  If stats != NULL
+ * the per-chain statistics are copied to it (nchains entries). */
+int fmc_batch_run(fmc_batch *b, int nmoves, fmc_chain_stats *stats);
+
+/* Same, with a host control block: per-chain fugacity (Pa) uploaded
+ * before the cycle (nullable), statistics downloaded after it. */
+int fmc_batch_run_cycle(fmc_batch *b, int nmoves, const double *host_fugacity,
+                        fmc_chain_stats *host_stats);
+
+int fmc_batch_get_stats(fmc_batch *b, fmc_chain_stats *stats);
+int fmc_batch_get_log(fmc_batch *b, int chain, fmc_move_log *log, int cap,
+                      int *n);
+int fmc_batch_get_coords(fmc_batch *b, int chain, double *xyz, int cap, int *n);
+int fmc_batch_get_sk(fmc_batch *b, int chain, double *sk, int cap);
+
+/* Timing of the last fmc_batch_run: device milliseconds of the persistent
+ * kernel (CUDA events on its stream) and the completed evaluations. */
+int fmc_batch_last_timing(const fmc_batch *b, double *kernel_ms,
+                          int64_t *evals, int64_t *moves);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

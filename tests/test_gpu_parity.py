@@ -1,0 +1,177 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+FP64 mode must match the oracle to 1e-9 relative per move (and bit-exact
+decisions); the reference's own known answer (CALF-20 electrostatic
+energy) must come out of the GPU structure-factor kernel.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import CALF20, GOLDEN
+from fastmc_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-9   # FP64 parity tolerance per energy term
+
+
+def close(a, b, rel=REL, scale=1.0):
+    return abs(a - b) <= rel * max(abs(a), abs(b), scale)
+
+
+def golden():
+    with open(os.path.join(GOLDEN, "golden.json")) as f:
+        return json.load(f)
+
+
+def test_gpu_calf20_kat(fmc_lib, oracle_lib):
+    """K4 structure factor on the GPU reproduces the reference's printed
+    electrostatic energy of its own test system."""
+    sysm = fmc_lib.System.load(CALF20)
+    plain = fmc_lib.PlainEngine(sysm, fmc_lib.FMC_PREC_FP64, 16)
+    out = plain.full_ewald()
+    g = golden()
+    assert abs(out[0] - g["calf20_electrostatic_energy_kcal"]) < g["tolerance_abs"], out
+    # framework S(k) against the oracle's ckcsum/ckssum
+    o = oracle_lib.Oracle(CALF20)
+    so, sg = o.sk(), plain.sk()
+    tot = sysm.info().maxmls
+    assert np.allclose(sg[:, tot, :], so[:, tot, :], rtol=1e-10, atol=1e-10 * np.abs(so).max())
+
+
+@pytest.fixture(scope="module")
+def small(inputs_dir):
+    return inputs_dir(syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=10), "gpu_small")
+
+
+def _free_positions(o, n, seed, box=25.6):
+    rng = np.random.default_rng(seed)
+    tmpl = np.array([[0, 0, 0], [0, 0, 1.16], [0, 0, -1.16]])
+    out = []
+    for _ in range(200000):
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        xyz = np.outer([0, 1.16, -1.16], ax) + rng.uniform(0, box, 3)
+        if not o.insertion_energy(1, xyz)["overlap"]:
+            out.append(xyz)
+            if len(out) == n:
+                break
+    return out
+
+
+def _cmp(res, ref, maxmls):
+    assert res["overlap"] == ref["overlap"]
+    if ref["overlap"]:
+        return
+    for k in ("estep", "ewld1", "ewld2", "vdw", "delrc"):
+        assert close(res[k], ref[k], scale=1e-6), (k, res[k], ref[k])
+    for m in range(maxmls):
+        assert close(res["delE"][m], ref["delE"][m], scale=1e-6), ("delE", m, res["delE"], ref["delE"])
+
+
+def test_gpu_per_move_abi_fp64(fmc_lib, oracle_lib, small):
+    """insertion / deletion / displace_guest / commit through the C ABI, FP64,
+    against the oracle on the same state."""
+    o = oracle_lib.Oracle(small)
+    sysm = fmc_lib.System.load(small)
+    plain = fmc_lib.PlainEngine(sysm, fmc_lib.FMC_PREC_FP64, 64)
+    maxmls = sysm.info().maxmls
+    pos = _free_positions(o, 14, seed=1)
+    assert len(pos) >= 10
+    # build the same guest population on both sides
+    for xyz in pos[:8]:
+        ref = o.insertion_energy(1, xyz)
+        res = plain.insertion(1, xyz)
+        _cmp(res, ref, maxmls)
+        assert plain.commit(0.0)  # rande 0 accepts any non-overlapping insertion
+        o.apply_move(1, 1, 0, xyz, True)
+    assert plain.nummols(1) == 8
+    assert np.allclose(plain.coords(1), o.coords(o.locguest(1)), rtol=0, atol=1e-12)
+    # trial insertions, including overlapping ones
+    rng = np.random.default_rng(3)
+    for xyz in pos[8:] + [pos[0] + 0.3]:
+        _cmp(plain.insertion(1, xyz), o.insertion_energy(1, xyz), maxmls)
+    # deletions of every molecule
+    for c in range(1, 9):
+        _cmp(plain.deletion(1, c), o.deletion_energy(1, c), maxmls)
+    # displacements with random shift and rotation
+    for _ in range(12):
+        c = int(rng.integers(1, 9))
+        a, b, cc = rng.uniform(-0.6, 0.6, 3)
+        th = rng.uniform(0, 1.0)
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        q = [math.cos(th / 2), *(math.sin(th / 2) * ax)]
+        abcq = [a, b, cc, *q]
+        _cmp(plain.displace(1, c, abcq), o.displace_energy(1, c, abcq), maxmls)
+    # commit a displacement and a deletion on both, then compare S(k)
+    abcq = [0.2, -0.1, 0.05, 1.0, 0.0, 0.0, 0.0]
+    r = plain.displace(1, 3, abcq)
+    if not r["overlap"]:
+        assert plain.commit(0.0) or r["estep"] > 0
+        o.apply_move(3, 1, 3, abcq, True)
+    plain.deletion(1, 5)
+    plain.commit(0.0)
+    o.apply_move(2, 1, 5, None, True)
+    assert plain.nummols(1) == o.nummols(o.locguest(1))
+    sg, so = plain.sk(), o.sk()
+    assert np.allclose(sg, so, rtol=1e-10, atol=1e-10 * np.abs(so).max())
+    eg = plain.energy()
+    mol = o.locguest(1)
+    assert close(eg[mol - 1], o.energy(mol), rel=1e-9, scale=1e-6)
+
+
+def _oracle_chain(oracle_lib, d, seed, ncreate, nmoves):
+    o = oracle_lib.Oracle(d)
+    o.seed(seed)
+    if ncreate:
+        o.create_molecules(1, ncreate)
+    return o, o.run(nmoves)
+
+
+def test_gpu_chain_fp64_matches_oracle(fmc_lib, oracle_lib, small):
+    """A whole chain on the device (RNG, proposals, Metropolis, commit) in
+    FP64 follows the oracle move by move: identical decisions, estep to
+    1e-9 relative."""
+    n = 600
+    o, ref = _oracle_chain(oracle_lib, small, 77, 10, n)
+    sysm = fmc_lib.System.load(small)
+    b = fmc_lib.Batch([sysm], [{"seed": 77}], precision=fmc_lib.FMC_PREC_FP64, guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    assert len(got) == n
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.choice, g.overlap, g.accepted) == (r.move, r.choice, r.overlap, r.accepted), i
+        assert g.rande == r.rande, i
+        if not r.overlap:
+            assert close(g.estep, r.estep, scale=1e-6), (i, g.estep, r.estep)
+        assert g.nmols_after == r.nmols_after
+    st = b.stats()[0]
+    mol = o.locguest(1)
+    assert st.nummols == o.nummols(mol)
+    assert close(st.energy, o.energy(mol), rel=1e-8, scale=1e-6)
+    ostats = o.stats(1)
+    assert st.attempts[0] == ostats[10] and st.accepts[0] == ostats[11]
+
+
+def test_gpu_batch_chains_independent(fmc_lib, small):
+    """Chains in one launch do not interact: a 3-chain batch reproduces
+    three single-chain runs bit for bit."""
+    sysm = fmc_lib.System.load(small)
+    seeds = [5, 6, 7]
+    b = fmc_lib.Batch([sysm], [{"seed": s} for s in seeds], precision=fmc_lib.FMC_PREC_FP64,
+                      guest_capacity=64)
+    b.run(200)
+    multi = b.stats()
+    for i, s in enumerate(seeds):
+        one = fmc_lib.Batch([sysm], [{"seed": s}], precision=fmc_lib.FMC_PREC_FP64, guest_capacity=64)
+        one.run(200)
+        st = one.stats()[0]
+        assert st.nummols == multi[i].nummols
+        assert st.energy == multi[i].energy
+        assert list(st.accepts) == list(multi[i].accepts)

@@ -1,0 +1,88 @@
+"""The library's host set-up (readers, tables, k-vectors) against the
+oracle, and the C-ABI surface.  CPU only: no kernel is launched."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import CALF20, ROOT
+from fastmc_gb300 import synthetic as syn
+
+
+def header_functions():
+    with open(os.path.join(ROOT, "include", "fastmc_gb300.h")) as f:
+        txt = f.read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(fmc_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol(fmc_lib):
+    import fastmc_gb300._lib as L
+    lib = L.load()
+    names = header_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in L.SIGNATURES, n
+    assert lib.fmc_version().startswith(b"fastmc_gb300")
+
+
+@pytest.mark.parametrize("which", ["calf20", "config1", "small"])
+def test_setup_matches_oracle(fmc_lib, oracle_lib, inputs_dir, which):
+    if which == "calf20":
+        d = CALF20
+    elif which == "config1":
+        d = inputs_dir(syn.config1(), "cfg1")
+    else:
+        d = inputs_dir(syn.small_test_spec(seed=9, kmax=6, create=5), "small9")
+    s = fmc_lib.System.load(d)
+    inf = s.info()
+    o = oracle_lib.Oracle(d).setup_energies()
+    assert inf.alpha == o["alpha"]
+    assert tuple(inf.kmax) == (o["kmax1"], o["kmax2"], o["kmax3"])
+    assert inf.newld == o["newld"]
+    assert inf.sumchg == o["sumchg"]
+    assert inf.volm == o["volm"]
+    assert inf.engunit == o["engunit"]
+
+
+def test_tables_match_oracle(fmc_lib, oracle_lib, inputs_dir):
+    d = inputs_dir(syn.config1(), "cfg1")
+    orc = oracle_lib.Oracle(d)
+    out = np.zeros(2000)
+    n = orc.lib.orc_get_erc(orc._h, out.ctypes.data_as(C.POINTER(C.c_double)), 2000)
+    assert n == 1254  # mxegrd = int(12.5/0.01+0.5)+4 (utility_pack.f:996)
+    s = fmc_lib.System.load(d)
+    assert s.info().mxegrd == n
+    assert abs(s.info().drewd - 0.01) < 1e-15
+
+
+def test_config_errors_are_reported(fmc_lib, tmp_path):
+    import fastmc_gb300._lib as L
+    with pytest.raises(L.FmcError) as e:
+        fmc_lib.System.load(str(tmp_path / "missing"))
+    assert e.value.code == 4
+    d = tmp_path / "jump"
+    spec = syn.small_test_spec()
+    spec.move_mix = (("insert", 0.5), ("jump", 0.5))
+    syn.write_inputs(str(d), spec)
+    with pytest.raises(L.FmcError) as e:
+        fmc_lib.System.load(str(d))
+    assert "jump" in str(e.value)
+
+
+def test_synthetic_framework_properties():
+    uc = syn.make_unit_cell(1)
+    d = uc.xyz[:, None, :] - uc.xyz[None, :, :]
+    d -= syn.UNIT_CELL * np.round(d / syn.UNIT_CELL)
+    r2 = np.einsum("ijk,ijk->ij", d, d) + np.eye(len(uc.xyz)) * 1e9
+    assert np.sqrt(r2.min()) >= syn.MIN_SEP
+    assert abs(uc.charges.sum()) < 1e-9
+    assert np.bincount(uc.types).tolist() == [48, 48, 48, 48]
+    assert np.all((uc.eps >= 0.02) & (uc.eps <= 0.10))
+    assert np.all((uc.sigma >= 2.5) & (uc.sigma <= 3.8))
+    chains = syn.config3_chains()
+    assert len(chains) == 64
+    assert sorted({round(c.box, 6) for c in chains}) == [25.6, 38.4, 51.2, 64.0]

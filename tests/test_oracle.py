@@ -1,0 +1,103 @@
+"""The CPU oracle against the reference's own known answer and its own
+internal identities.  These run on the CPU only."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import CALF20, GOLDEN
+from fastmc_gb300 import synthetic as syn
+
+
+def golden():
+    with open(os.path.join(GOLDEN, "golden.json")) as f:
+        return json.load(f)
+
+
+def test_calf20_electrostatic_kat(oracle_lib):
+    """Initial electrostatic energy of the reference test system equals the
+    value the reference prints (run_test.py:39, gcmc.f:585-586)."""
+    o = oracle_lib.Oracle(CALF20)
+    e = o.setup_energies()
+    g = golden()
+    assert abs(e["ecoul"] - g["calf20_electrostatic_energy_kcal"]) < g["tolerance_abs"]
+    # the k-machinery the KAT pins (utility_pack.f:412-423, ewald.f:91-94)
+    assert (e["kmax1"], e["kmax2"], e["kmax3"]) == (9, 8, 8)
+    assert e["newld"] == 870
+    assert abs(e["alpha"] - 0.2539648) < 1e-6
+
+
+def test_duni_reproducible_and_uniform(oracle_lib):
+    a = oracle_lib.duni_sequence(12345, 20000)
+    b = oracle_lib.duni_sequence(12345, 20000)
+    c = oracle_lib.duni_sequence(54321, 20000)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+    assert a.min() >= 0.0 and a.max() < 1.0
+    assert abs(a.mean() - 0.5) < 0.01
+    # REAL*4 values: every draw is a float32 number
+    assert np.array_equal(a.astype(np.float32).astype(np.float64), a)
+
+
+@pytest.fixture(scope="module")
+def small_dir(inputs_dir):
+    return inputs_dir(syn.small_test_spec(seed=3, kmax=5, pressure_bar=1.0, create=12), "orc_small")
+
+
+def test_insert_delete_reciprocity(oracle_lib, small_dir):
+    """Deleting a just-inserted molecule costs exactly its insertion energy:
+    deletion's estep is the molecule's own energy (energy_eval receives
+    -estep, gcmc.f:1795) and its delE is the negative (mc_moves.f:477).
+    This checks the structure-factor and tail bookkeeping of accept_move."""
+    o = oracle_lib.Oracle(small_dir)
+    o.seed(11)
+    o.create_molecules(1, 12)
+    rng = np.random.default_rng(5)
+    tmpl = np.array([[0, 0, 0], [0, 0, 1.16], [0, 0, -1.16]])
+    done = 0
+    for _ in range(20000):
+        c = rng.uniform(0, 25.6, 3)
+        xyz = tmpl + c
+        ins = o.insertion_energy(1, xyz)
+        if ins["overlap"]:
+            continue
+        o.apply_move(1, 1, 0, xyz, True)
+        n = o.nummols(o.locguest(1))
+        dele = o.deletion_energy(1, n)
+        assert math.isclose(ins["estep"], dele["estep"], rel_tol=1e-9, abs_tol=1e-9)
+        mol = o.locguest(1)
+        assert math.isclose(ins["delE"][mol - 1], -dele["delE"][mol - 1], rel_tol=1e-9, abs_tol=1e-9)
+        o.apply_move(2, 1, n, None, True)
+        done += 1
+        if done == 5:
+            break
+    assert done >= 3
+
+
+def test_chain_deterministic(oracle_lib, small_dir):
+    runs = []
+    for _ in range(2):
+        o = oracle_lib.Oracle(small_dir)
+        o.seed(77)
+        o.create_molecules(1, 12)
+        logs = o.run(300)
+        runs.append([(l.move, l.choice, l.overlap, l.accepted, l.estep) for l in logs])
+    assert runs[0] == runs[1]
+    kinds = {r[0] for r in runs[0]}
+    assert {1, 2, 3, 5} <= kinds
+
+
+def test_move_mix_and_counts(oracle_lib, small_dir):
+    o = oracle_lib.Oracle(small_dir)
+    o.seed(5)
+    o.create_molecules(1, 12)
+    logs = o.run(400)
+    st = o.stats(1)
+    ins = sum(1 for l in logs if l.move == 1)
+    dele = sum(1 for l in logs if l.move == 2)
+    assert st[10] == ins and st[12] == dele
+    assert st[11] == sum(1 for l in logs if l.move == 1 and l.accepted)
+    # an overlapped insertion never draws the Metropolis number (gcmc.f:1730-1736)
+    assert all(l.rande == -1.0 for l in logs if l.move == 1 and l.overlap)
