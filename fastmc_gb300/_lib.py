@@ -33,7 +33,8 @@ class SystemInfo(C.Structure):
                 ("drewd", C.c_double), ("cell", C.c_double * 9),
                 ("fugacity", C.c_double * MAX_GUEST_TYPES),
                 ("ewald3en", C.c_double * MAX_GUEST_TYPES),
-                ("mcsteps", C.c_int), ("eqsteps", C.c_int), ("nwindsteps", C.c_int)]
+                ("mcsteps", C.c_int), ("eqsteps", C.c_int), ("nwindsteps", C.c_int),
+                ("overlap", C.c_double)]
 
 
 class MoveResult(C.Structure):

@@ -20,7 +20,8 @@ LIB = os.path.join(OUT_DIR, "libfastmc_gb300.so")
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [GENCODE, "-std=c++17", "-O3", "-lineinfo", "-diag-suppress", "1444",
-              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-Xcompiler", "-Wno-deprecated-declarations"]
 SOURCES = ["engine.cu", "host_setup.cpp"]
 
 

@@ -63,6 +63,16 @@ struct GuestType {
   int type[kMaxS];         // atom type 1..ntpatm
   int frz[kMaxS];
   double ewald3en;
+  // constants of the energy expressions of this guest type
+  double chgtmp;           // sum of site charges
+  double engsic0;          // self-interaction -r4pie0/epsq*alpha*sum(q^2)/sqrt(pi)
+  double qfa, qfb;         // charged-system term qfix = qfa*sumchg + qfb
+  double qfm;              // qfixmol(m) = qfm * chgsum_mol(m)
+  double rmass;            // 1 / molecular mass (com)
+  // LJ long-range tail of one molecule (gstlrcorrect) as a linear function
+  // of the guest counts: insert lrcA + sum_g2 N_g2 lrcB[g2];
+  // delete -lrcA + 2 lrcC - sum_g2 N_g2 lrcB[g2]; framework part lrcA - lrcC
+  double lrcA, lrcC, lrcB[kMaxG];
   double rmax;             // max site distance from the template centre
   double delr;             // displacement size / list skin
   double disp_ratio, tran_ratio, rota_ratio;
@@ -74,7 +84,7 @@ struct SysDev {
   // cell
   int imcon;
   double cell[9], rcell[9], box[3];
-  double volm, statvolm, temp, beta, engunit, epsq, alpha;
+  double volm, statvolm, temp, beta, engunit, rengunit, epsq, alpha;
   double rcut, rc2, overlap_sq, surftol;
   double sumchg0;          // system charge without guests
   double chgsum_fw;        // framework charge (chgsum_mol of the framework)
@@ -89,6 +99,11 @@ struct SysDev {
   int use_cells;
   int nc[3];
   double csz[3];
+  double rcsz[3];          // 1 / csz
+  double rbox[3];          // 1 / L, the reference's aaa = 1/cell (images)
+  float boxh[3], boxl[3];  // L as a float hi/lo pair
+  float rboxf[3], rcszf[3], cszf[3];
+  float overlap_sqf, rc2f, rdrewdf, rdlrpotf;
   const int *cell_start;   // [nc0*nc1*nc2+1], z fastest
   // tables
   int mxegrd;
@@ -100,6 +115,7 @@ struct SysDev {
   int tabstride;           // mxegrd+3
   const int *pairtab;      // [(ntpatm+1)^2] -> table row or -1
   const double *sig2;      // [(ntpatm+1)^2] (surftol + sigma)^2
+  const float *sig2f;
   const double *steadd;    // [loc2 pair] tail constants
   const int *numtyp_fw, *numfrz_fw;   // [ntpatm+1]
   // k-space
@@ -108,6 +124,7 @@ struct SysDev {
   const double *akk;
   const float *akk32;
   const double2 *skfw;     // framework S(k)
+  const float4 *skfw_df;   // framework S(k) as FP32 hi/lo pairs (re_hi, im_hi, re_lo, im_lo)
   double krecip;           // 2 * rvolm * r4pie0 / epsq
   // guests
   GuestType g[kMaxG];
@@ -155,13 +172,14 @@ struct ChainArrays {
   float4 *glo;      // [chain][g][slot][site] lo mirror
   int *ord;         // [chain][g][cap] slot ids in molecule order
   int *freel;       // [chain][g][cap]
-  double2 *sk;      // [chain][g][nkmax] guest S(k)
-  float2 *sk32;     // [chain][maxmls+1][nkmax]: per mol type and total (FP32 mirror)
+  double2 *sk;      // [chain][g][nkmax] guest S(k), FP64 path
+  float4 *skdf;     // [chain][g][nkmax] guest S(k) as FP32 hi/lo pairs, FP32 path
   double2 *snew;    // [chain][nkmax] scratch s(k) of the evaluated position
   double2 *sold;    // [chain][nkmax] scratch s(k) of the old position
+  float2 *snew32;   // FP32 path: the same scratch in FP32
+  float2 *sold32;
   int cap;          // molecules per guest type
   int nkmax;
-  int nmt;          // rows of sk32 per chain (max maxmls over systems + 1)
 };
 
 // Description of one trial move (shared memory; copied to global between
@@ -199,7 +217,7 @@ struct Acc {  // per-position partial sums
 // ----------------------------------------------------------- MZT generator
 // duni (utility_pack.f:2768-2857): REAL*4 lagged subtract-with-borrow plus
 // a Weyl term; bit-exact because only float add/sub/compare are used.
-__device__ __forceinline__ double duni_next(ChainHdr &h) {
+__device__ __forceinline__ float duni_f(ChainHdr &h) {
   float uni = h.u[h.ir - 1] - h.u[h.jr - 1];
   if (uni < 0.0f) uni = uni + 1.0f;
   h.u[h.ir - 1] = uni;
@@ -211,7 +229,14 @@ __device__ __forceinline__ double duni_next(ChainHdr &h) {
   if (h.c < 0.0f) h.c = h.c + h.cm;
   uni = uni - h.c;
   if (uni < 0.0f) uni = uni + 1.0f;
-  return double(uni);
+  return uni;
+}
+
+// floor(u * n) + 1 for a generator value u (a multiple of 2^-24), exactly
+// as the reference's floor(duni()*n)+1 in FP64 (gcmc.f:1782, 1870).
+__device__ __forceinline__ int pick1(float u, int n) {
+  unsigned long long m = (unsigned long long)(u * 16777216.0f);
+  return (int)((m * (unsigned long long)n) >> 24) + 1;
 }
 
 // Initialisation from the clock values the reference reads
@@ -382,6 +407,116 @@ __device__ inline int block_scan(int v, int &excl, int *scratch) {
   excl = base + x - v;
   __syncthreads();
   return tot;
+}
+
+// ------------------------------------------- error-free FP32 arithmetic
+// A value held as an unevaluated sum hi + lo of two floats (about 48
+// significant bits).  Used for the FP32 path's accumulators and for its
+// running structure factor, so no FP64 instruction is needed there.
+__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+struct DF {
+  float hi, lo;
+  __device__ __forceinline__ void add(float x) {
+    float s, e;
+    two_sum_f(hi, x, s, e);
+    hi = s;
+    lo += e;
+  }
+  __device__ __forceinline__ void add(DF o) {
+    float s, e;
+    two_sum_f(hi, o.hi, s, e);
+    e += lo + o.lo;
+    hi = s + e;
+    lo = e - (hi - s);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <bool F32>
+struct AccT;
+template <>
+struct AccT<false> {
+  double v;
+  __device__ __forceinline__ void zero() { v = 0.0; }
+  __device__ __forceinline__ void add(double x) { v += x; }
+};
+template <>
+struct AccT<true> {
+  DF v;
+  __device__ __forceinline__ void zero() { v.hi = v.lo = 0.f; }
+  __device__ __forceinline__ void add(float x) { v.add(x); }
+};
+
+// Per-position partial sums of one thread.
+template <bool F32>
+struct PosAcc {
+  AccT<F32> e2fw, vdwfw, recip, mixfw;
+  AccT<F32> e2g[kMaxG], vdwg[kMaxG], mixg[kMaxG];
+  __device__ void zero() {
+    e2fw.zero();
+    vdwfw.zero();
+    recip.zero();
+    mixfw.zero();
+    for (int g = 0; g < kMaxG; ++g) {
+      e2g[g].zero();
+      vdwg[g].zero();
+      mixg[g].zero();
+    }
+  }
+};
+
+// Fixed-order block reduction of n accumulators per thread (n <= 32).
+// out[i] receives the block total as a double (valid after the call).
+__device__ inline void block_reduce(AccT<false> *v, int n, double *scratch, double *out) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = 0; i < n; ++i) {
+    double x = warp_sum(v[i].v);
+    if (lane == 0) scratch[w * 32 + i] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < n) {
+    double s = 0.0;
+    for (int k = 0; k < kWarps; ++k) s += scratch[k * 32 + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+__device__ inline void block_reduce(AccT<true> *v, int n, double *scratch, double *out) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float *sc = reinterpret_cast<float *>(scratch);
+  for (int i = 0; i < n; ++i) {
+    DF x = v[i].v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      DF y;
+      y.hi = __shfl_xor_sync(0xffffffffu, x.hi, o);
+      y.lo = __shfl_xor_sync(0xffffffffu, x.lo, o);
+      x.add(y);
+    }
+    if (lane == 0) {
+      sc[2 * (w * 32 + i)] = x.hi;
+      sc[2 * (w * 32 + i) + 1] = x.lo;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < n) {
+    DF s;
+    s.hi = s.lo = 0.f;
+    for (int k = 0; k < kWarps; ++k) {
+      DF y;
+      y.hi = sc[2 * (k * 32 + threadIdx.x)];
+      y.lo = sc[2 * (k * 32 + threadIdx.x) + 1];
+      s.add(y);
+    }
+    out[threadIdx.x] = s.value();
+  }
+  __syncthreads();
 }
 
 }  // namespace fmcdev

@@ -11,7 +11,12 @@
 //     interpolation (FP64 path) or the same quadratic written as
 //     A + p(B + pC) with FP64-built FP32 coefficients (FP32 path);
 //   ewald1_guest (ewald.f:32-352): per-k structure factor of the guest,
-//     its energy against S(k) and the per-molecule-type mixing terms.
+//     its energy against S(k) and the per-molecule-type mixing terms
+//     (engine.cuh).
+//
+// The FP32 path keeps distances accurate to about one FP32 rounding of r:
+// coordinates are float hi/lo pairs and periodic shifts are applied with
+// error-free sums, so no FP64 instruction runs per pair.
 #pragma once
 
 #include "device_core.cuh"
@@ -26,12 +31,17 @@ struct EvalSmem {
   // power tables e^{i 2 pi j s_d}: [pos][site][axis][j]
   double2 pw64[F32 ? 1 : 2][F32 ? 1 : kMaxS][3][F32 ? 1 : kMaxKm];
   float2 pw32[F32 ? 2 : 1][F32 ? kMaxS : 1][3][F32 ? kMaxKm : 1];
+  float fhi[2][kMaxS][3];   // fractional coordinates as float hi/lo pairs
+  float flo[2][kMaxS][3];
+  float cen[2][3];          // centre and bounding radius of each position
+  float rmx[2];
   int seg_start[kMaxSeg];
   int seg_pref[kMaxSeg + 1];
   int seg_shift[kMaxSeg];
   int nslots;
   int red_i[kWarps + 1];
-  double red[kWarps * 48 + 48];
+  double red[kWarps * 32];
+  double out[64];
 };
 
 // -------------------------------------------------------------- pair terms
@@ -70,16 +80,16 @@ __device__ __forceinline__ float interp32(const float4 *tab, float r, float rd,
 struct SiteInfo {
   double q;      // site charge
   double chgea;  // q / epsq * r4pie0
+  float chgeaf;
+  float qf;
   int type;
 };
 
-// One site-atom pair.  Adds the erfc and van der Waals terms when r < rc,
-// sets the overlap and surface flags like surface_check.
-template <bool F32>
-__device__ __forceinline__ void pair_term64(const SysDev &S, const SiteInfo &si,
-                                            double qb, int tb, int frozen_b,
-                                            double r2, double &e2, double &vdw,
-                                            int &ov, int &sf, int &st) {
+// One site-atom pair: erfc and van der Waals terms when r < rc, overlap and
+// surface flags like surface_check.
+__device__ __forceinline__ void pair_term64(const SysDev &S, const SiteInfo &si, double qb,
+                                            int tb, int frozen_b, double r2, double &e2,
+                                            double &vdw, int &ov, int &sf, int &st) {
   int pi = si.type * (S.ntpatm + 1) + tb;
   if (r2 < S.overlap_sq) ov = 1;
   if (frozen_b && r2 < __ldg(S.sig2 + pi)) sf = 1;
@@ -92,36 +102,47 @@ __device__ __forceinline__ void pair_term64(const SysDev &S, const SiteInfo &si,
   }
 }
 
-__device__ __forceinline__ void pair_term32(const SysDev &S, const SiteInfo &si,
-                                            float chgprd, int tb, int frozen_b,
-                                            float r2, float &e2, float &vdw,
-                                            int &ov, int &sf, int &st) {
+__device__ __forceinline__ void pair_term32(const SysDev &S, const SiteInfo &si, float chgprd,
+                                            int tb, int frozen_b, float r2, float &e2,
+                                            float &vdw, int &ov, int &sf, int &st) {
   int pi = si.type * (S.ntpatm + 1) + tb;
-  if (r2 < (float)S.overlap_sq) ov = 1;
-  if (frozen_b && r2 < (float)__ldg(S.sig2 + pi)) sf = 1;
-  if (r2 < (float)S.rc2) {
+  if (r2 < S.overlap_sqf) ov = 1;
+  if (frozen_b && r2 < __ldg(S.sig2f + pi)) sf = 1;
+  if (r2 < S.rc2f) {
     float r = sqrtf(r2);
-    if (fabsf(chgprd) > 1.0e-10f)
-      e2 = fmaf(interp32(S.ercq, r, (float)S.rdrewd, S.mxegrd, st), chgprd, e2);
+    if (fabsf(chgprd) > 1.0e-10f) e2 = fmaf(interp32(S.ercq, r, S.rdrewdf, S.mxegrd, st), chgprd, e2);
     int k = __ldg(S.pairtab + pi);
-    if (k >= 0) vdw += interp32(S.vvvq + (size_t)k * S.tabstride, r, (float)S.rdlrpot, S.mxegrd, st);
+    if (k >= 0) vdw += interp32(S.vvvq + (size_t)k * S.tabstride, r, S.rdlrpotf, S.mxegrd, st);
   }
 }
 
-// Error-free sum a + b = s + e.
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = a + b;
-  float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
+// Minimum-image difference p - q of two points given as float hi/lo pairs
+// (one axis).  The image shift is applied with an error-free sum so the
+// result keeps the relative accuracy of a single FP32 subtraction.
+__device__ __forceinline__ float mi_diff32(float ph, float pl, float qh, float ql, float Lh,
+                                           float Ll, float rL) {
+  float dh = ph - qh;
+  float k = rintf(dh * rL);
+  if (k != 0.0f) {
+    float h, e;
+    two_sum_f(ph, -k * Lh, h, e);
+    return (h - qh) + ((pl - ql) + (e - k * Ll));
+  }
+  return dh + (pl - ql);
+}
+
+__device__ __forceinline__ int image_of(int ic, int n) {
+  return (ic >= 0) ? ic / n : -((-ic + n - 1) / n);
 }
 
 // ---------------------------------------------------- framework neighbours
-// Build the list of framework atom segments (runs of cells along z in one
-// column and one periodic image) that cover the sphere of radius R around
-// c.  Slots with zero atoms are allowed; seg_pref is the prefix over slots.
+// List of framework atom segments (runs of cells along z in one column and
+// one periodic image) covering the sphere of radius R around c.  Slots with
+// zero atoms are allowed; seg_pref is the prefix over slots.  The geometry
+// is conservative (FP32 with a margin): it only selects candidates.
 template <bool F32>
-__device__ void build_segments(const SysDev &S, EvalSmem<F32> &sm, const double *c,
-                               double R, int &st) {
+__device__ void build_segments(const SysDev &S, EvalSmem<F32> &sm, const float *c, float R,
+                               int &st) {
   if (!S.use_cells) {
     if (threadIdx.x == 0) {
       sm.seg_start[0] = 0;
@@ -133,8 +154,9 @@ __device__ void build_segments(const SysDev &S, EvalSmem<F32> &sm, const double 
     __syncthreads();
     return;
   }
-  int ix0 = (int)floor((c[0] - R) / S.csz[0]), ix1 = (int)floor((c[0] + R) / S.csz[0]);
-  int iy0 = (int)floor((c[1] - R) / S.csz[1]), iy1 = (int)floor((c[1] + R) / S.csz[1]);
+  const float *cs = S.cszf, *rc = S.rcszf;
+  int ix0 = (int)floorf((c[0] - R) * rc[0]), ix1 = (int)floorf((c[0] + R) * rc[0]);
+  int iy0 = (int)floorf((c[1] - R) * rc[1]), iy1 = (int)floorf((c[1] + R) * rc[1]);
   int nx = ix1 - ix0 + 1, ny = iy1 - iy0 + 1;
   int ncol = nx * ny;
   const int kRuns = 4;
@@ -148,14 +170,14 @@ __device__ void build_segments(const SysDev &S, EvalSmem<F32> &sm, const double 
     __syncthreads();
     return;
   }
-  double R2 = R * R;
+  float R2 = R * R;
   for (int col = threadIdx.x; col < ncol; col += kThreads) {
     int ix = ix0 + col / ny, iy = iy0 + col % ny;
-    double xlo = ix * S.csz[0], xhi = xlo + S.csz[0];
-    double ylo = iy * S.csz[1], yhi = ylo + S.csz[1];
-    double dx = fmax(0.0, fmax(xlo - c[0], c[0] - xhi));
-    double dy = fmax(0.0, fmax(ylo - c[1], c[1] - yhi));
-    double d2 = dx * dx + dy * dy;
+    float xlo = ix * cs[0], xhi = xlo + cs[0];
+    float ylo = iy * cs[1], yhi = ylo + cs[1];
+    float dx = fmaxf(0.f, fmaxf(xlo - c[0], c[0] - xhi));
+    float dy = fmaxf(0.f, fmaxf(ylo - c[1], c[1] - yhi));
+    float d2 = dx * dx + dy * dy;
     int base = col * kRuns;
     for (int r = 0; r < kRuns; ++r) {
       sm.seg_start[base + r] = 0;
@@ -163,16 +185,15 @@ __device__ void build_segments(const SysDev &S, EvalSmem<F32> &sm, const double 
       sm.seg_pref[base + r] = 0;  // count for now
     }
     if (d2 > R2) continue;
-    double hz = sqrt(R2 - d2);
-    int iz0 = (int)floor((c[2] - hz) / S.csz[2]), iz1 = (int)floor((c[2] + hz) / S.csz[2]);
-    int imx = (ix >= 0) ? ix / S.nc[0] : -((-ix + S.nc[0] - 1) / S.nc[0]);
-    int imy = (iy >= 0) ? iy / S.nc[1] : -((-iy + S.nc[1] - 1) / S.nc[1]);
+    float hz = sqrtf(R2 - d2);
+    int iz0 = (int)floorf((c[2] - hz) * rc[2]), iz1 = (int)floorf((c[2] + hz) * rc[2]);
+    int imx = image_of(ix, S.nc[0]), imy = image_of(iy, S.nc[1]);
     int ixw = ix - imx * S.nc[0], iyw = iy - imy * S.nc[1];
     int colbase = (ixw * S.nc[1] + iyw) * S.nc[2];
     int r = 0;
     int iz = iz0;
     while (iz <= iz1) {
-      int imz = (iz >= 0) ? iz / S.nc[2] : -((-iz + S.nc[2] - 1) / S.nc[2]);
+      int imz = image_of(iz, S.nc[2]);
       int izw = iz - imz * S.nc[2];
       int run_end = min(iz1, (imz + 1) * S.nc[2] - 1);
       int izw_end = run_end - imz * S.nc[2];
@@ -211,7 +232,7 @@ __device__ void build_segments(const SysDev &S, EvalSmem<F32> &sm, const double 
 }
 
 __device__ __forceinline__ int find_slot(const int *pref, int n, int t) {
-  // largest s in [0, n) with pref[s] <= t and pref[s+1] > t
+  // largest s in [0, n) with pref[s] <= t
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
@@ -221,10 +242,10 @@ __device__ __forceinline__ int find_slot(const int *pref, int n, int t) {
   return lo;
 }
 
-// Scan the framework for position `pos` (ns sites) and accumulate into acc.
+// Scan the framework for position `pos` (ns sites).
 template <bool F32>
 __device__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos, int ns,
-                               const SiteInfo *si, Acc &acc, int &ov, int &sf,
+                               const SiteInfo *si, PosAcc<F32> &acc, int &ov, int &sf,
                                int &st) {
   int nslot = sm.nslots;
   int total = sm.seg_pref[nslot];
@@ -255,18 +276,15 @@ __device__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos, int 
           dz = c[2] * fx + c[5] * fy + c[8] * fz;
         }
         double r2 = dx * dx + dy * dy + dz * dz;
-        pair_term64<false>(S, si[k], A.w, tb, 1, r2, e2, vdw, ov, sf, st);
+        pair_term64(S, si[k], A.w, tb, 1, r2, e2, vdw, ov, sf, st);
       }
     }
-    acc.e2_fw += e2;
-    acc.vdw_fw += vdw;
+    acc.e2fw.add(e2);
+    acc.vdwfw.add(vdw);
   } else {
     float e2 = 0.0f, vdw = 0.0f;
-    double e2d = 0.0, vdwd = 0.0;
     int cnt = 0;
-    const float Lh[3] = {(float)S.box[0], (float)S.box[1], (float)S.box[2]};
-    const float Ll[3] = {(float)(S.box[0] - (double)Lh[0]), (float)(S.box[1] - (double)Lh[1]),
-                         (float)(S.box[2] - (double)Lh[2])};
+    const float *Lh = S.boxh, *Ll = S.boxl;
     for (int t = threadIdx.x; t < total; t += kThreads) {
       int s = find_slot(sm.seg_pref, nslot, t);
       int a = sm.seg_start[s] + (t - sm.seg_pref[s]);
@@ -280,7 +298,7 @@ __device__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos, int 
       for (int d = 0; d < 3; ++d) {
         if (im[d] != 0) {
           float h, e;
-          two_sum(ah[d], float(im[d]) * Lh[d], h, e);
+          two_sum_f(ah[d], float(im[d]) * Lh[d], h, e);
           ah[d] = h;
           al[d] = al[d] + (e + float(im[d]) * Ll[d]);
         }
@@ -290,95 +308,139 @@ __device__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos, int 
         float dy = (sm.phi[pos][k][1] - ah[1]) + (sm.plo[pos][k][1] - al[1]);
         float dz = (sm.phi[pos][k][2] - ah[2]) + (sm.plo[pos][k][2] - al[2]);
         float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        float chgprd = (float)si[k].chgea * H.w;
-        pair_term32(S, si[k], chgprd, tb, 1, r2, e2, vdw, ov, sf, st);
+        pair_term32(S, si[k], si[k].chgeaf * H.w, tb, 1, r2, e2, vdw, ov, sf, st);
       }
       if (++cnt == 8) {
-        e2d += e2;
-        vdwd += vdw;
+        acc.e2fw.add(e2);
+        acc.vdwfw.add(vdw);
         e2 = vdw = 0.0f;
         cnt = 0;
       }
     }
-    acc.e2_fw += e2d + (double)e2;
-    acc.vdw_fw += vdwd + (double)vdw;
+    acc.e2fw.add(e2);
+    acc.vdwfw.add(vdw);
   }
 }
 
 // Guest-guest part: every molecule of every guest type except the moving
-// one (the reference's ind exclusion, utility_pack.f:3736-3741).
+// one (the reference's ind exclusion, utility_pack.f:3736-3741).  Minimum
+// image per site pair, as images() does for each list entry.
 template <bool F32>
 __device__ void scan_guests(const SysDev &S, const ChainHdr &H, const ChainArrays &CA,
                             int chain, EvalSmem<F32> &sm, int pos, int ns, int self_g,
-                            int self_slot, double rmax_self, const SiteInfo *si,
-                            Acc &acc, int &ov, int &sf, int &st) {
+                            int self_slot, float rmax_self, const SiteInfo *si,
+                            PosAcc<F32> &acc, int &ov, int &sf, int &st) {
   for (int g2 = 0; g2 < S.ntpguest; ++g2) {
     const GuestType &G2 = S.g[g2];
     int n2 = H.nummols[g2];
     const int *ord = CA.ord + ((size_t)chain * kMaxG + g2) * CA.cap;
-    double pre = S.rcut + 2.0 * rmax_self + 2.0 * G2.rmax + 0.01;
-    double pre2 = pre * pre;
-    double e2 = 0.0, vdw = 0.0;
-    for (int i = threadIdx.x; i < n2; i += kThreads) {
-      int slot = ord[i];
-      if (g2 == self_g && slot == self_slot) continue;
-      size_t base = (((size_t)chain * kMaxG + g2) * CA.cap + slot) * kMaxS;
-      // prefilter on site 0 - site 0 (minimum image)
-      const double *q0 = CA.gpos + base * 3;
-      double dx = sm.p64[pos][0][0] - q0[0], dy = sm.p64[pos][0][1] - q0[1],
-             dz = sm.p64[pos][0][2] - q0[2];
-      if (S.use_cells) {
-        dx -= S.box[0] * round(dx / S.box[0]);
-        dy -= S.box[1] * round(dy / S.box[1]);
-        dz -= S.box[2] * round(dz / S.box[2]);
-        if (dx * dx + dy * dy + dz * dz > pre2) continue;
-      }
-      for (int b = 0; b < G2.ns; ++b) {
-        const double *qb = CA.gpos + (base + b) * 3;
-        double qq = G2.q[b];
-        int tb = G2.type[b];
-        for (int k = 0; k < ns; ++k) {
-          double ddx = sm.p64[pos][k][0] - qb[0], ddy = sm.p64[pos][k][1] - qb[1],
-                 ddz = sm.p64[pos][k][2] - qb[2];
-          if (S.use_cells) {
-            ddx -= S.box[0] * round(ddx / S.box[0]);
-            ddy -= S.box[1] * round(ddy / S.box[1]);
-            ddz -= S.box[2] * round(ddz / S.box[2]);
-          } else {
-            const double *r = S.rcell, *c = S.cell;
-            double fx = r[0] * ddx + r[3] * ddy + r[6] * ddz;
-            double fy = r[1] * ddx + r[4] * ddy + r[7] * ddz;
-            double fz = r[2] * ddx + r[5] * ddy + r[8] * ddz;
-            fx -= round(fx);
-            fy -= round(fy);
-            fz -= round(fz);
-            ddx = c[0] * fx + c[3] * fy + c[6] * fz;
-            ddy = c[1] * fx + c[4] * fy + c[7] * fz;
-            ddz = c[2] * fx + c[5] * fy + c[8] * fz;
+    float pre = (float)S.rcut + 2.0f * rmax_self + 2.0f * (float)G2.rmax + 0.01f;
+    if constexpr (F32) {
+      const float4 *gh = CA.ghi + ((size_t)chain * kMaxG + g2) * CA.cap * kMaxS;
+      const float4 *gl = CA.glo + ((size_t)chain * kMaxG + g2) * CA.cap * kMaxS;
+      float pre2 = pre * pre;
+      for (int i = threadIdx.x; i < n2; i += kThreads) {
+        int slot = ord[i];
+        if (g2 == self_g && slot == self_slot) continue;
+        float4 q0 = gh[(size_t)slot * kMaxS];
+        float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y,
+              dz = sm.phi[pos][0][2] - q0.z;
+        dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
+        dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
+        dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+        float e2 = 0.f, vdw = 0.f;
+        for (int b = 0; b < G2.ns; ++b) {
+          float4 qh = gh[(size_t)slot * kMaxS + b];
+          float4 ql = gl[(size_t)slot * kMaxS + b];
+          int tb = G2.type[b];
+          for (int k = 0; k < ns; ++k) {
+            float ex = mi_diff32(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
+                                 S.boxl[0], S.rboxf[0]);
+            float ey = mi_diff32(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
+                                 S.boxl[1], S.rboxf[1]);
+            float ez = mi_diff32(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2],
+                                 S.boxl[2], S.rboxf[2]);
+            float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+            pair_term32(S, si[k], si[k].chgeaf * qh.w, tb, G2.frz[b], r2, e2, vdw, ov, sf, st);
           }
-          double r2 = ddx * ddx + ddy * ddy + ddz * ddz;
-          if constexpr (!F32) {
-            pair_term64<false>(S, si[k], qq, tb, G2.frz[b], r2, e2, vdw, ov, sf, st);
-          } else {
-            float fe2 = 0.0f, fv = 0.0f;
-            pair_term32(S, si[k], (float)(si[k].chgea * qq), tb, G2.frz[b], (float)r2,
-                        fe2, fv, ov, sf, st);
-            e2 += fe2;
-            vdw += fv;
+        }
+        acc.e2g[g2].add(e2);
+        acc.vdwg[g2].add(vdw);
+      }
+    } else {
+      double pre2 = (double)pre * (double)pre;
+      double e2 = 0.0, vdw = 0.0;
+      for (int i = threadIdx.x; i < n2; i += kThreads) {
+        int slot = ord[i];
+        if (g2 == self_g && slot == self_slot) continue;
+        size_t base = (((size_t)chain * kMaxG + g2) * CA.cap + slot) * kMaxS;
+        const double *q0 = CA.gpos + base * 3;
+        if (S.use_cells) {  // prefilter on site 0 - site 0
+          double dx = sm.p64[pos][0][0] - q0[0], dy = sm.p64[pos][0][1] - q0[1],
+                 dz = sm.p64[pos][0][2] - q0[2];
+          dx -= S.box[0] * round(S.rbox[0] * dx);
+          dy -= S.box[1] * round(S.rbox[1] * dy);
+          dz -= S.box[2] * round(S.rbox[2] * dz);
+          if (dx * dx + dy * dy + dz * dz > pre2) continue;
+        }
+        for (int b = 0; b < G2.ns; ++b) {
+          const double *qb = CA.gpos + (base + b) * 3;
+          double qq = G2.q[b];
+          int tb = G2.type[b];
+          for (int k = 0; k < ns; ++k) {
+            double ddx = sm.p64[pos][k][0] - qb[0], ddy = sm.p64[pos][k][1] - qb[1],
+                   ddz = sm.p64[pos][k][2] - qb[2];
+            if (S.use_cells) {
+              ddx -= S.box[0] * round(S.rbox[0] * ddx);
+              ddy -= S.box[1] * round(S.rbox[1] * ddy);
+              ddz -= S.box[2] * round(S.rbox[2] * ddz);
+            } else {
+              const double *r = S.rcell, *c = S.cell;
+              double fx = r[0] * ddx + r[3] * ddy + r[6] * ddz;
+              double fy = r[1] * ddx + r[4] * ddy + r[7] * ddz;
+              double fz = r[2] * ddx + r[5] * ddy + r[8] * ddz;
+              fx -= round(fx);
+              fy -= round(fy);
+              fz -= round(fz);
+              ddx = c[0] * fx + c[3] * fy + c[6] * fz;
+              ddy = c[1] * fx + c[4] * fy + c[7] * fz;
+              ddz = c[2] * fx + c[5] * fy + c[8] * fz;
+            }
+            double r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            pair_term64(S, si[k], qq, tb, G2.frz[b], r2, e2, vdw, ov, sf, st);
           }
         }
       }
+      acc.e2g[g2].add(e2);
+      acc.vdwg[g2].add(vdw);
     }
-    acc.e2_g[g2] += e2;
-    acc.vdw_g[g2] += vdw;
   }
 }
 
 // ----------------------------------------------------------------- k-space
-// Power tables for npos positions of ns sites.
+// Power tables e^{i 2 pi j s_d} for npos positions of ns sites
+// (the first harmonics and recurrences of ewald.f:108-147, evaluated
+// directly for each power j).  FP64 path: sincospi of the reduced phase.
+// FP32 path: the fractional coordinate is split into a float hi/lo pair
+// and j*s is reduced exactly with an FMA before sincospif.
 template <bool F32>
 __device__ void build_powers(const SysDev &S, EvalSmem<F32> &sm, int npos, int ns) {
   int k1 = S.kmax[0], k2 = S.kmax[1], k3 = S.kmax[2];
+  if constexpr (F32) {
+    int nf = npos * ns * 3;
+    if (threadIdx.x < nf) {
+      int pos = threadIdx.x / (ns * 3), rem = threadIdx.x % (ns * 3), s = rem / 3, d = rem % 3;
+      const double *p = sm.p64[pos][s];
+      const double *r = S.rcell;
+      double f = r[d] * p[0] + r[3 + d] * p[1] + r[6 + d] * p[2];
+      f -= floor(f);
+      float h = (float)f;
+      sm.fhi[pos][s][d] = h;
+      sm.flo[pos][s][d] = (float)(f - (double)h);
+    }
+    __syncthreads();
+  }
   int per = k1 + k2 + k3 + 3;
   int total = npos * ns * per;
   for (int t = threadIdx.x; t < total; t += kThreads) {
@@ -395,25 +457,27 @@ __device__ void build_powers(const SysDev &S, EvalSmem<F32> &sm, int npos, int n
         d = 2;
       }
     }
-    const double *p = sm.p64[pos][s];
-    const double *r = S.rcell;
-    double f = r[d] * p[0] + r[3 + d] * p[1] + r[6 + d] * p[2];
-    double x = double(j) * f;
-    x -= rint(x);
     if constexpr (!F32) {
+      const double *p = sm.p64[pos][s];
+      const double *r = S.rcell;
+      double f = r[d] * p[0] + r[3 + d] * p[1] + r[6 + d] * p[2];
+      double x = double(j) * f;
+      x -= rint(x);
       double sn, cs;
       sincospi(2.0 * x, &sn, &cs);
       sm.pw64[pos][s][d][j] = make_double2(cs, sn);
     } else {
+      float fj = (float)j;
+      float ph = fj * sm.fhi[pos][s][d];
+      float pe = fmaf(fj, sm.fhi[pos][s][d], -ph);  // exact product error
+      float x = (ph - rintf(ph)) + fmaf(fj, sm.flo[pos][s][d], pe);
       float sn, cs;
-      sincospif((float)(2.0 * x), &sn, &cs);
+      sincospif(2.0f * x, &sn, &cs);
       sm.pw32[pos][s][d][j] = make_float2(cs, sn);
     }
   }
 }
 
-// e^{i k.r} for one site from the power tables, with the reference's sign
-// conventions for negative m and n (ewald.f:191-251).
 template <class T2>
 __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
   T2 r;

@@ -101,34 +101,6 @@ __device__ void block_copy(T *dst, const T *src) {
 }
 
 template <bool F32>
-__device__ void propose_insert(BlockShared<F32> &B, int g) {
-  SysDev &S = B.S;
-  ChainHdr &H = B.H;
-  MoveCtx &mc = B.mc;
-  const GuestType &G = S.g[g];
-  double ra = duni_next(H), rb = duni_next(H), rc = duni_next(H);
-  double r1 = duni_next(H), r2 = duni_next(H), r3 = duni_next(H), r4 = duni_next(H);
-  double cc[3];
-  cartesian(S, ra, rb, rc, cc);
-  for (int s = 0; s < G.ns; ++s)
-    for (int d = 0; d < 3; ++d) mc.pos[0][s][d] = G.tmpl[s][d];
-  double q[4], zero[3] = {0.0, 0.0, 0.0};
-  quaternion(r1, r2, r3, r4, 2.0 * kPi, q);
-  rotate_sites(mc.pos[0], G.ns, zero, q[0], q[1], q[2], q[3]);
-  for (int s = 0; s < G.ns; ++s)
-    for (int d = 0; d < 3; ++d) mc.pos[0][s][d] += cc[d];
-  mc.kind = 1;
-  mc.g = g;
-  mc.ns = G.ns;
-  mc.npos = 1;
-  mc.slot = -1;
-  mc.choice = 0;
-  mc.overlap = 0;
-  mc.accepted = 0;
-  mc.rande = -1.0;
-}
-
-template <bool F32>
 __global__ void __launch_bounds__(kThreads, 1)
     chain_kernel(const SysDev *__restrict__ systems, ChainHdr *hdrs, ChainArrays CA,
                  MoveCtx *gctx, LogRec *logs, int logcap, int nmoves, int mode) {
@@ -143,11 +115,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   int st = 0;
   if (mode == kModeMoves) {
     for (int it = 0; it < nmoves; ++it) {
-      if (threadIdx.x == 0) {
-        propose(B, CA, chain);
-        geometry(B, CA, chain);
-      }
-      __syncthreads();
+      propose(B, CA, chain, kPropMC, 0);
       int full = 0;
       if (B.mc.kind != 0) full = evaluate(B, CA, chain, st);
       if (threadIdx.x == 0) {
@@ -186,8 +154,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           st |= kStCapacity;
           break;
         }
-        if (threadIdx.x == 0) propose_insert(B, g);
-        __syncthreads();
+        propose(B, CA, chain, kPropInsert, g);
         evaluate(B, CA, chain, st);
         if (threadIdx.x == 0) B.mc.accepted = B.mc.overlap ? 0 : 1;
         __syncthreads();
@@ -197,11 +164,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else if (mode == kModeEval) {
-    if (threadIdx.x == 0) {
-      B.mc = gctx[chain];
-      geometry(B, CA, chain);
-    }
+    if (threadIdx.x == 0) B.mc = gctx[chain];
     __syncthreads();
+    propose(B, CA, chain, kPropExternal, 0);
     int full = 0;
     if (B.mc.kind != 0) full = evaluate(B, CA, chain, st);
     if (threadIdx.x == 0) {
@@ -263,7 +228,8 @@ struct DevSystem {
   DBuf<int> fwtype, cell_start, pairtab, numtyp_fw, numfrz_fw;
   DBuf<double> erc, vvv, sig2, steadd, akk;
   DBuf<float4> ercq, vvvq;
-  DBuf<float> akk32;
+  DBuf<float> akk32, sig2f;
+  DBuf<float4> skfw_df;
   DBuf<int4> klmn;
   DBuf<double2> skfw;
   std::vector<double2> skfw_host;
@@ -310,16 +276,25 @@ void build_device_system(const System &s, DevSystem &D) {
   d.box[0] = s.cell[0];
   d.box[1] = s.cell[4];
   d.box[2] = s.cell[8];
+  for (int dd = 0; dd < 3; ++dd) {
+    d.rbox[dd] = 1.0 / d.box[dd];
+    d.boxh[dd] = (float)d.box[dd];
+    d.boxl[dd] = (float)(d.box[dd] - (double)d.boxh[dd]);
+    d.rboxf[dd] = (float)d.rbox[dd];
+  }
   d.volm = s.volm;
   d.statvolm = s.statvolm;
   d.temp = s.temp;
   d.beta = s.beta;
   d.engunit = s.engunit;
+  d.rengunit = 1.0 / s.engunit;
   d.epsq = s.epsq;
   d.alpha = s.alpha;
   d.rcut = s.rcut;
   d.rc2 = s.rcut * s.rcut;
   d.overlap_sq = s.overlap_sq;
+  d.overlap_sqf = (float)s.overlap_sq;
+  d.rc2f = (float)(s.rcut * s.rcut);
   d.surftol = s.surftol;
   d.sumchg0 = s.sumchg;
   d.maxmls = s.maxmls;
@@ -359,6 +334,9 @@ void build_device_system(const System &s, DevSystem &D) {
     for (int dd = 0; dd < 3; ++dd) {
       d.nc[dd] = std::max(3, (int)std::floor(d.box[dd] / 2.5));
       d.csz[dd] = d.box[dd] / d.nc[dd];
+      d.rcsz[dd] = 1.0 / d.csz[dd];
+      d.rcszf[dd] = (float)d.rcsz[dd];
+      d.cszf[dd] = (float)d.csz[dd];
     }
     std::vector<int> cell(n);
     for (int i = 0; i < n; ++i) {
@@ -407,6 +385,8 @@ void build_device_system(const System &s, DevSystem &D) {
   d.tabstride = s.mxegrd + 3;
   d.rdrewd = 1.0 / s.drewd;
   d.rdlrpot = 1.0 / s.dlrpot;
+  d.rdrewdf = (float)d.rdrewd;
+  d.rdlrpotf = (float)d.rdlrpot;
   std::vector<double> erc(d.tabstride, 0.0);
   for (int i = 1; i <= s.mxegrd; ++i) erc[i] = s.erc[i];
   D.erc.upload(erc);
@@ -437,6 +417,9 @@ void build_device_system(const System &s, DevSystem &D) {
     }
   D.pairtab.upload(ptab);
   D.sig2.upload(sig2);
+  std::vector<float> sig2f(sig2.begin(), sig2.end());
+  D.sig2f.upload(sig2f);
+  d.sig2f = D.sig2f.p;
   D.steadd.upload(s.steadd);
   D.numtyp_fw.upload(s.numtyp_fw);
   D.numfrz_fw.upload(s.numfrz_fw);
@@ -471,6 +454,16 @@ void build_device_system(const System &s, DevSystem &D) {
   if (s.newld)
     FMC_CUDA(cudaMemcpy(D.skfw_host.data(), D.skfw.p, s.newld * sizeof(double2), cudaMemcpyDeviceToHost));
   d.skfw = D.skfw.p;
+  {
+    std::vector<float4> df(std::max(1, s.newld));
+    for (int k = 0; k < s.newld; ++k) {
+      double2 v = D.skfw_host[k];
+      float hx = (float)v.x, hy = (float)v.y;
+      df[k] = make_float4(hx, hy, (float)(v.x - (double)hx), (float)(v.y - (double)hy));
+    }
+    D.skfw_df.upload(df);
+    d.skfw_df = D.skfw_df.p;
+  }
   // guest types
   for (int g = 1; g <= s.ntpguest; ++g) {
     GuestType &G = d.g[g - 1];
@@ -499,6 +492,59 @@ void build_device_system(const System &s, DevSystem &D) {
     }
     G.rmax = rmax;
     G.ewald3en = s.ewald3en[G.mol];
+    double qs = 0.0, q2 = 0.0, mass = 0.0;
+    for (int i = 0; i < m.natoms; ++i) {
+      qs += m.chg[i];
+      q2 += m.chg[i] * m.chg[i];
+      mass += m.wght[i];
+    }
+    double r4 = kR4pie0 / s.epsq;
+    G.chgtmp = qs;
+    G.engsic0 = -r4 * s.alpha * q2 / kSqrPi;  // ewald.f:105
+    G.qfa = -(0.5 * kPi * r4) * (qs / s.alpha) / s.volm;  // ewald.f:317-318
+    G.qfb = -(0.5 * kPi * r4) * ((qs / s.alpha) * (qs / s.alpha)) / s.volm;
+    G.qfm = -(kPi * r4) * qs / (s.alpha * s.alpha * s.volm);  // ewald.f:336-337
+    G.rmass = 1.0 / mass;
+    // gstlrcorrect (vdw_terms.f:686-776) as a linear function of the
+    // guest counts: per unique type pair k = 2 pi / V * eadd(i,j).
+    {
+      std::vector<int> ntg(s.ntpatm + 1, 0), nfg(s.ntpatm + 1, 0);
+      for (int i = 0; i < m.natoms; ++i) {
+        ntg[m.ltp[i]]++;
+        if (m.frz[i]) nfg[m.ltp[i]]++;
+      }
+      double A = 0.0, Cc = 0.0, Bv[kMaxG] = {0, 0, 0, 0};
+      int iv = 0;
+      for (int i = 1; i <= s.ntpatm; ++i)
+        for (int j = 1; j <= i; ++j) {
+          ++iv;
+          double kk = 2.0 * kPi / s.volm * s.steadd[iv];
+          double na = ntg[i], nb = ntg[j], fa = nfg[i], fb = nfg[j];
+          double pfw = na * s.numtyp_fw[j] + nb * s.numtyp_fw[i] - fa * s.numfrz_fw[j] -
+                       fb * s.numfrz_fw[i];
+          double self = na * nb - fa * fb;
+          A += kk * (pfw + self);
+          Cc += kk * self;
+          for (int g2 = 1; g2 <= s.ntpguest; ++g2) {
+            const MolType &m2 = s.mol[s.locguest[g2]];
+            double t2i = 0, t2j = 0, f2i = 0, f2j = 0;
+            for (int q = 0; q < m2.natoms; ++q) {
+              if (m2.ltp[q] == i) {
+                t2i += 1;
+                if (m2.frz[q]) f2i += 1;
+              }
+              if (m2.ltp[q] == j) {
+                t2j += 1;
+                if (m2.frz[q]) f2j += 1;
+              }
+            }
+            Bv[g2 - 1] += kk * (na * t2j + nb * t2i - fa * f2j - fb * f2i);
+          }
+        }
+      G.lrcA = A;
+      G.lrcC = Cc;
+      for (int g2 = 0; g2 < kMaxG; ++g2) G.lrcB[g2] = Bv[g2];
+    }
     G.delr = s.delr[g];
     G.disp_ratio = s.disp_ratio[g];
     G.tran_ratio = s.tran_ratio[g];
@@ -561,7 +607,8 @@ struct Chains {
   DBuf<float4> ghi, glo;
   DBuf<int> ord, freel;
   DBuf<double2> sk, snew, sold;
-  DBuf<float2> sk32;
+  DBuf<float2> snew32, sold32;
+  DBuf<float4> skdf;
   DBuf<MoveCtx> ctx;
   DBuf<LogRec> logs;
   ChainArrays CA{};
@@ -652,7 +699,6 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   ChainArrays &CA = C.CA;
   CA.cap = cap;
   CA.nkmax = nkmax;
-  CA.nmt = maxmls + 1;
   size_t nsl = (size_t)nchains * kMaxG * cap * kMaxS;
   C.gpos.alloc(nsl * 3);
   C.gpos.zero();
@@ -670,22 +716,12 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   C.sold.alloc((size_t)nchains * nkmax);
   C.snew.zero();
   C.sold.zero();
-  C.sk32.alloc((size_t)nchains * (maxmls + 1) * nkmax);
-  // FP32 mirrors start from the framework S(k)
-  {
-    std::vector<float2> m((size_t)nchains * (maxmls + 1) * nkmax, make_float2(0.f, 0.f));
-    for (int c = 0; c < nchains; ++c) {
-      const DevSystem &D = *C.sys[hh[c].system];
-      const System &s = *D.host;
-      for (int k = 0; k < s.newld; ++k) {
-        double2 v = D.skfw_host[k];
-        float2 f = make_float2((float)v.x, (float)v.y);
-        m[((size_t)c * (maxmls + 1) + (s.fw_mol - 1)) * nkmax + k] = f;
-        m[((size_t)c * (maxmls + 1) + s.maxmls) * nkmax + k] = f;
-      }
-    }
-    FMC_CUDA(cudaMemcpy(C.sk32.p, m.data(), m.size() * sizeof(float2), cudaMemcpyHostToDevice));
-  }
+  C.snew32.alloc((size_t)nchains * nkmax);
+  C.sold32.alloc((size_t)nchains * nkmax);
+  C.snew32.zero();
+  C.sold32.zero();
+  C.skdf.alloc((size_t)nchains * kMaxG * nkmax);
+  C.skdf.zero();
   C.ctx.alloc(nchains);
   C.ctx.zero();
   C.logs.alloc(1);
@@ -695,9 +731,11 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   CA.ord = C.ord.p;
   CA.freel = C.freel.p;
   CA.sk = C.sk.p;
-  CA.sk32 = C.sk32.p;
+  CA.skdf = C.skdf.p;
   CA.snew = C.snew.p;
   CA.sold = C.sold.p;
+  CA.snew32 = C.snew32.p;
+  CA.sold32 = C.sold32.p;
   FMC_CUDA(cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking));
   FMC_CUDA(cudaEventCreate(&C.ev0));
   FMC_CUDA(cudaEventCreate(&C.ev1));
@@ -816,6 +854,7 @@ int fmc_system_get_info(const fmc_system *sys, fmc_system_info *info) {
     info->mcsteps = s.mcsteps;
     info->eqsteps = s.eqsteps;
     info->nwindsteps = s.nwindsteps;
+    info->overlap = std::sqrt(s.overlap_sq);
     return FMC_OK;
   });
 }
@@ -893,9 +932,18 @@ int fmc_full_ewald(fmc_plain *h, double *out4) {
         FMC_CUDA(cudaMemcpy(sg.data(), tmp.p, nk * sizeof(double2), cudaMemcpyDeviceToHost));
       }
       // reset the running S(k) of this guest type to the recomputed one
-      if (nk)
+      if (nk && C.precision == FMC_PREC_FP32) {
+        std::vector<float4> df(nk);
+        for (int k = 0; k < nk; ++k) {
+          float hx = (float)sg[k].x, hy = (float)sg[k].y;
+          df[k] = make_float4(hx, hy, (float)(sg[k].x - hx), (float)(sg[k].y - hy));
+        }
+        FMC_CUDA(cudaMemcpy(C.skdf.p + (size_t)g * C.CA.nkmax, df.data(), nk * sizeof(float4),
+                            cudaMemcpyHostToDevice));
+      } else if (nk) {
         FMC_CUDA(cudaMemcpy(C.sk.p + (size_t)g * C.CA.nkmax, sg.data(), nk * sizeof(double2),
                             cudaMemcpyHostToDevice));
+      }
       for (int k = 0; k < nk; ++k) {
         stot[k].x += sg[k].x;
         stot[k].y += sg[k].y;
@@ -1090,8 +1138,16 @@ static int chain_sk(const Chains &C, int chain, double *out, int cap) {
   int nk = s.newld, nm = s.maxmls + 1;
   if (cap < 2 * nm * nk) raise(FMC_ERR_CAPACITY, "output buffer too small for S(k)");
   std::vector<double2> g((size_t)kMaxG * C.CA.nkmax);
-  FMC_CUDA(cudaMemcpy(g.data(), C.sk.p + (size_t)chain * kMaxG * C.CA.nkmax,
-                      g.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+  if (C.precision == FMC_PREC_FP32) {
+    std::vector<float4> df(g.size());
+    FMC_CUDA(cudaMemcpy(df.data(), C.skdf.p + (size_t)chain * kMaxG * C.CA.nkmax,
+                        df.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < g.size(); ++i)
+      g[i] = make_double2((double)df[i].x + (double)df[i].z, (double)df[i].y + (double)df[i].w);
+  } else {
+    FMC_CUDA(cudaMemcpy(g.data(), C.sk.p + (size_t)chain * kMaxG * C.CA.nkmax,
+                        g.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+  }
   for (int k = 0; k < nk; ++k) {
     double tx = 0, ty = 0;
     for (int m = 0; m < nm; ++m) {

@@ -1,15 +1,24 @@
 // engine.cuh -- the GCMC move loop of one chain on one CTA.
 //
 // Phases of one main-loop iteration (gcmc.f:704-1164):
-//   propose  (thread 0)  guest and move choice, adaptive step sizes,
-//                        trial geometry from the MZT generator;
-//   evaluate (all)       overlap pre-check, pair scans, k-space, fixed-order
-//                        reductions, estep and delE as the reference forms
-//                        them (mc_moves.f:150-484, gcmc.f:2816-2901);
-//   decide   (thread 0)  energy_eval (utility_pack.f:3637-3693);
-//   commit   (all)       accept_move (mc_moves.f:485-621): S(k), molecule
-//                        order, coordinates, counters;
-//   stats    (thread 0)  production averages and windows (gcmc.f:1050-1128).
+//   propose  (warp 0)   lane 0 draws from the MZT generator and picks the
+//                       guest and the move (gcmc.f:806-900); the lanes of
+//                       warp 0 then build the trial geometry together
+//                       (random_ins / random_disp / random_rot / translate /
+//                       rotation, utility_pack.f:3161-3563);
+//   evaluate (all)      overlap pre-check, pair scans, k-space, fixed-order
+//                       reductions, estep and delE as the reference forms
+//                       them (mc_moves.f:150-484, gcmc.f:2816-2901);
+//   decide   (thread 0) energy_eval (utility_pack.f:3637-3693);
+//   commit   (all)      accept_move (mc_moves.f:485-621): S(k), molecule
+//                       order, coordinates, counters;
+//   stats    (thread 0) production averages and windows (gcmc.f:1050-1128).
+//
+// GB300 executes FP64 at a small fraction of its FP32 rate, so every phase
+// keeps FP64 instructions off the per-pair and per-k loops: positions are
+// FP64 (parity of the geometry), pair and k-space terms are FP32 on the FP32
+// path, and that path's sums and running S(k) are error-free FP32 hi/lo
+// pairs (about 48 significant bits).
 #pragma once
 
 #include "device_eval.cuh"
@@ -29,6 +38,9 @@ struct BlockShared {
   MoveCtx mc;
   EvalSmem<F32> ev;
   SiteInfo si[kMaxS];
+  float draws[8];
+  double geo[12];    // a, b, c, q1..q4, rotation angle, com/frac scratch
+  double vtmp[3];
   int flags[4];
 };
 
@@ -36,44 +48,13 @@ __device__ __forceinline__ size_t gslot_base(const ChainArrays &CA, int chain, i
   return (((size_t)chain * kMaxG + g) * CA.cap + slot) * kMaxS;
 }
 
-// ------------------------------------------------- per-guest LJ tail delta
-// gstlrcorrect (vdw_terms.f:686-776) from the chain's type counters.
-__device__ void gst_lrc(const SysDev &S, const ChainHdr &H, int g, bool lexisting,
-                        double &delrc, double *delrc_mol) {
+// gstlrcorrect (vdw_terms.f:686-776) from the host-built coefficients.
+__device__ __forceinline__ double lrc_delta(const SysDev &S, const ChainHdr &H, int g,
+                                            bool lexisting) {
   const GuestType &G = S.g[g];
-  int mol = G.mol;
-  double twopi = 2.0 * kPi;
-  int ntg[kMaxT + 1], nfg[kMaxT + 1];
-  for (int a = 0; a <= S.ntpatm; ++a) ntg[a] = nfg[a] = 0;
-  for (int s = 0; s < G.ns; ++s) {
-    ntg[G.type[s]]++;
-    if (G.frz[s]) nfg[G.type[s]]++;
-  }
-  delrc = 0.0;
-  for (int m = 0; m <= S.maxmls; ++m) delrc_mol[m] = 0.0;
-  int iv = 0;
-  double v2 = S.volm * S.volm;
-  for (int i = 1; i <= S.ntpatm; ++i)
-    for (int j = 1; j <= i; ++j) {
-      ++iv;
-      double eadd = S.steadd[iv];
-      double na = ntg[i], nb = ntg[j], fa = nfg[i], fb = nfg[j];
-      double den = na * double(H.numtyp[j]) + nb * double(H.numtyp[i]) -
-                   fa * double(H.numfrz[j]) - fb * double(H.numfrz[i]);
-      if (lexisting) den = -1.0 * den;
-      den = den + (na * nb - fa * fb);
-      delrc = delrc + S.volm * twopi * den / v2 * eadd;
-      for (int jt = 1; jt <= S.maxmls; ++jt) {
-        double nc = H.numtyp_mol[jt][j], nd = H.numtyp_mol[jt][i];
-        double fc = H.numfrz_mol[jt][j], fd = H.numfrz_mol[jt][i];
-        double sic = na * nc + nb * nd - fa * fc - fb * fd, self = 0.0;
-        if (jt == mol) {
-          self = na * nb - fa * fb;
-          if (lexisting) sic = -1.0 * sic;
-        }
-        delrc_mol[jt] += S.volm * eadd * (twopi * (sic + self) / v2);
-      }
-    }
+  double s = 0.0;
+  for (int g2 = 0; g2 < S.ntpguest; ++g2) s += double(H.nummols[g2]) * G.lrcB[g2];
+  return lexisting ? (-G.lrcA + 2.0 * G.lrcC - s) : (G.lrcA + s);
 }
 
 // energy_eval (utility_pack.f:3637-3693)
@@ -95,10 +76,14 @@ __device__ bool energy_eval(const SysDev &S, const ChainHdr &H, int g, double en
 }
 
 // ----------------------------------------------------------------- propose
-// Thread 0: one iteration's draws (gcmc.f:806-900, 1693-1870).  Returns
-// false if the chain has nothing to do this step.
+// Proposal modes.
+constexpr int kPropMC = 0;        // main loop: draw guest, move and geometry
+constexpr int kPropInsert = 1;    // create molecules: forced insertion of guest g
+constexpr int kPropExternal = 2;  // per-move ABI: move given by the host
+
+// Lane 0 of warp 0: move selection and draws (gcmc.f:806-900, 1693-1870).
 template <bool F32>
-__device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
+__device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   SysDev &S = B.S;
   ChainHdr &H = B.H;
   MoveCtx &mc = B.mc;
@@ -106,26 +91,27 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   if (H.gcmccount % S.minchk == 0)
     if (!H.production && S.eqsteps > 0 && H.gcmccount >= S.eqsteps) H.production = 1;
   int g = 0;
-  if (S.ntpguest > 1) g = (int)floor(duni_next(H) * S.ntpguest);
+  if (S.ntpguest > 1) g = pick1(duni_f(H), S.ntpguest) - 1;
   const GuestType &G = S.g[g];
   int nmols = H.nummols[g];
-  double randmov = duni_next(H);
+  float randmov = duni_f(H);
   int kind;
   if (randmov < G.mcinsf) kind = 1;
   else if (randmov < G.mcdelf) kind = 2;
   else if (randmov < G.mcdisf) kind = 3;
-  else if (randmov < G.mcjmpf) kind = 3;  // not reachable: refused at set-up
+  else if (randmov < G.mcjmpf) kind = 3;  // jump/swap are refused at set-up
   else if (randmov < G.mcswpf) kind = 3;
   else if (randmov < G.mctraf) kind = 4;
   else if (randmov < G.mcrotf) kind = 5;
   else kind = 3;
   // adaptive step sizes (gcmc.f:859-900)
   if (nmols >= 1 && H.disp_count[g] >= 1) {
-    double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
     if (H.disp_count[g] % 100 == 0) {
+      double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
       if (ratio > G.disp_ratio) H.delrdisp[g] *= 1.05;
       else if (H.delrdisp[g] > kDelrMin) H.delrdisp[g] *= 0.95;
     } else if (H.disp_count[g] % 50 == 0) {
+      double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
       if (ratio > G.disp_ratio) H.rotangle *= 1.05;
       else if (H.rotangle > kMinAngle) H.rotangle *= 0.95;
     }
@@ -144,147 +130,276 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   mc.kind = kind;
   mc.g = g;
   mc.ns = G.ns;
-  mc.rande = -1.0;
-  mc.estep = 0.0;
-  mc.overlap = 0;
-  mc.accepted = 0;
-  mc.surf_new = mc.surf_old = 0;
-  mc.npos = 1;
   mc.choice = 0;
   mc.slot = -1;
+  mc.npos = 1;
   if (kind == 1) {
     H.ins_count[g]++;
-    // random_ins (utility_pack.f:3220-3331)
-    double ra = duni_next(H), rb = duni_next(H), rc = duni_next(H);
-    double r1 = duni_next(H), r2 = duni_next(H), r3 = duni_next(H), r4 = duni_next(H);
-    double cc[3];
-    cartesian(S, ra, rb, rc, cc);
-    for (int s = 0; s < G.ns; ++s)
-      for (int d = 0; d < 3; ++d) mc.pos[0][s][d] = G.tmpl[s][d];
-    double q[4], zero[3] = {0.0, 0.0, 0.0};
-    quaternion(r1, r2, r3, r4, 2.0 * kPi, q);
-    rotate_sites(mc.pos[0], G.ns, zero, q[0], q[1], q[2], q[3]);
-    for (int s = 0; s < G.ns; ++s)
-      for (int d = 0; d < 3; ++d) mc.pos[0][s][d] += cc[d];
+    for (int i = 0; i < 7; ++i) B.draws[i] = duni_f(H);  // random_ins
   } else if (kind == 2) {
     H.del_count[g]++;
-    int choice = (int)floor(duni_next(H) * nmols) + 1;
-    mc.choice = choice;
+    mc.choice = pick1(duni_f(H), nmols);
   } else {
-    double a = 0, b = 0, c = 0, q[4] = {0, 0, 0, 0};
-    auto disp = [&](double dd) {
-      a = duni_next(H);
-      b = duni_next(H);
-      c = duni_next(H);
+    double a = 0.0, b = 0.0, c = 0.0;
+    B.draws[3] = -1.0f;  // no rotation unless drawn
+    if (kind != 5) {     // random_disp (utility_pack.f:3333-3357)
+      double dd = kind == 4 ? H.tran_delr[g] : H.delrdisp[g];
       double h = dd * 0.5;
-      a = (2.0 * a - 1.0) * h;
-      b = (2.0 * b - 1.0) * h;
-      c = (2.0 * c - 1.0) * h;
-    };
-    auto rot = [&](double ang) {
-      double r1 = duni_next(H), r2 = duni_next(H), r3 = duni_next(H), r4 = duni_next(H);
-      quaternion(r1, r2, r3, r4, ang, q);
-    };
-    if (kind == 4) {
-      H.tran_count[g]++;
-      disp(H.tran_delr[g]);
-    } else if (kind == 5) {
-      H.rota_count[g]++;
-      rot(H.rota_rotangle);
-    } else {
-      H.disp_count[g]++;
-      disp(H.delrdisp[g]);
-      rot(H.rotangle);
+      a = (2.0 * (double)duni_f(H) - 1.0) * h;
+      b = (2.0 * (double)duni_f(H) - 1.0) * h;
+      c = (2.0 * (double)duni_f(H) - 1.0) * h;
     }
-    int choice = (int)floor(duni_next(H) * nmols) + 1;
-    mc.choice = choice;
-    mc.pos[1][0][0] = a;  // stash shift and quaternion for geometry()
-    mc.pos[1][0][1] = b;
-    mc.pos[1][0][2] = c;
-    mc.pos[1][1][0] = q[0];
-    mc.pos[1][1][1] = q[1];
-    mc.pos[1][1][2] = q[2];
-    mc.pos[1][2][0] = q[3];
+    if (kind != 4) {  // random_rot (utility_pack.f:3526-3563)
+      for (int i = 3; i < 7; ++i) B.draws[i] = duni_f(H);
+      B.geo[7] = kind == 5 ? H.rota_rotangle : H.rotangle;
+      B.flags[2] = 0;
+    } else {
+      // "move translate" keeps q1..q4 = 0 (gcmc.f:1842), and rotation()
+      // with a zero quaternion applies Q = -I: the molecule is inverted
+      // through its centre of mass.  Reproduced as the reference does it.
+      B.geo[3] = B.geo[4] = B.geo[5] = B.geo[6] = 0.0;
+      B.draws[3] = 1.0f;
+      B.flags[2] = 1;
+    }
+    if (kind == 4) H.tran_count[g]++;
+    else if (kind == 5) H.rota_count[g]++;
+    else H.disp_count[g]++;
+    B.geo[0] = a;
+    B.geo[1] = b;
+    B.geo[2] = c;
+    mc.choice = pick1(duni_f(H), nmols);
+    mc.npos = 2;
   }
 }
 
-// Thread 0: molecule lookup and trial geometry for delete / displace
-// (get_guest utility_pack.f:3776-3807, translate + rotation gcmc.f:2873-2876).
+// Quaternion of random_ins / random_rot from four draws and an angle:
+// theta = r1 * angle, axis (2 r2 - 1, 2 r3 - 1, 2 r4 - 1) normalised.
+__device__ __forceinline__ void draw_quaternion(const float *d, double angle, double *q) {
+  double half = 0.5 * ((double)d[3] * angle);
+  double sn, cs;
+  sincos(half, &sn, &cs);
+  double b1 = 2.0 * (double)d[4] - 1.0, b2 = 2.0 * (double)d[5] - 1.0,
+         b3 = 2.0 * (double)d[6] - 1.0;
+  double rn = 1.0 / sqrt(b1 * b1 + b2 * b2 + b3 * b3);
+  q[0] = cs;
+  q[1] = sn * (b1 * rn);
+  q[2] = sn * (b2 * rn);
+  q[3] = sn * (b3 * rn);
+}
+
+// Row d of the rotation matrix of rotation() (utility_pack.f:3497-3506).
+__device__ __forceinline__ void qrow(const double *q, int d, double *row) {
+  double q1 = q[0], q2 = q[1], q3 = q[2], q4 = q[3];
+  if (d == 0) {
+    row[0] = 2.0 * q2 * q2 + 2.0 * q1 * q1 - 1.0;
+    row[1] = 2.0 * q2 * q3 - 2.0 * q1 * q4;
+    row[2] = 2.0 * q2 * q4 + 2.0 * q1 * q3;
+  } else if (d == 1) {
+    row[0] = 2.0 * q2 * q3 + 2.0 * q1 * q4;
+    row[1] = 2.0 * q1 * q1 + 2.0 * q3 * q3 - 1.0;
+    row[2] = 2.0 * q3 * q4 - 2.0 * q1 * q2;
+  } else {
+    row[0] = 2.0 * q2 * q4 - 2.0 * q1 * q3;
+    row[1] = 2.0 * q3 * q4 + 2.0 * q1 * q2;
+    row[2] = 2.0 * q4 * q4 + 2.0 * q1 * q1 - 1.0;
+  }
+}
+
+// Warp 0: the trial geometry, one lane per site coordinate.
 template <bool F32>
-__device__ void geometry(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
-  SysDev &S = B.S;
-  ChainHdr &H = B.H;
+__device__ void geometry_warp(BlockShared<F32> &B, const ChainArrays &CA, int chain, int mode) {
+  const SysDev &S = B.S;
   MoveCtx &mc = B.mc;
+  const int lane = threadIdx.x & 31;
+  if (mc.kind == 0) return;
   const GuestType &G = S.g[mc.g];
-  if (mc.kind == 1) return;
-  int nm = H.nummols[mc.g];
-  if (mc.choice < 1 || mc.choice > nm) {
-    H.status |= kStBadChoice;
-    mc.kind = 0;
-    return;
-  }
-  int slot = CA.ord[((size_t)chain * kMaxG + mc.g) * CA.cap + (mc.choice - 1)];
-  mc.slot = slot;
-  const double *src = CA.gpos + gslot_base(CA, chain, mc.g, slot) * 3;
-  if (mc.kind == 2) {
-    for (int s = 0; s < G.ns; ++s)
-      for (int d = 0; d < 3; ++d) mc.pos[0][s][d] = src[3 * s + d];
-    return;
-  }
-  double a = mc.pos[1][0][0], b = mc.pos[1][0][1], c = mc.pos[1][0][2];
-  double q1 = mc.pos[1][1][0], q2 = mc.pos[1][1][1], q3 = mc.pos[1][1][2],
-         q4 = mc.pos[1][2][0];
-  for (int s = 0; s < G.ns; ++s)
-    for (int d = 0; d < 3; ++d) {
-      mc.pos[1][s][d] = src[3 * s + d];
-      mc.pos[0][s][d] = src[3 * s + d];
+  const int ns = G.ns;
+  const bool mine = lane < 3 * ns;
+  const int s = lane / 3, d = lane % 3;
+  if (mc.kind == 1) {
+    if (mode == kPropExternal) return;  // positions given by the host
+    // random_ins: centre from three fractions, orientation from four draws
+    double q[4], row[3];
+    draw_quaternion(B.draws, 2.0 * kPi, q);
+    if (mine) {
+      qrow(q, d, row);
+      const double *t = G.tmpl[s];
+      double v = row[0] * t[0] + row[1] * t[1] + row[2] * t[2];
+      double cc = (double)B.draws[0] * S.cell[d] + (double)B.draws[1] * S.cell[3 + d] +
+                  (double)B.draws[2] * S.cell[6 + d];
+      mc.pos[0][s][d] = v + cc;
     }
-  translate_sites(S, G, mc.pos[0], a, b, c);
-  double cm[3];
-  centre_of_mass(G, mc.pos[0], cm);
-  rotate_sites(mc.pos[0], G.ns, cm, q1, q2, q3, q4);
-  mc.npos = 2;
+    return;
+  }
+  // delete / displace: the molecule's current sites (get_guest)
+  const double *src = CA.gpos + gslot_base(CA, chain, mc.g, mc.slot) * 3;
+  double old = mine ? src[3 * s + d] : 0.0;
+  if (mc.kind == 2) {
+    if (mine) mc.pos[0][s][d] = old;
+    return;
+  }
+  // translate (utility_pack.f:3161-3218): shift, wrap the centre of mass
+  if (mine) {
+    mc.pos[1][s][d] = old;
+    mc.pos[0][s][d] = B.geo[d] + old;
+  }
+  __syncwarp();
+  if (lane < 3) {  // centre of mass
+    double cm = 0.0;
+    for (int k = 0; k < ns; ++k) cm += mc.pos[0][k][lane] * G.mass[k];
+    B.vtmp[lane] = cm * G.rmass;
+  }
+  __syncwarp();
+  if (lane < 3) {
+    const double *r = S.rcell;
+    double f = r[lane] * B.vtmp[0] + r[3 + lane] * B.vtmp[1] + r[6 + lane] * B.vtmp[2];
+    B.geo[8 + lane] = f - floor(f);
+  }
+  __syncwarp();
+  double w = S.cell[d] * B.geo[8] + S.cell[3 + d] * B.geo[9] + S.cell[6 + d] * B.geo[10];
+  if (mine) mc.pos[0][s][d] += w - B.vtmp[d];
+  __syncwarp();
+  // rotation about the wrapped centre (gcmc.f:2876)
+  if (B.draws[3] >= 0.0f) {
+    double q[4], row[3];
+    if (mode == kPropExternal || B.flags[2]) {
+      q[0] = B.geo[3];
+      q[1] = B.geo[4];
+      q[2] = B.geo[5];
+      q[3] = B.geo[6];
+    } else {
+      draw_quaternion(B.draws, B.geo[7], q);
+    }
+    double wx = S.cell[0] * B.geo[8] + S.cell[3] * B.geo[9] + S.cell[6] * B.geo[10];
+    double wy = S.cell[1] * B.geo[8] + S.cell[4] * B.geo[9] + S.cell[7] * B.geo[10];
+    double wz = S.cell[2] * B.geo[8] + S.cell[5] * B.geo[9] + S.cell[8] * B.geo[10];
+    double x = 0, y = 0, z = 0;
+    if (mine) {
+      x = mc.pos[0][s][0] - wx;
+      y = mc.pos[0][s][1] - wy;
+      z = mc.pos[0][s][2] - wz;
+    }
+    __syncwarp();
+    if (mine) {
+      qrow(q, d, row);
+      double wd = d == 0 ? wx : (d == 1 ? wy : wz);
+      mc.pos[0][s][d] = (row[0] * x + row[1] * y + row[2] * z) + wd;
+    }
+  }
+}
+
+// Warp 0 proposal for all modes; ends with a block barrier.
+template <bool F32>
+__device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, int mode, int g_forced) {
+  if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) {
+      MoveCtx &mc = B.mc;
+      mc.rande = -1.0;
+      mc.estep = 0.0;
+      mc.overlap = 0;
+      mc.accepted = 0;
+      mc.surf_new = mc.surf_old = 0;
+      if (mode == kPropMC) {
+        select_move(B, CA, chain);
+      } else if (mode == kPropInsert) {
+        mc.kind = 1;
+        mc.g = g_forced;
+        mc.ns = B.S.g[g_forced].ns;
+        mc.npos = 1;
+        mc.slot = -1;
+        mc.choice = 0;
+        for (int i = 0; i < 7; ++i) B.draws[i] = duni_f(B.H);
+      } else {  // external: kind, g, choice, positions or a,b,c,q given in mc
+        mc.ns = B.S.g[mc.g].ns;
+        mc.slot = -1;
+        mc.npos = mc.kind >= 3 ? 2 : 1;
+        if (mc.kind >= 3) {
+          B.geo[0] = mc.pos[1][0][0];
+          B.geo[1] = mc.pos[1][0][1];
+          B.geo[2] = mc.pos[1][0][2];
+          B.geo[3] = mc.pos[1][1][0];
+          B.geo[4] = mc.pos[1][1][1];
+          B.geo[5] = mc.pos[1][1][2];
+          B.geo[6] = mc.pos[1][2][0];
+          B.draws[3] = 1.0f;  // rotation present
+        }
+      }
+      if (mc.kind == 2 || mc.kind >= 3) {
+        int nm = B.H.nummols[mc.g];
+        if (mc.choice < 1 || mc.choice > nm) {
+          B.H.status |= kStBadChoice;
+          mc.kind = 0;
+        } else {
+          mc.slot = CA.ord[((size_t)chain * kMaxG + mc.g) * CA.cap + (mc.choice - 1)];
+        }
+      }
+    }
+    __syncwarp();
+    geometry_warp(B, CA, chain, mode);
+  }
+  __syncthreads();
 }
 
 // ------------------------------------------------------------- overlap test
 // Any framework or guest site within the overlap distance of any site of
-// position 0 (the pre-check that lets an insertion or displacement exit
-// before the full sums, as insertion / guest_energy do, mc_moves.f:221-225).
+// position 0: the test that lets an insertion or displacement exit before
+// the full sums (insertion / guest_energy, mc_moves.f:217-225, 347-355).
 template <bool F32>
 __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   const SysDev &S = B.S;
   const MoveCtx &mc = B.mc;
+  const EvalSmem<F32> &ev = B.ev;
   int ns = mc.ns;
   int hit = 0;
   if (S.use_cells) {
     int nrad = 1;
-    double ov = sqrt(S.overlap_sq);
-    while (nrad * fmin(S.csz[0], fmin(S.csz[1], S.csz[2])) < ov && nrad < 4) ++nrad;
+    float mincs = fminf(S.cszf[0], fminf(S.cszf[1], S.cszf[2]));
+    float ov = sqrtf(S.overlap_sqf) + 0.01f;
+    while (nrad * mincs < ov && nrad < 4) ++nrad;
     int span = 2 * nrad + 1;
     int per_site = span * span * span;
     for (int t = threadIdx.x; t < ns * per_site && !hit; t += kThreads) {
       int s = t / per_site, c = t % per_site;
-      int ox = c / (span * span) - nrad, oy = (c / span) % span - nrad, oz = c % span - nrad;
-      const double *p = mc.pos[0][s];
-      int ix = (int)floor(p[0] / S.csz[0]) + ox, iy = (int)floor(p[1] / S.csz[1]) + oy,
-          iz = (int)floor(p[2] / S.csz[2]) + oz;
-      int imx = (ix >= 0) ? ix / S.nc[0] : -((-ix + S.nc[0] - 1) / S.nc[0]);
-      int imy = (iy >= 0) ? iy / S.nc[1] : -((-iy + S.nc[1] - 1) / S.nc[1]);
-      int imz = (iz >= 0) ? iz / S.nc[2] : -((-iz + S.nc[2] - 1) / S.nc[2]);
-      int cell = ((ix - imx * S.nc[0]) * S.nc[1] + (iy - imy * S.nc[1])) * S.nc[2] +
-                 (iz - imz * S.nc[2]);
+      int o3[3] = {c / (span * span) - nrad, (c / span) % span - nrad, c % span - nrad};
+      int im[3], iw[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        int ic = (int)floorf(ev.phi[0][s][d] * S.rcszf[d]) + o3[d];
+        im[d] = image_of(ic, S.nc[d]);
+        iw[d] = ic - im[d] * S.nc[d];
+      }
+      int cell = (iw[0] * S.nc[1] + iw[1]) * S.nc[2] + iw[2];
       int a0 = __ldg(S.cell_start + cell), a1 = __ldg(S.cell_start + cell + 1);
       for (int a = a0; a < a1; ++a) {
-        double4 A = S.fw64[a];
-        double dx = p[0] - (A.x + imx * S.box[0]), dy = p[1] - (A.y + imy * S.box[1]),
-               dz = p[2] - (A.z + imz * S.box[2]);
-        if (dx * dx + dy * dy + dz * dz < S.overlap_sq) hit = 1;
+        if constexpr (F32) {
+          float4 H = __ldg(S.fwhi + a), L = __ldg(S.fwlo + a);
+          float ah[3] = {H.x, H.y, H.z}, al[3] = {L.x, L.y, L.z};
+          float r2 = 0.f;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            if (im[d] != 0) {
+              float h, e;
+              two_sum_f(ah[d], float(im[d]) * S.boxh[d], h, e);
+              ah[d] = h;
+              al[d] = al[d] + (e + float(im[d]) * S.boxl[d]);
+            }
+            float dd = (ev.phi[0][s][d] - ah[d]) + (ev.plo[0][s][d] - al[d]);
+            r2 = fmaf(dd, dd, r2);
+          }
+          if (r2 < S.overlap_sqf) hit = 1;
+        } else {
+          double4 A = S.fw64[a];
+          double dx = ev.p64[0][s][0] - (A.x + im[0] * S.box[0]);
+          double dy = ev.p64[0][s][1] - (A.y + im[1] * S.box[1]);
+          double dz = ev.p64[0][s][2] - (A.z + im[2] * S.box[2]);
+          if (dx * dx + dy * dy + dz * dz < S.overlap_sq) hit = 1;
+        }
       }
     }
   } else {
     for (int t = threadIdx.x; t < ns * S.nfw && !hit; t += kThreads) {
       int s = t / S.nfw, a = t % S.nfw;
-      const double *p = mc.pos[0][s];
+      const double *p = ev.p64[0][s];
       double4 A = S.fw64[a];
       double dx = p[0] - A.x, dy = p[1] - A.y, dz = p[2] - A.z;
       const double *r = S.rcell, *c = S.cell;
@@ -305,84 +420,106 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
     const GuestType &G2 = S.g[g2];
     int n2 = B.H.nummols[g2];
     const int *ord = CA.ord + ((size_t)chain * kMaxG + g2) * CA.cap;
-    double pre = sqrt(S.overlap_sq) + 2.0 * G.rmax + 2.0 * G2.rmax + 0.01;
-    for (int i = threadIdx.x; i < n2 && !hit; i += kThreads) {
-      int slot = ord[i];
-      if (g2 == mc.g && slot == mc.slot) continue;
-      const double *q = CA.gpos + gslot_base(CA, chain, g2, slot) * 3;
-      double dx = mc.pos[0][0][0] - q[0], dy = mc.pos[0][0][1] - q[1], dz = mc.pos[0][0][2] - q[2];
-      if (S.use_cells) {
-        dx -= S.box[0] * round(dx / S.box[0]);
-        dy -= S.box[1] * round(dy / S.box[1]);
-        dz -= S.box[2] * round(dz / S.box[2]);
-        if (dx * dx + dy * dy + dz * dz > pre * pre) continue;
-      }
-      for (int b = 0; b < G2.ns; ++b)
-        for (int s = 0; s < ns; ++s) {
-          double ex = mc.pos[0][s][0] - q[3 * b], ey = mc.pos[0][s][1] - q[3 * b + 1],
-                 ez = mc.pos[0][s][2] - q[3 * b + 2];
-          if (S.use_cells) {
-            ex -= S.box[0] * round(ex / S.box[0]);
-            ey -= S.box[1] * round(ey / S.box[1]);
-            ez -= S.box[2] * round(ez / S.box[2]);
-          } else {
-            const double *r = S.rcell, *c = S.cell;
-            double fx = r[0] * ex + r[3] * ey + r[6] * ez, fy = r[1] * ex + r[4] * ey + r[7] * ez,
-                   fz = r[2] * ex + r[5] * ey + r[8] * ez;
-            fx -= round(fx);
-            fy -= round(fy);
-            fz -= round(fz);
-            ex = c[0] * fx + c[3] * fy + c[6] * fz;
-            ey = c[1] * fx + c[4] * fy + c[7] * fz;
-            ez = c[2] * fx + c[5] * fy + c[8] * fz;
+    float pre = sqrtf(S.overlap_sqf) + 2.0f * (float)G.rmax + 2.0f * (float)G2.rmax + 0.01f;
+    if constexpr (F32) {
+      const float4 *gh = CA.ghi + ((size_t)chain * kMaxG + g2) * CA.cap * kMaxS;
+      const float4 *gl = CA.glo + ((size_t)chain * kMaxG + g2) * CA.cap * kMaxS;
+      float pre2 = pre * pre;
+      for (int i = threadIdx.x; i < n2 && !hit; i += kThreads) {
+        int slot = ord[i];
+        if (g2 == mc.g && slot == mc.slot) continue;
+        float4 q0 = gh[(size_t)slot * kMaxS];
+        float dx = ev.phi[0][0][0] - q0.x, dy = ev.phi[0][0][1] - q0.y, dz = ev.phi[0][0][2] - q0.z;
+        dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
+        dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
+        dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+        for (int b = 0; b < G2.ns; ++b) {
+          float4 qh = gh[(size_t)slot * kMaxS + b], ql = gl[(size_t)slot * kMaxS + b];
+          for (int s = 0; s < ns; ++s) {
+            float ex = mi_diff32(ev.phi[0][s][0], ev.plo[0][s][0], qh.x, ql.x, S.boxh[0], S.boxl[0], S.rboxf[0]);
+            float ey = mi_diff32(ev.phi[0][s][1], ev.plo[0][s][1], qh.y, ql.y, S.boxh[1], S.boxl[1], S.rboxf[1]);
+            float ez = mi_diff32(ev.phi[0][s][2], ev.plo[0][s][2], qh.z, ql.z, S.boxh[2], S.boxl[2], S.rboxf[2]);
+            if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < S.overlap_sqf) hit = 1;
           }
-          if (ex * ex + ey * ey + ez * ez < S.overlap_sq) hit = 1;
         }
+      }
+    } else {
+      for (int i = threadIdx.x; i < n2 && !hit; i += kThreads) {
+        int slot = ord[i];
+        if (g2 == mc.g && slot == mc.slot) continue;
+        const double *q = CA.gpos + gslot_base(CA, chain, g2, slot) * 3;
+        if (S.use_cells) {
+          double dx = ev.p64[0][0][0] - q[0], dy = ev.p64[0][0][1] - q[1], dz = ev.p64[0][0][2] - q[2];
+          dx -= S.box[0] * round(S.rbox[0] * dx);
+          dy -= S.box[1] * round(S.rbox[1] * dy);
+          dz -= S.box[2] * round(S.rbox[2] * dz);
+          if (dx * dx + dy * dy + dz * dz > (double)pre * (double)pre) continue;
+        }
+        for (int b = 0; b < G2.ns; ++b)
+          for (int s = 0; s < ns; ++s) {
+            double ex = ev.p64[0][s][0] - q[3 * b], ey = ev.p64[0][s][1] - q[3 * b + 1],
+                   ez = ev.p64[0][s][2] - q[3 * b + 2];
+            if (S.use_cells) {
+              ex -= S.box[0] * round(S.rbox[0] * ex);
+              ey -= S.box[1] * round(S.rbox[1] * ey);
+              ez -= S.box[2] * round(S.rbox[2] * ez);
+            } else {
+              const double *r = S.rcell, *c = S.cell;
+              double fx = r[0] * ex + r[3] * ey + r[6] * ez, fy = r[1] * ex + r[4] * ey + r[7] * ez,
+                     fz = r[2] * ex + r[5] * ey + r[8] * ez;
+              fx -= round(fx);
+              fy -= round(fy);
+              fz -= round(fz);
+              ex = c[0] * fx + c[3] * fy + c[6] * fz;
+              ey = c[1] * fx + c[4] * fy + c[7] * fz;
+              ez = c[2] * fx + c[5] * fy + c[8] * fz;
+            }
+            if (ex * ex + ey * ey + ez * ez < S.overlap_sq) hit = 1;
+          }
+      }
     }
   }
   return block_or(hit, B.ev.red_i);
 }
 
 // ----------------------------------------------------------------- k-space
-// One pass over the k-vectors for npos positions; writes s(k) of position 0
-// to snew and of position 1 to sold, accumulates energies and mixing terms.
+// One pass over the k-vectors for npos positions (ewald1_guest, ewald.f:
+// 151-315): s(k) of position 0 goes to the snew scratch and of position 1 to
+// sold; energies and mixing terms accumulate in acc.
 template <bool F32>
-__device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain,
-                       bool exist0, double *E, double (*mix)[kMaxM + 1]) {
+__device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain, bool exist0,
+                       PosAcc<F32> *acc) {
   const SysDev &S = B.S;
   const MoveCtx &mc = B.mc;
   const GuestType &G = S.g[mc.g];
-  int ns = mc.ns, npos = mc.npos;
-  int mol = G.mol;
-  bool disp = npos == 2;
-  double2 *snew = CA.snew + (size_t)chain * CA.nkmax;
-  double2 *sold = CA.sold + (size_t)chain * CA.nkmax;
-  const double2 *skg = CA.sk + (size_t)chain * kMaxG * CA.nkmax;
-  const float2 *sk32 = CA.sk32 + (size_t)chain * CA.nmt * CA.nkmax;
-  double e[2] = {0.0, 0.0};
-  double mx[2][kMaxM + 1];
-  for (int p = 0; p < 2; ++p)
-    for (int m = 0; m <= kMaxM; ++m) mx[p][m] = 0.0;
-  float ef[2] = {0.f, 0.f};
-  int cnt = 0;
-  for (int k = threadIdx.x; k < S.nk; k += kThreads) {
-    int4 lmn = __ldg(S.klmn + k);
-    int am = abs(lmn.y), an = abs(lmn.z);
-    bool cm = lmn.y < 0, cn = lmn.z < 0;
-    if constexpr (!F32) {
+  const int ns = mc.ns, npos = mc.npos, mol = G.mol, NG = S.ntpguest;
+  const bool disp = npos == 2;
+  if constexpr (!F32) {
+    double2 *snew = CA.snew + (size_t)chain * CA.nkmax;
+    double2 *sold = CA.sold + (size_t)chain * CA.nkmax;
+    const double2 *skg = CA.sk + (size_t)chain * kMaxG * CA.nkmax;
+    double e[2] = {0.0, 0.0}, mfw[2] = {0.0, 0.0}, mg[2][kMaxG];
+    for (int g2 = 0; g2 < kMaxG; ++g2) mg[0][g2] = mg[1][g2] = 0.0;
+    for (int k = threadIdx.x; k < S.nk; k += kThreads) {
+      int4 lmn = __ldg(S.klmn + k);
+      int am = abs(lmn.y), an = abs(lmn.z);
+      bool cm = lmn.y < 0, cn = lmn.z < 0;
       double akk = __ldg(S.akk + k);
-      // S(k) per molecule type and total
       double2 sfw = __ldg(S.skfw + k);
       double2 stot = sfw;
       double2 sgt[kMaxG];
-      for (int g2 = 0; g2 < S.ntpguest; ++g2) {
-        sgt[g2] = skg[(size_t)g2 * CA.nkmax + k];
-        stot.x += sgt[g2].x;
-        stot.y += sgt[g2].y;
+#pragma unroll
+      for (int g2 = 0; g2 < kMaxG; ++g2) {
+        if (g2 < NG) {
+          sgt[g2] = skg[(size_t)g2 * CA.nkmax + k];
+          stot.x += sgt[g2].x;
+          stot.y += sgt[g2].y;
+        }
       }
       double2 sp[2];
       for (int p = 0; p < npos; ++p) {
-        double2 acc = make_double2(0.0, 0.0);
+        double2 a = make_double2(0.0, 0.0);
         for (int s = 0; s < ns; ++s) {
           double2 ex = B.ev.pw64[p][s][0][lmn.x];
           double2 ey = B.ev.pw64[p][s][1][am];
@@ -390,14 +527,14 @@ __device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain,
           if (cm) ey.y = -ey.y;
           if (cn) ez.y = -ez.y;
           double2 t = cmul(cmul(ex, ey), ez);
-          acc.x += G.q[s] * t.x;
-          acc.y += G.q[s] * t.y;
+          a.x += G.q[s] * t.x;
+          a.y += G.q[s] * t.y;
         }
-        sp[p] = acc;
+        sp[p] = a;
       }
       for (int p = 0; p < npos; ++p) {
         double2 su = stot;
-        if (disp && p == 0) {  // new position sees S - s_old (gcmc.f:2862-2871)
+        if (disp && p == 0) {  // the new position sees S - s_old (gcmc.f:2862-2871)
           su.x -= sp[1].x;
           su.y -= sp[1].y;
         }
@@ -407,21 +544,51 @@ __device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain,
         if (exist) mixterm = -1.0 * mixterm;
         e[p] += akk * (mixterm + sumsqd);
         double f2 = 2.0 * akk;
-        mx[p][S.fw_mol] += f2 * (sp[p].x * sfw.x + sp[p].y * sfw.y);
-        for (int g2 = 0; g2 < S.ntpguest; ++g2) {
-          int m2 = S.g[g2].mol;
-          if (m2 == mol) continue;
-          mx[p][m2] += f2 * (sp[p].x * sgt[g2].x + sp[p].y * sgt[g2].y);
-        }
+        mfw[p] += f2 * (sp[p].x * sfw.x + sp[p].y * sfw.y);
+#pragma unroll
+        for (int g2 = 0; g2 < kMaxG; ++g2)
+          if (g2 < NG && S.g[g2].mol != mol) mg[p][g2] += f2 * (sp[p].x * sgt[g2].x + sp[p].y * sgt[g2].y);
       }
       snew[k] = sp[0];
       if (disp) sold[k] = sp[1];
-    } else {
+    }
+    for (int p = 0; p < 2; ++p) {
+      acc[p].recip.add(e[p]);
+      acc[p].mixfw.add(mfw[p]);
+      for (int g2 = 0; g2 < kMaxG; ++g2) acc[p].mixg[g2].add(mg[p][g2]);
+    }
+  } else {
+    float2 *snew32 = CA.snew32 + (size_t)chain * CA.nkmax;
+    float2 *sold32 = CA.sold32 + (size_t)chain * CA.nkmax;
+    const float4 *skg = CA.skdf + (size_t)chain * kMaxG * CA.nkmax;
+    float e[2] = {0.f, 0.f}, mfw[2] = {0.f, 0.f}, mg[2][kMaxG];
+#pragma unroll
+    for (int g2 = 0; g2 < kMaxG; ++g2) mg[0][g2] = mg[1][g2] = 0.f;
+    int cnt = 0;
+    for (int k = threadIdx.x; k < S.nk; k += kThreads) {
+      int4 lmn = __ldg(S.klmn + k);
+      int am = abs(lmn.y), an = abs(lmn.z);
+      bool cm = lmn.y < 0, cn = lmn.z < 0;
       float akk = __ldg(S.akk32 + k);
-      float2 stot = sk32[(size_t)S.maxmls * CA.nkmax + k];
+      float4 fw = __ldg(S.skfw_df + k);
+      float thx = fw.x, thy = fw.y, tlx = fw.z, tly = fw.w;
+      float2 sfw = make_float2(fw.x + fw.z, fw.y + fw.w);
+      float2 sgt[kMaxG];
+#pragma unroll
+      for (int g2 = 0; g2 < kMaxG; ++g2) {
+        if (g2 < NG) {
+          float4 v = skg[(size_t)g2 * CA.nkmax + k];
+          thx += v.x;
+          thy += v.y;
+          tlx += v.z;
+          tly += v.w;
+          sgt[g2] = make_float2(v.x + v.z, v.y + v.w);
+        }
+      }
+      float2 stot = make_float2(thx + tlx, thy + tly);
       float2 sp[2];
       for (int p = 0; p < npos; ++p) {
-        float2 acc = make_float2(0.f, 0.f);
+        float2 a = make_float2(0.f, 0.f);
         for (int s = 0; s < ns; ++s) {
           float2 ex = B.ev.pw32[p][s][0][lmn.x];
           float2 ey = B.ev.pw32[p][s][1][am];
@@ -429,11 +596,11 @@ __device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain,
           if (cm) ey.y = -ey.y;
           if (cn) ez.y = -ez.y;
           float2 t = cmul(cmul(ex, ey), ez);
-          float q = (float)G.q[s];
-          acc.x = fmaf(q, t.x, acc.x);
-          acc.y = fmaf(q, t.y, acc.y);
+          float q = B.si[s].qf;
+          a.x = fmaf(q, t.x, a.x);
+          a.y = fmaf(q, t.y, a.y);
         }
-        sp[p] = acc;
+        sp[p] = a;
       }
       for (int p = 0; p < npos; ++p) {
         float2 su = stot;
@@ -445,200 +612,195 @@ __device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain,
         float sumsqd = fmaf(sp[p].x, sp[p].x, sp[p].y * sp[p].y);
         float mixterm = 2.0f * fmaf(sp[p].x, su.x, sp[p].y * su.y);
         if (exist) mixterm = -mixterm;
-        ef[p] = fmaf(akk, mixterm + sumsqd, ef[p]);
+        e[p] = fmaf(akk, mixterm + sumsqd, e[p]);
         float f2 = 2.0f * akk;
-        for (int m2 = 1; m2 <= S.maxmls; ++m2) {
-          if (m2 == mol) continue;
-          float2 si2 = sk32[(size_t)(m2 - 1) * CA.nkmax + k];
-          mx[p][m2] += (double)(f2 * fmaf(sp[p].x, si2.x, sp[p].y * si2.y));
-        }
+        mfw[p] = fmaf(f2, fmaf(sp[p].x, sfw.x, sp[p].y * sfw.y), mfw[p]);
+#pragma unroll
+        for (int g2 = 0; g2 < kMaxG; ++g2)
+          if (g2 < NG && S.g[g2].mol != mol)
+            mg[p][g2] = fmaf(f2, fmaf(sp[p].x, sgt[g2].x, sp[p].y * sgt[g2].y), mg[p][g2]);
       }
-      snew[k] = make_double2(sp[0].x, sp[0].y);
-      if (disp) sold[k] = make_double2(sp[1].x, sp[1].y);
+      snew32[k] = sp[0];
+      if (disp) sold32[k] = sp[1];
       if (++cnt == 8) {
-        e[0] += ef[0];
-        e[1] += ef[1];
-        ef[0] = ef[1] = 0.f;
+        for (int p = 0; p < 2; ++p) {
+          acc[p].recip.add(e[p]);
+          acc[p].mixfw.add(mfw[p]);
+          e[p] = mfw[p] = 0.f;
+#pragma unroll
+          for (int g2 = 0; g2 < kMaxG; ++g2) {
+            acc[p].mixg[g2].add(mg[p][g2]);
+            mg[p][g2] = 0.f;
+          }
+        }
         cnt = 0;
       }
     }
-  }
-  if constexpr (F32) {
-    e[0] += ef[0];
-    e[1] += ef[1];
-  }
-  for (int p = 0; p < 2; ++p) {
-    E[p] = e[p];
-    for (int m = 0; m <= kMaxM; ++m) mix[p][m] = mx[p][m];
+    for (int p = 0; p < 2; ++p) {
+      acc[p].recip.add(e[p]);
+      acc[p].mixfw.add(mfw[p]);
+#pragma unroll
+      for (int g2 = 0; g2 < kMaxG; ++g2) acc[p].mixg[g2].add(mg[p][g2]);
+    }
   }
 }
 
 // --------------------------------------------------------------- evaluate
-// Evaluate the proposed move; fills mc.estep, mc.delE, flags.  Returns 1 if
-// a full evaluation ran (no overlap exit).
+// Evaluate the proposed move; fills mc.estep, mc.delE and the flags.
+// Returns 1 if a full evaluation ran (no overlap exit).
 template <bool F32>
 __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, int &st) {
-  SysDev &S = B.S;
+  const SysDev &S = B.S;
   MoveCtx &mc = B.mc;
   const GuestType &G = S.g[mc.g];
-  int ns = mc.ns;
-  // site data to shared memory
+  const int ns = mc.ns, npos = mc.npos, NG = S.ntpguest;
   if (threadIdx.x < ns) {
     int s = threadIdx.x;
     B.si[s].q = G.q[s];
     B.si[s].chgea = G.q[s] / S.epsq * kR4pie0;
+    B.si[s].chgeaf = (float)B.si[s].chgea;
+    B.si[s].qf = (float)G.q[s];
     B.si[s].type = G.type[s];
   }
-  if (threadIdx.x < 2 * kMaxS) {
-    int p = threadIdx.x / kMaxS, s = threadIdx.x % kMaxS;
-    if (p < mc.npos && s < ns) {
-      for (int d = 0; d < 3; ++d) {
-        double v = mc.pos[p][s][d];
-        B.ev.p64[p][s][d] = v;
-        float h = (float)v;
-        B.ev.phi[p][s][d] = h;
-        B.ev.plo[p][s][d] = (float)(v - (double)h);
-      }
+  if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * kMaxS * 3) {
+    int t = threadIdx.x - 32;
+    int p = t / (kMaxS * 3), s = (t / 3) % kMaxS, d = t % 3;
+    if (p < npos && s < ns) {
+      double v = mc.pos[p][s][d];
+      B.ev.p64[p][s][d] = v;
+      float h = (float)v;
+      B.ev.phi[p][s][d] = h;
+      B.ev.plo[p][s][d] = (float)(v - (double)h);
     }
   }
   __syncthreads();
-  bool needs_ov = (mc.kind == 1 || mc.kind >= 3);
-  if (needs_ov) {
-    int hit = overlap_check(B, CA, chain);
-    if (hit) {
+  if (threadIdx.x < npos) {  // conservative centre and radius (FP32)
+    int p = threadIdx.x;
+    float c[3] = {0.f, 0.f, 0.f};
+    for (int s = 0; s < ns; ++s)
+      for (int d = 0; d < 3; ++d) c[d] += B.ev.phi[p][s][d];
+    float rn = 1.0f / ns, rm2 = 0.f;
+    for (int d = 0; d < 3; ++d) c[d] *= rn;
+    for (int s = 0; s < ns; ++s) {
+      float dx = B.ev.phi[p][s][0] - c[0], dy = B.ev.phi[p][s][1] - c[1], dz = B.ev.phi[p][s][2] - c[2];
+      rm2 = fmaxf(rm2, dx * dx + dy * dy + dz * dz);
+    }
+    for (int d = 0; d < 3; ++d) B.ev.cen[p][d] = c[d];
+    B.ev.rmx[p] = sqrtf(rm2) + 1e-3f;
+  }
+  __syncthreads();
+  if (mc.kind == 1 || mc.kind >= 3) {
+    if (overlap_check(B, CA, chain)) {
       if (threadIdx.x == 0) mc.overlap = 1;
       __syncthreads();
       return 0;
     }
   }
-  // ---- pair sums, one position at a time
-  Acc acc[2];
-  for (int p = 0; p < 2; ++p) {
-    acc[p].e2_fw = acc[p].vdw_fw = acc[p].recip = 0.0;
-    for (int g2 = 0; g2 < kMaxG; ++g2) acc[p].e2_g[g2] = acc[p].vdw_g[g2] = 0.0;
-    for (int m = 0; m <= kMaxM; ++m) acc[p].mix[m] = 0.0;
-  }
+  PosAcc<F32> acc[2];
+  acc[0].zero();
+  acc[1].zero();
   int sf[2] = {0, 0}, ovd = 0;
-  for (int p = 0; p < mc.npos; ++p) {
-    double c[3] = {0, 0, 0};
-    for (int s = 0; s < ns; ++s)
-      for (int d = 0; d < 3; ++d) c[d] += B.ev.p64[p][s][d];
-    for (int d = 0; d < 3; ++d) c[d] /= ns;
-    double rm = 0.0;
-    for (int s = 0; s < ns; ++s) {
-      double dx = B.ev.p64[p][s][0] - c[0], dy = B.ev.p64[p][s][1] - c[1],
-             dz = B.ev.p64[p][s][2] - c[2];
-      rm = fmax(rm, sqrt(dx * dx + dy * dy + dz * dz));
-    }
-    build_segments<F32>(S, B.ev, c, S.rcut + rm + 1e-6, st);
+  for (int p = 0; p < npos; ++p) {
+    build_segments<F32>(S, B.ev, B.ev.cen[p], (float)S.rcut + B.ev.rmx[p] + 1e-3f, st);
     scan_framework<F32>(S, B.ev, p, ns, B.si, acc[p], ovd, sf[p], st);
-    __syncthreads();
-    scan_guests<F32>(S, B.H, CA, chain, B.ev, p, ns, mc.g, mc.slot, rm, B.si, acc[p], ovd,
-                     sf[p], st);
+    scan_guests<F32>(S, B.H, CA, chain, B.ev, p, ns, mc.g, mc.slot, B.ev.rmx[p], B.si, acc[p],
+                     ovd, sf[p], st);
     __syncthreads();
   }
-  // ---- k-space
-  build_powers<F32>(S, B.ev, mc.npos, ns);
+  build_powers<F32>(S, B.ev, npos, ns);
   __syncthreads();
-  double E[2], mix[2][kMaxM + 1];
-  kspace<F32>(B, CA, chain, mc.kind == 2, E, mix);
-  // ---- reduce: per position 2 + 2*G + 1 + maxmls values
-  const int nper = 2 + 2 * kMaxG + 1 + (kMaxM + 1);
-  double vals[2 * nper];
-  for (int p = 0; p < 2; ++p) {
-    double *v = vals + p * nper;
-    v[0] = acc[p].e2_fw;
-    v[1] = acc[p].vdw_fw;
-    for (int g2 = 0; g2 < kMaxG; ++g2) {
-      v[2 + g2] = acc[p].e2_g[g2];
-      v[2 + kMaxG + g2] = acc[p].vdw_g[g2];
-    }
-    v[2 + 2 * kMaxG] = E[p];
-    for (int m = 0; m <= kMaxM; ++m) v[3 + 2 * kMaxG + m] = mix[p][m];
+  kspace<F32>(B, CA, chain, mc.kind == 2, acc);
+  // reduce [e2fw, vdwfw, recip, mixfw, e2g[NG], vdwg[NG], mixg[NG]] per position
+  const int nper = 4 + 3 * NG;
+  AccT<F32> v[32];
+  int n = 0;
+  for (int p = 0; p < npos; ++p) {
+    v[n++] = acc[p].e2fw;
+    v[n++] = acc[p].vdwfw;
+    v[n++] = acc[p].recip;
+    v[n++] = acc[p].mixfw;
+    for (int g2 = 0; g2 < NG; ++g2) v[n++] = acc[p].e2g[g2];
+    for (int g2 = 0; g2 < NG; ++g2) v[n++] = acc[p].vdwg[g2];
+    for (int g2 = 0; g2 < NG; ++g2) v[n++] = acc[p].mixg[g2];
   }
-  block_sum(vals, 2 * nper, B.ev.red);
+  block_reduce(v, n, B.ev.red, B.ev.out);
   int sfa = block_or(sf[0], B.ev.red_i);
   int sfb = block_or(sf[1], B.ev.red_i);
   if (threadIdx.x == 0) {
-    const double *R = B.ev.red + kWarps * 2 * nper;
-    mc.surf_new = sfa;  // position 0
+    const double *R = B.ev.out;
+    mc.surf_new = sfa;
     mc.surf_old = sfb;
-    int mol = G.mol;
-    double chgtmp = 0.0, sq = 0.0;
-    for (int s = 0; s < ns; ++s) {
-      chgtmp += G.q[s];
-      sq += G.q[s] * G.q[s];
+    const int mol = G.mol;
+    const double sumchg = B.H.sumchg, eu = S.rengunit, e3 = G.ewald3en;
+    double ewld1[2], e2[2], vd[2];
+    for (int p = 0; p < npos; ++p) {
+      const double *r = R + p * nper;
+      bool exist = (npos == 2) ? (p == 1) : (mc.kind == 2);
+      double sic = exist ? -G.engsic0 : G.engsic0;
+      double qfix = G.qfa * sumchg + G.qfb;
+      if (exist) qfix = -qfix;
+      ewld1[p] = S.krecip * r[2] + sic + qfix;
+      e2[p] = r[0];
+      vd[p] = r[1];
+      for (int g2 = 0; g2 < NG; ++g2) {
+        e2[p] += r[4 + g2];
+        vd[p] += r[4 + NG + g2];
+      }
     }
-    double r4 = kR4pie0 / S.epsq;
-    double engsic0 = -r4 * S.alpha * sq / kSqrPi;
-    double sumchg = B.H.sumchg;
-    // per position: ewld1, ewald1en(mol,i), ewald2, vdw, ewald2en, vdwen
-    double ewld1[2], e2[2], vd[2], e1en[2][kMaxM + 1], e2en[2][kMaxM + 1], vden[2][kMaxM + 1];
-    for (int p = 0; p < mc.npos; ++p) {
-      const double *v = R + p * nper;
-      bool exist = (mc.npos == 2) ? (p == 1) : (mc.kind == 2);
-      double qfix = -(0.5 * kPi * r4) *
-                    ((chgtmp * sumchg) / S.alpha + (chgtmp / S.alpha) * (chgtmp / S.alpha)) / S.volm;
-      double sic = engsic0;
-      if (exist) {
-        sic = -sic;
-        qfix = -qfix;
+    // per-molecule-type terms against type m != mol (delE(m))
+    auto pair_terms = [&](int p, int m, double delrc_m) {
+      const double *r = R + p * nper;
+      bool exist = (npos == 2) ? (p == 1) : (mc.kind == 2);
+      double qfm = G.qfm * B.H.chgsum_mol[m];
+      if (exist) qfm = -qfm;
+      double e1 = 0.0, e2m = 0.0, vdm = 0.0;
+      if (m == S.fw_mol) {
+        e1 = S.krecip * r[3] + qfm;
+        e2m = r[0];
+        vdm = r[1];
+      } else {
+        e1 = qfm;
+        for (int g2 = 0; g2 < NG; ++g2)
+          if (S.g[g2].mol == m) {
+            e1 += S.krecip * r[4 + 2 * NG + g2];
+            e2m += r[4 + g2];
+            vdm += r[4 + NG + g2];
+          }
       }
-      ewld1[p] = S.krecip * v[2 + 2 * kMaxG] + sic + qfix;
-      e2[p] = v[0];
-      vd[p] = v[1];
-      for (int m = 0; m <= kMaxM; ++m) e1en[p][m] = e2en[p][m] = vden[p][m] = 0.0;
-      e2en[p][S.fw_mol] = v[0];
-      vden[p][S.fw_mol] = v[1];
-      for (int g2 = 0; g2 < S.ntpguest; ++g2) {
-        e2[p] += v[2 + g2];
-        vd[p] += v[2 + kMaxG + g2];
-        e2en[p][S.g[g2].mol] += v[2 + g2];
-        vden[p][S.g[g2].mol] += v[2 + kMaxG + g2];
-      }
+      return e1 + e2m + vdm + delrc_m;
+    };
+    for (int m = 0; m <= kMaxM; ++m) mc.delE[m] = 0.0;
+    if (mc.kind == 1 || mc.kind == 2) {
+      bool del = mc.kind == 2;
+      double delrc = lrc_delta(S, B.H, mc.g, del);
+      mc.delrc = delrc;
+      if (!del) mc.estep = (ewld1[0] + e2[0] - e3 + vd[0] + delrc) * eu;
+      else mc.estep = (-ewld1[0] + e2[0] + vd[0] - e3) * eu - delrc * eu;
       for (int m = 1; m <= S.maxmls; ++m) {
         if (m == mol) continue;
-        double qfm = -(1.0 * kPi * r4) * (B.H.chgsum_mol[m] * chgtmp) / (S.alpha * S.alpha * S.volm);
-        if (exist) qfm = -qfm;
-        e1en[p][m] = S.krecip * v[3 + 2 * kMaxG + m] + qfm;
+        double dm = 0.0;  // delrc_mol(loc2(mol,m)), vdw_terms.f:743-761
+        if (m == S.fw_mol) dm = G.lrcA - G.lrcC;
+        else
+          for (int g2 = 0; g2 < NG; ++g2)
+            if (S.g[g2].mol == m) dm = double(B.H.nummols[g2]) * G.lrcB[g2];
+        double t = pair_terms(0, m, dm) * eu;
+        mc.delE[m] = del ? -t : t;
       }
-    }
-    double e3 = G.ewald3en, eu = S.engunit;
-    for (int m = 0; m <= kMaxM; ++m) mc.delE[m] = 0.0;
-    if (mc.kind == 1) {
-      double delrc;
-      gst_lrc(S, B.H, mc.g, false, delrc, mc.delrc_mol);
-      mc.delrc = delrc;
-      mc.estep = (ewld1[0] + e2[0] - e3 + vd[0] + delrc) / eu;
-      for (int m = 1; m <= S.maxmls; ++m)
-        if (m != mol) mc.delE[m] = (e1en[0][m] + e2en[0][m] + vden[0][m] + mc.delrc_mol[m]) / eu;
-      mc.delE[mol] = mc.estep;
-    } else if (mc.kind == 2) {
-      double delrc;
-      gst_lrc(S, B.H, mc.g, true, delrc, mc.delrc_mol);
-      mc.delrc = delrc;
-      double est = (-ewld1[0] + e2[0] + vd[0] - e3) / eu;
-      mc.estep = est - delrc / eu;
-      for (int m = 1; m <= S.maxmls; ++m)
-        if (m != mol) mc.delE[m] = -(e1en[0][m] + e2en[0][m] + vden[0][m] + mc.delrc_mol[m]) / eu;
-      mc.delE[mol] = -mc.estep;
+      mc.delE[mol] = del ? -mc.estep : mc.estep;
     } else {
-      double enginit = (-ewld1[1] + e2[1] + vd[1] - e3) / eu;
-      double enew = (ewld1[0] + e2[0] + vd[0] - e3) / eu;
+      double enginit = (-ewld1[1] + e2[1] + vd[1] - e3) * eu;
+      double enew = (ewld1[0] + e2[0] + vd[0] - e3) * eu;
       mc.estep = enew - enginit;
       mc.delrc = 0.0;
       for (int m = 1; m <= S.maxmls; ++m)
-        if (m != mol)
-          mc.delE[m] = (e1en[0][m] - e1en[1][m] + e2en[0][m] - e2en[1][m] + vden[0][m] - vden[1][m]) / eu;
+        if (m != mol) mc.delE[m] = (pair_terms(0, m, 0.0) - pair_terms(1, m, 0.0)) * eu;
       mc.delE[mol] = mc.estep;
     }
     mc.parts[0] = ewld1[0];
     mc.parts[1] = e2[0];
     mc.parts[2] = vd[0];
     mc.parts[3] = mc.delrc;
-    mc.ewld1_b = mc.npos == 2 ? ewld1[1] : 0.0;
-    mc.chgtmp = chgtmp;
-    mc.engsictmp = engsic0;
+    mc.chgtmp = G.chgtmp;
     if (!isfinite(mc.estep)) st |= kStNonFinite;
   }
   __syncthreads();
@@ -646,7 +808,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
 }
 
 // ----------------------------------------------------------------- decide
-// Thread 0.  rande < 0 asks for a draw from the chain's generator.
+// Thread 0.  `draw`: take the Metropolis number from the chain's generator.
 template <bool F32>
 __device__ void decide(BlockShared<F32> &B, bool draw) {
   MoveCtx &mc = B.mc;
@@ -660,10 +822,10 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
       mc.accepted = 0;
       return;
     }
-    if (draw) mc.rande = duni_next(H);
+    if (draw) mc.rande = (double)duni_f(H);
     mc.accepted = energy_eval(B.S, H, mc.g, mc.estep, mc.rande, 1);
   } else if (mc.kind == 2) {
-    if (draw) mc.rande = duni_next(H);
+    if (draw) mc.rande = (double)duni_f(H);
     mc.accepted = energy_eval(B.S, H, mc.g, -mc.estep, mc.rande, 2);
   } else {
     if (mc.overlap) {
@@ -674,28 +836,19 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
       mc.accepted = 1;
       if (draw) mc.rande = -1.0;
     } else {
-      if (draw) mc.rande = duni_next(H);
+      if (draw) mc.rande = (double)duni_f(H);
       mc.accepted = energy_eval(B.S, H, mc.g, mc.estep, mc.rande, mc.kind);
     }
   }
 }
 
-// Refresh the FP32 mirror of S(k) for k (guest type g changed).
-template <bool F32>
-__device__ __forceinline__ void refresh_mirror(const SysDev &S, const ChainArrays &CA, int chain,
-                                               int k) {
-  const double2 *skg = CA.sk + (size_t)chain * kMaxG * CA.nkmax;
-  float2 *sk32 = CA.sk32 + (size_t)chain * CA.nmt * CA.nkmax;
-  double2 fw = __ldg(S.skfw + k);
-  double tx = fw.x, ty = fw.y;
-  sk32[(size_t)(S.fw_mol - 1) * CA.nkmax + k] = make_float2((float)fw.x, (float)fw.y);
-  for (int g2 = 0; g2 < S.ntpguest; ++g2) {
-    double2 v = skg[(size_t)g2 * CA.nkmax + k];
-    tx += v.x;
-    ty += v.y;
-    sk32[(size_t)(S.g[g2].mol - 1) * CA.nkmax + k] = make_float2((float)v.x, (float)v.y);
-  }
-  sk32[(size_t)S.maxmls * CA.nkmax + k] = make_float2((float)tx, (float)ty);
+// Error-free update of one double-float component: (hi, lo) += x.
+__device__ __forceinline__ void df_inc(float &hi, float &lo, float x) {
+  float s, e;
+  two_sum_f(hi, x, s, e);
+  e += lo;
+  hi = s + e;
+  lo = e - (hi - s);
 }
 
 // ----------------------------------------------------------------- commit
@@ -709,31 +862,52 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
   __syncthreads();  // every thread has read the decision before anyone moves on
   if (!accepted) return;
   const GuestType &G = S.g[mc.g];
-  int g = mc.g;
-  double2 *skg = CA.sk + ((size_t)chain * kMaxG + g) * CA.nkmax;
-  const double2 *snew = CA.snew + (size_t)chain * CA.nkmax;
-  const double2 *sold = CA.sold + (size_t)chain * CA.nkmax;
-  for (int k = threadIdx.x; k < S.nk; k += kThreads) {
-    double2 v = skg[k];
-    double2 n = snew[k];
-    if (mc.kind == 1) {
-      v.x += n.x;
-      v.y += n.y;
-    } else if (mc.kind == 2) {
-      v.x -= n.x;
-      v.y -= n.y;
-    } else {
-      double2 o = sold[k];
-      v.x = (v.x - o.x) + n.x;
-      v.y = (v.y - o.y) + n.y;
+  const int g = mc.g;
+  if constexpr (!F32) {
+    double2 *skg = CA.sk + ((size_t)chain * kMaxG + g) * CA.nkmax;
+    const double2 *snew = CA.snew + (size_t)chain * CA.nkmax;
+    const double2 *sold = CA.sold + (size_t)chain * CA.nkmax;
+    for (int k = threadIdx.x; k < S.nk; k += kThreads) {
+      double2 v = skg[k], n = snew[k];
+      if (mc.kind == 1) {
+        v.x += n.x;
+        v.y += n.y;
+      } else if (mc.kind == 2) {
+        v.x -= n.x;
+        v.y -= n.y;
+      } else {
+        double2 o = sold[k];
+        v.x = (v.x - o.x) + n.x;
+        v.y = (v.y - o.y) + n.y;
+      }
+      skg[k] = v;
     }
-    skg[k] = v;
-    if constexpr (F32) refresh_mirror<F32>(S, CA, chain, k);
+  } else {
+    float4 *skg = CA.skdf + ((size_t)chain * kMaxG + g) * CA.nkmax;
+    const float2 *snew = CA.snew32 + (size_t)chain * CA.nkmax;
+    const float2 *sold = CA.sold32 + (size_t)chain * CA.nkmax;
+    for (int k = threadIdx.x; k < S.nk; k += kThreads) {
+      float4 v = skg[k];
+      float2 n = snew[k];
+      if (mc.kind == 1) {
+        df_inc(v.x, v.z, n.x);
+        df_inc(v.y, v.w, n.y);
+      } else if (mc.kind == 2) {
+        df_inc(v.x, v.z, -n.x);
+        df_inc(v.y, v.w, -n.y);
+      } else {
+        float2 o = sold[k];
+        df_inc(v.x, v.z, -o.x);
+        df_inc(v.y, v.w, -o.y);
+        df_inc(v.x, v.z, n.x);
+        df_inc(v.y, v.w, n.y);
+      }
+      skg[k] = v;
+    }
   }
   // molecule order and coordinates
   int *ord = CA.ord + ((size_t)chain * kMaxG + g) * CA.cap;
   int *freel = CA.freel + ((size_t)chain * kMaxG + g) * CA.cap;
-  __shared__ int s_slot;
   if (threadIdx.x == 0) {
     int slot = mc.slot;
     if (mc.kind == 1) {
@@ -745,10 +919,10 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
       }
       if (slot >= 0) ord[H.nummols[g]] = slot;
     }
-    s_slot = slot;
+    B.flags[1] = slot;
   }
   __syncthreads();
-  int slot = s_slot;
+  const int slot = B.flags[1];
   if (mc.kind == 2) {
     // remove entry choice-1 from the order list (mc_moves.f:574-590)
     int n = H.nummols[g];
@@ -761,47 +935,38 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     for (int i = c0 + threadIdx.x; i < n - 1; i += kThreads) ord[i] = vals[cntv++];
     __syncthreads();
   }
-  if (slot >= 0 && (mc.kind == 1 || mc.kind >= 3) && threadIdx.x < G.ns) {
-    int s = threadIdx.x;
+  if (slot >= 0 && (mc.kind == 1 || mc.kind >= 3) && threadIdx.x < 3 * G.ns) {
+    int s = threadIdx.x / 3, d = threadIdx.x % 3;
     size_t b = gslot_base(CA, chain, g, slot) + s;
-    for (int d = 0; d < 3; ++d) CA.gpos[b * 3 + d] = mc.pos[0][s][d];
-    float hx = (float)mc.pos[0][s][0], hy = (float)mc.pos[0][s][1], hz = (float)mc.pos[0][s][2];
-    CA.ghi[b] = make_float4(hx, hy, hz, (float)G.q[s]);
-    CA.glo[b] = make_float4((float)(mc.pos[0][s][0] - hx), (float)(mc.pos[0][s][1] - hy),
-                            (float)(mc.pos[0][s][2] - hz), 0.f);
+    double v = mc.pos[0][s][d];
+    CA.gpos[b * 3 + d] = v;
+    float h = (float)v;
+    reinterpret_cast<float *>(CA.ghi + b)[d] = h;
+    reinterpret_cast<float *>(CA.glo + b)[d] = (float)(v - (double)h);
+    if (d == 0) {
+      reinterpret_cast<float *>(CA.ghi + b)[3] = (float)G.q[s];
+      reinterpret_cast<float *>(CA.glo + b)[3] = 0.f;
+    }
   }
   if (threadIdx.x == 0 && slot >= 0) {
     for (int m = 1; m <= S.maxmls; ++m) H.energy[m] += mc.delE[m];
     int mol = G.mol;
-    if (mc.kind == 1) {
-      H.chgsum_mol[mol] += mc.chgtmp;
-      H.sumchg += mc.chgtmp;
-      if (mc.surf_new) H.surfacemols[mol] += 1;
+    if (mc.kind == 1 || mc.kind == 2) {
+      int sg = mc.kind == 1 ? 1 : -1;
+      H.chgsum_mol[mol] += sg * mc.chgtmp;
+      H.sumchg += sg * mc.chgtmp;
+      if (mc.surf_new) H.surfacemols[mol] += sg;
       for (int s = 0; s < G.ns; ++s) {
         int ka = G.type[s];
-        H.numtyp[ka]++;
-        H.numtyp_mol[mol][ka]++;
+        H.numtyp[ka] += sg;
+        H.numtyp_mol[mol][ka] += sg;
         if (G.frz[s]) {
-          H.numfrz[ka]++;
-          H.numfrz_mol[mol][ka]++;
+          H.numfrz[ka] += sg;
+          H.numfrz_mol[mol][ka] += sg;
         }
       }
-      H.nummols[g]++;
-    } else if (mc.kind == 2) {
-      H.chgsum_mol[mol] -= mc.chgtmp;
-      H.sumchg -= mc.chgtmp;
-      if (mc.surf_new) H.surfacemols[mol] -= 1;
-      for (int s = 0; s < G.ns; ++s) {
-        int ka = G.type[s];
-        H.numtyp[ka]--;
-        H.numtyp_mol[mol][ka]--;
-        if (G.frz[s]) {
-          H.numfrz[ka]--;
-          H.numfrz_mol[mol][ka]--;
-        }
-      }
-      H.nummols[g]--;
-      freel[H.nfree[g]++] = slot;
+      H.nummols[g] += sg;
+      if (mc.kind == 2) freel[H.nfree[g]++] = slot;
     } else {
       // surface molecule tally of a displacement (gcmc.f:1900-1906)
       if (mc.surf_old && !mc.surf_new) {

@@ -55,7 +55,8 @@ struct System {
   std::vector<int> numtyp_fw, numfrz_fw;           // [atype]
   // control
   double temp = 0, rcut = 0, rvdw = 0, initdelr = 0, alpha = 0, eps = 0;
-  double overlap_sq = 2.25, surftol = 0.0, beta = 0, epsq = 1.0;
+  // overlap distance (default 1.5 A, gcmc.f:153); squared after CONTROL
+  double overlap_sq = 1.5, surftol = 0.0, beta = 0, epsq = 1.0;
   int kmax[3] = {0, 0, 0};
   int mcsteps = 1, eqsteps = 0, nwind = 1, nwindsteps = 1, nnumg = 1;
   int minchk = 1;

@@ -93,6 +93,7 @@ typedef struct {
   double fugacity[FMC_MAX_GUEST_TYPES]; /* Pa */
   double ewald3en[FMC_MAX_GUEST_TYPES]; /* per guest type, internal units */
   int mcsteps, eqsteps, nwindsteps;
+  double overlap;   /* overlap distance (A) of the trial-position test */
 } fmc_system_info;
 
 int fmc_system_get_info(const fmc_system *sys, fmc_system_info *info);

@@ -101,10 +101,10 @@ class Oracle:
         return rc
 
     def setup_energies(self):
-        out = (C.c_double * 12)()
+        out = (C.c_double * 13)()
         self.lib.orc_setup_energies(self._h, out)
         keys = ["vdw", "ecoul", "dlpoly", "ewald1", "alpha", "kmax1", "kmax2", "kmax3",
-                "newld", "volm", "engunit", "sumchg"]
+                "newld", "volm", "engunit", "sumchg", "overlap"]
         return dict(zip(keys, out[:]))
 
     def seed(self, s: int):

@@ -2892,6 +2892,7 @@ void orc_setup_energies(const orc_sim *h, double *out) {
   out[9] = s.volm;
   out[10] = s.engunit;
   out[11] = s.sumchg;
+  out[12] = std::sqrt(s.overlap);
 }
 
 void orc_seed(orc_sim *h, long long seed) {

@@ -39,7 +39,8 @@ void orc_destroy(orc_sim *s);
  * out[1]=electrostatic ecoul/engunit, out[2]=DL_POLY energy/engunit,
  * out[3]=ewald1 reciprocal sum (internal units), out[4]=alpha,
  * out[5]=kmax1, out[6]=kmax2, out[7]=kmax3, out[8]=newld (k-vector count),
- * out[9]=volume, out[10]=engunit, out[11]=sumchg. */
+ * out[9]=volume, out[10]=engunit, out[11]=sumchg, out[12]=overlap
+ * distance (A). */
 void orc_setup_energies(const orc_sim *s, double *out);
 
 /* Seed the MZT generator deterministically.  The reference seeds from the

@@ -46,6 +46,7 @@ def test_setup_matches_oracle(fmc_lib, oracle_lib, inputs_dir, which):
     assert inf.sumchg == o["sumchg"]
     assert inf.volm == o["volm"]
     assert inf.engunit == o["engunit"]
+    assert inf.overlap == o["overlap"] == 1.5
 
 
 def test_tables_match_oracle(fmc_lib, oracle_lib, inputs_dir):
