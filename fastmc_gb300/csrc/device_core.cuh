@@ -26,7 +26,7 @@
 
 namespace fmcdev {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxS = 8;    // sites per guest
 constexpr int kMaxG = 4;    // guest types

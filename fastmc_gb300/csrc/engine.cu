@@ -103,14 +103,18 @@ __device__ void block_copy(T *dst, const T *src) {
 template <bool F32>
 __global__ void __launch_bounds__(kThreads, 1)
     chain_kernel(const SysDev *__restrict__ systems, ChainHdr *hdrs, ChainArrays CA,
-                 MoveCtx *gctx, LogRec *logs, int logcap, int nmoves, int mode) {
+                 MoveCtx *gctx, LogRec *logs, int logcap, int nmoves, int mode,
+                 const double *__restrict__ ctl_fuga) {
   extern __shared__ __align__(16) unsigned char dyn[];
   BlockShared<F32> &B = *reinterpret_cast<BlockShared<F32> *>(dyn);
   const int chain = blockIdx.x;
   block_copy(&B.H, hdrs + chain);
   __syncthreads();
   block_copy(&B.S, systems + B.H.system);
-  if (threadIdx.x == 0) B.flags[0] = 0;
+  if (threadIdx.x == 0) {
+    B.flags[0] = 0;
+    if (ctl_fuga && mode == kModeMoves) B.H.fuga[0] = ctl_fuga[chain];  // host control block
+  }
   __syncthreads();
   int st = 0;
   if (mode == kModeMoves) {
@@ -611,6 +615,7 @@ struct Chains {
   DBuf<float4> skdf;
   DBuf<MoveCtx> ctx;
   DBuf<LogRec> logs;
+  DBuf<double> ctl_fuga;
   ChainArrays CA{};
   int nchains = 0, precision = 0, logcap = 0, maxmls = 0;
   cudaStream_t stream = nullptr;
@@ -618,6 +623,7 @@ struct Chains {
   cudaGraphExec_t graph = nullptr;
   int graph_moves = -1;
   size_t smem = 0;
+  bool headers_stale = true;  // host_hdr no longer mirrors the device headers
   double last_ms = 0.0;
   long long last_evals = 0, last_moves = 0;
   std::vector<ChainHdr> host_hdr;
@@ -630,13 +636,14 @@ struct Chains {
   }
 
   void launch(int mode, int nmoves) {
+    headers_stale = true;
     dim3 grid(nchains), block(kThreads);
     if (precision == FMC_PREC_FP32)
       chain_kernel<true><<<grid, block, smem, stream>>>(sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
-                                                        nmoves, mode);
+                                                        nmoves, mode, ctl_fuga.p);
     else
       chain_kernel<false><<<grid, block, smem, stream>>>(sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
-                                                         nmoves, mode);
+                                                         nmoves, mode, ctl_fuga.p);
     FMC_CUDA(cudaGetLastError());
   }
 
@@ -647,6 +654,7 @@ struct Chains {
     FMC_CUDA(cudaMemcpyAsync(host_hdr.data(), hdr.p, nchains * sizeof(ChainHdr),
                              cudaMemcpyDeviceToHost, stream));
     sync();
+    headers_stale = false;
   }
 
   void check_status() {
@@ -696,6 +704,11 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
     hh.push_back(initial_header(*systems[si], si, seed, &fu));
   }
   C.hdr.upload(hh);
+  {
+    std::vector<double> f(nchains);
+    for (int c = 0; c < nchains; ++c) f[c] = hh[c].fuga[0];
+    C.ctl_fuga.upload(f);
+  }
   ChainArrays &CA = C.CA;
   CA.cap = cap;
   CA.nkmax = nkmax;
@@ -1260,6 +1273,7 @@ int fmc_batch_set_log(fmc_batch *b, int cap) {
     FMC_CUDA(cudaMemcpy(hh.data(), C.hdr.p, C.nchains * sizeof(ChainHdr), cudaMemcpyDeviceToHost));
     for (auto &h : hh) h.log_n = 0;
     FMC_CUDA(cudaMemcpy(C.hdr.p, hh.data(), C.nchains * sizeof(ChainHdr), cudaMemcpyHostToDevice));
+    C.headers_stale = true;
     if (C.graph) {
       cudaGraphExecDestroy(C.graph);
       C.graph = nullptr;
@@ -1284,8 +1298,7 @@ static void run_cycle(Chains &C, int nmoves) {
     cudaGraphDestroy(g);
     C.graph_moves = nmoves;
   }
-  std::vector<long long> e0(C.nchains), m0(C.nchains);
-  C.pull_headers();
+  if ((int)C.host_hdr.size() != C.nchains || C.headers_stale) C.pull_headers();
   long long evals0 = 0, moves0 = 0;
   for (auto &h : C.host_hdr) {
     evals0 += h.evals;
@@ -1322,13 +1335,9 @@ int fmc_batch_run_cycle(fmc_batch *b, int nmoves, const double *host_fugacity,
   return guard([&] {
     if (!b) raise(FMC_ERR_ARG, "null batch");
     Chains &C = b->C;
-    if (host_fugacity) {
-      // patch the per-chain fugacities in the device headers
-      C.pull_headers();
-      for (int c = 0; c < C.nchains; ++c) C.host_hdr[c].fuga[0] = host_fugacity[c];
-      FMC_CUDA(cudaMemcpyAsync(C.hdr.p, C.host_hdr.data(), C.nchains * sizeof(ChainHdr),
+    if (host_fugacity)  // per-chain fugacity of guest 1, applied at the cycle start
+      FMC_CUDA(cudaMemcpyAsync(C.ctl_fuga.p, host_fugacity, C.nchains * sizeof(double),
                                cudaMemcpyHostToDevice, C.stream));
-    }
     run_cycle(C, nmoves);
     if (host_stats) fill_stats(C, host_stats);
     return FMC_OK;

@@ -927,7 +927,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     // remove entry choice-1 from the order list (mc_moves.f:574-590)
     int n = H.nummols[g];
     int c0 = mc.choice - 1;
-    int vals[16];  // capacity <= 4096 = 16 * kThreads
+    int vals[8];  // capacity <= 4096 = 8 * kThreads
     int cntv = 0;
     for (int i = c0 + threadIdx.x; i < n - 1; i += kThreads) vals[cntv++] = ord[i + 1];
     __syncthreads();
