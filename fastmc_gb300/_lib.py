@@ -12,6 +12,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libfastmc_gb300.so")
 
 FMC_OK = 0
+FMC_ERR_ARG = 1
+FMC_ERR_CUDA = 2
+FMC_ERR_CAPACITY = 3
+FMC_ERR_INPUT = 4
+FMC_ERR_DEVICE = 5
+FMC_ERR_STATE = 6
+FMC_ERR_NODEVICE = 7
 FMC_PREC_FP64 = 0
 FMC_PREC_FP32 = 1
 MAX_MOLTYPES = 8
@@ -83,6 +90,7 @@ SIGNATURES = {
     "fmc_plain_create": (C.c_int, [vp, C.c_int, C.c_int, pp]),
     "fmc_plain_destroy": (C.c_int, [vp]),
     "fmc_full_ewald": (C.c_int, [vp, dp]),
+    "fmc_full_ewald_noalloc": (C.c_int, [vp, dp]),
     "fmc_insertion": (C.c_int, [vp, C.c_int, dp, C.POINTER(MoveResult)]),
     "fmc_deletion": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(MoveResult)]),
     "fmc_displace": (C.c_int, [vp, C.c_int, C.c_int, dp, C.POINTER(MoveResult)]),

@@ -3,9 +3,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -792,6 +794,127 @@ void fill_stats(const Chains &C, fmc_chain_stats *out) {
   }
 }
 
+
+// ------------------------------------ full Ewald sum without allocation
+// fmc_full_ewald_noalloc recomputes what fmc_full_ewald does without any
+// device allocation.  Its scratch -- one FP64 partial energy per block of
+// kKB k-vectors, then the total -- is this fixed array in the module's
+// static device memory, shared by every engine on a device.  Each call
+// writes every word it later reads (partials first, then the total), so
+// nothing in it has to start at zero; two calls running at the same time on
+// one device would overwrite each other's partials, which is why the host
+// side serialises its calls with g_noalloc_mu and waits for the kernels
+// before it returns.
+constexpr int kNoallocScratchDoubles = 8192;  // 64 KiB: up to 8191 blocks = 65528 k-vectors
+static __device__ __align__(256) double g_ewald_scratch[kNoallocScratchDoubles];
+
+struct GuestSites {
+  int ntp;
+  int n[kMaxG];             // molecules of each guest type
+  int ns[kMaxG];            // sites per molecule
+  double q[kMaxG][kMaxS];   // site charges
+};
+
+// Variant of structure_factor_kernel for the guests of chain 0: each block
+// takes kKB k-vectors, sums every guest type's S(k) over that type's atoms in
+// molecule order straight from the chain's coordinate storage (the same atom
+// order and per-thread striding as the staged-copy path), writes it to the
+// chain's running sums (sk in FP64, skdf as FP32 hi/lo pairs; the other
+// pointer is null), and leaves sum_j akk |S_fw + sum_g S_g|^2 of its
+// k-vectors in partial[block].
+__global__ void __launch_bounds__(kThreads) guest_ewald_kernel(
+    const double *__restrict__ gpos, const int *__restrict__ ord, int cap, GuestSites gs,
+    const int4 *__restrict__ klmn, int nk, Rcell rc, const double *__restrict__ akk,
+    const double2 *__restrict__ skfw, double2 *sk, float4 *skdf, int nkmax,
+    double *__restrict__ partial) {
+  __shared__ double red[kWarps * 2 * kKB + 2 * kKB];
+  __shared__ double eterm[kKB];
+  const int k0 = blockIdx.x * kKB;
+  const int jt = threadIdx.x;
+  int4 kv[kKB];
+  for (int j = 0; j < kKB; ++j) kv[j] = (k0 + j < nk) ? klmn[k0 + j] : make_int4(0, 0, 0, 0);
+  double2 tot = make_double2(0.0, 0.0);
+  if (jt < kKB && k0 + jt < nk) tot = skfw[k0 + jt];
+  for (int g = 0; g < gs.ntp; ++g) {
+    double ax[kKB], ay[kKB];
+    for (int j = 0; j < kKB; ++j) ax[j] = ay[j] = 0.0;
+    const int ns = gs.ns[g], na = gs.n[g] * ns;
+    for (int a = threadIdx.x; a < na; a += kThreads) {
+      const int i = a / ns, sidx = a - i * ns;
+      const int slot = ord[(size_t)g * cap + i];
+      const double *p = gpos + (((size_t)g * cap + slot) * kMaxS + sidx) * 3;
+      const double x = p[0], y = p[1], z = p[2], q = gs.q[g][sidx];
+      double f[3];
+      for (int d = 0; d < 3; ++d) f[d] = rc.r[d] * x + rc.r[3 + d] * y + rc.r[6 + d] * z;
+      for (int j = 0; j < kKB; ++j) {
+        double t = double(kv[j].x) * f[0] + double(kv[j].y) * f[1] + double(kv[j].z) * f[2];
+        t -= rint(t);
+        double sn, cs;
+        sincospi(2.0 * t, &sn, &cs);
+        ax[j] += q * cs;
+        ay[j] += q * sn;
+      }
+    }
+    double vals[2 * kKB];
+    for (int j = 0; j < kKB; ++j) {
+      vals[2 * j] = ax[j];
+      vals[2 * j + 1] = ay[j];
+    }
+    block_sum(vals, 2 * kKB, red);
+    if (jt < kKB && k0 + jt < nk) {
+      const double *R = red + kWarps * 2 * kKB;
+      const double sx = R[2 * jt], sy = R[2 * jt + 1];
+      const size_t o = (size_t)g * nkmax + k0 + jt;
+      if (sk) sk[o] = make_double2(sx, sy);
+      if (skdf) {
+        const float hx = (float)sx, hy = (float)sy;
+        skdf[o] = make_float4(hx, hy, (float)(sx - hx), (float)(sy - hy));
+      }
+      tot.x += sx;
+      tot.y += sy;
+    }
+  }
+  if (jt < kKB) eterm[jt] = (k0 + jt < nk) ? akk[k0 + jt] * (tot.x * tot.x + tot.y * tot.y) : 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double e = 0.0;
+    for (int j = 0; j < kKB; ++j) e += eterm[j];
+    partial[blockIdx.x] = e;
+  }
+}
+
+// Sum of n partials into *out (one block).
+__global__ void __launch_bounds__(kThreads) partial_sum_kernel(const double *__restrict__ partial,
+                                                               int n, double *out) {
+  __shared__ double red[kWarps + 1];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += kThreads) v += partial[i];
+  block_sum(&v, 1, red);
+  if (threadIdx.x == 0) *out = red[kWarps];
+}
+
+std::mutex g_noalloc_mu;
+constexpr int kNoallocDevices = 64;
+double *g_noalloc_addr[kNoallocDevices] = {};
+
+// Device address of g_ewald_scratch on the current device, looked up once
+// per device (the first call on a device is the one that may load the
+// module there).  Called with g_noalloc_mu held.
+double *noalloc_scratch() {
+  int dev = -1;
+  FMC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoallocDevices) raise(FMC_ERR_ARG, "device ordinal out of range");
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_ewald_scratch);
+    if (e != cudaSuccess || !p)
+      raise(FMC_ERR_CUDA, std::string("cudaGetSymbolAddress of the static Ewald scratch: ") +
+                              cudaGetErrorString(e));
+    g_noalloc_addr[dev] = static_cast<double *>(p);
+  }
+  return g_noalloc_addr[dev];
+}
+
 }  // namespace fmc
 
 // =================================================================== C ABI
@@ -1393,6 +1516,80 @@ int fmc_batch_last_timing(const fmc_batch *b, double *kernel_ms, int64_t *evals,
     if (kernel_ms) *kernel_ms = b->C.last_ms;
     if (evals) *evals = b->C.last_evals;
     if (moves) *moves = b->C.last_moves;
+    return FMC_OK;
+  });
+}
+
+// Same result and side effect as fmc_full_ewald, with no device allocation:
+// the kernels read the guests where the chain keeps them and use the static
+// scratch above.  Limit: newld <= 65528 k-vectors (FMC_ERR_ARG beyond).
+int fmc_full_ewald_noalloc(fmc_plain *h, double *out4) {
+  return guard([&] {
+    if (!h || !out4) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = h->C;
+    const System &s = *C.hsys[0];
+    const DevSystem &D = *C.sys[0];
+    const int nk = s.newld;
+    const int nb = (nk + kKB - 1) / kKB;
+    if (nb + 1 > kNoallocScratchDoubles) {
+      char buf[256];
+      std::snprintf(buf, sizeof buf,
+                    "fmc_full_ewald_noalloc: %d k-vectors need %d partial sums but its static "
+                    "scratch holds %d (at most %d k-vectors); use fmc_full_ewald",
+                    nk, nb, kNoallocScratchDoubles - 1, (kNoallocScratchDoubles - 1) * kKB);
+      raise(FMC_ERR_ARG, buf);
+    }
+    if (s.ntpguest > kMaxG) raise(FMC_ERR_ARG, "too many guest types");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    double *scr = noalloc_scratch();
+    // guest counts and system charge of chain 0, straight from its header
+    int nummols[kMaxG] = {};
+    double sumchg = 0.0;
+    const char *hdr0 = reinterpret_cast<const char *>(C.hdr.p);
+    FMC_CUDA(cudaMemcpyAsync(nummols, hdr0 + offsetof(ChainHdr, nummols), sizeof nummols,
+                             cudaMemcpyDeviceToHost, C.stream));
+    FMC_CUDA(cudaMemcpyAsync(&sumchg, hdr0 + offsetof(ChainHdr, sumchg), sizeof sumchg,
+                             cudaMemcpyDeviceToHost, C.stream));
+    C.sync();
+    GuestSites gs{};
+    gs.ntp = s.ntpguest;
+    double sq = 0.0, e3 = 0.0;
+    const MolType &fw = s.mol[s.fw_mol];
+    for (int m = 0; m < fw.nummols; ++m)
+      for (int i = 0; i < fw.natoms; ++i) sq += fw.chg[i] * fw.chg[i];
+    for (int g = 0; g < s.ntpguest; ++g) {
+      const MolType &gm = s.mol[s.locguest[g + 1]];
+      if (gm.natoms > kMaxS) raise(FMC_ERR_ARG, "too many guest sites");
+      if (nummols[g] < 0 || nummols[g] > C.CA.cap) raise(FMC_ERR_DEVICE, "guest count out of range");
+      gs.n[g] = nummols[g];
+      gs.ns[g] = gm.natoms;
+      for (int i = 0; i < gm.natoms; ++i) gs.q[g][i] = gm.chg[i];
+      for (int m = 0; m < nummols[g]; ++m)
+        for (int i = 0; i < gm.natoms; ++i) sq += gm.chg[i] * gm.chg[i];
+      e3 += nummols[g] * s.ewald3en[s.locguest[g + 1]];
+    }
+    double eng = 0.0;
+    if (nk > 0) {
+      Rcell rc;
+      for (int i = 0; i < 9; ++i) rc.r[i] = D.d.rcell[i];
+      const bool f32 = C.precision == FMC_PREC_FP32;
+      guest_ewald_kernel<<<nb, kThreads, 0, C.stream>>>(
+          C.gpos.p, C.ord.p, C.CA.cap, gs, D.klmn.p, nk, rc, D.akk.p, D.skfw.p,
+          f32 ? nullptr : C.sk.p, f32 ? C.skdf.p : nullptr, C.CA.nkmax, scr);
+      FMC_CUDA(cudaGetLastError());
+      partial_sum_kernel<<<1, kThreads, 0, C.stream>>>(scr, nb, scr + nb);
+      FMC_CUDA(cudaGetLastError());
+      FMC_CUDA(cudaMemcpyAsync(&eng, scr + nb, sizeof eng, cudaMemcpyDeviceToHost, C.stream));
+      C.sync();
+    }
+    const double r4 = fmc::kR4pie0 / s.epsq;
+    const double sic = -r4 * s.alpha * sq / fmc::kSqrPi;
+    const double qfix = -(0.5 * fmc::kPi * r4) * ((sumchg / s.alpha) * (sumchg / s.alpha) / s.volm);
+    const double ew1 = 2.0 * (2.0 * fmc::kPi / s.volm) * r4 * eng + sic + qfix;
+    out4[0] = (ew1 - e3) / s.engunit;
+    out4[1] = ew1;
+    out4[2] = sic;
+    out4[3] = qfix;
     return FMC_OK;
   });
 }

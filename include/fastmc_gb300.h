@@ -132,6 +132,27 @@ int fmc_plain_destroy(fmc_plain *h);
  * out[3] = qfix.  Resets the device S(k) to the recomputed values. */
 int fmc_full_ewald(fmc_plain *h, double *out4);
 
+/* The same recomputation, result and S(k) reset as fmc_full_ewald, made
+ * without allocating any device memory.  It has no counterpart in the
+ * reference (whose ewald1 runs on the host); it is for hosts that cannot let
+ * a library allocate in the middle of a run: fmc_full_ewald stages the
+ * guests in device buffers it allocates and frees on every call, and a
+ * device allocation or free can wait for all work on the device or fail
+ * once a host has handed the device's memory to its own allocator.
+ *   - Scratch is a fixed 64 KiB array in the library's static device memory
+ *     (one partial sum per 8 k-vectors): systems with more than 65528
+ *     k-vectors (newld) are refused with FMC_ERR_ARG before anything runs.
+ *   - The first call on a device looks up that array's device address
+ *     (cudaGetSymbolAddress, with the engine's device current), which may
+ *     load the library's kernels on that device; make that first call
+ *     before any stream capture on the device.
+ *   - Every engine on a device shares the array.  Calls through this entry
+ *     point are serialised by a lock held until their kernels finish;
+ *     anything else that ran these kernels on the same array at the same
+ *     time would race with them.
+ * Call with the device the engine was created on current. */
+int fmc_full_ewald_noalloc(fmc_plain *h, double *out4);
+
 /* insertion (mc_moves.f:150-276) of guest type iguest at site coordinates
  * xyz (natms triples x,y,z). */
 int fmc_insertion(fmc_plain *h, int iguest, const double *xyz,
