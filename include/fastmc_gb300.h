@@ -10,8 +10,7 @@
  * Three groups of entry points:
  *  1. Host set-up.  fmc_system_load reads FIELD, CONFIG and CONTROL and
  *     builds the tables and constants that the reference computes at start
- *     (gcmc.f:203-590).  A Fortran host that already holds these arrays
- *     replaces it by fmc_system_create_from_arrays.
+ *     (gcmc.f:203-590) from the same input files the reference reads.
  *  2. Per-move drop-in ("plain" mode).  The device mirrors the host's
  *     guest coordinates and structure factor; each call evaluates one trial
  *     move and leaves s(k) on the device for the commit, exactly like
@@ -29,8 +28,8 @@
 extern "C" {
 #endif
 
-/* status codes; positive values map to the reference's error() codes in
- * INTEGRATION.md */
+/* status codes; a Fortran caller turns a positive value into a call of
+ * the reference's error() routine with a code of its choosing */
 #define FMC_OK 0
 #define FMC_ERR_ARG 1      /* invalid argument or handle */
 #define FMC_ERR_CUDA 2     /* CUDA runtime failure (message has details) */
@@ -42,7 +41,7 @@ extern "C" {
 
 /* arithmetic of the pair and k-space terms */
 #define FMC_PREC_FP64 0 /* everything FP64: parity mode */
-#define FMC_PREC_FP32 1 /* FP32 terms, FP64 accumulation, FP64 S(k) */
+#define FMC_PREC_FP32 1 /* FP32 terms; sums and S(k) as FP32 hi/lo pairs */
 
 /* move kinds (the reference's insert / delete / displace flags) */
 #define FMC_MOVE_INSERT 1
