@@ -310,8 +310,7 @@ def run_ours(args, rank, world, local_rank):
     achieved = per_launch_bytes / mean_launch_s / 1e9
     peak, peak_kind = measured_peak_hbm()
 
-    h2d = fug.nbytes
-    d2h = len(specs) * 3096  # one chain header per chain (statistics)
+    h2d, d2h = batch.cycle_bytes()  # fugacities up, chain state records down
 
     if rank == 0:
         ovl = sum(after[c].overlap_exits - before[c].overlap_exits for c in range(len(specs)))

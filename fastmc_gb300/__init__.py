@@ -1,7 +1,7 @@
 """fastmc_gb300: GB300-native (sm_103a) GCMC trial-move energy path.
 
 The hot path (pair energies over cell columns, Ewald k-space, Metropolis
-and the FP64 structure-factor commit) runs as hand-written CUDA kernels
+and the structure-factor commit) runs as hand-written CUDA kernels
 behind the C ABI in include/fastmc_gb300.h.  This package holds the build
 script, the ctypes binding and a small Python API; see api.py.
 """

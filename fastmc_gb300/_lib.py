@@ -111,6 +111,7 @@ SIGNATURES = {
     "fmc_batch_get_coords": (C.c_int, [vp, C.c_int, dp, C.c_int, ip]),
     "fmc_batch_get_sk": (C.c_int, [vp, C.c_int, dp, C.c_int]),
     "fmc_batch_last_timing": (C.c_int, [vp, dp, i64p, i64p]),
+    "fmc_batch_cycle_bytes": (C.c_int, [vp, i64p, i64p]),
 }
 
 _lib = None

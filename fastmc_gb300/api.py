@@ -200,6 +200,13 @@ class Batch:
         L.check(L.load().fmc_batch_get_sk(self._h, chain, out.ctypes.data_as(L.dp), out.size))
         return out.reshape(nk, maxmls + 1, 2)
 
+    def cycle_bytes(self):
+        """(host->device, device->host) bytes of one run() call with a
+        fugacity array."""
+        h, d = C.c_int64(), C.c_int64()
+        L.check(L.load().fmc_batch_cycle_bytes(self._h, C.byref(h), C.byref(d)))
+        return h.value, d.value
+
     def last_timing(self):
         ms = C.c_double()
         ev = C.c_int64()

@@ -1,0 +1,9 @@
+// chain_f32_g1.cu -- one instantiation of the chain kernel (F32 = true, GN = 1).
+#include "chain_kernel.cuh"
+
+namespace fmc {
+template cudaError_t launch_chain<true, 1>(dim3, size_t, cudaStream_t, const SysDev *,
+                                               ChainHdr *, const ChainArrays &, MoveCtx *,
+                                               LogRec *, int, int, int, const double *);
+template cudaError_t set_chain_smem<true, 1>(size_t);
+}  // namespace fmc

@@ -1,0 +1,9 @@
+// chain_f64.cu -- one instantiation of the chain kernel (F32 = false, GN = kMaxG).
+#include "chain_kernel.cuh"
+
+namespace fmc {
+template cudaError_t launch_chain<false, kMaxG>(dim3, size_t, cudaStream_t, const SysDev *,
+                                               ChainHdr *, const ChainArrays &, MoveCtx *,
+                                               LogRec *, int, int, int, const double *);
+template cudaError_t set_chain_smem<false, kMaxG>(size_t);
+}  // namespace fmc

@@ -1,0 +1,145 @@
+// chain_kernel.cuh -- the persistent chain kernel (one CTA per chain) and
+// the host wrappers each of its instantiations exports.  Every
+// instantiation lives in its own translation unit (chain_*.cu) so they
+// compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "engine.cuh"
+
+namespace fmc {
+using namespace fmcdev;
+
+// Modes of the chain kernel.
+constexpr int kModeMoves = 0;   // nmoves main-loop iterations
+constexpr int kModeCreate = 1;  // "create molecules" pre-loading
+constexpr int kModeEval = 2;    // evaluate the move in gctx (per-move ABI)
+constexpr int kModeCommit = 3;  // decide with gctx.rande and commit
+
+template <class T>
+__device__ void block_copy(T *dst, const T *src) {
+  static_assert(sizeof(T) % 4 == 0, "copy granularity");
+  const int *s = reinterpret_cast<const int *>(src);
+  int *d = reinterpret_cast<int *>(dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(T) / 4); i += kThreads) d[i] = s[i];
+}
+
+template <bool F32, int GN>
+__global__ void __launch_bounds__(kThreads, 1)
+    chain_kernel(const SysDev *__restrict__ systems, ChainHdr *hdrs, ChainArrays CA,
+                 MoveCtx *gctx, LogRec *logs, int logcap, int nmoves, int mode,
+                 const double *__restrict__ ctl_fuga) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  BlockShared<F32> &B = *reinterpret_cast<BlockShared<F32> *>(dyn);
+  const int chain = blockIdx.x;
+  block_copy(&B.H, hdrs + chain);
+  __syncthreads();
+  block_copy(&B.S, systems + B.H.system);
+  if (threadIdx.x == 0) {
+    B.flags[0] = 0;
+    if (ctl_fuga && mode == kModeMoves) B.H.fuga[0] = ctl_fuga[chain];  // host control block
+  }
+  __syncthreads();
+  int st = 0;
+  if (mode == kModeMoves) {
+    for (int it = 0; it < nmoves; ++it) {
+      propose(B, CA, chain, kPropMC, 0);
+      int full = 0;
+      if (B.mc.kind != 0) full = evaluate_any<F32, GN>(B, CA, chain, st);
+      if (threadIdx.x == 0) {
+        decide(B, true);
+        if (full) B.H.evals += B.mc.npos;
+        else if (B.mc.overlap) B.H.overlap_exits++;
+        if (logcap > 0 && B.H.log_n < logcap) {
+          LogRec &L = logs[(size_t)chain * logcap + B.H.log_n];
+          L.move = B.mc.kind;
+          L.iguest = B.mc.g + 1;
+          L.choice = B.mc.choice;
+          L.overlap = B.mc.overlap;
+          L.accepted = B.mc.accepted;
+          L.estep = B.mc.estep;
+          L.rande = B.mc.rande;
+          for (int s = 0; s < 3 && s < B.mc.ns; ++s)
+            for (int d = 0; d < 3; ++d)
+              L.newxyz[3 * s + d] = F32 ? (double)B.ev.phi[0][s][d] + (double)B.ev.plo[0][s][d]
+                                        : B.mc.pos[0][s][d];
+        }
+      }
+      __syncthreads();
+      commit(B, CA, chain, st);
+      if (threadIdx.x == 0) {
+        stats(B);
+        if (logcap > 0 && B.H.log_n < logcap) {
+          logs[(size_t)chain * logcap + B.H.log_n].nmols_after = B.H.nummols[B.mc.g];
+          B.H.log_n++;
+        }
+      }
+      __syncthreads();
+    }
+  } else if (mode == kModeCreate) {
+    for (int g = 0; g < B.S.ntpguest; ++g) {
+      long long maxiter = 1000LL * B.S.g[g].insert0, iter = 0;
+      while (B.H.nummols[g] < B.S.g[g].insert0) {
+        if (iter >= maxiter) {  // insert_guests iteration cap (error 2320)
+          st |= kStCapacity;
+          break;
+        }
+        propose(B, CA, chain, kPropInsert, g);
+        evaluate_any<F32, GN>(B, CA, chain, st);
+        if (threadIdx.x == 0) B.mc.accepted = B.mc.overlap ? 0 : 1;
+        __syncthreads();
+        commit(B, CA, chain, st);
+        __syncthreads();
+        ++iter;
+      }
+    }
+  } else if (mode == kModeEval) {
+    if (threadIdx.x == 0) B.mc = gctx[chain];
+    __syncthreads();
+    propose(B, CA, chain, kPropExternal, 0);
+    int full = 0;
+    if (B.mc.kind != 0) full = evaluate_any<F32, GN>(B, CA, chain, st);
+    if (threadIdx.x == 0) {
+      B.mc.evaluated = 1;
+      B.mc.accepted = 0;
+      (void)full;
+      gctx[chain] = B.mc;
+    }
+  } else if (mode == kModeCommit) {
+    if (threadIdx.x == 0) {
+      B.mc = gctx[chain];
+      decide(B, false);
+    }
+    __syncthreads();
+    commit(B, CA, chain, st);
+    if (threadIdx.x == 0) {
+      B.mc.evaluated = 0;
+      gctx[chain] = B.mc;
+    }
+  }
+  if (st) atomicOr(&B.flags[0], st);
+  __syncthreads();
+  if (threadIdx.x == 0) B.H.status |= B.flags[0];
+  __syncthreads();
+  block_copy(hdrs + chain, &B.H);
+}
+
+
+// Launch and set-up of one instantiation, for the host side of the library.
+template <bool F32, int GN>
+cudaError_t launch_chain(dim3 grid, size_t smem, cudaStream_t stream, const SysDev *systems,
+                         ChainHdr *hdrs, const ChainArrays &CA, MoveCtx *gctx, LogRec *logs,
+                         int logcap, int nmoves, int mode, const double *ctl_fuga) {
+  chain_kernel<F32, GN><<<grid, kThreads, smem, stream>>>(systems, hdrs, CA, gctx, logs, logcap,
+                                                          nmoves, mode, ctl_fuga);
+  return cudaGetLastError();
+}
+
+template <bool F32, int GN>
+cudaError_t set_chain_smem(size_t smem) {
+  return cudaFuncSetAttribute(chain_kernel<F32, GN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
+}
+
+}  // namespace fmc

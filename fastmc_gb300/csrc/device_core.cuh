@@ -33,6 +33,7 @@ constexpr int kMaxG = 4;    // guest types
 constexpr int kMaxM = 8;    // molecule types
 constexpr int kMaxT = 16;   // atom types
 constexpr int kMaxKm = 40;  // kmax per axis + 1
+constexpr int kPlmMax = 6144;  // entries of the FP32 (l, m) phase table (48 KB)
 constexpr int kMaxSeg = 1536;
 
 // status word bits (ChainHdr::status)
@@ -42,6 +43,7 @@ constexpr int kStCapacity = 4;     // guest capacity exceeded
 constexpr int kStNonFinite = 8;    // non-finite energy
 constexpr int kStBadChoice = 16;   // molecule index out of range
 constexpr int kStKmax = 32;        // kmax beyond the shared tables
+constexpr int kStWait = 64;        // a bounded wait on an asynchronous copy ran out
 
 constexpr double kPi = 3.141592653589793;
 constexpr double kSqrPi = 1.7724538509055159;
@@ -63,6 +65,11 @@ struct GuestType {
   int type[kMaxS];         // atom type 1..ntpatm
   int frz[kMaxS];
   double ewald3en;
+  double chgea[kMaxS];     // q / epsq * r4pie0 per site (ewald2's charge factor)
+  float tmplf[kMaxS][3];   // centred template in FP32 (FP32 trial geometry)
+  float wf[kMaxS];         // mass fraction of each site (centre of mass)
+  float chgeaf[kMaxS];     // the same as an FP32 hi/lo pair
+  float chgeaf_lo[kMaxS];
   // constants of the energy expressions of this guest type
   double chgtmp;           // sum of site charges
   double engsic0;          // self-interaction -r4pie0/epsq*alpha*sum(q^2)/sqrt(pi)
@@ -103,14 +110,20 @@ struct SysDev {
   double rbox[3];          // 1 / L, the reference's aaa = 1/cell (images)
   float boxh[3], boxl[3];  // L as a float hi/lo pair
   float rboxf[3], rcszf[3], cszf[3];
+  float rboxf_lo[3];       // 1/L - rboxf
   float overlap_sqf, rc2f, rdrewdf, rdlrpotf;
+  float rdlrpotf_lo;       // rdlrpot - rdlrpotf (double-float bin index of close pairs)
   const int *cell_start;   // [nc0*nc1*nc2+1], z fastest
+  // the same cells padded to 2^cpad_log2 slots (empty slots far away):
+  // the overlap test reads a cell's atoms without reading cell_start first
+  int cpad_log2;
+  const float4 *cpad_hi, *cpad_lo;
   // tables
   int mxegrd;
   double rdrewd, rdlrpot;
   const double *erc;       // [mxegrd+3], 1-based
   const double *vvv;       // [ntab][mxegrd+3]
-  const float4 *ercq;      // per interval (A,B,C,0): value = A + p(B + pC)
+  const float4 *ercq;      // per interval (A,B,C,A_lo): value = A + p(B + pC), A_lo = v0 - A
   const float4 *vvvq;      // [ntab][mxegrd+3]
   int tabstride;           // mxegrd+3
   const int *pairtab;      // [(ntpatm+1)^2] -> table row or -1
@@ -121,6 +134,7 @@ struct SysDev {
   // k-space
   int nk, kmax[3];
   const int4 *klmn;        // (l,m,n,0)
+  const unsigned *kpk;     // l * (2 kmax_y + 1) + m + kmax_y | (n + 128) << 16
   const double *akk;
   const float *akk32;
   const double2 *skfw;     // framework S(k)
@@ -153,7 +167,11 @@ struct ChainHdr {
   long long disp_count[kMaxG], accept_disp[kMaxG], tran_count[kMaxG], accept_tran[kMaxG];
   long long rota_count[kMaxG], accept_rota[kMaxG];
   long long gcmccount, prodcount, rollcount;
-  int production, pad0;
+  int production;
+  int minchk_left;         // moves until gcmccount is next a multiple of minchk
+  int window_left;         // production moves until the next window ends
+  int pad_w;
+  long long pend;          // production moves not yet added to chainstats (FP32 path)
   double chainstats[kMaxG][6];
   double wsum;
   double wacc[kMaxG][8];
@@ -213,6 +231,55 @@ struct Acc {  // per-position partial sums
   double recip;
   double mix[kMaxM + 1];
 };
+
+// ------------------------------------------ bulk copies and mbarriers
+// One-dimensional bulk asynchronous copies global -> shared that complete
+// on an mbarrier (transaction count), and bounded waits on it.
+constexpr int kKT = kThreads;       // k-vectors per staged tile
+constexpr int kWaitLimit = 1 << 22; // try_wait polls before a wait gives up
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for the given phase parity; false if it did not complete in time.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+  for (int it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// Order this thread's generic-proxy global writes before later bulk copies
+// that read the same data.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async;" ::: "memory");
+}
 
 // ----------------------------------------------------------- MZT generator
 // duni (utility_pack.f:2768-2857): REAL*4 lagged subtract-with-borrow plus
@@ -450,71 +517,102 @@ struct AccT<true> {
   DF v;
   __device__ __forceinline__ void zero() { v.hi = v.lo = 0.f; }
   __device__ __forceinline__ void add(float x) { v.add(x); }
+  __device__ __forceinline__ void add_df(DF x) { v.add(x); }
 };
 
-// Per-position partial sums of one thread.
-template <bool F32>
+// Per-position partial sums of one thread, for up to GN guest types.  The
+// members are always addressed with compile-time indices so the whole set
+// stays in registers.
+template <bool F32, int GN>
 struct PosAcc {
+  static constexpr int kN = 4 + 3 * GN;  // values per position
   AccT<F32> e2fw, vdwfw, recip, mixfw;
-  AccT<F32> e2g[kMaxG], vdwg[kMaxG], mixg[kMaxG];
-  __device__ void zero() {
+  AccT<F32> e2g[GN], vdwg[GN], mixg[GN];
+  __device__ __forceinline__ void zero() {
     e2fw.zero();
     vdwfw.zero();
     recip.zero();
     mixfw.zero();
-    for (int g = 0; g < kMaxG; ++g) {
+#pragma unroll
+    for (int g = 0; g < GN; ++g) {
       e2g[g].zero();
       vdwg[g].zero();
       mixg[g].zero();
     }
   }
+  // value j of the reduction layout: e2fw, vdwfw, recip, mixfw, e2g[GN],
+  // vdwg[GN], mixg[GN]
+  __device__ __forceinline__ const AccT<F32> &at(int j) const {
+    if (j == 0) return e2fw;
+    if (j == 1) return vdwfw;
+    if (j == 2) return recip;
+    if (j == 3) return mixfw;
+    if (j < 4 + GN) return e2g[j - 4];
+    if (j < 4 + 2 * GN) return vdwg[j - 4 - GN];
+    return mixg[j - 4 - 2 * GN];
+  }
 };
 
-// Fixed-order block reduction of n accumulators per thread (n <= 32).
-// out[i] receives the block total as a double (valid after the call).
-__device__ inline void block_reduce(AccT<false> *v, int n, double *scratch, double *out) {
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int i = 0; i < n; ++i) {
-    double x = warp_sum(v[i].v);
-    if (lane == 0) scratch[w * 32 + i] = x;
+__device__ __forceinline__ double warp_total(const AccT<false> &a) { return warp_sum(a.v); }
+__device__ __forceinline__ DF warp_total(const AccT<true> &a) {
+  DF x = a.v;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DF y;
+    y.hi = __shfl_xor_sync(0xffffffffu, x.hi, o);
+    y.lo = __shfl_xor_sync(0xffffffffu, x.lo, o);
+    x.add(y);
   }
-  __syncthreads();
-  if (threadIdx.x < n) {
-    double s = 0.0;
-    for (int k = 0; k < kWarps; ++k) s += scratch[k * 32 + threadIdx.x];
-    out[threadIdx.x] = s;
-  }
-  __syncthreads();
+  return x;
 }
 
-__device__ inline void block_reduce(AccT<true> *v, int n, double *scratch, double *out) {
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float *sc = reinterpret_cast<float *>(scratch);
-  for (int i = 0; i < n; ++i) {
-    DF x = v[i].v;
+// Fixed-order block reduction of the partial sums of both positions:
+// out[p * kN + j] = block total of value j of position p (as a double).
+// Positions >= npos and guest types >= ng are skipped.
+template <bool F32, int GN>
+__device__ void block_reduce_pos(const PosAcc<F32, GN> &a0, const PosAcc<F32, GN> &a1, int npos,
+                                 int ng, double *scratch, double *out) {
+  constexpr int N = PosAcc<F32, GN>::kN;
+  static_assert(2 * N <= 32, "reduction scratch holds 32 values per warp");
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      DF y;
-      y.hi = __shfl_xor_sync(0xffffffffu, x.hi, o);
-      y.lo = __shfl_xor_sync(0xffffffffu, x.lo, o);
-      x.add(y);
-    }
+  for (int i = 0; i < 2 * N; ++i) {
+    const int p = i / N, j = i % N;
+    if (p >= npos) continue;
+    if (j >= 4 && (j - 4) % GN >= ng) continue;
+    const auto x = warp_total(p == 0 ? a0.at(j) : a1.at(j));
     if (lane == 0) {
-      sc[2 * (w * 32 + i)] = x.hi;
-      sc[2 * (w * 32 + i) + 1] = x.lo;
+      if constexpr (F32) {
+        float *sc = reinterpret_cast<float *>(scratch);
+        sc[2 * (w * 32 + i)] = x.hi;
+        sc[2 * (w * 32 + i) + 1] = x.lo;
+      } else {
+        scratch[w * 32 + i] = x;
+      }
     }
   }
   __syncthreads();
-  if (threadIdx.x < n) {
-    DF s;
-    s.hi = s.lo = 0.f;
-    for (int k = 0; k < kWarps; ++k) {
-      DF y;
-      y.hi = sc[2 * (k * 32 + threadIdx.x)];
-      y.lo = sc[2 * (k * 32 + threadIdx.x) + 1];
-      s.add(y);
+  const int i = threadIdx.x;
+  if (i < 2 * N) {
+    const int p = i / N, j = i % N;
+    double tot = 0.0;
+    if (p < npos && !(j >= 4 && (j - 4) % GN >= ng)) {
+      if constexpr (F32) {
+        const float *sc = reinterpret_cast<const float *>(scratch);
+        DF s;
+        s.hi = s.lo = 0.f;
+        for (int k = 0; k < kWarps; ++k) {
+          DF y;
+          y.hi = sc[2 * (k * 32 + i)];
+          y.lo = sc[2 * (k * 32 + i) + 1];
+          s.add(y);
+        }
+        tot = s.value();
+      } else {
+        for (int k = 0; k < kWarps; ++k) tot += scratch[k * 32 + i];
+      }
     }
-    out[threadIdx.x] = s.value();
+    out[i] = tot;
   }
   __syncthreads();
 }

@@ -31,6 +31,9 @@ struct EvalSmem {
   // power tables e^{i 2 pi j s_d}: [pos][site][axis][j]
   double2 pw64[F32 ? 1 : 2][F32 ? 1 : kMaxS][3][F32 ? 1 : kMaxKm];
   float2 pw32[F32 ? 2 : 1][F32 ? kMaxS : 1][3][F32 ? kMaxKm : 1];
+  // FP32 path: e^{i 2 pi (l s_x + m s_y)} per position and site, indexed
+  // [(p * ns + s) * nlm + l * (2 kmax_y + 1) + m + kmax_y], when it fits
+  float2 plm[F32 ? kPlmMax : 1];
   float fhi[2][kMaxS][3];   // fractional coordinates as float hi/lo pairs
   float flo[2][kMaxS][3];
   float cen[2][3];          // centre and bounding radius of each position
@@ -80,7 +83,8 @@ __device__ __forceinline__ float interp32(const float4 *tab, float r, float rd,
 struct SiteInfo {
   double q;      // site charge
   double chgea;  // q / epsq * r4pie0
-  float chgeaf;
+  float chgeaf;  // chgea as an FP32 hi/lo pair
+  float chgeaf_lo;
   float qf;
   int type;
 };
@@ -102,18 +106,88 @@ __device__ __forceinline__ void pair_term64(const SysDev &S, const SiteInfo &si,
   }
 }
 
-__device__ __forceinline__ void pair_term32(const SysDev &S, const SiteInfo &si, float chgprd,
-                                            int tb, int frozen_b, float r2, float &e2,
-                                            float &vdw, int &ov, int &sf, int &st) {
+// FP32 path.  The erfc term is formed and summed as a hi/lo pair: the
+// charge product (site factor and atom charge both as pairs), the table
+// value A + A_lo + p(B + pC) and the product's FMA residual, so each term
+// keeps about 1e-9 of its value apart from the FP32 distance.
+__device__ __forceinline__ void pair_term32(const SysDev &S, const SiteInfo &si, float qh, float ql,
+                                            int tb, int frozen_b, float r2, AccT<true> &e2,
+                                            float &vdw, int &ov, int &sf, int &st,
+                                            bool skip_vdw = false) {
   int pi = si.type * (S.ntpatm + 1) + tb;
   if (r2 < S.overlap_sqf) ov = 1;
   if (frozen_b && r2 < __ldg(S.sig2f + pi)) sf = 1;
   if (r2 < S.rc2f) {
     float r = sqrtf(r2);
-    if (fabsf(chgprd) > 1.0e-10f) e2 = fmaf(interp32(S.ercq, r, S.rdrewdf, S.mxegrd, st), chgprd, e2);
+    const float ch = si.chgeaf * qh;
+    if (fabsf(ch) > 1.0e-10f) {
+      const float cl = fmaf(si.chgeaf, qh, -ch) + fmaf(si.chgeaf, ql, si.chgeaf_lo * qh);
+      float t = r * S.rdrewdf;
+      float e = fmaf(r, S.rdrewdf, -t);
+      int l = int(t);
+      if (l < 1 || l > S.mxegrd) {
+        st |= kStTableLow;
+      } else {
+        float p = (t - float(l)) + e;
+        float4 c = __ldg(S.ercq + l);
+        float vl = fmaf(p, fmaf(p, c.z, c.y), c.w);
+        float ph = c.x * ch;
+        float pl = fmaf(c.x, ch, -ph) + fmaf(c.x, cl, vl * ch);
+        e2.add_df(DF{ph, pl});
+      }
+    }
     int k = __ldg(S.pairtab + pi);
-    if (k >= 0) vdw += interp32(S.vvvq + (size_t)k * S.tabstride, r, S.rdlrpotf, S.mxegrd, st);
+    if (k >= 0 && !skip_vdw) vdw += interp32(S.vvvq + (size_t)k * S.tabstride, r, S.rdlrpotf, S.mxegrd, st);
   }
+}
+
+// Close pairs: below 3 A the Lennard-Jones table is steep enough (tens of
+// thousands of kcal/mol per A near the overlap distance) that an FP32
+// distance alone would cost ~1e-6 of the term.  These pairs take r^2, r,
+// the bin index r*rdlrpot and the table value as float hi/lo pairs.
+constexpr float kNear2 = 9.0f;
+
+__device__ __forceinline__ bool vdw_is_near(const SysDev &S, const SiteInfo &si, int tb, float r2) {
+  return r2 < kNear2 && __ldg(S.pairtab + si.type * (S.ntpatm + 1) + tb) >= 0;
+}
+
+// Lennard-Jones term of one close pair from the difference vector given as
+// hi/lo pairs per axis.
+__device__ __forceinline__ DF vdw_near_df(const SysDev &S, const SiteInfo &si, int tb,
+                                          const float *dh, const float *dl, int &st) {
+  float ph[3], pe[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    ph[d] = dh[d] * dh[d];
+    pe[d] = fmaf(dh[d], dh[d], -ph[d]) + 2.0f * dh[d] * dl[d];
+  }
+  float s1, e1, s2, e2;
+  two_sum_f(ph[0], ph[1], s1, e1);
+  two_sum_f(s1, ph[2], s2, e2);
+  const float r2l = (e1 + e2) + (pe[0] + pe[1] + pe[2]);
+  const float rh = sqrtf(s2);
+  const float rl = (fmaf(-rh, rh, s2) + r2l) * (0.5f / rh);
+  const float th = rh * S.rdlrpotf;
+  const float tl = fmaf(rh, S.rdlrpotf, -th) + fmaf(rh, S.rdlrpotf_lo, rl * S.rdlrpotf);
+  int l = (int)floorf(th);
+  float p = (th - (float)l) + tl;
+  if (p < 0.0f) {
+    l -= 1;
+    p += 1.0f;
+  } else if (p >= 1.0f) {
+    l += 1;
+    p -= 1.0f;
+  }
+  DF out{0.0f, 0.0f};
+  if (l < 1 || l > S.mxegrd) {
+    st |= kStTableLow;
+    return out;
+  }
+  const int k = __ldg(S.pairtab + si.type * (S.ntpatm + 1) + tb);
+  const float4 c = __ldg(S.vvvq + (size_t)k * S.tabstride + l);
+  const float q = fmaf(p, fmaf(p, c.z, c.y), c.w);  // A_lo + p(B + pC)
+  two_sum_f(c.x, q, out.hi, out.lo);
+  return out;
 }
 
 // Minimum-image difference p - q of two points given as float hi/lo pairs
@@ -129,6 +203,23 @@ __device__ __forceinline__ float mi_diff32(float ph, float pl, float qh, float q
     return (h - qh) + ((pl - ql) + (e - k * Ll));
   }
   return dh + (pl - ql);
+}
+
+// The same difference as a hi/lo pair (close pairs).
+__device__ __forceinline__ void mi_diff_df(float ph, float pl, float qh, float ql, float Lh,
+                                           float Ll, float rL, float &dh, float &dl) {
+  float k = rintf((ph - qh) * rL);
+  float a = ph, al = pl;
+  if (k != 0.0f) {
+    float h, e;
+    two_sum_f(ph, -k * Lh, h, e);
+    a = h;
+    al = pl + (e - k * Ll);
+  }
+  float s, e;
+  two_sum_f(a, -qh, s, e);
+  dh = s;
+  dl = e + (al - ql);
 }
 
 __device__ __forceinline__ int image_of(int ic, int n) {
@@ -243,10 +334,12 @@ __device__ __forceinline__ int find_slot(const int *pref, int n, int t) {
 }
 
 // Scan the framework for position `pos` (ns sites).
-template <bool F32>
-__device__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos, int ns,
-                               const SiteInfo *si, PosAcc<F32> &acc, int &ov, int &sf,
-                               int &st) {
+// NS > 0: the site count is a compile-time constant (site loops unroll).
+template <bool F32, int NS, class PA>
+__device__ __forceinline__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos,
+                                               int ns_rt, const SiteInfo *si, PA &acc, int &ov,
+                                               int &sf, int &st) {
+  const int ns = NS > 0 ? NS : ns_rt;
   int nslot = sm.nslots;
   int total = sm.seg_pref[nslot];
   if constexpr (!F32) {
@@ -282,7 +375,7 @@ __device__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos, int 
     acc.e2fw.add(e2);
     acc.vdwfw.add(vdw);
   } else {
-    float e2 = 0.0f, vdw = 0.0f;
+    float vdw = 0.0f;
     int cnt = 0;
     const float *Lh = S.boxh, *Ll = S.boxl;
     for (int t = threadIdx.x; t < total; t += kThreads) {
@@ -303,21 +396,31 @@ __device__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos, int 
           al[d] = al[d] + (e + float(im[d]) * Ll[d]);
         }
       }
-      for (int k = 0; k < ns; ++k) {
+#pragma unroll
+      for (int k = 0; k < (NS > 0 ? NS : ns); ++k) {
         float dx = (sm.phi[pos][k][0] - ah[0]) + (sm.plo[pos][k][0] - al[0]);
         float dy = (sm.phi[pos][k][1] - ah[1]) + (sm.plo[pos][k][1] - al[1]);
         float dz = (sm.phi[pos][k][2] - ah[2]) + (sm.plo[pos][k][2] - al[2]);
         float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        pair_term32(S, si[k], si[k].chgeaf * H.w, tb, 1, r2, e2, vdw, ov, sf, st);
+        const bool near = vdw_is_near(S, si[k], tb, r2);
+        pair_term32(S, si[k], H.w, Lo.w, tb, 1, r2, acc.e2fw, vdw, ov, sf, st, near);
+        if (near) {
+          float dh[3], dl[3];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            float e;
+            two_sum_f(sm.phi[pos][k][d], -ah[d], dh[d], e);
+            dl[d] = e + (sm.plo[pos][k][d] - al[d]);
+          }
+          acc.vdwfw.add_df(vdw_near_df(S, si[k], tb, dh, dl, st));
+        }
       }
       if (++cnt == 8) {
-        acc.e2fw.add(e2);
         acc.vdwfw.add(vdw);
-        e2 = vdw = 0.0f;
+        vdw = 0.0f;
         cnt = 0;
       }
     }
-    acc.e2fw.add(e2);
     acc.vdwfw.add(vdw);
   }
 }
@@ -325,12 +428,16 @@ __device__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos, int 
 // Guest-guest part: every molecule of every guest type except the moving
 // one (the reference's ind exclusion, utility_pack.f:3736-3741).  Minimum
 // image per site pair, as images() does for each list entry.
-template <bool F32>
-__device__ void scan_guests(const SysDev &S, const ChainHdr &H, const ChainArrays &CA,
-                            int chain, EvalSmem<F32> &sm, int pos, int ns, int self_g,
-                            int self_slot, float rmax_self, const SiteInfo *si,
-                            PosAcc<F32> &acc, int &ov, int &sf, int &st) {
-  for (int g2 = 0; g2 < S.ntpguest; ++g2) {
+template <bool F32, int GN, int NS>
+__device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
+                                            const ChainArrays &CA, int chain, EvalSmem<F32> &sm,
+                                            int pos, int ns_rt, int self_g, int self_slot,
+                                            float rmax_self, const SiteInfo *si,
+                                            PosAcc<F32, GN> &acc, int &ov, int &sf, int &st) {
+  const int ns = NS > 0 ? NS : ns_rt;
+#pragma unroll
+  for (int g2 = 0; g2 < GN; ++g2) {
+    if (g2 >= S.ntpguest) break;
     const GuestType &G2 = S.g[g2];
     int n2 = H.nummols[g2];
     const int *ord = CA.ord + ((size_t)chain * kMaxG + g2) * CA.cap;
@@ -349,12 +456,13 @@ __device__ void scan_guests(const SysDev &S, const ChainHdr &H, const ChainArray
         dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
         dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
         if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
-        float e2 = 0.f, vdw = 0.f;
+        float vdw = 0.f;
         for (int b = 0; b < G2.ns; ++b) {
           float4 qh = gh[(size_t)slot * kMaxS + b];
           float4 ql = gl[(size_t)slot * kMaxS + b];
           int tb = G2.type[b];
-          for (int k = 0; k < ns; ++k) {
+#pragma unroll
+          for (int k = 0; k < (NS > 0 ? NS : ns); ++k) {
             float ex = mi_diff32(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
                                  S.boxl[0], S.rboxf[0]);
             float ey = mi_diff32(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
@@ -362,10 +470,21 @@ __device__ void scan_guests(const SysDev &S, const ChainHdr &H, const ChainArray
             float ez = mi_diff32(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2],
                                  S.boxl[2], S.rboxf[2]);
             float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-            pair_term32(S, si[k], si[k].chgeaf * qh.w, tb, G2.frz[b], r2, e2, vdw, ov, sf, st);
+            const bool near = vdw_is_near(S, si[k], tb, r2);
+            pair_term32(S, si[k], qh.w, ql.w, tb, G2.frz[b], r2, acc.e2g[g2], vdw, ov, sf, st,
+                        near);
+            if (near) {
+              float dh[3], dl[3];
+              mi_diff_df(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0], S.boxl[0],
+                         S.rboxf[0], dh[0], dl[0]);
+              mi_diff_df(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1], S.boxl[1],
+                         S.rboxf[1], dh[1], dl[1]);
+              mi_diff_df(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2], S.boxl[2],
+                         S.rboxf[2], dh[2], dl[2]);
+              acc.vdwg[g2].add_df(vdw_near_df(S, si[k], tb, dh, dl, st));
+            }
           }
         }
-        acc.e2g[g2].add(e2);
         acc.vdwg[g2].add(vdw);
       }
     } else {
@@ -428,16 +547,21 @@ template <bool F32>
 __device__ void build_powers(const SysDev &S, EvalSmem<F32> &sm, int npos, int ns) {
   int k1 = S.kmax[0], k2 = S.kmax[1], k3 = S.kmax[2];
   if constexpr (F32) {
+    // fractional coordinate x / L of the hi/lo position as a hi/lo pair
+    // (orthorhombic cells), reduced by whole cells: e^{i 2 pi j f} only
+    // needs f modulo 1
     int nf = npos * ns * 3;
     if (threadIdx.x < nf) {
       int pos = threadIdx.x / (ns * 3), rem = threadIdx.x % (ns * 3), s = rem / 3, d = rem % 3;
-      const double *p = sm.p64[pos][s];
-      const double *r = S.rcell;
-      double f = r[d] * p[0] + r[3 + d] * p[1] + r[6 + d] * p[2];
-      f -= floor(f);
-      float h = (float)f;
-      sm.fhi[pos][s][d] = h;
-      sm.flo[pos][s][d] = (float)(f - (double)h);
+      const float xh = sm.phi[pos][s][d], xl = sm.plo[pos][s][d];
+      const float rh = S.rboxf[d], rl = S.rboxf_lo[d];
+      const float fh = xh * rh;
+      const float fe = fmaf(xh, rh, -fh) + fmaf(xh, rl, xl * rh);
+      float s0, e0, hi, lo;
+      two_sum_f(fh, -floorf(fh), s0, e0);
+      two_sum_f(s0, e0 + fe, hi, lo);
+      sm.fhi[pos][s][d] = hi;
+      sm.flo[pos][s][d] = lo;
     }
     __syncthreads();
   }
@@ -474,6 +598,23 @@ __device__ void build_powers(const SysDev &S, EvalSmem<F32> &sm, int npos, int n
       float sn, cs;
       sincospif(2.0f * x, &sn, &cs);
       sm.pw32[pos][s][d][j] = make_float2(cs, sn);
+    }
+  }
+  if constexpr (F32) {
+    // (l, m) products, so the k loop needs one complex product per site
+    const int w = 2 * k2 + 1, nlm = (k1 + 1) * w;
+    if (npos * ns * nlm <= kPlmMax) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < nlm; e += kThreads) {
+        const int l = e / w, mm = e - l * w - k2, am = abs(mm);
+        for (int p = 0; p < npos; ++p)
+          for (int s = 0; s < ns; ++s) {
+            const float2 X = sm.pw32[p][s][0][l];
+            float2 Y = sm.pw32[p][s][1][am];
+            if (mm < 0) Y.y = -Y.y;
+            sm.plm[(p * ns + s) * nlm + e] = make_float2(X.x * Y.x - X.y * Y.y, X.y * Y.x + X.x * Y.y);
+          }
+      }
     }
   }
 }

@@ -88,117 +88,33 @@ __global__ void __launch_bounds__(kThreads) structure_factor_kernel(
   }
 }
 
-// Modes of the chain kernel.
-constexpr int kModeMoves = 0;   // nmoves main-loop iterations
-constexpr int kModeCreate = 1;  // "create molecules" pre-loading
-constexpr int kModeEval = 2;    // evaluate the move in gctx (per-move ABI)
-constexpr int kModeCommit = 3;  // decide with gctx.rande and commit
+// The chain kernel's instantiations (chain_f32_g1.cu, chain_f32_g4.cu,
+// chain_f64.cu): launch wrappers and shared-memory set-up.
+template <bool F32, int GN>
+cudaError_t launch_chain(dim3 grid, size_t smem, cudaStream_t stream, const SysDev *systems,
+                         ChainHdr *hdrs, const ChainArrays &CA, MoveCtx *gctx, LogRec *logs,
+                         int logcap, int nmoves, int mode, const double *ctl_fuga);
+template <bool F32, int GN>
+cudaError_t set_chain_smem(size_t smem);
+extern template cudaError_t launch_chain<true, 1>(dim3, size_t, cudaStream_t, const SysDev *,
+                                                  ChainHdr *, const ChainArrays &, MoveCtx *,
+                                                  LogRec *, int, int, int, const double *);
+extern template cudaError_t launch_chain<true, kMaxG>(dim3, size_t, cudaStream_t, const SysDev *,
+                                                      ChainHdr *, const ChainArrays &, MoveCtx *,
+                                                      LogRec *, int, int, int, const double *);
+extern template cudaError_t launch_chain<false, kMaxG>(dim3, size_t, cudaStream_t,
+                                                       const SysDev *, ChainHdr *,
+                                                       const ChainArrays &, MoveCtx *, LogRec *,
+                                                       int, int, int, const double *);
+extern template cudaError_t set_chain_smem<true, 1>(size_t);
+extern template cudaError_t set_chain_smem<true, kMaxG>(size_t);
+extern template cudaError_t set_chain_smem<false, kMaxG>(size_t);
 
-template <class T>
-__device__ void block_copy(T *dst, const T *src) {
-  static_assert(sizeof(T) % 4 == 0, "copy granularity");
-  const int *s = reinterpret_cast<const int *>(src);
-  int *d = reinterpret_cast<int *>(dst);
-  for (int i = threadIdx.x; i < (int)(sizeof(T) / 4); i += kThreads) d[i] = s[i];
-}
-
-template <bool F32>
-__global__ void __launch_bounds__(kThreads, 1)
-    chain_kernel(const SysDev *__restrict__ systems, ChainHdr *hdrs, ChainArrays CA,
-                 MoveCtx *gctx, LogRec *logs, int logcap, int nmoves, int mode,
-                 const double *__restrict__ ctl_fuga) {
-  extern __shared__ __align__(16) unsigned char dyn[];
-  BlockShared<F32> &B = *reinterpret_cast<BlockShared<F32> *>(dyn);
-  const int chain = blockIdx.x;
-  block_copy(&B.H, hdrs + chain);
-  __syncthreads();
-  block_copy(&B.S, systems + B.H.system);
-  if (threadIdx.x == 0) {
-    B.flags[0] = 0;
-    if (ctl_fuga && mode == kModeMoves) B.H.fuga[0] = ctl_fuga[chain];  // host control block
-  }
-  __syncthreads();
-  int st = 0;
-  if (mode == kModeMoves) {
-    for (int it = 0; it < nmoves; ++it) {
-      propose(B, CA, chain, kPropMC, 0);
-      int full = 0;
-      if (B.mc.kind != 0) full = evaluate(B, CA, chain, st);
-      if (threadIdx.x == 0) {
-        decide(B, true);
-        if (full) B.H.evals += B.mc.npos;
-        else if (B.mc.overlap) B.H.overlap_exits++;
-        if (logcap > 0 && B.H.log_n < logcap) {
-          LogRec &L = logs[(size_t)chain * logcap + B.H.log_n];
-          L.move = B.mc.kind;
-          L.iguest = B.mc.g + 1;
-          L.choice = B.mc.choice;
-          L.overlap = B.mc.overlap;
-          L.accepted = B.mc.accepted;
-          L.estep = B.mc.estep;
-          L.rande = B.mc.rande;
-          for (int s = 0; s < 3 && s < B.mc.ns; ++s)
-            for (int d = 0; d < 3; ++d) L.newxyz[3 * s + d] = B.mc.pos[0][s][d];
-        }
-      }
-      __syncthreads();
-      commit(B, CA, chain, st);
-      if (threadIdx.x == 0) {
-        stats(B);
-        if (logcap > 0 && B.H.log_n < logcap) {
-          logs[(size_t)chain * logcap + B.H.log_n].nmols_after = B.H.nummols[B.mc.g];
-          B.H.log_n++;
-        }
-      }
-      __syncthreads();
-    }
-  } else if (mode == kModeCreate) {
-    for (int g = 0; g < B.S.ntpguest; ++g) {
-      long long maxiter = 1000LL * B.S.g[g].insert0, iter = 0;
-      while (B.H.nummols[g] < B.S.g[g].insert0) {
-        if (iter >= maxiter) {  // insert_guests iteration cap (error 2320)
-          st |= kStCapacity;
-          break;
-        }
-        propose(B, CA, chain, kPropInsert, g);
-        evaluate(B, CA, chain, st);
-        if (threadIdx.x == 0) B.mc.accepted = B.mc.overlap ? 0 : 1;
-        __syncthreads();
-        commit(B, CA, chain, st);
-        __syncthreads();
-        ++iter;
-      }
-    }
-  } else if (mode == kModeEval) {
-    if (threadIdx.x == 0) B.mc = gctx[chain];
-    __syncthreads();
-    propose(B, CA, chain, kPropExternal, 0);
-    int full = 0;
-    if (B.mc.kind != 0) full = evaluate(B, CA, chain, st);
-    if (threadIdx.x == 0) {
-      B.mc.evaluated = 1;
-      B.mc.accepted = 0;
-      (void)full;
-      gctx[chain] = B.mc;
-    }
-  } else if (mode == kModeCommit) {
-    if (threadIdx.x == 0) {
-      B.mc = gctx[chain];
-      decide(B, false);
-    }
-    __syncthreads();
-    commit(B, CA, chain, st);
-    if (threadIdx.x == 0) {
-      B.mc.evaluated = 0;
-      gctx[chain] = B.mc;
-    }
-  }
-  if (st) atomicOr(&B.flags[0], st);
-  __syncthreads();
-  if (threadIdx.x == 0) B.H.status |= B.flags[0];
-  __syncthreads();
-  block_copy(hdrs + chain, &B.H);
-}
+// Modes of the chain kernel (chain_kernel.cuh).
+constexpr int kModeMoves = 0;
+constexpr int kModeCreate = 1;
+constexpr int kModeEval = 2;
+constexpr int kModeCommit = 3;
 
 // ----------------------------------------------------- device allocations
 template <class T>
@@ -230,13 +146,14 @@ struct DBuf {
 struct DevSystem {
   SysDev d{};
   DBuf<double4> fw64;
-  DBuf<float4> fwhi, fwlo;
+  DBuf<float4> fwhi, fwlo, cpad_hi, cpad_lo;
   DBuf<int> fwtype, cell_start, pairtab, numtyp_fw, numfrz_fw;
   DBuf<double> erc, vvv, sig2, steadd, akk;
   DBuf<float4> ercq, vvvq;
   DBuf<float> akk32, sig2f;
   DBuf<float4> skfw_df;
   DBuf<int4> klmn;
+  DBuf<unsigned> kpk;
   DBuf<double2> skfw;
   std::vector<double2> skfw_host;
   const System *host = nullptr;
@@ -253,7 +170,8 @@ std::vector<float4> quad_coeffs(const std::vector<double> &tab, int mx) {
   for (int l = 1; l <= mx; ++l) {
     double v0 = tab[l], v1 = tab[l + 1], v2 = (l + 2 < (int)tab.size()) ? tab[l + 2] : 0.0;
     double D = v2 - 2.0 * v1 + v0;
-    q[l] = make_float4((float)v0, (float)(v1 - v0 - 0.5 * D), (float)(0.5 * D), 0.f);
+    const float a = (float)v0;
+    q[l] = make_float4(a, (float)(v1 - v0 - 0.5 * D), (float)(0.5 * D), (float)(v0 - (double)a));
   }
   return q;
 }
@@ -287,6 +205,7 @@ void build_device_system(const System &s, DevSystem &D) {
     d.boxh[dd] = (float)d.box[dd];
     d.boxl[dd] = (float)(d.box[dd] - (double)d.boxh[dd]);
     d.rboxf[dd] = (float)d.rbox[dd];
+    d.rboxf_lo[dd] = (float)(d.rbox[dd] - (double)d.rboxf[dd]);
   }
   d.volm = s.volm;
   d.statvolm = s.statvolm;
@@ -373,7 +292,8 @@ void build_device_system(const System &s, DevSystem &D) {
     a64[i] = make_double4(x[o], y[o], z[o], q[o]);
     float hx = (float)x[o], hy = (float)y[o], hz = (float)z[o];
     ahi[i] = make_float4(hx, hy, hz, (float)q[o]);
-    alo[i] = make_float4((float)(x[o] - hx), (float)(y[o] - hy), (float)(z[o] - hz), 0.f);
+    alo[i] = make_float4((float)(x[o] - hx), (float)(y[o] - hy), (float)(z[o] - hz),
+                         (float)(q[o] - (double)(float)q[o]));
     at[i] = t[o];
   }
   D.fw64.upload(a64);
@@ -381,6 +301,25 @@ void build_device_system(const System &s, DevSystem &D) {
   D.fwlo.upload(alo);
   D.fwtype.upload(at);
   D.cell_start.upload(cstart);
+  if (d.use_cells) {
+    int ncell = d.nc[0] * d.nc[1] * d.nc[2], maxc = 1;
+    for (int c = 0; c < ncell; ++c) maxc = std::max(maxc, cstart[c + 1] - cstart[c]);
+    int lp = 0;
+    while ((1 << lp) < maxc) ++lp;
+    const int pad = 1 << lp;
+    std::vector<float4> ph((size_t)ncell * pad, make_float4(1e18f, 1e18f, 1e18f, 0.f));
+    std::vector<float4> pl((size_t)ncell * pad, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int c = 0; c < ncell; ++c)
+      for (int j = 0; j < cstart[c + 1] - cstart[c]; ++j) {
+        ph[(size_t)c * pad + j] = ahi[cstart[c] + j];
+        pl[(size_t)c * pad + j] = alo[cstart[c] + j];
+      }
+    D.cpad_hi.upload(ph);
+    D.cpad_lo.upload(pl);
+    d.cpad_log2 = lp;
+    d.cpad_hi = D.cpad_hi.p;
+    d.cpad_lo = D.cpad_lo.p;
+  }
   d.fw64 = D.fw64.p;
   d.fwhi = D.fwhi.p;
   d.fwlo = D.fwlo.p;
@@ -393,6 +332,7 @@ void build_device_system(const System &s, DevSystem &D) {
   d.rdlrpot = 1.0 / s.dlrpot;
   d.rdrewdf = (float)d.rdrewd;
   d.rdlrpotf = (float)d.rdlrpot;
+  d.rdlrpotf_lo = (float)(d.rdlrpot - (double)d.rdlrpotf);
   std::vector<double> erc(d.tabstride, 0.0);
   for (int i = 1; i <= s.mxegrd; ++i) erc[i] = s.erc[i];
   D.erc.upload(erc);
@@ -440,15 +380,30 @@ void build_device_system(const System &s, DevSystem &D) {
   d.numfrz_fw = D.numfrz_fw.p;
   // k vectors
   d.nk = s.newld;
+  // FP32 path arrays are padded to whole tiles of kKT k-vectors: padding
+  // entries are k = (0,0,0) with a_k = 0 and S_fw = 0, so they add nothing
+  const int nkpad = std::max(1, (s.newld + kKT - 1) / kKT) * kKT;
   std::vector<int4> lmn(s.newld);
-  std::vector<float> a32(s.newld);
+  std::vector<float> a32(nkpad, 0.0f);
+  for (int dd = 0; dd < 3; ++dd)
+    if (s.kmax[dd] + 1 > kMaxKm)
+      raise(FMC_ERR_INPUT, "kmax above " + std::to_string(kMaxKm - 1) + " is not supported");
+  // packed k for the FP32 loop: l * (2 kmax_y + 1) + m + kmax_y | (n + 128) << 16
+  const int wlm = 2 * s.kmax[1] + 1;
+  std::vector<unsigned> pk(nkpad, (unsigned)s.kmax[1] | (128u << 16));
   for (int k = 0; k < s.newld; ++k) {
     lmn[k] = make_int4(s.kl[k], s.km[k], s.kn[k], 0);
     a32[k] = (float)s.akk[k];
+    if (s.kl[k] < 0 || s.kl[k] > s.kmax[0] || std::abs(s.km[k]) > s.kmax[1] ||
+        std::abs(s.kn[k]) > s.kmax[2])
+      raise(FMC_ERR_INPUT, "k-vector index outside kmax");
+    pk[k] = (unsigned)(s.kl[k] * wlm + s.km[k] + s.kmax[1]) | ((unsigned)(s.kn[k] + 128) << 16);
   }
   D.klmn.upload(lmn);
+  D.kpk.upload(pk);
   D.akk.upload(s.akk);
   D.akk32.upload(a32);
+  d.kpk = D.kpk.p;
   d.klmn = D.klmn.p;
   d.akk = D.akk.p;
   d.akk32 = D.akk32.p;
@@ -461,7 +416,7 @@ void build_device_system(const System &s, DevSystem &D) {
     FMC_CUDA(cudaMemcpy(D.skfw_host.data(), D.skfw.p, s.newld * sizeof(double2), cudaMemcpyDeviceToHost));
   d.skfw = D.skfw.p;
   {
-    std::vector<float4> df(std::max(1, s.newld));
+    std::vector<float4> df(nkpad, make_float4(0.f, 0.f, 0.f, 0.f));
     for (int k = 0; k < s.newld; ++k) {
       double2 v = D.skfw_host[k];
       float hx = (float)v.x, hy = (float)v.y;
@@ -497,6 +452,14 @@ void build_device_system(const System &s, DevSystem &D) {
       rmax = std::max(rmax, std::sqrt(dx * dx + dy * dy + dz * dz));
     }
     G.rmax = rmax;
+    {
+      double mt = 0.0;
+      for (int i = 0; i < m.natoms; ++i) mt += m.wght[i];
+      for (int i = 0; i < m.natoms; ++i) {
+        for (int dd = 0; dd < 3; ++dd) G.tmplf[i][dd] = (float)G.tmpl[i][dd];
+        G.wf[i] = (float)(m.wght[i] / mt);
+      }
+    }
     G.ewald3en = s.ewald3en[G.mol];
     double qs = 0.0, q2 = 0.0, mass = 0.0;
     for (int i = 0; i < m.natoms; ++i) {
@@ -505,6 +468,11 @@ void build_device_system(const System &s, DevSystem &D) {
       mass += m.wght[i];
     }
     double r4 = kR4pie0 / s.epsq;
+    for (int i = 0; i < m.natoms; ++i) {
+      G.chgea[i] = m.chg[i] / s.epsq * kR4pie0;  // ewald.f:688 (chgea)
+      G.chgeaf[i] = (float)G.chgea[i];
+      G.chgeaf_lo[i] = (float)(G.chgea[i] - (double)G.chgeaf[i]);
+    }
     G.chgtmp = qs;
     G.engsic0 = -r4 * s.alpha * q2 / kSqrPi;  // ewald.f:105
     G.qfa = -(0.5 * kPi * r4) * (qs / s.alpha) / s.volm;  // ewald.f:317-318
@@ -584,6 +552,8 @@ ChainHdr initial_header(const System &s, int system_index, long long seed,
   h.rotangle = kPi / 3.0;
   h.rota_rotangle = h.rotangle;
   h.production = s.eqsteps == 0 ? 1 : 0;
+  h.minchk_left = std::max(1, s.minchk);
+  h.window_left = std::max(1, s.nwindsteps);
   h.sumchg = s.sumchg;
   const MolType &fw = s.mol[s.fw_mol];
   double cf = 0.0;
@@ -620,6 +590,7 @@ struct Chains {
   DBuf<double> ctl_fuga;
   ChainArrays CA{};
   int nchains = 0, precision = 0, logcap = 0, maxmls = 0;
+  int gn = kMaxG;  // guest-type capacity of the kernel's accumulators (1 or kMaxG)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -639,14 +610,18 @@ struct Chains {
 
   void launch(int mode, int nmoves) {
     headers_stale = true;
-    dim3 grid(nchains), block(kThreads);
-    if (precision == FMC_PREC_FP32)
-      chain_kernel<true><<<grid, block, smem, stream>>>(sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
-                                                        nmoves, mode, ctl_fuga.p);
+    dim3 grid(nchains);
+    cudaError_t e;
+    if (precision == FMC_PREC_FP32 && gn == 1)
+      e = launch_chain<true, 1>(grid, smem, stream, sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
+                                nmoves, mode, ctl_fuga.p);
+    else if (precision == FMC_PREC_FP32)
+      e = launch_chain<true, kMaxG>(grid, smem, stream, sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
+                                    nmoves, mode, ctl_fuga.p);
     else
-      chain_kernel<false><<<grid, block, smem, stream>>>(sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
-                                                         nmoves, mode, ctl_fuga.p);
-    FMC_CUDA(cudaGetLastError());
+      e = launch_chain<false, kMaxG>(grid, smem, stream, sysarr.p, hdr.p, CA, ctx.p, logs.p,
+                                     logcap, nmoves, mode, ctl_fuga.p);
+    FMC_CUDA(e);
   }
 
   void sync() { FMC_CUDA(cudaStreamSynchronize(stream)); }
@@ -663,10 +638,11 @@ struct Chains {
     pull_headers();
     for (int c = 0; c < nchains; ++c)
       if (host_hdr[c].status) {
-        char buf[160];
+        char buf[256];
         std::snprintf(buf, sizeof buf,
                       "chain %d raised device status 0x%x (1 table range, 2 segment overflow, "
-                      "4 capacity, 8 non-finite, 16 bad molecule index)",
+                      "4 capacity, 8 non-finite, 16 bad molecule index, 32 kmax, "
+                      "64 copy wait timed out)",
                       c, host_hdr[c].status);
         raise(FMC_ERR_DEVICE, buf);
       }
@@ -688,7 +664,7 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
       raise(FMC_ERR_INPUT, "the FP32 path supports orthorhombic cells (imcon 1, 2)");
     auto D = std::make_unique<DevSystem>();
     build_device_system(*systems[i], *D);
-    nkmax = std::max(nkmax, systems[i]->newld);
+    nkmax = std::max(nkmax, std::max(1, (systems[i]->newld + kKT - 1) / kKT) * kKT);
     maxmls = std::max(maxmls, systems[i]->maxmls);
     C.hsys.push_back(systems[i]);
     C.sys.push_back(std::move(D));
@@ -755,12 +731,14 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   FMC_CUDA(cudaEventCreate(&C.ev0));
   FMC_CUDA(cudaEventCreate(&C.ev1));
   C.smem = precision == FMC_PREC_FP32 ? sizeof(BlockShared<true>) : sizeof(BlockShared<false>);
-  if (precision == FMC_PREC_FP32)
-    FMC_CUDA(cudaFuncSetAttribute(chain_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)C.smem));
-  else
-    FMC_CUDA(cudaFuncSetAttribute(chain_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)C.smem));
+  int ngmax = 1;
+  for (int i = 0; i < nsys; ++i) ngmax = std::max(ngmax, systems[i]->ntpguest);
+  C.gn = (precision == FMC_PREC_FP32 && ngmax == 1) ? 1 : kMaxG;
+  cudaError_t e;
+  if (precision == FMC_PREC_FP32 && C.gn == 1) e = set_chain_smem<true, 1>(C.smem);
+  else if (precision == FMC_PREC_FP32) e = set_chain_smem<true, kMaxG>(C.smem);
+  else e = set_chain_smem<false, kMaxG>(C.smem);
+  FMC_CUDA(e);
 }
 
 void fill_stats(const Chains &C, fmc_chain_stats *out) {
@@ -1590,6 +1568,15 @@ int fmc_full_ewald_noalloc(fmc_plain *h, double *out4) {
     out4[1] = ew1;
     out4[2] = sic;
     out4[3] = qfix;
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_cycle_bytes(const fmc_batch *b, int64_t *h2d, int64_t *d2h) {
+  return guard([&] {
+    if (!b) raise(FMC_ERR_ARG, "null batch");
+    if (h2d) *h2d = (int64_t)b->C.nchains * (int64_t)sizeof(double);
+    if (d2h) *d2h = (int64_t)b->C.nchains * (int64_t)sizeof(ChainHdr);
     return FMC_OK;
   });
 }

@@ -40,6 +40,7 @@ struct BlockShared {
   SiteInfo si[kMaxS];
   float draws[8];
   double geo[12];    // a, b, c, q1..q4, rotation angle, com/frac scratch
+  float geof[4];     // FP32 path: shift a, b, c and the rotation angle
   double vtmp[3];
   int flags[4];
 };
@@ -58,7 +59,7 @@ __device__ __forceinline__ double lrc_delta(const SysDev &S, const ChainHdr &H, 
 }
 
 // energy_eval (utility_pack.f:3637-3693)
-__device__ bool energy_eval(const SysDev &S, const ChainHdr &H, int g, double eng,
+__device__ inline bool energy_eval(const SysDev &S, const ChainHdr &H, int g, double eng,
                             double rande, int kind) {
   double ipress = H.fuga[g];
   int ing = H.nummols[g];
@@ -88,8 +89,10 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   ChainHdr &H = B.H;
   MoveCtx &mc = B.mc;
   H.gcmccount++;
-  if (H.gcmccount % S.minchk == 0)
+  if (--H.minchk_left == 0) {  // gcmccount is a multiple of minchk
+    H.minchk_left = S.minchk;
     if (!H.production && S.eqsteps > 0 && H.gcmccount >= S.eqsteps) H.production = 1;
+  }
   int g = 0;
   if (S.ntpguest > 1) g = pick1(duni_f(H), S.ntpguest) - 1;
   const GuestType &G = S.g[g];
@@ -142,16 +145,23 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   } else {
     double a = 0.0, b = 0.0, c = 0.0;
     B.draws[3] = -1.0f;  // no rotation unless drawn
+    B.geof[0] = B.geof[1] = B.geof[2] = 0.0f;
     if (kind != 5) {     // random_disp (utility_pack.f:3333-3357)
       double dd = kind == 4 ? H.tran_delr[g] : H.delrdisp[g];
-      double h = dd * 0.5;
-      a = (2.0 * (double)duni_f(H) - 1.0) * h;
-      b = (2.0 * (double)duni_f(H) - 1.0) * h;
-      c = (2.0 * (double)duni_f(H) - 1.0) * h;
+      if constexpr (F32) {
+        const float hf = (float)(dd * 0.5);
+        for (int i = 0; i < 3; ++i) B.geof[i] = (2.0f * duni_f(H) - 1.0f) * hf;
+      } else {
+        double h = dd * 0.5;
+        a = (2.0 * (double)duni_f(H) - 1.0) * h;
+        b = (2.0 * (double)duni_f(H) - 1.0) * h;
+        c = (2.0 * (double)duni_f(H) - 1.0) * h;
+      }
     }
     if (kind != 4) {  // random_rot (utility_pack.f:3526-3563)
       for (int i = 3; i < 7; ++i) B.draws[i] = duni_f(H);
       B.geo[7] = kind == 5 ? H.rota_rotangle : H.rotangle;
+      B.geof[3] = (float)B.geo[7];
       B.flags[2] = 0;
     } else {
       // "move translate" keeps q1..q4 = 0 (gcmc.f:1842), and rotation()
@@ -188,20 +198,21 @@ __device__ __forceinline__ void draw_quaternion(const float *d, double angle, do
 }
 
 // Row d of the rotation matrix of rotation() (utility_pack.f:3497-3506).
-__device__ __forceinline__ void qrow(const double *q, int d, double *row) {
-  double q1 = q[0], q2 = q[1], q3 = q[2], q4 = q[3];
+template <class T>
+__device__ __forceinline__ void qrow(const T *q, int d, T *row) {
+  T q1 = q[0], q2 = q[1], q3 = q[2], q4 = q[3];
   if (d == 0) {
-    row[0] = 2.0 * q2 * q2 + 2.0 * q1 * q1 - 1.0;
-    row[1] = 2.0 * q2 * q3 - 2.0 * q1 * q4;
-    row[2] = 2.0 * q2 * q4 + 2.0 * q1 * q3;
+    row[0] = T(2) * q2 * q2 + T(2) * q1 * q1 - T(1);
+    row[1] = T(2) * q2 * q3 - T(2) * q1 * q4;
+    row[2] = T(2) * q2 * q4 + T(2) * q1 * q3;
   } else if (d == 1) {
-    row[0] = 2.0 * q2 * q3 + 2.0 * q1 * q4;
-    row[1] = 2.0 * q1 * q1 + 2.0 * q3 * q3 - 1.0;
-    row[2] = 2.0 * q3 * q4 - 2.0 * q1 * q2;
+    row[0] = T(2) * q2 * q3 + T(2) * q1 * q4;
+    row[1] = T(2) * q1 * q1 + T(2) * q3 * q3 - T(1);
+    row[2] = T(2) * q3 * q4 - T(2) * q1 * q2;
   } else {
-    row[0] = 2.0 * q2 * q4 - 2.0 * q1 * q3;
-    row[1] = 2.0 * q3 * q4 + 2.0 * q1 * q2;
-    row[2] = 2.0 * q4 * q4 + 2.0 * q1 * q1 - 1.0;
+    row[0] = T(2) * q2 * q4 - T(2) * q1 * q3;
+    row[1] = T(2) * q3 * q4 + T(2) * q1 * q2;
+    row[2] = T(2) * q4 * q4 + T(2) * q1 * q1 - T(1);
   }
 }
 
@@ -288,6 +299,136 @@ __device__ void geometry_warp(BlockShared<F32> &B, const ChainArrays &CA, int ch
   }
 }
 
+// Centre and bounding radius of each evaluated position from its FP32
+// coordinates (lanes p < npos of one warp).
+template <bool F32>
+__device__ __forceinline__ void position_bounds(BlockShared<F32> &B, int p) {
+  const int ns = B.mc.ns;
+  float c[3] = {0.f, 0.f, 0.f};
+  for (int s = 0; s < ns; ++s)
+    for (int d = 0; d < 3; ++d) c[d] += B.ev.phi[p][s][d];
+  float rn = 1.0f / ns, rm2 = 0.f;
+  for (int d = 0; d < 3; ++d) c[d] *= rn;
+  for (int s = 0; s < ns; ++s) {
+    float dx = B.ev.phi[p][s][0] - c[0], dy = B.ev.phi[p][s][1] - c[1], dz = B.ev.phi[p][s][2] - c[2];
+    rm2 = fmaxf(rm2, dx * dx + dy * dy + dz * dz);
+  }
+  for (int d = 0; d < 3; ++d) B.ev.cen[p][d] = c[d];
+  B.ev.rmx[p] = sqrtf(rm2) + 1e-3f;
+}
+
+// FP32 path, moves drawn on the device: geometry_warp's construction with
+// the positions built directly as float hi/lo pairs and no FP64 instruction
+// (orthorhombic cells).  One lane per site coordinate.  Insertion: the
+// template rotated by the drawn quaternion plus the drawn fractional centre
+// times the edge (an exact hi/lo product).  Displacement: shift, wrap the
+// centre of mass into the cell by whole edges, rotate about it.  Also fills
+// the site constants and the bounds of each position.
+template <bool F32>
+__device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
+  const SysDev &S = B.S;
+  MoveCtx &mc = B.mc;
+  EvalSmem<F32> &ev = B.ev;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  if (mc.kind == 0) return;
+  const GuestType &G = S.g[mc.g];
+  const int ns = G.ns;
+  const bool mine = lane < 3 * ns;
+  const int s = mine ? lane / 3 : 0;
+  const int d = lane % 3;
+  const float Lh = S.boxh[d], Ll = S.boxl[d];
+  float ph = 0.f, pl = 0.f, e;
+  if (mc.kind == 1) {
+    float sn, cs;
+    sincospif(B.draws[3], &sn, &cs);  // half of the angle 2 pi r
+    const float b1 = 2.0f * B.draws[4] - 1.0f, b2 = 2.0f * B.draws[5] - 1.0f,
+                b3 = 2.0f * B.draws[6] - 1.0f;
+    const float rn = rsqrtf(b1 * b1 + b2 * b2 + b3 * b3);
+    const float q[4] = {cs, sn * (b1 * rn), sn * (b2 * rn), sn * (b3 * rn)};
+    float row[3];
+    qrow(q, d, row);
+    const float *t = G.tmplf[s];
+    const float v = row[0] * t[0] + row[1] * t[1] + row[2] * t[2];
+    const float u = B.draws[d];
+    const float ch = u * Lh;
+    const float cl = fmaf(u, Lh, -ch) + u * Ll;
+    two_sum_f(ch, v, ph, e);
+    pl = cl + e;
+  } else {
+    const size_t b = gslot_base(CA, chain, mc.g, mc.slot) + s;
+    const float oh = mine ? reinterpret_cast<const float *>(CA.ghi + b)[d] : 0.f;
+    const float ol = mine ? reinterpret_cast<const float *>(CA.glo + b)[d] : 0.f;
+    if (mc.kind == 2) {
+      ph = oh;
+      pl = ol;
+    } else {
+      if (mine) {
+        ev.phi[1][s][d] = oh;
+        ev.plo[1][s][d] = ol;
+      }
+      two_sum_f(oh, B.geof[d], ph, e);  // shift (zero for "move rotate")
+      pl = ol + e;
+      // centre of mass, relative to site 0, as a hi/lo pair
+      const float p0h = __shfl_sync(full, ph, d), p0l = __shfl_sync(full, pl, d);
+      const float off = mine ? ((ph - p0h) + (pl - p0l)) * G.wf[s] : 0.f;
+      float cof = 0.f;
+      for (int s2 = 0; s2 < ns; ++s2) cof += __shfl_sync(full, off, 3 * s2 + d);
+      float cmh, cml;
+      two_sum_f(p0h, cof, cmh, e);
+      cml = p0l + e;
+      // wrap the centre into the cell by whole edges (translate)
+      const float k = floorf((cmh + cml) * S.rboxf[d]);
+      if (k != 0.0f) {
+        float t;
+        two_sum_f(ph, -k * Lh, t, e);
+        ph = t;
+        pl += e - k * Ll;
+        two_sum_f(cmh, -k * Lh, t, e);
+        cmh = t;
+        cml += e - k * Ll;
+      }
+      if (B.draws[3] >= 0.0f) {  // rotation about the wrapped centre
+        float q[4] = {0.f, 0.f, 0.f, 0.f};  // "move translate": q = 0, Q = -I
+        if (!B.flags[2]) {
+          float sn, cs;
+          sincosf(0.5f * (B.draws[3] * B.geof[3]), &sn, &cs);
+          const float b1 = 2.0f * B.draws[4] - 1.0f, b2 = 2.0f * B.draws[5] - 1.0f,
+                      b3 = 2.0f * B.draws[6] - 1.0f;
+          const float rn = rsqrtf(b1 * b1 + b2 * b2 + b3 * b3);
+          q[0] = cs;
+          q[1] = sn * (b1 * rn);
+          q[2] = sn * (b2 * rn);
+          q[3] = sn * (b3 * rn);
+        }
+        const float x = (ph - cmh) + (pl - cml);
+        const float x0 = __shfl_sync(full, x, 3 * s), x1 = __shfl_sync(full, x, 3 * s + 1),
+                    x2 = __shfl_sync(full, x, 3 * s + 2);
+        float row[3];
+        qrow(q, d, row);
+        const float v = row[0] * x0 + row[1] * x1 + row[2] * x2;
+        two_sum_f(cmh, v, ph, e);
+        pl = cml + e;
+      }
+    }
+  }
+  if (mine) {
+    ev.phi[0][s][d] = ph;
+    ev.plo[0][s][d] = pl;
+  }
+  if (lane < ns) {
+    SiteInfo &si = B.si[lane];
+    si.q = G.q[lane];
+    si.chgea = G.chgea[lane];
+    si.chgeaf = G.chgeaf[lane];
+    si.chgeaf_lo = G.chgeaf_lo[lane];
+    si.qf = (float)G.q[lane];
+    si.type = G.type[lane];
+  }
+  __syncwarp();
+  if (lane < mc.npos) position_bounds(B, lane);
+}
+
 // Warp 0 proposal for all modes; ends with a block barrier.
 template <bool F32>
 __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, int mode, int g_forced) {
@@ -334,8 +475,10 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
         }
       }
     }
+    if (threadIdx.x == 0) B.flags[3] = (F32 && mode != kPropExternal) ? 1 : 0;
     __syncwarp();
-    geometry_warp(B, CA, chain, mode);
+    if (F32 && mode != kPropExternal) geometry_f32(B, CA, chain);
+    else geometry_warp(B, CA, chain, mode);
   }
   __syncthreads();
 }
@@ -358,6 +501,45 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
     while (nrad * mincs < ov && nrad < 4) ++nrad;
     int span = 2 * nrad + 1;
     int per_site = span * span * span;
+    if (F32 && nrad == 1) {
+      // 27 neighbour cells per site, every padded slot of each cell one
+      // work item: a single round of independent loads
+      const int lp = S.cpad_log2;
+      const int nitem = (ns * 27) << lp;
+      for (int t = threadIdx.x; t < nitem && !hit; t += kThreads) {
+        const int j = t & ((1 << lp) - 1);
+        const int sc = t >> lp;
+        const int s = sc / 27, c = sc - 27 * s;
+        const int o3[3] = {c / 9 - 1, (c / 3) % 3 - 1, c % 3 - 1};
+        int im[3], iw[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          int ic = (int)floorf(ev.phi[0][s][d] * S.rcszf[d]) + o3[d];
+          int k = 0;
+          if (ic < 0) k = -1;
+          else if (ic >= S.nc[d]) k = 1;
+          if (ic - k * S.nc[d] < 0 || ic - k * S.nc[d] >= S.nc[d]) k = image_of(ic, S.nc[d]);
+          im[d] = k;
+          iw[d] = ic - k * S.nc[d];
+        }
+        const size_t a = ((size_t)((iw[0] * S.nc[1] + iw[1]) * S.nc[2] + iw[2]) << lp) + j;
+        const float4 H = __ldg(S.cpad_hi + a), L = __ldg(S.cpad_lo + a);
+        float ah[3] = {H.x, H.y, H.z}, al[3] = {L.x, L.y, L.z};
+        float r2 = 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          if (im[d] != 0) {
+            float h, e;
+            two_sum_f(ah[d], float(im[d]) * S.boxh[d], h, e);
+            ah[d] = h;
+            al[d] = al[d] + (e + float(im[d]) * S.boxl[d]);
+          }
+          float dd = (ev.phi[0][s][d] - ah[d]) + (ev.plo[0][s][d] - al[d]);
+          r2 = fmaf(dd, dd, r2);
+        }
+        if (r2 < S.overlap_sqf) hit = 1;
+      }
+    } else
     for (int t = threadIdx.x; t < ns * per_site && !hit; t += kThreads) {
       int s = t / per_site, c = t % per_site;
       int o3[3] = {c / (span * span) - nrad, (c / span) % span - nrad, c % span - nrad};
@@ -487,20 +669,22 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
 // One pass over the k-vectors for npos positions (ewald1_guest, ewald.f:
 // 151-315): s(k) of position 0 goes to the snew scratch and of position 1 to
 // sold; energies and mixing terms accumulate in acc.
-template <bool F32>
-__device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain, bool exist0,
-                       PosAcc<F32> *acc) {
+template <bool F32, int GN, int NS>
+__device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain,
+                                       bool exist0, PosAcc<F32, GN> &acc0, PosAcc<F32, GN> &acc1,
+                                       int &st) {
   const SysDev &S = B.S;
   const MoveCtx &mc = B.mc;
   const GuestType &G = S.g[mc.g];
-  const int ns = mc.ns, npos = mc.npos, mol = G.mol, NG = S.ntpguest;
+  const int ns = NS > 0 ? NS : mc.ns, npos = mc.npos, mol = G.mol, NG = S.ntpguest;
   const bool disp = npos == 2;
   if constexpr (!F32) {
     double2 *snew = CA.snew + (size_t)chain * CA.nkmax;
     double2 *sold = CA.sold + (size_t)chain * CA.nkmax;
     const double2 *skg = CA.sk + (size_t)chain * kMaxG * CA.nkmax;
-    double e[2] = {0.0, 0.0}, mfw[2] = {0.0, 0.0}, mg[2][kMaxG];
-    for (int g2 = 0; g2 < kMaxG; ++g2) mg[0][g2] = mg[1][g2] = 0.0;
+    double e[2] = {0.0, 0.0}, mfw[2] = {0.0, 0.0}, mg[2][GN];
+#pragma unroll
+    for (int g2 = 0; g2 < GN; ++g2) mg[0][g2] = mg[1][g2] = 0.0;
     for (int k = threadIdx.x; k < S.nk; k += kThreads) {
       int4 lmn = __ldg(S.klmn + k);
       int am = abs(lmn.y), an = abs(lmn.z);
@@ -508,17 +692,19 @@ __device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain, bo
       double akk = __ldg(S.akk + k);
       double2 sfw = __ldg(S.skfw + k);
       double2 stot = sfw;
-      double2 sgt[kMaxG];
+      double2 sgt[GN];
 #pragma unroll
-      for (int g2 = 0; g2 < kMaxG; ++g2) {
+      for (int g2 = 0; g2 < GN; ++g2) {
         if (g2 < NG) {
           sgt[g2] = skg[(size_t)g2 * CA.nkmax + k];
           stot.x += sgt[g2].x;
           stot.y += sgt[g2].y;
         }
       }
-      double2 sp[2];
-      for (int p = 0; p < npos; ++p) {
+      double2 sp[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        if (p >= npos) break;
         double2 a = make_double2(0.0, 0.0);
         for (int s = 0; s < ns; ++s) {
           double2 ex = B.ev.pw64[p][s][0][lmn.x];
@@ -532,7 +718,9 @@ __device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain, bo
         }
         sp[p] = a;
       }
-      for (int p = 0; p < npos; ++p) {
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        if (p >= npos) break;
         double2 su = stot;
         if (disp && p == 0) {  // the new position sees S - s_old (gcmc.f:2862-2871)
           su.x -= sp[1].x;
@@ -546,101 +734,152 @@ __device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain, bo
         double f2 = 2.0 * akk;
         mfw[p] += f2 * (sp[p].x * sfw.x + sp[p].y * sfw.y);
 #pragma unroll
-        for (int g2 = 0; g2 < kMaxG; ++g2)
+        for (int g2 = 0; g2 < GN; ++g2)
           if (g2 < NG && S.g[g2].mol != mol) mg[p][g2] += f2 * (sp[p].x * sgt[g2].x + sp[p].y * sgt[g2].y);
       }
       snew[k] = sp[0];
       if (disp) sold[k] = sp[1];
     }
+#pragma unroll
     for (int p = 0; p < 2; ++p) {
-      acc[p].recip.add(e[p]);
-      acc[p].mixfw.add(mfw[p]);
-      for (int g2 = 0; g2 < kMaxG; ++g2) acc[p].mixg[g2].add(mg[p][g2]);
+      PosAcc<F32, GN> &A = p == 0 ? acc0 : acc1;
+      A.recip.add(e[p]);
+      A.mixfw.add(mfw[p]);
+#pragma unroll
+      for (int g2 = 0; g2 < GN; ++g2) A.mixg[g2].add(mg[p][g2]);
     }
   } else {
+    // Two k-vectors per thread in flight.  e^{i k.r} of a site is the (l, m)
+    // table entry times e^{i 2 pi n s_z} (conjugated for n < 0); without the
+    // table (large kmax) it is X_l Y_m Z_n from the power tables.
     float2 *snew32 = CA.snew32 + (size_t)chain * CA.nkmax;
     float2 *sold32 = CA.sold32 + (size_t)chain * CA.nkmax;
     const float4 *skg = CA.skdf + (size_t)chain * kMaxG * CA.nkmax;
-    float e[2] = {0.f, 0.f}, mfw[2] = {0.f, 0.f}, mg[2][kMaxG];
+    const int k2 = S.kmax[1], w = 2 * k2 + 1, nlm = (S.kmax[0] + 1) * w;
+    const bool tab = npos * ns * nlm <= kPlmMax;
+    unsigned mixmask = 0;  // guest types of another molecule type (mixing terms)
+    for (int g2 = 0; g2 < NG && g2 < GN; ++g2)
+      if (S.g[g2].mol != mol) mixmask |= 1u << g2;
+    float e[2] = {0.f, 0.f}, mfw[2] = {0.f, 0.f}, mg[2][GN];
 #pragma unroll
-    for (int g2 = 0; g2 < kMaxG; ++g2) mg[0][g2] = mg[1][g2] = 0.f;
+    for (int g2 = 0; g2 < GN; ++g2) mg[0][g2] = mg[1][g2] = 0.f;
     int cnt = 0;
-    for (int k = threadIdx.x; k < S.nk; k += kThreads) {
-      int4 lmn = __ldg(S.klmn + k);
-      int am = abs(lmn.y), an = abs(lmn.z);
-      bool cm = lmn.y < 0, cn = lmn.z < 0;
-      float akk = __ldg(S.akk32 + k);
-      float4 fw = __ldg(S.skfw_df + k);
-      float thx = fw.x, thy = fw.y, tlx = fw.z, tly = fw.w;
-      float2 sfw = make_float2(fw.x + fw.z, fw.y + fw.w);
-      float2 sgt[kMaxG];
+    constexpr int U = 2;
+    for (int k0 = threadIdx.x; k0 < S.nk; k0 += U * kThreads) {
+      unsigned pk[U];
+      float akk[U];
+      float4 fw[U], st4[U];
 #pragma unroll
-      for (int g2 = 0; g2 < kMaxG; ++g2) {
-        if (g2 < NG) {
-          float4 v = skg[(size_t)g2 * CA.nkmax + k];
-          thx += v.x;
-          thy += v.y;
-          tlx += v.z;
-          tly += v.w;
-          sgt[g2] = make_float2(v.x + v.z, v.y + v.w);
-        }
-      }
-      float2 stot = make_float2(thx + tlx, thy + tly);
-      float2 sp[2];
-      for (int p = 0; p < npos; ++p) {
-        float2 a = make_float2(0.f, 0.f);
-        for (int s = 0; s < ns; ++s) {
-          float2 ex = B.ev.pw32[p][s][0][lmn.x];
-          float2 ey = B.ev.pw32[p][s][1][am];
-          float2 ez = B.ev.pw32[p][s][2][an];
-          if (cm) ey.y = -ey.y;
-          if (cn) ez.y = -ez.y;
-          float2 t = cmul(cmul(ex, ey), ez);
-          float q = B.si[s].qf;
-          a.x = fmaf(q, t.x, a.x);
-          a.y = fmaf(q, t.y, a.y);
-        }
-        sp[p] = a;
-      }
-      for (int p = 0; p < npos; ++p) {
-        float2 su = stot;
-        if (disp && p == 0) {
-          su.x -= sp[1].x;
-          su.y -= sp[1].y;
-        }
-        bool exist = disp ? (p == 1) : exist0;
-        float sumsqd = fmaf(sp[p].x, sp[p].x, sp[p].y * sp[p].y);
-        float mixterm = 2.0f * fmaf(sp[p].x, su.x, sp[p].y * su.y);
-        if (exist) mixterm = -mixterm;
-        e[p] = fmaf(akk, mixterm + sumsqd, e[p]);
-        float f2 = 2.0f * akk;
-        mfw[p] = fmaf(f2, fmaf(sp[p].x, sfw.x, sp[p].y * sfw.y), mfw[p]);
-#pragma unroll
-        for (int g2 = 0; g2 < kMaxG; ++g2)
-          if (g2 < NG && S.g[g2].mol != mol)
-            mg[p][g2] = fmaf(f2, fmaf(sp[p].x, sgt[g2].x, sp[p].y * sgt[g2].y), mg[p][g2]);
-      }
-      snew32[k] = sp[0];
-      if (disp) sold32[k] = sp[1];
-      if (++cnt == 8) {
-        for (int p = 0; p < 2; ++p) {
-          acc[p].recip.add(e[p]);
-          acc[p].mixfw.add(mfw[p]);
-          e[p] = mfw[p] = 0.f;
-#pragma unroll
-          for (int g2 = 0; g2 < kMaxG; ++g2) {
-            acc[p].mixg[g2].add(mg[p][g2]);
-            mg[p][g2] = 0.f;
+      for (int u = 0; u < U; ++u) {
+        const int k = k0 + u * kThreads;
+        pk[u] = 0u;
+        akk[u] = 0.f;
+        fw[u] = st4[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (k < S.nk) {
+          pk[u] = __ldg(S.kpk + k);
+          akk[u] = __ldg(S.akk32 + k);
+          fw[u] = __ldg(S.skfw_df + k);
+          st4[u] = fw[u];
+          for (int g2 = 0; g2 < NG; ++g2) {
+            const float4 v = skg[(size_t)g2 * CA.nkmax + k];
+            st4[u].x += v.x;
+            st4[u].y += v.y;
+            st4[u].z += v.z;
+            st4[u].w += v.w;
           }
         }
-        cnt = 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int k = k0 + u * kThreads;
+        if (k >= S.nk) continue;
+        const int lm = (int)(pk[u] & 0xffffu), nz = (int)(pk[u] >> 16) - 128;
+        const int an = abs(nz);
+        const bool cn = nz < 0;
+        int lx = 0, am = 0;
+        bool cm = false;
+        if (!tab) {
+          lx = lm / w;
+          const int mm = lm - lx * w - k2;
+          am = abs(mm);
+          cm = mm < 0;
+        }
+        const float2 stot = make_float2(st4[u].x + st4[u].z, st4[u].y + st4[u].w);
+        const float2 sfw = make_float2(fw[u].x + fw[u].z, fw[u].y + fw[u].w);
+        float2 sp[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          if (p >= npos) break;
+          float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int s = 0; s < (NS > 0 ? NS : ns); ++s) {
+            float2 P;
+            if (tab) {
+              P = B.ev.plm[(p * ns + s) * nlm + lm];
+            } else {
+              float2 ey = B.ev.pw32[p][s][1][am];
+              if (cm) ey.y = -ey.y;
+              P = cmul(B.ev.pw32[p][s][0][lx], ey);
+            }
+            float2 ez = B.ev.pw32[p][s][2][an];
+            if (cn) ez.y = -ez.y;
+            const float2 tt = cmul(P, ez);
+            const float q = B.si[s].qf;
+            a.x = fmaf(q, tt.x, a.x);
+            a.y = fmaf(q, tt.y, a.y);
+          }
+          sp[p] = a;
+        }
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          if (p >= npos) break;
+          float2 su = stot;
+          if (disp && p == 0) {  // the new position sees S - s_old (gcmc.f:2862-2871)
+            su.x -= sp[1].x;
+            su.y -= sp[1].y;
+          }
+          const bool exist = disp ? (p == 1) : exist0;
+          const float sumsqd = fmaf(sp[p].x, sp[p].x, sp[p].y * sp[p].y);
+          float mixterm = 2.0f * fmaf(sp[p].x, su.x, sp[p].y * su.y);
+          if (exist) mixterm = -mixterm;
+          e[p] = fmaf(akk[u], mixterm + sumsqd, e[p]);
+          const float f2 = 2.0f * akk[u];
+          mfw[p] = fmaf(f2, fmaf(sp[p].x, sfw.x, sp[p].y * sfw.y), mfw[p]);
+          if (mixmask) {
+#pragma unroll
+            for (int g2 = 0; g2 < GN; ++g2)
+              if (mixmask & (1u << g2)) {
+                const float4 v = skg[(size_t)g2 * CA.nkmax + k];
+                mg[p][g2] = fmaf(f2, fmaf(sp[p].x, v.x + v.z, sp[p].y * (v.y + v.w)), mg[p][g2]);
+              }
+          }
+        }
+        snew32[k] = sp[0];
+        if (disp) sold32[k] = sp[1];
+        if (++cnt == 8) {
+#pragma unroll
+          for (int p = 0; p < 2; ++p) {
+            PosAcc<F32, GN> &A = p == 0 ? acc0 : acc1;
+            A.recip.add(e[p]);
+            A.mixfw.add(mfw[p]);
+            e[p] = mfw[p] = 0.f;
+#pragma unroll
+            for (int g2 = 0; g2 < GN; ++g2) {
+              A.mixg[g2].add(mg[p][g2]);
+              mg[p][g2] = 0.f;
+            }
+          }
+          cnt = 0;
+        }
       }
     }
-    for (int p = 0; p < 2; ++p) {
-      acc[p].recip.add(e[p]);
-      acc[p].mixfw.add(mfw[p]);
 #pragma unroll
-      for (int g2 = 0; g2 < kMaxG; ++g2) acc[p].mixg[g2].add(mg[p][g2]);
+    for (int p = 0; p < 2; ++p) {
+      PosAcc<F32, GN> &A = p == 0 ? acc0 : acc1;
+      A.recip.add(e[p]);
+      A.mixfw.add(mfw[p]);
+#pragma unroll
+      for (int g2 = 0; g2 < GN; ++g2) A.mixg[g2].add(mg[p][g2]);
     }
   }
 }
@@ -648,47 +887,37 @@ __device__ void kspace(BlockShared<F32> &B, const ChainArrays &CA, int chain, bo
 // --------------------------------------------------------------- evaluate
 // Evaluate the proposed move; fills mc.estep, mc.delE and the flags.
 // Returns 1 if a full evaluation ran (no overlap exit).
-template <bool F32>
+template <bool F32, int GN, int NS>
 __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, int &st) {
   const SysDev &S = B.S;
   MoveCtx &mc = B.mc;
   const GuestType &G = S.g[mc.g];
-  const int ns = mc.ns, npos = mc.npos, NG = S.ntpguest;
-  if (threadIdx.x < ns) {
-    int s = threadIdx.x;
-    B.si[s].q = G.q[s];
-    B.si[s].chgea = G.q[s] / S.epsq * kR4pie0;
-    B.si[s].chgeaf = (float)B.si[s].chgea;
-    B.si[s].qf = (float)G.q[s];
-    B.si[s].type = G.type[s];
-  }
-  if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * kMaxS * 3) {
-    int t = threadIdx.x - 32;
-    int p = t / (kMaxS * 3), s = (t / 3) % kMaxS, d = t % 3;
-    if (p < npos && s < ns) {
-      double v = mc.pos[p][s][d];
-      B.ev.p64[p][s][d] = v;
-      float h = (float)v;
-      B.ev.phi[p][s][d] = h;
-      B.ev.plo[p][s][d] = (float)(v - (double)h);
+  const int ns = NS > 0 ? NS : mc.ns, npos = mc.npos, NG = S.ntpguest;
+  if (!B.flags[3]) {  // positions from FP64 geometry: site constants, FP32 pairs, bounds
+    if (threadIdx.x < ns) {
+      int s = threadIdx.x;
+      B.si[s].q = G.q[s];
+      B.si[s].chgea = G.chgea[s];
+      B.si[s].chgeaf = G.chgeaf[s];
+      B.si[s].chgeaf_lo = G.chgeaf_lo[s];
+      B.si[s].qf = (float)G.q[s];
+      B.si[s].type = G.type[s];
     }
-  }
-  __syncthreads();
-  if (threadIdx.x < npos) {  // conservative centre and radius (FP32)
-    int p = threadIdx.x;
-    float c[3] = {0.f, 0.f, 0.f};
-    for (int s = 0; s < ns; ++s)
-      for (int d = 0; d < 3; ++d) c[d] += B.ev.phi[p][s][d];
-    float rn = 1.0f / ns, rm2 = 0.f;
-    for (int d = 0; d < 3; ++d) c[d] *= rn;
-    for (int s = 0; s < ns; ++s) {
-      float dx = B.ev.phi[p][s][0] - c[0], dy = B.ev.phi[p][s][1] - c[1], dz = B.ev.phi[p][s][2] - c[2];
-      rm2 = fmaxf(rm2, dx * dx + dy * dy + dz * dz);
+    if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * kMaxS * 3) {
+      int t = threadIdx.x - 32;
+      int p = t / (kMaxS * 3), s = (t / 3) % kMaxS, d = t % 3;
+      if (p < npos && s < ns) {
+        double v = mc.pos[p][s][d];
+        B.ev.p64[p][s][d] = v;
+        float h = (float)v;
+        B.ev.phi[p][s][d] = h;
+        B.ev.plo[p][s][d] = (float)(v - (double)h);
+      }
     }
-    for (int d = 0; d < 3; ++d) B.ev.cen[p][d] = c[d];
-    B.ev.rmx[p] = sqrtf(rm2) + 1e-3f;
+    __syncthreads();
+    if (threadIdx.x < npos) position_bounds(B, threadIdx.x);  // conservative (FP32)
+    __syncthreads();
   }
-  __syncthreads();
   if (mc.kind == 1 || mc.kind >= 3) {
     if (overlap_check(B, CA, chain)) {
       if (threadIdx.x == 0) mc.overlap = 1;
@@ -696,36 +925,28 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       return 0;
     }
   }
-  PosAcc<F32> acc[2];
-  acc[0].zero();
-  acc[1].zero();
-  int sf[2] = {0, 0}, ovd = 0;
-  for (int p = 0; p < npos; ++p) {
+  PosAcc<F32, GN> acc0, acc1;
+  acc0.zero();
+  acc1.zero();
+  int sf0 = 0, sf1 = 0, ovd = 0;
+  auto scan_position = [&](int p, PosAcc<F32, GN> &A, int &sfp) {
     build_segments<F32>(S, B.ev, B.ev.cen[p], (float)S.rcut + B.ev.rmx[p] + 1e-3f, st);
-    scan_framework<F32>(S, B.ev, p, ns, B.si, acc[p], ovd, sf[p], st);
-    scan_guests<F32>(S, B.H, CA, chain, B.ev, p, ns, mc.g, mc.slot, B.ev.rmx[p], B.si, acc[p],
-                     ovd, sf[p], st);
+    scan_framework<F32, NS>(S, B.ev, p, ns, B.si, A, ovd, sfp, st);
+    scan_guests<F32, GN, NS>(S, B.H, CA, chain, B.ev, p, ns, mc.g, mc.slot, B.ev.rmx[p], B.si, A, ovd,
+                         sfp, st);
     __syncthreads();
-  }
+  };
+  scan_position(0, acc0, sf0);
+  if (npos == 2) scan_position(1, acc1, sf1);
   build_powers<F32>(S, B.ev, npos, ns);
   __syncthreads();
-  kspace<F32>(B, CA, chain, mc.kind == 2, acc);
-  // reduce [e2fw, vdwfw, recip, mixfw, e2g[NG], vdwg[NG], mixg[NG]] per position
-  const int nper = 4 + 3 * NG;
-  AccT<F32> v[32];
-  int n = 0;
-  for (int p = 0; p < npos; ++p) {
-    v[n++] = acc[p].e2fw;
-    v[n++] = acc[p].vdwfw;
-    v[n++] = acc[p].recip;
-    v[n++] = acc[p].mixfw;
-    for (int g2 = 0; g2 < NG; ++g2) v[n++] = acc[p].e2g[g2];
-    for (int g2 = 0; g2 < NG; ++g2) v[n++] = acc[p].vdwg[g2];
-    for (int g2 = 0; g2 < NG; ++g2) v[n++] = acc[p].mixg[g2];
-  }
-  block_reduce(v, n, B.ev.red, B.ev.out);
-  int sfa = block_or(sf[0], B.ev.red_i);
-  int sfb = block_or(sf[1], B.ev.red_i);
+  kspace<F32, GN, NS>(B, CA, chain, mc.kind == 2, acc0, acc1, st);
+  // block totals: out[p * nper + j], j = e2fw, vdwfw, recip, mixfw,
+  // e2g[GN], vdwg[GN], mixg[GN]
+  constexpr int nper = PosAcc<F32, GN>::kN;
+  block_reduce_pos<F32, GN>(acc0, acc1, npos, NG, B.ev.red, B.ev.out);
+  int sfa = block_or(sf0, B.ev.red_i);
+  int sfb = block_or(sf1, B.ev.red_i);
   if (threadIdx.x == 0) {
     const double *R = B.ev.out;
     mc.surf_new = sfa;
@@ -744,7 +965,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       vd[p] = r[1];
       for (int g2 = 0; g2 < NG; ++g2) {
         e2[p] += r[4 + g2];
-        vd[p] += r[4 + NG + g2];
+        vd[p] += r[4 + GN + g2];
       }
     }
     // per-molecule-type terms against type m != mol (delE(m))
@@ -762,9 +983,9 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
         e1 = qfm;
         for (int g2 = 0; g2 < NG; ++g2)
           if (S.g[g2].mol == m) {
-            e1 += S.krecip * r[4 + 2 * NG + g2];
+            e1 += S.krecip * r[4 + 2 * GN + g2];
             e2m += r[4 + g2];
-            vdm += r[4 + NG + g2];
+            vdm += r[4 + GN + g2];
           }
       }
       return e1 + e2m + vdm + delrc_m;
@@ -805,6 +1026,16 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
   }
   __syncthreads();
   return 1;
+}
+
+// evaluate with the site loops unrolled for three-site guests (FP32 path).
+template <bool F32, int GN>
+__device__ __forceinline__ int evaluate_any(BlockShared<F32> &B, const ChainArrays &CA, int chain,
+                                            int &st) {
+  if constexpr (F32) {
+    if (B.mc.ns == 3) return evaluate<F32, GN, 3>(B, CA, chain, st);
+  }
+  return evaluate<F32, GN, 0>(B, CA, chain, st);
 }
 
 // ----------------------------------------------------------------- decide
@@ -851,6 +1082,27 @@ __device__ __forceinline__ void df_inc(float &hi, float &lo, float x) {
   lo = e - (hi - s);
 }
 
+// FP32 path: the production sums of H.pend moves that all saw the current
+// state (the reference adds one move at a time, gcmc.f:1050-1075; here the
+// run is added at once when the state changes or a window ends).
+__device__ inline void flush_stats(const SysDev &S, ChainHdr &H) {
+  if (H.pend == 0) return;
+  const double n = (double)H.pend;
+  for (int i = 0; i < S.ntpguest; ++i) {
+    int m = S.g[i].mol;
+    double dm = double((float)H.nummols[i]);
+    double e = H.energy[m];
+    double sm = double((float)H.surfacemols[m]);
+    H.chainstats[i][0] += n * dm;
+    H.chainstats[i][1] += n * e;
+    H.chainstats[i][2] += n * (e * dm);
+    H.chainstats[i][3] += n * (dm * dm);
+    H.chainstats[i][4] += n * (e * e);
+    H.chainstats[i][5] += n * sm;
+  }
+  H.pend = 0;
+}
+
 // ----------------------------------------------------------------- commit
 // accept_move (mc_moves.f:485-621) for the evaluated move, if accepted.
 template <bool F32>
@@ -886,23 +1138,38 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     float4 *skg = CA.skdf + ((size_t)chain * kMaxG + g) * CA.nkmax;
     const float2 *snew = CA.snew32 + (size_t)chain * CA.nkmax;
     const float2 *sold = CA.sold32 + (size_t)chain * CA.nkmax;
-    for (int k = threadIdx.x; k < S.nk; k += kThreads) {
-      float4 v = skg[k];
-      float2 n = snew[k];
-      if (mc.kind == 1) {
-        df_inc(v.x, v.z, n.x);
-        df_inc(v.y, v.w, n.y);
-      } else if (mc.kind == 2) {
-        df_inc(v.x, v.z, -n.x);
-        df_inc(v.y, v.w, -n.y);
-      } else {
-        float2 o = sold[k];
-        df_inc(v.x, v.z, -o.x);
-        df_inc(v.y, v.w, -o.y);
-        df_inc(v.x, v.z, n.x);
-        df_inc(v.y, v.w, n.y);
+    constexpr int U = 4;  // k-vectors per thread in flight
+    for (int k0 = threadIdx.x; k0 < S.nk; k0 += U * kThreads) {
+      float4 v[U];
+      float2 n[U], o[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int k = k0 + u * kThreads;
+        if (k < S.nk) {
+          v[u] = skg[k];
+          n[u] = snew[k];
+          o[u] = mc.kind >= 3 ? sold[k] : make_float2(0.f, 0.f);
+        }
       }
-      skg[k] = v;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int k = k0 + u * kThreads;
+        if (k < S.nk) {
+          if (mc.kind == 1) {
+            df_inc(v[u].x, v[u].z, n[u].x);
+            df_inc(v[u].y, v[u].w, n[u].y);
+          } else if (mc.kind == 2) {
+            df_inc(v[u].x, v[u].z, -n[u].x);
+            df_inc(v[u].y, v[u].w, -n[u].y);
+          } else {
+            df_inc(v[u].x, v[u].z, -o[u].x);
+            df_inc(v[u].y, v[u].w, -o[u].y);
+            df_inc(v[u].x, v[u].z, n[u].x);
+            df_inc(v[u].y, v[u].w, n[u].y);
+          }
+          skg[k] = v[u];
+        }
+      }
     }
   }
   // molecule order and coordinates
@@ -927,28 +1194,44 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     // remove entry choice-1 from the order list (mc_moves.f:574-590)
     int n = H.nummols[g];
     int c0 = mc.choice - 1;
-    int vals[8];  // capacity <= 4096 = 8 * kThreads
-    int cntv = 0;
-    for (int i = c0 + threadIdx.x; i < n - 1; i += kThreads) vals[cntv++] = ord[i + 1];
+    constexpr int kPer = 8;  // capacity <= 4096 = 8 * kThreads
+    int vals[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int i = c0 + threadIdx.x + j * kThreads;
+      if (i < n - 1) vals[j] = ord[i + 1];
+    }
     __syncthreads();
-    cntv = 0;
-    for (int i = c0 + threadIdx.x; i < n - 1; i += kThreads) ord[i] = vals[cntv++];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int i = c0 + threadIdx.x + j * kThreads;
+      if (i < n - 1) ord[i] = vals[j];
+    }
     __syncthreads();
   }
   if (slot >= 0 && (mc.kind == 1 || mc.kind >= 3) && threadIdx.x < 3 * G.ns) {
     int s = threadIdx.x / 3, d = threadIdx.x % 3;
     size_t b = gslot_base(CA, chain, g, slot) + s;
-    double v = mc.pos[0][s][d];
-    CA.gpos[b * 3 + d] = v;
-    float h = (float)v;
-    reinterpret_cast<float *>(CA.ghi + b)[d] = h;
-    reinterpret_cast<float *>(CA.glo + b)[d] = (float)(v - (double)h);
+    if constexpr (F32) {  // the evaluated position is the hi/lo pair
+      const float h = B.ev.phi[0][s][d], l = B.ev.plo[0][s][d];
+      CA.gpos[b * 3 + d] = (double)h + (double)l;
+      reinterpret_cast<float *>(CA.ghi + b)[d] = h;
+      reinterpret_cast<float *>(CA.glo + b)[d] = l;
+    } else {
+      double v = mc.pos[0][s][d];
+      CA.gpos[b * 3 + d] = v;
+      float h = (float)v;
+      reinterpret_cast<float *>(CA.ghi + b)[d] = h;
+      reinterpret_cast<float *>(CA.glo + b)[d] = (float)(v - (double)h);
+    }
     if (d == 0) {
-      reinterpret_cast<float *>(CA.ghi + b)[3] = (float)G.q[s];
-      reinterpret_cast<float *>(CA.glo + b)[3] = 0.f;
+      const float qh = (float)G.q[s];
+      reinterpret_cast<float *>(CA.ghi + b)[3] = qh;
+      reinterpret_cast<float *>(CA.glo + b)[3] = (float)(G.q[s] - (double)qh);
     }
   }
   if (threadIdx.x == 0 && slot >= 0) {
+    if constexpr (F32) flush_stats(S, H);  // the pending moves saw the old state
     for (int m = 1; m <= S.maxmls; ++m) H.energy[m] += mc.delE[m];
     int mol = G.mol;
     if (mc.kind == 1 || mc.kind == 2) {
@@ -1015,19 +1298,25 @@ __device__ void stats(BlockShared<F32> &B) {
   if (S.laccsample && !mc.accepted) return;
   H.prodcount++;
   H.rollcount++;
-  for (int i = 0; i < S.ntpguest; ++i) {
-    int m = S.g[i].mol;
-    double dm = double((float)H.nummols[i]);
-    double e = H.energy[m];
-    double sm = double((float)H.surfacemols[m]);
-    H.chainstats[i][0] += dm;
-    H.chainstats[i][1] += e;
-    H.chainstats[i][2] += e * dm;
-    H.chainstats[i][3] += dm * dm;
-    H.chainstats[i][4] += e * e;
-    H.chainstats[i][5] += sm;
+  if (F32 && !S.laccsample) {
+    H.pend++;
+  } else {
+    for (int i = 0; i < S.ntpguest; ++i) {
+      int m = S.g[i].mol;
+      double dm = double((float)H.nummols[i]);
+      double e = H.energy[m];
+      double sm = double((float)H.surfacemols[m]);
+      H.chainstats[i][0] += dm;
+      H.chainstats[i][1] += e;
+      H.chainstats[i][2] += e * dm;
+      H.chainstats[i][3] += dm * dm;
+      H.chainstats[i][4] += e * e;
+      H.chainstats[i][5] += sm;
+    }
   }
-  if (H.prodcount % S.nwindsteps == 0) {
+  if (--H.window_left == 0) {  // prodcount is a multiple of nwindsteps
+    H.window_left = S.nwindsteps;
+    flush_stats(S, H);
     double rc = double(H.rollcount);
     H.wsum += rc;
     for (int i = 0; i < S.ntpguest; ++i) {

@@ -256,6 +256,12 @@ int fmc_batch_get_sk(fmc_batch *b, int chain, double *sk, int cap);
 int fmc_batch_last_timing(const fmc_batch *b, double *kernel_ms,
                           int64_t *evals, int64_t *moves);
 
+/* Bytes one fmc_batch_run_cycle call copies host -> device (the fugacity
+ * array, when given) and device -> host (every chain's state record, from
+ * which the statistics are filled).  A measurement helper; no counterpart
+ * in the reference. */
+int fmc_batch_cycle_bytes(const fmc_batch *b, int64_t *h2d, int64_t *d2h);
+
 #ifdef __cplusplus
 }
 #endif
