@@ -254,6 +254,9 @@ def run_ours(args, rank, world, local_rank):
     systems = [F.System.load(d) for d in dirs]
     infos = [s.info() for s in systems]
     batch = F.Batch(systems, specs, precision=F.FMC_PREC_FP32, guest_capacity=1024)
+    # CTAs per chain for each framework, from timed trial cycles (the
+    # chains' state is restored afterwards); set-up, outside the timing
+    clusters = batch.autotune(args.moves) if not args.no_autotune else [1] * len(systems)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
     # per step: the host uploads the chains' fugacities (pinned-free host
@@ -324,6 +327,7 @@ def run_ours(args, rank, world, local_rank):
                                    "double-float sums and S(k)",
                        "chains": len(specs), "moves_per_step_per_chain": args.moves,
                        "parallelism": f"replicas x{world}",
+                       "ctas_per_chain_by_framework": clusters,
                        "l2": "flushed (256 MB write) before every timed step"},
             "trial_moves_per_s": moves / (dev_ms / 1000.0),
             "full_evals_per_s": full / (dev_ms / 1000.0),
@@ -352,6 +356,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

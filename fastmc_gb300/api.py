@@ -165,6 +165,7 @@ class Batch:
                                           guest_capacity, C.byref(h)))
         self._h = h
         self.nchains = len(chains)
+        self._nsys = len(systems)
 
     def set_log(self, cap: int) -> None:
         L.check(L.load().fmc_batch_set_log(self._h, cap))
@@ -199,6 +200,25 @@ class Batch:
         out = np.zeros(2 * nk * (maxmls + 1))
         L.check(L.load().fmc_batch_get_sk(self._h, chain, out.ctypes.data_as(L.dp), out.size))
         return out.reshape(nk, maxmls + 1, 2)
+
+    def set_cluster(self, sizes):
+        """CTAs per chain for the chains of each system (1..8)."""
+        a = (C.c_int * len(sizes))(*[int(v) for v in sizes])
+        L.check(L.load().fmc_batch_set_cluster(self._h, a, len(sizes)))
+
+    def cluster(self):
+        n = self._nsys
+        a = (C.c_int * n)()
+        L.check(L.load().fmc_batch_get_cluster(self._h, a, n))
+        return list(a)
+
+    def autotune(self, nmoves: int = 256):
+        """Pick per-system cluster sizes by timed trial cycles (the chains'
+        state is left unchanged); returns the sizes."""
+        n = self._nsys
+        a = (C.c_int * n)()
+        L.check(L.load().fmc_batch_autotune(self._h, nmoves, a, n))
+        return list(a)
 
     def cycle_bytes(self):
         """(host->device, device->host) bytes of one run() call with a

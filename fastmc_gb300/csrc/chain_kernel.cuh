@@ -1,7 +1,11 @@
-// chain_kernel.cuh -- the persistent chain kernel (one CTA per chain) and
-// the host wrappers each of its instantiations exports.  Every
-// instantiation lives in its own translation unit (chain_*.cu) so they
-// compile in parallel.
+// chain_kernel.cuh -- the persistent chain kernel and the host wrappers each
+// of its instantiations exports.  A chain runs on a cluster of `csize` CTAs
+// (1 .. kMaxCluster): every CTA runs the same control flow on the same
+// replicated state (generator, proposal, decision), takes its share of the
+// framework atoms, guests and k-vectors, and the shares' totals are
+// exchanged through distributed shared memory.  Rank 0 alone writes the
+// chain's guest arrays, log and state record.  Every instantiation lives in
+// its own translation unit (chain_*.cu) so they compile in parallel.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -29,18 +33,26 @@ template <bool F32, int GN>
 __global__ void __launch_bounds__(kThreads, 1)
     chain_kernel(const SysDev *__restrict__ systems, ChainHdr *hdrs, ChainArrays CA,
                  MoveCtx *gctx, LogRec *logs, int logcap, int nmoves, int mode,
-                 const double *__restrict__ ctl_fuga) {
+                 const double *__restrict__ ctl_fuga, const int *__restrict__ chain_ids,
+                 int csize) {
   extern __shared__ __align__(16) unsigned char dyn[];
   BlockShared<F32> &B = *reinterpret_cast<BlockShared<F32> *>(dyn);
-  const int chain = blockIdx.x;
+  const int rank = csize > 1 ? (int)cluster_rank() : 0;
+  const int chain = chain_ids ? chain_ids[blockIdx.x / csize] : (int)blockIdx.x / csize;
   block_copy(&B.H, hdrs + chain);
   __syncthreads();
   block_copy(&B.S, systems + B.H.system);
   if (threadIdx.x == 0) {
     B.flags[0] = 0;
     if (ctl_fuga && mode == kModeMoves) B.H.fuga[0] = ctl_fuga[chain];  // host control block
+    B.ev.rank = rank;
+    B.ev.csize = csize;
+    B.xseq = B.cseq = 0u;
+    B.cflag = 0u;
   }
+  if (threadIdx.x < kMaxCluster) B.xflag[threadIdx.x] = 0u;
   __syncthreads();
+  if (csize > 1) cluster_barrier();  // every CTA's flags are cleared before anyone posts
   int st = 0;
   if (mode == kModeMoves) {
     for (int it = 0; it < nmoves; ++it) {
@@ -51,7 +63,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         decide(B, true);
         if (full) B.H.evals += B.mc.npos;
         else if (B.mc.overlap) B.H.overlap_exits++;
-        if (logcap > 0 && B.H.log_n < logcap) {
+        if (logcap > 0 && B.H.log_n < logcap && rank == 0) {
           LogRec &L = logs[(size_t)chain * logcap + B.H.log_n];
           L.move = B.mc.kind;
           L.iguest = B.mc.g + 1;
@@ -71,7 +83,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (threadIdx.x == 0) {
         stats(B);
         if (logcap > 0 && B.H.log_n < logcap) {
-          logs[(size_t)chain * logcap + B.H.log_n].nmols_after = B.H.nummols[B.mc.g];
+          if (rank == 0) logs[(size_t)chain * logcap + B.H.log_n].nmols_after = B.H.nummols[B.mc.g];
           B.H.log_n++;
         }
       }
@@ -120,20 +132,62 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (st) atomicOr(&B.flags[0], st);
   __syncthreads();
+  if (csize > 1) {
+    cluster_barrier();  // every CTA's status is final
+    if (rank == 0 && threadIdx.x == 0)
+      for (int q = 1; q < csize; ++q) B.flags[0] |= dsmem_load_s32(dsmem_addr(&B.flags[0], q));
+    cluster_barrier();  // the peers stay resident until rank 0 has read them
+  }
   if (threadIdx.x == 0) B.H.status |= B.flags[0];
   __syncthreads();
-  block_copy(hdrs + chain, &B.H);
+  if (rank == 0) block_copy(hdrs + chain, &B.H);
 }
 
 
 // Launch and set-up of one instantiation, for the host side of the library.
+// `nchains` chains (ids in chain_ids, or 0..nchains-1 when null), each on a
+// cluster of csize CTAs.
 template <bool F32, int GN>
-cudaError_t launch_chain(dim3 grid, size_t smem, cudaStream_t stream, const SysDev *systems,
-                         ChainHdr *hdrs, const ChainArrays &CA, MoveCtx *gctx, LogRec *logs,
-                         int logcap, int nmoves, int mode, const double *ctl_fuga) {
-  chain_kernel<F32, GN><<<grid, kThreads, smem, stream>>>(systems, hdrs, CA, gctx, logs, logcap,
-                                                          nmoves, mode, ctl_fuga);
-  return cudaGetLastError();
+cudaError_t launch_chain(int nchains, int csize, const int *chain_ids, size_t smem,
+                         cudaStream_t stream, const SysDev *systems, ChainHdr *hdrs,
+                         const ChainArrays &CA, MoveCtx *gctx, LogRec *logs, int logcap,
+                         int nmoves, int mode, const double *ctl_fuga) {
+  if (csize == 1) {
+    chain_kernel<F32, GN><<<nchains, kThreads, smem, stream>>>(
+        systems, hdrs, CA, gctx, logs, logcap, nmoves, mode, ctl_fuga, chain_ids, 1);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nchains * csize));
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, chain_kernel<F32, GN>, systems, hdrs, CA, gctx, logs, logcap,
+                            nmoves, mode, ctl_fuga, chain_ids, csize);
+}
+
+// Clusters of csize CTAs that can be resident at once (0: cannot launch).
+template <bool F32, int GN>
+cudaError_t max_clusters(int csize, size_t smem, int *out) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)csize);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaOccupancyMaxActiveClusters(out, chain_kernel<F32, GN>, &cfg);
 }
 
 template <bool F32, int GN>

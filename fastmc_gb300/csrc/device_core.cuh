@@ -281,6 +281,59 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async;" ::: "memory");
 }
 
+// ------------------------------------------------- thread-block clusters
+// A chain may run on a cluster of up to kMaxCluster CTAs.  Exchanges between
+// them go through distributed shared memory: release/acquire flag stores
+// into the peers' shared memory and bounded polling of one's own flags.
+constexpr int kMaxCluster = 8;
+
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Every thread of every CTA of the cluster (unconditional call sites only).
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+// Shared-memory address of the same variable in CTA `rank` of the cluster.
+__device__ __forceinline__ unsigned dsmem_addr(const void *p, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void dsmem_store_release(unsigned addr, unsigned v) {
+  asm volatile("st.release.cluster.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned dsmem_load_acquire(unsigned addr) {
+  unsigned v;
+  asm volatile("ld.acquire.cluster.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ double dsmem_load_f64(unsigned addr) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ int dsmem_load_s32(unsigned addr) {
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+// Poll one's own flag until it reaches `seq`; false if it did not in time.
+__device__ __forceinline__ bool wait_flag(const unsigned *flag, unsigned seq) {
+  const unsigned a = smem_u32(flag);
+  for (int it = 0; it < kWaitLimit; ++it)
+    if ((int)(dsmem_load_acquire(a) - seq) >= 0) return true;
+  return false;
+}
+// [lo, hi) of `n` items for member `r` of `c`.
+__device__ __forceinline__ void share_of(int n, int r, int c, int &lo, int &hi) {
+  lo = (int)(((long long)n * r) / c);
+  hi = (int)(((long long)n * (r + 1)) / c);
+}
+
 // ----------------------------------------------------------- MZT generator
 // duni (utility_pack.f:2768-2857): REAL*4 lagged subtract-with-borrow plus
 // a Weyl term; bit-exact because only float add/sub/compare are used.

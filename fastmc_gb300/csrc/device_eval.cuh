@@ -42,6 +42,7 @@ struct EvalSmem {
   int seg_pref[kMaxSeg + 1];
   int seg_shift[kMaxSeg];
   int nslots;
+  int rank, csize;          // this CTA's place in the chain's cluster
   int red_i[kWarps + 1];
   double red[kWarps * 32];
   double out[64];
@@ -341,10 +342,11 @@ __device__ __forceinline__ void scan_framework(const SysDev &S, EvalSmem<F32> &s
                                                int &sf, int &st) {
   const int ns = NS > 0 ? NS : ns_rt;
   int nslot = sm.nslots;
-  int total = sm.seg_pref[nslot];
+  int t0, total;  // this CTA's share of the candidate atoms
+  share_of(sm.seg_pref[nslot], sm.rank, sm.csize, t0, total);
   if constexpr (!F32) {
     double e2 = 0.0, vdw = 0.0;
-    for (int t = threadIdx.x; t < total; t += kThreads) {
+    for (int t = t0 + threadIdx.x; t < total; t += kThreads) {
       int s = find_slot(sm.seg_pref, nslot, t);
       int a = sm.seg_start[s] + (t - sm.seg_pref[s]);
       int sh = sm.seg_shift[s];
@@ -378,7 +380,7 @@ __device__ __forceinline__ void scan_framework(const SysDev &S, EvalSmem<F32> &s
     float vdw = 0.0f;
     int cnt = 0;
     const float *Lh = S.boxh, *Ll = S.boxl;
-    for (int t = threadIdx.x; t < total; t += kThreads) {
+    for (int t = t0 + threadIdx.x; t < total; t += kThreads) {
       int s = find_slot(sm.seg_pref, nslot, t);
       int a = sm.seg_start[s] + (t - sm.seg_pref[s]);
       int sh = sm.seg_shift[s];
@@ -446,7 +448,9 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
       const float4 *gh = CA.ghi + ((size_t)chain * kMaxG + g2) * CA.cap * kMaxS;
       const float4 *gl = CA.glo + ((size_t)chain * kMaxG + g2) * CA.cap * kMaxS;
       float pre2 = pre * pre;
-      for (int i = threadIdx.x; i < n2; i += kThreads) {
+      int i0, i1;
+      share_of(n2, sm.rank, sm.csize, i0, i1);
+      for (int i = i0 + threadIdx.x; i < i1; i += kThreads) {
         int slot = ord[i];
         if (g2 == self_g && slot == self_slot) continue;
         float4 q0 = gh[(size_t)slot * kMaxS];
@@ -490,7 +494,9 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
     } else {
       double pre2 = (double)pre * (double)pre;
       double e2 = 0.0, vdw = 0.0;
-      for (int i = threadIdx.x; i < n2; i += kThreads) {
+      int i0, i1;
+      share_of(n2, sm.rank, sm.csize, i0, i1);
+      for (int i = i0 + threadIdx.x; i < i1; i += kThreads) {
         int slot = ord[i];
         if (g2 == self_g && slot == self_slot) continue;
         size_t base = (((size_t)chain * kMaxG + g2) * CA.cap + slot) * kMaxS;

@@ -89,26 +89,27 @@ __global__ void __launch_bounds__(kThreads) structure_factor_kernel(
 }
 
 // The chain kernel's instantiations (chain_f32_g1.cu, chain_f32_g4.cu,
-// chain_f64.cu): launch wrappers and shared-memory set-up.
+// chain_f64.cu): launch wrappers, shared-memory set-up, cluster occupancy.
 template <bool F32, int GN>
-cudaError_t launch_chain(dim3 grid, size_t smem, cudaStream_t stream, const SysDev *systems,
-                         ChainHdr *hdrs, const ChainArrays &CA, MoveCtx *gctx, LogRec *logs,
-                         int logcap, int nmoves, int mode, const double *ctl_fuga);
+cudaError_t launch_chain(int nchains, int csize, const int *chain_ids, size_t smem,
+                         cudaStream_t stream, const SysDev *systems, ChainHdr *hdrs,
+                         const ChainArrays &CA, MoveCtx *gctx, LogRec *logs, int logcap,
+                         int nmoves, int mode, const double *ctl_fuga);
 template <bool F32, int GN>
 cudaError_t set_chain_smem(size_t smem);
-extern template cudaError_t launch_chain<true, 1>(dim3, size_t, cudaStream_t, const SysDev *,
-                                                  ChainHdr *, const ChainArrays &, MoveCtx *,
-                                                  LogRec *, int, int, int, const double *);
-extern template cudaError_t launch_chain<true, kMaxG>(dim3, size_t, cudaStream_t, const SysDev *,
-                                                      ChainHdr *, const ChainArrays &, MoveCtx *,
-                                                      LogRec *, int, int, int, const double *);
-extern template cudaError_t launch_chain<false, kMaxG>(dim3, size_t, cudaStream_t,
-                                                       const SysDev *, ChainHdr *,
-                                                       const ChainArrays &, MoveCtx *, LogRec *,
-                                                       int, int, int, const double *);
-extern template cudaError_t set_chain_smem<true, 1>(size_t);
-extern template cudaError_t set_chain_smem<true, kMaxG>(size_t);
-extern template cudaError_t set_chain_smem<false, kMaxG>(size_t);
+template <bool F32, int GN>
+cudaError_t max_clusters(int csize, size_t smem, int *out);
+#define FMC_CHAIN_EXTERN(F32, GN)                                                               \
+  extern template cudaError_t launch_chain<F32, GN>(int, int, const int *, size_t, cudaStream_t, \
+                                                    const SysDev *, ChainHdr *,                  \
+                                                    const ChainArrays &, MoveCtx *, LogRec *, int, \
+                                                    int, int, const double *);                   \
+  extern template cudaError_t set_chain_smem<F32, GN>(size_t);                                   \
+  extern template cudaError_t max_clusters<F32, GN>(int, size_t, int *);
+FMC_CHAIN_EXTERN(true, 1)
+FMC_CHAIN_EXTERN(true, kMaxG)
+FMC_CHAIN_EXTERN(false, kMaxG)
+#undef FMC_CHAIN_EXTERN
 
 // Modes of the chain kernel (chain_kernel.cuh).
 constexpr int kModeMoves = 0;
@@ -600,28 +601,102 @@ struct Chains {
   double last_ms = 0.0;
   long long last_evals = 0, last_moves = 0;
   std::vector<ChainHdr> host_hdr;
+  // chains grouped by the cluster size of their system; one launch per
+  // group, the groups on their own streams (parallel branches of the graph)
+  struct Group {
+    int csize = 1, n = 0;
+    DBuf<int> ids;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+  };
+  std::vector<int> csys;  // cluster size per system
+  std::vector<std::unique_ptr<Group>> groups;
+  cudaEvent_t fork = nullptr;
 
   ~Chains() {
+    for (auto &g : groups) {
+      if (g->done) cudaEventDestroy(g->done);
+      if (g->stream) cudaStreamDestroy(g->stream);
+    }
+    if (fork) cudaEventDestroy(fork);
     if (graph) cudaGraphExecDestroy(graph);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
   }
 
+  cudaError_t launch_one(int n, int csize, const int *ids, cudaStream_t st, int mode, int nmoves) {
+    if (precision == FMC_PREC_FP32 && gn == 1)
+      return launch_chain<true, 1>(n, csize, ids, smem, st, sysarr.p, hdr.p, CA, ctx.p, logs.p,
+                                   logcap, nmoves, mode, ctl_fuga.p);
+    if (precision == FMC_PREC_FP32)
+      return launch_chain<true, kMaxG>(n, csize, ids, smem, st, sysarr.p, hdr.p, CA, ctx.p,
+                                       logs.p, logcap, nmoves, mode, ctl_fuga.p);
+    return launch_chain<false, kMaxG>(n, csize, ids, smem, st, sysarr.p, hdr.p, CA, ctx.p, logs.p,
+                                      logcap, nmoves, mode, ctl_fuga.p);
+  }
+
+  int occupancy(int csize) {
+    int n = 0;
+    cudaError_t e;
+    if (precision == FMC_PREC_FP32 && gn == 1) e = max_clusters<true, 1>(csize, smem, &n);
+    else if (precision == FMC_PREC_FP32) e = max_clusters<true, kMaxG>(csize, smem, &n);
+    else e = max_clusters<false, kMaxG>(csize, smem, &n);
+    FMC_CUDA(e);
+    return n;
+  }
+
+  // Regroup the chains after a change of the per-system cluster sizes.
+  void set_clusters(const std::vector<int> &cs) {
+    std::vector<int> sys_of(nchains);
+    if (host_hdr.size() != (size_t)nchains || headers_stale) pull_headers();
+    for (int c = 0; c < nchains; ++c) sys_of[c] = host_hdr[c].system;
+    for (int v : cs)
+      if (v < 1 || v > kMaxCluster) raise(FMC_ERR_ARG, "cluster size must be 1..8");
+    for (auto &g : groups) {
+      if (g->done) cudaEventDestroy(g->done);
+      if (g->stream) cudaStreamDestroy(g->stream);
+    }
+    groups.clear();
+    csys = cs;
+    for (int v = 1; v <= kMaxCluster; ++v) {
+      std::vector<int> ids;
+      for (int c = 0; c < nchains; ++c)
+        if (csys[sys_of[c]] == v) ids.push_back(c);
+      if (ids.empty()) continue;
+      if (v > 1 && occupancy(v) < 1)
+        raise(FMC_ERR_ARG, "clusters of " + std::to_string(v) + " CTAs cannot be resident");
+      auto g = std::make_unique<Group>();
+      g->csize = v;
+      g->n = (int)ids.size();
+      g->ids.upload(ids);
+      FMC_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+      FMC_CUDA(cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming));
+      groups.push_back(std::move(g));
+    }
+    if (!fork) FMC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    if (graph) {
+      cudaGraphExecDestroy(graph);
+      graph = nullptr;
+    }
+    graph_moves = -1;
+  }
+
   void launch(int mode, int nmoves) {
     headers_stale = true;
-    dim3 grid(nchains);
-    cudaError_t e;
-    if (precision == FMC_PREC_FP32 && gn == 1)
-      e = launch_chain<true, 1>(grid, smem, stream, sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
-                                nmoves, mode, ctl_fuga.p);
-    else if (precision == FMC_PREC_FP32)
-      e = launch_chain<true, kMaxG>(grid, smem, stream, sysarr.p, hdr.p, CA, ctx.p, logs.p, logcap,
-                                    nmoves, mode, ctl_fuga.p);
-    else
-      e = launch_chain<false, kMaxG>(grid, smem, stream, sysarr.p, hdr.p, CA, ctx.p, logs.p,
-                                     logcap, nmoves, mode, ctl_fuga.p);
-    FMC_CUDA(e);
+    if (groups.size() <= 1 && (groups.empty() || groups[0]->csize == 1)) {
+      FMC_CUDA(launch_one(nchains, 1, nullptr, stream, mode, nmoves));
+      return;
+    }
+    // fork: every group waits for what is queued on the chain stream, and
+    // the chain stream waits for every group
+    FMC_CUDA(cudaEventRecord(fork, stream));
+    for (auto &g : groups) {
+      FMC_CUDA(cudaStreamWaitEvent(g->stream, fork, 0));
+      FMC_CUDA(launch_one(g->n, g->csize, g->ids.p, g->stream, mode, nmoves));
+      FMC_CUDA(cudaEventRecord(g->done, g->stream));
+    }
+    for (auto &g : groups) FMC_CUDA(cudaStreamWaitEvent(stream, g->done, 0));
   }
 
   void sync() { FMC_CUDA(cudaStreamSynchronize(stream)); }
@@ -907,6 +982,46 @@ struct fmc_plain {
 struct fmc_batch {
   Chains C;
 };
+
+// Device copy of every chain's mutable state (for trial runs).
+struct ChainSnapshot {
+  DBuf<ChainHdr> hdr;
+  DBuf<double> gpos;
+  DBuf<float4> ghi, glo, skdf;
+  DBuf<int> ord, freel;
+  DBuf<double2> sk;
+};
+
+template <class T>
+static void copy_buf(DBuf<T> &dst, const DBuf<T> &src, cudaStream_t st) {
+  if (dst.n != src.n) dst.alloc(src.n);
+  if (src.n) FMC_CUDA(cudaMemcpyAsync(dst.p, src.p, src.n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+}
+
+static void save_state(Chains &C, ChainSnapshot &s) {
+  copy_buf(s.hdr, C.hdr, C.stream);
+  copy_buf(s.gpos, C.gpos, C.stream);
+  copy_buf(s.ghi, C.ghi, C.stream);
+  copy_buf(s.glo, C.glo, C.stream);
+  copy_buf(s.skdf, C.skdf, C.stream);
+  copy_buf(s.ord, C.ord, C.stream);
+  copy_buf(s.freel, C.freel, C.stream);
+  copy_buf(s.sk, C.sk, C.stream);
+  C.sync();
+}
+
+static void restore_state(Chains &C, ChainSnapshot &s) {
+  copy_buf(C.hdr, s.hdr, C.stream);
+  copy_buf(C.gpos, s.gpos, C.stream);
+  copy_buf(C.ghi, s.ghi, C.stream);
+  copy_buf(C.glo, s.glo, C.stream);
+  copy_buf(C.skdf, s.skdf, C.stream);
+  copy_buf(C.ord, s.ord, C.stream);
+  copy_buf(C.freel, s.freel, C.stream);
+  copy_buf(C.sk, s.sk, C.stream);
+  C.sync();
+  C.headers_stale = true;
+}
 
 extern "C" {
 
@@ -1485,6 +1600,81 @@ int fmc_batch_get_sk(fmc_batch *b, int chain, double *sk, int cap) {
     if (!b || !sk) raise(FMC_ERR_ARG, "null argument");
     if (chain < 0 || chain >= b->C.nchains) raise(FMC_ERR_ARG, "bad chain index");
     return chain_sk(b->C, chain, sk, cap);
+  });
+}
+
+int fmc_batch_autotune(fmc_batch *b, int nmoves, int *csize_out, int nsys) {
+  return guard([&] {
+    if (!b) raise(FMC_ERR_ARG, "null batch");
+    Chains &C = b->C;
+    if (nmoves < 1) raise(FMC_ERR_ARG, "nmoves must be positive");
+    if (csize_out && nsys != (int)C.sys.size())
+      raise(FMC_ERR_ARG, "one cluster size per system is required");
+    ChainSnapshot snap;
+    save_state(C, snap);
+    const long long ev0 = C.last_evals, mv0 = C.last_moves;
+    const double ms0 = C.last_ms;
+    // time of one cycle from the saved state (best of two)
+    auto trial = [&](const std::vector<int> &cs) {
+      C.set_clusters(cs);
+      double best = 1e300;
+      for (int r = 0; r < 2; ++r) {
+        restore_state(C, snap);
+        run_cycle(C, nmoves);
+        best = std::min(best, C.last_ms);
+      }
+      return best;
+    };
+    const int ns = (int)C.sys.size();
+    std::vector<int> cur(ns, 1);
+    double tcur = trial(cur);
+    // greedy: double the cluster of one system at a time while it helps
+    for (;;) {
+      std::vector<int> best_cs;
+      double tbest = tcur;
+      for (int i = 0; i < ns; ++i) {
+        if (cur[i] * 2 > kMaxCluster) continue;
+        std::vector<int> cs = cur;
+        cs[i] *= 2;
+        if (C.occupancy(cs[i]) < 1) continue;
+        double t = trial(cs);
+        if (t < tbest * 0.97) {
+          tbest = t;
+          best_cs = cs;
+        }
+      }
+      if (best_cs.empty()) break;
+      cur = best_cs;
+      tcur = tbest;
+    }
+    C.set_clusters(cur);
+    restore_state(C, snap);
+    C.last_evals = ev0;
+    C.last_moves = mv0;
+    C.last_ms = ms0;
+    if (csize_out)
+      for (int i = 0; i < nsys; ++i) csize_out[i] = cur[i];
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_set_cluster(fmc_batch *b, const int *csize, int nsys) {
+  return guard([&] {
+    if (!b || !csize) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (nsys != (int)C.sys.size()) raise(FMC_ERR_ARG, "one cluster size per system is required");
+    C.set_clusters(std::vector<int>(csize, csize + nsys));
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_get_cluster(const fmc_batch *b, int *csize, int nsys) {
+  return guard([&] {
+    if (!b || !csize) raise(FMC_ERR_ARG, "null argument");
+    const Chains &C = b->C;
+    if (nsys != (int)C.sys.size()) raise(FMC_ERR_ARG, "one cluster size per system is required");
+    for (int i = 0; i < nsys; ++i) csize[i] = C.csys.empty() ? 1 : C.csys[i];
+    return FMC_OK;
   });
 }
 

@@ -43,7 +43,60 @@ struct BlockShared {
   float geof[4];     // FP32 path: shift a, b, c and the rotation angle
   double vtmp[3];
   int flags[4];
+  // cluster exchange (chains on more than one CTA): per-CTA partial totals,
+  // double-buffered, and the flags the peers raise in this CTA's memory
+  double xv[2][40];
+  unsigned xflag[kMaxCluster];  // xflag[q]: last exchange CTA q has posted here
+  unsigned cflag;               // last commit rank 0 has finished
+  unsigned xseq, cseq;          // exchanges and commits done (same in every CTA)
 };
+
+// Sum ev.out[0..nv) over the CTAs of the chain's cluster, in rank order (so
+// every CTA gets the same bits).  All threads; no-op on a single CTA.
+template <bool F32>
+__device__ void cluster_exchange(BlockShared<F32> &B, int nv, int &st) {
+  const int C = B.ev.csize, r = B.ev.rank;
+  if (C == 1) return;
+  const unsigned n = B.xseq + 1;
+  const int par = n & 1;
+  for (int i = threadIdx.x; i < nv; i += kThreads) B.xv[par][i] = B.ev.out[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    B.xseq = n;
+    for (int q = 0; q < C; ++q)
+      if (q != r) dsmem_store_release(dsmem_addr(&B.xflag[r], q), n);
+    for (int q = 0; q < C; ++q)
+      if (q != r && !wait_flag(&B.xflag[q], n)) st |= kStWait;
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    const int i = threadIdx.x;
+    double sum = 0.0;
+    for (int q = 0; q < C; ++q)
+      sum += q == r ? B.xv[par][i] : dsmem_load_f64(dsmem_addr(&B.xv[par][i], q));
+    B.ev.out[i] = sum;
+  }
+  __syncthreads();
+}
+
+// After an accepted commit: rank 0 has written the chain's guest arrays;
+// the other CTAs wait until those writes are visible before they read them.
+template <bool F32>
+__device__ void cluster_commit_sync(BlockShared<F32> &B, int &st) {
+  const int C = B.ev.csize;
+  if (C == 1) return;
+  if (B.ev.rank == 0) __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned n = ++B.cseq;
+    if (B.ev.rank == 0) {
+      for (int q = 1; q < C; ++q) dsmem_store_release(dsmem_addr(&B.cflag, q), n);
+    } else if (!wait_flag(&B.cflag, n)) {
+      st |= kStWait;
+    }
+  }
+  __syncthreads();
+}
 
 __device__ __forceinline__ size_t gslot_base(const ChainArrays &CA, int chain, int g, int slot) {
   return (((size_t)chain * kMaxG + g) * CA.cap + slot) * kMaxS;
@@ -685,7 +738,9 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
     double e[2] = {0.0, 0.0}, mfw[2] = {0.0, 0.0}, mg[2][GN];
 #pragma unroll
     for (int g2 = 0; g2 < GN; ++g2) mg[0][g2] = mg[1][g2] = 0.0;
-    for (int k = threadIdx.x; k < S.nk; k += kThreads) {
+    int kb, ke;  // this CTA's share of the k-vectors
+    share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
+    for (int k = kb + threadIdx.x; k < ke; k += kThreads) {
       int4 lmn = __ldg(S.klmn + k);
       int am = abs(lmn.y), an = abs(lmn.z);
       bool cm = lmn.y < 0, cn = lmn.z < 0;
@@ -765,7 +820,9 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
     for (int g2 = 0; g2 < GN; ++g2) mg[0][g2] = mg[1][g2] = 0.f;
     int cnt = 0;
     constexpr int U = 2;
-    for (int k0 = threadIdx.x; k0 < S.nk; k0 += U * kThreads) {
+    int kb, ke;  // this CTA's share of the k-vectors
+    share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
+    for (int k0 = kb + threadIdx.x; k0 < ke; k0 += U * kThreads) {
       unsigned pk[U];
       float akk[U];
       float4 fw[U], st4[U];
@@ -775,7 +832,7 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
         pk[u] = 0u;
         akk[u] = 0.f;
         fw[u] = st4[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (k < S.nk) {
+        if (k < ke) {
           pk[u] = __ldg(S.kpk + k);
           akk[u] = __ldg(S.akk32 + k);
           fw[u] = __ldg(S.skfw_df + k);
@@ -792,7 +849,7 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int k = k0 + u * kThreads;
-        if (k >= S.nk) continue;
+        if (k >= ke) continue;
         const int lm = (int)(pk[u] & 0xffffu), nz = (int)(pk[u] >> 16) - 128;
         const int an = abs(nz);
         const bool cn = nz < 0;
@@ -947,6 +1004,15 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
   block_reduce_pos<F32, GN>(acc0, acc1, npos, NG, B.ev.red, B.ev.out);
   int sfa = block_or(sf0, B.ev.red_i);
   int sfb = block_or(sf1, B.ev.red_i);
+  if (B.ev.csize > 1) {  // totals over the cluster
+    if (threadIdx.x == 0) {
+      B.ev.out[2 * nper] = sfa;
+      B.ev.out[2 * nper + 1] = sfb;
+    }
+    cluster_exchange(B, 2 * nper + 2, st);
+    sfa = B.ev.out[2 * nper] > 0.5;
+    sfb = B.ev.out[2 * nper + 1] > 0.5;
+  }
   if (threadIdx.x == 0) {
     const double *R = B.ev.out;
     mc.surf_new = sfa;
@@ -1119,7 +1185,9 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     double2 *skg = CA.sk + ((size_t)chain * kMaxG + g) * CA.nkmax;
     const double2 *snew = CA.snew + (size_t)chain * CA.nkmax;
     const double2 *sold = CA.sold + (size_t)chain * CA.nkmax;
-    for (int k = threadIdx.x; k < S.nk; k += kThreads) {
+    int kb, ke;
+    share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
+    for (int k = kb + threadIdx.x; k < ke; k += kThreads) {
       double2 v = skg[k], n = snew[k];
       if (mc.kind == 1) {
         v.x += n.x;
@@ -1139,13 +1207,15 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     const float2 *snew = CA.snew32 + (size_t)chain * CA.nkmax;
     const float2 *sold = CA.sold32 + (size_t)chain * CA.nkmax;
     constexpr int U = 4;  // k-vectors per thread in flight
-    for (int k0 = threadIdx.x; k0 < S.nk; k0 += U * kThreads) {
+    int kb, ke;
+    share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
+    for (int k0 = kb + threadIdx.x; k0 < ke; k0 += U * kThreads) {
       float4 v[U];
       float2 n[U], o[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int k = k0 + u * kThreads;
-        if (k < S.nk) {
+        if (k < ke) {
           v[u] = skg[k];
           n[u] = snew[k];
           o[u] = mc.kind >= 3 ? sold[k] : make_float2(0.f, 0.f);
@@ -1154,7 +1224,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int k = k0 + u * kThreads;
-        if (k < S.nk) {
+        if (k < ke) {
           if (mc.kind == 1) {
             df_inc(v[u].x, v[u].z, n[u].x);
             df_inc(v[u].y, v[u].w, n[u].y);
@@ -1184,13 +1254,13 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
         st |= kStCapacity;
         slot = -1;
       }
-      if (slot >= 0) ord[H.nummols[g]] = slot;
+      if (slot >= 0 && B.ev.rank == 0) ord[H.nummols[g]] = slot;
     }
     B.flags[1] = slot;
   }
   __syncthreads();
   const int slot = B.flags[1];
-  if (mc.kind == 2) {
+  if (mc.kind == 2 && B.ev.rank == 0) {
     // remove entry choice-1 from the order list (mc_moves.f:574-590)
     int n = H.nummols[g];
     int c0 = mc.choice - 1;
@@ -1209,7 +1279,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     }
     __syncthreads();
   }
-  if (slot >= 0 && (mc.kind == 1 || mc.kind >= 3) && threadIdx.x < 3 * G.ns) {
+  if (slot >= 0 && (mc.kind == 1 || mc.kind >= 3) && threadIdx.x < 3 * G.ns && B.ev.rank == 0) {
     int s = threadIdx.x / 3, d = threadIdx.x % 3;
     size_t b = gslot_base(CA, chain, g, slot) + s;
     if constexpr (F32) {  // the evaluated position is the hi/lo pair
@@ -1249,7 +1319,10 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
         }
       }
       H.nummols[g] += sg;
-      if (mc.kind == 2) freel[H.nfree[g]++] = slot;
+      if (mc.kind == 2) {
+        if (B.ev.rank == 0) freel[H.nfree[g]] = slot;
+        H.nfree[g]++;
+      }
     } else {
       // surface molecule tally of a displacement (gcmc.f:1900-1906)
       if (mc.surf_old && !mc.surf_new) {
@@ -1261,6 +1334,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     }
   }
   __syncthreads();
+  cluster_commit_sync(B, st);
 }
 
 __device__ inline double calc_qst(double E, double N, double N2, double EN, double T) {

@@ -251,6 +251,22 @@ int fmc_batch_get_log(fmc_batch *b, int chain, fmc_move_log *log, int cap,
 int fmc_batch_get_coords(fmc_batch *b, int chain, double *xyz, int cap, int *n);
 int fmc_batch_get_sk(fmc_batch *b, int chain, double *sk, int cap);
 
+/* Thread-block clusters: the chains of system i run on clusters of
+ * csize[i] CTAs (1..8; default 1).  Each CTA of a cluster takes a share of
+ * the chain's framework atoms, guests and k-vectors; results do not depend
+ * on the cluster size beyond the order of the final sums.  nsys must be the
+ * batch's number of systems.  No counterpart in the reference (its chains
+ * are MPI ranks of one core each). */
+int fmc_batch_set_cluster(fmc_batch *b, const int *csize, int nsys);
+int fmc_batch_get_cluster(const fmc_batch *b, int *csize, int nsys);
+
+/* Autotuner: picks the cluster size of every system by timing trial cycles
+ * of `nmoves` moves from a copy of the chains' state (greedy doubling of
+ * one system's cluster at a time while the cycle gets >3% faster), sets
+ * it, and restores the chains' state, so the chains continue exactly as if
+ * it had not run.  csize_out (nullable) receives the choice. */
+int fmc_batch_autotune(fmc_batch *b, int nmoves, int *csize_out, int nsys);
+
 /* Timing of the last fmc_batch_run: device milliseconds of the persistent
  * kernel (CUDA events on its stream) and the completed evaluations. */
 int fmc_batch_last_timing(const fmc_batch *b, double *kernel_ms,
