@@ -195,6 +195,65 @@ def profiled_traffic():
         return None
 
 
+def reduce_over_ranks(dist, device, max_vals, sum_vals):
+    """Replicas: the job's time is the slowest rank's, its work the sum of
+    every rank's.  Returns (max_vals, sum_vals) over all ranks."""
+    if dist is None:
+        return list(max_vals), list(sum_vals)
+    import torch
+    t = torch.tensor(list(max_vals), device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e = torch.tensor(list(sum_vals), device=device, dtype=torch.float64)
+    dist.all_reduce(e)
+    return [float(x) for x in t.tolist()], [float(x) for x in e.tolist()]
+
+
+def plain_single_chain(F, seconds: float = 2.0):
+    """The single-chain GPU paths the batched kernel is compared with, on
+    config 1 (25.6 A, 1536 atoms, kmax 7, P 0.1 bar, one CTA):
+    - "device": one chain run by the persistent kernel (FP32);
+    - "per_move_abi": the drop-in path, one C-ABI call per trial insertion /
+      deletion and one per commit, driven from the host (FP64, random
+      positions from numpy), the way a Fortran host would call it.
+    Both in trial-move ΔE evaluations per second."""
+    import numpy as np
+    from fastmc_gb300 import synthetic as syn
+    d = tempfile.mkdtemp()
+    syn.write_inputs(d, syn.config1())
+    sysm = F.System.load(d)
+    out = {}
+    b = F.Batch([sysm], [{"seed": 1}], precision=F.FMC_PREC_FP32, guest_capacity=1024)
+    b.run(256)
+    s0 = b.stats()[0]
+    t0 = time.perf_counter()
+    dev_ms = 0.0
+    while time.perf_counter() - t0 < seconds:
+        b.run(1024)
+        dev_ms += b.last_timing()[0]
+    s1 = b.stats()[0]
+    out["device"] = {"value": (trial_evals(s1) - trial_evals(s0)) / (dev_ms / 1000.0), "unit": UNIT,
+                     "workload": "config1 one chain, FP32, device-resident"}
+    p = F.PlainEngine(sysm, F.FMC_PREC_FP64, 1024)
+    rng = np.random.default_rng(1)
+    n = evals = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        if n == 0 or rng.random() < 0.5:
+            ax = rng.normal(size=3)
+            ax /= np.linalg.norm(ax)
+            xyz = np.outer([0.0, 1.16, -1.16], ax) + rng.uniform(0, 25.6, 3)
+            p.insertion(1, xyz)
+        else:
+            p.deletion(1, int(rng.integers(1, n + 1)))
+        evals += 1
+        p.commit(float(rng.random()))
+        n = p.nummols(1)
+    out["per_move_abi"] = {"value": evals / (time.perf_counter() - t0), "unit": UNIT,
+                           "workload": "config1 one chain, FP64, host-driven per-move C ABI "
+                                       "(insert/delete, wall time)"}
+    return out
+
+
 # ------------------------------------------------------------------ arms
 def run_reference(args, rank, world):
     if rank != 0:
@@ -293,13 +352,8 @@ def run_ours(args, rank, world, local_rank):
     moves = sum(after[c].moves - before[c].moves for c in range(len(specs)))
     dev_ms = sum(ms_list)
     e2e_s = sum(wall)
-    if dist:
-        t = torch.tensor([dev_ms, e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e = torch.tensor([evals, moves, full], device="cuda", dtype=torch.float64)
-        dist.all_reduce(e)
-        dev_ms, e2e_s = float(t[0].item()), float(t[1].item())
-        evals, moves, full = int(e[0].item()), int(e[1].item()), int(e[2].item())
+    (dev_ms, e2e_s), (evals, moves, full) = reduce_over_ranks(
+        dist, "cuda", [dev_ms, e2e_s], [evals, moves, full])
     value = evals / (dev_ms / 1000.0)
 
     # roofline of the chain kernel: algorithmic bytes of the completed
@@ -342,6 +396,8 @@ def run_ours(args, rank, world, local_rank):
                     "d2h_bytes_per_step": d2h},
             "cpu_baseline": cpu,
         }
+        if not args.no_plain:
+            out["plain_single_chain"] = plain_single_chain(F)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -357,6 +413,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
+    ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

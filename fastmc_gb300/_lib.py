@@ -64,7 +64,7 @@ class ChainStats(C.Structure):
                 ("avg_n", C.c_double), ("avg_e", C.c_double), ("avg_en", C.c_double),
                 ("avg_n2", C.c_double), ("avg_e2", C.c_double), ("avg_nf", C.c_double),
                 ("qst", C.c_double), ("cv", C.c_double), ("prodcount", C.c_int64),
-                ("windows", C.c_int64)]
+                ("windows", C.c_int64), ("device_ns", C.c_int64)]
 
 
 class MoveLog(C.Structure):

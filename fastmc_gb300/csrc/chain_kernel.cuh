@@ -37,6 +37,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                  int csize) {
   extern __shared__ __align__(16) unsigned char dyn[];
   BlockShared<F32> &B = *reinterpret_cast<BlockShared<F32> *>(dyn);
+  const unsigned long long t_start = global_ns();
   const int rank = csize > 1 ? (int)cluster_rank() : 0;
   const int chain = chain_ids ? chain_ids[blockIdx.x / csize] : (int)blockIdx.x / csize;
   block_copy(&B.H, hdrs + chain);
@@ -61,6 +62,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (B.mc.kind != 0) full = evaluate_any<F32, GN>(B, CA, chain, st);
       if (threadIdx.x == 0) {
         decide(B, true);
+        if (B.mc.accepted && B.flags[4]) other_mol_delE<F32, GN>(B);
         if (full) B.H.evals += B.mc.npos;
         else if (B.mc.overlap) B.H.overlap_exits++;
         if (logcap > 0 && B.H.log_n < logcap && rank == 0) {
@@ -138,7 +140,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int q = 1; q < csize; ++q) B.flags[0] |= dsmem_load_s32(dsmem_addr(&B.flags[0], q));
     cluster_barrier();  // the peers stay resident until rank 0 has read them
   }
-  if (threadIdx.x == 0) B.H.status |= B.flags[0];
+  if (threadIdx.x == 0) {
+    B.H.status |= B.flags[0];
+    B.H.dev_ns += (long long)(global_ns() - t_start);
+  }
   __syncthreads();
   if (rank == 0) block_copy(hdrs + chain, &B.H);
 }

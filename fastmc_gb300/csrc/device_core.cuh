@@ -172,6 +172,7 @@ struct ChainHdr {
   int window_left;         // production moves until the next window ends
   int pad_w;
   long long pend;          // production moves not yet added to chainstats (FP32 path)
+  long long dev_ns;        // device time spent in this chain's launches (ns)
   double chainstats[kMaxG][6];
   double wsum;
   double wacc[kMaxG][8];
@@ -286,6 +287,12 @@ __device__ __forceinline__ void fence_proxy_async() {
 // them go through distributed shared memory: release/acquire flag stores
 // into the peers' shared memory and bounded polling of one's own flags.
 constexpr int kMaxCluster = 8;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ unsigned cluster_rank() {
   unsigned r;

@@ -229,7 +229,8 @@ __device__ __forceinline__ int image_of(int ic, int n) {
 
 // ---------------------------------------------------- framework neighbours
 // List of framework atom segments (runs of cells along z in one column and
-// one periodic image) covering the sphere of radius R around c.  Slots with
+// one periodic image) covering the sphere of radius R around c.  On a
+// cluster each CTA takes every csize-th column.  Slots with
 // zero atoms are allowed; seg_pref is the prefix over slots.  The geometry
 // is conservative (FP32 with a margin): it only selects candidates.
 template <bool F32>
@@ -277,6 +278,7 @@ __device__ void build_segments(const SysDev &S, EvalSmem<F32> &sm, const float *
       sm.seg_pref[base + r] = 0;  // count for now
     }
     if (d2 > R2) continue;
+    if (col % sm.csize != sm.rank) continue;  // another CTA of the cluster takes this column
     float hz = sqrtf(R2 - d2);
     int iz0 = (int)floorf((c[2] - hz) * rc[2]), iz1 = (int)floorf((c[2] + hz) * rc[2]);
     int imx = image_of(ix, S.nc[0]), imy = image_of(iy, S.nc[1]);
@@ -342,8 +344,7 @@ __device__ __forceinline__ void scan_framework(const SysDev &S, EvalSmem<F32> &s
                                                int &sf, int &st) {
   const int ns = NS > 0 ? NS : ns_rt;
   int nslot = sm.nslots;
-  int t0, total;  // this CTA's share of the candidate atoms
-  share_of(sm.seg_pref[nslot], sm.rank, sm.csize, t0, total);
+  const int t0 = 0, total = sm.seg_pref[nslot];  // this CTA's columns only
   if constexpr (!F32) {
     double e2 = 0.0, vdw = 0.0;
     for (int t = t0 + threadIdx.x; t < total; t += kThreads) {

@@ -844,6 +844,7 @@ void fill_stats(const Chains &C, fmc_chain_stats *out) {
     }
     o.prodcount = h.prodcount;
     o.windows = h.windows;
+    o.device_ns = h.dev_ns;
   }
 }
 

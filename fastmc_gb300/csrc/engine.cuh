@@ -42,7 +42,7 @@ struct BlockShared {
   double geo[12];    // a, b, c, q1..q4, rotation angle, com/frac scratch
   float geof[4];     // FP32 path: shift a, b, c and the rotation angle
   double vtmp[3];
-  int flags[4];
+  int flags[8];     // 0 status, 1 slot, 2 "translate" (q = 0), 3 FP32 geometry, 4 delE deferred
   // cluster exchange (chains on more than one CTA): per-CTA partial totals,
   // double-buffered, and the flags the peers raise in this CTA's memory
   double xv[2][40];
@@ -71,9 +71,14 @@ __device__ void cluster_exchange(BlockShared<F32> &B, int nv, int &st) {
   __syncthreads();
   if (threadIdx.x < nv) {
     const int i = threadIdx.x;
+    double v[kMaxCluster];
+#pragma unroll
+    for (int q = 0; q < kMaxCluster; ++q)  // all loads in flight, then the sum in rank order
+      v[q] = q >= C ? 0.0 : (q == r ? B.xv[par][i] : dsmem_load_f64(dsmem_addr(&B.xv[par][i], q)));
     double sum = 0.0;
-    for (int q = 0; q < C; ++q)
-      sum += q == r ? B.xv[par][i] : dsmem_load_f64(dsmem_addr(&B.xv[par][i], q));
+#pragma unroll
+    for (int q = 0; q < kMaxCluster; ++q)
+      if (q < C) sum += v[q];
     B.ev.out[i] = sum;
   }
   __syncthreads();
@@ -528,7 +533,10 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
         }
       }
     }
-    if (threadIdx.x == 0) B.flags[3] = (F32 && mode != kPropExternal) ? 1 : 0;
+    if (threadIdx.x == 0) {
+      B.flags[3] = (F32 && mode != kPropExternal) ? 1 : 0;
+      B.flags[4] = mode == kPropMC ? 1 : 0;  // delE of other molecule types only if accepted
+    }
     __syncwarp();
     if (F32 && mode != kPropExternal) geometry_f32(B, CA, chain);
     else geometry_warp(B, CA, chain, mode);
@@ -941,6 +949,57 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
   }
 }
 
+// delE(m) against every molecule type m other than the moving one, from
+// the block totals in ev.out (thread 0).  In the main loop it is needed only
+// to update energy(m) of an accepted move, so it runs after the decision.
+template <bool F32, int GN>
+__device__ void other_mol_delE(BlockShared<F32> &B) {
+  const SysDev &S = B.S;
+  MoveCtx &mc = B.mc;
+  const GuestType &G = S.g[mc.g];
+  constexpr int nper = PosAcc<F32, GN>::kN;
+  const double *R = B.ev.out;
+  const int npos = mc.npos, NG = S.ntpguest, mol = G.mol;
+  const double eu = S.rengunit;
+  auto pair_terms = [&](int p, int m, double delrc_m) {
+    const double *r = R + p * nper;
+    bool exist = (npos == 2) ? (p == 1) : (mc.kind == 2);
+    double qfm = G.qfm * B.H.chgsum_mol[m];
+    if (exist) qfm = -qfm;
+    double e1 = 0.0, e2m = 0.0, vdm = 0.0;
+    if (m == S.fw_mol) {
+      e1 = S.krecip * r[3] + qfm;
+      e2m = r[0];
+      vdm = r[1];
+    } else {
+      e1 = qfm;
+      for (int g2 = 0; g2 < NG; ++g2)
+        if (S.g[g2].mol == m) {
+          e1 += S.krecip * r[4 + 2 * GN + g2];
+          e2m += r[4 + g2];
+          vdm += r[4 + GN + g2];
+        }
+    }
+    return e1 + e2m + vdm + delrc_m;
+  };
+  if (mc.kind == 1 || mc.kind == 2) {
+    const bool del = mc.kind == 2;
+    for (int m = 1; m <= S.maxmls; ++m) {
+      if (m == mol) continue;
+      double dm = 0.0;  // delrc_mol(loc2(mol,m)), vdw_terms.f:743-761
+      if (m == S.fw_mol) dm = G.lrcA - G.lrcC;
+      else
+        for (int g2 = 0; g2 < NG; ++g2)
+          if (S.g[g2].mol == m) dm = double(B.H.nummols[g2]) * G.lrcB[g2];
+      const double t = pair_terms(0, m, dm) * eu;
+      mc.delE[m] = del ? -t : t;
+    }
+  } else {
+    for (int m = 1; m <= S.maxmls; ++m)
+      if (m != mol) mc.delE[m] = (pair_terms(0, m, 0.0) - pair_terms(1, m, 0.0)) * eu;
+  }
+}
+
 // --------------------------------------------------------------- evaluate
 // Evaluate the proposed move; fills mc.estep, mc.delE and the flags.
 // Returns 1 if a full evaluation ran (no overlap exit).
@@ -1034,28 +1093,6 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
         vd[p] += r[4 + GN + g2];
       }
     }
-    // per-molecule-type terms against type m != mol (delE(m))
-    auto pair_terms = [&](int p, int m, double delrc_m) {
-      const double *r = R + p * nper;
-      bool exist = (npos == 2) ? (p == 1) : (mc.kind == 2);
-      double qfm = G.qfm * B.H.chgsum_mol[m];
-      if (exist) qfm = -qfm;
-      double e1 = 0.0, e2m = 0.0, vdm = 0.0;
-      if (m == S.fw_mol) {
-        e1 = S.krecip * r[3] + qfm;
-        e2m = r[0];
-        vdm = r[1];
-      } else {
-        e1 = qfm;
-        for (int g2 = 0; g2 < NG; ++g2)
-          if (S.g[g2].mol == m) {
-            e1 += S.krecip * r[4 + 2 * GN + g2];
-            e2m += r[4 + g2];
-            vdm += r[4 + GN + g2];
-          }
-      }
-      return e1 + e2m + vdm + delrc_m;
-    };
     for (int m = 0; m <= kMaxM; ++m) mc.delE[m] = 0.0;
     if (mc.kind == 1 || mc.kind == 2) {
       bool del = mc.kind == 2;
@@ -1063,26 +1100,15 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       mc.delrc = delrc;
       if (!del) mc.estep = (ewld1[0] + e2[0] - e3 + vd[0] + delrc) * eu;
       else mc.estep = (-ewld1[0] + e2[0] + vd[0] - e3) * eu - delrc * eu;
-      for (int m = 1; m <= S.maxmls; ++m) {
-        if (m == mol) continue;
-        double dm = 0.0;  // delrc_mol(loc2(mol,m)), vdw_terms.f:743-761
-        if (m == S.fw_mol) dm = G.lrcA - G.lrcC;
-        else
-          for (int g2 = 0; g2 < NG; ++g2)
-            if (S.g[g2].mol == m) dm = double(B.H.nummols[g2]) * G.lrcB[g2];
-        double t = pair_terms(0, m, dm) * eu;
-        mc.delE[m] = del ? -t : t;
-      }
       mc.delE[mol] = del ? -mc.estep : mc.estep;
     } else {
       double enginit = (-ewld1[1] + e2[1] + vd[1] - e3) * eu;
       double enew = (ewld1[0] + e2[0] + vd[0] - e3) * eu;
       mc.estep = enew - enginit;
       mc.delrc = 0.0;
-      for (int m = 1; m <= S.maxmls; ++m)
-        if (m != mol) mc.delE[m] = (pair_terms(0, m, 0.0) - pair_terms(1, m, 0.0)) * eu;
       mc.delE[mol] = mc.estep;
     }
+    if (!B.flags[4]) other_mol_delE<F32, GN>(B);
     mc.parts[0] = ewld1[0];
     mc.parts[1] = e2[0];
     mc.parts[2] = vd[0];

@@ -206,6 +206,7 @@ typedef struct {
   double avg_n, avg_e, avg_en, avg_n2, avg_e2, avg_nf, qst, cv;
   int64_t prodcount;
   int64_t windows;
+  int64_t device_ns;       /* device time of this chain's launches so far */
 } fmc_chain_stats;
 
 /* One entry of the optional per-move log (parity tests). */
