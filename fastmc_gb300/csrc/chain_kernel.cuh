@@ -52,6 +52,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     B.cflag = 0u;
   }
   if (threadIdx.x < kMaxCluster) B.xflag[threadIdx.x] = 0u;
+  __syncthreads();  // the system record and header are complete
+  if (F32 && CA.resident) {  // guests into shared memory, molecule order
+    const int n = B.H.nummols[0], ns = B.S.g[0].ns;
+    const int *ord = CA.ord + (size_t)chain * kMaxG * CA.cap;
+    const float4 *gh = CA.ghi + (size_t)chain * kMaxG * CA.cap * kMaxS;
+    const float4 *gl = CA.glo + (size_t)chain * kMaxG * CA.cap * kMaxS;
+    for (int idx = threadIdx.x; idx < n * ns; idx += kThreads) {
+      const int i = idx / ns, sidx = idx - i * ns;
+      const size_t o = (size_t)ord[i] * kMaxS + sidx;
+      B.grh[idx] = gh[o];
+      B.grl[idx] = gl[o];
+    }
+  }
   __syncthreads();
   if (csize > 1) cluster_barrier();  // every CTA's flags are cleared before anyone posts
   int st = 0;
@@ -139,6 +152,27 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (rank == 0 && threadIdx.x == 0)
       for (int q = 1; q < csize; ++q) B.flags[0] |= dsmem_load_s32(dsmem_addr(&B.flags[0], q));
     cluster_barrier();  // the peers stay resident until rank 0 has read them
+  }
+  if (F32 && CA.resident && rank == 0) {
+    // write the guests back in molecule order: molecule i in slot i
+    const int n = B.H.nummols[0], ns = B.S.g[0].ns;
+    const size_t base = (size_t)chain * kMaxG * CA.cap * kMaxS;
+    int *ord = CA.ord + (size_t)chain * kMaxG * CA.cap;
+    for (int idx = threadIdx.x; idx < n * ns; idx += kThreads) {
+      const int i = idx / ns, sidx = idx - i * ns;
+      const size_t o = base + (size_t)i * kMaxS + sidx;
+      const float4 h = B.grh[idx], l = B.grl[idx];
+      CA.ghi[o] = h;
+      CA.glo[o] = l;
+      CA.gpos[o * 3] = (double)h.x + (double)l.x;
+      CA.gpos[o * 3 + 1] = (double)h.y + (double)l.y;
+      CA.gpos[o * 3 + 2] = (double)h.z + (double)l.z;
+    }
+    for (int i = threadIdx.x; i < n; i += kThreads) ord[i] = i;
+    if (threadIdx.x == 0) {
+      B.H.nslots[0] = n;
+      B.H.nfree[0] = 0;
+    }
   }
   if (threadIdx.x == 0) {
     B.H.status |= B.flags[0];

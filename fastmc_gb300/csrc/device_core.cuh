@@ -67,6 +67,8 @@ struct GuestType {
   double ewald3en;
   double chgea[kMaxS];     // q / epsq * r4pie0 per site (ewald2's charge factor)
   float tmplf[kMaxS][3];   // centred template in FP32 (FP32 trial geometry)
+  int prow[kMaxS][kMaxT + 1];      // table row of site s with atom type t (-1: none)
+  float psig2[kMaxS][kMaxT + 1];   // (surftol + sigma)^2 of site s with atom type t
   float wf[kMaxS];         // mass fraction of each site (centre of mass)
   float chgeaf[kMaxS];     // the same as an FP32 hi/lo pair
   float chgeaf_lo[kMaxS];
@@ -199,7 +201,11 @@ struct ChainArrays {
   float2 *sold32;
   int cap;          // molecules per guest type
   int nkmax;
+  int resident;     // FP32 batches of one guest type: guests held in shared memory
 };
+
+// Guest sites a CTA can hold in shared memory (molecule order, hi/lo).
+constexpr int kGuestSmem = 3072;
 
 // Description of one trial move (shared memory; copied to global between
 // the evaluate and commit kernels of the per-move ABI).

@@ -88,6 +88,8 @@ struct SiteInfo {
   float chgeaf_lo;
   float qf;
   int type;
+  const int *prow;     // table row per partner atom type (the guest type's record)
+  const float *psig2;  // surface distance squared per partner atom type
 };
 
 // One site-atom pair: erfc and van der Waals terms when r < rc, overlap and
@@ -115,9 +117,8 @@ __device__ __forceinline__ void pair_term32(const SysDev &S, const SiteInfo &si,
                                             int tb, int frozen_b, float r2, AccT<true> &e2,
                                             float &vdw, int &ov, int &sf, int &st,
                                             bool skip_vdw = false) {
-  int pi = si.type * (S.ntpatm + 1) + tb;
   if (r2 < S.overlap_sqf) ov = 1;
-  if (frozen_b && r2 < __ldg(S.sig2f + pi)) sf = 1;
+  if (frozen_b && r2 < si.psig2[tb]) sf = 1;
   if (r2 < S.rc2f) {
     float r = sqrtf(r2);
     const float ch = si.chgeaf * qh;
@@ -137,7 +138,7 @@ __device__ __forceinline__ void pair_term32(const SysDev &S, const SiteInfo &si,
         e2.add_df(DF{ph, pl});
       }
     }
-    int k = __ldg(S.pairtab + pi);
+    const int k = si.prow[tb];
     if (k >= 0 && !skip_vdw) vdw += interp32(S.vvvq + (size_t)k * S.tabstride, r, S.rdlrpotf, S.mxegrd, st);
   }
 }
@@ -149,7 +150,7 @@ __device__ __forceinline__ void pair_term32(const SysDev &S, const SiteInfo &si,
 constexpr float kNear2 = 9.0f;
 
 __device__ __forceinline__ bool vdw_is_near(const SysDev &S, const SiteInfo &si, int tb, float r2) {
-  return r2 < kNear2 && __ldg(S.pairtab + si.type * (S.ntpatm + 1) + tb) >= 0;
+  return r2 < kNear2 && si.prow[tb] >= 0;
 }
 
 // Lennard-Jones term of one close pair from the difference vector given as
@@ -184,7 +185,7 @@ __device__ __forceinline__ DF vdw_near_df(const SysDev &S, const SiteInfo &si, i
     st |= kStTableLow;
     return out;
   }
-  const int k = __ldg(S.pairtab + si.type * (S.ntpatm + 1) + tb);
+  const int k = si.prow[tb];
   const float4 c = __ldg(S.vvvq + (size_t)k * S.tabstride + l);
   const float q = fmaf(p, fmaf(p, c.z, c.y), c.w);  // A_lo + p(B + pC)
   two_sum_f(c.x, q, out.hi, out.lo);

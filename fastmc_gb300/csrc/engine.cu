@@ -453,6 +453,17 @@ void build_device_system(const System &s, DevSystem &D) {
       rmax = std::max(rmax, std::sqrt(dx * dx + dy * dy + dz * dz));
     }
     G.rmax = rmax;
+    for (int i = 0; i < kMaxS; ++i)
+      for (int t = 0; t <= kMaxT; ++t) {
+        G.prow[i][t] = -1;
+        G.psig2[i][t] = 0.f;
+      }
+    for (int i = 0; i < m.natoms; ++i)
+      for (int t = 0; t <= s.ntpatm && t <= kMaxT; ++t) {
+        const int pi = m.ltp[i] * (s.ntpatm + 1) + t;
+        G.prow[i][t] = ptab[pi];
+        G.psig2[i][t] = (float)sig2[pi];
+      }
     {
       double mt = 0.0;
       for (int i = 0; i < m.natoms; ++i) mt += m.wght[i];
@@ -806,9 +817,17 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   FMC_CUDA(cudaEventCreate(&C.ev0));
   FMC_CUDA(cudaEventCreate(&C.ev1));
   C.smem = precision == FMC_PREC_FP32 ? sizeof(BlockShared<true>) : sizeof(BlockShared<false>);
-  int ngmax = 1;
-  for (int i = 0; i < nsys; ++i) ngmax = std::max(ngmax, systems[i]->ntpguest);
+  int ngmax = 1, nsmax = 1;
+  for (int i = 0; i < nsys; ++i) {
+    ngmax = std::max(ngmax, systems[i]->ntpguest);
+    for (int g = 1; g <= systems[i]->ntpguest; ++g)
+      nsmax = std::max(nsmax, systems[i]->mol[systems[i]->locguest[g]].natoms);
+  }
   C.gn = (precision == FMC_PREC_FP32 && ngmax == 1) ? 1 : kMaxG;
+  // guests resident in shared memory during a launch (FP32, one guest type,
+  // capacity x sites within the shared array); the per-move ABI keeps them
+  // in global memory (its launches are single moves)
+  CA.resident = (precision == FMC_PREC_FP32 && ngmax == 1 && cap * nsmax <= kGuestSmem) ? 1 : 0;
   cudaError_t e;
   if (precision == FMC_PREC_FP32 && C.gn == 1) e = set_chain_smem<true, 1>(C.smem);
   else if (precision == FMC_PREC_FP32) e = set_chain_smem<true, kMaxG>(C.smem);
@@ -1105,6 +1124,7 @@ int fmc_plain_create(const fmc_system *sys, int precision, int guest_capacity, f
     const System *sp = &sys->s;
     fmc_chain_spec spec{0, -1.0, 1, 0};
     init_chains(h->C, &sp, 1, &spec, 1, precision, guest_capacity);
+    h->C.CA.resident = 0;  // one move per launch: guests stay in global memory
     *out = h.release();
     return FMC_OK;
   });
@@ -1615,38 +1635,49 @@ int fmc_batch_autotune(fmc_batch *b, int nmoves, int *csize_out, int nsys) {
     save_state(C, snap);
     const long long ev0 = C.last_evals, mv0 = C.last_moves;
     const double ms0 = C.last_ms;
-    // time of one cycle from the saved state (best of two)
-    auto trial = [&](const std::vector<int> &cs) {
+    C.pull_headers();
+    const int ns = (int)C.sys.size();
+    std::vector<long long> t0(C.nchains);
+    for (int c = 0; c < C.nchains; ++c) t0[c] = C.host_hdr[c].dev_ns;
+    // cycle time from the saved state (best of two) and, per system, the
+    // device time of its slowest chain in that run
+    auto trial = [&](const std::vector<int> &cs, std::vector<double> &sysmax) {
       C.set_clusters(cs);
       double best = 1e300;
       for (int r = 0; r < 2; ++r) {
         restore_state(C, snap);
         run_cycle(C, nmoves);
-        best = std::min(best, C.last_ms);
+        if (C.last_ms < best) {
+          best = C.last_ms;
+          sysmax.assign(ns, 0.0);
+          for (int c = 0; c < C.nchains; ++c) {
+            const ChainHdr &h = C.host_hdr[c];
+            sysmax[h.system] = std::max(sysmax[h.system], 1e-6 * double(h.dev_ns - t0[c]));
+          }
+        }
       }
       return best;
     };
-    const int ns = (int)C.sys.size();
     std::vector<int> cur(ns, 1);
-    double tcur = trial(cur);
-    // greedy: double the cluster of one system at a time while it helps
+    std::vector<double> smax;
+    double tcur = trial(cur, smax);
+    // double the cluster of every system whose slowest chain is within 20%
+    // of the cycle, while the cycle gets more than 3% faster
     for (;;) {
-      std::vector<int> best_cs;
-      double tbest = tcur;
-      for (int i = 0; i < ns; ++i) {
-        if (cur[i] * 2 > kMaxCluster) continue;
-        std::vector<int> cs = cur;
-        cs[i] *= 2;
-        if (C.occupancy(cs[i]) < 1) continue;
-        double t = trial(cs);
-        if (t < tbest * 0.97) {
-          tbest = t;
-          best_cs = cs;
+      std::vector<int> cand = cur;
+      bool changed = false;
+      for (int i = 0; i < ns; ++i)
+        if (smax[i] >= 0.8 * tcur && cur[i] * 2 <= kMaxCluster && C.occupancy(cur[i] * 2) >= 1) {
+          cand[i] = cur[i] * 2;
+          changed = true;
         }
-      }
-      if (best_cs.empty()) break;
-      cur = best_cs;
-      tcur = tbest;
+      if (!changed) break;
+      std::vector<double> s2;
+      const double t = trial(cand, s2);
+      if (t >= 0.97 * tcur) break;
+      cur = cand;
+      tcur = t;
+      smax = s2;
     }
     C.set_clusters(cur);
     restore_state(C, snap);

@@ -33,6 +33,10 @@ struct LogRec {  // mirrors fmc_move_log
 
 template <bool F32>
 struct BlockShared {
+  // FP32 batches of one guest type: every guest site in molecule order as
+  // hi/lo pairs (x, y, z, q), for the whole launch (ChainArrays::resident)
+  float4 grh[F32 ? kGuestSmem : 1];
+  float4 grl[F32 ? kGuestSmem : 1];
   SysDev S;
   ChainHdr H;
   MoveCtx mc;
@@ -414,9 +418,15 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
     two_sum_f(ch, v, ph, e);
     pl = cl + e;
   } else {
-    const size_t b = gslot_base(CA, chain, mc.g, mc.slot) + s;
-    const float oh = mine ? reinterpret_cast<const float *>(CA.ghi + b)[d] : 0.f;
-    const float ol = mine ? reinterpret_cast<const float *>(CA.glo + b)[d] : 0.f;
+    float oh = 0.f, ol = 0.f;
+    if (mine && CA.resident) {
+      oh = reinterpret_cast<const float *>(&B.grh[mc.slot * ns + s])[d];
+      ol = reinterpret_cast<const float *>(&B.grl[mc.slot * ns + s])[d];
+    } else if (mine) {
+      const size_t b = gslot_base(CA, chain, mc.g, mc.slot) + s;
+      oh = reinterpret_cast<const float *>(CA.ghi + b)[d];
+      ol = reinterpret_cast<const float *>(CA.glo + b)[d];
+    }
     if (mc.kind == 2) {
       ph = oh;
       pl = ol;
@@ -482,6 +492,8 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
     si.chgeaf_lo = G.chgeaf_lo[lane];
     si.qf = (float)G.q[lane];
     si.type = G.type[lane];
+    si.prow = G.prow[lane];
+    si.psig2 = G.psig2[lane];
   }
   __syncwarp();
   if (lane < mc.npos) position_bounds(B, lane);
@@ -529,7 +541,8 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
           B.H.status |= kStBadChoice;
           mc.kind = 0;
         } else {
-          mc.slot = CA.ord[((size_t)chain * kMaxG + mc.g) * CA.cap + (mc.choice - 1)];
+          mc.slot = (F32 && CA.resident) ? mc.choice - 1
+                                         : CA.ord[((size_t)chain * kMaxG + mc.g) * CA.cap + (mc.choice - 1)];
         }
       }
     }
@@ -659,6 +672,31 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
   }
   // guests
   const GuestType &G = S.g[mc.g];
+  if (F32 && CA.resident) {  // one guest type, resident in shared memory
+    const GuestType &G2 = S.g[0];
+    const int n2 = B.H.nummols[0], ns2 = G2.ns;
+    const float pre = sqrtf(S.overlap_sqf) + 2.0f * (float)G.rmax + 2.0f * (float)G2.rmax + 0.01f;
+    const float pre2 = pre * pre;
+    for (int i = threadIdx.x; i < n2 && !hit; i += kThreads) {
+      if (i == mc.slot) continue;
+      const float4 q0 = B.grh[i * ns2];
+      float dx = ev.phi[0][0][0] - q0.x, dy = ev.phi[0][0][1] - q0.y, dz = ev.phi[0][0][2] - q0.z;
+      dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
+      dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
+      dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+      if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+      for (int b = 0; b < ns2; ++b) {
+        const float4 qh = B.grh[i * ns2 + b], ql = B.grl[i * ns2 + b];
+        for (int s = 0; s < ns; ++s) {
+          float ex = mi_diff32(ev.phi[0][s][0], ev.plo[0][s][0], qh.x, ql.x, S.boxh[0], S.boxl[0], S.rboxf[0]);
+          float ey = mi_diff32(ev.phi[0][s][1], ev.plo[0][s][1], qh.y, ql.y, S.boxh[1], S.boxl[1], S.rboxf[1]);
+          float ez = mi_diff32(ev.phi[0][s][2], ev.plo[0][s][2], qh.z, ql.z, S.boxh[2], S.boxl[2], S.rboxf[2]);
+          if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < S.overlap_sqf) hit = 1;
+        }
+      }
+    }
+    return block_or(hit, B.ev.red_i);
+  }
   for (int g2 = 0; g2 < S.ntpguest && !hit; ++g2) {
     const GuestType &G2 = S.g[g2];
     int n2 = B.H.nummols[g2];
@@ -949,6 +987,64 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
   }
 }
 
+// Guest-guest terms with the guests resident in shared memory (one guest
+// type, molecule order): the terms of scan_guests, without the slot
+// indirection and global loads.
+template <bool F32, int GN, int NS>
+__device__ __forceinline__ void scan_guests_resident(BlockShared<F32> &B, int pos, int ns_rt,
+                                                     int self_i, float rmax_self,
+                                                     PosAcc<F32, GN> &acc, int &ov, int &sf,
+                                                     int &st) {
+  const SysDev &S = B.S;
+  const EvalSmem<F32> &sm = B.ev;
+  const SiteInfo *si = B.si;
+  const int ns = NS > 0 ? NS : ns_rt;
+  const GuestType &G2 = S.g[0];
+  const int n2 = B.H.nummols[0], ns2 = G2.ns;
+  const float pre = (float)S.rcut + 2.0f * rmax_self + 2.0f * (float)G2.rmax + 0.01f;
+  const float pre2 = pre * pre;
+  int i0, i1;
+  share_of(n2, sm.rank, sm.csize, i0, i1);
+  for (int i = i0 + threadIdx.x; i < i1; i += kThreads) {
+    if (i == self_i) continue;
+    const float4 q0 = B.grh[i * ns2];
+    float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y, dz = sm.phi[pos][0][2] - q0.z;
+    dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
+    dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
+    dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+    float vdw = 0.f;
+#pragma unroll
+    for (int b = 0; b < (NS > 0 ? NS : ns2); ++b) {  // the same guest type: ns2 == ns
+      const float4 qh = B.grh[i * ns2 + b], ql = B.grl[i * ns2 + b];
+      const int tb = G2.type[b];
+#pragma unroll
+      for (int k = 0; k < (NS > 0 ? NS : ns); ++k) {
+        float ex = mi_diff32(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
+                             S.boxl[0], S.rboxf[0]);
+        float ey = mi_diff32(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
+                             S.boxl[1], S.rboxf[1]);
+        float ez = mi_diff32(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2],
+                             S.boxl[2], S.rboxf[2]);
+        float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+        const bool near = vdw_is_near(S, si[k], tb, r2);
+        pair_term32(S, si[k], qh.w, ql.w, tb, G2.frz[b], r2, acc.e2g[0], vdw, ov, sf, st, near);
+        if (near) {
+          float dh[3], dl[3];
+          mi_diff_df(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0], S.boxl[0],
+                     S.rboxf[0], dh[0], dl[0]);
+          mi_diff_df(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1], S.boxl[1],
+                     S.rboxf[1], dh[1], dl[1]);
+          mi_diff_df(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2], S.boxl[2],
+                     S.rboxf[2], dh[2], dl[2]);
+          acc.vdwg[0].add_df(vdw_near_df(S, si[k], tb, dh, dl, st));
+        }
+      }
+    }
+    acc.vdwg[0].add(vdw);
+  }
+}
+
 // delE(m) against every molecule type m other than the moving one, from
 // the block totals in ev.out (thread 0).  In the main loop it is needed only
 // to update energy(m) of an accepted move, so it runs after the decision.
@@ -1018,6 +1114,8 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       B.si[s].chgeaf_lo = G.chgeaf_lo[s];
       B.si[s].qf = (float)G.q[s];
       B.si[s].type = G.type[s];
+      B.si[s].prow = G.prow[s];
+      B.si[s].psig2 = G.psig2[s];
     }
     if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * kMaxS * 3) {
       int t = threadIdx.x - 32;
@@ -1048,8 +1146,16 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
   auto scan_position = [&](int p, PosAcc<F32, GN> &A, int &sfp) {
     build_segments<F32>(S, B.ev, B.ev.cen[p], (float)S.rcut + B.ev.rmx[p] + 1e-3f, st);
     scan_framework<F32, NS>(S, B.ev, p, ns, B.si, A, ovd, sfp, st);
-    scan_guests<F32, GN, NS>(S, B.H, CA, chain, B.ev, p, ns, mc.g, mc.slot, B.ev.rmx[p], B.si, A, ovd,
-                         sfp, st);
+    bool done = false;
+    if constexpr (F32) {
+      if (CA.resident) {
+        scan_guests_resident<F32, GN, NS>(B, p, ns, mc.slot, B.ev.rmx[p], A, ovd, sfp, st);
+        done = true;
+      }
+    }
+    if (!done)
+      scan_guests<F32, GN, NS>(S, B.H, CA, chain, B.ev, p, ns, mc.g, mc.slot, B.ev.rmx[p], B.si, A,
+                               ovd, sfp, st);
     __syncthreads();
   };
   scan_position(0, acc0, sf0);
@@ -1271,7 +1377,48 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
   // molecule order and coordinates
   int *ord = CA.ord + ((size_t)chain * kMaxG + g) * CA.cap;
   int *freel = CA.freel + ((size_t)chain * kMaxG + g) * CA.cap;
-  if (threadIdx.x == 0) {
+  const bool res = F32 && CA.resident;
+  if (res) {
+    // shared-memory copy, molecule order: insertion appends, deletion shifts
+    // the later molecules down (mc_moves.f:574-590), displacement overwrites
+    const int n = H.nummols[g], ns = G.ns;
+    if (threadIdx.x == 0) {
+      int slot = mc.slot;
+      if (mc.kind == 1) {
+        slot = n < CA.cap ? n : -1;
+        if (slot < 0) st |= kStCapacity;
+      }
+      B.flags[1] = slot;
+    }
+    __syncthreads();
+    if (mc.kind == 2) {
+      const int from = (mc.choice - 1) * ns, cnt = (n - mc.choice) * ns;
+      for (int base = 0; base < cnt; base += kThreads) {
+        const int j = base + threadIdx.x;
+        float4 vh = make_float4(0.f, 0.f, 0.f, 0.f), vl = vh;
+        if (j < cnt) {
+          vh = B.grh[from + j + ns];
+          vl = B.grl[from + j + ns];
+        }
+        __syncthreads();
+        if (j < cnt) {
+          B.grh[from + j] = vh;
+          B.grl[from + j] = vl;
+        }
+        __syncthreads();
+      }
+    } else if (B.flags[1] >= 0 && threadIdx.x < 3 * ns) {
+      const int s = threadIdx.x / 3, d = threadIdx.x % 3, i = B.flags[1];
+      reinterpret_cast<float *>(&B.grh[i * ns + s])[d] = B.ev.phi[0][s][d];
+      reinterpret_cast<float *>(&B.grl[i * ns + s])[d] = B.ev.plo[0][s][d];
+      if (d == 0) {
+        const float qh = (float)G.q[s];
+        B.grh[i * ns + s].w = qh;
+        B.grl[i * ns + s].w = (float)(G.q[s] - (double)qh);
+      }
+    }
+  }
+  if (!res && threadIdx.x == 0) {
     int slot = mc.slot;
     if (mc.kind == 1) {
       if (H.nfree[g] > 0) slot = freel[--H.nfree[g]];
@@ -1286,7 +1433,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
   }
   __syncthreads();
   const int slot = B.flags[1];
-  if (mc.kind == 2 && B.ev.rank == 0) {
+  if (mc.kind == 2 && B.ev.rank == 0 && !res) {
     // remove entry choice-1 from the order list (mc_moves.f:574-590)
     int n = H.nummols[g];
     int c0 = mc.choice - 1;
@@ -1305,7 +1452,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     }
     __syncthreads();
   }
-  if (slot >= 0 && (mc.kind == 1 || mc.kind >= 3) && threadIdx.x < 3 * G.ns && B.ev.rank == 0) {
+  if (slot >= 0 && (mc.kind == 1 || mc.kind >= 3) && threadIdx.x < 3 * G.ns && B.ev.rank == 0 && !res) {
     int s = threadIdx.x / 3, d = threadIdx.x % 3;
     size_t b = gslot_base(CA, chain, g, slot) + s;
     if constexpr (F32) {  // the evaluated position is the hi/lo pair
@@ -1345,7 +1492,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
         }
       }
       H.nummols[g] += sg;
-      if (mc.kind == 2) {
+      if (mc.kind == 2 && !res) {
         if (B.ev.rank == 0) freel[H.nfree[g]] = slot;
         H.nfree[g]++;
       }
@@ -1360,7 +1507,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     }
   }
   __syncthreads();
-  cluster_commit_sync(B, st);
+  if (!res) cluster_commit_sync(B, st);  // resident guests: every CTA updated its own copy
 }
 
 __device__ inline double calc_qst(double E, double N, double N2, double EN, double T) {

@@ -262,10 +262,11 @@ int fmc_batch_set_cluster(fmc_batch *b, const int *csize, int nsys);
 int fmc_batch_get_cluster(const fmc_batch *b, int *csize, int nsys);
 
 /* Autotuner: picks the cluster size of every system by timing trial cycles
- * of `nmoves` moves from a copy of the chains' state (greedy doubling of
- * one system's cluster at a time while the cycle gets >3% faster), sets
- * it, and restores the chains' state, so the chains continue exactly as if
- * it had not run.  csize_out (nullable) receives the choice. */
+ * of `nmoves` moves from a copy of the chains' state: starting from one CTA
+ * per chain, it doubles the cluster of every system whose slowest chain is
+ * within 20% of the cycle time, while the cycle gets more than 3% faster.
+ * It sets the choice and restores the chains' state, so the chains continue
+ * exactly as if it had not run.  csize_out (nullable) receives the choice. */
 int fmc_batch_autotune(fmc_batch *b, int nmoves, int *csize_out, int nsys);
 
 /* Timing of the last fmc_batch_run: device milliseconds of the persistent

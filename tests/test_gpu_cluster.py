@@ -97,3 +97,30 @@ def test_autotune_leaves_chain_state(fmc_lib, inputs_dir):
         for i, (u, v) in enumerate(zip(la, lb)):
             assert (u.move, u.choice, u.overlap, u.accepted, u.estep) == \
                    (v.move, v.choice, v.overlap, v.accepted, v.estep), (c, i)
+
+
+def test_resident_guests_match_global(fmc_lib, inputs_dir):
+    """FP32 batches keep the guests in shared memory when capacity x sites
+    fits (3072 sites); a larger capacity keeps them in global memory.  Both
+    visit the molecules in the same order, so the moves and energies are
+    identical, and so are the coordinates written back."""
+    d = inputs_dir(syn.small_test_spec(seed=5, kmax=8, ntile=3, pressure_bar=5.0, create=40), "cl_b")
+    sysm = fmc_lib.System.load(d)
+    specs = [{"seed": 31}, {"seed": 32}]
+    n = 300
+    out = []
+    for cap in (256, 2048):  # 768 sites: resident; 6144 sites: global
+        b = fmc_lib.Batch([sysm], specs, precision=fmc_lib.FMC_PREC_FP32, guest_capacity=cap)
+        b.set_log(n)
+        b.run(n // 2)
+        b.run(n - n // 2)  # two launches: write-back and reload in between
+        out.append((b, [b.log(c, n) for c in range(2)], b.stats()))
+    (b1, l1, s1), (b2, l2, s2) = out
+    for c in range(2):
+        assert s1[c].nummols == s2[c].nummols and s1[c].energy == s2[c].energy
+        for i, (u, v) in enumerate(zip(l1[c], l2[c])):
+            assert (u.move, u.choice, u.overlap, u.accepted, u.estep) == \
+                   (v.move, v.choice, v.overlap, v.accepted, v.estep), (c, i)
+        x1, n1 = b1.coords(c)
+        x2, n2 = b2.coords(c)
+        assert n1 == n2 and np.array_equal(x1[:9 * n1], x2[:9 * n2])  # 3 sites x 3
