@@ -185,12 +185,12 @@ def measured_peak_hbm():
 
 
 def profiled_traffic():
-    """DRAM bytes per launch of the chain kernel from the committed ncu
-    summary of this workload, if present."""
+    """DRAM bytes (read + write) of one step's chain-kernel launches, from
+    the committed ncu summary of this workload, if present."""
     p = os.path.join(ROOT, "profiles", "chain_kernel_config3.json")
     try:
         with open(p) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+            return json.load(f).get("dram_bytes_per_step")
     except Exception:
         return None
 
@@ -315,7 +315,13 @@ def run_ours(args, rank, world, local_rank):
     batch = F.Batch(systems, specs, precision=F.FMC_PREC_FP32, guest_capacity=1024)
     # CTAs per chain for each framework, from timed trial cycles (the
     # chains' state is restored afterwards); set-up, outside the timing
-    clusters = batch.autotune(args.moves) if not args.no_autotune else [1] * len(systems)
+    if args.clusters:
+        clusters = [int(v) for v in args.clusters.split(",")]
+        batch.set_cluster(clusters)
+    elif args.no_autotune:
+        clusters = [1] * len(systems)
+    else:
+        clusters = batch.autotune(args.moves)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
     # per step: the host uploads the chains' fugacities (pinned-free host
@@ -414,6 +420,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
+    ap.add_argument("--clusters", default="", help="CTAs per chain per framework, e.g. 1,2,2,4 "
+                    "(default: autotuned)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -115,6 +115,11 @@ SIGNATURES = {
     "fmc_batch_set_cluster": (C.c_int, [vp, ip, C.c_int]),
     "fmc_batch_get_cluster": (C.c_int, [vp, ip, C.c_int]),
     "fmc_batch_autotune": (C.c_int, [vp, C.c_int, ip, C.c_int]),
+    "fmc_batch_save": (C.c_int, [vp, C.c_char_p]),
+    "fmc_batch_load": (C.c_int, [vp, C.c_char_p]),
+    "fmc_widom_grid": (C.c_int, [vp, C.c_int, C.c_int, ip, C.c_int, C.c_int64, dp, i64p, dp, ip,
+                                 dp]),
+    "fmc_widom_positions": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, ip]),
 }
 
 _lib = None

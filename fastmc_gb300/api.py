@@ -13,6 +13,7 @@ Every call goes to the CUDA library; a missing library raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -166,6 +167,7 @@ class Batch:
         self._h = h
         self.nchains = len(chains)
         self._nsys = len(systems)
+        self._sys_of = [int(c.get("system", 0)) for c in chains]
 
     def set_log(self, cap: int) -> None:
         L.check(L.load().fmc_batch_set_log(self._h, cap))
@@ -219,6 +221,48 @@ class Batch:
         a = (C.c_int * n)()
         L.check(L.load().fmc_batch_autotune(self._h, nmoves, a, n))
         return list(a)
+
+    def save(self, path: str) -> None:
+        """Checkpoint every chain's device state for an exact resume."""
+        L.check(L.load().fmc_batch_save(self._h, os.fsencode(path)))
+
+    def load(self, path: str) -> None:
+        """Resume from a checkpoint of a batch built the same way."""
+        L.check(L.load().fmc_batch_load(self._h, os.fsencode(path)))
+
+    def widom_grid(self, chain: int, ngrid, nstep: int, seed: int = 1, iguest: int = 1,
+                   details: bool = False):
+        """Widom test insertions on a grid (widom_grid): returns
+        (henry, non_overlapping, total) and, with details, per-trial
+        estep, overlap flags and site coordinates."""
+        g = (C.c_int * 3)(*[int(v) for v in ngrid])
+        h = C.c_double()
+        cnt = (C.c_int64 * 2)()
+        nt = int(ngrid[0]) * int(ngrid[1]) * int(ngrid[2]) * int(nstep)
+        ns = self.systems[self._sys_of[chain]].info().guest_nsites[iguest - 1]
+        est = np.zeros(nt) if details else None
+        ovl = np.zeros(nt, dtype=np.int32) if details else None
+        xyz = np.zeros(nt * ns * 3) if details else None
+        L.check(L.load().fmc_widom_grid(
+            self._h, chain, iguest, g, nstep, seed, C.byref(h), cnt,
+            est.ctypes.data_as(L.dp) if details else None,
+            ovl.ctypes.data_as(L.ip) if details else None,
+            xyz.ctypes.data_as(L.dp) if details else None))
+        out = (h.value, cnt[0], cnt[1])
+        if details:
+            return out, est, ovl, xyz.reshape(nt, ns, 3)
+        return out
+
+    def widom_positions(self, chain: int, xyz, iguest: int = 1):
+        """Test-insertion energies (kcal/mol) and overlap flags at given site
+        coordinates, shape (npos, natms, 3)."""
+        a = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64))
+        npos = a.shape[0]
+        est = np.zeros(npos)
+        ovl = np.zeros(npos, dtype=np.int32)
+        L.check(L.load().fmc_widom_positions(self._h, chain, iguest, npos, a.ctypes.data_as(L.dp),
+                                             est.ctypes.data_as(L.dp), ovl.ctypes.data_as(L.ip)))
+        return est, ovl
 
     def cycle_bytes(self):
         """(host->device, device->host) bytes of one run() call with a

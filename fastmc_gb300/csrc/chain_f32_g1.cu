@@ -5,7 +5,7 @@ namespace fmc {
 template cudaError_t launch_chain<true, 1>(int, int, const int *, size_t, cudaStream_t,
                                                const SysDev *, ChainHdr *, const ChainArrays &,
                                                MoveCtx *, LogRec *, int, int, int,
-                                               const double *);
+                                               const double *, const WidomJob &);
 template cudaError_t set_chain_smem<true, 1>(size_t);
 template cudaError_t max_clusters<true, 1>(int, size_t, int *);
 }  // namespace fmc

@@ -20,6 +20,56 @@ constexpr int kModeMoves = 0;   // nmoves main-loop iterations
 constexpr int kModeCreate = 1;  // "create molecules" pre-loading
 constexpr int kModeEval = 2;    // evaluate the move in gctx (per-move ABI)
 constexpr int kModeCommit = 3;  // decide with gctx.rande and commit
+constexpr int kModeWidom = 4;   // test insertions of a WidomJob (no state change)
+
+// Warp 0: trial t of a Widom job as an external insertion (FP64 positions).
+template <bool F32>
+__device__ void widom_propose(BlockShared<F32> &B, const WidomJob &wj, int t) {
+  const int lane = threadIdx.x & 31;
+  MoveCtx &mc = B.mc;
+  const SysDev &S = B.S;
+  const GuestType &G = S.g[wj.iguest];
+  const int ns = G.ns;
+  if (lane == 0) {
+    mc.kind = 1;
+    mc.g = wj.iguest;
+    mc.ns = ns;
+    mc.npos = 1;
+    mc.slot = -1;
+    mc.choice = 0;
+    mc.overlap = 0;
+    mc.accepted = 0;
+    mc.rande = -1.0;
+    mc.estep = 0.0;
+    mc.surf_new = mc.surf_old = 0;
+    B.flags[3] = 0;  // FP64 positions: the evaluation converts them
+    B.flags[4] = 1;  // no delE of other molecule types
+  }
+  if (lane < 3 * ns) {
+    const int s = lane / 3, d = lane % 3;
+    double v;
+    if (wj.xyz_in) {
+      v = wj.xyz_in[((size_t)t * ns + s) * 3 + d];
+    } else {
+      // grid point (1-based fractions) and a random orientation
+      // (random_rot with angle 2 pi, rotation about the origin)
+      const int gi = t / wj.nstep;
+      const int i = gi / (wj.ng[1] * wj.ng[2]) + 1, j = (gi / wj.ng[2]) % wj.ng[1] + 1,
+                k = gi % wj.ng[2] + 1;
+      const double f[3] = {double(i) / wj.ng[0], double(j) / wj.ng[1], double(k) / wj.ng[2]};
+      float dr[7];
+      for (int q = 3; q < 7; ++q) dr[q] = hash_uniform(wj.seed, 4ull * (unsigned long long)t + (q - 3));
+      double qt[4], row[3];
+      draw_quaternion(dr, 2.0 * kPi, qt);
+      qrow(qt, d, row);
+      const double *tp = G.tmpl[s];
+      v = row[0] * tp[0] + row[1] * tp[1] + row[2] * tp[2] + S.cell[d] * f[0] + S.cell[3 + d] * f[1] +
+          S.cell[6 + d] * f[2];
+    }
+    mc.pos[0][s][d] = v;
+    if (wj.xyz_out) wj.xyz_out[((size_t)t * ns + s) * 3 + d] = v;
+  }
+}
 
 template <class T>
 __device__ void block_copy(T *dst, const T *src) {
@@ -34,12 +84,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     chain_kernel(const SysDev *__restrict__ systems, ChainHdr *hdrs, ChainArrays CA,
                  MoveCtx *gctx, LogRec *logs, int logcap, int nmoves, int mode,
                  const double *__restrict__ ctl_fuga, const int *__restrict__ chain_ids,
-                 int csize) {
+                 int csize, WidomJob wj) {
   extern __shared__ __align__(16) unsigned char dyn[];
   BlockShared<F32> &B = *reinterpret_cast<BlockShared<F32> *>(dyn);
   const unsigned long long t_start = global_ns();
   const int rank = csize > 1 ? (int)cluster_rank() : 0;
-  const int chain = chain_ids ? chain_ids[blockIdx.x / csize] : (int)blockIdx.x / csize;
+  const int chain = mode == kModeWidom ? wj.chain
+                    : (chain_ids ? chain_ids[blockIdx.x / csize] : (int)blockIdx.x / csize);
   block_copy(&B.H, hdrs + chain);
   __syncthreads();
   block_copy(&B.S, systems + B.H.system);
@@ -133,6 +184,29 @@ __global__ void __launch_bounds__(kThreads, 1)
       (void)full;
       gctx[chain] = B.mc;
     }
+  } else if (mode == kModeWidom) {
+    double hsum = 0.0;
+    long long nok = 0, ntot = 0;
+    for (int t = blockIdx.x; t < wj.ntrial; t += gridDim.x) {
+      if (threadIdx.x < 32) widom_propose(B, wj, t);
+      __syncthreads();
+      evaluate_any<F32, GN>(B, CA, chain, st);
+      if (threadIdx.x == 0) {
+        ++ntot;
+        if (!B.mc.overlap) {  // H_const = exp(-estep / kboltz / temp), gcmc.f:2537-2541
+          ++nok;
+          hsum += exp(-1.0 * B.mc.estep / kKboltz / B.S.temp);
+        }
+        if (wj.estep_out) wj.estep_out[t] = B.mc.overlap ? 0.0 : B.mc.estep;
+        if (wj.overlap_out) wj.overlap_out[t] = B.mc.overlap;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      wj.partial[3 * blockIdx.x] = hsum;
+      wj.partial[3 * blockIdx.x + 1] = (double)nok;
+      wj.partial[3 * blockIdx.x + 2] = (double)ntot;
+    }
   } else if (mode == kModeCommit) {
     if (threadIdx.x == 0) {
       B.mc = gctx[chain];
@@ -152,6 +226,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (rank == 0 && threadIdx.x == 0)
       for (int q = 1; q < csize; ++q) B.flags[0] |= dsmem_load_s32(dsmem_addr(&B.flags[0], q));
     cluster_barrier();  // the peers stay resident until rank 0 has read them
+  }
+  if (mode == kModeWidom) {  // read-only: the chain's state is left as it was
+    if (st) wj.partial[3 * blockIdx.x + 2] = -1.0;  // flags a device status to the host
+    return;
   }
   if (F32 && CA.resident && rank == 0) {
     // write the guests back in molecule order: molecule i in slot i
@@ -190,10 +268,10 @@ template <bool F32, int GN>
 cudaError_t launch_chain(int nchains, int csize, const int *chain_ids, size_t smem,
                          cudaStream_t stream, const SysDev *systems, ChainHdr *hdrs,
                          const ChainArrays &CA, MoveCtx *gctx, LogRec *logs, int logcap,
-                         int nmoves, int mode, const double *ctl_fuga) {
+                         int nmoves, int mode, const double *ctl_fuga, const WidomJob &wj) {
   if (csize == 1) {
     chain_kernel<F32, GN><<<nchains, kThreads, smem, stream>>>(
-        systems, hdrs, CA, gctx, logs, logcap, nmoves, mode, ctl_fuga, chain_ids, 1);
+        systems, hdrs, CA, gctx, logs, logcap, nmoves, mode, ctl_fuga, chain_ids, 1, wj);
     return cudaGetLastError();
   }
   cudaLaunchConfig_t cfg = {};
@@ -209,7 +287,7 @@ cudaError_t launch_chain(int nchains, int csize, const int *chain_ids, size_t sm
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, chain_kernel<F32, GN>, systems, hdrs, CA, gctx, logs, logcap,
-                            nmoves, mode, ctl_fuga, chain_ids, csize);
+                            nmoves, mode, ctl_fuga, chain_ids, csize, wj);
 }
 
 // Clusters of csize CTAs that can be resident at once (0: cannot launch).

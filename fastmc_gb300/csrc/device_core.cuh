@@ -48,7 +48,8 @@ constexpr int kStWait = 64;        // a bounded wait on an asynchronous copy ran
 constexpr double kPi = 3.141592653589793;
 constexpr double kSqrPi = 1.7724538509055159;
 constexpr double kR4pie0 = 138935.4835;
-constexpr double kBoltz = 1.3806503e-23;
+constexpr double kBoltz = 1.3806503e-23;  // J/K (boltz, utility_pack.f:124)
+constexpr double kKboltz = 1.9872041e-3;  // kcal/mol/K (kboltz, utility_pack.f:121)
 constexpr double kRgas = 8.314472 / 4184.0;
 constexpr double kMinAngle = kPi / 18.0;
 constexpr double kDelrMin = 0.1;
@@ -206,6 +207,34 @@ struct ChainArrays {
 
 // Guest sites a CTA can hold in shared memory (molecule order, hi/lo).
 constexpr int kGuestSmem = 3072;
+
+// Widom test insertions against one chain's current state (widom_grid,
+// gcmc.f:2454-2548): trial t is grid point t / nstep (fractions i/ng0,
+// j/ng1, k/ng2, 1-based as the reference loops) with a random orientation,
+// or the given site coordinates xyz_in[t].  Per CTA: sum of
+// exp(-estep/(kB T)) over non-overlapping trials, their count, all trials.
+struct WidomJob {
+  int chain, iguest;       // chain index, guest type (0-based)
+  int ntrial, nstep;
+  int ng[3];
+  int pad;
+  unsigned long long seed;
+  const double *xyz_in;    // [ntrial][ns][3] or null
+  double *estep_out;       // [ntrial] or null (0 for an overlap)
+  int *overlap_out;        // [ntrial] or null
+  double *xyz_out;         // [ntrial][ns][3] or null
+  double *partial;         // [gridDim.x][3]
+};
+
+// Counter-based uniform variate in [0, 1) with 24 bits, like the
+// generator's values: the splitmix64 finaliser of (seed, index).
+__host__ __device__ inline float hash_uniform(unsigned long long seed, unsigned long long i) {
+  unsigned long long z = seed + 0x9e3779b97f4a7c15ULL * (i + 1);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  z ^= z >> 31;
+  return (float)(z >> 40) * (1.0f / 16777216.0f);
+}
 
 // Description of one trial move (shared memory; copied to global between
 // the evaluate and commit kernels of the per-move ABI).

@@ -94,7 +94,7 @@ template <bool F32, int GN>
 cudaError_t launch_chain(int nchains, int csize, const int *chain_ids, size_t smem,
                          cudaStream_t stream, const SysDev *systems, ChainHdr *hdrs,
                          const ChainArrays &CA, MoveCtx *gctx, LogRec *logs, int logcap,
-                         int nmoves, int mode, const double *ctl_fuga);
+                         int nmoves, int mode, const double *ctl_fuga, const WidomJob &wj);
 template <bool F32, int GN>
 cudaError_t set_chain_smem(size_t smem);
 template <bool F32, int GN>
@@ -103,7 +103,7 @@ cudaError_t max_clusters(int csize, size_t smem, int *out);
   extern template cudaError_t launch_chain<F32, GN>(int, int, const int *, size_t, cudaStream_t, \
                                                     const SysDev *, ChainHdr *,                  \
                                                     const ChainArrays &, MoveCtx *, LogRec *, int, \
-                                                    int, int, const double *);                   \
+                                                    int, int, const double *, const WidomJob &); \
   extern template cudaError_t set_chain_smem<F32, GN>(size_t);                                   \
   extern template cudaError_t max_clusters<F32, GN>(int, size_t, int *);
 FMC_CHAIN_EXTERN(true, 1)
@@ -116,6 +116,7 @@ constexpr int kModeMoves = 0;
 constexpr int kModeCreate = 1;
 constexpr int kModeEval = 2;
 constexpr int kModeCommit = 3;
+constexpr int kModeWidom = 4;
 
 // ----------------------------------------------------- device allocations
 template <class T>
@@ -636,15 +637,16 @@ struct Chains {
     if (stream) cudaStreamDestroy(stream);
   }
 
-  cudaError_t launch_one(int n, int csize, const int *ids, cudaStream_t st, int mode, int nmoves) {
+  cudaError_t launch_one(int n, int csize, const int *ids, cudaStream_t st, int mode, int nmoves,
+                         const WidomJob &wj = WidomJob{}) {
     if (precision == FMC_PREC_FP32 && gn == 1)
       return launch_chain<true, 1>(n, csize, ids, smem, st, sysarr.p, hdr.p, CA, ctx.p, logs.p,
-                                   logcap, nmoves, mode, ctl_fuga.p);
+                                   logcap, nmoves, mode, ctl_fuga.p, wj);
     if (precision == FMC_PREC_FP32)
       return launch_chain<true, kMaxG>(n, csize, ids, smem, st, sysarr.p, hdr.p, CA, ctx.p,
-                                       logs.p, logcap, nmoves, mode, ctl_fuga.p);
+                                       logs.p, logcap, nmoves, mode, ctl_fuga.p, wj);
     return launch_chain<false, kMaxG>(n, csize, ids, smem, st, sysarr.p, hdr.p, CA, ctx.p, logs.p,
-                                      logcap, nmoves, mode, ctl_fuga.p);
+                                      logcap, nmoves, mode, ctl_fuga.p, wj);
   }
 
   int occupancy(int csize) {
@@ -1041,6 +1043,29 @@ static void restore_state(Chains &C, ChainSnapshot &s) {
   copy_buf(C.sk, s.sk, C.stream);
   C.sync();
   C.headers_stale = true;
+}
+
+// Checkpoint file: a header of sizes, then every chain's mutable device
+// arrays as raw bytes (state records, coordinates, order lists, S(k)).
+static const char kCkptMagic[8] = {'F', 'M', 'C', 'G', 'B', '3', '0', '1'};
+
+template <class T>
+static void ckpt_write(std::FILE *f, const DBuf<T> &d) {
+  std::vector<T> h(d.n);
+  if (d.n) FMC_CUDA(cudaMemcpy(h.data(), d.p, d.n * sizeof(T), cudaMemcpyDeviceToHost));
+  const unsigned long long n = d.n;
+  if (std::fwrite(&n, sizeof n, 1, f) != 1 || (n && std::fwrite(h.data(), sizeof(T), n, f) != n))
+    raise(FMC_ERR_ARG, "checkpoint write failed");
+}
+
+template <class T>
+static void ckpt_read(std::FILE *f, DBuf<T> &d) {
+  unsigned long long n = 0;
+  if (std::fread(&n, sizeof n, 1, f) != 1 || n != d.n)
+    raise(FMC_ERR_INPUT, "checkpoint does not match this batch (array size)");
+  std::vector<T> h(n);
+  if (n && std::fread(h.data(), sizeof(T), n, f) != n) raise(FMC_ERR_INPUT, "checkpoint truncated");
+  if (n) FMC_CUDA(cudaMemcpy(d.p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice));
 }
 
 extern "C" {
@@ -1686,6 +1711,166 @@ int fmc_batch_autotune(fmc_batch *b, int nmoves, int *csize_out, int nsys) {
     C.last_ms = ms0;
     if (csize_out)
       for (int i = 0; i < nsys; ++i) csize_out[i] = cur[i];
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_save(fmc_batch *b, const char *path) {
+  return guard([&] {
+    if (!b || !path) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    C.sync();
+    std::unique_ptr<std::FILE, int (*)(std::FILE *)> f(std::fopen(path, "wb"), &std::fclose);
+    if (!f) raise(FMC_ERR_ARG, std::string("cannot open ") + path);
+    const int meta[6] = {C.nchains, (int)C.sys.size(), C.CA.cap, C.CA.nkmax, C.precision,
+                         (int)sizeof(ChainHdr)};
+    if (std::fwrite(kCkptMagic, 1, 8, f.get()) != 8 || std::fwrite(meta, sizeof meta, 1, f.get()) != 1)
+      raise(FMC_ERR_ARG, "checkpoint write failed");
+    ckpt_write(f.get(), C.hdr);
+    ckpt_write(f.get(), C.gpos);
+    ckpt_write(f.get(), C.ghi);
+    ckpt_write(f.get(), C.glo);
+    ckpt_write(f.get(), C.ord);
+    ckpt_write(f.get(), C.freel);
+    ckpt_write(f.get(), C.sk);
+    ckpt_write(f.get(), C.skdf);
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_load(fmc_batch *b, const char *path) {
+  return guard([&] {
+    if (!b || !path) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    C.sync();
+    std::unique_ptr<std::FILE, int (*)(std::FILE *)> f(std::fopen(path, "rb"), &std::fclose);
+    if (!f) raise(FMC_ERR_ARG, std::string("cannot open ") + path);
+    char magic[8];
+    int meta[6];
+    if (std::fread(magic, 1, 8, f.get()) != 8 || std::memcmp(magic, kCkptMagic, 8) != 0)
+      raise(FMC_ERR_INPUT, "not a fastmc_gb300 checkpoint");
+    if (std::fread(meta, sizeof meta, 1, f.get()) != 1) raise(FMC_ERR_INPUT, "checkpoint truncated");
+    const int want[6] = {C.nchains, (int)C.sys.size(), C.CA.cap, C.CA.nkmax, C.precision,
+                         (int)sizeof(ChainHdr)};
+    if (std::memcmp(meta, want, sizeof meta) != 0)
+      raise(FMC_ERR_INPUT, "checkpoint does not match this batch (chains, systems, capacity, "
+                           "k-vectors, precision or library version)");
+    ckpt_read(f.get(), C.hdr);
+    ckpt_read(f.get(), C.gpos);
+    ckpt_read(f.get(), C.ghi);
+    ckpt_read(f.get(), C.glo);
+    ckpt_read(f.get(), C.ord);
+    ckpt_read(f.get(), C.freel);
+    ckpt_read(f.get(), C.sk);
+    ckpt_read(f.get(), C.skdf);
+    C.headers_stale = true;
+    C.pull_headers();
+    for (int c = 0; c < C.nchains; ++c)
+      if (C.host_hdr[c].system < 0 || C.host_hdr[c].system >= (int)C.sys.size())
+        raise(FMC_ERR_INPUT, "checkpoint chain refers to a missing system");
+    return FMC_OK;
+  });
+}
+
+// Widom test insertions (widom_grid, gcmc.f:2454-2548) on one chain: one
+// CTA per SM, each taking every gridDim-th trial against the chain's state,
+// which no trial changes.
+static void run_widom(Chains &C, WidomJob wj, int ns, double *henry, int64_t *counts,
+                      double *estep_out, int *overlap_out, double *xyz_out) {
+  if (wj.ntrial < 1) raise(FMC_ERR_ARG, "no trial insertions");
+  int dev = 0, nsm = 1;
+  FMC_CUDA(cudaGetDevice(&dev));
+  FMC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = std::min(wj.ntrial, nsm);
+  DBuf<double> partial, est, xyz;
+  DBuf<int> ovl;
+  partial.alloc((size_t)grid * 3);
+  if (estep_out) est.alloc(wj.ntrial);
+  if (overlap_out) ovl.alloc(wj.ntrial);
+  if (xyz_out) xyz.alloc((size_t)wj.ntrial * ns * 3);
+  wj.partial = partial.p;
+  wj.estep_out = est.p;
+  wj.overlap_out = ovl.p;
+  wj.xyz_out = xyz.p;
+  FMC_CUDA(C.launch_one(grid, 1, nullptr, C.stream, kModeWidom, 0, wj));
+  C.sync();
+  std::vector<double> part((size_t)grid * 3);
+  FMC_CUDA(cudaMemcpy(part.data(), partial.p, part.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  double sum = 0.0, nok = 0.0, ntot = 0.0;
+  for (int i = 0; i < grid; ++i) {
+    if (part[3 * i + 2] < 0.0)
+      raise(FMC_ERR_DEVICE, "a Widom trial raised a device status (table range, segments)");
+    sum += part[3 * i];
+    nok += part[3 * i + 1];
+    ntot += part[3 * i + 2];
+  }
+  // gcmc.f:2544-2545: averaged over every trial, overlapping ones included
+  if (henry) *henry = ntot > 0 ? sum / ntot : 0.0;
+  if (counts) {
+    counts[0] = (int64_t)nok;
+    counts[1] = (int64_t)ntot;
+  }
+  if (estep_out)
+    FMC_CUDA(cudaMemcpy(estep_out, est.p, wj.ntrial * sizeof(double), cudaMemcpyDeviceToHost));
+  if (overlap_out)
+    FMC_CUDA(cudaMemcpy(overlap_out, ovl.p, wj.ntrial * sizeof(int), cudaMemcpyDeviceToHost));
+  if (xyz_out)
+    FMC_CUDA(cudaMemcpy(xyz_out, xyz.p, (size_t)wj.ntrial * ns * 3 * sizeof(double),
+                        cudaMemcpyDeviceToHost));
+}
+
+static int widom_guest(const Chains &C, int chain, int iguest, int *ns) {
+  if (chain < 0 || chain >= C.nchains) raise(FMC_ERR_ARG, "bad chain index");
+  const ChainHdr &h = C.host_hdr[chain];
+  const System &s = *C.hsys[h.system];
+  if (iguest < 1 || iguest > s.ntpguest) raise(FMC_ERR_ARG, "bad guest type");
+  *ns = s.mol[s.locguest[iguest]].natoms;
+  return h.system;
+}
+
+int fmc_widom_grid(fmc_batch *b, int chain, int iguest, const int *ngrid, int nstep, int64_t seed,
+                   double *henry, int64_t *counts, double *estep_out, int *overlap_out,
+                   double *xyz_out) {
+  return guard([&] {
+    if (!b || !ngrid) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (C.headers_stale || (int)C.host_hdr.size() != C.nchains) C.pull_headers();
+    int ns = 0;
+    widom_guest(C, chain, iguest, &ns);
+    if (ngrid[0] < 1 || ngrid[1] < 1 || ngrid[2] < 1 || nstep < 1) raise(FMC_ERR_ARG, "empty grid");
+    const long long nt = (long long)ngrid[0] * ngrid[1] * ngrid[2] * nstep;
+    if (nt > (1LL << 31) - 1) raise(FMC_ERR_ARG, "too many trials in one call");
+    WidomJob wj{};
+    wj.chain = chain;
+    wj.iguest = iguest - 1;
+    wj.ntrial = (int)nt;
+    wj.nstep = nstep;
+    for (int d = 0; d < 3; ++d) wj.ng[d] = ngrid[d];
+    wj.seed = (unsigned long long)seed;
+    run_widom(C, wj, ns, henry, counts, estep_out, overlap_out, xyz_out);
+    return FMC_OK;
+  });
+}
+
+int fmc_widom_positions(fmc_batch *b, int chain, int iguest, int npos, const double *xyz,
+                        double *estep_out, int *overlap_out) {
+  return guard([&] {
+    if (!b || !xyz) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (C.headers_stale || (int)C.host_hdr.size() != C.nchains) C.pull_headers();
+    int ns = 0;
+    widom_guest(C, chain, iguest, &ns);
+    if (npos < 1) raise(FMC_ERR_ARG, "no positions");
+    DBuf<double> in;
+    in.upload(std::vector<double>(xyz, xyz + (size_t)npos * ns * 3));
+    WidomJob wj{};
+    wj.chain = chain;
+    wj.iguest = iguest - 1;
+    wj.ntrial = npos;
+    wj.nstep = 1;
+    wj.ng[0] = wj.ng[1] = wj.ng[2] = 1;
+    wj.xyz_in = in.p;
+    run_widom(C, wj, ns, nullptr, nullptr, estep_out, overlap_out, nullptr);
     return FMC_OK;
   });
 }

@@ -1,6 +1,6 @@
 """Small, fixed workloads for profiling the chain kernel.
 
-    python -m fastmc_gb300.profile_case --framework 4 --chains 1 --moves 64 --launches 3
+    python -m fastmc_gb300.profile_case --framework 4 --chains 1 --moves 64 --launches 3 [--cluster 4]
 
 builds one of the four batched-isotherm frameworks (1: 25.6 A ... 4: 64.0 A),
 creates the first `--chains` chains of that framework with their initial
@@ -24,6 +24,7 @@ def main() -> None:
     ap.add_argument("--moves", type=int, default=64)
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--fp64", action="store_true")
+    ap.add_argument("--cluster", type=int, default=1, help="CTAs per chain (1..8)")
     args = ap.parse_args()
 
     from . import build, synthetic as syn
@@ -40,6 +41,7 @@ def main() -> None:
               "create_molecules": c.create_molecules} for i, c in sel]
     prec = L.FMC_PREC_FP64 if args.fp64 else L.FMC_PREC_FP32
     b = F.Batch([sysm], specs, precision=prec, guest_capacity=1024)
+    b.set_cluster([args.cluster])
     for it in range(args.launches):
         st = b.run(args.moves)
         ms, ev, mv = b.last_timing()

@@ -252,6 +252,34 @@ int fmc_batch_get_log(fmc_batch *b, int chain, fmc_move_log *log, int cap,
 int fmc_batch_get_coords(fmc_batch *b, int chain, double *xyz, int cap, int *n);
 int fmc_batch_get_sk(fmc_batch *b, int chain, double *sk, int cap);
 
+/* Checkpoint / restart of every chain's device state: state records
+ * (generator, counters, step sizes, energies, averages), guest coordinates,
+ * molecule order and the running S(k), for an exact resume.  The reference
+ * writes REVIVE / REVCON files (utility_pack.f:2299-2405) with coordinates
+ * and averages only; this file also holds S(k) and the generator.  Load
+ * into a batch created from the same systems, chain count, capacity and
+ * precision (checked). */
+int fmc_batch_save(fmc_batch *b, const char *path);
+int fmc_batch_load(fmc_batch *b, const char *path);
+
+/* Widom test-particle insertions of guest type iguest (1-based) against
+ * chain `chain`'s current state, which they do not change (widom_grid,
+ * gcmc.f:2454-2548): trial t is grid point t / nstep (fractions i/ngrid[0],
+ * j/ngrid[1], k/ngrid[2], i = 1..ngrid[0] ..., as the reference loops) with
+ * a random orientation (random_rot with angle 2 pi about the template
+ * origin).  The orientations come from a counter-based hash of (seed,
+ * trial), not from the chain's sequential generator, so that all trials run
+ * in parallel.  henry = sum over non-overlapping trials of
+ * exp(-estep / (kboltz T)) divided by all trials (gcmc.f:2537-2545);
+ * counts = {non-overlapping, all}.  Per-trial estep (kcal/mol, 0 for an
+ * overlap), overlap flags and site coordinates are optional outputs. */
+int fmc_widom_grid(fmc_batch *b, int chain, int iguest, const int *ngrid, int nstep,
+                   int64_t seed, double *henry, int64_t *counts, double *estep_out,
+                   int *overlap_out, double *xyz_out);
+/* The same test insertions at given site coordinates (npos x natms x 3). */
+int fmc_widom_positions(fmc_batch *b, int chain, int iguest, int npos, const double *xyz,
+                        double *estep_out, int *overlap_out);
+
 /* Thread-block clusters: the chains of system i run on clusters of
  * csize[i] CTAs (1..8; default 1).  Each CTA of a cluster takes a share of
  * the chain's framework atoms, guests and k-vectors; results do not depend

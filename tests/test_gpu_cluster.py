@@ -124,3 +124,34 @@ def test_resident_guests_match_global(fmc_lib, inputs_dir):
         x1, n1 = b1.coords(c)
         x2, n2 = b2.coords(c)
         assert n1 == n2 and np.array_equal(x1[:9 * n1], x2[:9 * n2])  # 3 sites x 3
+
+
+def test_checkpoint_resume_exact(fmc_lib, inputs_dir, tmp_path):
+    """A batch resumed from a checkpoint continues bit for bit like the
+    batch that wrote it."""
+    d1 = inputs_dir(syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=10), "cl_a")
+    d2 = inputs_dir(syn.small_test_spec(seed=5, kmax=8, ntile=3, pressure_bar=5.0, create=40), "cl_b")
+    systems = [fmc_lib.System.load(d1), fmc_lib.System.load(d2)]
+    specs = [{"system": s, "seed": 41 + i} for i, s in enumerate([0, 1, 1])]
+    path = str(tmp_path / "chains.ckpt")
+    for prec in (fmc_lib.FMC_PREC_FP32, fmc_lib.FMC_PREC_FP64):
+        a = fmc_lib.Batch(systems, specs, precision=prec, guest_capacity=256)
+        a.set_cluster([1, 2])
+        a.run(150)
+        a.save(path)
+        a.set_log(150)
+        a.run(150)
+        b = fmc_lib.Batch(systems, specs, precision=prec, guest_capacity=256)
+        b.set_cluster([1, 2])
+        b.load(path)
+        b.set_log(150)
+        b.run(150)
+        sa, sb = a.stats(), b.stats()
+        for c in range(len(specs)):
+            assert (sa[c].nummols, sa[c].energy, sa[c].moves) == (sb[c].nummols, sb[c].energy, sb[c].moves)
+            la, lb = a.log(c, 150), b.log(c, 150)
+            for i, (u, v) in enumerate(zip(la, lb)):
+                assert (u.move, u.choice, u.accepted, u.estep) == (v.move, v.choice, v.accepted, v.estep), (c, i)
+    other = fmc_lib.Batch(systems, specs[:2], precision=fmc_lib.FMC_PREC_FP64, guest_capacity=256)
+    with pytest.raises(fmc_lib.FmcError):
+        other.load(path)
