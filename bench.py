@@ -128,7 +128,7 @@ def oracle_built():
 
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -142,12 +142,14 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """Median SM clock and the throttle reasons seen between host times
+        t0 and t1 (seconds since the epoch; all samples when not given)."""
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -156,23 +158,28 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.fh.close()
+        import datetime
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
+            if len(p) < 10:
                 continue
             try:
-                sm.append(float(p[1]))
-                smax.append(float(p[2]))
+                ts = datetime.datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                clk, cmax = float(p[2]), float(p[3])
             except ValueError:
                 continue
-            for n, v in zip(names, p[5:9]):
+            if t0 is not None and not (t0 - 0.025 <= ts <= t1 + 0.025):
+                continue
+            sm.append(clk)
+            smax.append(cmax)
+            for n, v in zip(names, p[6:10]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+                "samples": len(sm), "interval_ms": 20, "reasons": sorted(reasons)}
 
 
 def measured_peak_hbm():
@@ -339,19 +346,22 @@ def run_ours(args, rank, world, local_rank):
         timed_ms.append(ms)
         return st
 
+    clocks = ClockSampler(local_rank)
+    clocks.start()  # running before the timed region; samples inside it are kept
+    time.sleep(0.5)  # nvidia-smi's start-up
     for _ in range(args.warmup):
         step([], [])
     before = batch.stats()
-    clocks = ClockSampler(local_rank)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
+    t_start = time.time()
     ms_list, wall = [], []
     for _ in range(args.steps):
         step(ms_list, wall)
     torch.cuda.synchronize()
-    clk = clocks.stop()
+    t_end = time.time()
+    clk = clocks.stop(t_start, t_end)
     after = batch.stats()
     evals = sum(trial_evals(after[c]) - trial_evals(before[c]) for c in range(len(specs)))
     full = sum(after[c].evals - before[c].evals for c in range(len(specs)))
@@ -392,7 +402,8 @@ def run_ours(args, rank, world, local_rank):
             "trial_moves_per_s": moves / (dev_ms / 1000.0),
             "full_evals_per_s": full / (dev_ms / 1000.0),
             "overlap_exits_per_step": ovl / args.steps,
-            "gpu_launches": args.steps,
+            # one chain-kernel launch per cluster-size group per step
+            "gpu_launches": args.steps * len(set(clusters)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profiled_traffic(),
                          "peak_source": peak_kind,
