@@ -33,8 +33,8 @@ constexpr int kMaxG = 4;    // guest types
 constexpr int kMaxM = 8;    // molecule types
 constexpr int kMaxT = 16;   // atom types
 constexpr int kMaxKm = 40;  // kmax per axis + 1
-constexpr int kPlmMax = 6144;  // entries of the FP32 (l, m) phase table (48 KB)
-constexpr int kMaxSeg = 1536;
+constexpr int kPlmMax = 4352;  // entries of the FP32 (l, m) phase table (34 KB)
+constexpr int kMaxSeg = 1024;
 
 // status word bits (ChainHdr::status)
 constexpr int kStTableLow = 1;     // pair closer than one grid step
