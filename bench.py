@@ -54,7 +54,7 @@ def algorithmic_bytes_per_eval(cutoff: float, nk: int) -> float:
 def trial_evals(st) -> int:
     """Energy evaluations of the trial moves in a chain's counters."""
     a = st.attempts
-    return int(a[0] + a[1] + 2 * (a[2] + a[3] + a[4]))
+    return int(a[0] + a[1] + 2 * (a[2] + a[3] + a[4] + a[5]))
 
 
 def workload(tmp: str):

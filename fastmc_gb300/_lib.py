@@ -25,7 +25,7 @@ MAX_MOLTYPES = 8
 MAX_GUEST_TYPES = 4
 MAX_SITES = 8
 
-MOVE_NAMES = {1: "insert", 2: "delete", 3: "displace", 4: "translate", 5: "rotate"}
+MOVE_NAMES = {1: "insert", 2: "delete", 3: "displace", 4: "translate", 5: "rotate", 6: "jump"}
 
 
 class SystemInfo(C.Structure):
@@ -59,7 +59,7 @@ class ChainSpec(C.Structure):
 
 class ChainStats(C.Structure):
     _fields_ = [("moves", C.c_int64), ("evals", C.c_int64), ("overlap_exits", C.c_int64),
-                ("attempts", C.c_int64 * 5), ("accepts", C.c_int64 * 5),
+                ("attempts", C.c_int64 * 6), ("accepts", C.c_int64 * 6),
                 ("nummols", C.c_int), ("status", C.c_int), ("energy", C.c_double),
                 ("avg_n", C.c_double), ("avg_e", C.c_double), ("avg_en", C.c_double),
                 ("avg_n2", C.c_double), ("avg_e2", C.c_double), ("avg_nf", C.c_double),

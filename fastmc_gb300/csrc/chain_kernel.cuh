@@ -103,6 +103,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     B.cflag = 0u;
   }
   if (threadIdx.x < kMaxCluster) B.xflag[threadIdx.x] = 0u;
+  if constexpr (F32) {
+    for (int i = threadIdx.x; i < kTrigN; i += kThreads) B.trig[i] = CA.trig[i];
+  }
   __syncthreads();  // the system record and header are complete
   if (F32 && CA.resident) {  // guests into shared memory, molecule order
     const int n = B.H.nummols[0], ns = B.S.g[0].ns;

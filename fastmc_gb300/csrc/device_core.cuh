@@ -68,9 +68,11 @@ struct GuestType {
   double ewald3en;
   double chgea[kMaxS];     // q / epsq * r4pie0 per site (ewald2's charge factor)
   float tmplf[kMaxS][3];   // centred template in FP32 (FP32 trial geometry)
+  float tmplf_lo[kMaxS][3];  // template - tmplf (double-float trial geometry)
   int prow[kMaxS][kMaxT + 1];      // table row of site s with atom type t (-1: none)
   float psig2[kMaxS][kMaxT + 1];   // (surftol + sigma)^2 of site s with atom type t
   float wf[kMaxS];         // mass fraction of each site (centre of mass)
+  float wf_lo[kMaxS];      // mass fraction - wf
   float chgeaf[kMaxS];     // the same as an FP32 hi/lo pair
   float chgeaf_lo[kMaxS];
   // constants of the energy expressions of this guest type
@@ -169,6 +171,7 @@ struct ChainHdr {
   long long ins_count[kMaxG], accept_ins[kMaxG], del_count[kMaxG], accept_del[kMaxG];
   long long disp_count[kMaxG], accept_disp[kMaxG], tran_count[kMaxG], accept_tran[kMaxG];
   long long rota_count[kMaxG], accept_rota[kMaxG];
+  long long jump_count[kMaxG], accept_jump[kMaxG];
   long long gcmccount, prodcount, rollcount;
   int production;
   int minchk_left;         // moves until gcmccount is next a multiple of minchk
@@ -181,11 +184,29 @@ struct ChainHdr {
   double wacc[kMaxG][8];
   long long windows;
   long long moves, evals, overlap_exits;
-  long long attempts[5], accepts[5];
+  long long attempts[6], accepts[6];  // insert, delete, displace, translate, rotate, jump
   long long log_n;
   int system;
   int pad1;
+  // FP32 path: the step sizes as float hi/lo pairs, kept equal to the
+  // doubles above (sync_step_pairs after every change)
+  float sh_disp[kMaxG][2];  // 0.5 * delrdisp
+  float sh_tran[kMaxG][2];  // 0.5 * tran_delr
+  float rho_rot[2][2];      // rotangle / (2 pi), rota_rotangle / (2 pi)
 };
+
+__host__ __device__ inline void split_pair(double x, float *out) {
+  out[0] = (float)x;
+  out[1] = (float)(x - (double)out[0]);
+}
+
+// The pairs of guest type g and the two rotation angles.
+__host__ __device__ inline void sync_step_pairs(ChainHdr &h, int g) {
+  split_pair(0.5 * h.delrdisp[g], h.sh_disp[g]);
+  split_pair(0.5 * h.tran_delr[g], h.sh_tran[g]);
+  split_pair(h.rotangle * (0.5 / kPi), h.rho_rot[0]);
+  split_pair(h.rota_rotangle * (0.5 / kPi), h.rho_rot[1]);
+}
 
 // Per-chain arrays.
 struct ChainArrays {
@@ -200,10 +221,16 @@ struct ChainArrays {
   double2 *sold;    // [chain][nkmax] scratch s(k) of the old position
   float2 *snew32;   // FP32 path: the same scratch in FP32
   float2 *sold32;
+  const float4 *trig;  // [kTrigN] sin(2 pi k/kTrigN) hi, lo, cos(2 pi k/kTrigN) hi, lo
   int cap;          // molecules per guest type
   int nkmax;
   int resident;     // FP32 batches of one guest type: guests held in shared memory
 };
+
+// Entries of the sine/cosine table of the double-float quaternions (one
+// turn): half angles pi * rho are split at the nearest multiple of
+// 2 pi / kTrigN.
+constexpr int kTrigN = 128;
 
 // Guest sites a CTA can hold in shared memory (molecule order, hi/lo).
 constexpr int kGuestSmem = 3072;
@@ -598,6 +625,48 @@ struct DF {
   }
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
+
+// Double-float values for the FP32 path's trial geometry: h + l with
+// |l| <= ulp(h)/2.  Products use __fmul_rn and explicit fmaf so that no
+// product is contracted into a following sum (which would break the
+// error-free steps).  Sums: two_sum of the high parts, low parts added,
+// renormalised; products: exact high product by fmaf plus cross terms.
+struct F2 {
+  float h, l;
+};
+__device__ __forceinline__ F2 f2_norm(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  float s, e;
+  two_sum_f(a.h, b.h, s, e);
+  e += a.l + b.l;
+  return f2_norm(s, e);
+}
+__device__ __forceinline__ F2 f2_addf(F2 a, float b) {
+  float s, e;
+  two_sum_f(a.h, b, s, e);
+  return f2_norm(s, e + a.l);
+}
+__device__ __forceinline__ F2 f2_neg(F2 a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ F2 f2_sub(F2 a, F2 b) { return f2_add(a, f2_neg(b)); }
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return f2_norm(p, e);
+}
+__device__ __forceinline__ F2 f2_mulf(F2 a, float b) {
+  const float p = __fmul_rn(a.h, b);
+  float e = fmaf(a.h, b, -p);
+  e = fmaf(a.l, b, e);
+  return f2_norm(p, e);
+}
+__device__ __forceinline__ F2 f2_shfl(F2 a, int src) {
+  return {__shfl_sync(0xffffffffu, a.h, src), __shfl_sync(0xffffffffu, a.l, src)};
+}
 
 template <bool F32>
 struct AccT;

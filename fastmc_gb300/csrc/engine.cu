@@ -469,8 +469,12 @@ void build_device_system(const System &s, DevSystem &D) {
       double mt = 0.0;
       for (int i = 0; i < m.natoms; ++i) mt += m.wght[i];
       for (int i = 0; i < m.natoms; ++i) {
-        for (int dd = 0; dd < 3; ++dd) G.tmplf[i][dd] = (float)G.tmpl[i][dd];
+        for (int dd = 0; dd < 3; ++dd) {
+          G.tmplf[i][dd] = (float)G.tmpl[i][dd];
+          G.tmplf_lo[i][dd] = (float)(G.tmpl[i][dd] - (double)G.tmplf[i][dd]);
+        }
         G.wf[i] = (float)(m.wght[i] / mt);
+        G.wf_lo[i] = (float)(m.wght[i] / mt - (double)G.wf[i]);
       }
     }
     G.ewald3en = s.ewald3en[G.mol];
@@ -564,6 +568,7 @@ ChainHdr initial_header(const System &s, int system_index, long long seed,
   if (fuga_override && *fuga_override >= 0.0) h.fuga[0] = *fuga_override;
   h.rotangle = kPi / 3.0;
   h.rota_rotangle = h.rotangle;
+  for (int g = 0; g < kMaxG; ++g) sync_step_pairs(h, g);
   h.production = s.eqsteps == 0 ? 1 : 0;
   h.minchk_left = std::max(1, s.minchk);
   h.window_left = std::max(1, s.nwindsteps);
@@ -598,6 +603,7 @@ struct Chains {
   DBuf<double2> sk, snew, sold;
   DBuf<float2> snew32, sold32;
   DBuf<float4> skdf;
+  DBuf<float4> trig;  // sin/cos(pi k / 256) hi/lo pairs
   DBuf<MoveCtx> ctx;
   DBuf<LogRec> logs;
   DBuf<double> ctl_fuga;
@@ -804,6 +810,18 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   C.ctx.alloc(nchains);
   C.ctx.zero();
   C.logs.alloc(1);
+  {  // sin and cos of 2 pi k / kTrigN as float hi/lo pairs (double-float quaternions)
+    std::vector<float4> t(kTrigN);
+    for (int k = 0; k < kTrigN; ++k) {
+      float a[2], b[2];
+      split_pair(std::sin(2.0 * kPi * k / kTrigN), a);
+      split_pair(std::cos(2.0 * kPi * k / kTrigN), b);
+      t[k] = make_float4(a[0], a[1], b[0], b[1]);
+    }
+    C.trig.alloc(kTrigN);
+    FMC_CUDA(cudaMemcpy(C.trig.p, t.data(), kTrigN * sizeof(float4), cudaMemcpyHostToDevice));
+  }
+  CA.trig = C.trig.p;
   CA.gpos = C.gpos.p;
   CA.ghi = C.ghi.p;
   CA.glo = C.glo.p;
@@ -845,7 +863,7 @@ void fill_stats(const Chains &C, fmc_chain_stats *out) {
     o.moves = h.moves;
     o.evals = h.evals;
     o.overlap_exits = h.overlap_exits;
-    for (int i = 0; i < 5; ++i) {
+    for (int i = 0; i < 6; ++i) {
       o.attempts[i] = h.attempts[i];
       o.accepts[i] = h.accepts[i];
     }

@@ -43,8 +43,9 @@ struct BlockShared {
   EvalSmem<F32> ev;
   SiteInfo si[kMaxS];
   float draws[8];
+  float stepf[4];    // FP32 path: shift half-width and half-angle / pi scale, hi/lo
+  float4 trig[kTrigN];  // FP32 path: the quaternion table (copied per launch)
   double geo[12];    // a, b, c, q1..q4, rotation angle, com/frac scratch
-  float geof[4];     // FP32 path: shift a, b, c and the rotation angle
   double vtmp[3];
   int flags[8];     // 0 status, 1 slot, 2 "translate" (q = 0), 3 FP32 geometry, 4 delE deferred
   // cluster exchange (chains on more than one CTA): per-CTA partial totals,
@@ -164,33 +165,39 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   if (randmov < G.mcinsf) kind = 1;
   else if (randmov < G.mcdelf) kind = 2;
   else if (randmov < G.mcdisf) kind = 3;
-  else if (randmov < G.mcjmpf) kind = 3;  // jump/swap are refused at set-up
+  else if (randmov < G.mcjmpf) kind = 6;  // jump (swap is refused at set-up)
   else if (randmov < G.mcswpf) kind = 3;
   else if (randmov < G.mctraf) kind = 4;
   else if (randmov < G.mcrotf) kind = 5;
   else kind = 3;
   // adaptive step sizes (gcmc.f:859-900)
+  bool upd = false;
   if (nmols >= 1 && H.disp_count[g] >= 1) {
     if (H.disp_count[g] % 100 == 0) {
+      upd = true;
       double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
       if (ratio > G.disp_ratio) H.delrdisp[g] *= 1.05;
       else if (H.delrdisp[g] > kDelrMin) H.delrdisp[g] *= 0.95;
     } else if (H.disp_count[g] % 50 == 0) {
+      upd = true;
       double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
       if (ratio > G.disp_ratio) H.rotangle *= 1.05;
       else if (H.rotangle > kMinAngle) H.rotangle *= 0.95;
     }
   }
   if (nmols >= 1 && H.tran_count[g] >= 1 && H.tran_count[g] % 100 == 0) {
+    upd = true;
     double ratio = double(H.accept_tran[g]) / double(H.tran_count[g]);
     if (ratio > G.tran_ratio) H.tran_delr[g] *= 1.05;
     else if (H.tran_delr[g] > kDelrMin) H.tran_delr[g] *= 0.95;
   }
   if (nmols >= 1 && H.rota_count[g] >= 1 && H.rota_count[g] % 100 == 0) {
+    upd = true;
     double ratio = double(H.accept_rota[g]) / double(H.rota_count[g]);
     if (ratio > G.rota_ratio) H.rota_rotangle *= 1.05;
     else if (H.rota_rotangle > kMinAngle) H.rota_rotangle *= 0.95;
   }
+  if (F32 && upd) sync_step_pairs(H, g);
   if (nmols == 0) kind = 1;
   mc.kind = kind;
   mc.g = g;
@@ -204,16 +211,26 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   } else if (kind == 2) {
     H.del_count[g]++;
     mc.choice = pick1(duni_f(H), nmols);
+  } else if (kind == 6) {
+    // mc_jump (gcmc.f:1937-2039): the molecule, then random_jump's point
+    // (utility_pack.f:3359-3380) and random_rot with angle 2 pi
+    H.jump_count[g]++;
+    mc.choice = pick1(duni_f(H), nmols);
+    for (int i = 0; i < 7; ++i) B.draws[i] = duni_f(H);
+    if constexpr (!F32) B.geo[7] = 2.0 * kPi;
+    B.flags[2] = 0;
+    mc.npos = 2;
   } else {
     double a = 0.0, b = 0.0, c = 0.0;
     B.draws[3] = -1.0f;  // no rotation unless drawn
-    B.geof[0] = B.geof[1] = B.geof[2] = 0.0f;
     if (kind != 5) {     // random_disp (utility_pack.f:3333-3357)
-      double dd = kind == 4 ? H.tran_delr[g] : H.delrdisp[g];
-      if constexpr (F32) {
-        const float hf = (float)(dd * 0.5);
-        for (int i = 0; i < 3; ++i) B.geof[i] = (2.0f * duni_f(H) - 1.0f) * hf;
+      if constexpr (F32) {  // the draws; the shift is built by the geometry
+        for (int i = 0; i < 3; ++i) B.draws[i] = duni_f(H);
+        const float *hp = kind == 4 ? H.sh_tran[g] : H.sh_disp[g];
+        B.stepf[0] = hp[0];
+        B.stepf[1] = hp[1];
       } else {
+        double dd = kind == 4 ? H.tran_delr[g] : H.delrdisp[g];
         double h = dd * 0.5;
         a = (2.0 * (double)duni_f(H) - 1.0) * h;
         b = (2.0 * (double)duni_f(H) - 1.0) * h;
@@ -222,8 +239,13 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
     }
     if (kind != 4) {  // random_rot (utility_pack.f:3526-3563)
       for (int i = 3; i < 7; ++i) B.draws[i] = duni_f(H);
-      B.geo[7] = kind == 5 ? H.rota_rotangle : H.rotangle;
-      B.geof[3] = (float)B.geo[7];
+      if constexpr (F32) {
+        const float *rp = H.rho_rot[kind == 5 ? 1 : 0];
+        B.stepf[2] = rp[0];
+        B.stepf[3] = rp[1];
+      } else {
+        B.geo[7] = kind == 5 ? H.rota_rotangle : H.rotangle;
+      }
       B.flags[2] = 0;
     } else {
       // "move translate" keeps q1..q4 = 0 (gcmc.f:1842), and rotation()
@@ -311,6 +333,19 @@ __device__ void geometry_warp(BlockShared<F32> &B, const ChainArrays &CA, int ch
     if (mine) mc.pos[0][s][d] = old;
     return;
   }
+  if (mc.kind == 6) {
+    // jump: the translation from the old centre of mass to the drawn point
+    if (mine) mc.pos[1][s][d] = old;
+    __syncwarp();
+    if (lane < 3) {
+      double cm = 0.0;
+      for (int k = 0; k < ns; ++k) cm += mc.pos[1][k][lane] * G.mass[k];
+      const double cart = (double)B.draws[0] * S.cell[lane] + (double)B.draws[1] * S.cell[3 + lane] +
+                          (double)B.draws[2] * S.cell[6 + lane];
+      B.geo[lane] = cart - cm * G.rmass;
+    }
+    __syncwarp();
+  }
   // translate (utility_pack.f:3161-3218): shift, wrap the centre of mass
   if (mine) {
     mc.pos[1][s][d] = old;
@@ -379,13 +414,26 @@ __device__ __forceinline__ void position_bounds(BlockShared<F32> &B, int p) {
   B.ev.rmx[p] = sqrtf(rm2) + 1e-3f;
 }
 
-// FP32 path, moves drawn on the device: geometry_warp's construction with
-// the positions built directly as float hi/lo pairs and no FP64 instruction
-// (orthorhombic cells).  One lane per site coordinate.  Insertion: the
-// template rotated by the drawn quaternion plus the drawn fractional centre
-// times the edge (an exact hi/lo product).  Displacement: shift, wrap the
-// centre of mass into the cell by whole edges, rotate about it.  Also fills
-// the site constants and the bounds of each position.
+// FP32 quaternion of random_ins / random_rot: half angle pi * r * scale
+// (scale = angle / 2 pi), axis (2 r - 1) normalised.
+__device__ __forceinline__ void quat_f32(const float *dr, float scale, float *q) {
+  float sn, cs;
+  sincospif(dr[3] * scale, &sn, &cs);
+  const float b1 = 2.0f * dr[4] - 1.0f, b2 = 2.0f * dr[5] - 1.0f, b3 = 2.0f * dr[6] - 1.0f;
+  const float rn = rsqrtf(b1 * b1 + b2 * b2 + b3 * b3);
+  q[0] = cs;
+  q[1] = sn * (b1 * rn);
+  q[2] = sn * (b2 * rn);
+  q[3] = sn * (b3 * rn);
+}
+
+// FP32 path, moves drawn on the device, first pass: geometry_warp's
+// construction in plain FP32 arithmetic on hi/lo positions (good to about
+// 1e-7 A), for the overlap test that ends most trial moves.  A move that
+// passes it gets its positions again from refine_geometry at double-float
+// precision before its energy is evaluated.  One lane per site coordinate;
+// orthorhombic cells.  Also fills the site constants and the bounds of each
+// position (their 1e-3 A margin covers the refinement).
 template <bool F32>
 __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   const SysDev &S = B.S;
@@ -402,18 +450,13 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
   const float Lh = S.boxh[d], Ll = S.boxl[d];
   float ph = 0.f, pl = 0.f, e;
   if (mc.kind == 1) {
-    float sn, cs;
-    sincospif(B.draws[3], &sn, &cs);  // half of the angle 2 pi r
-    const float b1 = 2.0f * B.draws[4] - 1.0f, b2 = 2.0f * B.draws[5] - 1.0f,
-                b3 = 2.0f * B.draws[6] - 1.0f;
-    const float rn = rsqrtf(b1 * b1 + b2 * b2 + b3 * b3);
-    const float q[4] = {cs, sn * (b1 * rn), sn * (b2 * rn), sn * (b3 * rn)};
-    float row[3];
+    float q[4], row[3];
+    quat_f32(B.draws, 1.0f, q);
     qrow(q, d, row);
     const float *t = G.tmplf[s];
     const float v = row[0] * t[0] + row[1] * t[1] + row[2] * t[2];
     const float u = B.draws[d];
-    const float ch = u * Lh;
+    const float ch = __fmul_rn(u, Lh);
     const float cl = fmaf(u, Lh, -ch) + u * Ll;
     two_sum_f(ch, v, ph, e);
     pl = cl + e;
@@ -435,16 +478,28 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
         ev.phi[1][s][d] = oh;
         ev.plo[1][s][d] = ol;
       }
-      two_sum_f(oh, B.geof[d], ph, e);  // shift (zero for "move rotate")
+      // centre of mass of the old molecule, relative to site 0 (jump only)
+      const float p0h = __shfl_sync(full, oh, d), p0l = __shfl_sync(full, ol, d);
+      float sh = 0.f;
+      if (mc.kind == 6) {  // jump: the old centre of mass to the drawn point
+        const float off = mine ? ((oh - p0h) + (ol - p0l)) * G.wf[s] : 0.f;
+        float cof = 0.f;
+        for (int s2 = 0; s2 < ns; ++s2) cof += __shfl_sync(full, off, 3 * s2 + d);
+        const float u = B.draws[d];
+        sh = (__fmul_rn(u, Lh) - p0h) + ((fmaf(u, Lh, -__fmul_rn(u, Lh)) + u * Ll) - p0l) - cof;
+      } else if (mc.kind != 5) {
+        sh = __fmul_rn(2.0f * B.draws[d] - 1.0f, B.stepf[0]);
+      }
+      two_sum_f(oh, sh, ph, e);
       pl = ol + e;
       // centre of mass, relative to site 0, as a hi/lo pair
-      const float p0h = __shfl_sync(full, ph, d), p0l = __shfl_sync(full, pl, d);
-      const float off = mine ? ((ph - p0h) + (pl - p0l)) * G.wf[s] : 0.f;
+      const float s0h = __shfl_sync(full, ph, d), s0l = __shfl_sync(full, pl, d);
+      const float off = mine ? ((ph - s0h) + (pl - s0l)) * G.wf[s] : 0.f;
       float cof = 0.f;
       for (int s2 = 0; s2 < ns; ++s2) cof += __shfl_sync(full, off, 3 * s2 + d);
       float cmh, cml;
-      two_sum_f(p0h, cof, cmh, e);
-      cml = p0l + e;
+      two_sum_f(s0h, cof, cmh, e);
+      cml = s0l + e;
       // wrap the centre into the cell by whole edges (translate)
       const float k = floorf((cmh + cml) * S.rboxf[d]);
       if (k != 0.0f) {
@@ -456,19 +511,10 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
         cmh = t;
         cml += e - k * Ll;
       }
-      if (B.draws[3] >= 0.0f) {  // rotation about the wrapped centre
+      if (mc.kind == 6 || B.draws[3] >= 0.0f) {  // rotation about the wrapped centre
         float q[4] = {0.f, 0.f, 0.f, 0.f};  // "move translate": q = 0, Q = -I
-        if (!B.flags[2]) {
-          float sn, cs;
-          sincosf(0.5f * (B.draws[3] * B.geof[3]), &sn, &cs);
-          const float b1 = 2.0f * B.draws[4] - 1.0f, b2 = 2.0f * B.draws[5] - 1.0f,
-                      b3 = 2.0f * B.draws[6] - 1.0f;
-          const float rn = rsqrtf(b1 * b1 + b2 * b2 + b3 * b3);
-          q[0] = cs;
-          q[1] = sn * (b1 * rn);
-          q[2] = sn * (b2 * rn);
-          q[3] = sn * (b3 * rn);
-        }
+        if (mc.kind == 6) quat_f32(B.draws, 1.0f, q);
+        else if (!B.flags[2]) quat_f32(B.draws, B.stepf[2], q);
         const float x = (ph - cmh) + (pl - cml);
         const float x0 = __shfl_sync(full, x, 3 * s), x1 = __shfl_sync(full, x, 3 * s + 1),
                     x2 = __shfl_sync(full, x, 3 * s + 2);
@@ -497,6 +543,140 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
   }
   __syncwarp();
   if (lane < mc.npos) position_bounds(B, lane);
+}
+
+// Double-float quaternion: the half angle pi * rho, rho = r * scale (scale
+// = angle / 2 pi), from the table of sin/cos(pi k / 64) at the nearest k
+// and the Taylor series of the remainder t (|t| <= pi / 128: sin t = t -
+// t^3/6 + t^5/120, cos t = 1 - t^2/2 + t^4/24 - t^6/720, the next terms
+// below 2e-15); the axis (2 r - 1, exact in double-float) scaled by 1/|axis|
+// from rsqrtf and one Newton step.
+__device__ __forceinline__ void quat_df(const float *dr, F2 scale, const float4 *trig, F2 *q) {
+  const F2 rho = f2_mulf(scale, dr[3]);
+  const float nf = rintf(rho.h * 64.0f);
+  float rh, rl;
+  two_sum_f(rho.h - nf * 0.015625f, rho.l, rh, rl);  // rho.h - nf/64 is exact
+  const float4 T = trig[((int)nf) & (kTrigN - 1)];
+  const F2 t = f2_mul(F2{3.14159274f, -8.74227766e-8f}, F2{rh, rl});
+  const float t2 = __fmul_rn(t.h, t.h);
+  const float s3 = __fmul_rn(t.h, t2) * fmaf(t2, 1.0f / 120.0f, -1.0f / 6.0f);
+  const F2 st = f2_addf(t, s3);
+  const float tte = fmaf(2.0f * t.h, t.l, fmaf(t.h, t.h, -t2));
+  F2 ct = f2_add(F2{1.0f, 0.0f}, F2{-0.5f * t2, -0.5f * tte});
+  ct = f2_addf(ct, __fmul_rn(t2, t2) * fmaf(t2, -1.0f / 720.0f, 1.0f / 24.0f));
+  const F2 Sk = {T.x, T.y}, Ck = {T.z, T.w};
+  const F2 sn = f2_add(f2_mul(Sk, ct), f2_mul(Ck, st));
+  const F2 cs = f2_sub(f2_mul(Ck, ct), f2_mul(Sk, st));
+  F2 b[3];
+  for (int i = 0; i < 3; ++i) two_sum_f(2.0f * dr[4 + i], -1.0f, b[i].h, b[i].l);
+  const F2 n2 = f2_add(f2_add(f2_mul(b[0], b[0]), f2_mul(b[1], b[1])), f2_mul(b[2], b[2]));
+  const float y = rsqrtf(n2.h);
+  const F2 r = f2_mul(n2, f2_mulf(F2{y, 0.0f}, y));
+  const float res = (1.0f - r.h) - r.l;
+  const F2 rn = f2_addf(F2{y, 0.0f}, __fmul_rn(0.5f * y, res));
+  const F2 srn = f2_mul(sn, rn);
+  q[0] = cs;
+  for (int i = 0; i < 3; ++i) q[i + 1] = f2_mul(srn, b[i]);
+}
+
+// Row d of rotation() (utility_pack.f:3497-3506) in double-float.  The ten
+// quaternion products are formed on every lane (no divergence on d).
+__device__ __forceinline__ void qrow_df(const F2 *q, int d, F2 *row) {
+  auto m2 = [](F2 x, F2 y) {
+    const F2 p = f2_mul(x, y);
+    return F2{2.0f * p.h, 2.0f * p.l};
+  };
+  const F2 q11 = m2(q[0], q[0]), q22 = m2(q[1], q[1]), q33 = m2(q[2], q[2]), q44 = m2(q[3], q[3]);
+  const F2 q12 = m2(q[0], q[1]), q13 = m2(q[0], q[2]), q14 = m2(q[0], q[3]);
+  const F2 q23 = m2(q[1], q[2]), q24 = m2(q[1], q[3]), q34 = m2(q[2], q[3]);
+  const F2 dg = d == 0 ? q22 : (d == 1 ? q33 : q44);
+  const F2 diag = f2_addf(f2_add(dg, q11), -1.0f);
+  if (d == 0) {
+    row[0] = diag;
+    row[1] = f2_sub(q23, q14);
+    row[2] = f2_add(q24, q13);
+  } else if (d == 1) {
+    row[0] = f2_add(q23, q14);
+    row[1] = diag;
+    row[2] = f2_sub(q34, q12);
+  } else {
+    row[0] = f2_sub(q24, q13);
+    row[1] = f2_add(q34, q12);
+    row[2] = diag;
+  }
+}
+
+// Second pass of the FP32 path's device-drawn geometry, for a move that
+// passed the overlap test: geometry_warp's construction in double-float
+// (about 48-bit significands), so that the positions agree with the FP64
+// construction to ~1e-13 A.  A position error of 1e-7 A (plain FP32)
+// would move a repulsive r^-12 term near the overlap distance by ~1e-6
+// relative; this one moves it by ~1e-12.  Warp 0, one lane per site
+// coordinate; the draws, old positions (phi/plo[1]) and step sizes are the
+// first pass's.
+template <bool F32>
+__device__ __noinline__ void refine_geometry(BlockShared<F32> &B, const ChainArrays &CA) {
+  const SysDev &S = B.S;
+  const MoveCtx &mc = B.mc;
+  EvalSmem<F32> &ev = B.ev;
+  const int lane = threadIdx.x & 31;
+  const GuestType &G = S.g[mc.g];
+  const int ns = G.ns;
+  const bool mine = lane < 3 * ns;
+  const int s = mine ? lane / 3 : 0;
+  const int d = lane % 3;
+  const F2 L = {S.boxh[d], S.boxl[d]};
+  const bool free_rot = mc.kind == 1 || mc.kind == 6;  // angle 2 pi
+  const bool rot = free_rot || B.draws[3] >= 0.0f;
+  F2 q[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};  // "move translate": Q = -I
+  if (rot && (free_rot || !B.flags[2]))
+    quat_df(B.draws, free_rot ? F2{1.0f, 0.0f} : F2{B.stepf[2], B.stepf[3]}, B.trig, q);
+  F2 row[3];
+  if (rot) qrow_df(q, d, row);
+  auto cart = [&]() {  // the drawn point u * L, u = draws[d]
+    const float u = B.draws[d];
+    const float ch = __fmul_rn(u, L.h);
+    return f2_norm(ch, fmaf(u, L.h, -ch) + __fmul_rn(u, L.l));
+  };
+  auto com = [&](F2 p) {  // centre of mass, coordinate d (sum of m_k/M x_k)
+    F2 c = {0.f, 0.f};
+    for (int k = 0; k < ns; ++k) c = f2_add(c, f2_mul(F2{G.wf[k], G.wf_lo[k]}, f2_shfl(p, 3 * k + d)));
+    return c;
+  };
+  auto rotate = [&](F2 x) {  // row d of Q times the site's offset x
+    const F2 x0 = f2_shfl(x, 3 * s), x1 = f2_shfl(x, 3 * s + 1), x2 = f2_shfl(x, 3 * s + 2);
+    return f2_add(f2_add(f2_mul(row[0], x0), f2_mul(row[1], x1)), f2_mul(row[2], x2));
+  };
+  F2 p;
+  if (mc.kind == 1) {  // random_ins: template rotated about the drawn point
+    F2 t = {0.f, 0.f};
+    if (mine) t = {G.tmplf[s][d], G.tmplf_lo[s][d]};
+    p = f2_add(cart(), rotate(t));
+  } else {
+    F2 o = {0.f, 0.f};
+    if (mine) o = {ev.phi[1][s][d], ev.plo[1][s][d]};
+    F2 a = {0.f, 0.f};
+    if (mc.kind == 6) {
+      a = f2_sub(cart(), com(o));
+    } else if (mc.kind != 5) {
+      F2 b;
+      two_sum_f(2.0f * B.draws[d], -1.0f, b.h, b.l);
+      a = f2_mul(b, F2{B.stepf[0], B.stepf[1]});
+    }
+    p = f2_add(o, a);
+    F2 c = com(p);
+    const float k = floorf(c.h * S.rboxf[d]);  // wrap the centre into the cell
+    if (k != 0.0f) {
+      const F2 kL = f2_mulf(L, k);
+      p = f2_sub(p, kL);
+      c = f2_sub(c, kL);
+    }
+    if (rot) p = f2_add(c, rotate(f2_sub(p, c)));
+  }
+  if (mine) {
+    ev.phi[0][s][d] = p.h;
+    ev.plo[0][s][d] = p.l;
+  }
 }
 
 // Warp 0 proposal for all modes; ends with a block barrier.
@@ -1138,6 +1318,11 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       __syncthreads();
       return 0;
     }
+    if constexpr (F32) {
+      // FP32 first-pass geometry: warp 0 refines it; the positions are
+      // next read after build_segments' barriers
+      if (B.flags[3] && threadIdx.x < 32) refine_geometry(B, CA);
+    }
   }
   PosAcc<F32, GN> acc0, acc1;
   acc0.zero();
@@ -1534,6 +1719,7 @@ __device__ void stats(BlockShared<F32> &B) {
     else if (mc.kind == 2) H.accept_del[g]++;
     else if (mc.kind == 4) H.accept_tran[g]++;
     else if (mc.kind == 5) H.accept_rota[g]++;
+    else if (mc.kind == 6) H.accept_jump[g]++;
     else H.accept_disp[g]++;
   }
   if (mc.kind >= 1) {

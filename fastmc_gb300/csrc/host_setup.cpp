@@ -745,9 +745,9 @@ void finish_control(System &s) {
     s.mctraf[i] = s.mcswpf[i] + (s.mctraf[i] / nrm);
     s.mcrotf[i] = s.mctraf[i] + (s.mcrotf[i] / nrm);
     s.mcswif[i] = s.mcrotf[i] + (s.mcswif[i] / nrm);
-    // jump, swap and switch are not on this path: refuse inputs that use them
-    if (s.mcjmpf[i] > s.mcdisf[i] || s.mcswpf[i] > s.mcjmpf[i] || s.mcswif[i] > s.mcrotf[i])
-      raise(FMC_ERR_INPUT, "jump, swap and switch moves are not supported");
+    // swap and switch are not on this path: refuse inputs that use them
+    if (s.mcswpf[i] > s.mcjmpf[i] || s.mcswif[i] > s.mcrotf[i])
+      raise(FMC_ERR_INPUT, "swap and switch moves are not supported");
   }
   s.beta = 1.0 / (kKboltz * s.temp);
   s.statvolm = s.volm * 1e-30;

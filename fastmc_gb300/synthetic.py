@@ -247,8 +247,11 @@ def config5() -> GcmcSpec:
 
 def small_test_spec(seed: int = 7, kmax: int = 5, ntile: int = 2,
                     pressure_bar: float = 10.0, create: int = 0,
-                    cutoff: float = 12.5) -> GcmcSpec:
+                    cutoff: float = 12.5, move_mix: Optional[Sequence[tuple]] = None) -> GcmcSpec:
     """A small case for parity tests (seconds on the oracle)."""
-    return GcmcSpec(ntile=ntile, fw_seed=seed, alpha=0.26, kmax=kmax,
+    spec = GcmcSpec(ntile=ntile, fw_seed=seed, alpha=0.26, kmax=kmax,
                     pressure_bar=pressure_bar, steps=10000, create_molecules=create,
                     cutoff=cutoff, title=f"test seed{seed}")
+    if move_mix is not None:
+        spec.move_mix = tuple(move_mix)
+    return spec

@@ -49,6 +49,7 @@ extern "C" {
 #define FMC_MOVE_DISPLACE 3  /* "move displace": translation + rotation */
 #define FMC_MOVE_TRANSLATE 4 /* "move translate" */
 #define FMC_MOVE_ROTATE 5    /* "move rotate" */
+#define FMC_MOVE_JUMP 6      /* "move jump" (mc_jump, gcmc.f:1937-2039) */
 
 #define FMC_MAX_MOLTYPES 8
 #define FMC_MAX_GUEST_TYPES 4
@@ -198,8 +199,8 @@ typedef struct {
   int64_t moves;           /* trial moves done */
   int64_t evals;           /* completed energy evaluations (no overlap exit) */
   int64_t overlap_exits;   /* positions rejected by the overlap test */
-  int64_t attempts[5];     /* insert, delete, displace, translate, rotate */
-  int64_t accepts[5];
+  int64_t attempts[6];     /* insert, delete, displace, translate, rotate, jump */
+  int64_t accepts[6];
   int nummols;
   int status;              /* device status word */
   double energy;           /* energy(guest mol), FIELD unit */

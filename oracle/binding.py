@@ -185,7 +185,7 @@ class Oracle:
                                          a.ctypes.data_as(C.POINTER(C.c_double)), int(accepted)))
 
     def stats(self, iguest: int = 1):
-        out = (C.c_double * 23)()
+        out = (C.c_double * 25)()
         self.lib.orc_stats(self._h, iguest, out)
         return list(out[:])
 

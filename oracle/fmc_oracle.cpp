@@ -417,7 +417,7 @@ struct Sim {
   double rotangle = PI / 3.0, rota_rotangle = PI / 3.0;
   std::vector<long long> ins_count, accept_ins, del_count, accept_del,
       disp_count, accept_disp, tran_count, accept_tran, rota_count,
-      accept_rota;
+      accept_rota, jump_count, accept_jump;
   // statistics
   bool production = false;
   long long gcmccount = 0, prodcount = 0, rollcount = 0, cycle_step = 0;
@@ -494,6 +494,7 @@ struct Sim {
   void mc_insert(int iguest, orc_move_log *lg);
   void mc_delete(int iguest, orc_move_log *lg);
   void mc_displace(int iguest, bool tran, bool rota, orc_move_log *lg);
+  void mc_jump(int iguest, orc_move_log *lg);
   void step(orc_move_log *lg);
   int insert_guests(int iguest, int nguests);
   void production_stats(bool accepted);
@@ -1933,7 +1934,7 @@ void Sim::read_all(const std::string &dir) {
   int ng = ntpguest + 1;
   ins_count.assign(ng, 0);
   accept_ins = del_count = accept_del = disp_count = accept_disp = tran_count =
-      accept_tran = rota_count = accept_rota = ins_count;
+      accept_tran = rota_count = accept_rota = jump_count = accept_jump = ins_count;
   condense();  // gcmc.f:515-516
   beta = 1.0 / (KBOLTZ * temp);
   epsq = 1.0;
@@ -2689,6 +2690,78 @@ void Sim::mc_displace(int iguest, bool tran, bool rota, orc_move_log *lg) {
   if (lg) lg->accepted = accepted;
 }
 
+// mc_jump (gcmc.f:1937-2039): a random molecule moved to a random point of
+// the cell (random_jump, utility_pack.f:3359-3380) with a random
+// orientation (random_rot with angle 2 pi), written as the translation
+// a,b,c = new centre - old centre of mass for displace_guest.
+void Sim::mc_jump(int iguest, orc_move_log *lg) {
+  int m0 = locguest[iguest];
+  int nmol = mol[m0].nummols;
+  int natms = mol[m0].natoms;
+  jump_count[iguest]++;
+  int randchoice = (int)std::floor(rng.next() * nmol) + 1;
+  for (int ik = 1; ik <= newld; ++ik) {
+    ckc(ckcsorig, m0, ik) = ckc(ckcsum, m0, ik);
+    ckc(ckssorig, m0, ik) = ckc(ckssum, m0, ik);
+    ckc(ckcsorig, maxmls + 1, ik) = ckc(ckcsum, maxmls + 1, ik);
+    ckc(ckssorig, maxmls + 1, ik) = ckc(ckssum, maxmls + 1, ik);
+  }
+  int molt = 0, na = 0, nm = 0;
+  get_guest(iguest, randchoice, molt, na, nm);
+  double comx, comy, comz;
+  com(natms, m0, comx, comy, comz);
+  double randa = rng.next(), randb = rng.next(), randc = rng.next();  // random_jump
+  double xc, yc, zc;
+  cartesian(randa, randb, randc, xc, yc, zc);
+  const double jumpangle = 8.0 * std::atan(1.0);
+  double q1, q2, q3, q4;
+  random_rot(jumpangle, q1, q2, q3, q4);
+  const double a = xc - comx, b = yc - comy, c = zc - comz;
+  bool linitsurf = false, lnewsurf = false, loverlap = false;
+  double estep = 0.0;
+  displace_guest(iguest, randchoice, a, b, c, q1, q2, q3, q4, linitsurf, lnewsurf, loverlap, estep);
+  bool accepted = false;
+  double rande = -1.0;
+  if (!loverlap) {
+    if (estep < 0.0) {
+      accepted = true;
+    } else {
+      rande = rng.next();
+      accepted = energy_eval(estep, rande, iguest, true, false, false);
+    }
+  }
+  fill_log_xyz(*this, natms, lg);
+  if (lg) {
+    lg->move = 6;
+    lg->choice = randchoice;
+    lg->overlap = loverlap;
+    lg->estep = estep;
+    lg->rande = rande;
+    lg->dele_other = sum_other_dele(*this, m0);
+  }
+  if (accepted) {
+    accept_jump[iguest]++;
+    int rc = randchoice;
+    accept_move(iguest, false, false, true, lnewsurf, 0.0, rc, 0.0, 0.0);
+    if (linitsurf && !lnewsurf) {
+      surfacemols[m0] -= 1;
+      if (surfacemols[m0] < 0) surfacemols[m0] = 0;
+    } else if (!linitsurf && lnewsurf) {
+      surfacemols[m0] += 1;
+    }
+  } else {
+    for (int ik = 1; ik <= newld; ++ik) {
+      ckc(ckcsum, m0, ik) = ckc(ckcsorig, m0, ik);
+      ckc(ckssum, m0, ik) = ckc(ckssorig, m0, ik);
+      ckc(ckcsum, maxmls + 1, ik) = ckc(ckcsorig, maxmls + 1, ik);
+      ckc(ckssum, maxmls + 1, ik) = ckc(ckssorig, maxmls + 1, ik);
+    }
+    reject_move(iguest, false, false, true);
+  }
+  production_stats(accepted);
+  if (lg) lg->accepted = accepted;
+}
+
 double calc_qst(double E, double N, double N2, double EN, double temp) {
   double q = 0.0, denom = N2 - N * N;
   if (std::fabs(denom) > 0.0) q = -1.0 * (EN - E * N) / denom + RGAS * temp;
@@ -2759,11 +2832,11 @@ void Sim::step(orc_move_log *lg) {
   int m0 = locguest[iguest];
   int nmols = mol[m0].nummols;
   double randmov = rng.next();
-  bool insert = false, del = false, disp = false, tran = false, rota = false;
+  bool insert = false, del = false, disp = false, tran = false, rota = false, jump = false;
   if (randmov < mcinsf[iguest]) insert = true;
   else if (randmov < mcdelf[iguest]) del = true;
   else if (randmov < mcdisf[iguest]) disp = true;
-  else if (randmov < mcjmpf[iguest]) fail("oracle: jump moves are not restated");
+  else if (randmov < mcjmpf[iguest]) jump = true;
   else if (randmov < mcswpf[iguest]) fail("oracle: swap moves are not restated");
   else if (randmov < mctraf[iguest]) { disp = true; tran = true; }
   else if (randmov < mcrotf[iguest]) { disp = true; rota = true; }
@@ -2800,7 +2873,7 @@ void Sim::step(orc_move_log *lg) {
   }
   if (nmols == 0) {
     insert = true;
-    del = disp = tran = rota = false;
+    del = disp = tran = rota = jump = false;
   }
   if (lg) {
     std::memset(lg, 0, sizeof(*lg));
@@ -2810,6 +2883,8 @@ void Sim::step(orc_move_log *lg) {
     mc_insert(iguest, lg);
   else if (del)
     mc_delete(iguest, lg);
+  else if (jump)
+    mc_jump(iguest, lg);
   else
     mc_displace(iguest, tran, rota, lg);
   if (lg) lg->nmols_after = mol[m0].nummols;
@@ -3088,6 +3163,8 @@ void orc_stats(const orc_sim *h, int ig, double *out) {
   out[20] = s.delrdisp[ig];
   out[21] = s.rotangle;
   out[22] = s.rota_rotangle;
+  out[23] = (double)s.jump_count[ig];
+  out[24] = (double)s.accept_jump[ig];
 }
 
 void orc_duni_sequence(long long seed, int n, double *out) {

@@ -118,7 +118,8 @@ int orc_apply_move(orc_sim *s, int kind, int iguest, int choice,
  * out[10..13] = ins_count, accept_ins, del_count, accept_del,
  * out[14..17] = disp_count, accept_disp, rota_count, accept_rota,
  * out[18..19] = tran_count, accept_tran,
- * out[20..22] = delrdisp, rotangle, rota_rotangle. */
+ * out[20..22] = delrdisp, rotangle, rota_rotangle,
+ * out[23..24] = jump_count, accept_jump. */
 void orc_stats(const orc_sim *s, int iguest, double *out);
 
 /* MZT generator alone (for RNG parity tests): seed like orc_seed on a

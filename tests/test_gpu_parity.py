@@ -184,3 +184,72 @@ def test_gpu_batch_chains_independent(fmc_lib, small):
         assert st.nummols == multi[i].nummols
         assert st.energy == multi[i].energy
         assert list(st.accepts) == list(multi[i].accepts)
+
+
+def _jump_dir(inputs_dir):
+    """Jump-heavy moves (gcmc.f:1937-2039) with no deletions and a 1.0 A
+    overlap distance, so that some jumps land free and are accepted."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=20,
+                               move_mix=(("insert", 0.1), ("displace", 0.3), ("jump", 0.6)))
+    spec.overlap = 1.0
+    return inputs_dir(spec, "gpu_jump")
+
+
+def test_gpu_chain_fp64_jump_matches_oracle(fmc_lib, oracle_lib, inputs_dir):
+    """Jump moves in an FP64 device chain follow the oracle move by move."""
+    d = _jump_dir(inputs_dir)
+    n = 600
+    o, ref = _oracle_chain(oracle_lib, d, 9, 20, n)
+    sysm = fmc_lib.System.load(d)
+    b = fmc_lib.Batch([sysm], [{"seed": 9}], precision=fmc_lib.FMC_PREC_FP64, guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.choice, g.overlap, g.accepted) == (r.move, r.choice, r.overlap, r.accepted), i
+        assert g.rande == r.rande, i
+        if not r.overlap:
+            assert close(g.estep, r.estep, scale=1e-6), (i, g.estep, r.estep)
+    jumps = [r for r in ref if r.move == 6]
+    assert len(jumps) > 100 and sum(r.accepted for r in jumps) >= 5
+    st = b.stats()[0]
+    ostats = o.stats(1)
+    assert st.attempts[5] == ostats[23] and st.accepts[5] == ostats[24]
+    mol = o.locguest(1)
+    assert close(st.energy, o.energy(mol), rel=1e-9, scale=max(abs(r.estep) for r in ref))
+    x, nm = b.coords(0)
+    assert np.allclose(x[:9 * nm].reshape(-1, 3), o.coords(mol), rtol=0, atol=1e-9)
+
+
+def test_gpu_chain_fp32_jump(fmc_lib, oracle_lib, inputs_dir):
+    """Jump moves built in FP32 hi/lo geometry on the device: same moves as
+    the oracle until the first decision at the Metropolis threshold, with
+    estep within 1e-6 of the larger of |estep| and the jumping molecule's
+    energy before the move (the oracle's deletion energy of that molecule)."""
+    d = _jump_dir(inputs_dir)
+    n = 600
+    _, ref = _oracle_chain(oracle_lib, d, 9, 20, n)
+    o = oracle_lib.Oracle(d)
+    o.seed(9)
+    o.create_molecules(1, 20)
+    e_old = []
+    for r in ref:
+        e_old.append(o.deletion_energy(1, r.choice)["estep"] if r.move in (3, 6) else 0.0)
+        step = o.run(1)[0]
+        assert (step.move, step.choice, step.accepted) == (r.move, r.choice, r.accepted)
+    sysm = fmc_lib.System.load(d)
+    b = fmc_lib.Batch([sysm], [{"seed": 9}], precision=fmc_lib.FMC_PREC_FP32, guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    njump = 0
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.choice) == (r.move, r.choice), i
+        if g.overlap != r.overlap or g.accepted != r.accepted:
+            break  # a threshold decision; the chains part here
+        if r.overlap:
+            continue
+        assert abs(g.estep - r.estep) <= 1e-6 * max(abs(r.estep), abs(e_old[i]), 1.0), \
+            (i, g.estep, r.estep, e_old[i])
+        njump += r.move == 6
+    assert njump >= 20

@@ -65,13 +65,13 @@ def test_config_errors_are_reported(fmc_lib, tmp_path):
     with pytest.raises(L.FmcError) as e:
         fmc_lib.System.load(str(tmp_path / "missing"))
     assert e.value.code == 4
-    d = tmp_path / "jump"
+    d = tmp_path / "swap"
     spec = syn.small_test_spec()
-    spec.move_mix = (("insert", 0.5), ("jump", 0.5))
+    spec.move_mix = (("insert", 0.5), ("swap", 0.5))
     syn.write_inputs(str(d), spec)
     with pytest.raises(L.FmcError) as e:
         fmc_lib.System.load(str(d))
-    assert "jump" in str(e.value)
+    assert "swap" in str(e.value)
 
 
 def test_synthetic_framework_properties():

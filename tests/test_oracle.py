@@ -101,3 +101,44 @@ def test_move_mix_and_counts(oracle_lib, small_dir):
     assert st[11] == sum(1 for l in logs if l.move == 1 and l.accepted)
     # an overlapped insertion never draws the Metropolis number (gcmc.f:1730-1736)
     assert all(l.rande == -1.0 for l in logs if l.move == 1 and l.overlap)
+
+
+JUMP_MIX = (("insert", 0.1), ("displace", 0.3), ("jump", 0.6))
+
+
+def jump_spec():
+    """Jump-heavy moves on the small framework, no deletions (the molecules
+    stay) and a 1.0 A overlap distance, so that some jumps land free."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=20, move_mix=JUMP_MIX)
+    spec.overlap = 1.0
+    return spec
+
+
+def test_jump_moves(oracle_lib, inputs_dir):
+    """mc_jump (gcmc.f:1937-2039): counted in jump_count / accept_jump, a
+    negative estep is accepted without a Metropolis draw, and after a run of
+    jumps the running energy equals the energy of the final configuration
+    rebuilt by inserting its molecules one by one into an empty framework."""
+    d = inputs_dir(jump_spec(), "orc_jump")
+    o = oracle_lib.Oracle(d)
+    o.seed(9)
+    o.create_molecules(1, 20)
+    mol = o.locguest(1)
+    logs = o.run(600)
+    st = o.stats(1)
+    jumps = [l for l in logs if l.move == 6]
+    assert len(jumps) == st[23] and sum(l.accepted for l in jumps) == st[24]
+    assert st[24] >= 5 and sum(l.overlap for l in jumps) >= 5
+    for l in jumps:
+        if l.overlap:
+            assert not l.accepted and l.rande == -1.0
+        elif l.estep < 0:
+            assert l.accepted and l.rande == -1.0
+        else:
+            assert l.rande >= 0.0
+    xyz = o.coords(mol).reshape(-1, 3, 3)
+    assert len(xyz) == 20
+    f = oracle_lib.Oracle(d)
+    for m in xyz:
+        f.apply_move(1, 1, 0, m, True)
+    assert math.isclose(o.energy(mol), f.energy(mol), rel_tol=1e-12)
