@@ -44,6 +44,8 @@ constexpr int kStNonFinite = 8;    // non-finite energy
 constexpr int kStBadChoice = 16;   // molecule index out of range
 constexpr int kStKmax = 32;        // kmax beyond the shared tables
 constexpr int kStWait = 64;        // a bounded wait on an asynchronous copy ran out
+constexpr int kStDraws = 128;      // generator buffer empty (internal error)
+constexpr int kRBuf = 64;          // generator outputs drawn ahead per chain
 
 constexpr double kPi = 3.141592653589793;
 constexpr double kSqrPi = 1.7724538509055159;
@@ -193,6 +195,11 @@ struct ChainHdr {
   float sh_disp[kMaxG][2];  // 0.5 * delrdisp
   float sh_tran[kMaxG][2];  // 0.5 * tran_delr
   float rho_rot[2][2];      // rotangle / (2 pi), rota_rotangle / (2 pi)
+  // generator outputs drawn ahead (refill_draws), consumed in order
+  float rbuf[kRBuf];
+  int rhead, ravail;
+  // disp_count, tran_count, rota_count modulo 100 (the adaptive-step tests)
+  int disp_mod[kMaxG], tran_mod[kMaxG], rota_mod[kMaxG];
 };
 
 __host__ __device__ inline void split_pair(double x, float *out) {
@@ -419,6 +426,55 @@ __device__ __forceinline__ float duni_f(ChainHdr &h) {
   uni = uni - h.c;
   if (uni < 0.0f) uni = uni + 1.0f;
   return uni;
+}
+
+// The same generator run ahead by one warp: 32 consecutive outputs per
+// call, one per lane, appended to the chain's buffer.  duni's state update
+// is x_t = x_{t-97} - x_{t-33} (mod 1) on u[] and c_t = c_{t-1} - cd
+// (mod cm); within 32 steps a lane reads u[] entries no other lane writes
+// (the read of step t at offset 33 lies before the batch, the writes of the
+// batch are its own positions), and c after k steps is (c - k cd) mod cm in
+// exact units of 2^-24.  Outputs are bit-identical to 32 calls of duni_f.
+__device__ __forceinline__ void refill_draws(ChainHdr &h) {
+  const int lane = threadIdx.x & 31;
+  const int ir0 = h.ir, jr0 = h.jr;
+  int ir = ir0 - 1 - lane, jr = jr0 - 1 - lane;
+  if (ir < 0) ir += 97;
+  if (jr < 0) jr += 97;
+  float uni = h.u[ir] - h.u[jr];
+  if (uni < 0.0f) uni += 1.0f;
+  const int C0 = (int)(h.c * 16777216.0f), CD = (int)(h.cd * 16777216.0f),
+            CM = (int)(h.cm * 16777216.0f);
+  int ci = (C0 - (lane + 1) * CD) % CM;
+  if (ci < 0) ci += CM;
+  const float c = (float)ci * (1.0f / 16777216.0f);
+  float out = uni - c;
+  if (out < 0.0f) out += 1.0f;
+  const int pos = (h.rhead + h.ravail + lane) & (kRBuf - 1);
+  __syncwarp();
+  h.u[ir] = uni;
+  h.rbuf[pos] = out;
+  __syncwarp();
+  if (lane == 31) h.c = c;
+  if (lane == 0) {
+    h.ir = ir0 - 32 > 0 ? ir0 - 32 : ir0 - 32 + 97;
+    h.jr = jr0 - 32 > 0 ? jr0 - 32 : jr0 - 32 + 97;
+    h.ravail += 32;
+  }
+  __syncwarp();
+}
+
+// Next generator output (lane 0 of warp 0; the buffer holds at least one
+// move's draws, refilled at the start of every proposal).
+__device__ __forceinline__ float draw_f(ChainHdr &h) {
+  if (h.ravail <= 0) {
+    h.status |= kStDraws;
+    return 0.5f;
+  }
+  const float v = h.rbuf[h.rhead];
+  h.rhead = (h.rhead + 1) & (kRBuf - 1);
+  --h.ravail;
+  return v;
 }
 
 // floor(u * n) + 1 for a generator value u (a multiple of 2^-24), exactly

@@ -23,6 +23,9 @@
 
 namespace fmcdev {
 
+// Near molecules one CTA lists per evaluated position (resident guests).
+constexpr int kGList = 2 * kThreads;
+
 template <bool F32>
 struct EvalSmem {
   double p64[2][kMaxS][3];
@@ -42,6 +45,9 @@ struct EvalSmem {
   int seg_pref[kMaxSeg + 1];
   int seg_shift[kMaxSeg];
   int nslots;
+  // FP32 path, resident guests: molecules near the evaluated position
+  int glist[F32 ? kGList : 1];
+  int gcount;
   int rank, csize;          // this CTA's place in the chain's cluster
   int red_i[kWarps + 1];
   double red[kWarps * 32];

@@ -736,7 +736,7 @@ struct Chains {
         std::snprintf(buf, sizeof buf,
                       "chain %d raised device status 0x%x (1 table range, 2 segment overflow, "
                       "4 capacity, 8 non-finite, 16 bad molecule index, 32 kmax, "
-                      "64 copy wait timed out)",
+                      "64 copy wait timed out, 128 generator buffer empty)",
                       c, host_hdr[c].status);
         raise(FMC_ERR_DEVICE, buf);
       }

@@ -157,10 +157,10 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
     if (!H.production && S.eqsteps > 0 && H.gcmccount >= S.eqsteps) H.production = 1;
   }
   int g = 0;
-  if (S.ntpguest > 1) g = pick1(duni_f(H), S.ntpguest) - 1;
+  if (S.ntpguest > 1) g = pick1(draw_f(H), S.ntpguest) - 1;
   const GuestType &G = S.g[g];
   int nmols = H.nummols[g];
-  float randmov = duni_f(H);
+  float randmov = draw_f(H);
   int kind;
   if (randmov < G.mcinsf) kind = 1;
   else if (randmov < G.mcdelf) kind = 2;
@@ -173,25 +173,25 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   // adaptive step sizes (gcmc.f:859-900)
   bool upd = false;
   if (nmols >= 1 && H.disp_count[g] >= 1) {
-    if (H.disp_count[g] % 100 == 0) {
+    if (H.disp_mod[g] == 0) {  // disp_count % 100 == 0
       upd = true;
       double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
       if (ratio > G.disp_ratio) H.delrdisp[g] *= 1.05;
       else if (H.delrdisp[g] > kDelrMin) H.delrdisp[g] *= 0.95;
-    } else if (H.disp_count[g] % 50 == 0) {
+    } else if (H.disp_mod[g] == 50) {  // disp_count % 50 == 0
       upd = true;
       double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
       if (ratio > G.disp_ratio) H.rotangle *= 1.05;
       else if (H.rotangle > kMinAngle) H.rotangle *= 0.95;
     }
   }
-  if (nmols >= 1 && H.tran_count[g] >= 1 && H.tran_count[g] % 100 == 0) {
+  if (nmols >= 1 && H.tran_count[g] >= 1 && H.tran_mod[g] == 0) {
     upd = true;
     double ratio = double(H.accept_tran[g]) / double(H.tran_count[g]);
     if (ratio > G.tran_ratio) H.tran_delr[g] *= 1.05;
     else if (H.tran_delr[g] > kDelrMin) H.tran_delr[g] *= 0.95;
   }
-  if (nmols >= 1 && H.rota_count[g] >= 1 && H.rota_count[g] % 100 == 0) {
+  if (nmols >= 1 && H.rota_count[g] >= 1 && H.rota_mod[g] == 0) {
     upd = true;
     double ratio = double(H.accept_rota[g]) / double(H.rota_count[g]);
     if (ratio > G.rota_ratio) H.rota_rotangle *= 1.05;
@@ -207,16 +207,16 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   mc.npos = 1;
   if (kind == 1) {
     H.ins_count[g]++;
-    for (int i = 0; i < 7; ++i) B.draws[i] = duni_f(H);  // random_ins
+    for (int i = 0; i < 7; ++i) B.draws[i] = draw_f(H);  // random_ins
   } else if (kind == 2) {
     H.del_count[g]++;
-    mc.choice = pick1(duni_f(H), nmols);
+    mc.choice = pick1(draw_f(H), nmols);
   } else if (kind == 6) {
     // mc_jump (gcmc.f:1937-2039): the molecule, then random_jump's point
     // (utility_pack.f:3359-3380) and random_rot with angle 2 pi
     H.jump_count[g]++;
-    mc.choice = pick1(duni_f(H), nmols);
-    for (int i = 0; i < 7; ++i) B.draws[i] = duni_f(H);
+    mc.choice = pick1(draw_f(H), nmols);
+    for (int i = 0; i < 7; ++i) B.draws[i] = draw_f(H);
     if constexpr (!F32) B.geo[7] = 2.0 * kPi;
     B.flags[2] = 0;
     mc.npos = 2;
@@ -225,20 +225,20 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
     B.draws[3] = -1.0f;  // no rotation unless drawn
     if (kind != 5) {     // random_disp (utility_pack.f:3333-3357)
       if constexpr (F32) {  // the draws; the shift is built by the geometry
-        for (int i = 0; i < 3; ++i) B.draws[i] = duni_f(H);
+        for (int i = 0; i < 3; ++i) B.draws[i] = draw_f(H);
         const float *hp = kind == 4 ? H.sh_tran[g] : H.sh_disp[g];
         B.stepf[0] = hp[0];
         B.stepf[1] = hp[1];
       } else {
         double dd = kind == 4 ? H.tran_delr[g] : H.delrdisp[g];
         double h = dd * 0.5;
-        a = (2.0 * (double)duni_f(H) - 1.0) * h;
-        b = (2.0 * (double)duni_f(H) - 1.0) * h;
-        c = (2.0 * (double)duni_f(H) - 1.0) * h;
+        a = (2.0 * (double)draw_f(H) - 1.0) * h;
+        b = (2.0 * (double)draw_f(H) - 1.0) * h;
+        c = (2.0 * (double)draw_f(H) - 1.0) * h;
       }
     }
     if (kind != 4) {  // random_rot (utility_pack.f:3526-3563)
-      for (int i = 3; i < 7; ++i) B.draws[i] = duni_f(H);
+      for (int i = 3; i < 7; ++i) B.draws[i] = draw_f(H);
       if constexpr (F32) {
         const float *rp = H.rho_rot[kind == 5 ? 1 : 0];
         B.stepf[2] = rp[0];
@@ -255,13 +255,20 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
       B.draws[3] = 1.0f;
       B.flags[2] = 1;
     }
-    if (kind == 4) H.tran_count[g]++;
-    else if (kind == 5) H.rota_count[g]++;
-    else H.disp_count[g]++;
+    if (kind == 4) {
+      H.tran_count[g]++;
+      if (++H.tran_mod[g] == 100) H.tran_mod[g] = 0;
+    } else if (kind == 5) {
+      H.rota_count[g]++;
+      if (++H.rota_mod[g] == 100) H.rota_mod[g] = 0;
+    } else {
+      H.disp_count[g]++;
+      if (++H.disp_mod[g] == 100) H.disp_mod[g] = 0;
+    }
     B.geo[0] = a;
     B.geo[1] = b;
     B.geo[2] = c;
-    mc.choice = pick1(duni_f(H), nmols);
+    mc.choice = pick1(draw_f(H), nmols);
     mc.npos = 2;
   }
 }
@@ -683,6 +690,8 @@ __device__ __noinline__ void refine_geometry(BlockShared<F32> &B, const ChainArr
 template <bool F32>
 __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, int mode, int g_forced) {
   if (threadIdx.x < 32) {
+    // at least 16 draws in the buffer: a move takes at most 11
+    if (mode != kPropExternal && B.H.ravail < 16) refill_draws(B.H);
     if (threadIdx.x == 0) {
       MoveCtx &mc = B.mc;
       mc.rande = -1.0;
@@ -699,7 +708,7 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
         mc.npos = 1;
         mc.slot = -1;
         mc.choice = 0;
-        for (int i = 0; i < 7; ++i) B.draws[i] = duni_f(B.H);
+        for (int i = 0; i < 7; ++i) B.draws[i] = draw_f(B.H);
       } else {  // external: kind, g, choice, positions or a,b,c,q given in mc
         mc.ns = B.S.g[mc.g].ns;
         mc.slot = -1;
@@ -1225,6 +1234,116 @@ __device__ __forceinline__ void scan_guests_resident(BlockShared<F32> &B, int po
   }
 }
 
+// Guest sites of one guest type for the two-stage scan below: in shared
+// memory (resident, molecule i in slot i) or in global memory (slot ord[i]).
+template <bool F32>
+struct ResidentSites {
+  const BlockShared<F32> &B;
+  int ns;
+  __device__ __forceinline__ float4 hi(int i, int b) const { return B.grh[i * ns + b]; }
+  __device__ __forceinline__ float4 lo(int i, int b) const { return B.grl[i * ns + b]; }
+  __device__ __forceinline__ bool is_self(int i, int self_slot) const { return i == self_slot; }
+};
+struct GlobalSites {
+  const float4 *gh, *gl;
+  const int *ord;
+  __device__ __forceinline__ float4 hi(int i, int b) const {
+    return gh[(size_t)ord[i] * kMaxS + b];
+  }
+  __device__ __forceinline__ float4 lo(int i, int b) const {
+    return gl[(size_t)ord[i] * kMaxS + b];
+  }
+  __device__ __forceinline__ bool is_self(int i, int self_slot) const { return ord[i] == self_slot; }
+};
+
+// Guests of one type, first stage: this CTA's share of the molecules whose
+// first site lies within the cutoff plus both molecules' extents of
+// position pos, listed in a fixed order (thread, then stride) so that the
+// sums that follow do not depend on timing.  Returns false (uniformly)
+// when the share is longer than the list; the per-molecule loop then runs.
+// self_slot: the moving molecule's slot (-1 for an insertion).
+template <bool F32, class Sites>
+__device__ __forceinline__ bool list_near_guests(BlockShared<F32> &B, const Sites &gs, int pos,
+                                                 int self_slot, float rmax_self) {
+  const SysDev &S = B.S;
+  EvalSmem<F32> &sm = B.ev;
+  const GuestType &G2 = S.g[0];
+  const int n2 = B.H.nummols[0];
+  int i0, i1;
+  share_of(n2, sm.rank, sm.csize, i0, i1);
+  if (i1 - i0 > kGList) return false;
+  const float pre = (float)S.rcut + 2.0f * rmax_self + 2.0f * (float)G2.rmax + 0.01f;
+  const float pre2 = pre * pre;
+  int cnt = 0, m0 = 0, m1 = 0;
+#pragma unroll
+  for (int k = 0; k < kGList / kThreads; ++k) {
+    const int i = i0 + threadIdx.x + k * kThreads;
+    if (i < i1 && !gs.is_self(i, self_slot)) {
+      const float4 q0 = gs.hi(i, 0);
+      float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y, dz = sm.phi[pos][0][2] - q0.z;
+      dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
+      dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
+      dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+      if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= pre2) {
+        if (cnt == 0) m0 = i;
+        else m1 = i;
+        ++cnt;
+      }
+    }
+  }
+  int excl;
+  const int tot = block_scan(cnt, excl, sm.red_i);
+  if (cnt > 0) sm.glist[excl] = m0;
+  if (cnt > 1) sm.glist[excl + 1] = m1;
+  if (threadIdx.x == 0) sm.gcount = tot;
+  __syncthreads();
+  return true;
+}
+
+// Second stage: one site pair (molecule of the list, its site b, the
+// position's site k) per work item, so a near molecule's ns^2 pair terms
+// spread over ns^2 threads.  One guest type (the moving one: ns2 == ns).
+template <bool F32, int GN, int NS, class Sites>
+__device__ __forceinline__ void scan_guest_pairs(BlockShared<F32> &B, const Sites &gs, int pos,
+                                                 int ns_rt, PosAcc<F32, GN> &acc, int &ov, int &sf,
+                                                 int &st) {
+  const SysDev &S = B.S;
+  const EvalSmem<F32> &sm = B.ev;
+  const SiteInfo *si = B.si;
+  const int ns = NS > 0 ? NS : ns_rt;
+  const GuestType &G2 = S.g[0];
+  const int per = ns * ns;
+  const int nitem = sm.gcount * per;
+  for (int t = threadIdx.x; t < nitem; t += kThreads) {
+    const int j = t / per, r = t - j * per;
+    const int b = r / ns, k = r - b * ns;
+    const int i = sm.glist[j];
+    const float4 qh = gs.hi(i, b), ql = gs.lo(i, b);
+    const int tb = G2.type[b];
+    const float ex = mi_diff32(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
+                               S.boxl[0], S.rboxf[0]);
+    const float ey = mi_diff32(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
+                               S.boxl[1], S.rboxf[1]);
+    const float ez = mi_diff32(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2],
+                               S.boxl[2], S.rboxf[2]);
+    const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+    const bool near = vdw_is_near(S, si[k], tb, r2);
+    float vdw = 0.f;
+    pair_term32(S, si[k], qh.w, ql.w, tb, G2.frz[b], r2, acc.e2g[0], vdw, ov, sf, st, near);
+    if (near) {
+      float dh[3], dl[3];
+      mi_diff_df(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0], S.boxl[0],
+                 S.rboxf[0], dh[0], dl[0]);
+      mi_diff_df(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1], S.boxl[1],
+                 S.rboxf[1], dh[1], dl[1]);
+      mi_diff_df(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2], S.boxl[2],
+                 S.rboxf[2], dh[2], dl[2]);
+      acc.vdwg[0].add_df(vdw_near_df(S, si[k], tb, dh, dl, st));
+    }
+    acc.vdwg[0].add(vdw);
+  }
+}
+
 // delE(m) against every molecule type m other than the moving one, from
 // the block totals in ev.out (thread 0).  In the main loop it is needed only
 // to update energy(m) of an accepted move, so it runs after the decision.
@@ -1330,10 +1449,28 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
   int sf0 = 0, sf1 = 0, ovd = 0;
   auto scan_position = [&](int p, PosAcc<F32, GN> &A, int &sfp) {
     build_segments<F32>(S, B.ev, B.ev.cen[p], (float)S.rcut + B.ev.rmx[p] + 1e-3f, st);
+    // one guest type on the FP32 path: near molecules listed, then one
+    // site pair per work item (resident or global guests alike)
+    bool listed = false;
+    const ResidentSites<F32> rs{B, ns};
+    const GlobalSites gsites{CA.ghi + (size_t)chain * kMaxG * CA.cap * kMaxS,
+                             CA.glo + (size_t)chain * kMaxG * CA.cap * kMaxS,
+                             CA.ord + (size_t)chain * kMaxG * CA.cap};
+    if constexpr (F32 && GN == 1) {
+      if (CA.resident) listed = list_near_guests(B, rs, p, mc.slot, B.ev.rmx[p]);
+      else listed = list_near_guests(B, gsites, p, mc.slot, B.ev.rmx[p]);
+    }
     scan_framework<F32, NS>(S, B.ev, p, ns, B.si, A, ovd, sfp, st);
     bool done = false;
+    if constexpr (F32 && GN == 1) {
+      if (listed) {
+        if (CA.resident) scan_guest_pairs<F32, GN, NS>(B, rs, p, ns, A, ovd, sfp, st);
+        else scan_guest_pairs<F32, GN, NS>(B, gsites, p, ns, A, ovd, sfp, st);
+        done = true;
+      }
+    }
     if constexpr (F32) {
-      if (CA.resident) {
+      if (!done && CA.resident) {
         scan_guests_resident<F32, GN, NS>(B, p, ns, mc.slot, B.ev.rmx[p], A, ovd, sfp, st);
         done = true;
       }
@@ -1436,10 +1573,10 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
       mc.accepted = 0;
       return;
     }
-    if (draw) mc.rande = (double)duni_f(H);
+    if (draw) mc.rande = (double)draw_f(H);
     mc.accepted = energy_eval(B.S, H, mc.g, mc.estep, mc.rande, 1);
   } else if (mc.kind == 2) {
-    if (draw) mc.rande = (double)duni_f(H);
+    if (draw) mc.rande = (double)draw_f(H);
     mc.accepted = energy_eval(B.S, H, mc.g, -mc.estep, mc.rande, 2);
   } else {
     if (mc.overlap) {
@@ -1450,7 +1587,7 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
       mc.accepted = 1;
       if (draw) mc.rande = -1.0;
     } else {
-      if (draw) mc.rande = (double)duni_f(H);
+      if (draw) mc.rande = (double)draw_f(H);
       mc.accepted = energy_eval(B.S, H, mc.g, mc.estep, mc.rande, mc.kind);
     }
   }
