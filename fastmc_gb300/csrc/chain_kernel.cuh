@@ -97,6 +97,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (threadIdx.x == 0) {
     B.flags[0] = 0;
     if (ctl_fuga && mode == kModeMoves) B.H.fuga[0] = ctl_fuga[chain];  // host control block
+    if constexpr (F32) {  // log of energy_eval's prefactor, for the FP32 decisions
+      for (int g = 0; g < B.S.ntpguest; ++g) {
+        const double x = B.S.statvolm * B.H.fuga[g] / (kBoltz * B.S.temp);
+        B.H.lnpf[g] = x > 0.0 ? (float)log(x) : -INFINITY;
+      }
+    }
     B.ev.rank = rank;
     B.ev.csize = csize;
     B.xseq = B.cseq = 0u;

@@ -200,6 +200,7 @@ struct ChainHdr {
   int rhead, ravail;
   // disp_count, tran_count, rota_count modulo 100 (the adaptive-step tests)
   int disp_mod[kMaxG], tran_mod[kMaxG], rota_mod[kMaxG];
+  float lnpf[kMaxG];  // FP32 decisions: log(statvolm * fugacity / (kB T)), per launch
 };
 
 __host__ __device__ inline void split_pair(double x, float *out) {

@@ -122,8 +122,24 @@ __device__ __forceinline__ double lrc_delta(const SysDev &S, const ChainHdr &H, 
 }
 
 // energy_eval (utility_pack.f:3637-3693)
+template <bool F32>
 __device__ inline bool energy_eval(const SysDev &S, const ChainHdr &H, int g, double eng,
                             double rande, int kind) {
+  if constexpr (F32) {
+    // the same test in log space with FP32 instructions: rande < test
+    // <=> log(rande) < log(test); log(prefactor) = lnpf[g] -/+ log(N (+1))
+    // with lnpf = log(statvolm * fugacity / (kB T)) set per launch.  At the
+    // threshold the FP32 path's own estep error (~1e-7) dominates anyway.
+    const float be = (float)S.beta * (float)eng;
+    float lnt;
+    if (-be > 700.0f) lnt = 700.0f;
+    else if (be > 700.0f) lnt = -700.0f;
+    else if (kind >= 3) lnt = -be;
+    else if (kind == 1) lnt = H.lnpf[g] - logf((float)H.nummols[g] + 1.0f) - be;
+    else if (fabs(H.fuga[g]) < 1.0e-7) lnt = 0.0f;
+    else lnt = logf((float)H.nummols[g]) - H.lnpf[g] - be;
+    return logf((float)rande) < lnt;
+  }
   double ipress = H.fuga[g];
   int ing = H.nummols[g];
   double beta = S.beta, test = 0.0;
@@ -144,6 +160,34 @@ __device__ inline bool energy_eval(const SysDev &S, const ChainHdr &H, int g, do
 constexpr int kPropMC = 0;        // main loop: draw guest, move and geometry
 constexpr int kPropInsert = 1;    // create molecules: forced insertion of guest g
 constexpr int kPropExternal = 2;  // per-move ABI: move given by the host
+
+// The adaptive step-size updates of gcmc.f:859-900 for guest type g, when
+// a count sits at a multiple of 100 (50 for the rotation angle).
+template <bool F32>
+__device__ __noinline__ void adapt_steps(ChainHdr &H, const GuestType &G, int g) {
+  if (H.disp_count[g] >= 1) {
+    if (H.disp_mod[g] == 0) {  // disp_count % 100 == 0
+      double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
+      if (ratio > G.disp_ratio) H.delrdisp[g] *= 1.05;
+      else if (H.delrdisp[g] > kDelrMin) H.delrdisp[g] *= 0.95;
+    } else if (H.disp_mod[g] == 50) {  // disp_count % 50 == 0
+      double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
+      if (ratio > G.disp_ratio) H.rotangle *= 1.05;
+      else if (H.rotangle > kMinAngle) H.rotangle *= 0.95;
+    }
+  }
+  if (H.tran_count[g] >= 1 && H.tran_mod[g] == 0) {
+    double ratio = double(H.accept_tran[g]) / double(H.tran_count[g]);
+    if (ratio > G.tran_ratio) H.tran_delr[g] *= 1.05;
+    else if (H.tran_delr[g] > kDelrMin) H.tran_delr[g] *= 0.95;
+  }
+  if (H.rota_count[g] >= 1 && H.rota_mod[g] == 0) {
+    double ratio = double(H.accept_rota[g]) / double(H.rota_count[g]);
+    if (ratio > G.rota_ratio) H.rota_rotangle *= 1.05;
+    else if (H.rota_rotangle > kMinAngle) H.rota_rotangle *= 0.95;
+  }
+  if (F32) sync_step_pairs(H, g);
+}
 
 // Lane 0 of warp 0: move selection and draws (gcmc.f:806-900, 1693-1870).
 template <bool F32>
@@ -170,34 +214,12 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   else if (randmov < G.mctraf) kind = 4;
   else if (randmov < G.mcrotf) kind = 5;
   else kind = 3;
-  // adaptive step sizes (gcmc.f:859-900)
-  bool upd = false;
-  if (nmols >= 1 && H.disp_count[g] >= 1) {
-    if (H.disp_mod[g] == 0) {  // disp_count % 100 == 0
-      upd = true;
-      double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
-      if (ratio > G.disp_ratio) H.delrdisp[g] *= 1.05;
-      else if (H.delrdisp[g] > kDelrMin) H.delrdisp[g] *= 0.95;
-    } else if (H.disp_mod[g] == 50) {  // disp_count % 50 == 0
-      upd = true;
-      double ratio = double(H.accept_disp[g]) / double(H.disp_count[g]);
-      if (ratio > G.disp_ratio) H.rotangle *= 1.05;
-      else if (H.rotangle > kMinAngle) H.rotangle *= 0.95;
-    }
-  }
-  if (nmols >= 1 && H.tran_count[g] >= 1 && H.tran_mod[g] == 0) {
-    upd = true;
-    double ratio = double(H.accept_tran[g]) / double(H.tran_count[g]);
-    if (ratio > G.tran_ratio) H.tran_delr[g] *= 1.05;
-    else if (H.tran_delr[g] > kDelrMin) H.tran_delr[g] *= 0.95;
-  }
-  if (nmols >= 1 && H.rota_count[g] >= 1 && H.rota_mod[g] == 0) {
-    upd = true;
-    double ratio = double(H.accept_rota[g]) / double(H.rota_count[g]);
-    if (ratio > G.rota_ratio) H.rota_rotangle *= 1.05;
-    else if (H.rota_rotangle > kMinAngle) H.rota_rotangle *= 0.95;
-  }
-  if (F32 && upd) sync_step_pairs(H, g);
+  // adaptive step sizes (gcmc.f:859-900); the updates themselves (FP64) are
+  // out of line, the tests here are integer compares
+  if (nmols >= 1 && ((H.disp_count[g] >= 1 && (H.disp_mod[g] == 0 || H.disp_mod[g] == 50)) ||
+                     (H.tran_count[g] >= 1 && H.tran_mod[g] == 0) ||
+                     (H.rota_count[g] >= 1 && H.rota_mod[g] == 0)))
+    adapt_steps<F32>(H, G, g);
   if (nmols == 0) kind = 1;
   mc.kind = kind;
   mc.g = g;
@@ -1574,10 +1596,10 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
       return;
     }
     if (draw) mc.rande = (double)draw_f(H);
-    mc.accepted = energy_eval(B.S, H, mc.g, mc.estep, mc.rande, 1);
+    mc.accepted = energy_eval<F32>(B.S, H, mc.g, mc.estep, mc.rande, 1);
   } else if (mc.kind == 2) {
     if (draw) mc.rande = (double)draw_f(H);
-    mc.accepted = energy_eval(B.S, H, mc.g, -mc.estep, mc.rande, 2);
+    mc.accepted = energy_eval<F32>(B.S, H, mc.g, -mc.estep, mc.rande, 2);
   } else {
     if (mc.overlap) {
       mc.accepted = 0;
@@ -1588,7 +1610,7 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
       if (draw) mc.rande = -1.0;
     } else {
       if (draw) mc.rande = (double)draw_f(H);
-      mc.accepted = energy_eval(B.S, H, mc.g, mc.estep, mc.rande, mc.kind);
+      mc.accepted = energy_eval<F32>(B.S, H, mc.g, mc.estep, mc.rande, mc.kind);
     }
   }
 }
