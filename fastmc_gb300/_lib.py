@@ -120,6 +120,8 @@ SIGNATURES = {
     "fmc_widom_grid": (C.c_int, [vp, C.c_int, C.c_int, ip, C.c_int, C.c_int64, dp, i64p, dp, ip,
                                  dp]),
     "fmc_widom_positions": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, ip]),
+    "fmc_batch_prob_info": (C.c_int, [vp, C.c_int, ip, ip]),
+    "fmc_batch_prob_grid": (C.c_int, [vp, C.c_int, C.c_int, dp, C.c_int64]),
 }
 
 _lib = None

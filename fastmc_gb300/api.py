@@ -264,6 +264,23 @@ class Batch:
                                              est.ctypes.data_as(L.dp), ovl.ctypes.data_as(L.ip)))
         return est, ovl
 
+    def prob_info(self, chain: int):
+        """((na, nb, nc) voxels of the unit cell, number of probability grids)."""
+        ng = (C.c_int * 3)()
+        n = C.c_int()
+        L.check(L.load().fmc_batch_prob_info(self._h, chain, ng, C.byref(n)))
+        return tuple(ng), n.value
+
+    def prob_grid(self, chain: int):
+        """The chain's probability grids, shape (grids, na, nb, nc): sums of
+        the equitable_bin weights over the production moves so far."""
+        (na, nb, nc), n = self.prob_info(chain)
+        out = np.zeros((n, na, nb, nc))
+        for k in range(n):
+            g = out[k]
+            L.check(L.load().fmc_batch_prob_grid(self._h, chain, k, g.ctypes.data_as(L.dp), g.size))
+        return out
+
     def cycle_bytes(self):
         """(host->device, device->host) bytes of one run() call with a
         fugacity array."""

@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     B.cflag = 0u;
   }
   if (threadIdx.x < kMaxCluster) B.xflag[threadIdx.x] = 0u;
+  if (threadIdx.x == 0) B.si_g = -1;
   if constexpr (F32) {
     for (int i = threadIdx.x; i < kTrigN; i += kThreads) B.trig[i] = CA.trig[i];
   }
@@ -163,6 +164,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       __syncthreads();
+      // probability grids after every production move (gcmc.f:1129-1130)
+      if (B.S.prob_nsub > 0 && CA.grid && B.H.production) store_prob(B, CA, chain);
     }
   } else if (mode == kModeCreate) {
     for (int g = 0; g < B.S.ntpguest; ++g) {

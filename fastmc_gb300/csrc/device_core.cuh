@@ -30,6 +30,7 @@ constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxS = 8;    // sites per guest
 constexpr int kMaxG = 4;    // guest types
+constexpr int kMaxProbItems = 32;  // probability-grid (subgrid, site) items per system
 constexpr int kMaxM = 8;    // molecule types
 constexpr int kMaxT = 16;   // atom types
 constexpr int kMaxKm = 40;  // kmax per axis + 1
@@ -147,6 +148,14 @@ struct SysDev {
   const double2 *skfw;     // framework S(k)
   const float4 *skfw_df;   // framework S(k) as FP32 hi/lo pairs (re_hi, im_hi, re_lo, im_lo)
   double krecip;           // 2 * rvolm * r4pie0 / epsq
+  // probability grids (storeprob): per guest type, items (subgrid, site)
+  // binned for every molecule after each production move
+  int prob_nsub, prob_gridsize;
+  int ngrid[3];
+  double rucell[9];        // inverse of the unit (folding) cell
+  int prob_nitem[kMaxG], prob_item0[kMaxG];
+  short prob_sub[kMaxProbItems];   // 0-based subgrid
+  short prob_site[kMaxProbItems];  // 0: centre of mass, else 1-based site
   // guests
   GuestType g[kMaxG];
 };
@@ -230,6 +239,8 @@ struct ChainArrays {
   float2 *snew32;   // FP32 path: the same scratch in FP32
   float2 *sold32;
   const float4 *trig;  // [kTrigN] sin(2 pi k/kTrigN) hi, lo, cos(2 pi k/kTrigN) hi, lo
+  double *grid;        // [chain][subgrid][bin] probability grids (null: none)
+  size_t grid_stride;  // doubles per chain
   int cap;          // molecules per guest type
   int nkmax;
   int resident;     // FP32 batches of one guest type: guests held in shared memory

@@ -410,6 +410,38 @@ void build_device_system(const System &s, DevSystem &D) {
   d.akk = D.akk.p;
   d.akk32 = D.akk32.p;
   d.krecip = 2.0 * (2.0 * kPi / s.volm) * kR4pie0 / s.epsq;
+  // probability grids: (subgrid, site) items per guest type, in storeprob's
+  // order (utility_pack.f:636-685)
+  d.prob_nsub = s.lprob ? s.ntprob : 0;
+  for (int k = 0; k < 3; ++k) d.ngrid[k] = s.ngrid[k];
+  d.prob_gridsize = s.lprob ? s.ngrid[0] * s.ngrid[1] * s.ngrid[2] : 0;
+  for (int k = 0; k < 9; ++k) d.rucell[k] = s.rucell[k];
+  {
+    int nit = 0, itprob = 0;
+    for (int ig = 1; ig <= s.ntpguest; ++ig) {
+      d.prob_item0[ig - 1] = nit;
+      d.prob_nitem[ig - 1] = 0;
+      if (!s.lprob) continue;
+      int np = s.nprob[ig];
+      if (s.lprobeng[ig]) np -= 2;
+      const int natms = s.mol[s.locguest[ig]].natoms;
+      for (int ip = 1; ip <= np; ++ip) {
+        const int sub = itprob + ip;
+        if (sub > s.ntprob) raise(FMC_ERR_INPUT, "probability blocks inconsistent");
+        for (int j = 1; j <= s.nprobsites[sub]; ++j) {
+          const int site = s.lprobsites[sub][j];
+          if (site < 0 || site > natms) raise(FMC_ERR_INPUT, "probability site index out of range");
+          if (nit >= kMaxProbItems) raise(FMC_ERR_CAPACITY, "too many probability-grid sites");
+          d.prob_sub[nit] = (short)(sub - 1);
+          d.prob_site[nit] = (short)site;
+          ++nit;
+          d.prob_nitem[ig - 1]++;
+        }
+      }
+      itprob += np;
+      if (s.lprobeng[ig]) itprob += 2;
+    }
+  }
   // framework S(k) (K4)
   D.skfw.alloc(std::max(1, s.newld));
   compute_sk(a64, D, D.skfw.p);
@@ -603,7 +635,8 @@ struct Chains {
   DBuf<double2> sk, snew, sold;
   DBuf<float2> snew32, sold32;
   DBuf<float4> skdf;
-  DBuf<float4> trig;  // sin/cos(pi k / 256) hi/lo pairs
+  DBuf<float4> trig;  // sin/cos(2 pi k / kTrigN) hi/lo pairs
+  DBuf<double> grid;  // probability grids [chain][subgrid][bin]
   DBuf<MoveCtx> ctx;
   DBuf<LogRec> logs;
   DBuf<double> ctl_fuga;
@@ -822,6 +855,20 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
     FMC_CUDA(cudaMemcpy(C.trig.p, t.data(), kTrigN * sizeof(float4), cudaMemcpyHostToDevice));
   }
   CA.trig = C.trig.p;
+  {  // probability grids, when any system asks for them
+    size_t stride = 0;
+    for (int i = 0; i < nsys; ++i) {
+      const System &s = *systems[i];
+      if (s.lprob) stride = std::max(stride, (size_t)s.ntprob * s.ngrid[0] * s.ngrid[1] * s.ngrid[2]);
+    }
+    CA.grid_stride = stride;
+    CA.grid = nullptr;
+    if (stride) {
+      C.grid.alloc(stride * nchains);
+      C.grid.zero();
+      CA.grid = C.grid.p;
+    }
+  }
   CA.gpos = C.gpos.p;
   CA.ghi = C.ghi.p;
   CA.glo = C.glo.p;
@@ -1030,6 +1077,7 @@ struct ChainSnapshot {
   DBuf<float4> ghi, glo, skdf;
   DBuf<int> ord, freel;
   DBuf<double2> sk;
+  DBuf<double> grid;
 };
 
 template <class T>
@@ -1047,6 +1095,7 @@ static void save_state(Chains &C, ChainSnapshot &s) {
   copy_buf(s.ord, C.ord, C.stream);
   copy_buf(s.freel, C.freel, C.stream);
   copy_buf(s.sk, C.sk, C.stream);
+  copy_buf(s.grid, C.grid, C.stream);
   C.sync();
 }
 
@@ -1059,13 +1108,14 @@ static void restore_state(Chains &C, ChainSnapshot &s) {
   copy_buf(C.ord, s.ord, C.stream);
   copy_buf(C.freel, s.freel, C.stream);
   copy_buf(C.sk, s.sk, C.stream);
+  copy_buf(C.grid, s.grid, C.stream);
   C.sync();
   C.headers_stale = true;
 }
 
 // Checkpoint file: a header of sizes, then every chain's mutable device
 // arrays as raw bytes (state records, coordinates, order lists, S(k)).
-static const char kCkptMagic[8] = {'F', 'M', 'C', 'G', 'B', '3', '0', '1'};
+static const char kCkptMagic[8] = {'F', 'M', 'C', 'G', 'B', '3', '0', '2'};
 
 template <class T>
 static void ckpt_write(std::FILE *f, const DBuf<T> &d) {
@@ -1752,6 +1802,7 @@ int fmc_batch_save(fmc_batch *b, const char *path) {
     ckpt_write(f.get(), C.freel);
     ckpt_write(f.get(), C.sk);
     ckpt_write(f.get(), C.skdf);
+    ckpt_write(f.get(), C.grid);
     return FMC_OK;
   });
 }
@@ -1781,6 +1832,7 @@ int fmc_batch_load(fmc_batch *b, const char *path) {
     ckpt_read(f.get(), C.freel);
     ckpt_read(f.get(), C.sk);
     ckpt_read(f.get(), C.skdf);
+    ckpt_read(f.get(), C.grid);
     C.headers_stale = true;
     C.pull_headers();
     for (int c = 0; c < C.nchains; ++c)
@@ -1866,6 +1918,36 @@ int fmc_widom_grid(fmc_batch *b, int chain, int iguest, const int *ngrid, int ns
     for (int d = 0; d < 3; ++d) wj.ng[d] = ngrid[d];
     wj.seed = (unsigned long long)seed;
     run_widom(C, wj, ns, henry, counts, estep_out, overlap_out, xyz_out);
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_prob_info(fmc_batch *b, int chain, int *ngrid, int *nsub) {
+  return guard([&] {
+    if (!b || !ngrid || !nsub) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (chain < 0 || chain >= C.nchains) raise(FMC_ERR_ARG, "chain out of range");
+    C.pull_headers();
+    const System &s = *C.hsys[C.host_hdr[chain].system];
+    for (int d = 0; d < 3; ++d) ngrid[d] = s.lprob ? s.ngrid[d] : 0;
+    *nsub = s.lprob ? s.ntprob : 0;
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_prob_grid(fmc_batch *b, int chain, int sub, double *out, int64_t n) {
+  return guard([&] {
+    if (!b || !out) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (chain < 0 || chain >= C.nchains) raise(FMC_ERR_ARG, "chain out of range");
+    C.pull_headers();
+    const System &s = *C.hsys[C.host_hdr[chain].system];
+    if (!s.lprob || sub < 0 || sub >= s.ntprob) raise(FMC_ERR_ARG, "no such probability grid");
+    const int64_t gs = (int64_t)s.ngrid[0] * s.ngrid[1] * s.ngrid[2];
+    if (n < gs) raise(FMC_ERR_ARG, "output buffer too small");
+    C.sync();
+    FMC_CUDA(cudaMemcpy(out, C.grid.p + (size_t)chain * C.CA.grid_stride + (size_t)sub * gs,
+                        gs * sizeof(double), cudaMemcpyDeviceToHost));
     return FMC_OK;
   });
 }

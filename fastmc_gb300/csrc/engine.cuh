@@ -42,6 +42,7 @@ struct BlockShared {
   MoveCtx mc;
   EvalSmem<F32> ev;
   SiteInfo si[kMaxS];
+  int si_g;          // guest type si[] holds (-1: none yet)
   float draws[8];
   float stepf[4];    // FP32 path: shift half-width and half-angle / pi scale, hi/lo
   float4 trig[kTrigN];  // FP32 path: the quaternion table (copied per launch)
@@ -559,16 +560,20 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
     ev.phi[0][s][d] = ph;
     ev.plo[0][s][d] = pl;
   }
-  if (lane < ns) {
-    SiteInfo &si = B.si[lane];
-    si.q = G.q[lane];
-    si.chgea = G.chgea[lane];
-    si.chgeaf = G.chgeaf[lane];
-    si.chgeaf_lo = G.chgeaf_lo[lane];
-    si.qf = (float)G.q[lane];
-    si.type = G.type[lane];
-    si.prow = G.prow[lane];
-    si.psig2 = G.psig2[lane];
+  if (B.si_g != mc.g) {  // site constants of the moving guest type
+    if (lane < ns) {
+      SiteInfo &si = B.si[lane];
+      si.q = G.q[lane];
+      si.chgea = G.chgea[lane];
+      si.chgeaf = G.chgeaf[lane];
+      si.chgeaf_lo = G.chgeaf_lo[lane];
+      si.qf = (float)G.q[lane];
+      si.type = G.type[lane];
+      si.prow = G.prow[lane];
+      si.psig2 = G.psig2[lane];
+    }
+    __syncwarp();
+    if (lane == 0) B.si_g = mc.g;
   }
   __syncwarp();
   if (lane < mc.npos) position_bounds(B, lane);
@@ -1438,6 +1443,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       B.si[s].prow = G.prow[s];
       B.si[s].psig2 = G.psig2[s];
     }
+    if (threadIdx.x == 0) B.si_g = mc.g;
     if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * kMaxS * 3) {
       int t = threadIdx.x - 32;
       int p = t / (kMaxS * 3), s = (t / 3) % kMaxS, d = t % 3;
@@ -1922,6 +1928,157 @@ __device__ void stats(BlockShared<F32> &B) {
     }
     H.windows++;
     H.rollcount = 0;
+  }
+}
+
+// equitable_bin (utility_pack.f:2407-2519) into one subgrid with atomics:
+// val spread over the 2x2x2 voxels around a fractional point, including the
+// reference's wraps (a b-direction offset of 1 at the upper edge).
+__device__ inline void equitable_bin_dev(double *g, const int *ng, double fa, double fb,
+                                         double fc, double val) {
+  const int na = ng[0], nb = ng[1], nc = ng[2];
+  int alidx, aridx, blidx, bridx, clidx, cridx;
+  double al, ar, bl, br, cl, cr;
+  const double gpta = na * fa;
+  const int aidx = (int)ceil(gpta);
+  const double apart = gpta - floor(gpta);
+  if (apart > 0.5) {
+    if (aidx >= na) {
+      alidx = (na - 1) * nb * nc;
+      aridx = 0;
+    } else {
+      alidx = (aidx - 1) * nb * nc;
+      aridx = aidx * nb * nc;
+    }
+    al = 1.5 - apart;
+    ar = apart - 0.5;
+  } else {
+    if (aidx <= 1) {
+      alidx = (na - 1) * nb * nc;
+      aridx = 0;
+    } else {
+      alidx = (aidx - 2) * nb * nc;
+      aridx = (aidx - 1) * nb * nc;
+    }
+    al = 0.5 - apart;
+    ar = 0.5 + apart;
+  }
+  const double gptb = nb * fb;
+  const int bidx = (int)ceil(gptb);
+  const double bpart = gptb - floor(gptb);
+  if (bpart > 0.5) {
+    if (bidx >= nb) {
+      blidx = (nb - 1) * nc;
+      bridx = 1;
+    } else {
+      blidx = (bidx - 1) * nc;
+      bridx = bidx * nc;
+    }
+    bl = 1.5 - bpart;
+    br = bpart - 0.5;
+  } else {
+    if (bidx <= 1) {
+      blidx = (nb - 1) * nc;
+      bridx = 0;
+    } else {
+      blidx = (bidx - 2) * nc;
+      bridx = (bidx - 1) * nc;
+    }
+    bl = 0.5 - bpart;
+    br = 0.5 + bpart;
+  }
+  const double gptc = nc * fc;
+  const int cidx = (int)ceil(gptc);
+  const double cpart = gptc - floor(gptc);
+  if (cpart > 0.5) {
+    if (cidx >= nc) {
+      clidx = nc;
+      cridx = 1;
+    } else {
+      clidx = cidx;
+      cridx = cidx + 1;
+    }
+    cl = 1.5 - cpart;
+    cr = cpart - 0.5;
+  } else {
+    if (cidx <= 1) {
+      clidx = nc;
+      cridx = 1;
+    } else {
+      clidx = cidx - 1;
+      cridx = cidx;
+    }
+    cl = 0.5 - cpart;
+    cr = 0.5 + cpart;
+  }
+  g -= 1;  // bins are 1-based
+  atomicAdd(g + alidx + blidx + clidx, (al * bl * cl) * val);
+  atomicAdd(g + aridx + blidx + clidx, (ar * bl * cl) * val);
+  atomicAdd(g + alidx + bridx + clidx, (al * br * cl) * val);
+  atomicAdd(g + alidx + blidx + cridx, (al * bl * cr) * val);
+  atomicAdd(g + aridx + bridx + clidx, (ar * br * cl) * val);
+  atomicAdd(g + aridx + blidx + cridx, (ar * bl * cr) * val);
+  atomicAdd(g + alidx + bridx + cridx, (al * br * cr) * val);
+  atomicAdd(g + aridx + bridx + cridx, (ar * br * cr) * val);
+}
+
+// storeprob (utility_pack.f:621-687), all threads after a production move:
+// every molecule's centre of mass or listed sites, folded into the unit
+// cell, binned with weight 1.  One work item per (molecule, item); the CTAs
+// of a cluster take shares of the molecules.  FP64, as the reference (the
+// bin choice depends on the last bits of the fractional position).
+template <bool F32>
+__device__ void store_prob(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
+  const SysDev &S = B.S;
+  double *grid = CA.grid + (size_t)chain * CA.grid_stride;
+  for (int g = 0; g < S.ntpguest; ++g) {
+    const int nit = S.prob_nitem[g];
+    if (nit == 0) continue;
+    const GuestType &G = S.g[g];
+    const int n = B.H.nummols[g], ns = G.ns;
+    int i0, i1;
+    share_of(n, B.ev.rank, B.ev.csize, i0, i1);
+    const int *ord = CA.ord + ((size_t)chain * kMaxG + g) * CA.cap;
+    for (int t = threadIdx.x; t < (i1 - i0) * nit; t += kThreads) {
+      const int i = i0 + t / nit, it = S.prob_item0[g] + t % nit;
+      const int site = S.prob_site[it];
+      auto pos = [&](int sidx, int d) -> double {
+        if constexpr (F32) {
+          if (CA.resident) {
+            const float4 h = B.grh[i * ns + sidx], l = B.grl[i * ns + sidx];
+            return d == 0 ? (double)h.x + (double)l.x
+                          : (d == 1 ? (double)h.y + (double)l.y : (double)h.z + (double)l.z);
+          }
+        }
+        return CA.gpos[(gslot_base(CA, chain, g, ord[i]) + sidx) * 3 + d];
+      };
+      double px = 0.0, py = 0.0, pz = 0.0;
+      if (site == 0) {  // com (utility_pack.f:3565-3598)
+        double w = 0.0;
+        for (int k = 0; k < ns; ++k) {
+          const double m = G.mass[k];
+          w += m;
+          px += pos(k, 0) * m;
+          py += pos(k, 1) * m;
+          pz += pos(k, 2) * m;
+        }
+        px /= w;
+        py /= w;
+        pz /= w;
+      } else {
+        px = pos(site - 1, 0);
+        py = pos(site - 1, 1);
+        pz = pos(site - 1, 2);
+      }
+      const double *r = S.rucell;  // frac2 / frac: modulo 1 in the unit cell
+      double fx = px * r[0] + py * r[3] + pz * r[6];
+      double fy = px * r[1] + py * r[4] + pz * r[7];
+      double fz = px * r[2] + py * r[5] + pz * r[8];
+      fx -= floor(fx);
+      fy -= floor(fy);
+      fz -= floor(fz);
+      equitable_bin_dev(grid + (size_t)S.prob_sub[it] * S.prob_gridsize, S.ngrid, fx, fy, fz, 1.0);
+    }
   }
 }
 

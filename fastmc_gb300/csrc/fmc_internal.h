@@ -67,6 +67,17 @@ struct System {
   std::vector<float> mcinsf, mcdelf, mcdisf, mcjmpf, mcswpf, mctraf, mcrotf,
       mcswif;
   std::vector<int> guest_insert;
+  // probability grids (storeprob, gcmc.f:258-306): CONTROL "probability"
+  // blocks, "grid spacing", "grid factor"
+  bool lprob = false;
+  int ntprob = 0;
+  double griddim = 0.1;
+  int gridfactor[3] = {1, 1, 1};
+  int ngrid[3] = {0, 0, 0};
+  double ucell[9] = {0}, rucell[9] = {0};
+  std::vector<int> nprob, lprobeng;              // [iguest]
+  std::vector<int> nprobsites;                   // [1..ntprob]
+  std::vector<std::vector<int>> lprobsites;      // [1..ntprob][1..]
   // k vectors in the reference order (ewald.f:151-315)
   int newld = 0;
   std::vector<int> kl, km, kn;

@@ -303,18 +303,28 @@ void scan_inputs(const std::string &dir, System &s) {
           lower(r);
           strip_lead(r);
           if (r.c[0] == '#' || r.c[0] == ' ') continue;
-          if (has(r, "probability")) {
+          if (has(r, "probability")) {  // utility_pack.f:360-380
             int q = int_of(r), got = 0;
+            s.lprob = true;
+            s.ntprob += q;
             while (got < q) {
               f.need(r);
               strip_lead(r);
-              if (r.c[0] != '#' && r.c[0] != ' ') ++got;
+              if (r.c[0] == '#' || r.c[0] == ' ') continue;
+              if (r.c[0] == 'e') ++s.ntprob;  // energy grid: one more
+              ++got;
             }
           } else if (has(r, "&end")) {
             break;
           }
         }
       } else if (has(r, "henry")) {
+      } else if (has(r, "grid")) {  // utility_pack.f:436-443
+        if (has(r, "spa")) {
+          s.griddim = dbl_of(r);
+        } else if (has(r, "fac")) {
+          for (int d = 0; d < 3; ++d) s.gridfactor[d] = int_of(r);
+        }
       } else if (has(r, "delr")) {
         s.initdelr = dbl_of(r);
         ldelr = true;
@@ -604,7 +614,11 @@ void read_control(const std::string &dir, System &s) {
   const char *keys[8] = {"ins", "del", "dis", "jum", "swa", "swi", "tra", "rot"};
   double glob[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
   bool ltemp = false, lsteps = false, leq = false, lnumg = false;
-  int ngst = 0;
+  int ngst = 0, piprob = 0;
+  s.nprob.assign(G + 1, 0);
+  s.lprobeng.assign(G + 1, 0);
+  s.nprobsites.assign(s.ntprob + 1, 0);
+  s.lprobsites.assign(s.ntprob + 1, std::vector<int>());
   f.need(r);
   for (;;) {
     f.need(r);
@@ -624,6 +638,7 @@ void read_control(const std::string &dir, System &s) {
       ++ngst;
       int g = int_of(r);
       if (g < 1 || g > G) raise(FMC_ERR_INPUT, "&guest index out of range");
+      bool rprob = false;
       for (;;) {
         f.need(r);
         lower(r);
@@ -633,12 +648,30 @@ void read_control(const std::string &dir, System &s) {
         else if (has(r, "create molecules")) s.guest_insert[g] = int_of(r);
         else if (has(r, "min molecules") || has(r, "max molecules")) int_of(r);
         else if (has(r, "press")) s.gstpress[g] = dbl_of(r) * 1.0e5;
-        else if (has(r, "probability")) {
+        else if (has(r, "probability")) {  // readinputs.f:642-672
+          rprob = true;
+          bool leng = false;
           int q = int_of(r), got = 0;
+          s.nprob[g] = q;
           while (got < q) {
             f.need(r);
             strip_lead(r);
-            if (r.c[0] != '#' && r.c[0] != ' ') ++got;
+            if (r.c[0] == '#' || r.c[0] == ' ') continue;
+            ++got;
+            if (r.c[0] == 'e') {
+              leng = true;
+              continue;
+            }
+            ++piprob;
+            if (piprob > s.ntprob) raise(FMC_ERR_INPUT, "probability blocks inconsistent");
+            const int nsite = int_of(r);
+            s.nprobsites[piprob] = nsite;
+            s.lprobsites[piprob].assign(nsite + 1, 0);
+            for (int j = 1; j <= nsite; ++j) s.lprobsites[piprob][j] = int_of(r);
+          }
+          if (leng) {
+            s.lprobeng[g] = 1;
+            s.nprob[g] += 1;
           }
         } else if (has(r, "move")) {
           for (int q = 0; q < 8; ++q)
@@ -652,6 +685,7 @@ void read_control(const std::string &dir, System &s) {
           else if (has(r, "tra")) s.tran_ratio[g] = dbl_of(r);
         } else if (has(r, "&end")) break;
       }
+      if (!rprob) s.nprob[ngst] = 0;  // readinputs.f:706 (indexed by the block count)
     } else if (has(r, "steps")) {
       s.mcsteps = int_of(r);
       lsteps = true;
@@ -703,6 +737,20 @@ void read_control(const std::string &dir, System &s) {
 // the move-frequency normalisation (gcmc.f:341-386) in REAL*4.
 void finish_control(System &s) {
   int G = s.ntpguest;
+  // probability grid and folding cell (gcmc.f:258-306)
+  for (int i = 1; i <= 9; ++i) {
+    const int ci = (int)std::ceil(double(i) / 3.0);
+    s.ucell[i - 1] = s.cell[i - 1] / double(s.gridfactor[ci - 1]);
+  }
+  invert3(s.ucell, s.rucell);
+  if (s.lprob) {
+    for (int d = 0; d < 3; ++d) {
+      const double gd = s.celprp[d] / std::ceil(s.celprp[d] / s.gridfactor[d] / s.griddim) / s.gridfactor[d];
+      s.ngrid[d] = (int)std::ceil(s.celprp[d] / (gd * s.gridfactor[d]));
+    }
+    for (int i = 1; i <= G; ++i)
+      if (s.lprobeng[i]) raise(FMC_ERR_INPUT, "energy probability grids are not supported");
+  }
   bool lfract = false, lpress = true;
   double fsum = 0.0, nofract = 0.0;
   for (int i = 1; i <= G; ++i) {

@@ -96,6 +96,11 @@ class GcmcSpec:
                                  ("displace", 0.25), ("rotate", 0.25))
     overlap: Optional[float] = None
     title: str = "synthetic framework"
+    # probability grids: one entry per grid, the guest sites binned into it
+    # (0 = the centre of mass); grid spacing (A) and unit-cell factors
+    probability: Optional[Sequence[Sequence[int]]] = None
+    grid_spacing: Optional[float] = None
+    grid_factor: Optional[Sequence[int]] = None
 
     @property
     def box(self) -> float:
@@ -168,12 +173,20 @@ def control_text(spec: GcmcSpec) -> str:
              f"cutoff  {spec.cutoff:.6f} angstrom",
              f"delr  {spec.delr:.6f} angstrom",
              f"ewald sum {spec.alpha:.6f} {spec.kmax} {spec.kmax} {spec.kmax}"]
+    if spec.grid_spacing is not None:
+        lines.append(f"grid spacing {spec.grid_spacing:.6f}")
+    if spec.grid_factor is not None:
+        lines.append("grid factor " + " ".join(str(int(v)) for v in spec.grid_factor))
     if spec.overlap is not None:
         lines.append(f"overlap {spec.overlap:.6f}")
     lines.append("&guest 1")
     lines.append(f"  pressure (bar) {spec.pressure_bar:.9f}")
     if spec.create_molecules:
         lines.append(f"  create molecules {spec.create_molecules}")
+    if spec.probability:
+        lines.append(f"  probability {len(spec.probability)}")
+        for sites in spec.probability:
+            lines.append("  " + " ".join(str(int(v)) for v in [len(sites), *sites]))
     lines.append("&end")
     for name, f in spec.move_mix:
         lines.append(f"move {name} {f:.6f}")

@@ -281,6 +281,18 @@ int fmc_widom_grid(fmc_batch *b, int chain, int iguest, const int *ngrid, int ns
 int fmc_widom_positions(fmc_batch *b, int chain, int iguest, int npos, const double *xyz,
                         double *estep_out, int *overlap_out);
 
+/* Probability grids (storeprob, utility_pack.f:621-687; CONTROL
+ * "probability" blocks, "grid spacing", "grid factor"): after every
+ * production move each guest molecule's centre of mass or listed sites,
+ * folded into the unit cell, are spread over 2x2x2 voxels (equitable_bin,
+ * utility_pack.f:2407-2519).  ngrid = voxels along a, b, c of the unit
+ * cell; nsub = grids of the chain's system (0: none requested).
+ * fmc_batch_prob_grid copies grid `sub` (0-based) of one chain: ngrid[0] *
+ * ngrid[1] * ngrid[2] doubles, a outer, b middle, c inner, unnormalised
+ * (writeprob divides by the voxel volume and prodcount). */
+int fmc_batch_prob_info(fmc_batch *b, int chain, int *ngrid, int *nsub);
+int fmc_batch_prob_grid(fmc_batch *b, int chain, int sub, double *out, int64_t n);
+
 /* Thread-block clusters: the chains of system i run on clusters of
  * csize[i] CTAs (1..8; default 1).  Each CTA of a cluster takes a share of
  * the chain's framework atoms, guests and k-vectors; results do not depend

@@ -61,6 +61,9 @@ def load() -> C.CDLL:
             "orc_displace_energy": (i, [vp, i, i, dp, dp]),
             "orc_apply_move": (i, [vp, i, i, i, dp, i]),
             "orc_stats": (None, [vp, i, dp]),
+            "orc_prob_info": (i, [vp, C.POINTER(C.c_int)]),
+            "orc_prob_grid": (i, [vp, i, dp, i]),
+            "orc_prodcount": (C.c_longlong, [vp]),
             "orc_duni_sequence": (None, [C.c_longlong, i, dp]),
             "orc_get_erc": (i, [vp, dp, i]),
             "orc_get_vvv": (i, [vp, i, dp, i]),
@@ -183,6 +186,23 @@ class Oracle:
                                             dtype=np.float64).reshape(-1))
         self._ck(self.lib.orc_apply_move(self._h, kind, iguest, choice,
                                          a.ctypes.data_as(C.POINTER(C.c_double)), int(accepted)))
+
+    def prob_info(self):
+        """(ngrida, ngridb, ngridc, number of probability subgrids)."""
+        out = (C.c_int * 4)()
+        self.lib.orc_prob_info(self._h, out)
+        return tuple(out)
+
+    def prob_grid(self, sub: int):
+        """Probability subgrid `sub` (1-based) as an (na, nb, nc) array."""
+        import numpy as np
+        na, nb, nc, _ = self.prob_info()
+        out = np.zeros(na * nb * nc)
+        self._ck(self.lib.orc_prob_grid(self._h, sub, out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out.reshape(na, nb, nc)
+
+    def prodcount(self) -> int:
+        return self.lib.orc_prodcount(self._h)
 
     def stats(self, iguest: int = 1):
         out = (C.c_double * 25)()

@@ -356,6 +356,8 @@ struct MolType {
   std::vector<double> mx, my, mz;  // molxxx(mol, :) 1-based
 };
 
+constexpr int kMaxProbSites = 64;
+
 struct Sim {
   // ------------------------------------------------------------ inputs
   int imcon = 0, levcfg = 0;
@@ -388,6 +390,17 @@ struct Sim {
   int mcsteps = 1, eqsteps = 0, nwind = 1, nwindsteps = 1, nnumg = 1;
   int nhis = 0;
   bool lspe = false, laccsample = false;
+  // probability grids (gcmc.f:258-306, storeprob utility_pack.f:621-687)
+  double griddim = 0.1;
+  int gridfactor[3] = {1, 1, 1};
+  bool lprob = false;
+  int ntprob = 0;
+  std::vector<int> nprob, lprobeng;                 // [iguest]
+  std::vector<int> nprobsites;                      // [1..ntprob]
+  std::vector<std::vector<int>> lprobsites;         // [1..ntprob][1..]
+  int ngrida = 0, ngridb = 0, ngridc = 0, gridsize = 0;
+  double ucell[9] = {0}, rucell[9] = {0};
+  std::vector<double> grid;                         // [(sub - 1) * gridsize + bin - 1]
   double overlap = 1.5, surftol = 0.0;
   std::vector<double> gstpress, gstfuga, gstmolfract, delr;
   std::vector<float> mcinsf, mcdelf, mcdisf, mcjmpf, mcswpf, mctraf, mcrotf,
@@ -498,6 +511,9 @@ struct Sim {
   void step(orc_move_log *lg);
   int insert_guests(int iguest, int nguests);
   void production_stats(bool accepted);
+  void setup_grid();
+  void equitable_bin(double fa, double fb, double fc, int sub, double val);
+  void storeprob();
 };
 
 std::string path_join(const std::string &d, const char *f) {
@@ -604,13 +620,18 @@ void Sim::initscan(const std::string &dir) {
         lowcase(r, LENREC);
         strip(r, LENREC);
         if (r(1) == '#' || r(1) == ' ') {
-        } else if (findstring("probability", r)) {
+        } else if (findstring("probability", r)) {  // utility_pack.f:360-380
           int qprob = intstr(r);
+          lprob = true;
+          ntprob += qprob;
           int iprob = 0;
           while (iprob < qprob) {
             if (!getrec(f, r)) fail("oracle: CONTROL truncated");
             strip(r, LENREC);
             if (r(1) == '#' || r(1) == ' ') {
+            } else if (r(1) == 'e') {
+              ++ntprob;
+              ++iprob;
             } else {
               ++iprob;
             }
@@ -620,6 +641,14 @@ void Sim::initscan(const std::string &dir) {
         }
       }
     } else if (findstring("henry", r)) {
+    } else if (findstring("grid", r)) {  // utility_pack.f:436-443
+      if (findstring("spa", r)) {
+        griddim = dblstr(r);
+      } else if (findstring("fac", r)) {
+        gridfactor[0] = intstr(r);
+        gridfactor[1] = intstr(r);
+        gridfactor[2] = intstr(r);
+      }
     } else if (findstring("delr", r)) {
       initdelr = dblstr(r);
       ldelr = true;
@@ -1007,7 +1036,11 @@ void Sim::readcontrol(const std::string &dir) {
   double tmp[8] = {-1, -1, -1, -1, -1, -1, -1, -1};  // ins del dis jum swa swi tra rot
   double tmpdisp = -1, tmptran = -1, tmprota = -1;
   bool ltemp = false, lmcsteps = false, leqsteps = false, lnumg = false;
-  int ngst = 0;
+  int ngst = 0, piprob = 0;
+  nprob.assign(ntpguest + 1, 0);
+  lprobeng.assign(ntpguest + 1, 0);
+  nprobsites.assign(ntprob + 1, 0);
+  lprobsites.assign(ntprob + 1, std::vector<int>());
   getrec(f, r);
   bool loop = true;
   while (loop) {
@@ -1031,6 +1064,7 @@ void Sim::readcontrol(const std::string &dir) {
       ++ngst;
       int idg = intstr(r);
       if (idg < 1 || idg > ntpguest) fail("oracle: bad &guest index");
+      bool rprob = false;
       bool loop2 = true;
       while (loop2) {
         if (!getrec(f, r)) fail("oracle: CONTROL guest block truncated");
@@ -1047,16 +1081,35 @@ void Sim::readcontrol(const std::string &dir) {
           intstr(r);
         } else if (findstring("press", r)) {
           gstpress[idg] = dblstr(r) * 1.0e5;
-        } else if (findstring("probability", r)) {
+        } else if (findstring("probability", r)) {  // readinputs.f:642-672
+          rprob = true;
+          bool leng = false;
           int nnprob = intstr(r);
+          nprob[idg] = nnprob;
           int cprob = 0;
           while (cprob < nnprob) {
             if (!getrec(f, r)) fail("oracle: CONTROL truncated");
             strip(r, LENREC);
             if (r(1) == '#' || r(1) == ' ') {
-            } else {
+            } else if (r(1) == 'e') {
+              leng = true;
               ++cprob;
+            } else {
+              ++piprob;
+              ++cprob;
+              int ntpsite = intstr(r);
+              if ((int)nprobsites.size() <= piprob) {
+                nprobsites.resize(piprob + 1, 0);
+                lprobsites.resize(piprob + 1);
+              }
+              nprobsites[piprob] = ntpsite;
+              lprobsites[piprob].assign(ntpsite + 1, 0);
+              for (int j = 1; j <= ntpsite; ++j) lprobsites[piprob][j] = intstr(r);
             }
+          }
+          if (leng) {
+            lprobeng[idg] = 1;
+            nprob[idg] += 1;
           }
         } else if (findstring("move", r)) {
           if (findstring("ins", r)) mcinsf[idg] = (float)dblstr(r);
@@ -1076,6 +1129,7 @@ void Sim::readcontrol(const std::string &dir) {
           loop2 = false;
         }
       }
+      if (!rprob) nprob[ngst] = 0;  // readinputs.f:706 (indexed by the block count)
     } else if (findstring("steps", r)) {
       mcsteps = intstr(r);
       lmcsteps = true;
@@ -1920,11 +1974,14 @@ void Sim::read_all(const std::string &dir) {
   statvolm = volm * 1e-30;
   double det;
   invert(cell, rcell, det);
+  setup_grid();
   delr.assign(ntpguest + 1, initdelr);
   disp_ratio.assign(ntpguest + 1, 0.5);
   tran_ratio.assign(ntpguest + 1, 0.5);
   rota_ratio.assign(ntpguest + 1, 0.5);
   readcontrol(dir);
+  for (int i = 1; i <= ntpguest; ++i)
+    if (lprobeng[i]) fail("oracle: energy probability grids (storeenprob) are not restated");
   overlap = overlap * overlap;
   fugacity();
   normalise_moves();
@@ -2778,6 +2835,7 @@ double calc_cv(double E2, double E, double N, double N2, double EN, double temp)
 // production statistics (gcmc.f:1050-1128)
 void Sim::production_stats(bool accepted) {
   if (!production) return;
+  if (lprob) storeprob();  // gcmc.f:1129-1130, every production move
   if (!((laccsample && accepted) || !laccsample)) return;
   ++prodcount;
   ++rollcount;
@@ -2817,6 +2875,175 @@ void Sim::production_stats(bool accepted) {
     }
     avgwindow.push_back(w);
     rollcount = 0;
+  }
+}
+
+// Grid dimensions and the folding cell (gcmc.f:258-306): voxels of about
+// griddim per unit-cell edge, the unit cell = cell / gridfactor per vector.
+void Sim::setup_grid() {
+  for (int i = 1; i <= 9; ++i) {
+    int ci = (int)std::ceil(double(i) / 3.0);
+    ucell[i - 1] = cell[i - 1] / double(gridfactor[ci - 1]);
+  }
+  double det;
+  invert(ucell, rucell, det);
+  if (!lprob) return;
+  double gd[3];
+  int ng[3];
+  for (int d = 0; d < 3; ++d) {
+    gd[d] = celprp[d] / std::ceil(celprp[d] / gridfactor[d] / griddim) / gridfactor[d];
+    ng[d] = (int)std::ceil(celprp[d] / (gd[d] * gridfactor[d]));
+  }
+  ngrida = ng[0];
+  ngridb = ng[1];
+  ngridc = ng[2];
+  gridsize = ngrida * ngridb * ngridc;
+  grid.assign((size_t)std::max(ntprob, 1) * gridsize, 0.0);
+}
+
+// equitable_bin (utility_pack.f:2407-2519): val spread over the 2x2x2 voxels
+// around a fractional point, weights linear in the distance to the voxel
+// centres; the periodic wraps (including the b-direction offset of 1 at the
+// upper edge) as the reference has them.
+void Sim::equitable_bin(double fa, double fb, double fc, int sub, double val) {
+  const int na = ngrida, nb = ngridb, nc = ngridc;
+  int alidx, aridx, blidx, bridx, clidx, cridx;
+  double al, ar, bl, br, cl, cr;
+  double gpta = na * fa;
+  int aidx = (int)std::ceil(gpta);
+  double apart = gpta - std::floor(gpta);  // modulo(gpta, 1.d0)
+  if (apart > 0.5) {
+    if (aidx >= na) {
+      alidx = (na - 1) * nb * nc;
+      aridx = 0;
+    } else {
+      alidx = (aidx - 1) * nb * nc;
+      aridx = aidx * nb * nc;
+    }
+    al = 1.5 - apart;
+    ar = apart - 0.5;
+  } else {
+    if (aidx <= 1) {
+      alidx = (na - 1) * nb * nc;
+      aridx = 0;
+    } else {
+      alidx = (aidx - 2) * nb * nc;
+      aridx = (aidx - 1) * nb * nc;
+    }
+    al = 0.5 - apart;
+    ar = 0.5 + apart;
+  }
+  double gptb = nb * fb;
+  int bidx = (int)std::ceil(gptb);
+  double bpart = gptb - std::floor(gptb);
+  if (bpart > 0.5) {
+    if (bidx >= nb) {
+      blidx = (nb - 1) * nc;
+      bridx = 1;
+    } else {
+      blidx = (bidx - 1) * nc;
+      bridx = bidx * nc;
+    }
+    bl = 1.5 - bpart;
+    br = bpart - 0.5;
+  } else {
+    if (bidx <= 1) {
+      blidx = (nb - 1) * nc;
+      bridx = 0;
+    } else {
+      blidx = (bidx - 2) * nc;
+      bridx = (bidx - 1) * nc;
+    }
+    bl = 0.5 - bpart;
+    br = 0.5 + bpart;
+  }
+  double gptc = nc * fc;
+  int cidx = (int)std::ceil(gptc);
+  double cpart = gptc - std::floor(gptc);
+  if (cpart > 0.5) {
+    if (cidx >= nc) {
+      clidx = nc;
+      cridx = 1;
+    } else {
+      clidx = cidx;
+      cridx = cidx + 1;
+    }
+    cl = 1.5 - cpart;
+    cr = cpart - 0.5;
+  } else {
+    if (cidx <= 1) {
+      clidx = nc;
+      cridx = 1;
+    } else {
+      clidx = cidx - 1;
+      cridx = cidx;
+    }
+    cl = 0.5 - cpart;
+    cr = 0.5 + cpart;
+  }
+  double *g = grid.data() + (size_t)(sub - 1) * gridsize - 1;  // bins are 1-based
+  g[alidx + blidx + clidx] += (al * bl * cl) * val;
+  g[aridx + blidx + clidx] += (ar * bl * cl) * val;
+  g[alidx + bridx + clidx] += (al * br * cl) * val;
+  g[alidx + blidx + cridx] += (al * bl * cr) * val;
+  g[aridx + bridx + clidx] += (ar * br * cl) * val;
+  g[aridx + blidx + cridx] += (ar * bl * cr) * val;
+  g[alidx + bridx + cridx] += (al * br * cr) * val;
+  g[aridx + bridx + cridx] += (ar * br * cr) * val;
+}
+
+// storeprob (utility_pack.f:621-687): every guest molecule's centre of mass
+// or listed sites, folded into the unit cell, binned with weight 1.
+void Sim::storeprob() {
+  int itprob = 0;
+  for (int ig = 1; ig <= ntpguest; ++ig) {
+    int np = nprob[ig];
+    if (lprobeng[ig]) np -= 2;
+    int m0 = locguest[ig];
+    int nmols = mol[m0].nummols, natms = mol[m0].natoms;
+    int jj = 0;
+    for (int im = 1; im <= nmols; ++im) {
+      double x[kMaxProbSites + 1], y[kMaxProbSites + 1], z[kMaxProbSites + 1];
+      if (natms > kMaxProbSites) fail("oracle: guest too large for storeprob");
+      for (int a = 1; a <= natms; ++a) {
+        ++jj;
+        x[a] = mol[m0].mx[jj];
+        y[a] = mol[m0].my[jj];
+        z[a] = mol[m0].mz[jj];
+      }
+      double cx = 0, cy = 0, cz = 0, w = 0;
+      for (int a = 1; a <= natms; ++a) {  // com (utility_pack.f:3565-3598)
+        double mass = mol[m0].wght[a];
+        w += mass;
+        cx += x[a] * mass;
+        cy += y[a] * mass;
+        cz += z[a] * mass;
+      }
+      cx /= w;
+      cy /= w;
+      cz /= w;
+      auto fold = [&](double &px, double &py, double &pz) {  // frac2 / frac
+        const double *rc = rucell;
+        double sx = px * rc[0] + py * rc[3] + pz * rc[6];
+        double sy = px * rc[1] + py * rc[4] + pz * rc[7];
+        double sz = px * rc[2] + py * rc[5] + pz * rc[8];
+        px = sx - std::floor(sx);
+        py = sy - std::floor(sy);
+        pz = sz - std::floor(sz);
+      };
+      fold(cx, cy, cz);
+      for (int a = 1; a <= natms; ++a) fold(x[a], y[a], z[a]);
+      for (int ip = 1; ip <= np; ++ip) {
+        int sub = itprob + ip;
+        for (int i = 1; i <= nprobsites[sub]; ++i) {
+          int jatm = lprobsites[sub][i];
+          if (jatm == 0) equitable_bin(cx, cy, cz, sub, 1.0);
+          else equitable_bin(x[jatm], y[jatm], z[jatm], sub, 1.0);
+        }
+      }
+    }
+    itprob += np;
+    if (lprobeng[ig]) itprob += 2;
   }
 }
 
@@ -3138,6 +3365,27 @@ int orc_apply_move(orc_sim *h, int kind, int iguest, int choice, const double *p
     return 0;
   });
 }
+
+int orc_prob_info(const orc_sim *h, int *out4) {
+  const Sim &s = h->s;
+  out4[0] = s.ngrida;
+  out4[1] = s.ngridb;
+  out4[2] = s.ngridc;
+  out4[3] = s.lprob ? s.ntprob : 0;
+  return 0;
+}
+
+int orc_prob_grid(const orc_sim *h, int sub, double *out, int n) {
+  return guarded([&] {
+    const Sim &s = h->s;
+    if (!s.lprob || sub < 1 || sub > s.ntprob || n < s.gridsize) fail("oracle: bad probability grid request");
+    std::copy(s.grid.begin() + (size_t)(sub - 1) * s.gridsize,
+              s.grid.begin() + (size_t)sub * s.gridsize, out);
+    return 0;
+  });
+}
+
+long long orc_prodcount(const orc_sim *h) { return h->s.prodcount; }
 
 void orc_stats(const orc_sim *h, int ig, double *out) {
   const Sim &s = h->s;

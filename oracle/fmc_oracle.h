@@ -121,6 +121,12 @@ int orc_apply_move(orc_sim *s, int kind, int iguest, int choice,
  * out[20..22] = delrdisp, rotangle, rota_rotangle,
  * out[23..24] = jump_count, accept_jump. */
 void orc_stats(const orc_sim *s, int iguest, double *out);
+/* probability grids (storeprob): out4 = ngrida, ngridb, ngridc, number of
+ * subgrids (0 when none is requested); grid `sub` (1-based) as gridsize
+ * doubles, bin order a outer, b middle, c inner */
+int orc_prob_info(const orc_sim *s, int *out4);
+int orc_prob_grid(const orc_sim *s, int sub, double *out, int n);
+long long orc_prodcount(const orc_sim *s);
 
 /* MZT generator alone (for RNG parity tests): seed like orc_seed on a
  * private generator and draw n numbers (the initialising call excluded). */

@@ -142,3 +142,52 @@ def test_jump_moves(oracle_lib, inputs_dir):
     for m in xyz:
         f.apply_move(1, 1, 0, m, True)
     assert math.isclose(o.energy(mol), f.energy(mol), rel_tol=1e-12)
+
+
+def prob_spec():
+    """Jump-heavy moves with two probability grids (centre of mass; the
+    three sites) on 0.8 A voxels of the 12.8 A unit cell (grid factor 2)."""
+    spec = jump_spec()
+    spec.probability = [[0], [1, 2, 3]]
+    spec.grid_spacing = 0.8
+    spec.grid_factor = (2, 2, 2)
+    return spec
+
+
+def test_probability_grid_oracle(oracle_lib, inputs_dir):
+    """storeprob (utility_pack.f:621-687) after every production move: each
+    binned point spreads weight 1 over eight voxels, so a grid's total is
+    the number of binned points summed over the moves; the grid covers the
+    unit cell (cell / grid factor)."""
+    d = inputs_dir(prob_spec(), "orc_prob")
+    o = oracle_lib.Oracle(d)
+    o.seed(9)
+    o.create_molecules(1, 20)
+    logs = o.run(300)
+    na, nb, nc, nsub = o.prob_info()
+    assert (na, nb, nc, nsub) == (16, 16, 16, 2)
+    assert o.prodcount() == 300
+    pts = sum(l.nmols_after for l in logs)
+    g1, g2 = o.prob_grid(1), o.prob_grid(2)
+    assert math.isclose(g1.sum(), pts, rel_tol=1e-12)
+    assert math.isclose(g2.sum(), 3 * pts, rel_tol=1e-12)
+    assert g1.min() >= 0.0 and g2.min() >= 0.0
+
+
+def test_cube_writer_layout(tmp_path):
+    from fastmc_gb300.cube import fortran_e15_6, write_prob_cube
+    assert fortran_e15_6(0.0) == "   0.000000E+00"
+    assert fortran_e15_6(1.2345678) == "   0.123457E+01"
+    assert fortran_e15_6(3.0e-5) == "   0.300000E-04"
+    g = np.arange(2 * 3 * 7, dtype=float).reshape(2, 3, 7)
+    p = tmp_path / "prob.cube"
+    write_prob_cube(str(p), g, 10, [6.4, 0, 0, 0, 6.4, 0, 0, 0, 6.4], atoms=[(6, 1.0, 2.0, 3.0)])
+    lines = p.read_text().splitlines()
+    assert lines[0] == "probability cube file"
+    assert lines[2].split()[0] == "1"
+    assert int(lines[3].split()[0]) == 2 and int(lines[5].split()[0]) == 7
+    vals = [float(v) for ln in lines[7:] for v in ln.split()]
+    vol = (6.4 * 1.889725989) ** 3 / 42
+    assert np.allclose(vals, g.reshape(-1) / vol / 10, rtol=1e-5)
+    # six values per line, and a break at the end of every c row of 7
+    assert [len(ln.split()) for ln in lines[7:9]] == [6, 1]
