@@ -210,6 +210,7 @@ struct ChainHdr {
   // disp_count, tran_count, rota_count modulo 100 (the adaptive-step tests)
   int disp_mod[kMaxG], tran_mod[kMaxG], rota_mod[kMaxG];
   float lnpf[kMaxG];  // FP32 decisions: log(statvolm * fugacity / (kB T)), per launch
+  int skb[kMaxG];     // FP32 path: guest S(k) of type g is in skdf (0) or skdf2 (1)
 };
 
 __host__ __device__ inline void split_pair(double x, float *out) {
@@ -234,10 +235,10 @@ struct ChainArrays {
   int *freel;       // [chain][g][cap]
   double2 *sk;      // [chain][g][nkmax] guest S(k), FP64 path
   float4 *skdf;     // [chain][g][nkmax] guest S(k) as FP32 hi/lo pairs, FP32 path
+  float4 *skdf2;    // the second buffer: an evaluation writes the updated S(k)
+                    // there and an accepted move flips ChainHdr::skb
   double2 *snew;    // [chain][nkmax] scratch s(k) of the evaluated position
   double2 *sold;    // [chain][nkmax] scratch s(k) of the old position
-  float2 *snew32;   // FP32 path: the same scratch in FP32
-  float2 *sold32;
   const float4 *trig;  // [kTrigN] sin(2 pi k/kTrigN) hi, lo, cos(2 pi k/kTrigN) hi, lo
   double *grid;        // [chain][subgrid][bin] probability grids (null: none)
   size_t grid_stride;  // doubles per chain
@@ -802,11 +803,14 @@ __device__ __forceinline__ DF warp_total(const AccT<true> &a) {
 // out[p * kN + j] = block total of value j of position p (as a double).
 // Positions >= npos and guest types >= ng are skipped.
 template <bool F32, int GN>
-__device__ void block_reduce_pos(const PosAcc<F32, GN> &a0, const PosAcc<F32, GN> &a1, int npos,
-                                 int ng, double *scratch, double *out) {
+__device__ int block_reduce_pos(const PosAcc<F32, GN> &a0, const PosAcc<F32, GN> &a1, int npos,
+                                int ng, double *scratch, double *out, int flags, int *iscratch) {
   constexpr int N = PosAcc<F32, GN>::kN;
   static_assert(2 * N <= 32, "reduction scratch holds 32 values per warp");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // OR of the per-thread flag bits rides on the same barriers
+  const int wf = __reduce_or_sync(0xffffffffu, (unsigned)flags);
+  if (lane == 0) iscratch[w] = wf;
 #pragma unroll
   for (int i = 0; i < 2 * N; ++i) {
     const int p = i / N, j = i % N;
@@ -846,7 +850,10 @@ __device__ void block_reduce_pos(const PosAcc<F32, GN> &a0, const PosAcc<F32, GN
     }
     out[i] = tot;
   }
+  int r = 0;
+  for (int k = 0; k < kWarps; ++k) r |= iscratch[k];
   __syncthreads();
+  return r;
 }
 
 }  // namespace fmcdev

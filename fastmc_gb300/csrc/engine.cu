@@ -633,8 +633,7 @@ struct Chains {
   DBuf<float4> ghi, glo;
   DBuf<int> ord, freel;
   DBuf<double2> sk, snew, sold;
-  DBuf<float2> snew32, sold32;
-  DBuf<float4> skdf;
+  DBuf<float4> skdf, skdf2;
   DBuf<float4> trig;  // sin/cos(2 pi k / kTrigN) hi/lo pairs
   DBuf<double> grid;  // probability grids [chain][subgrid][bin]
   DBuf<MoveCtx> ctx;
@@ -753,6 +752,29 @@ struct Chains {
 
   void sync() { FMC_CUDA(cudaStreamSynchronize(stream)); }
 
+  // FP32 path: every chain's guest S(k) back into skdf (the chain kernel
+  // flips between skdf and skdf2 on accepted moves), before the host reads,
+  // resets, snapshots or saves it.
+  void normalize_sk() {
+    if (precision != FMC_PREC_FP32 || !skdf2.p) return;
+    pull_headers();
+    bool any = false;
+    for (int c = 0; c < nchains; ++c)
+      for (int g = 0; g < kMaxG; ++g)
+        if (host_hdr[c].skb[g]) {
+          const size_t o = ((size_t)c * kMaxG + g) * CA.nkmax;
+          FMC_CUDA(cudaMemcpyAsync(skdf.p + o, skdf2.p + o, CA.nkmax * sizeof(float4),
+                                   cudaMemcpyDeviceToDevice, stream));
+          host_hdr[c].skb[g] = 0;
+          any = true;
+        }
+    if (any) {
+      FMC_CUDA(cudaMemcpyAsync(hdr.p, host_hdr.data(), nchains * sizeof(ChainHdr),
+                               cudaMemcpyHostToDevice, stream));
+      sync();
+    }
+  }
+
   void pull_headers() {
     host_hdr.resize(nchains);
     FMC_CUDA(cudaMemcpyAsync(host_hdr.data(), hdr.p, nchains * sizeof(ChainHdr),
@@ -834,12 +856,12 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   C.sold.alloc((size_t)nchains * nkmax);
   C.snew.zero();
   C.sold.zero();
-  C.snew32.alloc((size_t)nchains * nkmax);
-  C.sold32.alloc((size_t)nchains * nkmax);
-  C.snew32.zero();
-  C.sold32.zero();
   C.skdf.alloc((size_t)nchains * kMaxG * nkmax);
   C.skdf.zero();
+  if (precision == FMC_PREC_FP32) {
+    C.skdf2.alloc((size_t)nchains * kMaxG * nkmax);
+    C.skdf2.zero();
+  }
   C.ctx.alloc(nchains);
   C.ctx.zero();
   C.logs.alloc(1);
@@ -878,8 +900,7 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   CA.skdf = C.skdf.p;
   CA.snew = C.snew.p;
   CA.sold = C.sold.p;
-  CA.snew32 = C.snew32.p;
-  CA.sold32 = C.sold32.p;
+  CA.skdf2 = C.skdf2.p;
   FMC_CUDA(cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking));
   FMC_CUDA(cudaEventCreate(&C.ev0));
   FMC_CUDA(cudaEventCreate(&C.ev1));
@@ -1087,6 +1108,7 @@ static void copy_buf(DBuf<T> &dst, const DBuf<T> &src, cudaStream_t st) {
 }
 
 static void save_state(Chains &C, ChainSnapshot &s) {
+  C.normalize_sk();
   copy_buf(s.hdr, C.hdr, C.stream);
   copy_buf(s.gpos, C.gpos, C.stream);
   copy_buf(s.ghi, C.ghi, C.stream);
@@ -1232,6 +1254,7 @@ int fmc_full_ewald(fmc_plain *h, double *out4) {
   return guard([&] {
     if (!h || !out4) raise(FMC_ERR_ARG, "null argument");
     Chains &C = h->C;
+    C.normalize_sk();
     const System &s = *C.hsys[0];
     const DevSystem &D = *C.sys[0];
     C.pull_headers();
@@ -1473,7 +1496,8 @@ int fmc_plain_get_coords(const fmc_plain *h, int iguest, double *xyz, int cap) {
   });
 }
 
-static int chain_sk(const Chains &C, int chain, double *out, int cap) {
+static int chain_sk(Chains &C, int chain, double *out, int cap) {
+  C.normalize_sk();
   ChainHdr hd;
   FMC_CUDA(cudaMemcpy(&hd, C.hdr.p + chain, sizeof hd, cudaMemcpyDeviceToHost));
   const System &s = *C.hsys[hd.system];
@@ -1519,7 +1543,8 @@ static int chain_sk(const Chains &C, int chain, double *out, int cap) {
 int fmc_plain_get_sk(const fmc_plain *h, double *sk, int cap) {
   return guard([&] {
     if (!h || !sk) raise(FMC_ERR_ARG, "null argument");
-    return chain_sk(h->C, 0, sk, cap);
+    // the buffer normalisation does not change what the handle holds
+    return chain_sk(const_cast<fmc_plain *>(h)->C, 0, sk, cap);
   });
 }
 
@@ -1788,6 +1813,7 @@ int fmc_batch_save(fmc_batch *b, const char *path) {
     if (!b || !path) raise(FMC_ERR_ARG, "null argument");
     Chains &C = b->C;
     C.sync();
+    C.normalize_sk();
     std::unique_ptr<std::FILE, int (*)(std::FILE *)> f(std::fopen(path, "wb"), &std::fclose);
     if (!f) raise(FMC_ERR_ARG, std::string("cannot open ") + path);
     const int meta[6] = {C.nchains, (int)C.sys.size(), C.CA.cap, C.CA.nkmax, C.precision,
@@ -2012,6 +2038,7 @@ int fmc_full_ewald_noalloc(fmc_plain *h, double *out4) {
   return guard([&] {
     if (!h || !out4) raise(FMC_ERR_ARG, "null argument");
     Chains &C = h->C;
+    C.normalize_sk();
     const System &s = *C.hsys[0];
     const DevSystem &D = *C.sys[0];
     const int nk = s.newld;

@@ -162,6 +162,15 @@ constexpr int kPropMC = 0;        // main loop: draw guest, move and geometry
 constexpr int kPropInsert = 1;    // create molecules: forced insertion of guest g
 constexpr int kPropExternal = 2;  // per-move ABI: move given by the host
 
+// Error-free update of one double-float component: (hi, lo) += x.
+__device__ __forceinline__ void df_inc(float &hi, float &lo, float x) {
+  float s, e;
+  two_sum_f(hi, x, s, e);
+  e += lo;
+  hi = s + e;
+  lo = e - (hi - s);
+}
+
 // The adaptive step-size updates of gcmc.f:859-900 for guest type g, when
 // a count sits at a multiple of 100 (50 for the rotation angle).
 template <bool F32>
@@ -1069,9 +1078,13 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
     // Two k-vectors per thread in flight.  e^{i k.r} of a site is the (l, m)
     // table entry times e^{i 2 pi n s_z} (conjugated for n < 0); without the
     // table (large kmax) it is X_l Y_m Z_n from the power tables.
-    float2 *snew32 = CA.snew32 + (size_t)chain * CA.nkmax;
-    float2 *sold32 = CA.sold32 + (size_t)chain * CA.nkmax;
-    const float4 *skg = CA.skdf + (size_t)chain * kMaxG * CA.nkmax;
+    // the guest S(k) of each type in its current buffer; the moving type's
+    // updated S(k) (as commit would form it) goes to its other buffer
+    auto skcur = [&](int g2) -> const float4 * {
+      return (B.H.skb[g2] ? CA.skdf2 : CA.skdf) + ((size_t)chain * kMaxG + g2) * CA.nkmax;
+    };
+    float4 *sknext = (B.H.skb[mc.g] ? CA.skdf : CA.skdf2) + ((size_t)chain * kMaxG + mc.g) * CA.nkmax;
+    const int kind = mc.kind;
     const int k2 = S.kmax[1], w = 2 * k2 + 1, nlm = (S.kmax[0] + 1) * w;
     const bool tab = npos * ns * nlm <= kPlmMax;
     unsigned mixmask = 0;  // guest types of another molecule type (mixing terms)
@@ -1087,20 +1100,21 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
     for (int k0 = kb + threadIdx.x; k0 < ke; k0 += U * kThreads) {
       unsigned pk[U];
       float akk[U];
-      float4 fw[U], st4[U];
+      float4 fw[U], st4[U], vg[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int k = k0 + u * kThreads;
         pk[u] = 0u;
         akk[u] = 0.f;
-        fw[u] = st4[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        fw[u] = st4[u] = vg[u] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (k < ke) {
           pk[u] = __ldg(S.kpk + k);
           akk[u] = __ldg(S.akk32 + k);
           fw[u] = __ldg(S.skfw_df + k);
           st4[u] = fw[u];
           for (int g2 = 0; g2 < NG; ++g2) {
-            const float4 v = skg[(size_t)g2 * CA.nkmax + k];
+            const float4 v = skcur(g2)[k];
+            if (g2 == mc.g) vg[u] = v;
             st4[u].x += v.x;
             st4[u].y += v.y;
             st4[u].z += v.z;
@@ -1168,13 +1182,27 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
 #pragma unroll
             for (int g2 = 0; g2 < GN; ++g2)
               if (mixmask & (1u << g2)) {
-                const float4 v = skg[(size_t)g2 * CA.nkmax + k];
+                const float4 v = skcur(g2)[k];
                 mg[p][g2] = fmaf(f2, fmaf(sp[p].x, v.x + v.z, sp[p].y * (v.y + v.w)), mg[p][g2]);
               }
           }
         }
-        snew32[k] = sp[0];
-        if (disp) sold32[k] = sp[1];
+        {  // the S(k) update of accept_move (mc_moves.f:485-622), in hi/lo
+          float4 v = vg[u];
+          if (kind == 1) {
+            df_inc(v.x, v.z, sp[0].x);
+            df_inc(v.y, v.w, sp[0].y);
+          } else if (kind == 2) {
+            df_inc(v.x, v.z, -sp[0].x);
+            df_inc(v.y, v.w, -sp[0].y);
+          } else {
+            df_inc(v.x, v.z, -sp[1].x);
+            df_inc(v.y, v.w, -sp[1].y);
+            df_inc(v.x, v.z, sp[0].x);
+            df_inc(v.y, v.w, sp[0].y);
+          }
+          sknext[k] = v;
+        }
         if (++cnt == 8) {
 #pragma unroll
           for (int p = 0; p < 2; ++p) {
@@ -1516,9 +1544,10 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
   // block totals: out[p * nper + j], j = e2fw, vdwfw, recip, mixfw,
   // e2g[GN], vdwg[GN], mixg[GN]
   constexpr int nper = PosAcc<F32, GN>::kN;
-  block_reduce_pos<F32, GN>(acc0, acc1, npos, NG, B.ev.red, B.ev.out);
-  int sfa = block_or(sf0, B.ev.red_i);
-  int sfb = block_or(sf1, B.ev.red_i);
+  const int sfl = block_reduce_pos<F32, GN>(acc0, acc1, npos, NG, B.ev.red, B.ev.out,
+                                            (sf0 ? 1 : 0) | (sf1 ? 2 : 0), B.ev.red_i);
+  int sfa = sfl & 1;
+  int sfb = (sfl >> 1) & 1;
   if (B.ev.csize > 1) {  // totals over the cluster
     if (threadIdx.x == 0) {
       B.ev.out[2 * nper] = sfa;
@@ -1621,14 +1650,6 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
   }
 }
 
-// Error-free update of one double-float component: (hi, lo) += x.
-__device__ __forceinline__ void df_inc(float &hi, float &lo, float x) {
-  float s, e;
-  two_sum_f(hi, x, s, e);
-  e += lo;
-  hi = s + e;
-  lo = e - (hi - s);
-}
 
 // FP32 path: the production sums of H.pend moves that all saw the current
 // state (the reference adds one move at a time, gcmc.f:1050-1075; here the
@@ -1685,44 +1706,8 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
       skg[k] = v;
     }
   } else {
-    float4 *skg = CA.skdf + ((size_t)chain * kMaxG + g) * CA.nkmax;
-    const float2 *snew = CA.snew32 + (size_t)chain * CA.nkmax;
-    const float2 *sold = CA.sold32 + (size_t)chain * CA.nkmax;
-    constexpr int U = 4;  // k-vectors per thread in flight
-    int kb, ke;
-    share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
-    for (int k0 = kb + threadIdx.x; k0 < ke; k0 += U * kThreads) {
-      float4 v[U];
-      float2 n[U], o[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int k = k0 + u * kThreads;
-        if (k < ke) {
-          v[u] = skg[k];
-          n[u] = snew[k];
-          o[u] = mc.kind >= 3 ? sold[k] : make_float2(0.f, 0.f);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int k = k0 + u * kThreads;
-        if (k < ke) {
-          if (mc.kind == 1) {
-            df_inc(v[u].x, v[u].z, n[u].x);
-            df_inc(v[u].y, v[u].w, n[u].y);
-          } else if (mc.kind == 2) {
-            df_inc(v[u].x, v[u].z, -n[u].x);
-            df_inc(v[u].y, v[u].w, -n[u].y);
-          } else {
-            df_inc(v[u].x, v[u].z, -o[u].x);
-            df_inc(v[u].y, v[u].w, -o[u].y);
-            df_inc(v[u].x, v[u].z, n[u].x);
-            df_inc(v[u].y, v[u].w, n[u].y);
-          }
-          skg[k] = v[u];
-        }
-      }
-    }
+    // the evaluation wrote the updated S(k) to the other buffer
+    if (threadIdx.x == 0) B.H.skb[g] ^= 1;
   }
   // molecule order and coordinates
   int *ord = CA.ord + ((size_t)chain * kMaxG + g) * CA.cap;
