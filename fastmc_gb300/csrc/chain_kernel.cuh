@@ -109,7 +109,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     B.cflag = 0u;
   }
   if (threadIdx.x < kMaxCluster) B.xflag[threadIdx.x] = 0u;
-  if (threadIdx.x == 0) B.si_g = -1;
+  if (threadIdx.x == 0) {
+    B.si_g = -1;
+    B.dfr.pending = 0;
+  }
   if constexpr (F32) {
     for (int i = threadIdx.x; i < kTrigN; i += kThreads) B.trig[i] = CA.trig[i];
   }
@@ -131,12 +134,20 @@ __global__ void __launch_bounds__(kThreads, 1)
   int st = 0;
   if (mode == kModeMoves) {
     for (int it = 0; it < nmoves; ++it) {
+      // the previous move's FP64 bookkeeping overlaps this proposal
+      if (threadIdx.x == 32) run_deferred<F32, GN>(B);
       propose(B, CA, chain, kPropMC, 0);
       int full = 0;
       if (B.mc.kind != 0) full = evaluate_any<F32, GN>(B, CA, chain, st);
       if (threadIdx.x == 0) {
         decide(B, true);
-        if (B.mc.accepted && B.flags[4]) other_mol_delE<F32, GN>(B);
+        auto &D = B.dfr;
+        D.kind = B.mc.kind;
+        D.g = B.mc.g;
+        D.npos = B.mc.npos;
+        D.accepted = B.mc.accepted;
+        D.other = B.mc.accepted && B.flags[4];  // delE of the other molecule types
+        D.booked = 0;
         if (full) B.H.evals += B.mc.npos;
         else if (B.mc.overlap) B.H.overlap_exits++;
         if (logcap > 0 && B.H.log_n < logcap && rank == 0) {
@@ -155,9 +166,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       __syncthreads();
-      commit(B, CA, chain, st);
+      commit(B, CA, chain, st, true);
       if (threadIdx.x == 0) {
-        stats(B);
+        stats(B, true);
         if (logcap > 0 && B.H.log_n < logcap) {
           if (rank == 0) logs[(size_t)chain * logcap + B.H.log_n].nmols_after = B.H.nummols[B.mc.g];
           B.H.log_n++;
@@ -165,8 +176,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       __syncthreads();
       // probability grids after every production move (gcmc.f:1129-1130)
-      if (B.S.prob_nsub > 0 && CA.grid && B.H.production) store_prob(B, CA, chain);
+      if (B.S.prob_nsub > 0 && CA.grid && B.dfr.production) store_prob(B, CA, chain);
     }
+    if (threadIdx.x == 32) run_deferred<F32, GN>(B);
+    __syncthreads();
   } else if (mode == kModeCreate) {
     for (int g = 0; g < B.S.ntpguest; ++g) {
       long long maxiter = 1000LL * B.S.g[g].insert0, iter = 0;

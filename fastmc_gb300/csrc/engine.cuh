@@ -43,6 +43,13 @@ struct BlockShared {
   EvalSmem<F32> ev;
   SiteInfo si[kMaxS];
   int si_g;          // guest type si[] holds (-1: none yet)
+  // FP64 bookkeeping of the previous move (energies, charges, production
+  // sums), done by thread 32 while warp 0 proposes the next move
+  struct Deferred {
+    int pending, kind, g, npos, accepted, booked, other, surf_new, surf_old, production, n_old;
+    double chgtmp;
+    double delE[kMaxM + 1];
+  } dfr;
   float draws[8];
   float stepf[4];    // FP32 path: shift half-width and half-angle / pi scale, hi/lo
   float4 trig[kTrigN];  // FP32 path: the quaternion table (copied per launch)
@@ -1403,17 +1410,16 @@ __device__ __forceinline__ void scan_guest_pairs(BlockShared<F32> &B, const Site
 // the block totals in ev.out (thread 0).  In the main loop it is needed only
 // to update energy(m) of an accepted move, so it runs after the decision.
 template <bool F32, int GN>
-__device__ void other_mol_delE(BlockShared<F32> &B) {
+__device__ void other_mol_delE(BlockShared<F32> &B, int kind, int g, int npos, double *delE) {
   const SysDev &S = B.S;
-  MoveCtx &mc = B.mc;
-  const GuestType &G = S.g[mc.g];
+  const GuestType &G = S.g[g];
   constexpr int nper = PosAcc<F32, GN>::kN;
   const double *R = B.ev.out;
-  const int npos = mc.npos, NG = S.ntpguest, mol = G.mol;
+  const int NG = S.ntpguest, mol = G.mol;
   const double eu = S.rengunit;
   auto pair_terms = [&](int p, int m, double delrc_m) {
     const double *r = R + p * nper;
-    bool exist = (npos == 2) ? (p == 1) : (mc.kind == 2);
+    bool exist = (npos == 2) ? (p == 1) : (kind == 2);
     double qfm = G.qfm * B.H.chgsum_mol[m];
     if (exist) qfm = -qfm;
     double e1 = 0.0, e2m = 0.0, vdm = 0.0;
@@ -1432,8 +1438,8 @@ __device__ void other_mol_delE(BlockShared<F32> &B) {
     }
     return e1 + e2m + vdm + delrc_m;
   };
-  if (mc.kind == 1 || mc.kind == 2) {
-    const bool del = mc.kind == 2;
+  if (kind == 1 || kind == 2) {
+    const bool del = kind == 2;
     for (int m = 1; m <= S.maxmls; ++m) {
       if (m == mol) continue;
       double dm = 0.0;  // delrc_mol(loc2(mol,m)), vdw_terms.f:743-761
@@ -1442,11 +1448,11 @@ __device__ void other_mol_delE(BlockShared<F32> &B) {
         for (int g2 = 0; g2 < NG; ++g2)
           if (S.g[g2].mol == m) dm = double(B.H.nummols[g2]) * G.lrcB[g2];
       const double t = pair_terms(0, m, dm) * eu;
-      mc.delE[m] = del ? -t : t;
+      delE[m] = del ? -t : t;
     }
   } else {
     for (int m = 1; m <= S.maxmls; ++m)
-      if (m != mol) mc.delE[m] = (pair_terms(0, m, 0.0) - pair_terms(1, m, 0.0)) * eu;
+      if (m != mol) delE[m] = (pair_terms(0, m, 0.0) - pair_terms(1, m, 0.0)) * eu;
   }
 }
 
@@ -1593,7 +1599,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       mc.delrc = 0.0;
       mc.delE[mol] = mc.estep;
     }
-    if (!B.flags[4]) other_mol_delE<F32, GN>(B);
+    if (!B.flags[4]) other_mol_delE<F32, GN>(B, mc.kind, mc.g, mc.npos, mc.delE);
     mc.parts[0] = ewld1[0];
     mc.parts[1] = e2[0];
     mc.parts[2] = vd[0];
@@ -1654,12 +1660,12 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
 // FP32 path: the production sums of H.pend moves that all saw the current
 // state (the reference adds one move at a time, gcmc.f:1050-1075; here the
 // run is added at once when the state changes or a window ends).
-__device__ inline void flush_stats(const SysDev &S, ChainHdr &H) {
+__device__ inline void flush_stats(const SysDev &S, ChainHdr &H, int g_old = -1, int n_old = 0) {
   if (H.pend == 0) return;
   const double n = (double)H.pend;
   for (int i = 0; i < S.ntpguest; ++i) {
     int m = S.g[i].mol;
-    double dm = double((float)H.nummols[i]);
+    double dm = double((float)(i == g_old ? n_old : H.nummols[i]));
     double e = H.energy[m];
     double sm = double((float)H.surfacemols[m]);
     H.chainstats[i][0] += n * dm;
@@ -1674,8 +1680,38 @@ __device__ inline void flush_stats(const SysDev &S, ChainHdr &H) {
 
 // ----------------------------------------------------------------- commit
 // accept_move (mc_moves.f:485-621) for the evaluated move, if accepted.
+// The FP64 state updates of accept_move (mc_moves.f:485-622) for one
+// accepted move of guest type g: production sums of the moves that saw the
+// old state (FP32 path, n_old = the type's count before the move), energies,
+// charges and the surface tally.
 template <bool F32>
-__device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, int &st) {
+__device__ inline void bookkeep(const SysDev &S, ChainHdr &H, int g, int n_old, int kind,
+                                const double *delE, double chgtmp, int surf_new, int surf_old) {
+  if constexpr (F32) flush_stats(S, H, g, n_old);  // the pending moves saw the old state
+  for (int m = 1; m <= S.maxmls; ++m) H.energy[m] += delE[m];
+  const int mol = S.g[g].mol;
+  if (kind == 1 || kind == 2) {
+    const int sg = kind == 1 ? 1 : -1;
+    H.chgsum_mol[mol] += sg * chgtmp;
+    H.sumchg += sg * chgtmp;
+    if (surf_new) H.surfacemols[mol] += sg;
+  } else {
+    // surface molecule tally of a displacement (gcmc.f:1900-1906)
+    if (surf_old && !surf_new) {
+      H.surfacemols[mol] -= 1;
+      if (H.surfacemols[mol] < 0) H.surfacemols[mol] = 0;
+    } else if (!surf_old && surf_new) {
+      H.surfacemols[mol] += 1;
+    }
+  }
+}
+
+// defer: the main loop's commit leaves bookkeep() to run_deferred (thread
+// 32, during the next proposal); the integer state the next move needs
+// (counts, slots) is updated here.
+template <bool F32>
+__device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, int &st,
+                       bool defer = false) {
   SysDev &S = B.S;
   ChainHdr &H = B.H;
   MoveCtx &mc = B.mc;
@@ -1809,14 +1845,20 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
     }
   }
   if (threadIdx.x == 0 && slot >= 0) {
-    if constexpr (F32) flush_stats(S, H);  // the pending moves saw the old state
-    for (int m = 1; m <= S.maxmls; ++m) H.energy[m] += mc.delE[m];
-    int mol = G.mol;
+    const int mol = G.mol, n_old = H.nummols[g];
+    if (defer) {
+      auto &D = B.dfr;
+      D.booked = 1;
+      D.n_old = n_old;
+      D.chgtmp = mc.chgtmp;
+      D.surf_new = mc.surf_new;
+      D.surf_old = mc.surf_old;
+      for (int m = 0; m <= S.maxmls; ++m) D.delE[m] = mc.delE[m];
+    } else {
+      bookkeep<F32>(S, H, g, n_old, mc.kind, mc.delE, mc.chgtmp, mc.surf_new, mc.surf_old);
+    }
     if (mc.kind == 1 || mc.kind == 2) {
       int sg = mc.kind == 1 ? 1 : -1;
-      H.chgsum_mol[mol] += sg * mc.chgtmp;
-      H.sumchg += sg * mc.chgtmp;
-      if (mc.surf_new) H.surfacemols[mol] += sg;
       for (int s = 0; s < G.ns; ++s) {
         int ka = G.type[s];
         H.numtyp[ka] += sg;
@@ -1830,14 +1872,6 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
       if (mc.kind == 2 && !res) {
         if (B.ev.rank == 0) freel[H.nfree[g]] = slot;
         H.nfree[g]++;
-      }
-    } else {
-      // surface molecule tally of a displacement (gcmc.f:1900-1906)
-      if (mc.surf_old && !mc.surf_new) {
-        H.surfacemols[mol] -= 1;
-        if (H.surfacemols[mol] < 0) H.surfacemols[mol] = 0;
-      } else if (!mc.surf_old && mc.surf_new) {
-        H.surfacemols[mol] += 1;
       }
     }
   }
@@ -1857,9 +1891,13 @@ __device__ inline double calc_cv(double E2, double E, double N, double N2, doubl
   return 0.0;
 }
 
-// Thread 0: acceptance counters and production statistics.
+// Thread 0: acceptance counters (the next move's step-size adaptation reads
+// them), then the production statistics, now or (defer) by run_deferred.
 template <bool F32>
-__device__ void stats(BlockShared<F32> &B) {
+__device__ void stats_production(const SysDev &S, ChainHdr &H, int production, int accepted);
+
+template <bool F32>
+__device__ void stats(BlockShared<F32> &B, bool defer = false) {
   SysDev &S = B.S;
   ChainHdr &H = B.H;
   MoveCtx &mc = B.mc;
@@ -1877,8 +1915,19 @@ __device__ void stats(BlockShared<F32> &B) {
     if (mc.accepted) H.accepts[mc.kind - 1]++;
   }
   H.moves++;
-  if (!H.production) return;
-  if (S.laccsample && !mc.accepted) return;
+  if (defer) {
+    B.dfr.production = H.production;
+    B.dfr.pending = 1;
+    return;
+  }
+  stats_production<F32>(S, H, H.production, mc.accepted);
+}
+
+// Production statistics of one move (gcmc.f:1047-1127).
+template <bool F32>
+__device__ void stats_production(const SysDev &S, ChainHdr &H, int production, int accepted) {
+  if (!production) return;
+  if (S.laccsample && !accepted) return;
   H.prodcount++;
   H.rollcount++;
   if (F32 && !S.laccsample) {
@@ -1914,6 +1963,22 @@ __device__ void stats(BlockShared<F32> &B) {
     H.windows++;
     H.rollcount = 0;
   }
+}
+
+// Thread 32: the previous move's deferred FP64 work, in the order the
+// reference does it (delE of the other molecule types, accept_move's
+// updates, the production sums).  It reads the previous evaluation's block
+// totals, which stay in ev.out until the next evaluation's reduction, and
+// touches no field the proposal reads.
+template <bool F32, int GN>
+__device__ void run_deferred(BlockShared<F32> &B) {
+  auto &D = B.dfr;
+  if (!D.pending) return;
+  if (D.other) other_mol_delE<F32, GN>(B, D.kind, D.g, D.npos, D.delE);
+  if (D.booked)
+    bookkeep<F32>(B.S, B.H, D.g, D.n_old, D.kind, D.delE, D.chgtmp, D.surf_new, D.surf_old);
+  stats_production<F32>(B.S, B.H, D.production, D.accepted);
+  D.pending = 0;
 }
 
 // equitable_bin (utility_pack.f:2407-2519) into one subgrid with atomics:
