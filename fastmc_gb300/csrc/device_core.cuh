@@ -61,6 +61,7 @@ constexpr double kDelrMin = 0.1;
 struct GuestType {
   int mol;        // molecule type (1-based)
   int ns;         // sites
+  float rns;      // 1 / ns
   int insert0;    // "create molecules"
   int pad;
   double q[kMaxS];
@@ -489,6 +490,25 @@ __device__ __forceinline__ float draw_f(ChainHdr &h) {
   --h.ravail;
   return v;
 }
+
+// Several consecutive draws with the buffer position held in registers
+// (the loads are independent); done() stores the position back.
+struct DrawCursor {
+  ChainHdr &h;
+  int head, avail;
+  __device__ __forceinline__ explicit DrawCursor(ChainHdr &hh) : h(hh), head(hh.rhead), avail(hh.ravail) {}
+  __device__ __forceinline__ float next() {
+    const float v = h.rbuf[head];
+    head = (head + 1) & (kRBuf - 1);
+    --avail;
+    return v;
+  }
+  __device__ __forceinline__ void done() {
+    if (avail < 0) h.status |= kStDraws;
+    h.rhead = head;
+    h.ravail = avail;
+  }
+};
 
 // floor(u * n) + 1 for a generator value u (a multiple of 2^-24), exactly
 // as the reference's floor(duni()*n)+1 in FP64 (gcmc.f:1782, 1870).

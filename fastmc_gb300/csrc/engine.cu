@@ -465,6 +465,7 @@ void build_device_system(const System &s, DevSystem &D) {
     const MolType &m = s.mol[s.locguest[g]];
     G.mol = s.locguest[g];
     G.ns = m.natoms;
+    G.rns = 1.0f / (float)m.natoms;
     G.insert0 = s.guest_insert[g];
     double cx = 0, cy = 0, cz = 0;
     for (int i = 0; i < m.natoms; ++i) {

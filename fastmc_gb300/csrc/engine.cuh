@@ -217,11 +217,12 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
     H.minchk_left = S.minchk;
     if (!H.production && S.eqsteps > 0 && H.gcmccount >= S.eqsteps) H.production = 1;
   }
+  DrawCursor dc(H);  // this move's draws, buffer position in registers
   int g = 0;
-  if (S.ntpguest > 1) g = pick1(draw_f(H), S.ntpguest) - 1;
+  if (S.ntpguest > 1) g = pick1(dc.next(), S.ntpguest) - 1;
   const GuestType &G = S.g[g];
   int nmols = H.nummols[g];
-  float randmov = draw_f(H);
+  float randmov = dc.next();
   int kind;
   if (randmov < G.mcinsf) kind = 1;
   else if (randmov < G.mcdelf) kind = 2;
@@ -246,16 +247,16 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   mc.npos = 1;
   if (kind == 1) {
     H.ins_count[g]++;
-    for (int i = 0; i < 7; ++i) B.draws[i] = draw_f(H);  // random_ins
+    for (int i = 0; i < 7; ++i) B.draws[i] = dc.next();  // random_ins
   } else if (kind == 2) {
     H.del_count[g]++;
-    mc.choice = pick1(draw_f(H), nmols);
+    mc.choice = pick1(dc.next(), nmols);
   } else if (kind == 6) {
     // mc_jump (gcmc.f:1937-2039): the molecule, then random_jump's point
     // (utility_pack.f:3359-3380) and random_rot with angle 2 pi
     H.jump_count[g]++;
-    mc.choice = pick1(draw_f(H), nmols);
-    for (int i = 0; i < 7; ++i) B.draws[i] = draw_f(H);
+    mc.choice = pick1(dc.next(), nmols);
+    for (int i = 0; i < 7; ++i) B.draws[i] = dc.next();
     if constexpr (!F32) B.geo[7] = 2.0 * kPi;
     B.flags[2] = 0;
     mc.npos = 2;
@@ -264,20 +265,20 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
     B.draws[3] = -1.0f;  // no rotation unless drawn
     if (kind != 5) {     // random_disp (utility_pack.f:3333-3357)
       if constexpr (F32) {  // the draws; the shift is built by the geometry
-        for (int i = 0; i < 3; ++i) B.draws[i] = draw_f(H);
+        for (int i = 0; i < 3; ++i) B.draws[i] = dc.next();
         const float *hp = kind == 4 ? H.sh_tran[g] : H.sh_disp[g];
         B.stepf[0] = hp[0];
         B.stepf[1] = hp[1];
       } else {
         double dd = kind == 4 ? H.tran_delr[g] : H.delrdisp[g];
         double h = dd * 0.5;
-        a = (2.0 * (double)draw_f(H) - 1.0) * h;
-        b = (2.0 * (double)draw_f(H) - 1.0) * h;
-        c = (2.0 * (double)draw_f(H) - 1.0) * h;
+        a = (2.0 * (double)dc.next() - 1.0) * h;
+        b = (2.0 * (double)dc.next() - 1.0) * h;
+        c = (2.0 * (double)dc.next() - 1.0) * h;
       }
     }
     if (kind != 4) {  // random_rot (utility_pack.f:3526-3563)
-      for (int i = 3; i < 7; ++i) B.draws[i] = draw_f(H);
+      for (int i = 3; i < 7; ++i) B.draws[i] = dc.next();
       if constexpr (F32) {
         const float *rp = H.rho_rot[kind == 5 ? 1 : 0];
         B.stepf[2] = rp[0];
@@ -307,9 +308,10 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
     B.geo[0] = a;
     B.geo[1] = b;
     B.geo[2] = c;
-    mc.choice = pick1(draw_f(H), nmols);
+    mc.choice = pick1(dc.next(), nmols);
     mc.npos = 2;
   }
+  dc.done();
 }
 
 // Quaternion of random_ins / random_rot from four draws and an angle:
@@ -443,21 +445,29 @@ __device__ void geometry_warp(BlockShared<F32> &B, const ChainArrays &CA, int ch
 }
 
 // Centre and bounding radius of each evaluated position from its FP32
-// coordinates (lanes p < npos of one warp).
+// coordinates; all lanes of one warp, lane 3p + d takes coordinate d of
+// position p (the radius carries a 1e-3 A margin).
 template <bool F32>
-__device__ __forceinline__ void position_bounds(BlockShared<F32> &B, int p) {
-  const int ns = B.mc.ns;
-  float c[3] = {0.f, 0.f, 0.f};
-  for (int s = 0; s < ns; ++s)
-    for (int d = 0; d < 3; ++d) c[d] += B.ev.phi[p][s][d];
-  float rn = 1.0f / ns, rm2 = 0.f;
-  for (int d = 0; d < 3; ++d) c[d] *= rn;
-  for (int s = 0; s < ns; ++s) {
-    float dx = B.ev.phi[p][s][0] - c[0], dy = B.ev.phi[p][s][1] - c[1], dz = B.ev.phi[p][s][2] - c[2];
-    rm2 = fmaxf(rm2, dx * dx + dy * dy + dz * dz);
+__device__ __forceinline__ void position_bounds(BlockShared<F32> &B, int lane) {
+  const unsigned full = 0xffffffffu;
+  const int ns = B.mc.ns, npos = B.mc.npos;
+  const int p = lane / 3, d = lane - 3 * (lane / 3);
+  const bool act = lane < 3 * npos;
+  float c = 0.f;
+  if (act) {
+    for (int s = 0; s < ns; ++s) c += B.ev.phi[p][s][d];
+    c *= B.S.g[B.mc.g].rns;
   }
-  for (int d = 0; d < 3; ++d) B.ev.cen[p][d] = c[d];
-  B.ev.rmx[p] = sqrtf(rm2) + 1e-3f;
+  float rm2 = 0.f;
+  const int b = act ? 3 * p : 0;
+  for (int s = 0; s < ns; ++s) {
+    const float dd = act ? B.ev.phi[p][s][d] - c : 0.f;
+    const float q = dd * dd;
+    const float t = __shfl_sync(full, q, b) + __shfl_sync(full, q, b + 1) + __shfl_sync(full, q, b + 2);
+    rm2 = fmaxf(rm2, t);
+  }
+  if (act) B.ev.cen[p][d] = c;
+  if (act && d == 0) B.ev.rmx[p] = sqrtf(rm2) + 1e-3f;
 }
 
 // FP32 quaternion of random_ins / random_rot: half angle pi * r * scale
@@ -592,7 +602,7 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
     if (lane == 0) B.si_g = mc.g;
   }
   __syncwarp();
-  if (lane < mc.npos) position_bounds(B, lane);
+  position_bounds(B, lane);
 }
 
 // Double-float quaternion: the half angle pi * rho, rho = r * scale (scale
@@ -751,7 +761,9 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
         mc.npos = 1;
         mc.slot = -1;
         mc.choice = 0;
-        for (int i = 0; i < 7; ++i) B.draws[i] = draw_f(B.H);
+        DrawCursor dc(B.H);
+        for (int i = 0; i < 7; ++i) B.draws[i] = dc.next();
+        dc.done();
       } else {  // external: kind, g, choice, positions or a,b,c,q given in mc
         mc.ns = B.S.g[mc.g].ns;
         mc.slot = -1;
@@ -1490,7 +1502,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       }
     }
     __syncthreads();
-    if (threadIdx.x < npos) position_bounds(B, threadIdx.x);  // conservative (FP32)
+    if (threadIdx.x < 32) position_bounds(B, threadIdx.x);  // conservative (FP32)
     __syncthreads();
   }
   if (mc.kind == 1 || mc.kind >= 3) {
