@@ -262,6 +262,10 @@ def plain_single_chain(F, seconds: float = 2.0):
 
 
 # ------------------------------------------------------------------ arms
+WORKLOAD = ("config3 batched isotherm: 64 chains = 16 pressures 0.002-1 bar x 4 frameworks "
+            "25.6/38.4/51.2/64.0 A, CO2, FP32 terms with double-float sums and S(k)")
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -281,7 +285,8 @@ def run_reference(args, rank, world):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per * 1000.0, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "config3 batched isotherm (CPU oracle sample)", "chains": 64},
+        "config": {"workload": WORKLOAD, "chains": 64,
+                   "sample": "CPU oracle chains of the same 4 frameworks, all host cores"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -392,9 +397,7 @@ def run_ours(args, rank, world, local_rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded frameworks and guests, no dataset)",
-            "config": {"workload": "config3 batched isotherm: 64 chains = 16 pressures 0.002-1 bar "
-                                   "x 4 frameworks 25.6/38.4/51.2/64.0 A, CO2, FP32 terms with "
-                                   "double-float sums and S(k)",
+            "config": {"workload": WORKLOAD,
                        "chains": len(specs), "moves_per_step_per_chain": args.moves,
                        "parallelism": f"replicas x{world}",
                        "ctas_per_chain_by_framework": clusters,
