@@ -325,15 +325,16 @@ def run_ours(args, rank, world, local_rank):
     systems = [F.System.load(d) for d in dirs]
     infos = [s.info() for s in systems]
     batch = F.Batch(systems, specs, precision=F.FMC_PREC_FP32, guest_capacity=1024)
-    # CTAs per chain for each framework, from timed trial cycles (the
-    # chains' state is restored afterwards); set-up, outside the timing
-    if args.clusters:
-        clusters = [int(v) for v in args.clusters.split(",")]
-        batch.set_cluster(clusters)
-    elif args.no_autotune:
-        clusters = [1] * len(systems)
-    else:
-        clusters = batch.autotune(args.moves)
+    # CTAs per chain, from timed trial cycles (the chains' state is restored
+    # afterwards); set-up, outside the timing
+    if args.chain_clusters:
+        batch.set_chain_cluster([int(v) for v in args.chain_clusters.split(",")])
+    elif args.clusters:
+        batch.set_cluster([int(v) for v in args.clusters.split(",")])
+    elif not args.no_autotune:
+        batch.autotune(args.moves)
+    per_chain = batch.chain_cluster()
+    clusters = [max(v for v, s in zip(per_chain, specs) if s["system"] == i) for i in range(len(systems))]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
     # per step: the host uploads the chains' fugacities (pinned-free host
@@ -400,13 +401,14 @@ def run_ours(args, rank, world, local_rank):
             "config": {"workload": WORKLOAD,
                        "chains": len(specs), "moves_per_step_per_chain": args.moves,
                        "parallelism": f"replicas x{world}",
-                       "ctas_per_chain_by_framework": clusters,
+                       "ctas_per_chain_by_framework": clusters,  # the largest per framework
+                       "ctas_per_chain": per_chain,
                        "l2": "flushed (256 MB write) before every timed step"},
             "trial_moves_per_s": moves / (dev_ms / 1000.0),
             "full_evals_per_s": full / (dev_ms / 1000.0),
             "overlap_exits_per_step": ovl / args.steps,
             # one chain-kernel launch per cluster-size group per step
-            "gpu_launches": args.steps * len(set(clusters)),
+            "gpu_launches": args.steps * len(set(per_chain)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profiled_traffic(),
                          "peak_source": peak_kind,
@@ -434,6 +436,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
+    ap.add_argument("--chain-clusters", default="", help="CTAs per chain, one value per chain")
     ap.add_argument("--clusters", default="", help="CTAs per chain per framework, e.g. 1,2,2,4 "
                     "(default: autotuned)")
     args = ap.parse_args()

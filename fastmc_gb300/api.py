@@ -264,6 +264,17 @@ class Batch:
                                              est.ctypes.data_as(L.dp), ovl.ctypes.data_as(L.ip)))
         return est, ovl
 
+    def set_chain_cluster(self, sizes) -> None:
+        """CTAs per chain (1..8), one entry per chain."""
+        a = (C.c_int * len(sizes))(*[int(v) for v in sizes])
+        L.check(L.load().fmc_batch_set_chain_cluster(self._h, a, len(sizes)))
+
+    def chain_cluster(self):
+        n = self.nchains
+        a = (C.c_int * n)()
+        L.check(L.load().fmc_batch_get_chain_cluster(self._h, a, n))
+        return list(a)
+
     def prob_info(self, chain: int):
         """((na, nb, nc) voxels of the unit cell, number of probability grids)."""
         ng = (C.c_int * 3)()

@@ -657,13 +657,8 @@ __device__ inline void block_sum(double *vals, int n, double *red) {
 }
 
 __device__ inline int block_or(int v, int *scratch) {
-  v = __any_sync(0xffffffffu, v) ? 1 : 0;
-  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
-  __syncthreads();
-  int r = 0;
-  for (int k = 0; k < kWarps; ++k) r |= scratch[k];
-  __syncthreads();
-  return r;
+  (void)scratch;
+  return __syncthreads_or(v) ? 1 : 0;  // one barrier that also reduces
 }
 
 // Exclusive block scan of one int per thread; returns the total.

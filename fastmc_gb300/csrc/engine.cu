@@ -660,7 +660,8 @@ struct Chains {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
   };
-  std::vector<int> csys;  // cluster size per system
+  std::vector<int> csys;    // cluster size per system (the last per-system setting)
+  std::vector<int> cchain;  // cluster size per chain
   std::vector<std::unique_ptr<Group>> groups;
   cudaEvent_t fork = nullptr;
 
@@ -698,23 +699,33 @@ struct Chains {
     return n;
   }
 
-  // Regroup the chains after a change of the per-system cluster sizes.
+  // Per-system cluster sizes: every chain of system i on cs[i] CTAs.
   void set_clusters(const std::vector<int> &cs) {
-    std::vector<int> sys_of(nchains);
     if (host_hdr.size() != (size_t)nchains || headers_stale) pull_headers();
-    for (int c = 0; c < nchains; ++c) sys_of[c] = host_hdr[c].system;
     for (int v : cs)
+      if (v < 1 || v > kMaxCluster) raise(FMC_ERR_ARG, "cluster size must be 1..8");
+    std::vector<int> cc(nchains);
+    for (int c = 0; c < nchains; ++c) cc[c] = cs[host_hdr[c].system];
+    set_chain_clusters(cc);
+    csys = cs;
+  }
+
+  // Regroup the chains after a change of their cluster sizes: one launch
+  // (graph branch) per distinct size.
+  void set_chain_clusters(const std::vector<int> &cc) {
+    for (int v : cc)
       if (v < 1 || v > kMaxCluster) raise(FMC_ERR_ARG, "cluster size must be 1..8");
     for (auto &g : groups) {
       if (g->done) cudaEventDestroy(g->done);
       if (g->stream) cudaStreamDestroy(g->stream);
     }
     groups.clear();
-    csys = cs;
+    cchain = cc;
+    csys.clear();
     for (int v = 1; v <= kMaxCluster; ++v) {
       std::vector<int> ids;
       for (int c = 0; c < nchains; ++c)
-        if (csys[sys_of[c]] == v) ids.push_back(c);
+        if (cchain[c] == v) ids.push_back(c);
       if (ids.empty()) continue;
       if (v > 1 && occupancy(v) < 1)
         raise(FMC_ERR_ARG, "clusters of " + std::to_string(v) + " CTAs cannot be resident");
@@ -1755,56 +1766,93 @@ int fmc_batch_autotune(fmc_batch *b, int nmoves, int *csize_out, int nsys) {
     const long long ev0 = C.last_evals, mv0 = C.last_moves;
     const double ms0 = C.last_ms;
     C.pull_headers();
-    const int ns = (int)C.sys.size();
     std::vector<long long> t0(C.nchains);
     for (int c = 0; c < C.nchains; ++c) t0[c] = C.host_hdr[c].dev_ns;
-    // cycle time from the saved state (best of two) and, per system, the
-    // device time of its slowest chain in that run
-    auto trial = [&](const std::vector<int> &cs, std::vector<double> &sysmax) {
-      C.set_clusters(cs);
+    // cycle time from the saved state (best of two) and the device time of
+    // every chain in that run
+    auto ctrial = [&](const std::vector<int> &cc, std::vector<double> &tchain) {
+      C.set_chain_clusters(cc);
       double best = 1e300;
       for (int r = 0; r < 2; ++r) {
         restore_state(C, snap);
         run_cycle(C, nmoves);
         if (C.last_ms < best) {
           best = C.last_ms;
-          sysmax.assign(ns, 0.0);
-          for (int c = 0; c < C.nchains; ++c) {
-            const ChainHdr &h = C.host_hdr[c];
-            sysmax[h.system] = std::max(sysmax[h.system], 1e-6 * double(h.dev_ns - t0[c]));
-          }
+          tchain.assign(C.nchains, 0.0);
+          for (int c = 0; c < C.nchains; ++c)
+            tchain[c] = 1e-6 * double(C.host_hdr[c].dev_ns - t0[c]);
         }
       }
       return best;
     };
-    std::vector<int> cur(ns, 1);
-    std::vector<double> smax;
-    double tcur = trial(cur, smax);
-    // double the cluster of every system whose slowest chain is within 20%
-    // of the cycle, while the cycle gets more than 3% faster
+    std::vector<int> sysof(C.nchains);
+    for (int c = 0; c < C.nchains; ++c) sysof[c] = C.host_hdr[c].system;
+    const int ns = (int)C.sys.size();
+    auto expand = [&](const std::vector<int> &cs) {
+      std::vector<int> cc(C.nchains);
+      for (int c = 0; c < C.nchains; ++c) cc[c] = cs[sysof[c]];
+      return cc;
+    };
+    // 1. per system: from one CTA per chain, double the cluster of every
+    // system whose slowest chain is within 20% of the cycle, while the
+    // cycle gets more than 3% faster
+    std::vector<int> cs(ns, 1);
+    std::vector<double> tch;
+    double tcur = ctrial(expand(cs), tch);  // ctrial: per-chain times in tch
     for (;;) {
-      std::vector<int> cand = cur;
+      std::vector<double> smax(ns, 0.0);
+      for (int c = 0; c < C.nchains; ++c) smax[sysof[c]] = std::max(smax[sysof[c]], tch[c]);
+      std::vector<int> cand = cs;
       bool changed = false;
       for (int i = 0; i < ns; ++i)
-        if (smax[i] >= 0.8 * tcur && cur[i] * 2 <= kMaxCluster && C.occupancy(cur[i] * 2) >= 1) {
-          cand[i] = cur[i] * 2;
+        if (smax[i] >= 0.8 * tcur && cs[i] * 2 <= kMaxCluster && C.occupancy(cs[i] * 2) >= 1) {
+          cand[i] = cs[i] * 2;
           changed = true;
         }
       if (!changed) break;
-      std::vector<double> s2;
-      const double t = trial(cand, s2);
+      std::vector<double> t2;
+      const double t = ctrial(expand(cand), t2);
       if (t >= 0.97 * tcur) break;
-      cur = cand;
+      cs = cand;
       tcur = t;
-      smax = s2;
+      tch = t2;
     }
-    C.set_clusters(cur);
+    // (A per-chain refinement, halving light chains' clusters and doubling
+    // the chains that set the cycle, won up to 1% on the trial cycle but
+    // lost up to 5% on the following cycles: the heavy chains change as the
+    // isotherm evolves, so the choice stays per system.)
+    const std::vector<int> cur = expand(cs);
+    C.set_chain_clusters(cur);
     restore_state(C, snap);
     C.last_evals = ev0;
     C.last_moves = mv0;
     C.last_ms = ms0;
-    if (csize_out)
-      for (int i = 0; i < nsys; ++i) csize_out[i] = cur[i];
+    if (csize_out)  // per system: the largest cluster of its chains
+      for (int i = 0; i < nsys; ++i) {
+        csize_out[i] = 1;
+        for (int c = 0; c < C.nchains; ++c)
+          if (C.host_hdr[c].system == i) csize_out[i] = std::max(csize_out[i], cur[c]);
+      }
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_set_chain_cluster(fmc_batch *b, const int *csize, int nchains) {
+  return guard([&] {
+    if (!b || !csize) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (nchains != C.nchains) raise(FMC_ERR_ARG, "one cluster size per chain is required");
+    C.set_chain_clusters(std::vector<int>(csize, csize + nchains));
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_get_chain_cluster(const fmc_batch *b, int *csize, int nchains) {
+  return guard([&] {
+    if (!b || !csize) raise(FMC_ERR_ARG, "null argument");
+    const Chains &C = b->C;
+    if (nchains != C.nchains) raise(FMC_ERR_ARG, "one cluster size per chain is required");
+    for (int c = 0; c < nchains; ++c) csize[c] = C.cchain.empty() ? 1 : C.cchain[c];
     return FMC_OK;
   });
 }
@@ -2017,7 +2065,15 @@ int fmc_batch_get_cluster(const fmc_batch *b, int *csize, int nsys) {
     if (!b || !csize) raise(FMC_ERR_ARG, "null argument");
     const Chains &C = b->C;
     if (nsys != (int)C.sys.size()) raise(FMC_ERR_ARG, "one cluster size per system is required");
-    for (int i = 0; i < nsys; ++i) csize[i] = C.csys.empty() ? 1 : C.csys[i];
+    if (!C.csys.empty()) {
+      for (int i = 0; i < nsys; ++i) csize[i] = C.csys[i];
+    } else {  // per-chain sizes: the largest of each system's chains
+      std::vector<ChainHdr> hh(C.nchains);
+      FMC_CUDA(cudaMemcpy(hh.data(), C.hdr.p, C.nchains * sizeof(ChainHdr), cudaMemcpyDeviceToHost));
+      for (int i = 0; i < nsys; ++i) csize[i] = 1;
+      for (int c = 0; c < C.nchains && !C.cchain.empty(); ++c)
+        csize[hh[c].system] = std::max(csize[hh[c].system], C.cchain[c]);
+    }
     return FMC_OK;
   });
 }

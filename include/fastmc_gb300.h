@@ -300,6 +300,11 @@ int fmc_batch_prob_grid(fmc_batch *b, int chain, int sub, double *out, int64_t n
  * batch's number of systems.  No counterpart in the reference (its chains
  * are MPI ranks of one core each). */
 int fmc_batch_set_cluster(fmc_batch *b, const int *csize, int nsys);
+/* The same per chain (nchains sizes): heavily loaded chains of a system can
+ * get more CTAs than its light ones.  fmc_batch_get_cluster then reports
+ * each system's largest size. */
+int fmc_batch_set_chain_cluster(fmc_batch *b, const int *csize, int nchains);
+int fmc_batch_get_chain_cluster(const fmc_batch *b, int *csize, int nchains);
 int fmc_batch_get_cluster(const fmc_batch *b, int *csize, int nsys);
 
 /* Autotuner: picks the cluster size of every system by timing trial cycles

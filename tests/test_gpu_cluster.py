@@ -86,8 +86,11 @@ def test_autotune_leaves_chain_state(fmc_lib, inputs_dir):
     sizes = a.autotune(64)
     assert len(sizes) == 2 and all(1 <= v <= 8 for v in sizes)
     assert a.cluster() == sizes
+    per_chain = a.chain_cluster()
+    assert len(per_chain) == len(specs) and all(1 <= v <= 8 for v in per_chain)
+    assert sizes == [max(v for v, s in zip(per_chain, specs) if s["system"] == i) for i in range(2)]
     b = fmc_lib.Batch(systems, specs, precision=fmc_lib.FMC_PREC_FP32, guest_capacity=256)
-    b.set_cluster(sizes)
+    b.set_chain_cluster(per_chain)
     for x in (a, b):
         x.set_log(150)
         x.run(150)
