@@ -1,0 +1,108 @@
+"""Differentiable guest-framework energy of guest snapshots.
+
+`GuestFrameworkEnergy` wraps the library's hand-written adjoint kernels
+(`fmc_adjoint_eval`) as a torch.autograd.Function: the forward pass returns
+E (kcal/mol) of one snapshot, the backward pass scales the analytic
+dE/d(guest site coordinates) and dE/d(eps_t, sigma_t, lambda_t) of every
+framework atom type by the incoming gradient.  E is the real-space erfc
+Coulomb and 12-6 Lennard-Jones interaction of the guest sites with the
+framework atoms within the cutoff plus the guest-framework cross term of
+the reciprocal Ewald sum; framework type t carries (eps_t, sigma_t,
+lambda_t), mixed with the guest sites by Lorentz-Berthelot, lambda_t
+scaling the type-t charges.
+
+`uptake_sensitivity` is the reweighting estimator of the derivative of the
+mean guest count with respect to a force-field parameter, from snapshots of
+a grand-canonical chain: d<N>/dtheta = -beta (<N dE/dtheta> - <N> <dE/dtheta>).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class Adjoint:
+    """Adjoint kernels bound to one system (framework, guest type, k-vectors)."""
+
+    def __init__(self, system):
+        h = C.c_void_p()
+        L.check(L.load().fmc_adjoint_create(system._h, C.byref(h)))
+        self._h = h
+        nt, ns = C.c_int(), C.c_int()
+        L.check(L.load().fmc_adjoint_info(self._h, C.byref(nt), C.byref(ns), None))
+        self.ntype, self.nsite = nt.value, ns.value
+
+    def base_params(self) -> np.ndarray:
+        """The FIELD's (eps_t, sigma_t, 1.0) per framework type, shape (ntype, 3)."""
+        out = np.zeros(3 * self.ntype)
+        L.check(L.load().fmc_adjoint_info(self._h, None, None, out.ctypes.data_as(L.dp)))
+        return out.reshape(self.ntype, 3)
+
+    def evaluate(self, xyz, params):
+        """E, dE/dxyz and dE/dparams of one snapshot.  xyz: CUDA float64
+        tensor (nmol, nsite, 3); params: (ntype, 3)."""
+        import torch
+        if not (xyz.is_cuda and xyz.dtype == torch.float64):
+            raise TypeError("xyz must be a CUDA float64 tensor")
+        x = xyz.contiguous()
+        nmol = x.shape[0]
+        if x.shape[1:] != (self.nsite, 3):
+            raise ValueError("xyz must have shape (nmol, %d, 3)" % self.nsite)
+        p = np.ascontiguousarray(np.asarray(params.detach().cpu() if hasattr(params, "detach") else params,
+                                            dtype=np.float64).reshape(-1))
+        if p.size != 3 * self.ntype:
+            raise ValueError("params must have shape (%d, 3)" % self.ntype)
+        gx = torch.empty_like(x)
+        gp = np.zeros(3 * self.ntype)
+        e = C.c_double()
+        torch.cuda.synchronize(x.device)
+        L.check(L.load().fmc_adjoint_eval(self._h, nmol, C.c_void_p(x.data_ptr()), p.ctypes.data_as(L.dp),
+                                          C.byref(e), C.c_void_p(gx.data_ptr()), gp.ctypes.data_as(L.dp)))
+        return e.value, gx, gp.reshape(self.ntype, 3)
+
+    def close(self) -> None:
+        if self._h:
+            L.load().fmc_adjoint_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _function():
+    import torch
+
+    class GuestFrameworkEnergy(torch.autograd.Function):
+        """E(xyz, params) of one snapshot with the adjoint as its backward."""
+
+        @staticmethod
+        def forward(ctx, adj, xyz, params):
+            e, gx, gp = adj.evaluate(xyz, params)
+            ctx.save_for_backward(gx, torch.as_tensor(gp, dtype=params.dtype, device=params.device))
+            return torch.tensor(e, dtype=torch.float64, device=params.device)
+
+        @staticmethod
+        def backward(ctx, grad):
+            gx, gp = ctx.saved_tensors
+            return None, grad.to(gx.device) * gx, grad.to(gp.device) * gp
+
+    return GuestFrameworkEnergy
+
+
+def guest_framework_energy(adj: Adjoint, xyz, params):
+    """Differentiable E (kcal/mol): torch autograd through the adjoint."""
+    return _function().apply(adj, xyz, params)
+
+
+def uptake_sensitivity(n, de_dtheta, beta: float):
+    """d<N>/dtheta from snapshots by reweighting: n (S,) guest counts,
+    de_dtheta (S, P) derivatives of each snapshot's energy; returns (P,)."""
+    n = np.asarray(n, dtype=np.float64)
+    g = np.asarray(de_dtheta, dtype=np.float64).reshape(len(n), -1)
+    return -beta * ((n[:, None] * g).mean(axis=0) - n.mean() * g.mean(axis=0))

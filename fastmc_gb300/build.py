@@ -22,7 +22,8 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [GENCODE, "-std=c++17", "-O3", "-lineinfo", "-diag-suppress", "1444",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-Xcompiler", "-Wno-deprecated-declarations"]
-SOURCES = ["chain_f32_g1.cu", "chain_f32_g4.cu", "chain_f64.cu", "engine.cu", "host_setup.cpp"]
+SOURCES = ["chain_f32_g1.cu", "chain_f32_g4.cu", "chain_f64.cu", "engine.cu", "host_setup.cpp",
+           "adjoint.cu"]
 
 
 def nvcc() -> str:

@@ -293,6 +293,26 @@ int fmc_widom_positions(fmc_batch *b, int chain, int iguest, int npos, const dou
 int fmc_batch_prob_info(fmc_batch *b, int chain, int *ngrid, int *nsub);
 int fmc_batch_prob_grid(fmc_batch *b, int chain, int sub, double *out, int64_t n);
 
+/* Adjoint of the guest-framework interaction energy (no counterpart in the
+ * reference).  For a snapshot of nmol guest molecules (one guest type; site
+ * coordinates xyz, nmol x natoms x 3 doubles in DEVICE memory, A):
+ *   E = real-space erfc Coulomb + 12-6 Lennard-Jones between guest sites
+ *       and framework atoms within the cutoff, + the guest-framework cross
+ *       term of the reciprocal Ewald sum (the system's k-vectors), kcal/mol;
+ * with per framework atom type t the parameters (eps_t, sigma_t, lambda_t):
+ * LJ mixed by Lorentz-Berthelot with the guest sites' self-pair values, and
+ * lambda_t a scale of the type-t charges.  fmc_adjoint_eval returns E,
+ * dE/dxyz (device, same layout) and dE/dparams (host, ntype x 3).  Exact
+ * erfc and analytic LJ (the trial-move path interpolates tables), FP64,
+ * orthorhombic cells.  fmc_adjoint_info: number of framework types, guest
+ * sites, and the FIELD's parameters (ntype x 3, lambda = 1). */
+typedef struct fmc_adjoint fmc_adjoint;
+int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out);
+int fmc_adjoint_info(const fmc_adjoint *a, int *ntype, int *nsite, double *base);
+int fmc_adjoint_eval(fmc_adjoint *a, int nmol, const double *xyz, const double *params,
+                     double *energy, double *gxyz, double *gparams);
+int fmc_adjoint_destroy(fmc_adjoint *a);
+
 /* Thread-block clusters: the chains of system i run on clusters of
  * csize[i] CTAs (1..8; default 1).  Each CTA of a cluster takes a share of
  * the chain's framework atoms, guests and k-vectors; results do not depend
