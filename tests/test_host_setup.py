@@ -87,3 +87,22 @@ def test_synthetic_framework_properties():
     chains = syn.config3_chains()
     assert len(chains) == 64
     assert sorted({round(c.box, 6) for c in chains}) == [25.6, 38.4, 51.2, 64.0]
+
+
+def test_probability_inputs(fmc_lib, tmp_path):
+    """CONTROL probability blocks and grid keywords load; energy grids (an
+    'e' line, storeenprob) are refused."""
+    import fastmc_gb300._lib as L
+    spec = syn.small_test_spec()
+    spec.probability = [[0], [1, 2, 3]]
+    spec.grid_spacing = 0.8
+    spec.grid_factor = (2, 2, 2)
+    d = tmp_path / "prob"
+    syn.write_inputs(str(d), spec)
+    fmc_lib.System.load(str(d))
+    txt = (d / "CONTROL").read_text().replace("  3 1 2 3\n", "  3 1 2 3\n  e\n").replace(
+        "probability 2", "probability 3")
+    (d / "CONTROL").write_text(txt)
+    with pytest.raises(L.FmcError) as e:
+        fmc_lib.System.load(str(d))
+    assert "energy probability" in str(e.value)
