@@ -426,29 +426,18 @@ __device__ __forceinline__ void share_of(int n, int r, int c, int &lo, int &hi) 
 
 // ----------------------------------------------------------- MZT generator
 // duni (utility_pack.f:2768-2857): REAL*4 lagged subtract-with-borrow plus
-// a Weyl term; bit-exact because only float add/sub/compare are used.
-__device__ __forceinline__ float duni_f(ChainHdr &h) {
-  float uni = h.u[h.ir - 1] - h.u[h.jr - 1];
-  if (uni < 0.0f) uni = uni + 1.0f;
-  h.u[h.ir - 1] = uni;
-  h.ir = h.ir - 1;
-  if (h.ir == 0) h.ir = 97;
-  h.jr = h.jr - 1;
-  if (h.jr == 0) h.jr = 97;
-  h.c = h.c - h.cd;
-  if (h.c < 0.0f) h.c = h.c + h.cm;
-  uni = uni - h.c;
-  if (uni < 0.0f) uni = uni + 1.0f;
-  return uni;
-}
+// a Weyl term; one step: uni = u[ir] - u[jr] (+1 if negative), u[ir] = uni,
+// ir and jr step down cyclically (97 -> 1), c -= cd (+cm if negative),
+// output uni - c (+1 if negative).  Bit-exact because only float
+// add/sub/compare of multiples of 2^-24 are used.
 
-// The same generator run ahead by one warp: 32 consecutive outputs per
+// The generator run ahead by one warp: 32 consecutive outputs per
 // call, one per lane, appended to the chain's buffer.  duni's state update
 // is x_t = x_{t-97} - x_{t-33} (mod 1) on u[] and c_t = c_{t-1} - cd
 // (mod cm); within 32 steps a lane reads u[] entries no other lane writes
 // (the read of step t at offset 33 lies before the batch, the writes of the
 // batch are its own positions), and c after k steps is (c - k cd) mod cm in
-// exact units of 2^-24.  Outputs are bit-identical to 32 calls of duni_f.
+// exact units of 2^-24.  Outputs are bit-identical to 32 sequential steps.
 __device__ __forceinline__ void refill_draws(ChainHdr &h) {
   const int lane = threadIdx.x & 31;
   const int ir0 = h.ir, jr0 = h.jr;

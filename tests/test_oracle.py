@@ -191,3 +191,64 @@ def test_cube_writer_layout(tmp_path):
     assert np.allclose(vals, g.reshape(-1) / vol / 10, rtol=1e-5)
     # six values per line, and a break at the end of every c row of 7
     assert [len(ln.split()) for ln in lines[7:9]] == [6, 1]
+
+
+def _duni_state(seed):
+    """duni's initial state for a seed (utility_pack.f:2796-2852, the seed
+    hook ms = seed % 1000, sec = (seed // 1000) % 60), in float32."""
+    f = np.float32
+    ms, sec = seed % 1000, (seed // 1000) % 60
+    i, j, k, l = (ms * 3) % 177 + 1, (sec * 23) % 177 + 1, (ms * 5) % 177 + 1, (sec * 3) % 168
+    u = []
+    for _ in range(97):
+        s, t = f(0), f(0.5)
+        for _ in range(24):
+            m = (((i * j) % 179) * k) % 179
+            i, j, k = j, k, m
+            l = (53 * l + 1) % 169
+            if (l * m) % 64 >= 32:
+                s = f(s + t)
+            t = f(0.5 * t)
+        u.append(s)
+    return dict(u=u, ir=97, jr=33, c=f(362436 / 16777216), cd=f(7654321 / 16777216),
+                cm=f(16777213 / 16777216))
+
+
+def _refill32(h):
+    """The device's warp-parallel refill (refill_draws): 32 steps at once,
+    lane k reading u[ir-k], u[jr-k] and c after k+1 steps in closed form."""
+    f = np.float32
+    ir0, jr0 = h["ir"], h["jr"]
+    c0, cd, cm = (int(h[x] * f(16777216)) for x in ("c", "cd", "cm"))
+    out, writes = [], []
+    for lane in range(32):
+        ir, jr = (ir0 - 1 - lane) % 97, (jr0 - 1 - lane) % 97
+        uni = f(h["u"][ir] - h["u"][jr])
+        if uni < 0:
+            uni = f(uni + f(1))
+        ci = int(np.fmod(c0 - (lane + 1) * cd, cm))
+        if ci < 0:
+            ci += cm
+        c = f(f(ci) * f(1 / 16777216))
+        o = f(uni - c)
+        if o < 0:
+            o = f(o + f(1))
+        writes.append((ir, uni))
+        out.append(o)
+    for ir, uni in writes:
+        h["u"][ir] = uni
+    h["c"] = c
+    h["ir"] = ir0 - 32 if ir0 - 32 > 0 else ir0 - 32 + 97
+    h["jr"] = jr0 - 32 if jr0 - 32 > 0 else jr0 - 32 + 97
+    return out
+
+
+def test_parallel_generator_refill_matches_duni(oracle_lib):
+    """The lane-parallel refill reproduces duni's sequence bit for bit."""
+    for seed in (77, 12345, 59999):
+        h = _duni_state(seed)
+        got = []
+        for _ in range(40):
+            got += _refill32(h)
+        ref = oracle_lib.duni_sequence(seed, 32 * 40)
+        assert np.array_equal(np.array(got, dtype=np.float64), ref), seed
