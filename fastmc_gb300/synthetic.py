@@ -36,6 +36,12 @@ CO2_SITES = [  # name, mass, charge, z offset along the molecular axis
     ("Og", 15.9994, -0.35, -1.16),
 ]
 GUEST_LJ = {"Cg": (0.054, 2.80), "Og": (0.157, 3.05)}
+# optional second guest type: a two-site dipolar molecule (N2-like, 1.10 A)
+GUEST2_SITES = [  # name, mass, charge, z offset
+    ("Na", 14.0067, 0.20, 0.55),
+    ("Nb", 14.0067, -0.20, -0.55),
+]
+GUEST2_LJ = {"Na": (0.072, 3.31), "Nb": (0.072, 3.31)}
 
 
 @dataclasses.dataclass
@@ -101,6 +107,10 @@ class GcmcSpec:
     probability: Optional[Sequence[Sequence[int]]] = None
     grid_spacing: Optional[float] = None
     grid_factor: Optional[Sequence[int]] = None
+    # a second guest type (GUEST2_SITES) with its own pressure and count
+    second_guest: bool = False
+    pressure2_bar: float = 5.0
+    create2: int = 0
 
     @property
     def box(self) -> float:
@@ -112,7 +122,7 @@ def _lb(eps_i, sig_i, eps_j, sig_j):
 
 
 def field_text(spec: GcmcSpec, uc: UnitCell) -> str:
-    lines = [spec.title, "UNITS   kcal", "molecular types 2"]
+    lines = [spec.title, "UNITS   kcal", f"molecular types {3 if spec.second_guest else 2}"]
     lines.append("&guest CO2 rigid three site")
     lines.append("NUMMOLS 0")
     lines.append(f"ATOMS {len(CO2_SITES)}")
@@ -121,6 +131,15 @@ def field_text(spec: GcmcSpec, uc: UnitCell) -> str:
     lines.append("rigid 1")
     lines.append("3 1 2 3")
     lines.append("finish")
+    if spec.second_guest:
+        lines.append("&guest N2 rigid two site")
+        lines.append("NUMMOLS 0")
+        lines.append(f"ATOMS {len(GUEST2_SITES)}")
+        for name, mass, chg, z in GUEST2_SITES:
+            lines.append(f"{name:<8s}{mass:14.6f}{chg:14.6f}{0.0:14.6f}{0.0:14.6f}{z:14.6f}")
+        lines.append("rigid 1")
+        lines.append("2 1 2")
+        lines.append("finish")
     lines.append("Framework")
     lines.append(f"NUMMOLS {spec.ntile ** 3}")
     lines.append(f"ATOMS {ATOMS_PER_UNIT}")
@@ -128,8 +147,8 @@ def field_text(spec: GcmcSpec, uc: UnitCell) -> str:
         lines.append(f"{FW_NAMES[t]:<8s}{20.0:14.6f}{q:20.12f}      1      1")
     lines.append("finish")
     # van der Waals: every pair of the 6 unique names, Lorentz-Berthelot
-    names = ["Cg", "Og"] + FW_NAMES
-    params = {"Cg": GUEST_LJ["Cg"], "Og": GUEST_LJ["Og"]}
+    names = ["Cg", "Og"] + (["Na", "Nb"] if spec.second_guest else []) + FW_NAMES
+    params = {"Cg": GUEST_LJ["Cg"], "Og": GUEST_LJ["Og"], **GUEST2_LJ}
     for i, n in enumerate(FW_NAMES):
         params[n] = (float(uc.eps[i]), float(uc.sigma[i]))
     pairs = []
@@ -188,6 +207,12 @@ def control_text(spec: GcmcSpec) -> str:
         for sites in spec.probability:
             lines.append("  " + " ".join(str(int(v)) for v in [len(sites), *sites]))
     lines.append("&end")
+    if spec.second_guest:
+        lines.append("&guest 2")
+        lines.append(f"  pressure (bar) {spec.pressure2_bar:.9f}")
+        if spec.create2:
+            lines.append(f"  create molecules {spec.create2}")
+        lines.append("&end")
     for name, f in spec.move_mix:
         lines.append(f"move {name} {f:.6f}")
     lines.append("finish")

@@ -253,3 +253,68 @@ def test_gpu_chain_fp32_jump(fmc_lib, oracle_lib, inputs_dir):
             (i, g.estep, r.estep, e_old[i])
         njump += r.move == 6
     assert njump >= 20
+
+
+def _two_guest_dir(inputs_dir):
+    """CO2 and a two-site dipolar guest in one framework (each type has its
+    own pressure, loading and guest-guest terms with the other), moves that
+    keep both populations: insert, displace, rotate, jump."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=10,
+                               move_mix=(("insert", 0.1), ("displace", 0.3), ("jump", 0.3),
+                                         ("rotate", 0.3)))
+    spec.overlap = 1.0
+    spec.second_guest = True
+    spec.create2 = 8
+    return inputs_dir(spec, "gpu_two_guests")
+
+
+def _two_guest_oracle(oracle_lib, d, n):
+    o = oracle_lib.Oracle(d)
+    o.seed(7)
+    o.create_molecules(1, 10)
+    o.create_molecules(2, 8)
+    return o, o.run(n)
+
+
+def test_gpu_two_guest_types_fp64(fmc_lib, oracle_lib, inputs_dir):
+    """Two guest types (the multi-type kernel: per-type accumulators, S(k),
+    delE of the other types): an FP64 chain follows the oracle move by move."""
+    d = _two_guest_dir(inputs_dir)
+    n = 400
+    o, ref = _two_guest_oracle(oracle_lib, d, n)
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 7}], precision=fmc_lib.FMC_PREC_FP64,
+                      guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.iguest, g.choice, g.overlap, g.accepted) == \
+               (r.move, r.iguest, r.choice, r.overlap, r.accepted), i
+        if not r.overlap:
+            assert close(g.estep, r.estep, scale=1e-6), (i, g.estep, r.estep)
+    assert {r.iguest for r in ref if r.accepted} == {1, 2}
+    x, m = b.coords(0)  # guest type 1
+    assert m == o.nummols(o.locguest(1))
+    assert np.allclose(x[:9 * m].reshape(-1, 3), o.coords(o.locguest(1)), rtol=0, atol=1e-9)
+
+
+def test_gpu_two_guest_types_fp32(fmc_lib, oracle_lib, inputs_dir):
+    """The same on the FP32 multi-type kernel, until the first decision at
+    the Metropolis threshold; estep within 1e-6 of max(|estep|, 1)."""
+    d = _two_guest_dir(inputs_dir)
+    n = 400
+    _, ref = _two_guest_oracle(oracle_lib, d, n)
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 7}], precision=fmc_lib.FMC_PREC_FP32,
+                      guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    nfull = 0
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.iguest, g.choice) == (r.move, r.iguest, r.choice), i
+        if g.overlap != r.overlap or g.accepted != r.accepted:
+            break
+        if not r.overlap:
+            assert abs(g.estep - r.estep) <= 2e-6 * max(abs(r.estep), 1.0), (i, g.estep, r.estep)
+            nfull += 1
+    assert nfull >= 10
