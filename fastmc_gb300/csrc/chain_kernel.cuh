@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         D.g = B.mc.g;
         D.npos = B.mc.npos;
         D.accepted = B.mc.accepted;
-        D.other = B.mc.accepted && B.flags[4];  // delE of the other molecule types
+        D.other = B.mc.accepted && B.mc.kind != 0 && B.flags[4];  // delE of the other molecule types
         D.booked = 0;
         if (full) B.H.evals += B.mc.npos;
         else if (B.mc.overlap) B.H.overlap_exits++;

@@ -188,7 +188,7 @@ struct ChainHdr {
   int production;
   int minchk_left;         // moves until gcmccount is next a multiple of minchk
   int window_left;         // production moves until the next window ends
-  int pad_w;
+  int last_accepted;       // the previous move's decision (a switch no-op keeps it)
   long long pend;          // production moves not yet added to chainstats (FP32 path)
   long long dev_ns;        // device time spent in this chain's launches (ns)
   double chainstats[kMaxG][6];

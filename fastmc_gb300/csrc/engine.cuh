@@ -55,7 +55,8 @@ struct BlockShared {
   float4 trig[kTrigN];  // FP32 path: the quaternion table (copied per launch)
   double geo[12];    // a, b, c, q1..q4, rotation angle, com/frac scratch
   double vtmp[3];
-  int flags[8];     // 0 status, 1 slot, 2 "translate" (q = 0), 3 FP32 geometry, 4 delE deferred
+  int flags[8];     // 0 status, 1 slot, 2 "translate" (q = 0), 3 FP32 geometry, 4 delE deferred,
+                    // 5 switch no-op
   // cluster exchange (chains on more than one CTA): per-CTA partial totals,
   // double-buffered, and the flags the peers raise in this CTA's memory
   double xv[2][40];
@@ -231,6 +232,7 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   else if (randmov < G.mcswpf) kind = 3;
   else if (randmov < G.mctraf) kind = 4;
   else if (randmov < G.mcrotf) kind = 5;
+  else if (randmov < G.mcswif) kind = 7;  // switch
   else kind = 3;
   // adaptive step sizes (gcmc.f:859-900); the updates themselves (FP64) are
   // out of line, the tests here are integer compares
@@ -239,6 +241,13 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
                      (H.rota_count[g] >= 1 && H.rota_mod[g] == 0)))
     adapt_steps<F32>(H, G, g);
   if (nmols == 0) kind = 1;
+  if (kind == 7) {
+    // mc_switch (gcmc.f:2041-2267) returns before any draw unless two other
+    // guest types hold molecules, which set-up rules out (at most two guest
+    // types with switch moves): no move, and `accepted` keeps its value
+    B.flags[5] = 1;
+    kind = 0;
+  }
   mc.kind = kind;
   mc.g = g;
   mc.ns = G.ns;
@@ -260,7 +269,7 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
     if constexpr (!F32) B.geo[7] = 2.0 * kPi;
     B.flags[2] = 0;
     mc.npos = 2;
-  } else {
+  } else if (kind != 0) {
     double a = 0.0, b = 0.0, c = 0.0;
     B.draws[3] = -1.0f;  // no rotation unless drawn
     if (kind != 5) {     // random_disp (utility_pack.f:3333-3357)
@@ -752,6 +761,7 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       mc.overlap = 0;
       mc.accepted = 0;
       mc.surf_new = mc.surf_old = 0;
+      B.flags[5] = 0;
       if (mode == kPropMC) {
         select_move(B, CA, chain);
       } else if (mode == kPropInsert) {
@@ -1640,7 +1650,7 @@ __device__ void decide(BlockShared<F32> &B, bool draw) {
   MoveCtx &mc = B.mc;
   ChainHdr &H = B.H;
   if (mc.kind == 0) {
-    mc.accepted = 0;
+    mc.accepted = B.flags[5] ? H.last_accepted : 0;
     return;
   }
   if (mc.kind == 1) {
@@ -1727,7 +1737,7 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
   SysDev &S = B.S;
   ChainHdr &H = B.H;
   MoveCtx &mc = B.mc;
-  const int accepted = mc.accepted;
+  const int accepted = mc.accepted && mc.kind != 0;  // a switch no-op keeps a stale `accepted`
   __syncthreads();  // every thread has read the decision before anyone moves on
   if (!accepted) return;
   const GuestType &G = S.g[mc.g];
@@ -1914,7 +1924,8 @@ __device__ void stats(BlockShared<F32> &B, bool defer = false) {
   ChainHdr &H = B.H;
   MoveCtx &mc = B.mc;
   int g = mc.g;
-  if (mc.accepted) {
+  H.last_accepted = mc.accepted;
+  if (mc.accepted && mc.kind >= 1) {
     if (mc.kind == 1) H.accept_ins[g]++;
     else if (mc.kind == 2) H.accept_del[g]++;
     else if (mc.kind == 4) H.accept_tran[g]++;

@@ -793,9 +793,12 @@ void finish_control(System &s) {
     s.mctraf[i] = s.mcswpf[i] + (s.mctraf[i] / nrm);
     s.mcrotf[i] = s.mctraf[i] + (s.mcrotf[i] / nrm);
     s.mcswif[i] = s.mcrotf[i] + (s.mcswif[i] / nrm);
-    // swap and switch are not on this path: refuse inputs that use them
-    if (s.mcswpf[i] > s.mcjmpf[i] || s.mcswif[i] > s.mcrotf[i])
-      raise(FMC_ERR_INPUT, "swap and switch moves are not supported");
+    // swap is not on this path; switch only as the move that returns
+    // without acting (fewer than two other loaded guest types, which holds
+    // for every move when the system has at most two guest types)
+    if (s.mcswpf[i] > s.mcjmpf[i]) raise(FMC_ERR_INPUT, "swap moves are not supported");
+    if (s.mcswif[i] > s.mcrotf[i] && G >= 3)
+      raise(FMC_ERR_INPUT, "switch moves with three or more guest types are not supported");
   }
   s.beta = 1.0 / (kKboltz * s.temp);
   s.statvolm = s.volm * 1e-30;

@@ -97,6 +97,7 @@ class GcmcSpec:
     pressure_bar: float = 0.1
     steps: int = 100000
     equilibration: int = 0
+    accepted_sampling: bool = False  # production statistics after accepted moves only
     create_molecules: int = 0
     move_mix: Sequence[tuple] = (("insert", 0.25), ("delete", 0.25),
                                  ("displace", 0.25), ("rotate", 0.25))
@@ -198,6 +199,8 @@ def control_text(spec: GcmcSpec) -> str:
         lines.append("grid factor " + " ".join(str(int(v)) for v in spec.grid_factor))
     if spec.overlap is not None:
         lines.append(f"overlap {spec.overlap:.6f}")
+    if spec.accepted_sampling:
+        lines.append("sampling accepted")
     lines.append("&guest 1")
     lines.append(f"  pressure (bar) {spec.pressure_bar:.9f}")
     if spec.create_molecules:

@@ -433,6 +433,7 @@ struct Sim {
       accept_rota, jump_count, accept_jump;
   // statistics
   bool production = false;
+  bool last_accepted = false;  // the main loop's `accepted` (not reset per move)
   long long gcmccount = 0, prodcount = 0, rollcount = 0, cycle_step = 0;
   int minchk = 1;
   std::vector<double> chainstats;
@@ -2834,6 +2835,7 @@ double calc_cv(double E2, double E, double N, double N2, double EN, double temp)
 
 // production statistics (gcmc.f:1050-1128)
 void Sim::production_stats(bool accepted) {
+  last_accepted = accepted;
   if (!production) return;
   if (lprob) storeprob();  // gcmc.f:1129-1130, every production move
   if (!((laccsample && accepted) || !laccsample)) return;
@@ -3059,7 +3061,8 @@ void Sim::step(orc_move_log *lg) {
   int m0 = locguest[iguest];
   int nmols = mol[m0].nummols;
   double randmov = rng.next();
-  bool insert = false, del = false, disp = false, tran = false, rota = false, jump = false;
+  bool insert = false, del = false, disp = false, tran = false, rota = false, jump = false,
+       sw = false;
   if (randmov < mcinsf[iguest]) insert = true;
   else if (randmov < mcdelf[iguest]) del = true;
   else if (randmov < mcdisf[iguest]) disp = true;
@@ -3067,7 +3070,7 @@ void Sim::step(orc_move_log *lg) {
   else if (randmov < mcswpf[iguest]) fail("oracle: swap moves are not restated");
   else if (randmov < mctraf[iguest]) { disp = true; tran = true; }
   else if (randmov < mcrotf[iguest]) { disp = true; rota = true; }
-  else if (randmov < mcswif[iguest]) fail("oracle: switch moves are not restated");
+  else if (randmov < mcswif[iguest]) sw = true;
   else disp = true;
   // adaptive step sizes (gcmc.f:859-900)
   if (nmols >= 1 && disp_count[iguest] >= 1) {
@@ -3100,20 +3103,34 @@ void Sim::step(orc_move_log *lg) {
   }
   if (nmols == 0) {
     insert = true;
-    del = disp = tran = rota = jump = false;
+    del = disp = tran = rota = jump = sw = false;
   }
   if (lg) {
     std::memset(lg, 0, sizeof(*lg));
     lg->iguest = iguest;
   }
-  if (insert)
+  if (insert) {
     mc_insert(iguest, lg);
-  else if (del)
+  } else if (del) {
     mc_delete(iguest, lg);
-  else if (jump)
+  } else if (jump) {
     mc_jump(iguest, lg);
-  else
+  } else if (sw) {
+    // mc_switch (gcmc.f:2041-2267) returns before any draw unless at least
+    // two other guest types hold molecules; `accepted` keeps the previous
+    // move's value for the production block
+    int nsw = 0;
+    for (int i = 1; i <= ntpguest; ++i)
+      if (i != iguest && mol[locguest[i]].nummols > 0) ++nsw;
+    if (nsw >= 2) fail("oracle: switch with three or more loaded guest types is not restated");
+    if (lg) {
+      lg->move = 0;
+      lg->accepted = last_accepted;
+    }
+    production_stats(last_accepted);
+  } else {
     mc_displace(iguest, tran, rota, lg);
+  }
   if (lg) lg->nmols_after = mol[m0].nummols;
 }
 

@@ -70,7 +70,8 @@ int orc_get_sk(const orc_sim *s, double *out, int cap);
 
 /* Per-move results (the values the reference computes for one move). */
 typedef struct {
-  int move;          /* 1 insert, 2 delete, 3 displace, 4 translate, 5 rotate */
+  int move;          /* 1 insert, 2 delete, 3 displace, 4 translate, 5 rotate,
+                        6 jump, 0 a switch that returned without acting */
   int iguest;        /* 1-based guest type */
   int choice;        /* 1-based molecule picked (delete/displace), 0 for insert */
   int overlap;       /* loverlap of the trial position */

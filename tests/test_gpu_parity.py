@@ -318,3 +318,50 @@ def test_gpu_two_guest_types_fp32(fmc_lib, oracle_lib, inputs_dir):
             assert abs(g.estep - r.estep) <= 2e-6 * max(abs(r.estep), 1.0), (i, g.estep, r.estep)
             nfull += 1
     assert nfull >= 10
+
+
+def _switch_dir(inputs_dir):
+    """Two guest types with switch moves (mc_switch, gcmc.f:2041-2267, which
+    returns without acting unless two other guest types hold molecules) and
+    "sampling accepted", so the production block reads the `accepted` a
+    switch leaves behind."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=6,
+                               move_mix=(("insert", 0.2), ("displace", 0.3), ("switch", 0.5)))
+    spec.overlap = 1.0
+    spec.second_guest = True
+    spec.create2 = 4
+    spec.accepted_sampling = True
+    return inputs_dir(spec, "gpu_switch")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_gpu_switch_no_op(fmc_lib, oracle_lib, inputs_dir, prec):
+    """Switch moves on the device: the same move sequence as the oracle, a
+    switch keeps the previous `accepted`, and (FP64, move by move) the same
+    decisions and production count."""
+    d = _switch_dir(inputs_dir)
+    n = 400
+    o = oracle_lib.Oracle(d)
+    o.seed(7)
+    o.create_molecules(1, 6)
+    o.create_molecules(2, 4)
+    ref = o.run(n)
+    p = fmc_lib.FMC_PREC_FP64 if prec == "fp64" else fmc_lib.FMC_PREC_FP32
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 7}], precision=p, guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    assert sum(r.move == 0 for r in ref) >= 100
+    same = True
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.iguest, g.choice) == (r.move, r.iguest, r.choice), i
+        if g.move == 0:
+            assert g.accepted == (got[i - 1].accepted if i else 0), i
+        if g.overlap != r.overlap or g.accepted != r.accepted:
+            assert prec == "fp32", i
+            same = False
+            break
+        if not r.overlap and r.move != 0:
+            assert abs(g.estep - r.estep) <= (1e-9 if prec == "fp64" else 2e-6) * max(abs(r.estep), 1.0), i
+    if prec == "fp64":
+        assert same and b.stats()[0].prodcount == o.prodcount() == sum(r.accepted for r in ref)

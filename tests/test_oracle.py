@@ -252,3 +252,44 @@ def test_parallel_generator_refill_matches_duni(oracle_lib):
             got += _refill32(h)
         ref = oracle_lib.duni_sequence(seed, 32 * 40)
         assert np.array_equal(np.array(got, dtype=np.float64), ref), seed
+
+
+SWITCH_MIX = (("insert", 0.2), ("displace", 0.3), ("switch", 0.5))
+
+
+def switch_spec():
+    """Two guest types with switch moves and production statistics after
+    accepted moves only, so that the `accepted` a switch leaves matters."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=6, move_mix=SWITCH_MIX)
+    spec.overlap = 1.0
+    spec.second_guest = True
+    spec.create2 = 4
+    spec.accepted_sampling = True
+    return spec
+
+
+def test_switch_returns_without_partners(oracle_lib, inputs_dir):
+    """mc_switch (gcmc.f:2041-2267) returns before any draw unless two guest
+    types other than the chosen one hold molecules.  With two guest types
+    every switch leaves the configuration alone, and the production block
+    (gcmc.f:1050-1083, with "sampling accepted") sees the previous move's
+    `accepted`, which the main loop does not reset."""
+    d = inputs_dir(switch_spec(), "orc_switch")
+    o = oracle_lib.Oracle(d)
+    o.seed(3)
+    o.create_molecules(1, 6)
+    o.create_molecules(2, 4)
+    logs = o.run(500)
+    counts = {1: 6, 2: 4}
+    prev = 0
+    nsw = 0
+    for l in logs:
+        if l.move == 0:
+            nsw += 1
+            assert l.accepted == prev and l.nmols_after == counts[l.iguest]
+            assert l.estep == 0.0 and not l.overlap
+        counts[l.iguest] = l.nmols_after
+        prev = l.accepted
+    assert nsw >= 150
+    assert sum(1 for l in logs if l.move == 0 and l.accepted) >= 10
+    assert o.prodcount() == sum(l.accepted for l in logs)
