@@ -113,6 +113,22 @@ class PlainEngine:
         L.check(L.load().fmc_metropolis_commit(self._h, rande, C.byref(acc)))
         return bool(acc.value)
 
+    def swap(self, iguest: int, choice: int, jguest: int, q: Sequence[float],
+             rande: Sequence[float]) -> dict:
+        """mc_swap with its draws given: molecule `choice` of iguest replaced
+        by a molecule of jguest at its centre of mass rotated by q; accepted
+        when rande[0] < testi and rande[1] < testj, else rolled back."""
+        qa = np.ascontiguousarray(np.asarray(q, dtype=np.float64))
+        ra = np.ascontiguousarray(np.asarray(rande, dtype=np.float64))
+        if qa.size != 4 or ra.size != 2:
+            raise ValueError("q has 4 components and rande 2")
+        r = L.SwapResult()
+        L.check(L.load().fmc_swap(self._h, iguest, choice, jguest, qa.ctypes.data_as(L.dp),
+                                  ra.ctypes.data_as(L.dp), C.byref(r)))
+        nj = self._ns(jguest)
+        return {"estepi": r.estepi, "estepj": r.estepj, "overlap": bool(r.overlap),
+                "accepted": bool(r.accepted), "newxyz": np.array(r.newxyz[:3 * nj]).reshape(nj, 3)}
+
     def nummols(self, iguest: int = 1) -> int:
         n = C.c_int()
         L.check(L.load().fmc_plain_get_nummols(self._h, iguest, C.byref(n)))

@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (mode == kModeCommit) {
     if (threadIdx.x == 0) {
       B.mc = gctx[chain];
-      decide(B, false);
+      if (B.mc.forced) B.mc.accepted = B.mc.overlap ? 0 : 1;  // accept_move called directly
+      else decide(B, false);
     }
     __syncthreads();
     commit(B, CA, chain, st);

@@ -297,7 +297,7 @@ struct MoveCtx {
   int accepted;
   int evaluated;
   int npos;           // 1 or 2 positions evaluated
-  int pad;
+  int forced;         // commit mode: accept without a decision (a swap's halves)
   double pos[2][kMaxS][3];   // [0] = new / inserted / deleted, [1] = old (displace)
   double estep;
   double rande;

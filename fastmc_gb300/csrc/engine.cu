@@ -1465,6 +1465,113 @@ int fmc_metropolis_commit(fmc_plain *h, double rande, int *accepted) {
   });
 }
 
+static int chain_coords(const Chains &C, int chain, int iguest, double *xyz, int cap, int *nout);
+
+// accept_move for the last evaluated move without energy_eval (mc_swap
+// commits its deletion and its insertion before deciding)
+static void forced_commit(fmc_plain *h) {
+  Chains &C = h->C;
+  MoveCtx mc;
+  FMC_CUDA(cudaMemcpy(&mc, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost));
+  mc.forced = 1;
+  FMC_CUDA(cudaMemcpyAsync(C.ctx.p, &mc, sizeof(MoveCtx), cudaMemcpyHostToDevice, C.stream));
+  C.launch(kModeCommit, 0);
+  C.sync();
+  C.check_status();
+  h->has_move = 0;
+}
+
+int fmc_swap(fmc_plain *h, int iguest, int choice, int jguest, const double *q4,
+             const double *rande2, fmc_swap_result *res) {
+  return guard([&] {
+    if (!h || !q4 || !rande2) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = h->C;
+    const System &s = *C.hsys[0];
+    if (iguest < 1 || iguest > s.ntpguest || jguest < 1 || jguest > s.ntpguest || jguest == iguest)
+      raise(FMC_ERR_ARG, "bad guest index");
+    const MolType &mi = s.mol[s.locguest[iguest]], &mj = s.mol[s.locguest[jguest]];
+    const int ni = mi.natoms, nj = mj.natoms;
+    ChainHdr hd;
+    FMC_CUDA(cudaMemcpy(&hd, C.hdr.p, sizeof hd, cudaMemcpyDeviceToHost));
+    const int nmols = hd.nummols[iguest - 1];
+    if (choice < 1 || choice > nmols) raise(FMC_ERR_ARG, "bad molecule index");
+    if (hd.nummols[jguest - 1] >= C.CA.cap) raise(FMC_ERR_CAPACITY, "guest capacity exceeded");
+    // centre of mass of the chosen molecule (com, utility_pack.f)
+    std::vector<double> xi((size_t)3 * ni * nmols);
+    int nout = 0;
+    chain_coords(C, 0, iguest, xi.data(), (int)xi.size(), &nout);
+    const double *x = xi.data() + (size_t)3 * ni * (choice - 1);
+    double c[3] = {0.0, 0.0, 0.0}, weight = 0.0;
+    for (int i = 0; i < ni; ++i) {
+      weight += mi.wght[i];
+      for (int d = 0; d < 3; ++d) c[d] += x[3 * i + d] * mi.wght[i];
+    }
+    for (int d = 0; d < 3; ++d) c[d] /= weight;
+    ChainSnapshot snap;  // what a rejection restores
+    save_state(C, snap);
+    // delete the first guest and commit it
+    MoveCtx mc;
+    std::memset(&mc, 0, sizeof mc);
+    mc.kind = 2;
+    mc.g = iguest - 1;
+    mc.ns = ni;
+    mc.npos = 1;
+    mc.choice = choice;
+    fmc_move_result r;
+    plain_eval(h, mc, &r, false);
+    const double estepi = -r.estep;
+    forced_commit(h);
+    // the partner type from its template at the centre of mass, rotated by
+    // q about it (rotation, utility_pack.f:3480-3524)
+    const double q1 = q4[0], q2 = q4[1], q3 = q4[2], qq = q4[3];
+    const double Q[9] = {2.0 * q2 * q2 + 2.0 * q1 * q1 - 1.0, 2.0 * q2 * q3 - 2.0 * q1 * qq,
+                         2.0 * q2 * qq + 2.0 * q1 * q3,       2.0 * q2 * q3 + 2.0 * q1 * qq,
+                         2.0 * q1 * q1 + 2.0 * q3 * q3 - 1.0, 2.0 * q3 * qq - 2.0 * q1 * q2,
+                         2.0 * q2 * qq - 2.0 * q1 * q3,       2.0 * q3 * qq + 2.0 * q1 * q2,
+                         2.0 * qq * qq + 2.0 * q1 * q1 - 1.0};
+    std::memset(&mc, 0, sizeof mc);
+    mc.kind = 1;
+    mc.g = jguest - 1;
+    mc.ns = nj;
+    mc.npos = 1;
+    mc.slot = -1;
+    const std::vector<double> &t = s.guest_tmpl[jguest];
+    for (int i = 0; i < nj; ++i) {
+      double v[3];
+      for (int d = 0; d < 3; ++d) v[d] = (t[3 * i + d] + c[d]) - c[d];
+      for (int d = 0; d < 3; ++d)
+        mc.pos[0][i][d] = Q[3 * d] * v[0] + Q[3 * d + 1] * v[1] + Q[3 * d + 2] * v[2] + c[d];
+    }
+    fmc_move_result r2;
+    plain_eval(h, mc, &r2, false);
+    const double estepj = r2.estep;
+    int accepted = 0;
+    if (!r2.overlap) {
+      forced_commit(h);
+      FMC_CUDA(cudaMemcpy(&hd, C.hdr.p, sizeof hd, cudaMemcpyDeviceToHost));
+      // the reference's test, its volume in cubic angstroms included
+      const int jn = hd.nummols[jguest - 1], in = hd.nummols[iguest - 1] + 1;
+      const double ipress = hd.fuga[iguest - 1], jpress = hd.fuga[jguest - 1];
+      const double testi = double(in) * fmc::kBoltz * s.temp / (s.volm * ipress) *
+                           std::exp(-1.0 * s.beta * estepi);
+      const double testj = s.volm * jpress / (double(jn) * fmc::kBoltz * s.temp) *
+                           std::exp(-1.0 * s.beta * estepj);
+      accepted = rande2[0] < testi && rande2[1] < testj;
+    }
+    if (!accepted) restore_state(C, snap);
+    h->has_move = 0;
+    if (res) {
+      std::memset(res, 0, sizeof *res);
+      res->estepi = estepi;
+      res->estepj = estepj;
+      res->overlap = r2.overlap;
+      res->accepted = accepted;
+      for (int i = 0; i < 3 * nj && i < 3 * FMC_MAX_SITES; ++i) res->newxyz[i] = r2.newxyz[i];
+    }
+    return FMC_OK;
+  });
+}
+
 int fmc_plain_get_nummols(const fmc_plain *h, int iguest, int *n) {
   return guard([&] {
     if (!h || !n) raise(FMC_ERR_ARG, "null argument");
@@ -1577,14 +1684,12 @@ int fmc_batch_create(const fmc_system *const *systems, int nsys, const fmc_chain
     if (!systems || !out) raise(FMC_ERR_ARG, "null argument");
     std::vector<const System *> sp;
     for (int i = 0; i < nsys; ++i) sp.push_back(systems[i] ? &systems[i]->s : nullptr);
+    for (const System *q : sp)
+      for (int g = 1; q && g <= q->ntpguest; ++g)
+        if (q->mcswpf[g] > q->mcjmpf[g])
+          raise(FMC_ERR_INPUT, "swap moves run through fmc_swap, not in device-resident chains");
     auto b = std::make_unique<fmc_batch>();
     init_chains(b->C, sp.data(), nsys, chains, nchains, precision, guest_capacity);
-    // per-chain "create molecules" override
-    if (chains) {
-      std::vector<ChainHdr> hh(nchains);
-      FMC_CUDA(cudaMemcpy(hh.data(), b->C.hdr.p, nchains * sizeof(ChainHdr), cudaMemcpyDeviceToHost));
-      (void)hh;
-    }
     // device-side pre-loading uses the system's insert0; per-chain counts
     // are applied by a system copy per distinct count
     bool custom = false;

@@ -793,10 +793,11 @@ void finish_control(System &s) {
     s.mctraf[i] = s.mcswpf[i] + (s.mctraf[i] / nrm);
     s.mcrotf[i] = s.mctraf[i] + (s.mcrotf[i] / nrm);
     s.mcswif[i] = s.mcrotf[i] + (s.mcswif[i] / nrm);
-    // swap is not on this path; switch only as the move that returns
+    // swap needs a partner type (device-resident chains refuse it; it runs
+    // through the per-move fmc_swap); switch only as the move that returns
     // without acting (fewer than two other loaded guest types, which holds
     // for every move when the system has at most two guest types)
-    if (s.mcswpf[i] > s.mcjmpf[i]) raise(FMC_ERR_INPUT, "swap moves are not supported");
+    if (s.mcswpf[i] > s.mcjmpf[i] && G < 2) raise(FMC_ERR_INPUT, "swap moves need two guest types");
     if (s.mcswif[i] > s.mcrotf[i] && G >= 3)
       raise(FMC_ERR_INPUT, "switch moves with three or more guest types are not supported");
   }

@@ -176,6 +176,25 @@ int fmc_guest_energy(fmc_plain *h, int iguest, int choice,
  * decision to *accepted. */
 int fmc_metropolis_commit(fmc_plain *h, double rande, int *accepted);
 
+/* mc_swap (gcmc.f:2269-2452) with its draws given by the host: molecule
+ * `choice` (1-based) of guest type iguest is deleted and committed, a
+ * molecule of jguest is built from its template at the deleted molecule's
+ * centre of mass, rotated by the quaternion q4 about it, inserted and
+ * committed; the swap is accepted when rande2[0] < testi and
+ * rande2[1] < testj (the reference's tests, volume in cubic angstroms).
+ * A rejected or overlapping swap restores the device state saved before it.
+ * It replaces the deletion / accept_move / insertion / accept_move /
+ * reject_move sequence of the reference's mc_swap. */
+typedef struct {
+  double estepi;   /* energy change of the deletion (-estep of deletion) */
+  double estepj;   /* energy change of the insertion */
+  int overlap;     /* the inserted molecule overlaps */
+  int accepted;
+  double newxyz[3 * FMC_MAX_SITES]; /* inserted site coordinates */
+} fmc_swap_result;
+int fmc_swap(fmc_plain *h, int iguest, int choice, int jguest, const double *q4,
+             const double *rande2, fmc_swap_result *res);
+
 /* Read back the device state: guest coordinates of guest type iguest
  * (3 * nsites * nummols doubles in molecule order) and the structure
  * factor S(k) per molecule type, [k][moltype][re,im] with moltype

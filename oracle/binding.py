@@ -64,6 +64,7 @@ def load() -> C.CDLL:
             "orc_prob_info": (i, [vp, C.POINTER(C.c_int)]),
             "orc_prob_grid": (i, [vp, i, dp, i]),
             "orc_prodcount": (C.c_longlong, [vp]),
+            "orc_swap": (i, [vp, i, i, i, dp, dp, dp]),
             "orc_duni_sequence": (None, [C.c_longlong, i, dp]),
             "orc_get_erc": (i, [vp, dp, i]),
             "orc_get_vvv": (i, [vp, i, dp, i]),
@@ -204,8 +205,16 @@ class Oracle:
     def prodcount(self) -> int:
         return self.lib.orc_prodcount(self._h)
 
+    def swap(self, iguest: int, choice: int, jguest: int, q, rande):
+        """One swap with its draws given: (estepi, estepj, overlap, accepted)."""
+        qa = (C.c_double * 4)(*[float(v) for v in q])
+        ra = (C.c_double * 2)(*[float(v) for v in rande])
+        out = (C.c_double * 4)()
+        self._ck(self.lib.orc_swap(self._h, iguest, choice, jguest, qa, ra, out))
+        return out[0], out[1], bool(out[2]), bool(out[3])
+
     def stats(self, iguest: int = 1):
-        out = (C.c_double * 25)()
+        out = (C.c_double * 27)()
         self.lib.orc_stats(self._h, iguest, out)
         return list(out[:])
 

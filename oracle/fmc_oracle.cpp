@@ -430,7 +430,7 @@ struct Sim {
   double rotangle = PI / 3.0, rota_rotangle = PI / 3.0;
   std::vector<long long> ins_count, accept_ins, del_count, accept_del,
       disp_count, accept_disp, tran_count, accept_tran, rota_count,
-      accept_rota, jump_count, accept_jump;
+      accept_rota, jump_count, accept_jump, swap_count, accept_swap;
   // statistics
   bool production = false;
   bool last_accepted = false;  // the main loop's `accepted` (not reset per move)
@@ -509,6 +509,11 @@ struct Sim {
   void mc_delete(int iguest, orc_move_log *lg);
   void mc_displace(int iguest, bool tran, bool rota, orc_move_log *lg);
   void mc_jump(int iguest, orc_move_log *lg);
+  // the swap itself, with its molecule, partner type and quaternion given;
+  // rande[0..1] are the Metropolis numbers, or null to draw them
+  void swap_move(int iguest, int ichoice, int jguest, const double *q,
+                 const double *rande, double *out, orc_move_log *lg);
+  void mc_swap(int iguest, orc_move_log *lg);
   void step(orc_move_log *lg);
   int insert_guests(int iguest, int nguests);
   void production_stats(bool accepted);
@@ -1992,7 +1997,8 @@ void Sim::read_all(const std::string &dir) {
   int ng = ntpguest + 1;
   ins_count.assign(ng, 0);
   accept_ins = del_count = accept_del = disp_count = accept_disp = tran_count =
-      accept_tran = rota_count = accept_rota = jump_count = accept_jump = ins_count;
+      accept_tran = rota_count = accept_rota = jump_count = accept_jump = swap_count =
+          accept_swap = ins_count;
   condense();  // gcmc.f:515-516
   beta = 1.0 / (KBOLTZ * temp);
   epsq = 1.0;
@@ -2834,6 +2840,149 @@ double calc_cv(double E2, double E, double N, double N2, double EN, double temp)
 }
 
 // production statistics (gcmc.f:1050-1128)
+// mc_swap (gcmc.f:2269-2452) after its draws: molecule `ichoice` of
+// iguest is deleted and committed, a molecule of jguest is built from its
+// template at the deleted centre of mass, rotated by q, inserted and
+// committed, and the pair is accepted when rande[0] < testi and then
+// rande[1] < testj.  A rejection restores what the reference saves:
+// coordinates and S(k) of both types, their chgsum_mol and surfacemols,
+// elrc, totatm, the counts and energy(); reject_move's swap branch
+// (mc_moves.f:646-669) restores engsic, elrc_mol and the site-type counts.
+// sumchg keeps the two accept_move updates (the reference does not save it).
+// out (if given): estepi, estepj, loverlap, accepted.
+void Sim::swap_move(int iguest, int ichoice, int jguest, const double *q,
+                    const double *rande, double *out, orc_move_log *lg) {
+  const int imol = locguest[iguest], jmol = locguest[jguest];
+  swap_count[iguest]++;
+  std::vector<double> origenergy = energy;
+  const double ochg_i = chgsum_mol[imol], ochg_j = chgsum_mol[jmol];
+  const double osurf_i = surfacemols[imol], osurf_j = surfacemols[jmol];
+  engsicorig = engsic;
+  const double origelrc = elrc;
+  const std::vector<double> origelrc_mol = elrc_mol;
+  const int origtotatm = totatm;
+  const std::vector<double> oix = mol[imol].mx, oiy = mol[imol].my, oiz = mol[imol].mz;
+  const std::vector<double> ojx = mol[jmol].mx, ojy = mol[jmol].my, ojz = mol[jmol].mz;
+  const std::vector<double> ockc = ckcsum, ocks = ckssum;
+  int molt, natms, nm;
+  get_guest(iguest, ichoice, molt, natms, nm);
+  double cx, cy, cz;
+  com(natms, imol, cx, cy, cz);
+  // delete the first guest and commit
+  double estep = 0.0, delrc = 0.0, engsictmp = 0.0, chgtmp = 0.0;
+  bool linitsurf = false;
+  deletion(iguest, ichoice, delrc, estep, linitsurf, engsictmp, chgtmp, nullptr);
+  int ch = ichoice;
+  accept_move(iguest, false, true, false, linitsurf, delrc, ch, engsictmp, chgtmp);
+  const double estepi = -estep;
+  // insert the second guest at the centre of mass and commit
+  const int jn = mol[jmol].natoms;
+  for (int i = 1; i <= jn; ++i) {
+    newx[i] = guestx[jguest][i] + cx;
+    newy[i] = guesty[jguest][i] + cy;
+    newz[i] = guestz[jguest][i] + cz;
+  }
+  rotation(jn, cx, cy, cz, q[0], q[1], q[2], q[3]);
+  fill_log_xyz(*this, jn, lg);
+  estep = delrc = chgtmp = engsictmp = 0.0;
+  bool loverlap = false, lnewsurf = false;
+  insertion(jguest, delrc, estep, chgtmp, engsictmp, loverlap, lnewsurf, nullptr);
+  int jc = 0;
+  accept_move(jguest, true, false, false, lnewsurf, delrc, jc, engsictmp, chgtmp);
+  const double estepj = estep;
+  bool accepted = false;
+  double r0 = -1.0;
+  if (!loverlap) {
+    r0 = rande ? rande[0] : rng.next();
+    const double jpress = gstfuga[jguest], ipress = gstfuga[iguest];
+    const int jnmols = mol[jmol].nummols;
+    const int inmols = mol[imol].nummols + 1;
+    const double testi = double(inmols) * BOLTZ * temp / (volm * ipress) *
+                         std::exp(-1.0 * beta * estepi);
+    const double testj = volm * jpress / (double(jnmols) * BOLTZ * temp) *
+                         std::exp(-1.0 * beta * estepj);
+    if (r0 < testi) {
+      const double r1 = rande ? rande[1] : rng.next();
+      if (r1 < testj) accepted = true;
+    }
+  }
+  if (accepted) {
+    accept_swap[iguest]++;
+    condense();
+  } else {
+    // reject_move(iguest, jguest, swap) (mc_moves.f:634-669)
+    std::fill(delE.begin(), delE.end(), 0.0);
+    engsic = engsicorig;
+    elrc_mol = origelrc_mol;
+    const MolType &mi = mol[imol], &mj = mol[jmol];
+    for (int i = 1; i <= mi.natoms; ++i) {
+      int ka = mi.ltp[i];
+      numtyp[ka]++;
+      numtyp_mol[imol][ka]++;
+      if (mi.frz[i] != 0) {
+        numfrz[ka]++;
+        numfrz_mol[imol][ka]++;
+      }
+    }
+    for (int i = 1; i <= mj.natoms; ++i) {
+      int ka = mj.ltp[i];
+      numtyp[ka]--;
+      numtyp_mol[jmol][ka]--;
+      if (mj.frz[i] != 0) {
+        numfrz[ka]--;
+        numfrz_mol[jmol][ka]--;
+      }
+    }
+    mol[imol].mx = oix;
+    mol[imol].my = oiy;
+    mol[imol].mz = oiz;
+    mol[jmol].mx = ojx;
+    mol[jmol].my = ojy;
+    mol[jmol].mz = ojz;
+    ckcsum = ockc;
+    ckssum = ocks;
+    chgsum_mol[imol] = ochg_i;
+    chgsum_mol[jmol] = ochg_j;
+    surfacemols[imol] = osurf_i;
+    surfacemols[jmol] = osurf_j;
+    elrc = origelrc;
+    totatm = origtotatm;
+    mol[imol].nummols += 1;
+    mol[jmol].nummols -= 1;
+    condense();
+    energy = origenergy;
+  }
+  if (lg) {
+    lg->move = 7;
+    lg->choice = ichoice;
+    lg->overlap = loverlap;
+    lg->accepted = accepted;
+    lg->estep = estepi + estepj;
+    lg->rande = r0;
+  }
+  if (out) {
+    out[0] = estepi;
+    out[1] = estepj;
+    out[2] = loverlap ? 1.0 : 0.0;
+    out[3] = accepted ? 1.0 : 0.0;
+  }
+  production_stats(accepted);
+}
+
+// mc_swap's draws (gcmc.f:2313-2318, 2349): the molecule, the partner
+// type among the others (switch_chosen_guest), and random_rot's quaternion
+// with the displacement angle
+void Sim::mc_swap(int iguest, orc_move_log *lg) {
+  if (ntpguest < 2) fail("oracle: swap moves need two guest types");
+  const int nmols = mol[locguest[iguest]].nummols;
+  const int ichoice = (int)std::floor(rng.next() * nmols + 1);
+  int jg = (int)std::floor(rng.next() * (ntpguest - 1) + 1);
+  const int jguest = jg < iguest ? jg : jg + 1;
+  double q[4];
+  random_rot(rotangle, q[0], q[1], q[2], q[3]);
+  swap_move(iguest, ichoice, jguest, q, nullptr, nullptr, lg);
+}
+
 void Sim::production_stats(bool accepted) {
   last_accepted = accepted;
   if (!production) return;
@@ -3062,12 +3211,12 @@ void Sim::step(orc_move_log *lg) {
   int nmols = mol[m0].nummols;
   double randmov = rng.next();
   bool insert = false, del = false, disp = false, tran = false, rota = false, jump = false,
-       sw = false;
+       sw = false, swp = false;
   if (randmov < mcinsf[iguest]) insert = true;
   else if (randmov < mcdelf[iguest]) del = true;
   else if (randmov < mcdisf[iguest]) disp = true;
   else if (randmov < mcjmpf[iguest]) jump = true;
-  else if (randmov < mcswpf[iguest]) fail("oracle: swap moves are not restated");
+  else if (randmov < mcswpf[iguest]) swp = true;
   else if (randmov < mctraf[iguest]) { disp = true; tran = true; }
   else if (randmov < mcrotf[iguest]) { disp = true; rota = true; }
   else if (randmov < mcswif[iguest]) sw = true;
@@ -3103,7 +3252,7 @@ void Sim::step(orc_move_log *lg) {
   }
   if (nmols == 0) {
     insert = true;
-    del = disp = tran = rota = jump = sw = false;
+    del = disp = tran = rota = jump = sw = swp = false;
   }
   if (lg) {
     std::memset(lg, 0, sizeof(*lg));
@@ -3115,6 +3264,8 @@ void Sim::step(orc_move_log *lg) {
     mc_delete(iguest, lg);
   } else if (jump) {
     mc_jump(iguest, lg);
+  } else if (swp) {
+    mc_swap(iguest, lg);
   } else if (sw) {
     // mc_switch (gcmc.f:2041-2267) returns before any draw unless at least
     // two other guest types hold molecules; `accepted` keeps the previous
@@ -3404,6 +3555,23 @@ int orc_prob_grid(const orc_sim *h, int sub, double *out, int n) {
 
 long long orc_prodcount(const orc_sim *h) { return h->s.prodcount; }
 
+int orc_swap(orc_sim *h, int iguest, int choice, int jguest, const double *q,
+             const double *rande, double *out) {
+  return guarded([&] {
+    Sim &s = h->s;
+    if (iguest < 1 || iguest > s.ntpguest || jguest < 1 || jguest > s.ntpguest ||
+        jguest == iguest)
+      fail("orc_swap: bad guest types");
+    if (choice < 1 || choice > s.mol[s.locguest[iguest]].nummols)
+      fail("orc_swap: bad molecule");
+    const bool prod = s.production;
+    s.production = false;  // a stand-alone swap adds no production sample
+    s.swap_move(iguest, choice, jguest, q, rande, out, nullptr);
+    s.production = prod;
+    return 0;
+  });
+}
+
 void orc_stats(const orc_sim *h, int ig, double *out) {
   const Sim &s = h->s;
   int vs = 1 + (ig - 1) * 9;
@@ -3430,6 +3598,8 @@ void orc_stats(const orc_sim *h, int ig, double *out) {
   out[22] = s.rota_rotangle;
   out[23] = (double)s.jump_count[ig];
   out[24] = (double)s.accept_jump[ig];
+  out[25] = (double)s.swap_count[ig];
+  out[26] = (double)s.accept_swap[ig];
 }
 
 void orc_duni_sequence(long long seed, int n, double *out) {

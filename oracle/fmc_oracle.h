@@ -89,6 +89,13 @@ typedef struct {
  * -1 on error. */
 int orc_run(orc_sim *s, int nsteps, orc_move_log *log, int cap);
 
+/* One swap (mc_swap, gcmc.f:2269-2452) with its draws given: molecule
+ * `choice` of iguest replaced by a molecule of jguest at its centre of mass,
+ * rotated by q[0..3]; rande[0..1] are the two Metropolis numbers.
+ * out: [0] estepi, [1] estepj, [2] loverlap, [3] accepted.  0 or -1. */
+int orc_swap(orc_sim *s, int iguest, int choice, int jguest, const double *q,
+             const double *rande, double *out);
+
 /* "create molecules" pre-loading (mc_moves.f:84-149), as gcmc.f:664-690
  * does for each guest with guest_insert > 0.  Returns the number of trials
  * or -1 on error. */

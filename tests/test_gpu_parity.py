@@ -365,3 +365,73 @@ def test_gpu_switch_no_op(fmc_lib, oracle_lib, inputs_dir, prec):
             assert abs(g.estep - r.estep) <= (1e-9 if prec == "fp64" else 2e-6) * max(abs(r.estep), 1.0), i
     if prec == "fp64":
         assert same and b.stats()[0].prodcount == o.prodcount() == sum(r.accepted for r in ref)
+
+
+def _swap_dir(inputs_dir):
+    """CO2 and the two-site dipolar guest, 8 and 6 molecules, with swap moves."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=8,
+                               move_mix=(("insert", 0.2), ("displace", 0.3), ("swap", 0.5)))
+    spec.overlap = 1.0
+    spec.second_guest = True
+    spec.create2 = 6
+    return inputs_dir(spec, "gpu_swap")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_gpu_swap_per_move(fmc_lib, oracle_lib, inputs_dir, prec):
+    """fmc_swap against the oracle's mc_swap (gcmc.f:2269-2452) on the same
+    loaded state, with the same draws: swaps the reference's test rejects,
+    swaps forced through (rande -1) and overlapping ones.  estepi, estepj
+    and every decision agree (FP64 to 1e-9, FP32 to 2e-6 of max(|e|, 1));
+    after the sequence both guest types' coordinates, S(k) and energies
+    agree, so rejections restored the state and acceptances committed both
+    halves."""
+    d = _swap_dir(inputs_dir)
+    o = oracle_lib.Oracle(d)
+    o.seed(5)
+    o.create_molecules(1, 8)
+    o.create_molecules(2, 6)
+    p = fmc_lib.PlainEngine(fmc_lib.System.load(d),
+                            fmc_lib.FMC_PREC_FP64 if prec == "fp64" else fmc_lib.FMC_PREC_FP32, 64)
+    with pytest.raises(fmc_lib.FmcError):
+        fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 1}])
+    moved = 0.0  # sum of |energy change| committed: the scale of the running energies' error
+    for g, ns in ((1, 3), (2, 2)):
+        for m in o.coords(o.locguest(g)).reshape(-1, ns, 3):
+            r = p.insertion(g, m)
+            assert not r["overlap"]
+            assert p.commit(0.0)
+            moved += abs(r["estep"])
+    tol = 1e-9 if prec == "fp64" else 2e-6
+    rng = np.random.default_rng(3)
+    nacc = nrej = nov = 0
+    for t in range(24):
+        ig = 1 + t % 2
+        jg = 3 - ig
+        choice = int(rng.integers(1, p.nummols(ig) + 1))
+        th = rng.uniform(0, 2 * math.pi)
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        q = [math.cos(th / 2), *(math.sin(th / 2) * ax)]
+        rande = [-1.0, -1.0] if t % 3 == 0 else list(rng.uniform(size=2))
+        ei, ej, ov, acc = o.swap(ig, choice, jg, q, rande)
+        got = p.swap(ig, choice, jg, q, rande)
+        assert (got["overlap"], got["accepted"]) == (ov, acc), t
+        assert abs(got["estepi"] - ei) <= tol * max(abs(ei), 1.0), (t, got["estepi"], ei)
+        if not ov:
+            assert abs(got["estepj"] - ej) <= tol * max(abs(ej), 1.0), (t, got["estepj"], ej)
+        nacc += acc
+        nov += ov
+        moved += abs(ei) + abs(ej) if acc else 0.0
+        nrej += not acc and not ov
+    assert nacc >= 2 and nrej >= 4 and nov >= 1
+    for g in (1, 2):
+        m = o.locguest(g)
+        assert p.nummols(g) == o.nummols(m)
+        assert np.allclose(p.coords(g), o.coords(m), rtol=0, atol=1e-9)
+    so = o.sk()
+    assert np.allclose(p.sk(), so, rtol=0, atol=(1e-10 if prec == "fp64" else 1e-5) * np.abs(so).max())
+    eg = p.energy()
+    for g in (1, 2):
+        m = o.locguest(g)
+        assert abs(eg[m - 1] - o.energy(m)) <= tol * moved, (g, eg[m - 1], o.energy(m), moved)

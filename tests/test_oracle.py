@@ -293,3 +293,91 @@ def test_switch_returns_without_partners(oracle_lib, inputs_dir):
     assert nsw >= 150
     assert sum(1 for l in logs if l.move == 0 and l.accepted) >= 10
     assert o.prodcount() == sum(l.accepted for l in logs)
+
+
+SWAP_MIX = (("insert", 0.2), ("displace", 0.3), ("swap", 0.5))
+
+
+def swap_spec():
+    """Two guest types (CO2 and a two-site dipolar molecule) with swap moves."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=8, move_mix=SWAP_MIX)
+    spec.overlap = 1.0
+    spec.second_guest = True
+    spec.create2 = 6
+    return spec
+
+
+def _state(o):
+    mols = [o.locguest(1), o.locguest(2)]
+    return ([o.coords(m).copy() for m in mols], [o.energy(m) for m in mols], o.sk().copy())
+
+
+def _same(a, b):
+    return (all(np.array_equal(x, y) for x, y in zip(a[0], b[0])) and a[1] == b[1]
+            and np.array_equal(a[2], b[2]))
+
+
+def test_swap_reject_restores_and_accept_equals_delete_insert(oracle_lib, inputs_dir):
+    """mc_swap (gcmc.f:2269-2452): a rejected swap leaves coordinates,
+    energies and S(k) bit for bit as they were; an accepted one leaves the
+    same state as deleting the molecule and inserting the partner type at
+    its centre of mass (rotated by q) through accept_move."""
+    d = inputs_dir(swap_spec(), "orc_swap")
+
+    def fresh():
+        o = oracle_lib.Oracle(d)
+        o.seed(5)
+        o.create_molecules(1, 8)
+        o.create_molecules(2, 6)
+        return o
+
+    o = fresh()
+    before = _state(o)
+    th = 0.7
+    q = [math.cos(th / 2), math.sin(th / 2) * 0.6, 0.0, math.sin(th / 2) * 0.8]
+    nrej = nacc = 0
+    for choice in range(1, 9):
+        ei, ej, ov, acc = o.swap(1, choice, 2, q, [math.inf, math.inf])
+        assert not acc and _same(_state(o), before)
+        nrej += 1
+    for choice in (3, 5, 7, 2):
+        o = fresh()
+        ref = fresh()
+        ei, ej, ov, acc = o.swap(1, choice, 2, q, [-1.0, -1.0])
+        assert acc == (not ov)
+        if ov:
+            assert _same(_state(o), before)
+            continue
+        nacc += 1
+        assert math.isclose(ei, ref.deletion_energy(1, choice)["estep"] * -1.0, rel_tol=1e-12)
+        ref.apply_move(2, 1, choice, None, True)
+        xyz2 = np.asarray(o.coords(o.locguest(2))).reshape(-1, 2, 3)[-1]
+        e2 = ref.insertion_energy(2, xyz2)
+        assert not e2["overlap"] and math.isclose(ej, e2["estep"], rel_tol=1e-12, abs_tol=1e-12)
+        ref.apply_move(1, 2, 0, xyz2, True)
+        assert _same(_state(o), _state(ref))
+    assert nrej == 8 and nacc >= 2
+
+
+def test_swap_moves_in_a_chain(oracle_lib, inputs_dir):
+    """Swaps in the main loop: counted in swap_count / accept_swap, and after
+    a run the running energy of each guest type and S(k) equal those of the
+    final configuration rebuilt molecule by molecule in an empty framework."""
+    d = inputs_dir(swap_spec(), "orc_swap")
+    o = oracle_lib.Oracle(d)
+    o.seed(5)
+    o.create_molecules(1, 8)
+    o.create_molecules(2, 6)
+    logs = o.run(600)
+    sw = {g: [l for l in logs if l.move == 7 and l.iguest == g] for g in (1, 2)}
+    for g in (1, 2):
+        st = o.stats(g)
+        assert len(sw[g]) == st[25] and sum(l.accepted for l in sw[g]) == st[26]
+    assert len(sw[1]) + len(sw[2]) >= 100
+    f = oracle_lib.Oracle(d)
+    for g, ns in ((1, 3), (2, 2)):
+        for m in o.coords(o.locguest(g)).reshape(-1, ns, 3):
+            f.apply_move(1, g, 0, m, True)
+    for g in (1, 2):
+        assert math.isclose(o.energy(o.locguest(g)), f.energy(f.locguest(g)), rel_tol=1e-10, abs_tol=1e-9)
+    assert np.allclose(o.sk(), f.sk(), rtol=0, atol=1e-9)
