@@ -53,8 +53,9 @@ class MoveResult(C.Structure):
 
 
 class SwapResult(C.Structure):
-    _fields_ = [("estepi", C.c_double), ("estepj", C.c_double), ("overlap", C.c_int),
-                ("accepted", C.c_int), ("newxyz", C.c_double * (3 * MAX_SITES))]
+    _fields_ = [("estepi", C.c_double), ("estepj", C.c_double), ("testi", C.c_double),
+                ("testj", C.c_double), ("overlap", C.c_int), ("pad", C.c_int),
+                ("newxyz", C.c_double * (3 * MAX_SITES))]
 
 
 class ChainSpec(C.Structure):
@@ -101,7 +102,8 @@ SIGNATURES = {
     "fmc_displace": (C.c_int, [vp, C.c_int, C.c_int, dp, C.POINTER(MoveResult)]),
     "fmc_guest_energy": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(MoveResult)]),
     "fmc_metropolis_commit": (C.c_int, [vp, C.c_double, ip]),
-    "fmc_swap": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, C.POINTER(SwapResult)]),
+    "fmc_swap": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, C.POINTER(SwapResult)]),
+    "fmc_swap_finish": (C.c_int, [vp, C.c_int]),
     "fmc_plain_get_nummols": (C.c_int, [vp, C.c_int, ip]),
     "fmc_plain_get_coords": (C.c_int, [vp, C.c_int, dp, C.c_int]),
     "fmc_plain_get_sk": (C.c_int, [vp, dp, C.c_int]),

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
-from typing import List, Optional, Sequence
+from typing import Callable, List, Optional, Sequence
 
 import numpy as np
 
@@ -114,20 +114,26 @@ class PlainEngine:
         return bool(acc.value)
 
     def swap(self, iguest: int, choice: int, jguest: int, q: Sequence[float],
-             rande: Sequence[float]) -> dict:
-        """mc_swap with its draws given: molecule `choice` of iguest replaced
-        by a molecule of jguest at its centre of mass rotated by q; accepted
-        when rande[0] < testi and rande[1] < testj, else rolled back."""
+             rande: Callable[[], float]) -> dict:
+        """mc_swap: molecule `choice` of iguest replaced by a molecule of
+        jguest at its centre of mass rotated by q, decided as the reference
+        decides (gcmc.f:2371-2411) with numbers taken from `rande()` only
+        when the reference draws them; rolled back unless accepted."""
         qa = np.ascontiguousarray(np.asarray(q, dtype=np.float64))
-        ra = np.ascontiguousarray(np.asarray(rande, dtype=np.float64))
-        if qa.size != 4 or ra.size != 2:
-            raise ValueError("q has 4 components and rande 2")
+        if qa.size != 4:
+            raise ValueError("q has 4 components")
         r = L.SwapResult()
-        L.check(L.load().fmc_swap(self._h, iguest, choice, jguest, qa.ctypes.data_as(L.dp),
-                                  ra.ctypes.data_as(L.dp), C.byref(r)))
+        L.check(L.load().fmc_swap(self._h, iguest, choice, jguest, qa.ctypes.data_as(L.dp), C.byref(r)))
+        accepted = False
+        try:
+            if not r.overlap and rande() < r.testi:
+                accepted = rande() < r.testj
+        finally:
+            L.check(L.load().fmc_swap_finish(self._h, int(accepted)))
         nj = self._ns(jguest)
         return {"estepi": r.estepi, "estepj": r.estepj, "overlap": bool(r.overlap),
-                "accepted": bool(r.accepted), "newxyz": np.array(r.newxyz[:3 * nj]).reshape(nj, 3)}
+                "accepted": accepted, "testi": r.testi, "testj": r.testj,
+                "newxyz": np.array(r.newxyz[:3 * nj]).reshape(nj, 3)}
 
     def nummols(self, iguest: int = 1) -> int:
         n = C.c_int()

@@ -1093,10 +1093,13 @@ double *noalloc_scratch() {
 // =================================================================== C ABI
 using namespace fmc;
 
+struct ChainSnapshot;
+
 struct fmc_plain {
   Chains C;
   fmc_system_info info{};
   int has_move = 0;
+  std::unique_ptr<ChainSnapshot> swap_saved;  // set while a swap awaits fmc_swap_finish
 };
 
 struct fmc_batch {
@@ -1343,6 +1346,7 @@ int fmc_full_ewald(fmc_plain *h, double *out4) {
 
 static int plain_eval(fmc_plain *h, MoveCtx &mc, fmc_move_result *res, bool guest_energy) {
   Chains &C = h->C;
+  if (h->swap_saved) raise(FMC_ERR_STATE, "a swap awaits fmc_swap_finish");
   const System &s = *C.hsys[0];
   mc.evaluated = 0;
   FMC_CUDA(cudaMemcpyAsync(C.ctx.p, &mc, sizeof(MoveCtx), cudaMemcpyHostToDevice, C.stream));
@@ -1482,9 +1486,10 @@ static void forced_commit(fmc_plain *h) {
 }
 
 int fmc_swap(fmc_plain *h, int iguest, int choice, int jguest, const double *q4,
-             const double *rande2, fmc_swap_result *res) {
+             fmc_swap_result *res) {
   return guard([&] {
-    if (!h || !q4 || !rande2) raise(FMC_ERR_ARG, "null argument");
+    if (!h || !q4) raise(FMC_ERR_ARG, "null argument");
+    if (h->swap_saved) raise(FMC_ERR_STATE, "a swap awaits fmc_swap_finish");
     Chains &C = h->C;
     const System &s = *C.hsys[0];
     if (iguest < 1 || iguest > s.ntpguest || jguest < 1 || jguest > s.ntpguest || jguest == iguest)
@@ -1507,8 +1512,8 @@ int fmc_swap(fmc_plain *h, int iguest, int choice, int jguest, const double *q4,
       for (int d = 0; d < 3; ++d) c[d] += x[3 * i + d] * mi.wght[i];
     }
     for (int d = 0; d < 3; ++d) c[d] /= weight;
-    ChainSnapshot snap;  // what a rejection restores
-    save_state(C, snap);
+    auto snap = std::make_unique<ChainSnapshot>();  // what a rejection restores
+    save_state(C, *snap);
     // delete the first guest and commit it
     MoveCtx mc;
     std::memset(&mc, 0, sizeof mc);
@@ -1545,29 +1550,37 @@ int fmc_swap(fmc_plain *h, int iguest, int choice, int jguest, const double *q4,
     fmc_move_result r2;
     plain_eval(h, mc, &r2, false);
     const double estepj = r2.estep;
-    int accepted = 0;
+    double testi = 0.0, testj = 0.0;
     if (!r2.overlap) {
       forced_commit(h);
       FMC_CUDA(cudaMemcpy(&hd, C.hdr.p, sizeof hd, cudaMemcpyDeviceToHost));
-      // the reference's test, its volume in cubic angstroms included
+      // the reference's tests, its volume in cubic angstroms included
       const int jn = hd.nummols[jguest - 1], in = hd.nummols[iguest - 1] + 1;
       const double ipress = hd.fuga[iguest - 1], jpress = hd.fuga[jguest - 1];
-      const double testi = double(in) * fmc::kBoltz * s.temp / (s.volm * ipress) *
-                           std::exp(-1.0 * s.beta * estepi);
-      const double testj = s.volm * jpress / (double(jn) * fmc::kBoltz * s.temp) *
-                           std::exp(-1.0 * s.beta * estepj);
-      accepted = rande2[0] < testi && rande2[1] < testj;
+      testi = double(in) * fmc::kBoltz * s.temp / (s.volm * ipress) * std::exp(-1.0 * s.beta * estepi);
+      testj = s.volm * jpress / (double(jn) * fmc::kBoltz * s.temp) * std::exp(-1.0 * s.beta * estepj);
     }
-    if (!accepted) restore_state(C, snap);
     h->has_move = 0;
+    h->swap_saved = std::move(snap);
     if (res) {
       std::memset(res, 0, sizeof *res);
       res->estepi = estepi;
       res->estepj = estepj;
+      res->testi = testi;
+      res->testj = testj;
       res->overlap = r2.overlap;
-      res->accepted = accepted;
       for (int i = 0; i < 3 * nj && i < 3 * FMC_MAX_SITES; ++i) res->newxyz[i] = r2.newxyz[i];
     }
+    return FMC_OK;
+  });
+}
+
+int fmc_swap_finish(fmc_plain *h, int accepted) {
+  return guard([&] {
+    if (!h) raise(FMC_ERR_ARG, "null argument");
+    if (!h->swap_saved) raise(FMC_ERR_STATE, "no swap to finish");
+    if (!accepted) restore_state(h->C, *h->swap_saved);
+    h->swap_saved.reset();
     return FMC_OK;
   });
 }

@@ -176,24 +176,32 @@ int fmc_guest_energy(fmc_plain *h, int iguest, int choice,
  * decision to *accepted. */
 int fmc_metropolis_commit(fmc_plain *h, double rande, int *accepted);
 
-/* mc_swap (gcmc.f:2269-2452) with its draws given by the host: molecule
- * `choice` (1-based) of guest type iguest is deleted and committed, a
- * molecule of jguest is built from its template at the deleted molecule's
- * centre of mass, rotated by the quaternion q4 about it, inserted and
- * committed; the swap is accepted when rande2[0] < testi and
- * rande2[1] < testj (the reference's tests, volume in cubic angstroms).
- * A rejected or overlapping swap restores the device state saved before it.
- * It replaces the deletion / accept_move / insertion / accept_move /
+/* mc_swap (gcmc.f:2269-2452) in two calls, the host drawing as the
+ * reference does.  fmc_swap: molecule `choice` (1-based) of guest type
+ * iguest is deleted and committed, a molecule of jguest is built from its
+ * template at the deleted molecule's centre of mass, rotated by the
+ * quaternion q4 about it, inserted and (unless it overlaps) committed; the
+ * result carries both energy changes and the reference's two tests
+ * (volume in cubic angstroms, as written there).  The host then decides as
+ * gcmc.f:2371-2411 does: if not overlap, rande = duni(); if rande < testi,
+ * rande = duni(); accepted if that rande < testj.  fmc_swap_finish(h,
+ * accepted) keeps the swap or restores the device state saved before it
+ * (an overlapping swap is finished with accepted = 0).  Until then every
+ * other move entry point of the engine refuses with FMC_ERR_STATE.  The
+ * pair replaces the deletion / accept_move / insertion / accept_move /
  * reject_move sequence of the reference's mc_swap. */
 typedef struct {
   double estepi;   /* energy change of the deletion (-estep of deletion) */
   double estepj;   /* energy change of the insertion */
+  double testi;    /* first acceptance test (0 when overlap) */
+  double testj;    /* second acceptance test (0 when overlap) */
   int overlap;     /* the inserted molecule overlaps */
-  int accepted;
+  int pad;
   double newxyz[3 * FMC_MAX_SITES]; /* inserted site coordinates */
 } fmc_swap_result;
 int fmc_swap(fmc_plain *h, int iguest, int choice, int jguest, const double *q4,
-             const double *rande2, fmc_swap_result *res);
+             fmc_swap_result *res);
+int fmc_swap_finish(fmc_plain *h, int accepted);
 
 /* Read back the device state: guest coordinates of guest type iguest
  * (3 * nsites * nummols doubles in molecule order) and the structure

@@ -381,7 +381,8 @@ def _swap_dir(inputs_dir):
 def test_gpu_swap_per_move(fmc_lib, oracle_lib, inputs_dir, prec):
     """fmc_swap against the oracle's mc_swap (gcmc.f:2269-2452) on the same
     loaded state, with the same draws: swaps the reference's test rejects,
-    swaps forced through (rande -1) and overlapping ones.  estepi, estepj
+    swaps forced through (rande -1) and overlapping ones, the engine taking
+    its numbers only when the reference draws them.  estepi, estepj
     and every decision agree (FP64 to 1e-9, FP32 to 2e-6 of max(|e|, 1));
     after the sequence both guest types' coordinates, S(k) and energies
     agree, so rejections restored the state and acceptances committed both
@@ -415,7 +416,8 @@ def test_gpu_swap_per_move(fmc_lib, oracle_lib, inputs_dir, prec):
         q = [math.cos(th / 2), *(math.sin(th / 2) * ax)]
         rande = [-1.0, -1.0] if t % 3 == 0 else list(rng.uniform(size=2))
         ei, ej, ov, acc = o.swap(ig, choice, jg, q, rande)
-        got = p.swap(ig, choice, jg, q, rande)
+        draws = iter(rande)
+        got = p.swap(ig, choice, jg, q, lambda: next(draws))
         assert (got["overlap"], got["accepted"]) == (ov, acc), t
         assert abs(got["estepi"] - ei) <= tol * max(abs(ei), 1.0), (t, got["estepi"], ei)
         if not ov:
@@ -435,3 +437,32 @@ def test_gpu_swap_per_move(fmc_lib, oracle_lib, inputs_dir, prec):
     for g in (1, 2):
         m = o.locguest(g)
         assert abs(eg[m - 1] - o.energy(m)) <= tol * moved, (g, eg[m - 1], o.energy(m), moved)
+
+
+def test_gpu_swap_pending_refuses_other_moves(fmc_lib, inputs_dir):
+    """Between fmc_swap and fmc_swap_finish the engine refuses other moves,
+    and a finished rejection leaves coordinates and S(k) as they were."""
+    import ctypes as C
+    from fastmc_gb300 import _lib as L
+    d = _swap_dir(inputs_dir)
+    p = fmc_lib.PlainEngine(fmc_lib.System.load(d), fmc_lib.FMC_PREC_FP64, 64)
+    rng = np.random.default_rng(2)
+    for g, n in ((1, 4), (2, 3)):
+        while p.nummols(g) < n:
+            x = rng.uniform(0, 25.6, 3)
+            m = np.array([[0.0, 0.0, 0.0], [1.16, 0.0, 0.0], [-1.16, 0.0, 0.0]])[:3 if g == 1 else 2] + x
+            if not p.insertion(g, m)["overlap"]:
+                p.commit(0.0)
+    x0, s0 = [p.coords(g).copy() for g in (1, 2)], p.sk().copy()
+    q = (C.c_double * 4)(1.0, 0.0, 0.0, 0.0)
+    r = L.SwapResult()
+    L.check(L.load().fmc_swap(p._h, 1, 2, 2, q, C.byref(r)))
+    with pytest.raises(fmc_lib.FmcError):
+        p.deletion(1, 1)
+    assert p.nummols(1) == 3 and p.nummols(2) == 3 + (not r.overlap)
+    L.check(L.load().fmc_swap_finish(p._h, 0))
+    assert [p.nummols(g) for g in (1, 2)] == [4, 3]
+    assert all(np.array_equal(p.coords(g), x) for g, x in zip((1, 2), x0))
+    assert np.array_equal(p.sk(), s0)
+    with pytest.raises(fmc_lib.FmcError):
+        L.check(L.load().fmc_swap_finish(p._h, 0))
