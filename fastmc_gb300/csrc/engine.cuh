@@ -228,7 +228,7 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   if (randmov < G.mcinsf) kind = 1;
   else if (randmov < G.mcdelf) kind = 2;
   else if (randmov < G.mcdisf) kind = 3;
-  else if (randmov < G.mcjmpf) kind = 6;  // jump (swap is refused at set-up)
+  else if (randmov < G.mcjmpf) kind = 6;  // jump (chains with swap moves are refused at creation)
   else if (randmov < G.mcswpf) kind = 3;
   else if (randmov < G.mctraf) kind = 4;
   else if (randmov < G.mcrotf) kind = 5;
