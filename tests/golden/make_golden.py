@@ -6,10 +6,12 @@ Run in a checkout where the reference is available:
 
 It copies the reference's own CALF-20 test inputs (test/CONFIG and
 test/FIELD) into tests/golden/calf20/, writes a CONTROL with the test's
-cutoff and Ewald precision (test/T293.0P0.002P0.008/CONTROL; the jump,
-swap and switch move lines are dropped because they are not on this path)
-and records the known answer printed by the reference, the initial
-"Electrostatic energy" of run_test.py (reference_energy), in golden.json.
+cutoff and Ewald precision (test/T293.0P0.002P0.008/CONTROL without its
+jump, swap and switch move lines, so that device-resident chains, which
+refuse swap moves, can run it), keeps the test's CONTROL with all six
+moves as CONTROL_all_moves, and records the known answer printed by the
+reference, the initial "Electrostatic energy" of run_test.py
+(reference_energy), in golden.json.
 """
 from __future__ import annotations
 
@@ -37,6 +39,7 @@ def main(ref: str) -> None:
             keep.append(line)
     with open(os.path.join(out, "CONTROL"), "w") as f:
         f.writelines(keep)
+    shutil.copyfile(ctl_src, os.path.join(out, "CONTROL_all_moves"))
     with open(os.path.join(ref, "run_test.py")) as f:
         src = f.read()
     m = re.search(r"reference_energy\s*=\s*([-0-9.eE+]+)", src)

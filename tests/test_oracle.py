@@ -381,3 +381,33 @@ def test_swap_moves_in_a_chain(oracle_lib, inputs_dir):
     for g in (1, 2):
         assert math.isclose(o.energy(o.locguest(g)), f.energy(f.locguest(g)), rel_tol=1e-10, abs_tol=1e-9)
     assert np.allclose(o.sk(), f.sk(), rtol=0, atol=1e-9)
+
+
+def test_reference_test_control_all_moves(oracle_lib, tmp_path):
+    """The reference's own test input (CALF-20 with CO2 and three-site N2,
+    insert / delete / displace / swap / switch / jump in equal shares,
+    probability grids) runs in the oracle with every move kind, and the
+    running energies and S(k) equal those of the final configuration rebuilt
+    molecule by molecule."""
+    import shutil
+    src = os.path.join(os.path.dirname(__file__), "golden", "calf20")
+    for f in ("CONFIG", "FIELD"):
+        shutil.copy(os.path.join(src, f), tmp_path / f)
+    shutil.copy(os.path.join(src, "CONTROL_all_moves"), tmp_path / "CONTROL")
+    o = oracle_lib.Oracle(str(tmp_path))
+    o.seed(11)
+    o.create_molecules(1, 20)
+    o.create_molecules(2, 20)
+    kinds = set()
+    for _ in range(5):  # the loading drains at these pressures: check along the way
+        logs = o.run(100)
+        kinds |= {l.move for l in logs}
+        f = oracle_lib.Oracle(str(tmp_path))
+        for g in (1, 2):
+            for m in o.coords(o.locguest(g)).reshape(-1, 3, 3):
+                f.apply_move(1, g, 0, m, True)
+        for g in (1, 2):
+            assert math.isclose(o.energy(o.locguest(g)), f.energy(f.locguest(g)),
+                                rel_tol=1e-9, abs_tol=1e-8)
+        assert np.allclose(o.sk(), f.sk(), rtol=0, atol=1e-9)
+    assert {0, 1, 2, 3, 6, 7} <= kinds, kinds
