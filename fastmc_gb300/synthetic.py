@@ -42,6 +42,13 @@ GUEST2_SITES = [  # name, mass, charge, z offset
     ("Nb", 14.0067, -0.20, -0.55),
 ]
 GUEST2_LJ = {"Na": (0.072, 3.31), "Nb": (0.072, 3.31)}
+# optional third guest type: a neutral three-site linear molecule
+GUEST3_SITES = [  # name, mass, charge, z offset
+    ("Ma", 15.9994, 0.25, 0.90),
+    ("Mb", 12.0107, -0.50, 0.0),
+    ("Mc", 15.9994, 0.25, -0.90),
+]
+GUEST3_LJ = {"Ma": (0.10, 3.00), "Mb": (0.06, 2.90), "Mc": (0.10, 3.00)}
 
 
 @dataclasses.dataclass
@@ -112,6 +119,10 @@ class GcmcSpec:
     second_guest: bool = False
     pressure2_bar: float = 5.0
     create2: int = 0
+    # a third guest type (GUEST3_SITES; needs the second)
+    third_guest: bool = False
+    pressure3_bar: float = 5.0
+    create3: int = 0
 
     @property
     def box(self) -> float:
@@ -123,7 +134,10 @@ def _lb(eps_i, sig_i, eps_j, sig_j):
 
 
 def field_text(spec: GcmcSpec, uc: UnitCell) -> str:
-    lines = [spec.title, "UNITS   kcal", f"molecular types {3 if spec.second_guest else 2}"]
+    if spec.third_guest and not spec.second_guest:
+        raise ValueError("a third guest type needs the second")
+    nmt = 2 + int(spec.second_guest) + int(spec.third_guest)
+    lines = [spec.title, "UNITS   kcal", f"molecular types {nmt}"]
     lines.append("&guest CO2 rigid three site")
     lines.append("NUMMOLS 0")
     lines.append(f"ATOMS {len(CO2_SITES)}")
@@ -141,6 +155,15 @@ def field_text(spec: GcmcSpec, uc: UnitCell) -> str:
         lines.append("rigid 1")
         lines.append("2 1 2")
         lines.append("finish")
+    if spec.third_guest:
+        lines.append("&guest M3 rigid three site")
+        lines.append("NUMMOLS 0")
+        lines.append(f"ATOMS {len(GUEST3_SITES)}")
+        for name, mass, chg, z in GUEST3_SITES:
+            lines.append(f"{name:<8s}{mass:14.6f}{chg:14.6f}{0.0:14.6f}{0.0:14.6f}{z:14.6f}")
+        lines.append("rigid 1")
+        lines.append("3 1 2 3")
+        lines.append("finish")
     lines.append("Framework")
     lines.append(f"NUMMOLS {spec.ntile ** 3}")
     lines.append(f"ATOMS {ATOMS_PER_UNIT}")
@@ -148,8 +171,9 @@ def field_text(spec: GcmcSpec, uc: UnitCell) -> str:
         lines.append(f"{FW_NAMES[t]:<8s}{20.0:14.6f}{q:20.12f}      1      1")
     lines.append("finish")
     # van der Waals: every pair of the 6 unique names, Lorentz-Berthelot
-    names = ["Cg", "Og"] + (["Na", "Nb"] if spec.second_guest else []) + FW_NAMES
-    params = {"Cg": GUEST_LJ["Cg"], "Og": GUEST_LJ["Og"], **GUEST2_LJ}
+    names = (["Cg", "Og"] + (["Na", "Nb"] if spec.second_guest else [])
+             + (["Ma", "Mb", "Mc"] if spec.third_guest else []) + FW_NAMES)
+    params = {"Cg": GUEST_LJ["Cg"], "Og": GUEST_LJ["Og"], **GUEST2_LJ, **GUEST3_LJ}
     for i, n in enumerate(FW_NAMES):
         params[n] = (float(uc.eps[i]), float(uc.sigma[i]))
     pairs = []
@@ -215,6 +239,12 @@ def control_text(spec: GcmcSpec) -> str:
         lines.append(f"  pressure (bar) {spec.pressure2_bar:.9f}")
         if spec.create2:
             lines.append(f"  create molecules {spec.create2}")
+        lines.append("&end")
+    if spec.third_guest:
+        lines.append("&guest 3")
+        lines.append(f"  pressure (bar) {spec.pressure3_bar:.9f}")
+        if spec.create3:
+            lines.append(f"  create molecules {spec.create3}")
         lines.append("&end")
     for name, f in spec.move_mix:
         lines.append(f"move {name} {f:.6f}")

@@ -430,7 +430,12 @@ struct Sim {
   double rotangle = PI / 3.0, rota_rotangle = PI / 3.0;
   std::vector<long long> ins_count, accept_ins, del_count, accept_del,
       disp_count, accept_disp, tran_count, accept_tran, rota_count,
-      accept_rota, jump_count, accept_jump, swap_count, accept_swap;
+      accept_rota, jump_count, accept_jump, swap_count, accept_swap, switch_count,
+      accept_switch;
+  // mc_swap's saved long-range corrections (gcmc.f:2312-2313); mc_switch
+  // restores them on rejection although it never sets them itself
+  double origelrc = 0.0;
+  std::vector<double> origelrc_mol;
   // statistics
   bool production = false;
   bool last_accepted = false;  // the main loop's `accepted` (not reset per move)
@@ -514,6 +519,7 @@ struct Sim {
   void swap_move(int iguest, int ichoice, int jguest, const double *q,
                  const double *rande, double *out, orc_move_log *lg);
   void mc_swap(int iguest, orc_move_log *lg);
+  void mc_switch(int iguest, orc_move_log *lg);
   void step(orc_move_log *lg);
   int insert_guests(int iguest, int nguests);
   void production_stats(bool accepted);
@@ -1998,7 +2004,7 @@ void Sim::read_all(const std::string &dir) {
   ins_count.assign(ng, 0);
   accept_ins = del_count = accept_del = disp_count = accept_disp = tran_count =
       accept_tran = rota_count = accept_rota = jump_count = accept_jump = swap_count =
-          accept_swap = ins_count;
+          accept_swap = switch_count = accept_switch = ins_count;
   condense();  // gcmc.f:515-516
   beta = 1.0 / (KBOLTZ * temp);
   epsq = 1.0;
@@ -2858,8 +2864,8 @@ void Sim::swap_move(int iguest, int ichoice, int jguest, const double *q,
   const double ochg_i = chgsum_mol[imol], ochg_j = chgsum_mol[jmol];
   const double osurf_i = surfacemols[imol], osurf_j = surfacemols[jmol];
   engsicorig = engsic;
-  const double origelrc = elrc;
-  const std::vector<double> origelrc_mol = elrc_mol;
+  origelrc = elrc;
+  origelrc_mol = elrc_mol;
   const int origtotatm = totatm;
   const std::vector<double> oix = mol[imol].mx, oiy = mol[imol].my, oiz = mol[imol].mz;
   const std::vector<double> ojx = mol[jmol].mx, ojy = mol[jmol].my, ojz = mol[jmol].mz;
@@ -2965,6 +2971,141 @@ void Sim::swap_move(int iguest, int ichoice, int jguest, const double *q,
     out[1] = estepj;
     out[2] = loverlap ? 1.0 : 0.0;
     out[3] = accepted ? 1.0 : 0.0;
+  }
+  production_stats(accepted);
+}
+
+// mc_switch (gcmc.f:2041-2267).  With fewer than two other guest types
+// holding molecules it returns before any draw, and the main loop's
+// `accepted` keeps the previous move's value.  Otherwise a molecule of
+// iguest and one of a partner type exchange centres of mass, each keeping
+// its orientation: both are deleted and committed, then the partner is
+// inserted at the first's centre and the first at the partner's, each
+// committed even when it overlaps; the pair is accepted when the summed
+// change is negative, else by energy_eval's displacement test (drawn
+// before the overlap veto).  A rejection restores energy(), surfacemols,
+// coordinates and S(k) of both types and engsic, and sets elrc and
+// elrc_mol to mc_swap's saved values (zero before any swap).
+void Sim::mc_switch(int iguest, orc_move_log *lg) {
+  std::vector<int> chosen(1, 0);  // switch_chosen_guest, 1-based
+  for (int i = 1; i <= ntpguest; ++i)
+    if (mol[locguest[i]].nummols > 0 && i != iguest) chosen.push_back(i);
+  const int nswitchgst = (int)chosen.size() - 1;
+  if (nswitchgst < 2) {
+    if (lg) {
+      lg->move = 0;
+      lg->accepted = last_accepted;
+    }
+    production_stats(last_accepted);
+    return;
+  }
+  switch_count[iguest]++;
+  engsicorig = engsic;
+  bool loverallap = false;
+  const int jguest = chosen[(int)std::floor(rng.next() * nswitchgst) + 1];
+  const int imol = locguest[iguest], jmol = locguest[jguest];
+  const int ichoice = (int)std::floor(rng.next() * mol[imol].nummols) + 1;
+  const int jchoice = (int)std::floor(rng.next() * mol[jmol].nummols) + 1;
+  const std::vector<double> origenergy = energy, origsurf = surfacemols;
+  const std::vector<double> oix = mol[imol].mx, oiy = mol[imol].my, oiz = mol[imol].mz;
+  const std::vector<double> ojx = mol[jmol].mx, ojy = mol[jmol].my, ojz = mol[jmol].mz;
+  const std::vector<double> ockc = ckcsum, ocks = ckssum;
+  // both molecules' orientations about their centres of mass
+  int molt, jn, in, nm;
+  double jc[3], ic[3];
+  get_guest(jguest, jchoice, molt, jn, nm);
+  com(jn, jmol, jc[0], jc[1], jc[2]);
+  std::vector<double> gj(3 * jn + 3);
+  for (int a = 1; a <= jn; ++a) {
+    gj[3 * a] = newx[a] - jc[0];
+    gj[3 * a + 1] = newy[a] - jc[1];
+    gj[3 * a + 2] = newz[a] - jc[2];
+  }
+  get_guest(iguest, ichoice, molt, in, nm);
+  com(in, imol, ic[0], ic[1], ic[2]);
+  std::vector<double> gi(3 * in + 3);
+  for (int a = 1; a <= in; ++a) {
+    gi[3 * a] = newx[a] - ic[0];
+    gi[3 * a + 1] = newy[a] - ic[1];
+    gi[3 * a + 2] = newz[a] - ic[2];
+  }
+  // delete both and commit
+  double estep = 0.0, delrc = 0.0, engsictmp = 0.0, chgtmp = 0.0;
+  bool linitsurf = false, linitsurfj = false;
+  deletion(iguest, ichoice, delrc, estep, linitsurf, engsictmp, chgtmp, nullptr);
+  int ch = ichoice;
+  accept_move(iguest, false, true, false, linitsurf, delrc, ch, engsictmp, chgtmp);
+  double estepi = -estep;
+  estep = 0.0;
+  deletion(jguest, jchoice, delrc, estep, linitsurfj, engsictmp, chgtmp, nullptr);
+  ch = jchoice;
+  accept_move(jguest, false, true, false, linitsurfj, delrc, ch, engsictmp, chgtmp);
+  double estepj = -estep;
+  // the partner at the first molecule's centre, then the first at the
+  // partner's, each committed
+  for (int a = 1; a <= jn; ++a) {
+    newx[a] = gj[3 * a] + ic[0];
+    newy[a] = gj[3 * a + 1] + ic[1];
+    newz[a] = gj[3 * a + 2] + ic[2];
+  }
+  estep = 0.0;
+  bool loverlap = false, lnewsurfj = false, lnewsurf = false;
+  insertion(jguest, delrc, estep, chgtmp, engsictmp, loverlap, lnewsurfj, nullptr);
+  if (loverlap) loverallap = true;
+  estepj += estep;
+  ch = jchoice;
+  accept_move(jguest, true, false, false, lnewsurfj, delrc, ch, engsictmp, chgtmp);
+  for (int a = 1; a <= in; ++a) {
+    newx[a] = gi[3 * a] + jc[0];
+    newy[a] = gi[3 * a + 1] + jc[1];
+    newz[a] = gi[3 * a + 2] + jc[2];
+  }
+  fill_log_xyz(*this, in, lg);
+  estep = 0.0;
+  insertion(iguest, delrc, estep, chgtmp, engsictmp, loverlap, lnewsurf, nullptr);
+  if (loverlap) loverallap = true;
+  estepi += estep;
+  ch = ichoice;
+  accept_move(iguest, true, false, false, lnewsurf, delrc, ch, engsictmp, chgtmp);
+  bool accepted;
+  double rande = -1.0;
+  if (estepi + estepj < 0.0) {
+    accepted = true;
+  } else {
+    rande = rng.next();
+    accepted = energy_eval(estepi + estepj, rande, iguest, true, false, false);
+  }
+  if (loverallap) accepted = false;
+  if (accepted) {
+    accept_switch[iguest]++;
+    condense();
+  } else {
+    for (int ik = 1; ik <= maxmls; ++ik) {
+      delE[ik] = 0.0;
+      energy[ik] = origenergy[ik];
+      surfacemols[ik] = origsurf[ik];
+    }
+    mol[imol].mx = oix;
+    mol[imol].my = oiy;
+    mol[imol].mz = oiz;
+    mol[jmol].mx = ojx;
+    mol[jmol].my = ojy;
+    mol[jmol].mz = ojz;
+    ckcsum = ockc;
+    ckssum = ocks;
+    elrc = origelrc;
+    if (origelrc_mol.empty()) origelrc_mol.assign(elrc_mol.size(), 0.0);
+    elrc_mol = origelrc_mol;
+    engsic = engsicorig;
+    condense();
+  }
+  if (lg) {
+    lg->move = 8;
+    lg->choice = ichoice;
+    lg->overlap = loverallap;
+    lg->accepted = accepted;
+    lg->estep = estepi + estepj;
+    lg->rande = rande;
   }
   production_stats(accepted);
 }
@@ -3267,18 +3408,7 @@ void Sim::step(orc_move_log *lg) {
   } else if (swp) {
     mc_swap(iguest, lg);
   } else if (sw) {
-    // mc_switch (gcmc.f:2041-2267) returns before any draw unless at least
-    // two other guest types hold molecules; `accepted` keeps the previous
-    // move's value for the production block
-    int nsw = 0;
-    for (int i = 1; i <= ntpguest; ++i)
-      if (i != iguest && mol[locguest[i]].nummols > 0) ++nsw;
-    if (nsw >= 2) fail("oracle: switch with three or more loaded guest types is not restated");
-    if (lg) {
-      lg->move = 0;
-      lg->accepted = last_accepted;
-    }
-    production_stats(last_accepted);
+    mc_switch(iguest, lg);
   } else {
     mc_displace(iguest, tran, rota, lg);
   }
@@ -3600,6 +3730,8 @@ void orc_stats(const orc_sim *h, int ig, double *out) {
   out[24] = (double)s.accept_jump[ig];
   out[25] = (double)s.swap_count[ig];
   out[26] = (double)s.accept_swap[ig];
+  out[27] = (double)s.switch_count[ig];
+  out[28] = (double)s.accept_switch[ig];
 }
 
 void orc_duni_sequence(long long seed, int n, double *out) {

@@ -71,7 +71,8 @@ int orc_get_sk(const orc_sim *s, double *out, int cap);
 /* Per-move results (the values the reference computes for one move). */
 typedef struct {
   int move;          /* 1 insert, 2 delete, 3 displace, 4 translate, 5 rotate,
-                        6 jump, 0 a switch that returned without acting */
+                        6 jump, 7 swap, 8 switch, 0 a switch that returned
+                        without acting */
   int iguest;        /* 1-based guest type */
   int choice;        /* 1-based molecule picked (delete/displace), 0 for insert */
   int overlap;       /* loverlap of the trial position */
@@ -127,7 +128,9 @@ int orc_apply_move(orc_sim *s, int kind, int iguest, int choice,
  * out[14..17] = disp_count, accept_disp, rota_count, accept_rota,
  * out[18..19] = tran_count, accept_tran,
  * out[20..22] = delrdisp, rotangle, rota_rotangle,
- * out[23..24] = jump_count, accept_jump. */
+ * out[23..24] = jump_count, accept_jump,
+ * out[25..28] = swap_count, accept_swap, switch_count, accept_switch
+ * (out holds 29 doubles). */
 void orc_stats(const orc_sim *s, int iguest, double *out);
 /* probability grids (storeprob): out4 = ngrida, ngridb, ngridc, number of
  * subgrids (0 when none is requested); grid `sub` (1-based) as gridsize

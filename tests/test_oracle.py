@@ -411,3 +411,44 @@ def test_reference_test_control_all_moves(oracle_lib, tmp_path):
                                 rel_tol=1e-9, abs_tol=1e-8)
         assert np.allclose(o.sk(), f.sk(), rtol=0, atol=1e-9)
     assert {0, 1, 2, 3, 6, 7} <= kinds, kinds
+
+
+def test_switch_with_three_guest_types(oracle_lib, inputs_dir):
+    """mc_switch (gcmc.f:2041-2267) acting: with three loaded guest types a
+    molecule and one of another type exchange centres of mass.  Counted in
+    switch_count / accept_switch; along the run the running energies and
+    S(k) equal those of the configuration rebuilt molecule by molecule, so
+    accepted switches committed all four halves and rejected ones restored
+    the state; an accepted switch keeps every type's count."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=8,
+                               move_mix=(("displace", 0.4), ("switch", 0.6)))
+    spec.overlap = 1.0
+    spec.second_guest = True
+    spec.create2 = 6
+    spec.third_guest = True
+    spec.create3 = 6
+    d = inputs_dir(spec, "orc_switch3")
+    o = oracle_lib.Oracle(d)
+    o.seed(5)
+    for g, n in ((1, 8), (2, 6), (3, 6)):
+        o.create_molecules(g, n)
+    nsite = {1: 3, 2: 2, 3: 3}
+    logs = []
+    for _ in range(4):
+        part = o.run(150)
+        logs += part
+        f = oracle_lib.Oracle(d)
+        for g in (1, 2, 3):
+            for m in o.coords(o.locguest(g)).reshape(-1, nsite[g], 3):
+                f.apply_move(1, g, 0, m, True)
+        for g in (1, 2, 3):
+            assert math.isclose(o.energy(o.locguest(g)), f.energy(f.locguest(g)),
+                                rel_tol=1e-9, abs_tol=1e-8), g
+        assert np.allclose(o.sk(), f.sk(), rtol=0, atol=1e-9)
+    sw = [l for l in logs if l.move == 8]
+    for g in (1, 2, 3):
+        st = o.stats(g)
+        mine = [l for l in sw if l.iguest == g]
+        assert len(mine) == st[27] and sum(l.accepted for l in mine) == st[28]
+    assert len(sw) >= 150 and sum(l.accepted for l in sw) >= 3
+    assert [o.nummols(o.locguest(g)) for g in (1, 2, 3)] == [8, 6, 6]
