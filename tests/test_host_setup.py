@@ -106,3 +106,29 @@ def test_probability_inputs(fmc_lib, tmp_path):
     with pytest.raises(L.FmcError) as e:
         fmc_lib.System.load(str(d))
     assert "energy probability" in str(e.value)
+
+
+def test_swap_and_switch_set_up(fmc_lib, tmp_path):
+    """Swap needs a partner type; switch loads with up to two guest types
+    (where mc_switch never acts) and is refused with three; three guest
+    types without switch load."""
+    import fastmc_gb300._lib as L
+
+    def spec(mix, ntypes):
+        s = syn.small_test_spec(move_mix=mix)
+        s.second_guest = ntypes >= 2
+        s.third_guest = ntypes >= 3
+        return s
+    for mix, ntypes, ok in (((("insert", 0.5), ("switch", 0.5)), 1, True),
+                            ((("insert", 0.5), ("switch", 0.5)), 2, True),
+                            ((("insert", 0.5), ("switch", 0.5)), 3, False),
+                            ((("insert", 0.5), ("displace", 0.5)), 3, True),
+                            ((("insert", 0.5), ("swap", 0.5)), 2, True)):
+        d = tmp_path / f"s{len(list(tmp_path.iterdir()))}"
+        syn.write_inputs(str(d), spec(mix, ntypes))
+        if ok:
+            assert fmc_lib.System.load(str(d)).info().ntpguest == ntypes
+        else:
+            with pytest.raises(L.FmcError) as e:
+                fmc_lib.System.load(str(d))
+            assert "switch" in str(e.value)
