@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/fmc_oracle.h).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, as the checker or the timed CPU reference.
+CPU-baseline leg of bench.py, to check results or as the timed CPU reference.
 """
 from __future__ import annotations
 
