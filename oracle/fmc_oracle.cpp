@@ -1,7 +1,7 @@
 // fmc_oracle.cpp -- CPU FP64 oracle for the FastMC GCMC trial-move energy path.
 //
-// TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
-// baseline.  The product library never links or loads this file.
+// TEST INFRASTRUCTURE ONLY: what the CUDA path is tested against, and the
+// timed CPU baseline.  The product library never links or loads this file.
 //
 // This is a plain C++ restatement of the reference Fortran.  Every routine
 // names the reference routine and file:line it follows.  Arrays keep the

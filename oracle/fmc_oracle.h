@@ -4,8 +4,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  The oracle is a plain C++ restatement of the
  * reference Fortran (ewald.f, vdw_terms.f, mc_moves.f, utility_pack.f,
- * gcmc.f, readinputs.f, parse_module.f) used as the checker for the CUDA
- * path and as the timed CPU baseline.  Nothing in fastmc_gb300/ links,
+ * gcmc.f, readinputs.f, parse_module.f) that the CUDA path is tested
+ * against, and the timed CPU baseline.  Nothing in fastmc_gb300/ links,
  * loads or calls it.
  *
  * Parity pin: the initial electrostatic energy of the reference's own
