@@ -62,6 +62,7 @@ struct System {
   int minchk = 1;
   bool laccsample = false;
   double total_pressure = -1.0;
+  bool lfuga = false;  // CONTROL "fugacity": Peng-Robinson fugacities
   std::vector<double> gstpress, gstmolfract, gstfuga, delr;  // [iguest]
   std::vector<double> disp_ratio, tran_ratio, rota_ratio;
   std::vector<float> mcinsf, mcdelf, mcdisf, mcjmpf, mcswpf, mctraf, mcrotf,

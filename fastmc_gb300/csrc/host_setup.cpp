@@ -695,8 +695,9 @@ void read_control(const std::string &dir, System &s) {
       lnumg = true;
       s.nnumg = int_of(r);
       if (s.nnumg <= 0) s.nnumg = 1000;
-    } else if (has(r, "fuga")) raise(FMC_ERR_INPUT, "Peng-Robinson fugacity is not supported");
-    else if (has(r, "hist")) {
+    } else if (has(r, "fuga")) {
+      s.lfuga = true;
+    } else if (has(r, "hist")) {
     } else if (has(r, "equilibr")) {
       s.eqsteps = int_of(r);
       leq = s.eqsteps != 0;
@@ -733,8 +734,65 @@ void read_control(const std::string &dir, System &s) {
   s.minchk = std::max(1, std::min(400, s.nnumg));
 }
 
-// fugacity (utility_pack.f:1206-1310) without the Peng-Robinson branch, and
-// the move-frequency normalisation (gcmc.f:341-386) in REAL*4.
+// Peng-Robinson fugacity of guest type ig (calc_fugacity,
+// utility_pack.f:1428-1500) with fluid_properties' constants
+// (utility_pack.f:1364-1424).  Single-precision literals of the reference
+// stay single precision (its 0.37464, sqrt(2.0), ...).  The Newton
+// iteration for the compressibility factor is capped (the reference's is
+// not).
+static double pr_fugacity(const System &s, int ig, const std::vector<int> &kind,
+                          const std::vector<std::vector<double>> &kfug) {
+  const int G = s.ntpguest;
+  const double R = (double)8.314f, T = s.temp;
+  static const float acc[6] = {0.0f, 0.037f, 0.225f, 0.011f, 0.099f, -0.217f};
+  static const float tcr[6] = {0.0f, 126.2f, 304.12f, 190.56f, 305.32f, 32.98f};
+  static const float pcr[6] = {0.0f, 3.398e6f, 7.374e6f, 4.599e6f, 4.872e6f, 1.293e6f};
+  std::vector<double> a(G + 1), b(G + 1);
+  for (int i = 1; i <= G; ++i) {
+    const double w = acc[kind[i]], tc = tcr[kind[i]], pc = pcr[kind[i]];
+    const double kappa = (double)0.37464f + (double)1.54226f * w - (double)0.26992f * w * w;
+    const double at = (1.0 + kappa * (1.0 - std::sqrt(T / tc)));
+    const double rt = R * tc;
+    a[i] = (double)0.45724f * (rt * rt) / pc * (at * at);
+    b[i] = (double)0.0778f * R * tc / pc;
+  }
+  double asys = 0.0, bsys = 0.0;
+  if (G == 1) {
+    asys = a[1];
+    bsys = b[1];
+  } else {
+    for (int i = 1; i <= G; ++i) {
+      for (int j = 1; j <= G; ++j)
+        asys = asys + s.gstmolfract[i] * s.gstmolfract[j] * std::sqrt(a[i] * a[j]) * (1.0 - kfug[i][j]);
+      bsys = bsys + s.gstmolfract[i] * b[i];
+    }
+  }
+  const double P = s.gstpress[ig];
+  const double A = asys * P / ((R * T) * (R * T));
+  const double B = bsys * P / R / T;
+  const double alpha = B - 1.0, beta_f = A - 3.0 * B * B - 2.0 * B, gamma = -A * B + B * B + B * B * B;
+  double z1 = 1.0, z0 = 0.0;
+  for (int it = 0;; ++it) {
+    if (it > 10000) raise(FMC_ERR_INPUT, "Peng-Robinson compressibility did not converge");
+    z0 = z1;
+    z1 = z0 - (z0 * z0 * z0 + alpha * (z0 * z0) + beta_f * z0 + gamma) /
+                  (3.0 * (z0 * z0) + 2.0 * alpha * z0 + beta_f);
+    if (std::fabs(z1 - z0) < 1.0e-5) break;
+  }
+  double sum_za = 0.0;
+  for (int i = 1; i <= G; ++i)
+    sum_za = sum_za + s.gstmolfract[i] * std::sqrt(a[ig] * a[i]) * (1.0 - kfug[ig][i]);
+  const float r2 = std::sqrt(2.0f);
+  const double two_r2 = (double)(2.0f * r2), p1 = (double)(1.0f + r2), m1 = (double)(1.0f - r2);
+  const double coeff = std::exp(b[ig] / bsys * (z1 - 1.0) - std::log(z1 - B) -
+                                asys / (two_r2 * bsys * R * T) * (2.0 * sum_za / asys - b[ig] / bsys) *
+                                    std::log((z1 + p1 * B) / (z1 + m1 * B)));
+  return coeff * s.gstmolfract[ig] * s.gstpress[ig];
+}
+
+// fugacity (utility_pack.f:1206-1310): partial pressures, mole fractions and
+// (CONTROL "fugacity") Peng-Robinson fugacities; then the move-frequency
+// normalisation (gcmc.f:341-386) in REAL*4.
 void finish_control(System &s) {
   int G = s.ntpguest;
   // probability grid and folding cell (gcmc.f:258-306)
@@ -752,9 +810,10 @@ void finish_control(System &s) {
       if (s.lprobeng[i]) raise(FMC_ERR_INPUT, "energy probability grids are not supported");
   }
   bool lfract = false, lpress = true;
-  double fsum = 0.0, nofract = 0.0;
+  double fsum = 0.0, nofract = 0.0, psum = 0.0;
   for (int i = 1; i <= G; ++i) {
     if (s.gstpress[i] < 0.0) lpress = false;
+    else psum += s.gstpress[i];
     if (s.gstmolfract[i] > 0.0) {
       lfract = true;
       fsum += s.gstmolfract[i];
@@ -773,10 +832,42 @@ void finish_control(System &s) {
         if (s.gstmolfract[i] < 0) s.gstmolfract[i] = (1.0 - fsum) / nofract;
     for (int i = 1; i <= G; ++i) s.gstpress[i] = s.total_pressure * s.gstmolfract[i];
   }
-  if (!lpress && !lfract && s.total_pressure > 0.0)
+  if (!lpress && !lfract && s.total_pressure > 0.0) {
     for (int i = 1; i <= G; ++i) s.gstpress[i] = s.total_pressure;
+    s.total_pressure = G * s.total_pressure;
+    psum = s.total_pressure;
+  }
+  if (s.total_pressure > 0.0 && !lfract) {
+    if (psum != s.total_pressure) s.total_pressure = psum;
+    for (int i = 1; i <= G; ++i) s.gstmolfract[i] = s.gstpress[i] / s.total_pressure;
+  } else if (lpress && !lfract) {
+    s.total_pressure = psum;
+    for (int i = 1; i <= G; ++i) s.gstmolfract[i] = s.gstpress[i] / s.total_pressure;
+  }
+  // fluid_properties / guess_guest (utility_pack.f:1311-1424): the guest is
+  // recognised by its molecular mass; an unknown guest turns the
+  // Peng-Robinson branch off for every guest type
+  std::vector<int> kind(G + 1, 0);
+  std::vector<std::vector<double>> kfug(G + 1, std::vector<double>(G + 1, 0.0));
+  bool lfuga = s.lfuga;
+  if (lfuga) {
+    for (int i = 1; i <= G; ++i) {
+      double mass = 0.0;
+      for (double w : s.mol[s.locguest[i]].wght) mass = mass + w;
+      int k = 0;
+      if (mass > 27.0 && mass < 29.0) k = 1;        // N2
+      else if (mass > 43.0 && mass < 45.0) k = 2;   // CO2
+      else if (mass > 15.5 && mass < 17.0) k = 3;   // CH4
+      else if (mass > 29.0 && mass < 31.0) k = 4;   // C2H6
+      else if (mass > 1.0 && mass < 3.0) k = 5;     // H2
+      kind[i] = k;
+      if (k == 0) lfuga = false;
+    }
+    if (G == 2 && ((kind[1] == 3 && kind[2] == 4) || (kind[1] == 4 && kind[2] == 3)))
+      kfug[1][2] = kfug[2][1] = (double)-0.003f;
+  }
   s.gstfuga.assign(G + 1, 0.0);
-  for (int i = 1; i <= G; ++i) s.gstfuga[i] = s.gstpress[i];
+  for (int i = 1; i <= G; ++i) s.gstfuga[i] = lfuga ? pr_fugacity(s, i, kind, kfug) : s.gstpress[i];
   for (int i = 1; i <= G; ++i) {
     float nrm = s.mcinsf[i] + s.mcdelf[i] + s.mcdisf[i] + s.mcjmpf[i] + s.mcswpf[i] +
                 s.mctraf[i] + s.mcrotf[i] + s.mcswif[i];

@@ -105,6 +105,7 @@ class GcmcSpec:
     steps: int = 100000
     equilibration: int = 0
     accepted_sampling: bool = False  # production statistics after accepted moves only
+    fugacity: bool = False           # Peng-Robinson fugacities from the pressures
     create_molecules: int = 0
     move_mix: Sequence[tuple] = (("insert", 0.25), ("delete", 0.25),
                                  ("displace", 0.25), ("rotate", 0.25))
@@ -225,6 +226,8 @@ def control_text(spec: GcmcSpec) -> str:
         lines.append(f"overlap {spec.overlap:.6f}")
     if spec.accepted_sampling:
         lines.append("sampling accepted")
+    if spec.fugacity:
+        lines.append("fugacity")
     lines.append("&guest 1")
     lines.append(f"  pressure (bar) {spec.pressure_bar:.9f}")
     if spec.create_molecules:

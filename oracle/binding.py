@@ -65,6 +65,7 @@ def load() -> C.CDLL:
             "orc_prob_grid": (i, [vp, i, dp, i]),
             "orc_prodcount": (C.c_longlong, [vp]),
             "orc_swap": (i, [vp, i, i, i, dp, dp, dp]),
+            "orc_fugacity": (d, [vp, i]),
             "orc_duni_sequence": (None, [C.c_longlong, i, dp]),
             "orc_get_erc": (i, [vp, dp, i]),
             "orc_get_vvv": (i, [vp, i, dp, i]),
@@ -201,6 +202,10 @@ class Oracle:
         out = np.zeros(na * nb * nc)
         self._ck(self.lib.orc_prob_grid(self._h, sub, out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
         return out.reshape(na, nb, nc)
+
+    def fugacity(self, iguest: int) -> float:
+        """gstfuga(iguest) in Pa."""
+        return self.lib.orc_fugacity(self._h, iguest)
 
     def prodcount(self) -> int:
         return self.lib.orc_prodcount(self._h)

@@ -403,6 +403,7 @@ struct Sim {
   std::vector<double> grid;                         // [(sub - 1) * gridsize + bin - 1]
   double overlap = 1.5, surftol = 0.0;
   std::vector<double> gstpress, gstfuga, gstmolfract, delr;
+  bool lfuga = false;
   std::vector<float> mcinsf, mcdelf, mcdisf, mcjmpf, mcswpf, mctraf, mcrotf,
       mcswif, mcmvnorm;
   std::vector<double> disp_ratio, tran_ratio, rota_ratio;
@@ -1152,7 +1153,7 @@ void Sim::readcontrol(const std::string &dir) {
       nnumg = intstr(r);
       if (nnumg <= 0) nnumg = 1000;
     } else if (findstring("fuga", r)) {
-      fail("oracle: Peng-Robinson fugacity is not restated");
+      lfuga = true;
     } else if (findstring("hist", r)) {
       nhis = intstr(r);
     } else if (findstring("equilibr", r)) {
@@ -1215,7 +1216,10 @@ void Sim::readcontrol(const std::string &dir) {
   if (!ltemp) fail("oracle: no temperature (error 380)");
 }
 
-// fugacity (utility_pack.f:1206-1310) without the Peng-Robinson branch.
+// fugacity (utility_pack.f:1206-1310) with fluid_properties / guess_guest
+// (utility_pack.f:1311-1424) and calc_fugacity (utility_pack.f:1428-1500).
+// REAL*4 literals of the reference are kept as float values; K_fug, which
+// the reference allocates without setting (apart from CH4 + C2H6), is zero.
 void Sim::fugacity() {
   bool lfract = false, lpress = true;
   double fract_sum = 0, press_sum = 0, no_fract = 0;
@@ -1243,9 +1247,95 @@ void Sim::fugacity() {
   }
   if (!lpress && !lfract && total_pressure > 0.0) {
     for (int i = 1; i <= ntpguest; ++i) gstpress[i] = total_pressure;
+    total_pressure = ntpguest * total_pressure;
+    press_sum = total_pressure;
+  }
+  if (total_pressure > 0.0 && !lfract) {
+    if (press_sum != total_pressure) total_pressure = press_sum;
+    for (int i = 1; i <= ntpguest; ++i) gstmolfract[i] = gstpress[i] / total_pressure;
+  } else if (lpress && !lfract) {
+    total_pressure = press_sum;
+    for (int i = 1; i <= ntpguest; ++i) gstmolfract[i] = gstpress[i] / total_pressure;
   }
   gstfuga.assign(ntpguest + 1, 0.0);
-  for (int i = 1; i <= ntpguest; ++i) gstfuga[i] = gstpress[i];
+  // fluid_properties: Acc_factor, T_crit, P_crit by guess_guest's mass bins
+  std::vector<double> acc(ntpguest + 1), tcrit(ntpguest + 1), pcrit(ntpguest + 1);
+  std::vector<int> iguess(ntpguest + 1, 0);
+  bool fuga_on = lfuga;
+  for (int j = 1; j <= ntpguest && lfuga; ++j) {
+    const MolType &m = mol[locguest[j]];
+    double mass = 0.0;
+    for (int i = 1; i <= m.natoms; ++i) mass += m.wght[i];
+    int g = 0;
+    if (mass > 27.0 && mass < 29.0) g = 1;
+    else if (mass > 43.0 && mass < 45.0) g = 2;
+    else if (mass > 15.5 && mass < 17.0) g = 3;
+    else if (mass > 29.0 && mass < 31.0) g = 4;
+    else if (mass > 1.0 && mass < 3.0) g = 5;
+    iguess[j] = g;
+    switch (g) {
+      case 1: acc[j] = 0.037f; tcrit[j] = 126.2f; pcrit[j] = 3.398e6f; break;
+      case 2: acc[j] = 0.225f; tcrit[j] = 304.12f; pcrit[j] = 7.374e6f; break;
+      case 3: acc[j] = 0.011f; tcrit[j] = 190.56f; pcrit[j] = 4.599e6f; break;
+      case 4: acc[j] = 0.099f; tcrit[j] = 305.32f; pcrit[j] = 4.872e6f; break;
+      case 5: acc[j] = -0.217f; tcrit[j] = 32.98f; pcrit[j] = 1.293e6f; break;
+      default: fuga_on = false;
+    }
+  }
+  if (!fuga_on) {
+    for (int i = 1; i <= ntpguest; ++i) gstfuga[i] = gstpress[i];
+    return;
+  }
+  std::vector<std::vector<double>> kfug(ntpguest + 1, std::vector<double>(ntpguest + 1, 0.0));
+  if (ntpguest == 2 && ((iguess[1] == 3 && iguess[2] == 4) || (iguess[1] == 4 && iguess[2] == 3))) {
+    kfug[1][2] = -0.003f;
+    kfug[2][1] = kfug[1][2];
+  }
+  // calc_fugacity for each guest type
+  const double R = 8.314f;
+  for (int ig = 1; ig <= ntpguest; ++ig) {
+    std::vector<double> kappa(ntpguest + 1), alphaT(ntpguest + 1), ag(ntpguest + 1), bg(ntpguest + 1);
+    for (int i = 1; i <= ntpguest; ++i) {
+      kappa[i] = double(0.37464f) + double(1.54226f) * acc[i] - double(0.26992f) * acc[i] * acc[i];
+      double t = 1 + kappa[i] * (1 - std::sqrt(temp / tcrit[i]));
+      alphaT[i] = t * t;
+      double rt = R * tcrit[i];
+      ag[i] = double(0.45724f) * (rt * rt) / pcrit[i] * alphaT[i];
+      bg[i] = double(0.0778f) * R * tcrit[i] / pcrit[i];
+    }
+    double as = 0.0, bs = 0.0;
+    if (ntpguest == 1) {
+      as = ag[1];
+      bs = bg[1];
+    } else {
+      for (int i = 1; i <= ntpguest; ++i) {
+        for (int j = 1; j <= ntpguest; ++j)
+          as = as + gstmolfract[i] * gstmolfract[j] * std::sqrt(ag[i] * ag[j]) * (1 - kfug[i][j]);
+        bs = bs + gstmolfract[i] * bg[i];
+      }
+    }
+    const double rT = R * temp;
+    const double A = as * gstpress[ig] / (rT * rT);
+    const double B = bs * gstpress[ig] / R / temp;
+    const double alpha = B - 1, beta_f = A - 3 * B * B - 2 * B, gamma = -A * B + B * B + B * B * B;
+    double z1 = 1.0, z0;
+    int iter = 0;
+    do {
+      if (++iter > 10000) fail("oracle: Peng-Robinson compressibility did not converge");
+      z0 = z1;
+      z1 = z0 - (z0 * z0 * z0 + alpha * (z0 * z0) + beta_f * z0 + gamma) /
+                    (3 * (z0 * z0) + 2 * alpha * z0 + beta_f);
+    } while (!(std::fabs(z1 - z0) < 1.0e-5));
+    double sum_za = 0.0;
+    for (int i = 1; i <= ntpguest; ++i)
+      sum_za = sum_za + gstmolfract[i] * std::sqrt(ag[ig] * ag[i]) * (1 - kfug[ig][i]);
+    const float sq2 = std::sqrt(2.0f);
+    const double phi =
+        std::exp(bg[ig] / bs * (z1 - 1) - std::log(z1 - B) -
+                 as / (double(2.0f * sq2) * bs * R * temp) * (2 * sum_za / as - bg[ig] / bs) *
+                     std::log((z1 + double(1.0f + sq2) * B) / (z1 + double(1.0f - sq2) * B)));
+    gstfuga[ig] = phi * gstmolfract[ig] * gstpress[ig];
+  }
 }
 
 // move-frequency normalisation (gcmc.f:341-386), REAL*4 arithmetic.
@@ -3684,6 +3774,11 @@ int orc_prob_grid(const orc_sim *h, int sub, double *out, int n) {
 }
 
 long long orc_prodcount(const orc_sim *h) { return h->s.prodcount; }
+
+double orc_fugacity(const orc_sim *h, int iguest) {
+  const Sim &s = h->s;
+  return iguest >= 1 && iguest <= s.ntpguest ? s.gstfuga[iguest] : -1.0;
+}
 
 int orc_swap(orc_sim *h, int iguest, int choice, int jguest, const double *q,
              const double *rande, double *out) {

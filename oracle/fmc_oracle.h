@@ -90,6 +90,9 @@ typedef struct {
  * -1 on error. */
 int orc_run(orc_sim *s, int nsteps, orc_move_log *log, int cap);
 
+/* gstfuga(iguest) in Pa after set-up (fugacity, utility_pack.f:1206-1310). */
+double orc_fugacity(const orc_sim *s, int iguest);
+
 /* One swap (mc_swap, gcmc.f:2269-2452) with its draws given: molecule
  * `choice` of iguest replaced by a molecule of jguest at its centre of mass,
  * rotated by q[0..3]; rande[0..1] are the two Metropolis numbers.

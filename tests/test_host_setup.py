@@ -132,3 +132,40 @@ def test_swap_and_switch_set_up(fmc_lib, tmp_path):
             with pytest.raises(L.FmcError) as e:
                 fmc_lib.System.load(str(d))
             assert "switch" in str(e.value)
+
+
+def test_peng_robinson_fugacity(fmc_lib, oracle_lib, tmp_path):
+    """CONTROL "fugacity" (fugacity / calc_fugacity, utility_pack.f:1206-1500):
+    the set-up's Peng-Robinson fugacities equal the oracle's bit for bit, the
+    CO2 fugacity coefficient at 293 K falls with pressure as the equation of
+    state gives it (0.994 at 1 bar, 0.94 at 10 bar, 0.78 at 40 bar), and for a
+    mixture the reference's fugacity is phi * y * p (the mole fraction times
+    the partial pressure)."""
+    cases = [(0.1, None), (1.0, None), (10.0, None), (40.0, None), (0.15, 0.85)]
+    bounds = {1.0: (0.990, 0.997), 10.0: (0.93, 0.955), 40.0: (0.75, 0.81)}
+    for k, (p1, p2) in enumerate(cases):
+        spec = syn.small_test_spec(pressure_bar=p1)
+        spec.fugacity = True
+        if p2 is not None:
+            spec.second_guest = True
+            spec.pressure2_bar = p2
+        d = tmp_path / f"f{k}"
+        syn.write_inputs(str(d), spec)
+        got = list(fmc_lib.System.load(str(d)).info().fugacity)
+        o = oracle_lib.Oracle(str(d))
+        ng = 1 if p2 is None else 2
+        assert got[:ng] == [o.fugacity(g) for g in range(1, ng + 1)]
+        if p2 is None:
+            phi = got[0] / (p1 * 1e5)
+            lo, hi = bounds.get(p1, (0.999, 1.0))
+            assert lo < phi < hi, (p1, phi)
+        else:
+            tot = p1 + p2
+            for g, p in ((0, p1), (1, p2)):
+                phi = got[g] / ((p / tot) * p * 1e5)
+                assert 0.995 < phi < 1.0, (g, phi)
+    # without the directive the fugacity is the partial pressure
+    spec = syn.small_test_spec(pressure_bar=10.0)
+    d = tmp_path / "plain"
+    syn.write_inputs(str(d), spec)
+    assert fmc_lib.System.load(str(d)).info().fugacity[0] == 10.0e5
