@@ -452,3 +452,21 @@ def test_switch_with_three_guest_types(oracle_lib, inputs_dir):
         assert len(mine) == st[27] and sum(l.accepted for l in mine) == st[28]
     assert len(sw) >= 150 and sum(l.accepted for l in sw) >= 3
     assert [o.nummols(o.locguest(g)) for g in (1, 2, 3)] == [8, 6, 6]
+
+
+def test_isotherm_fixtures_match_reference_keys():
+    """Each of the ten isotherm inputs maps to one published uptake of
+    run_test.py by its summed pressure, with the run length the reference
+    test uses (750000 + 500000 moves)."""
+    from oracle.isotherm import GOLD, control_numbers
+    g = golden()
+    keys = [float(k) for k in g["isotherm_avg_guests"]]
+    names = sorted(os.listdir(os.path.join(GOLD, "calf20", "isotherm")))
+    assert len(names) == len(keys) == 10
+    seen = set()
+    for n in names:
+        p, steps, eq = control_numbers(os.path.join(GOLD, "calf20", "isotherm", n, "CONTROL"))
+        k = min(keys, key=lambda v: abs(v - p))
+        assert abs(k - p) < 1e-9 and (steps, eq) == (500000, 750000), n
+        seen.add(k)
+    assert len(seen) == 10
