@@ -219,7 +219,7 @@ class Oracle:
         return out[0], out[1], bool(out[2]), bool(out[3])
 
     def stats(self, iguest: int = 1):
-        out = (C.c_double * 29)()
+        out = (C.c_double * 30)()
         self.lib.orc_stats(self._h, iguest, out)
         return list(out[:])
 

@@ -3827,6 +3827,14 @@ void orc_stats(const orc_sim *h, int ig, double *out) {
   out[26] = (double)s.accept_swap[ig];
   out[27] = (double)s.switch_count[ig];
   out[28] = (double)s.accept_switch[ig];
+  // "standard error" of <N> as the reference prints it (gcmc.f:1218-1241):
+  // the weighted standard deviation of the window averages
+  double sd = 0.0;
+  for (const auto &w : s.avgwindow) {
+    const double d = out[0] - w[vs + 1];
+    sd += w[1] * d * d;
+  }
+  out[29] = sw > 0 ? std::sqrt(sd / sw) : 0.0;
 }
 
 void orc_duni_sequence(long long seed, int n, double *out) {

@@ -132,8 +132,9 @@ int orc_apply_move(orc_sim *s, int kind, int iguest, int choice,
  * out[18..19] = tran_count, accept_tran,
  * out[20..22] = delrdisp, rotangle, rota_rotangle,
  * out[23..24] = jump_count, accept_jump,
- * out[25..28] = swap_count, accept_swap, switch_count, accept_switch
- * (out holds 29 doubles). */
+ * out[25..28] = swap_count, accept_swap, switch_count, accept_switch,
+ * out[29] = the "standard error" of <N> (gcmc.f:1218-1241)
+ * (out holds 30 doubles). */
 void orc_stats(const orc_sim *s, int iguest, double *out);
 /* probability grids (storeprob): out4 = ngrida, ngridb, ngridc, number of
  * subgrids (0 when none is requested); grid `sub` (1-based) as gridsize
