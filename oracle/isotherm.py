@@ -13,6 +13,17 @@ oracle on the same inputs the same way (one process per point, spawn pool)
 and applies that band; it also reports the band with se = 0:
 
     python oracle/isotherm.py [--seed S] [--workers W] [--out results.json]
+
+With --device the ten points run instead as ten device-resident chains of
+the CUDA library in one batch (FP32), and the CO2 averages (the chain
+statistics report guest type 1) are checked the same way with se = 0.
+Device-resident chains refuse swap moves, so their CONTROL files drop the
+"move swap" line: with these inputs the reference accepts no swap (its test
+with the volume in cubic angstroms), and switch never acts with two guest
+types, so both are moves that change nothing and the equilibrium averages
+are the same.
+
+    python oracle/isotherm.py --device [--seed S] [--moves N] [--out results.json]
 """
 from __future__ import annotations
 
@@ -66,14 +77,64 @@ def run_point(job):
                 "windows": int(s1[9]), "seconds": time.time() - t0}
 
 
+def run_device(seed: int, moves: int):
+    sys.path.insert(0, ROOT)
+    import fastmc_gb300 as F
+    names = sorted(os.listdir(os.path.join(GOLD, "calf20", "isotherm")))
+    rows, systems, tmp = [], [], tempfile.mkdtemp()
+    for i, name in enumerate(names):
+        ctl = os.path.join(GOLD, "calf20", "isotherm", name, "CONTROL")
+        p, steps, eq = control_numbers(ctl)
+        d = os.path.join(tmp, name)
+        os.makedirs(d)
+        for f in ("CONFIG", "FIELD"):
+            shutil.copy(os.path.join(GOLD, "calf20", f), d)
+        with open(ctl) as fi, open(os.path.join(d, "CONTROL"), "w") as fo:
+            fo.writelines(l for l in fi if not l.strip().lower().startswith("move swap"))
+        systems.append(F.System.load(d))
+        rows.append({"point": name, "pressure_bar": p, "moves": moves or eq + steps})
+    b = F.Batch(systems, [{"system": i, "seed": seed + i} for i in range(len(names))],
+                precision=F.FMC_PREC_FP32, guest_capacity=256)
+    total = rows[0]["moves"]
+    t0 = time.time()
+    done = 0
+    while done < total:
+        n = min(50000, total - done)
+        b.run(n)
+        done += n
+    st = b.stats()
+    for i, r in enumerate(rows):
+        r.update({"avg_co2": st[i].avg_n, "production_moves": int(st[i].prodcount),
+                  "status": int(st[i].status), "seconds": time.time() - t0})
+    shutil.rmtree(tmp, ignore_errors=True)
+    return rows
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
+    ap.add_argument("--device", action="store_true")
+    ap.add_argument("--moves", type=int, default=0)
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--workers", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
     with open(os.path.join(GOLD, "golden.json")) as f:
         ref = {float(k): v for k, v in json.load(f)["isotherm_avg_guests"].items()}
+    if a.device:
+        rows = run_device(a.seed, a.moves)
+        ok_all = True
+        for r in rows:
+            key = min(ref, key=lambda k: abs(k - r["pressure_bar"]))
+            co2 = ref[key][0]
+            r["reference_co2"] = co2
+            r["pass"] = bool(0.8 * r["avg_co2"] <= co2 <= 1.2 * r["avg_co2"]) and r["status"] == 0
+            ok_all &= r["pass"]
+            print("P %.6f bar  CO2 %7.3f (ref %6.2f)  %s" % (r["pressure_bar"], r["avg_co2"], co2,
+                                                           "PASS" if r["pass"] else "FAIL"))
+        if a.out:
+            with open(a.out, "w") as f:
+                json.dump({"seed": a.seed, "device": True, "rows": rows, "all_pass": ok_all}, f, indent=1)
+        sys.exit(0 if ok_all else 1)
     names = sorted(os.listdir(os.path.join(GOLD, "calf20", "isotherm")))
     with mp.get_context("spawn").Pool(min(a.workers, len(names))) as pool:
         rows = pool.map(run_point, [(n, a.seed) for n in names])
