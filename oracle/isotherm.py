@@ -15,7 +15,8 @@ and applies that band; it also reports the band with se = 0:
     python oracle/isotherm.py [--seed S] [--workers W] [--out results.json]
 
 With --device the ten points run instead as ten device-resident chains of
-the CUDA library in one batch (FP32), and the CO2 averages (the chain
+the CUDA library in one batch (FP64: the CALF-20 cell is a parallelepiped,
+which the FP32 path refuses), and the CO2 averages (the chain
 statistics report guest type 1) are checked the same way with se = 0.
 Device-resident chains refuse swap moves, so their CONTROL files drop the
 "move swap" line: with these inputs the reference accepts no swap (its test
@@ -94,7 +95,7 @@ def run_device(seed: int, moves: int):
         systems.append(F.System.load(d))
         rows.append({"point": name, "pressure_bar": p, "moves": moves or eq + steps})
     b = F.Batch(systems, [{"system": i, "seed": seed + i} for i in range(len(names))],
-                precision=F.FMC_PREC_FP32, guest_capacity=256)
+                precision=F.FMC_PREC_FP64, guest_capacity=256)
     total = rows[0]["moves"]
     t0 = time.time()
     done = 0
