@@ -169,3 +169,23 @@ def test_peng_robinson_fugacity(fmc_lib, oracle_lib, tmp_path):
     d = tmp_path / "plain"
     syn.write_inputs(str(d), spec)
     assert fmc_lib.System.load(str(d)).info().fugacity[0] == 10.0e5
+
+
+def test_reference_isotherm_inputs_load(fmc_lib, tmp_path):
+    """The ten reference isotherm inputs load in the set-up as they are (all
+    six moves, probability grids, ewald precision, CALF-20's parallelepiped
+    cell) with the guests' partial pressures as fugacities."""
+    import shutil
+    from oracle.isotherm import GOLD, control_numbers
+    base = os.path.join(GOLD, "calf20")
+    for name in sorted(os.listdir(os.path.join(base, "isotherm"))):
+        d = tmp_path / name
+        d.mkdir()
+        for f in ("CONFIG", "FIELD"):
+            shutil.copy(os.path.join(base, f), d / f)
+        ctl = os.path.join(base, "isotherm", name, "CONTROL")
+        shutil.copy(ctl, d / "CONTROL")
+        info = fmc_lib.System.load(str(d)).info()
+        assert info.ntpguest == 2 and info.imcon == 3
+        p, _, _ = control_numbers(ctl)
+        assert abs(sum(info.fugacity[:2]) - p * 1e5) < 1e-6 * p * 1e5
