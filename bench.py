@@ -5,28 +5,37 @@ Workload: the batched isotherm (64 independent chains in one persistent
 launch per cycle): 16 pressures log-spaced 0.002-1.0 bar at 293 K x 4 seeded
 synthetic frameworks (edges 25.6 / 38.4 / 51.2 / 64.0 A; 1536 / 5184 /
 12288 / 24000 atoms; kmax 7 / 10 / 12 / 18; alpha 0.24; cutoff 12.5 A),
-rigid CO2, uneven initial loadings 0-800 created on the device, equal
-insert / delete / displace / rotate mix, FP32 terms with double-float
-(~48-bit) accumulation and structure factor.
+rigid CO2, uneven initial loadings 0-800 ("create molecules", run on the
+device), equal insert / delete / displace / rotate mix, FP32 terms with
+double-float (~48-bit) accumulation and structure factor.
 
-A step is one cycle of --moves main-loop iterations on every chain.  The
-metric counts trial-move energy evaluations the way the reference spends
-them: an insertion or deletion is one evaluation, a displacement, rotation
-or translation two (old and new position).  A trial position that fails the
-1.5 A overlap test still counts (the reference's energy routine is called
-and exits early); the evaluations that ran to completion are reported
-beside it as full_evals_per_s.
+A step is one cycle of --moves main-loop iterations on every chain, always
+from the same state: the chains' state right after pre-loading is kept on
+the device (fmc_batch_snapshot) and put back before every step
+(fmc_batch_restore, outside the timed region), so every step does the same
+work and the number does not depend on --steps.  The metric counts trial-move
+energy evaluations the way the reference spends them: an insertion or
+deletion is one evaluation, a displacement, rotation or translation two (old
+and new position).  A trial position that fails the 1.5 A overlap test still
+counts (the reference's energy routine is called and exits early); the
+evaluations that ran to completion are reported beside it
+(full_evals_per_s).
+
+The CPU side runs the same 64 chains: the oracle (the FP64 restatement of
+the reference Fortran; the Fortran itself has no compiler on either
+machine) pre-loads each chain from the same seed, which gives the same
+molecules, keeps that state and replays the same cycle from it every step,
+one process per host core.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-prints one JSON line.  --impl reference times the CPU oracle (the FP64
-restatement of the reference Fortran; the Fortran itself has no compiler on
-either machine) on the host cores for the same workload.
+prints one JSON line.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -41,14 +50,30 @@ METRIC = "trial-move Î”E evals/sec on 1 GB300, batched vs plain at â‰¤1e-6 rel Î
 UNIT = "evals/s"
 RHO = 192.0 / 12.8 ** 3       # framework atoms per A^3
 GUEST_REACH = 1.16            # C-O distance of the CO2 guest
+NSITE = 3                     # CO2 sites
+WORKLOAD = ("config3 batched isotherm: 64 chains = 16 pressures 0.002-1 bar x 4 frameworks "
+            "25.6/38.4/51.2/64.0 A, CO2, FP32 terms with double-float sums and S(k); every step "
+            "replays the same cycle from the pre-loaded state")
+
+
+def n_env(cutoff: float) -> float:
+    """Unique framework atoms within rc + r_mol of a molecule."""
+    return RHO * 4.0 / 3.0 * math.pi * (cutoff + GUEST_REACH) ** 3
 
 
 def algorithmic_bytes_per_eval(cutoff: float, nk: int) -> float:
     """16 B per unique environment atom within rc + r_mol (x, y, z, q as
     float4) plus 32 B per k-vector (S(k) read and per-k constants)."""
-    import math
-    nc = RHO * 4.0 / 3.0 * math.pi * (cutoff + GUEST_REACH) ** 3
-    return 16.0 * nc + 32.0 * nk
+    return 16.0 * n_env(cutoff) + 32.0 * nk
+
+
+def algorithmic_flops_per_eval(cutoff: float, nk: int) -> float:
+    """20 flop per site and environment atom (minimum image, r^2, test), 40
+    per site and neighbour within rc (sqrt, two table interpolations, charge
+    products), 12 per site and k-vector (recurrence, charge products) and 8
+    per k-vector (S-dot, a_k)."""
+    nnb = RHO * 4.0 / 3.0 * math.pi * cutoff ** 3
+    return 20.0 * NSITE * n_env(cutoff) + 40.0 * NSITE * nnb + 12.0 * NSITE * nk + 8.0 * nk
 
 
 def trial_evals(st) -> int:
@@ -72,53 +97,125 @@ def workload(tmp: str):
 
 
 # ------------------------------------------------------------ CPU oracle arm
-def _cpu_chain(args):
-    """Run one oracle chain for `seconds` of main-loop work after its
-    pre-loading; returns (evals, moves, overlap_exits, seconds)."""
-    d, seed, create, seconds = args
+def _cpu_worker(conn, jobs, moves, core):
+    """One host process: pre-load its chains with the oracle (same seed and
+    count as the device chains), keep each state, then per command replay
+    `moves` moves of every chain from its kept state and report the work."""
     sys.path.insert(0, ROOT)
+    if core is not None:
+        try:
+            os.sched_setaffinity(0, {core})
+        except (AttributeError, OSError):
+            pass
     from oracle.binding import Oracle
-    o = Oracle(d)
-    o.seed(seed)
-    if create:
-        o.create_molecules(1, create)
-    evals = moves = full = 0
-    t0 = time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
-        for lg in o.run(50):
-            moves += 1
-            w = 1 if lg.move in (1, 2) else 2
-            evals += w
-            if not lg.overlap:
-                full += w
-    return evals, moves, full, time.perf_counter() - t0
+    sims = []
+    for d, seed, create in jobs:
+        o = Oracle(d)
+        o.seed(seed)
+        if create:
+            o.create_molecules(1, create)
+        o.save_state()
+        sims.append(o)
+    conn.send(("ready", sum(o.nummols(o.locguest(1)) for o in sims)))
+    while True:
+        cmd = conn.recv()
+        if cmd != "step":
+            break
+        evals = full = nmov = 0
+        t0 = time.perf_counter()
+        for o in sims:
+            o.restore_state()
+            for lg in o.run(moves):
+                nmov += 1
+                w = 0 if lg.move == 0 else (1 if lg.move in (1, 2) else 2)
+                evals += w
+                if not lg.overlap:
+                    full += w
+        conn.send((evals, full, nmov, time.perf_counter() - t0))
+    conn.close()
 
 
-def cpu_sample(dirs, specs, seconds: float, cores: int):
-    """A bounded sample of the workload: `cores` chains (spread over the four
-    frameworks, the lowest initial loadings so the oracle's pre-loading stays
-    short), all run concurrently on separate cores for `seconds` each."""
-    import multiprocessing as mp
-    byfw = {}
-    for s in specs:
-        byfw.setdefault(s["system"], []).append(s)
-    picks = []
-    i = 0
-    while len(picks) < cores:
-        fw = i % 4
-        lst = sorted(byfw[fw], key=lambda s: s["create_molecules"])
-        picks.append(lst[(i // 4) % len(lst)])
-        i += 1
-    jobs = [(dirs[p["system"]], p["seed"], min(p["create_molecules"], 20), seconds) for p in picks]
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_chain, jobs)
-    evals = sum(r[0] for r in res)
-    moves = sum(r[1] for r in res)
-    secs = max(r[3] for r in res)
-    sample = (f"{cores} oracle chains (4 frameworks, initial loading <= 20 CO2) run "
-              f"concurrently for {seconds:.0f} s each after pre-loading; {moves} moves")
-    return evals / secs, moves / secs, sample
+class CpuChains:
+    """The workload's chains on `procs` host processes (chains spread by an
+    estimate of their cost, largest first), each chain pre-loaded once."""
+
+    def __init__(self, dirs, specs, chain_ids, procs, moves, pin=False):
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        cost = {}
+        for c in chain_ids:
+            s = specs[c]
+            nk = (7, 10, 12, 18)[s["system"]] ** 3
+            cost[c] = nk * (1.0 + s["create_molecules"] / 100.0)
+        bins = [[] for _ in range(procs)]
+        load = [0.0] * procs
+        for c in sorted(chain_ids, key=lambda c: -cost[c]):
+            i = min(range(procs), key=lambda k: load[k])
+            bins[i].append(c)
+            load[i] += cost[c]
+        self.conns, self.procs = [], []
+        for i, b in enumerate(bins):
+            if not b:
+                continue
+            jobs = [(dirs[specs[c]["system"]], specs[c]["seed"], specs[c]["create_molecules"]) for c in b]
+            a, bconn = ctx.Pipe()
+            p = ctx.Process(target=_cpu_worker, args=(bconn, jobs, moves, i if pin else None))
+            p.start()
+            self.conns.append(a)
+            self.procs.append(p)
+        self.loaded = sum(c.recv()[1] for c in self.conns)
+        self.nchains = len(chain_ids)
+
+    def step(self):
+        """One replay of every chain; (evals, full evals, moves, wall s)."""
+        t0 = time.perf_counter()
+        for c in self.conns:
+            c.send("step")
+        res = [c.recv() for c in self.conns]
+        wall = time.perf_counter() - t0
+        return (sum(r[0] for r in res), sum(r[1] for r in res), sum(r[2] for r in res), wall)
+
+    def close(self):
+        for c in self.conns:
+            c.send("stop")
+        for p in self.procs:
+            p.join()
+
+
+def cpu_arm(dirs, specs, steps, warmup, moves, cores):
+    """The CPU oracle on all `cores` host cores, the same 64 chains and
+    pre-loaded states as the device batch; evals/s over the timed steps."""
+    cc = CpuChains(dirs, specs, list(range(len(specs))), cores, moves)
+    try:
+        for _ in range(warmup):
+            cc.step()
+        ev = fu = mv = 0
+        wall = 0.0
+        for _ in range(steps):
+            e, f, m, w = cc.step()
+            ev, fu, mv, wall = ev + e, fu + f, mv + m, wall + w
+    finally:
+        cc.close()
+    return {"value": ev / wall, "full_evals_per_s": fu / wall, "moves": mv, "seconds": wall,
+            "loaded_molecules": cc.loaded}
+
+
+def cpu_one_core(dirs, specs, moves):
+    """The oracle on one pinned core: two chains of each framework (the
+    chains 4 f + 1 and 4 f + 9 of framework f's 16 pressures), one replay."""
+    ids = []
+    for f in range(4):
+        fc = [c for c, s in enumerate(specs) if s["system"] == f]
+        ids += [fc[1], fc[9]]
+    cc = CpuChains(dirs, specs, ids, 1, moves, pin=True)
+    try:
+        cc.step()  # warm-up
+        e, f, m, w = cc.step()
+    finally:
+        cc.close()
+    return {"value": e / w, "unit": UNIT, "cores": 1, "full_evals_per_s": f / w,
+            "sample": f"oracle pinned to one core: chains {ids} (2 per framework), {m} moves "
+                      f"replayed from their pre-loaded states"}
 
 
 def oracle_built():
@@ -192,12 +289,12 @@ def measured_peak_hbm():
 
 
 def profiled_traffic():
-    """DRAM bytes (read + write) of one step's chain-kernel launches, from
-    the committed ncu summary of this workload, if present."""
+    """DRAM bytes (read + write) per chain-kernel launch of this workload,
+    from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "chain_kernel_config3.json")
     try:
         with open(p) as f:
-            return json.load(f).get("dram_bytes_per_step")
+            return json.load(f).get("dram_bytes_per_launch")
     except Exception:
         return None
 
@@ -215,78 +312,130 @@ def reduce_over_ranks(dist, device, max_vals, sum_vals):
     return [float(x) for x in t.tolist()], [float(x) for x in e.tolist()]
 
 
-def plain_single_chain(F, seconds: float = 2.0):
-    """The single-chain GPU paths the batched kernel is compared with, on
-    config 1 (25.6 A, 1536 atoms, kmax 7, P 0.1 bar, one CTA):
-    - "device": one chain run by the persistent kernel (FP32);
-    - "per_move_abi": the drop-in path, one C-ABI call per trial insertion /
-      deletion and one per commit, driven from the host (FP64, random
-      positions from numpy), the way a Fortran host would call it.
-    Both in trial-move Î”E evaluations per second."""
+def plain_paths(F, batch, systems, specs, snap_stats, moves, clusters):
+    """The single-chain GPU paths on the same workload and states:
+    - "device": every chain run alone (the others paused), from its
+      pre-loaded state, on the cluster size that is fastest for a lone chain
+      of its framework (4 or 8 CTAs, tried on one chain per framework);
+    - "per_move_abi": the drop-in, one C-ABI call per trial move and one per
+      commit driven from the host (FP64; insert / delete / displace / rotate
+      in equal shares with numpy draws), on one chain per framework loaded
+      with that chain's molecules, ~1 s each.
+    Both in trial-move evaluations per second."""
     import numpy as np
-    from fastmc_gb300 import synthetic as syn
-    d = tempfile.mkdtemp()
-    syn.write_inputs(d, syn.config1())
-    sysm = F.System.load(d)
     out = {}
-    b = F.Batch([sysm], [{"seed": 1}], precision=F.FMC_PREC_FP32, guest_capacity=1024)
-    b.run(256)
-    s0 = b.stats()[0]
-    t0 = time.perf_counter()
-    dev_ms = 0.0
-    while time.perf_counter() - t0 < seconds:
-        b.run(1024)
-        dev_ms += b.last_timing()[0]
-    s1 = b.stats()[0]
-    out["device"] = {"value": (trial_evals(s1) - trial_evals(s0)) / (dev_ms / 1000.0), "unit": UNIT,
-                     "workload": "config1 one chain, FP32, device-resident"}
-    p = F.PlainEngine(sysm, F.FMC_PREC_FP64, 1024)
+    n = len(specs)
+    best = {}
+    for f in range(len(systems)):
+        c = [i for i, s in enumerate(specs) if s["system"] == f][8]
+        tbest = None
+        for cs in (4, 8):
+            sizes = [0] * n
+            sizes[c] = cs
+            batch.set_chain_cluster(sizes)
+            batch.restore()
+            batch.run(moves)
+            ms = batch.last_timing()[0]
+            if tbest is None or ms < tbest:
+                tbest, best[f] = ms, cs
+    ev = 0
+    ms_tot = 0.0
+    for c in range(n):
+        sizes = [0] * n
+        sizes[c] = best[specs[c]["system"]]
+        batch.set_chain_cluster(sizes)
+        batch.restore()
+        st = batch.run(moves)
+        ev += trial_evals(st[c]) - trial_evals(snap_stats[c])
+        ms_tot += batch.last_timing()[0]
+    batch.set_chain_cluster(clusters)
+    batch.restore()
+    out["device"] = {"value": ev / (ms_tot / 1000.0), "unit": UNIT,
+                     "workload": "the same 64 chains and states, one chain at a time (FP32, "
+                                 "device-resident), cluster per framework " +
+                                 str([best[f] for f in range(len(systems))])}
     rng = np.random.default_rng(1)
-    n = evals = 0
-    t0 = time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
-        if n == 0 or rng.random() < 0.5:
-            ax = rng.normal(size=3)
-            ax /= np.linalg.norm(ax)
-            xyz = np.outer([0.0, 1.16, -1.16], ax) + rng.uniform(0, 25.6, 3)
-            p.insertion(1, xyz)
-        else:
-            p.deletion(1, int(rng.integers(1, n + 1)))
-        evals += 1
-        p.commit(float(rng.random()))
-        n = p.nummols(1)
-    out["per_move_abi"] = {"value": evals / (time.perf_counter() - t0), "unit": UNIT,
-                           "workload": "config1 one chain, FP64, host-driven per-move C ABI "
-                                       "(insert/delete, wall time)"}
+    tot_ev, tot_s = 0, 0.0
+    for f in range(len(systems)):
+        c = [i for i, s in enumerate(specs) if s["system"] == f][8]
+        x, m = batch.coords(c)
+        L = systems[f].info().cell[0]
+        p = F.PlainEngine(systems[f], F.FMC_PREC_FP64, 1024)
+        for mol in x[:9 * m].reshape(m, 3, 3):
+            p.insertion(1, mol)
+            p.commit(0.0)
+        nm = p.nummols(1)
+        t0 = time.perf_counter()
+        evals = 0
+        while time.perf_counter() - t0 < 1.0:
+            k = int(rng.integers(4)) if nm else 0
+            if k == 0:
+                ax = rng.normal(size=3)
+                ax /= np.linalg.norm(ax)
+                p.insertion(1, np.outer([0.0, 1.16, -1.16], ax) + rng.uniform(0, L, 3))
+                evals += 1
+            elif k == 1:
+                p.deletion(1, int(rng.integers(1, nm + 1)))
+                evals += 1
+            else:
+                th = rng.uniform(0, math.pi / 3)
+                ax = rng.normal(size=3)
+                ax /= np.linalg.norm(ax)
+                sh = rng.uniform(-0.25, 0.25, 3) if k == 2 else np.zeros(3)
+                p.displace(1, int(rng.integers(1, nm + 1)),
+                           [*sh, math.cos(th / 2), *(math.sin(th / 2) * ax)])
+                evals += 2
+            p.commit(float(rng.random()))
+            nm = p.nummols(1)
+        tot_s += time.perf_counter() - t0
+        tot_ev += evals
+        p.close()
+    out["per_move_abi"] = {"value": tot_ev / tot_s, "unit": UNIT,
+                           "workload": "chain 8 of each framework, its pre-loaded molecules, FP64, "
+                                       "host-driven per-move C ABI (insert/delete/displace/rotate), "
+                                       "wall time"}
     return out
 
 
+def config5_widom(F, tmp):
+    """Config 5's test insertions: 1e7 Widom trials (a 100^3 grid x 10
+    orientations, one launch) against the 102.4 A framework (98304 atoms,
+    cutoff 14 A, kmax 20) with 2000 CO2 loaded, FP32 terms."""
+    from fastmc_gb300 import synthetic as syn
+    d = os.path.join(tmp, "config5")
+    syn.write_inputs(d, syn.config5())
+    sysm = F.System.load(d)
+    b = F.Batch([sysm], [{"seed": 5}], precision=F.FMC_PREC_FP32, guest_capacity=2048)
+    b.widom_grid(0, (10, 10, 10), 1, seed=1)  # warm-up
+    t0 = time.perf_counter()
+    h, nok, ntot = b.widom_grid(0, (100, 100, 100), 10, seed=2)
+    s = time.perf_counter() - t0
+    return {"value": ntot / s, "unit": "trial insertions/s", "trials": ntot,
+            "non_overlapping": nok, "henry": h, "seconds": s,
+            "workload": "config5: 102.4 A, 98304 atoms, 2000 CO2, cutoff 14 A, kmax 20, FP32"}
+
+
 # ------------------------------------------------------------------ arms
-WORKLOAD = ("config3 batched isotherm: 64 chains = 16 pressures 0.002-1 bar x 4 frameworks "
-            "25.6/38.4/51.2/64.0 A, CO2, FP32 terms with double-float sums and S(k)")
-
-
 def run_reference(args, rank, world):
     if rank != 0:
         return
     oracle_built()
+    cores = os.cpu_count() or 1
     with tempfile.TemporaryDirectory() as tmp:
-        chains, dirs, specs = workload(tmp)
-        cores = os.cpu_count() or 1
-        per = max(2.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
-        vals = []
-        for i in range(args.warmup + args.steps):
-            v, mv, sample = cpu_sample(dirs, specs, per, cores)
-            if i >= args.warmup:
-                vals.append(v)
-        value = statistics.mean(vals)
+        _, dirs, specs = workload(tmp)
+        r = cpu_arm(dirs, specs, args.steps, args.warmup, args.moves, cores)
+    value = r["value"]
+    sample = (f"the oracle on {cores} processes: the same 64 chains, each pre-loaded from its seed "
+              f"({r['loaded_molecules']} molecules), {args.moves} moves replayed from that state per "
+              f"step; {r['moves']} timed moves")
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": per * 1000.0, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "chains": 64,
-                   "sample": "CPU oracle chains of the same 4 frameworks, all host cores"},
+        "ms_per_step": 1000.0 * r["seconds"] / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "chains": len(specs), "moves_per_step_per_chain": args.moves,
+                   "same_config": True},
+        "full_evals_per_s": r["full_evals_per_s"],
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -298,15 +447,20 @@ def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
 
-    cpu = None
+    cpu = cpu1 = None
+    tmp = tempfile.mkdtemp()
+    chains, dirs, specs = workload(tmp)
     if rank == 0 and not args.no_cpu:
-        # the CPU baseline runs first, in spawned processes, before CUDA starts
+        # the CPU baselines run first, in spawned processes, before CUDA starts
         oracle_built()
-        with tempfile.TemporaryDirectory() as tmp:
-            _, dirs, specs = workload(tmp)
-            cores = os.cpu_count() or 1
-            v, mv, sample = cpu_sample(dirs, specs, args.cpu_seconds, cores)
-            cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cores = os.cpu_count() or 1
+        r = cpu_arm(dirs, specs, args.cpu_steps, 1, args.moves, cores)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": cores, "kind": "port",
+               "full_evals_per_s": r["full_evals_per_s"],
+               "sample": f"the oracle on {cores} processes, the same 64 chains and pre-loaded states "
+                         f"({r['loaded_molecules']} molecules), {args.cpu_steps} replays of the "
+                         f"{args.moves}-move cycle ({r['moves']} moves, {r['seconds']:.1f} s)"}
+        cpu1 = cpu_one_core(dirs, specs, args.moves)
 
     torch.cuda.set_device(local_rank)
     import fastmc_gb300 as F
@@ -318,13 +472,12 @@ def run_ours(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    tmp = tempfile.mkdtemp()
-    chains, dirs, specs = workload(tmp)
     for s in specs:  # replicas: every rank runs its own seeded copy of the batch
         s["seed"] += 100000 * rank
     systems = [F.System.load(d) for d in dirs]
     infos = [s.info() for s in systems]
     batch = F.Batch(systems, specs, precision=F.FMC_PREC_FP32, guest_capacity=1024)
+    batch.snapshot()  # the pre-loaded state every step starts from
     # CTAs per chain, from timed trial cycles (the chains' state is restored
     # afterwards); set-up, outside the timing
     if args.chain_clusters:
@@ -335,21 +488,19 @@ def run_ours(args, rank, world, local_rank):
         batch.autotune(args.moves)
     per_chain = batch.chain_cluster()
     clusters = [max(v for v, s in zip(per_chain, specs) if s["system"] == i) for i in range(len(systems))]
+    batch.restore()
+    snap = batch.stats()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
-
-    # per step: the host uploads the chains' fugacities (pinned-free host
-    # array) and reads every chain's statistics back through the C ABI;
-    # the kernel time comes from CUDA events around the cycle's graph
     fug = np.array([s["pressure_pa"] for s in specs], dtype=np.float64)
 
-    def step(timed_ms, wall):
-        flush.zero_()
+    def step(ms_list, wall):
+        batch.restore()   # the same starting state for every step
+        flush.zero_()     # and a cold L2
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st = batch.run(args.moves, fugacity=fug)
+        st = batch.run(args.moves, fugacity=fug)  # public call: fugacities up, records down
         wall.append(time.perf_counter() - t0)
-        ms, ev, mv = batch.last_timing()
-        timed_ms.append(ms)
+        ms_list.append(batch.last_timing()[0])   # CUDA events around the cycle's graph
         return st
 
     clocks = ClockSampler(local_rank)
@@ -357,72 +508,120 @@ def run_ours(args, rank, world, local_rank):
     time.sleep(0.5)  # nvidia-smi's start-up
     for _ in range(args.warmup):
         step([], [])
-    before = batch.stats()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     t_start = time.time()
     ms_list, wall = [], []
     for _ in range(args.steps):
-        step(ms_list, wall)
+        after = step(ms_list, wall)
     torch.cuda.synchronize()
     t_end = time.time()
     clk = clocks.stop(t_start, t_end)
-    after = batch.stats()
-    evals = sum(trial_evals(after[c]) - trial_evals(before[c]) for c in range(len(specs)))
-    full = sum(after[c].evals - before[c].evals for c in range(len(specs)))
-    moves = sum(after[c].moves - before[c].moves for c in range(len(specs)))
+    # per step (every step does the same work from the same state)
+    n = len(specs)
+    ev1 = sum(trial_evals(after[c]) - trial_evals(snap[c]) for c in range(n))
+    full1 = sum(after[c].evals - snap[c].evals for c in range(n))
+    mv1 = sum(after[c].moves - snap[c].moves for c in range(n))
+    ovl1 = sum(after[c].overlap_exits - snap[c].overlap_exits for c in range(n))
     dev_ms = sum(ms_list)
     e2e_s = sum(wall)
     (dev_ms, e2e_s), (evals, moves, full) = reduce_over_ranks(
-        dist, "cuda", [dev_ms, e2e_s], [evals, moves, full])
+        dist, "cuda", [dev_ms, e2e_s], [ev1 * args.steps, mv1 * args.steps, full1 * args.steps])
     value = evals / (dev_ms / 1000.0)
 
-    # roofline of the chain kernel: algorithmic bytes of the completed
-    # evaluations per launch over the mean launch time
-    alg = 0.0
-    for c in range(len(specs)):
+    # rooflines of the chain kernel (the only kernel in the timed step):
+    # algorithmic bytes and flops of the completed evaluations per step over
+    # the mean step time
+    alg_b = alg_f = 0.0
+    for c in range(n):
         inf = infos[specs[c]["system"]]
-        alg += (after[c].evals - before[c].evals) * algorithmic_bytes_per_eval(inf.rcut, inf.newld)
-    per_launch_bytes = alg / args.steps
-    mean_launch_s = (sum(ms_list) / len(ms_list)) / 1000.0
-    achieved = per_launch_bytes / mean_launch_s / 1e9
+        fe = after[c].evals - snap[c].evals
+        alg_b += fe * algorithmic_bytes_per_eval(inf.rcut, inf.newld)
+        alg_f += fe * algorithmic_flops_per_eval(inf.rcut, inf.newld)
+    mean_s = (sum(ms_list) / len(ms_list)) / 1000.0
+    achieved = alg_b / mean_s / 1e9
     peak, peak_kind = measured_peak_hbm()
+    import ctypes as C
+    from fastmc_gb300 import _lib as L
+    fp32 = C.c_double()
+    L.check(L.load().fmc_measure_fp32_peak(C.byref(fp32)))
 
     h2d, d2h = batch.cycle_bytes()  # fugacities up, chain state records down
+    loads = [snap[c].nummols for c in range(n)]
 
     if rank == 0:
-        ovl = sum(after[c].overlap_exits - before[c].overlap_exits for c in range(len(specs)))
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded frameworks and guests, no dataset)",
             "config": {"workload": WORKLOAD,
-                       "chains": len(specs), "moves_per_step_per_chain": args.moves,
+                       "chains": n, "moves_per_step_per_chain": args.moves,
                        "parallelism": f"replicas x{world}",
                        "ctas_per_chain_by_framework": clusters,  # the largest per framework
                        "ctas_per_chain": per_chain,
+                       "molecules_at_step_start": {"total": sum(loads), "max": max(loads),
+                                                   "mean": sum(loads) / n},
+                       "same_config": True,
                        "l2": "flushed (256 MB write) before every timed step"},
             "trial_moves_per_s": moves / (dev_ms / 1000.0),
             "full_evals_per_s": full / (dev_ms / 1000.0),
-            "overlap_exits_per_step": ovl / args.steps,
+            "overlap_exits_per_step": ovl1,
             # one chain-kernel launch per cluster-size group per step
             "gpu_launches": args.steps * len(set(per_chain)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profiled_traffic(),
                          "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": per_launch_bytes},
+                         "algorithmic_bytes_per_launch": alg_b},
+            "roofline_flops": {"achieved": alg_f / mean_s / 1e12, "peak": fp32.value,
+                               "unit": "TFLOP/s", "frac": alg_f / mean_s / 1e12 / fp32.value,
+                               "peak_source": "FP32 FMA loop measured in this run "
+                                              "(fmc_measure_fp32_peak)",
+                               "algorithmic_flops_per_launch": alg_f},
             "clocks": clk,
             "e2e": {"value": evals / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "cpu_baseline": cpu,
+            "cpu_baseline_1core": cpu1,
         }
         if not args.no_plain:
-            out["plain_single_chain"] = plain_single_chain(F)
+            out["plain_single_chain"] = plain_paths(F, batch, systems, specs, snap, args.moves,
+                                                    per_chain)
+        if args.widom:
+            out["config5_widom"] = config5_widom(F, tmp)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def profile_case(args):
+    """A small fixed workload for ncu captures of the chain kernel: the
+    first `--chains` chains (from `--first`) of one framework with their
+    initial loadings, `--launches` cycles of `--moves` moves, printing the
+    device time of each.  Launches in order: the pre-loading launch (when
+    the chains pre-load guests), then one chain-kernel launch per cycle, so
+    `ncu -k regex:chain_kernel -s 2 -c 1` captures the second cycle."""
+    import fastmc_gb300 as F
+    from fastmc_gb300 import build
+    from fastmc_gb300 import synthetic as syn
+    build.build()
+    chains = syn.config3_chains()
+    sel = [(i, c) for i, c in enumerate(chains) if c.fw_seed == args.framework]
+    sel = sel[args.first:args.first + args.chains]
+    d = os.path.join(tempfile.mkdtemp(), "fw")
+    syn.write_inputs(d, sel[0][1])
+    sysm = F.System.load(d)
+    specs = [{"system": 0, "pressure_pa": c.pressure_bar * 1e5, "seed": 1000 + i,
+              "create_molecules": c.create_molecules} for i, c in sel]
+    prec = F.FMC_PREC_FP64 if args.fp64 else F.FMC_PREC_FP32
+    b = F.Batch([sysm], specs, precision=prec, guest_capacity=1024)
+    b.set_cluster([args.cluster])
+    for it in range(args.launches):
+        st = b.run(args.moves)
+        ms, ev, mv = b.last_timing()
+        print(f"launch {it}: {ms:.3f} ms, {mv} moves, {ev} full evaluations, "
+              f"N = {[s.nummols for s in st]}", flush=True)
 
 
 def main():
@@ -432,14 +631,26 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--moves", type=int, default=256)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-steps", type=int, default=3, help="timed replays of the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
+    ap.add_argument("--widom", action="store_true", help="also time config 5's 1e7 Widom trials")
     ap.add_argument("--chain-clusters", default="", help="CTAs per chain, one value per chain")
     ap.add_argument("--clusters", default="", help="CTAs per chain per framework, e.g. 1,2,2,4 "
                     "(default: autotuned)")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run the small profiling workload below instead of the benchmark")
+    ap.add_argument("--framework", type=int, default=4, choices=[1, 2, 3, 4])
+    ap.add_argument("--chains", type=int, default=1)
+    ap.add_argument("--first", type=int, default=0, help="first chain of the framework")
+    ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--fp64", action="store_true")
+    ap.add_argument("--cluster", type=int, default=1, help="CTAs per chain (1..8)")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -136,6 +136,10 @@ SIGNATURES = {
     "fmc_adjoint_destroy": (C.c_int, [vp]),
     "fmc_batch_get_chain_cluster": (C.c_int, [vp, ip, C.c_int]),
     "fmc_batch_prob_grid": (C.c_int, [vp, C.c_int, C.c_int, dp, C.c_int64]),
+    "fmc_alloc_count": (C.c_int, [i64p, i64p]),
+    "fmc_measure_fp32_peak": (C.c_int, [dp]),
+    "fmc_batch_snapshot": (C.c_int, [vp]),
+    "fmc_batch_restore": (C.c_int, [vp]),
 }
 
 _lib = None

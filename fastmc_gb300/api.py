@@ -244,6 +244,14 @@ class Batch:
         L.check(L.load().fmc_batch_autotune(self._h, nmoves, a, n))
         return list(a)
 
+    def snapshot(self) -> None:
+        """Keep a device copy of every chain's state (fmc_batch_snapshot)."""
+        L.check(L.load().fmc_batch_snapshot(self._h))
+
+    def restore(self) -> None:
+        """Put the last snapshot back (fmc_batch_restore)."""
+        L.check(L.load().fmc_batch_restore(self._h))
+
     def save(self, path: str) -> None:
         """Checkpoint every chain's device state for an exact resume."""
         L.check(L.load().fmc_batch_save(self._h, os.fsencode(path)))

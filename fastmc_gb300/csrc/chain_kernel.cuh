@@ -105,6 +105,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     B.ev.rank = rank;
     B.ev.csize = csize;
+    B.ev.tabpos = mode == kModeWidom ? 1 : 2;
     B.xseq = B.cseq = 0u;
     B.cflag = 0u;
   }

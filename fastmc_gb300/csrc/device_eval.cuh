@@ -49,6 +49,12 @@ struct EvalSmem {
   int glist[F32 ? kGList : 1];
   int gcount;
   int rank, csize;          // this CTA's place in the chain's cluster
+  // positions the (l, m) table is sized for when deciding whether it is
+  // used: 2 wherever S(k) is committed, so that a site's s(k) comes out of
+  // the same arithmetic whether one or two positions are evaluated and the
+  // running S(k) stays the exact sum of its molecules' terms; 1 for Widom
+  // trials, which commit nothing
+  int tabpos;
   int red_i[kWarps + 1];
   double red[kWarps * 32];
   double out[64];
@@ -617,7 +623,7 @@ __device__ void build_powers(const SysDev &S, EvalSmem<F32> &sm, int npos, int n
   if constexpr (F32) {
     // (l, m) products, so the k loop needs one complex product per site
     const int w = 2 * k2 + 1, nlm = (k1 + 1) * w;
-    if (npos * ns * nlm <= kPlmMax) {
+    if (sm.tabpos * ns * nlm <= kPlmMax) {
       __syncthreads();
       for (int e = threadIdx.x; e < nlm; e += kThreads) {
         const int l = e / w, mm = e - l * w - k2, am = abs(mm);

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
@@ -9,6 +10,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "engine.cuh"
@@ -88,6 +90,23 @@ __global__ void __launch_bounds__(kThreads) structure_factor_kernel(
   }
 }
 
+// FP32 issue-rate probe: 16 independent FMA chains per thread, so that the
+// FMA pipes, not their latency, bound it (2 flops per FMA).
+constexpr int kProbeChains = 16;
+__global__ void __launch_bounds__(256) fma_probe_kernel(float *out, int iters, float b, float c) {
+  float a[kProbeChains];
+#pragma unroll
+  for (int j = 0; j < kProbeChains; ++j) a[j] = (float)(threadIdx.x + j) * 1e-6f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < kProbeChains; ++j) a[j] = fmaf(a[j], b, c);
+  }
+  float t = 0.f;
+#pragma unroll
+  for (int j = 0; j < kProbeChains; ++j) t += a[j];
+  if (t == 12345.678f) out[0] = t;  // keeps the loop; practically never stores
+}
+
 // The chain kernel's instantiations (chain_f32_g1.cu, chain_f32_g4.cu,
 // chain_f64.cu): launch wrappers, shared-memory set-up, cluster occupancy.
 template <bool F32, int GN>
@@ -119,6 +138,10 @@ constexpr int kModeCommit = 3;
 constexpr int kModeWidom = 4;
 
 // ----------------------------------------------------- device allocations
+// Every cudaMalloc / cudaFree the library makes goes through DBuf and is
+// counted here (fmc_alloc_count).
+std::atomic<long long> g_dev_allocs{0}, g_dev_frees{0};
+
 template <class T>
 struct DBuf {
   T *p = nullptr;
@@ -126,14 +149,21 @@ struct DBuf {
   DBuf() = default;
   DBuf(const DBuf &) = delete;
   DBuf &operator=(const DBuf &) = delete;
-  ~DBuf() {
-    if (p) cudaFree(p);
+  ~DBuf() { release(); }
+  void release() {
+    if (p) {
+      cudaFree(p);
+      g_dev_frees.fetch_add(1);
+    }
+    p = nullptr;
   }
   void alloc(size_t count) {
-    if (p) cudaFree(p);
-    p = nullptr;
+    release();
     n = count;
-    if (count) FMC_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    if (count) {
+      FMC_CUDA(cudaMalloc(&p, count * sizeof(T)));
+      g_dev_allocs.fetch_add(1);
+    }
   }
   void upload(const std::vector<T> &v) {
     alloc(v.size());
@@ -642,6 +672,7 @@ struct Chains {
   DBuf<double> ctl_fuga;
   ChainArrays CA{};
   int nchains = 0, precision = 0, logcap = 0, maxmls = 0;
+  int device = -1;  // the CUDA device the chains were created on
   int gn = kMaxG;  // guest-type capacity of the kernel's accumulators (1 or kMaxG)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -712,9 +743,15 @@ struct Chains {
 
   // Regroup the chains after a change of their cluster sizes: one launch
   // (graph branch) per distinct size.
+  // Size 0 pauses a chain: it is left out of the launches until it gets a
+  // size again.
   void set_chain_clusters(const std::vector<int> &cc) {
-    for (int v : cc)
-      if (v < 1 || v > kMaxCluster) raise(FMC_ERR_ARG, "cluster size must be 1..8");
+    int active = 0;
+    for (int v : cc) {
+      if (v < 0 || v > kMaxCluster) raise(FMC_ERR_ARG, "cluster size must be 0..8");
+      active += v > 0;
+    }
+    if (active == 0) raise(FMC_ERR_ARG, "every chain paused");
     for (auto &g : groups) {
       if (g->done) cudaEventDestroy(g->done);
       if (g->stream) cudaStreamDestroy(g->stream);
@@ -747,7 +784,7 @@ struct Chains {
 
   void launch(int mode, int nmoves) {
     headers_stale = true;
-    if (groups.size() <= 1 && (groups.empty() || groups[0]->csize == 1)) {
+    if (groups.empty() || (groups.size() == 1 && groups[0]->csize == 1 && groups[0]->n == nchains)) {
       FMC_CUDA(launch_one(nchains, 1, nullptr, stream, mode, nmoves));
       return;
     }
@@ -818,6 +855,7 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   if (cap < 1 || cap > 4096) raise(FMC_ERR_ARG, "guest capacity must be in 1..4096");
   C.nchains = nchains;
   C.precision = precision;
+  FMC_CUDA(cudaGetDevice(&C.device));
   int nkmax = 1, maxmls = 1;
   for (int i = 0; i < nsys; ++i) {
     if (!systems[i]) raise(FMC_ERR_ARG, "null system");
@@ -1104,6 +1142,7 @@ struct fmc_plain {
 
 struct fmc_batch {
   Chains C;
+  std::unique_ptr<ChainSnapshot> snap;  // fmc_batch_snapshot
 };
 
 // Device copy of every chain's mutable state (for trial runs).
@@ -1163,17 +1202,91 @@ static void ckpt_write(std::FILE *f, const DBuf<T> &d) {
     raise(FMC_ERR_ARG, "checkpoint write failed");
 }
 
+// One array of the checkpoint into host memory; its length must match the
+// batch's device array.
 template <class T>
-static void ckpt_read(std::FILE *f, DBuf<T> &d) {
+static void ckpt_read(std::FILE *f, const DBuf<T> &d, std::vector<T> &h) {
   unsigned long long n = 0;
   if (std::fread(&n, sizeof n, 1, f) != 1 || n != d.n)
     raise(FMC_ERR_INPUT, "checkpoint does not match this batch (array size)");
-  std::vector<T> h(n);
+  h.resize(n);
   if (n && std::fread(h.data(), sizeof(T), n, f) != n) raise(FMC_ERR_INPUT, "checkpoint truncated");
-  if (n) FMC_CUDA(cudaMemcpy(d.p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+template <class T>
+static void ckpt_upload(DBuf<T> &d, const std::vector<T> &h) {
+  if (!h.empty()) FMC_CUDA(cudaMemcpy(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+// Every index a kernel takes from a chain record, order list or free list
+// of a checkpoint is in range for this batch (the kernels trust them).
+static void validate_headers(const Chains &C, const std::vector<ChainHdr> &hdr,
+                             const std::vector<int> &ord, const std::vector<int> &freel) {
+  const int cap = C.CA.cap;
+  auto bad = [](int c, const char *what) {
+    raise(FMC_ERR_INPUT, "checkpoint chain " + std::to_string(c) + ": " + what);
+  };
+  for (int c = 0; c < C.nchains; ++c) {
+    const ChainHdr &h = hdr[c];
+    if (h.system < 0 || h.system >= (int)C.sys.size()) bad(c, "refers to a missing system");
+    const System &s = *C.hsys[h.system];
+    if (h.ir < 1 || h.ir > 97 || h.jr < 1 || h.jr > 97) bad(c, "generator lags out of range");
+    if (h.rhead < 0 || h.rhead >= kRBuf || h.ravail < 0 || h.ravail > kRBuf)
+      bad(c, "generator buffer position out of range");
+    if (h.log_n < 0) bad(c, "negative log position");
+    for (int g = 0; g < kMaxG; ++g) {
+      const int n = h.nummols[g], ns = h.nslots[g], nf = h.nfree[g];
+      if (n < 0 || ns < 0 || nf < 0 || n > cap || ns > cap || nf > cap || n + nf > ns)
+        bad(c, "guest counts out of range");
+      if (g >= s.ntpguest && (n || ns || nf)) bad(c, "molecules of a guest type the system lacks");
+      if (h.skb[g] != 0 && h.skb[g] != 1) bad(c, "structure-factor buffer flag not 0 or 1");
+      const size_t base = ((size_t)c * kMaxG + g) * cap;
+      for (int i = 0; i < n; ++i)
+        if (ord[base + i] < 0 || ord[base + i] >= ns) bad(c, "molecule order entry out of range");
+      for (int i = 0; i < nf; ++i)
+        if (freel[base + i] < 0 || freel[base + i] >= ns) bad(c, "free-list entry out of range");
+    }
+  }
 }
 
 extern "C" {
+
+int fmc_alloc_count(int64_t *allocs, int64_t *frees) {
+  if (allocs) *allocs = g_dev_allocs.load();
+  if (frees) *frees = g_dev_frees.load();
+  return FMC_OK;
+}
+
+int fmc_measure_fp32_peak(double *tflops) {
+  return guard([&] {
+    if (!tflops) raise(FMC_ERR_ARG, "null argument");
+    ensure_device();
+    int dev = 0, nsm = 1;
+    FMC_CUDA(cudaGetDevice(&dev));
+    FMC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    DBuf<float> out;
+    out.alloc(1);
+    cudaEvent_t e0, e1;
+    FMC_CUDA(cudaEventCreate(&e0));
+    FMC_CUDA(cudaEventCreate(&e1));
+    const int blocks = nsm * 8, threads = 256, iters = 1 << 14;
+    double best = 0.0;
+    for (int r = 0; r < 4; ++r) {  // the first launch warms the clocks up
+      FMC_CUDA(cudaEventRecord(e0));
+      fma_probe_kernel<<<blocks, threads>>>(out.p, iters, 0.999999f, 1e-7f);
+      FMC_CUDA(cudaEventRecord(e1));
+      FMC_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      FMC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      const double flops = 2.0 * kProbeChains * (double)iters * blocks * threads;
+      best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
+    return FMC_OK;
+  });
+}
 
 int fmc_last_error(char *buf, int len) {
   int n = (int)g_error.size();
@@ -2017,20 +2130,52 @@ int fmc_batch_load(fmc_batch *b, const char *path) {
     if (std::memcmp(meta, want, sizeof meta) != 0)
       raise(FMC_ERR_INPUT, "checkpoint does not match this batch (chains, systems, capacity, "
                            "k-vectors, precision or library version)");
-    ckpt_read(f.get(), C.hdr);
-    ckpt_read(f.get(), C.gpos);
-    ckpt_read(f.get(), C.ghi);
-    ckpt_read(f.get(), C.glo);
-    ckpt_read(f.get(), C.ord);
-    ckpt_read(f.get(), C.freel);
-    ckpt_read(f.get(), C.sk);
-    ckpt_read(f.get(), C.skdf);
-    ckpt_read(f.get(), C.grid);
+    // everything is read and checked before anything reaches the device, so
+    // a rejected file leaves the batch as it was
+    std::vector<ChainHdr> hdr;
+    std::vector<double> gpos, grid;
+    std::vector<float4> ghi, glo, skdf;
+    std::vector<int> ord, freel;
+    std::vector<double2> sk;
+    ckpt_read(f.get(), C.hdr, hdr);
+    ckpt_read(f.get(), C.gpos, gpos);
+    ckpt_read(f.get(), C.ghi, ghi);
+    ckpt_read(f.get(), C.glo, glo);
+    ckpt_read(f.get(), C.ord, ord);
+    ckpt_read(f.get(), C.freel, freel);
+    ckpt_read(f.get(), C.sk, sk);
+    ckpt_read(f.get(), C.skdf, skdf);
+    ckpt_read(f.get(), C.grid, grid);
+    validate_headers(C, hdr, ord, freel);
+    ckpt_upload(C.hdr, hdr);
+    ckpt_upload(C.gpos, gpos);
+    ckpt_upload(C.ghi, ghi);
+    ckpt_upload(C.glo, glo);
+    ckpt_upload(C.ord, ord);
+    ckpt_upload(C.freel, freel);
+    ckpt_upload(C.sk, sk);
+    ckpt_upload(C.skdf, skdf);
+    ckpt_upload(C.grid, grid);
     C.headers_stale = true;
     C.pull_headers();
-    for (int c = 0; c < C.nchains; ++c)
-      if (C.host_hdr[c].system < 0 || C.host_hdr[c].system >= (int)C.sys.size())
-        raise(FMC_ERR_INPUT, "checkpoint chain refers to a missing system");
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_snapshot(fmc_batch *b) {
+  return guard([&] {
+    if (!b) raise(FMC_ERR_ARG, "null batch");
+    if (!b->snap) b->snap = std::make_unique<ChainSnapshot>();
+    save_state(b->C, *b->snap);
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_restore(fmc_batch *b) {
+  return guard([&] {
+    if (!b) raise(FMC_ERR_ARG, "null batch");
+    if (!b->snap) raise(FMC_ERR_STATE, "no snapshot taken (fmc_batch_snapshot)");
+    restore_state(b->C, *b->snap);  // the saved records select the first S(k) buffer
     return FMC_OK;
   });
 }
@@ -2227,9 +2372,16 @@ int fmc_full_ewald_noalloc(fmc_plain *h, double *out4) {
       raise(FMC_ERR_ARG, buf);
     }
     if (s.ntpguest > kMaxG) raise(FMC_ERR_ARG, "too many guest types");
+    int cur = -1;
+    FMC_CUDA(cudaGetDevice(&cur));
+    if (cur != C.device)
+      raise(FMC_ERR_ARG, "fmc_full_ewald_noalloc: call with device " + std::to_string(C.device) +
+                             " (the engine's) current, not device " + std::to_string(cur));
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     double *scr = noalloc_scratch();
     // guest counts and system charge of chain 0, straight from its header
+    static_assert(sizeof(ChainHdr::nummols) == sizeof(int) * kMaxG, "nummols layout");
+    static_assert(std::is_same<decltype(ChainHdr::sumchg), double>::value, "sumchg type");
     int nummols[kMaxG] = {};
     double sumchg = 0.0;
     const char *hdr0 = reinterpret_cast<const char *>(C.hdr.p);

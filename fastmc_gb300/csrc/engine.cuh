@@ -1115,7 +1115,7 @@ __device__ __forceinline__ void kspace(BlockShared<F32> &B, const ChainArrays &C
     float4 *sknext = (B.H.skb[mc.g] ? CA.skdf : CA.skdf2) + ((size_t)chain * kMaxG + mc.g) * CA.nkmax;
     const int kind = mc.kind;
     const int k2 = S.kmax[1], w = 2 * k2 + 1, nlm = (S.kmax[0] + 1) * w;
-    const bool tab = npos * ns * nlm <= kPlmMax;
+    const bool tab = B.ev.tabpos * ns * nlm <= kPlmMax;  // independent of npos (EvalSmem::tabpos)
     unsigned mixmask = 0;  // guest types of another molecule type (mixing terms)
     for (int g2 = 0; g2 < NG && g2 < GN; ++g2)
       if (S.g[g2].mol != mol) mixmask |= 1u << g2;

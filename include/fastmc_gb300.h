@@ -66,6 +66,17 @@ int fmc_last_error(char *buf, int len);
 /* Library version string, e.g. "fastmc_gb300 1.0 sm_103a". */
 const char *fmc_version(void);
 
+/* Device allocations (cudaMalloc) and frees (cudaFree) the library has made
+ * since it was loaded, over all handles and threads.  A diagnostic with no
+ * counterpart in the reference. */
+int fmc_alloc_count(int64_t *allocs, int64_t *frees);
+
+/* FP32 FMA throughput of the current device (TFLOP/s, 2 flops per FMA,
+ * best of a few launches of an FMA loop on every SM): the denominator of the
+ * chain kernel's flop roofline.  A measurement helper with no counterpart in
+ * the reference. */
+int fmc_measure_fp32_peak(double *tflops);
+
 /* ------------------------------------------------------------- set-up --
  * Replaces: initscan (utility_pack.f:207-508), readfield
  * (readinputs.f:11-307), define_van_der_waals + forgen (vdw_terms.f:1-380),
@@ -150,7 +161,11 @@ int fmc_full_ewald(fmc_plain *h, double *out4);
  *     point are serialised by a lock held until their kernels finish;
  *     anything else that ran these kernels on the same array at the same
  *     time would race with them.
- * Call with the device the engine was created on current. */
+ *   - The looked-up address is kept for the life of the process.  A
+ *     cudaDeviceReset of that device makes it stale: after one, do not call
+ *     this entry point on that device again in the same process.
+ * Call with the device the engine was created on current (FMC_ERR_ARG
+ * otherwise, before anything runs). */
 int fmc_full_ewald_noalloc(fmc_plain *h, double *out4);
 
 /* insertion (mc_moves.f:150-276) of guest type iguest at site coordinates
@@ -289,6 +304,18 @@ int fmc_batch_get_sk(fmc_batch *b, int chain, double *sk, int cap);
  * precision (checked). */
 int fmc_batch_save(fmc_batch *b, const char *path);
 int fmc_batch_load(fmc_batch *b, const char *path);
+/* fmc_batch_load reads and checks the whole file (array sizes, guest counts
+ * against the capacity, molecule-order and free-list entries, generator
+ * positions, system indices) before any of it reaches the device; a
+ * rejected file (FMC_ERR_INPUT) leaves the batch unchanged. */
+
+/* The same state copy kept in device memory: fmc_batch_snapshot copies
+ * every chain's state, fmc_batch_restore puts that copy back (any number
+ * of times), so that cycles can be replayed from one state -- e.g. timed
+ * cycles that all start from the same loadings.  No counterpart in the
+ * reference. */
+int fmc_batch_snapshot(fmc_batch *b);
+int fmc_batch_restore(fmc_batch *b);
 
 /* Widom test-particle insertions of guest type iguest (1-based) against
  * chain `chain`'s current state, which they do not change (widom_grid,
@@ -349,7 +376,8 @@ int fmc_adjoint_destroy(fmc_adjoint *a);
 int fmc_batch_set_cluster(fmc_batch *b, const int *csize, int nsys);
 /* The same per chain (nchains sizes): heavily loaded chains of a system can
  * get more CTAs than its light ones.  fmc_batch_get_cluster then reports
- * each system's largest size. */
+ * each system's largest size.  Size 0 pauses a chain (it is not run until
+ * it gets a size again); at least one chain must stay active. */
 int fmc_batch_set_chain_cluster(fmc_batch *b, const int *csize, int nchains);
 int fmc_batch_get_chain_cluster(const fmc_batch *b, int *csize, int nchains);
 int fmc_batch_get_cluster(const fmc_batch *b, int *csize, int nsys);

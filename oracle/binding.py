@@ -69,6 +69,9 @@ def load() -> C.CDLL:
             "orc_duni_sequence": (None, [C.c_longlong, i, dp]),
             "orc_get_erc": (i, [vp, dp, i]),
             "orc_get_vvv": (i, [vp, i, dp, i]),
+            "orc_set_prefilter": (None, [vp, i]),
+            "orc_save_state": (i, [vp]),
+            "orc_restore_state": (i, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -117,6 +120,15 @@ class Oracle:
 
     def create_molecules(self, iguest: int, n: int) -> int:
         return self._ck(self.lib.orc_create_molecules(self._h, iguest, n))
+
+    def set_prefilter(self, on: bool):
+        self.lib.orc_set_prefilter(self._h, int(on))
+
+    def save_state(self):
+        self._ck(self.lib.orc_save_state(self._h))
+
+    def restore_state(self):
+        self._ck(self.lib.orc_restore_state(self._h))
 
     def run(self, nsteps: int):
         logs = (MoveLog * max(1, nsteps))()

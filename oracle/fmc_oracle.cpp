@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -445,6 +446,7 @@ struct Sim {
   std::vector<double> chainstats;
   std::vector<std::vector<double>> avgwindow;  // [window][1..]
   Duni rng;
+  bool prefilter_inserts = true;  // insert_guests' framework pre-test (fw_overlap_certain)
   // results of set-up
   double spe_vdw = 0, spe_ecoul = 0, spe_dlpeng = 0, ewald1sum = 0;
 
@@ -523,6 +525,17 @@ struct Sim {
   void mc_switch(int iguest, orc_move_log *lg);
   void step(orc_move_log *lg);
   int insert_guests(int iguest, int nguests);
+  // Pre-loading only: the framework atoms on a cell grid, so that
+  // insert_guests can skip trial positions that certainly overlap a
+  // framework atom without the full list build of insertion().
+  struct FwGrid {
+    bool built = false;
+    int nc[3] = {0, 0, 0};
+    double csz[3] = {0, 0, 0};
+    std::vector<int> start;            // [cell] -> first atom, cells z fastest
+    std::vector<double> x, y, z;       // atoms sorted by cell
+  } fwgrid;
+  bool fw_overlap_certain(int natms);
   void production_stats(bool accepted);
   void setup_grid();
   void equitable_bin(double fa, double fb, double fc, int sub, double val);
@@ -3505,6 +3518,75 @@ void Sim::step(orc_move_log *lg) {
   if (lg) lg->nmols_after = mol[m0].nummols;
 }
 
+// True when a trial position (newx/newy/newz, sites 1..natms) lies within
+// the overlap distance of a framework atom by a clear margin, with the
+// distance formed as insertion() forms it (difference, images, sum of
+// squares).  Such a trial is rejected by insertion() whatever else it
+// finds, and its rejection leaves no state behind, so insert_guests may
+// skip the call.  Orthorhombic cells only (false otherwise); trials near
+// the threshold or overlapping only guests still go through insertion().
+bool Sim::fw_overlap_certain(int natms) {
+  if (imcon != 1 && imcon != 2) return false;
+  const double L[3] = {cell[0], cell[4], cell[8]};
+  const double ovd = std::sqrt(overlap);
+  if (!fwgrid.built) {
+    fwgrid.built = true;
+    for (int d = 0; d < 3; ++d) {
+      fwgrid.nc[d] = std::max(3, (int)std::floor(L[d] / std::max(ovd, 1e-3)));
+      fwgrid.csz[d] = L[d] / fwgrid.nc[d];
+    }
+    const int ncell = fwgrid.nc[0] * fwgrid.nc[1] * fwgrid.nc[2];
+    std::vector<std::vector<double>> bx(ncell), by(ncell), bz(ncell);
+    for (int fr = 1; fr <= ntpfram; ++fr) {
+      const MolType &m = mol[locfram[fr]];
+      const int n = m.nummols * m.natoms;
+      for (int i = 1; i <= n; ++i) {
+        const double p[3] = {m.mx[i], m.my[i], m.mz[i]};
+        int c3[3];
+        for (int d = 0; d < 3; ++d) {
+          const double w = p[d] - L[d] * std::floor(p[d] / L[d]);
+          c3[d] = std::min(fwgrid.nc[d] - 1, std::max(0, (int)(w / fwgrid.csz[d])));
+        }
+        const int c = (c3[0] * fwgrid.nc[1] + c3[1]) * fwgrid.nc[2] + c3[2];
+        bx[c].push_back(p[0]);
+        by[c].push_back(p[1]);
+        bz[c].push_back(p[2]);
+      }
+    }
+    fwgrid.start.assign(ncell + 1, 0);
+    for (int c = 0; c < ncell; ++c) {
+      fwgrid.start[c + 1] = fwgrid.start[c] + (int)bx[c].size();
+      fwgrid.x.insert(fwgrid.x.end(), bx[c].begin(), bx[c].end());
+      fwgrid.y.insert(fwgrid.y.end(), by[c].begin(), by[c].end());
+      fwgrid.z.insert(fwgrid.z.end(), bz[c].begin(), bz[c].end());
+    }
+  }
+  const double lim = overlap * (1.0 - 1.0e-9);
+  for (int i = 1; i <= natms; ++i) {
+    const double p[3] = {newx[i], newy[i], newz[i]};
+    int c3[3];
+    for (int d = 0; d < 3; ++d) {
+      const double w = p[d] - L[d] * std::floor(p[d] / L[d]);
+      c3[d] = std::min(fwgrid.nc[d] - 1, std::max(0, (int)(w / fwgrid.csz[d])));
+    }
+    for (int ox = -1; ox <= 1; ++ox)
+      for (int oy = -1; oy <= 1; ++oy)
+        for (int oz = -1; oz <= 1; ++oz) {
+          const int cx = (c3[0] + ox + fwgrid.nc[0]) % fwgrid.nc[0];
+          const int cy = (c3[1] + oy + fwgrid.nc[1]) % fwgrid.nc[1];
+          const int cz = (c3[2] + oz + fwgrid.nc[2]) % fwgrid.nc[2];
+          const int c = (cx * fwgrid.nc[1] + cy) * fwgrid.nc[2] + cz;
+          for (int a = fwgrid.start[c]; a < fwgrid.start[c + 1]; ++a) {
+            double dx = p[0] - fwgrid.x[a], dy = p[1] - fwgrid.y[a], dz = p[2] - fwgrid.z[a];
+            images(imcon, 1, cell, &dx, &dy, &dz);
+            const double rsq = dx * dx + dy * dy + dz * dz;
+            if (rsq < lim) return true;
+          }
+        }
+  }
+  return false;
+}
+
 // insert_guests (mc_moves.f:84-149)
 int Sim::insert_guests(int iguest, int nguests) {
   int m0 = locguest[iguest];
@@ -3514,6 +3596,10 @@ int Sim::insert_guests(int iguest, int nguests) {
   while (mol[m0].nummols < nguests) {
     if (iter >= maxiter) fail("oracle: insert_guests iteration cap (error 2320)");
     random_ins(iguest);
+    if (prefilter_inserts && fw_overlap_certain(mol[m0].natoms)) {
+      ++iter;  // insertion() would exit on this overlap; nothing to undo
+      continue;
+    }
     double estep = 0.0, delrc = 0.0, chgtmp = 0.0, engsictmp = 0.0;
     bool loverlap = false, lnewsurf = false;
     engsicorig = engsic;
@@ -3534,6 +3620,7 @@ int Sim::insert_guests(int iguest, int nguests) {
 
 struct orc_sim {
   Sim s;
+  std::unique_ptr<Sim> saved;  // orc_save_state
 };
 
 namespace {
@@ -3633,6 +3720,23 @@ int orc_run(orc_sim *h, int nsteps, orc_move_log *log, int cap) {
 
 int orc_create_molecules(orc_sim *h, int iguest, int nguests) {
   return guarded([&] { return h->s.insert_guests(iguest, nguests); });
+}
+
+void orc_set_prefilter(orc_sim *h, int on) { h->s.prefilter_inserts = on != 0; }
+
+int orc_save_state(orc_sim *h) {
+  return guarded([&] {
+    h->saved = std::make_unique<Sim>(h->s);
+    return 0;
+  });
+}
+
+int orc_restore_state(orc_sim *h) {
+  return guarded([&] {
+    if (!h->saved) fail("oracle: no saved state");
+    h->s = *h->saved;
+    return 0;
+  });
 }
 
 static void pack_out(Sim &s, int m0, double estep, double *parts, double delrc,

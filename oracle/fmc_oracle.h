@@ -105,6 +105,17 @@ int orc_swap(orc_sim *s, int iguest, int choice, int jguest, const double *q,
  * or -1 on error. */
 int orc_create_molecules(orc_sim *s, int iguest, int nguests);
 
+/* insert_guests' framework pre-test (on by default): trial positions that
+ * certainly overlap a framework atom skip insertion(), which would reject
+ * them without leaving any state behind; the created molecules and the
+ * generator's sequence are the same with it on or off. */
+void orc_set_prefilter(orc_sim *s, int on);
+
+/* Keep a copy of the whole simulation state (coordinates, S(k), energies,
+ * counters, generator) and put it back: replays of one state. 0 or -1. */
+int orc_save_state(orc_sim *s);
+int orc_restore_state(orc_sim *s);
+
 /* Stand-alone energy routines for parity of the C-ABI entry points.
  * Coordinates are site-major x,y,z triples (natms sites).  The state of
  * the simulation is not changed, except the scratch arrays the reference

@@ -1,0 +1,142 @@
+"""The benchmarked configuration against the oracle.
+
+bench.py times the batched isotherm: 64 FP32 chains over the four config-3
+frameworks (25.6 / 38.4 / 51.2 / 64.0 A, kmax 7 / 10 / 12 / 18), pre-loaded
+on the device, on clusters of 1 / 2 / 2 / 4 CTAs with the guests resident in
+shared memory, replaying 256 moves from the pre-loaded state.  Here that
+exact set-up is checked:
+
+- the device pre-loading creates the oracle's molecules (same seeds);
+- every chain follows the oracle's FP64 chain move by move (same move,
+  molecule and overlap outcome) until the first decision at the Metropolis
+  threshold, with estep within 1e-6 of max(|estep|, the moving molecule's
+  energy before the move, 1 kcal/mol);
+- an FP64 chain on a 4-CTA cluster of the 64 A / kmax 18 framework matches
+  the oracle to 1e-9 with identical decisions;
+- config 1 (25.6 A, kmax 7, alpha 0.26, 0.1 bar, seed 1): an FP64 device
+  chain makes the same decisions as the oracle for 1e5 moves.  The chain
+  starts empty and, at 0.1 bar in this pore-free framework, stays empty:
+  all 1e5 moves are insertions, about 300 of them free of overlap (full
+  evaluations, checked to 1e-9), none accepted.
+"""
+import multiprocessing as mp
+import os
+
+import numpy as np
+import pytest
+
+from fastmc_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+BENCH_CLUSTERS = [1, 2, 2, 4]
+MOVES = 256
+
+
+@pytest.fixture(scope="module")
+def config3(tmp_path_factory):
+    base = tmp_path_factory.mktemp("config3")
+    chains = syn.config3_chains()
+    dirs = []
+    for f in range(4):
+        spec = [c for c in chains if c.fw_seed == f + 1][0]
+        d = str(base / f"fw{f + 1}")
+        syn.write_inputs(d, spec)
+        dirs.append(d)
+    specs = [{"system": c.fw_seed - 1, "pressure_pa": c.pressure_bar * 1e5, "seed": 1000 + i,
+              "create_molecules": c.create_molecules} for i, c in enumerate(chains)]
+    return dirs, specs
+
+
+def _oracle_runs(jobs):
+    from oracle import replay
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        return pool.map(replay.chain_moves, jobs)
+
+
+def test_config3_fp32_clusters_follow_oracle(fmc_lib, oracle_lib, config3):
+    dirs, specs = config3
+    systems = [fmc_lib.System.load(d) for d in dirs]
+    b = fmc_lib.Batch(systems, specs, precision=fmc_lib.FMC_PREC_FP32, guest_capacity=1024)
+    b.set_cluster(BENCH_CLUSTERS)
+    b.set_log(MOVES)
+    created = [b.coords(c) for c in range(len(specs))]
+    b.run(MOVES)
+    assert all(s.status == 0 for s in b.stats())
+    jobs = [(dirs[s["system"]], s["seed"], s["create_molecules"], MOVES) for s in specs]
+    ref = _oracle_runs(jobs)
+    nfull = nchk = 0
+    parted = 0
+    for c, (xyz0, recs, e_old) in enumerate(ref):
+        x, n = created[c]
+        assert n == specs[c]["create_molecules"], c
+        assert np.allclose(x[:9 * n].reshape(-1, 3), xyz0, rtol=0, atol=1e-9), c
+        got = b.log(c, MOVES)
+        assert len(got) == MOVES
+        for i, (g, r) in enumerate(zip(got, recs)):
+            move, ig, choice, ovl, acc, estep = r[:6]
+            assert (g.move, g.iguest, g.choice) == (move, ig, choice), (c, i)
+            if g.overlap != ovl or g.accepted != acc:
+                parted += 1
+                break  # a decision at the threshold; the chains part here
+            nchk += 1
+            if ovl:
+                continue
+            tol = 1e-6 * max(abs(estep), abs(e_old[i]), 1.0)
+            assert abs(g.estep - estep) <= tol, (c, i, g.estep, estep, e_old[i])
+            nfull += 1
+    # most chains run their whole cycle with the oracle's decisions
+    assert parted <= len(specs) // 4
+    assert nfull >= 2000 and nchk >= 0.8 * len(specs) * MOVES
+
+
+def test_fp64_cluster4_64A_kmax18_matches_oracle(fmc_lib, oracle_lib, config3):
+    dirs, specs = config3
+    chain = [s for s in specs if s["system"] == 3 and 80 <= s["create_molecules"] <= 400][0]
+    sysm = fmc_lib.System.load(dirs[3])
+    b = fmc_lib.Batch([sysm], [{**chain, "system": 0}], precision=fmc_lib.FMC_PREC_FP64,
+                      guest_capacity=1024)
+    b.set_cluster([4])
+    b.set_log(MOVES)
+    b.run(MOVES)
+    got = b.log(0, MOVES)
+    ((xyz0, recs, e_old),) = _oracle_runs([(dirs[3], chain["seed"], chain["create_molecules"], MOVES)])
+    nfull = 0
+    for i, (g, r) in enumerate(zip(got, recs)):
+        move, ig, choice, ovl, acc, estep, rande, nafter = r
+        assert (g.move, g.choice, g.overlap, g.accepted) == (move, choice, ovl, acc), i
+        assert g.rande == rande, i
+        if not ovl:
+            assert abs(g.estep - estep) <= 1e-9 * max(abs(estep), 1e-6), (i, g.estep, estep)
+            nfull += 1
+        assert g.nmols_after == nafter
+    assert nfull >= 50
+
+
+def test_config1_fp64_1e5_moves(fmc_lib, oracle_lib, tmp_path):
+    n = 100000
+    d = str(tmp_path / "config1")
+    syn.write_inputs(d, syn.config1())
+    o = oracle_lib.Oracle(d)
+    o.seed(1)
+    ref = o.run(n)
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 1}], precision=fmc_lib.FMC_PREC_FP64,
+                      guest_capacity=256)
+    b.set_log(n)
+    for _ in range(10):
+        b.run(n // 10)
+    got = b.log(0, n)
+    assert len(got) == n
+    nfull = 0
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.choice, g.overlap, g.accepted) == (r.move, r.choice, r.overlap, r.accepted), i
+        assert g.rande == r.rande, i
+        if not r.overlap:
+            assert abs(g.estep - r.estep) <= 1e-9 * max(abs(r.estep), 1e-6), (i, g.estep, r.estep)
+            nfull += 1
+    st = b.stats()[0]
+    mol = o.locguest(1)
+    assert st.nummols == o.nummols(mol)
+    assert abs(st.energy - o.energy(mol)) <= 1e-9 * max(1.0, max(abs(r.estep) for r in ref))
+    assert nfull >= 100

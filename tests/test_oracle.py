@@ -470,3 +470,40 @@ def test_isotherm_fixtures_match_reference_keys():
         assert abs(k - p) < 1e-9 and (steps, eq) == (500000, 750000), n
         seen.add(k)
     assert len(seen) == 10
+
+
+def test_preload_prefilter_changes_nothing(oracle_lib, inputs_dir):
+    """insert_guests' framework pre-test skips only trial positions that
+    insertion() rejects anyway: with it on and off the same molecules are
+    created after the same number of trials, and the chains continue
+    identically."""
+    d = inputs_dir(syn.small_test_spec(seed=5, kmax=6, ntile=3, pressure_bar=5.0), "prefilter")
+    runs = []
+    for on in (True, False):
+        o = oracle_lib.Oracle(d)
+        o.set_prefilter(on)
+        o.seed(31)
+        it = o.create_molecules(1, 25)
+        mol = o.locguest(1)
+        x = o.coords(mol)
+        lg = [(r.move, r.choice, r.overlap, r.accepted, r.estep) for r in o.run(300)]
+        runs.append((it, x, o.sk(), lg))
+    (i1, x1, s1, l1), (i2, x2, s2, l2) = runs
+    assert i1 == i2 and i1 > 25
+    assert np.array_equal(x1, x2)
+    assert np.array_equal(s1, s2)
+    assert l1 == l2
+
+
+def test_oracle_state_save_restore_replays(oracle_lib, inputs_dir):
+    """orc_save_state / orc_restore_state: every replay from the saved
+    state makes the same moves with the same energies."""
+    d = inputs_dir(syn.small_test_spec(seed=5, kmax=6, ntile=3, pressure_bar=5.0, create=20), "replay")
+    o = oracle_lib.Oracle(d)
+    o.seed(9)
+    o.create_molecules(1, 20)
+    o.save_state()
+    a = [(r.move, r.choice, r.accepted, r.estep) for r in o.run(200)]
+    for _ in range(2):
+        o.restore_state()
+        assert [(r.move, r.choice, r.accepted, r.estep) for r in o.run(200)] == a

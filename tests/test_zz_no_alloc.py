@@ -27,6 +27,12 @@ def noalloc(plain):
     return rc, np.array(out[:])
 
 
+def allocs():
+    a, f = C.c_int64(), C.c_int64()
+    L.check(L.load().fmc_alloc_count(C.byref(a), C.byref(f)))
+    return a.value, f.value
+
+
 def close(a, b):
     scale = np.maximum(np.maximum(np.abs(a), np.abs(b)), 1e-6)
     return np.all(np.abs(a - b) <= REL * scale)
@@ -60,13 +66,19 @@ def test_noalloc_matches_full_ewald(fmc_lib, inputs_dir, precision):
     ref = plain.full_ewald()
     sk_ref = plain.sk()
     # two calls in a row: each agrees with the allocating entry point and
-    # leaves the same guest S(k)
+    # leaves the same guest S(k); neither allocates or frees device memory
     for _ in range(2):
+        a0 = allocs()
         rc, out = noalloc(plain)
         assert rc == L.FMC_OK, L.last_error()
+        assert allocs() == a0
         assert close(out, ref), (out, ref)
         sk = plain.sk()
         assert np.allclose(sk, sk_ref, rtol=0, atol=1e-12 * np.abs(sk_ref).max())
+    # the allocating entry point, for contrast, is seen by the counter
+    a0 = allocs()
+    plain.full_ewald()
+    assert allocs()[0] > a0[0]
     # and the engine keeps working from that state
     assert plain.deletion(1, 1)["overlap"] == 0
 
