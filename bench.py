@@ -549,6 +549,12 @@ def run_ours(args, rank, world, local_rank):
 
     h2d, d2h = batch.cycle_bytes()  # fugacities up, chain state records down
     loads = [snap[c].nummols for c in range(n)]
+    # each chain's own device time in the last step (its CTAs' kernel time)
+    chain_ms = {}
+    for f in range(len(systems)):
+        t = sorted((after[c].device_ns - snap[c].device_ns) / 1e6 for c in range(n)
+                   if specs[c]["system"] == f)
+        chain_ms[f"fw{f + 1}"] = {"max": t[-1], "median": t[len(t) // 2]}
 
     if rank == 0:
         out = {
@@ -568,6 +574,7 @@ def run_ours(args, rank, world, local_rank):
             "trial_moves_per_s": moves / (dev_ms / 1000.0),
             "full_evals_per_s": full / (dev_ms / 1000.0),
             "overlap_exits_per_step": ovl1,
+            "chain_ms_per_step": chain_ms,
             # one chain-kernel launch per cluster-size group per step
             "gpu_launches": args.steps * len(set(per_chain)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -44,6 +44,29 @@ class SystemInfo(C.Structure):
                 ("overlap", C.c_double)]
 
 
+class SystemDesc(C.Structure):
+    """fmc_system_desc: a host's start-up arrays (fmc_upload_system)."""
+    _fields_ = [("imcon", C.c_int), ("cell", C.c_double * 9), ("engunit", C.c_double),
+                ("temp", C.c_double), ("rcut", C.c_double), ("alpha", C.c_double),
+                ("kmax", C.c_int * 3), ("newld", C.c_int), ("epsq", C.c_double),
+                ("overlap", C.c_double), ("surftol", C.c_double), ("eqsteps", C.c_int),
+                ("nwindsteps", C.c_int), ("minchk", C.c_int), ("laccsample", C.c_int),
+                ("ntpatm", C.c_int), ("mxegrd", C.c_int), ("drewd", C.c_double),
+                ("dlrpot", C.c_double), ("erc", C.POINTER(C.c_double)), ("ntpvdw", C.c_int),
+                ("vvv", C.POINTER(C.c_double)), ("ltpvdw", C.POINTER(C.c_int)),
+                ("prmvdw", C.POINTER(C.c_double)), ("lstvdw", C.POINTER(C.c_int)),
+                ("steadd", C.POINTER(C.c_double)), ("maxmls", C.c_int),
+                ("numatoms", C.POINTER(C.c_int)), ("nummols", C.POINTER(C.c_int)),
+                ("is_guest", C.POINTER(C.c_int)), ("ltype", C.POINTER(C.c_int)),
+                ("charge", C.POINTER(C.c_double)), ("mass", C.POINTER(C.c_double)),
+                ("frozen", C.POINTER(C.c_int)), ("fw_xyz", C.POINTER(C.c_double)),
+                ("ntpguest", C.c_int), ("guest_tmpl", C.POINTER(C.c_double)),
+                ("fugacity", C.POINTER(C.c_double)), ("delr", C.POINTER(C.c_double)),
+                ("disp_ratio", C.POINTER(C.c_double)), ("tran_ratio", C.POINTER(C.c_double)),
+                ("rota_ratio", C.POINTER(C.c_double)), ("move_freq", C.POINTER(C.c_float)),
+                ("create", C.POINTER(C.c_int))]
+
+
 class MoveResult(C.Structure):
     _fields_ = [("estep", C.c_double), ("ewld1", C.c_double), ("ewld2", C.c_double),
                 ("vdw", C.c_double), ("delrc", C.c_double),
@@ -70,7 +93,10 @@ class ChainStats(C.Structure):
                 ("avg_n", C.c_double), ("avg_e", C.c_double), ("avg_en", C.c_double),
                 ("avg_n2", C.c_double), ("avg_e2", C.c_double), ("avg_nf", C.c_double),
                 ("qst", C.c_double), ("cv", C.c_double), ("prodcount", C.c_int64),
-                ("windows", C.c_int64), ("device_ns", C.c_int64)]
+                ("windows", C.c_int64), ("device_ns", C.c_int64),
+                ("guest_avg_n", C.c_double * MAX_GUEST_TYPES),
+                ("guest_se_n", C.c_double * MAX_GUEST_TYPES),
+                ("phase_cycles", C.c_int64 * 16)]
 
 
 class MoveLog(C.Structure):
@@ -90,6 +116,7 @@ SIGNATURES = {
     "fmc_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "fmc_version": (C.c_char_p, []),
     "fmc_system_load": (C.c_int, [C.c_char_p, pp]),
+    "fmc_upload_system": (C.c_int, [C.POINTER(SystemDesc), pp]),
     "fmc_system_free": (C.c_int, [vp]),
     "fmc_system_get_info": (C.c_int, [vp, C.POINTER(SystemInfo)]),
     "fmc_system_set_fugacity": (C.c_int, [vp, C.c_int, C.c_double]),

@@ -34,6 +34,45 @@ class System:
         L.check(lib.fmc_system_load(directory.encode(), C.byref(h)))
         return cls(h.value)
 
+    # fields of fmc_system_desc by kind, for System.upload
+    _DESC_INT = ("imcon", "newld", "eqsteps", "nwindsteps", "minchk", "laccsample", "ntpatm",
+                 "mxegrd", "ntpvdw", "maxmls", "ntpguest")
+    _DESC_DBL = ("engunit", "temp", "rcut", "alpha", "epsq", "overlap", "surftol", "drewd", "dlrpot")
+    _DESC_IARR = ("ltpvdw", "lstvdw", "numatoms", "nummols", "is_guest", "ltype", "frozen", "create")
+    _DESC_DARR = ("erc", "vvv", "prmvdw", "steadd", "charge", "mass", "fw_xyz", "guest_tmpl",
+                  "fugacity", "delr", "disp_ratio", "tran_ratio", "rota_ratio")
+
+    @classmethod
+    def upload(cls, arrays: dict) -> "System":
+        """fmc_upload_system: the system from a host's start-up arrays,
+        given by the field names of fmc_system_desc (scalars, "cell" with 9
+        values, "kmax" with 3, arrays as sequences; "create" may be left
+        out)."""
+        d = L.SystemDesc()
+        keep = []
+        for k in cls._DESC_INT:
+            setattr(d, k, int(np.asarray(arrays[k]).reshape(-1)[0]))
+        for k in cls._DESC_DBL:
+            setattr(d, k, float(np.asarray(arrays[k]).reshape(-1)[0]))
+        d.cell = (C.c_double * 9)(*[float(v) for v in arrays["cell"]])
+        d.kmax = (C.c_int * 3)(*[int(v) for v in arrays["kmax"]])
+        for k in cls._DESC_IARR:
+            if k not in arrays:
+                continue
+            a = np.ascontiguousarray(np.asarray(arrays[k]).astype(np.int32))
+            keep.append(a)
+            setattr(d, k, a.ctypes.data_as(L.ip))
+        for k in cls._DESC_DARR:
+            a = np.ascontiguousarray(np.asarray(arrays[k], dtype=np.float64))
+            keep.append(a)
+            setattr(d, k, a.ctypes.data_as(L.dp))
+        mf = np.ascontiguousarray(np.asarray(arrays["move_freq"], dtype=np.float32))
+        keep.append(mf)
+        d.move_freq = mf.ctypes.data_as(C.POINTER(C.c_float))
+        h = C.c_void_p()
+        L.check(L.load().fmc_upload_system(C.byref(d), C.byref(h)))
+        return cls(h.value)
+
     @property
     def handle(self) -> C.c_void_p:
         return self._h

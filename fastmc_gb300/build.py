@@ -33,9 +33,16 @@ def nvcc() -> str:
     return path
 
 
+def _flags():
+    """FMC_PHASE_TIMERS=1 in the environment builds the per-phase move-loop
+    clocks in (fmc_chain_stats.phase_cycles)."""
+    extra = ["-DFMC_PHASE_TIMERS"] if os.environ.get("FMC_PHASE_TIMERS") == "1" else []
+    return NVCC_FLAGS + extra
+
+
 def _compile(src: str) -> str:
     obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
-    cmd = [nvcc(), *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc(), *_flags(), "-c", os.path.join(CSRC, src), "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
@@ -52,12 +59,27 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
+def _obj_stale(src: str) -> bool:
+    """An object needs compiling when it is missing or older than its
+    source or any header (every source includes the headers)."""
+    obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    deps = [os.path.join(CSRC, src), os.path.join(HERE, "..", "include", "fastmc_gb300.h"),
+            os.path.abspath(__file__)]
+    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     if not force and not _stale():
         return LIB
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(_compile, SOURCES))
+    todo = [s for s in SOURCES if force or _obj_stale(s)]
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(todo))) as ex:
+        list(ex.map(_compile, todo))
+    objs = [os.path.join(OUT_DIR, os.path.basename(s) + ".o") for s in SOURCES]
     cmd = [nvcc(), GENCODE, "-shared", "-o", LIB, *objs, "-lcudart"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:

@@ -133,11 +133,15 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   if (csize > 1) cluster_barrier();  // every CTA's flags are cleared before anyone posts
   int st = 0;
+#ifdef FMC_PHASE_TIMERS
+  if (threadIdx.x == 0) B.tmark = clock64();
+#endif
   if (mode == kModeMoves) {
     for (int it = 0; it < nmoves; ++it) {
       // the previous move's FP64 bookkeeping overlaps this proposal
       if (threadIdx.x == 32) run_deferred<F32, GN>(B);
       propose(B, CA, chain, kPropMC, 0);
+      FMC_PHASE(B, 0);
       int full = 0;
       if (B.mc.kind != 0) full = evaluate_any<F32, GN>(B, CA, chain, st);
       if (threadIdx.x == 0) {
@@ -167,7 +171,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       __syncthreads();
+      FMC_PHASE(B, 9);
       commit(B, CA, chain, st, true);
+      FMC_PHASE_SYNC(B, 10);
       if (threadIdx.x == 0) {
         stats(B, true);
         if (logcap > 0 && B.H.log_n < logcap) {
@@ -178,6 +184,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncthreads();
       // probability grids after every production move (gcmc.f:1129-1130)
       if (B.S.prob_nsub > 0 && CA.grid && B.dfr.production) store_prob(B, CA, chain);
+      FMC_PHASE_SYNC(B, 11);
     }
     if (threadIdx.x == 32) run_deferred<F32, GN>(B);
     __syncthreads();

@@ -194,6 +194,7 @@ struct ChainHdr {
   double chainstats[kMaxG][6];
   double wsum;
   double wacc[kMaxG][8];
+  double wsq[kMaxG];       // sum over windows of weight x <N>_window^2 (standard error)
   long long windows;
   long long moves, evals, overlap_exits;
   long long attempts[6], accepts[6];  // insert, delete, displace, translate, rotate, jump
@@ -212,6 +213,7 @@ struct ChainHdr {
   int disp_mod[kMaxG], tran_mod[kMaxG], rota_mod[kMaxG];
   float lnpf[kMaxG];  // FP32 decisions: log(statvolm * fugacity / (kB T)), per launch
   int skb[kMaxG];     // FP32 path: guest S(k) of type g is in skdf (0) or skdf2 (1)
+  long long phase_cycles[16];  // move-loop clocks per phase (FMC_PHASE_TIMERS builds)
 };
 
 __host__ __device__ inline void split_pair(double x, float *out) {

@@ -1002,6 +1002,15 @@ void fill_stats(const Chains &C, fmc_chain_stats *out) {
     o.prodcount = h.prodcount;
     o.windows = h.windows;
     o.device_ns = h.dev_ns;
+    for (int i = 0; i < 16; ++i) o.phase_cycles[i] = h.phase_cycles[i];
+    // per guest type: <N> and the reference's "standard error" of it, the
+    // weighted standard deviation of the window averages (gcmc.f:1218-1241)
+    for (int g = 0; g < s.ntpguest && g < FMC_MAX_GUEST_TYPES; ++g) {
+      if (h.wsum <= 0) continue;
+      const double m = h.wacc[g][0] / h.wsum;
+      o.guest_avg_n[g] = m;
+      o.guest_se_n[g] = std::sqrt(std::max(0.0, h.wsq[g] / h.wsum - m * m));
+    }
   }
 }
 
@@ -1305,6 +1314,16 @@ int fmc_system_load(const char *dir, fmc_system **out) {
     if (!out) raise(FMC_ERR_ARG, "null output pointer");
     auto p = std::make_unique<fmc_system>();
     load_system(dir ? dir : ".", p->s);
+    *out = p.release();
+    return FMC_OK;
+  });
+}
+
+int fmc_upload_system(const fmc_system_desc *desc, fmc_system **out) {
+  return guard([&] {
+    if (!desc || !out) raise(FMC_ERR_ARG, "null argument");
+    auto p = std::make_unique<fmc_system>();
+    upload_system(*desc, p->s);
     *out = p.release();
     return FMC_OK;
   });

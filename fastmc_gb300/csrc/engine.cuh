@@ -25,6 +25,37 @@
 
 namespace fmcdev {
 
+// Per-phase device clocks of the move loop (built with FMC_PHASE_TIMERS,
+// e.g. FMC_PHASE_TIMERS=1 python -m fastmc_gb300.build --force): thread 0
+// of each CTA adds the cycles since the previous mark to phase n of its
+// chain record; the stats report rank 0's sums.  Compiled out otherwise.
+// Phases: 0 proposal, 1 overlap test, 2 neighbour segments and near-guest
+// list, 3 framework and guest pair terms, 4 power tables, 5 k-space,
+// 6 block reduction, 7 cluster exchange, 8 epilogue, 9 decision and log,
+// 10 commit, 11 statistics.
+#ifdef FMC_PHASE_TIMERS
+#define FMC_PHASE(B, n)                                     \
+  do {                                                      \
+    if (threadIdx.x == 0) {                                 \
+      const long long t_ = clock64();                       \
+      (B).H.phase_cycles[n] += t_ - (B).tmark;              \
+      (B).tmark = t_;                                       \
+    }                                                       \
+  } while (0)
+#define FMC_PHASE_SYNC(B, n) \
+  do {                       \
+    __syncthreads();         \
+    FMC_PHASE(B, n);         \
+  } while (0)
+#else
+#define FMC_PHASE(B, n) \
+  do {                  \
+  } while (0)
+#define FMC_PHASE_SYNC(B, n) \
+  do {                       \
+  } while (0)
+#endif
+
 struct LogRec {  // mirrors fmc_move_log
   int move, iguest, choice, overlap, accepted, nmols_after;
   double estep, rande;
@@ -63,6 +94,7 @@ struct BlockShared {
   unsigned xflag[kMaxCluster];  // xflag[q]: last exchange CTA q has posted here
   unsigned cflag;               // last commit rank 0 has finished
   unsigned xseq, cseq;          // exchanges and commits done (same in every CTA)
+  long long tmark;              // FMC_PHASE: clock of the previous mark
 };
 
 // Sum ev.out[0..nv) over the CTAs of the chain's cluster, in rank order (so
@@ -1516,7 +1548,9 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
     __syncthreads();
   }
   if (mc.kind == 1 || mc.kind >= 3) {
-    if (overlap_check(B, CA, chain)) {
+    const int hit = overlap_check(B, CA, chain);
+    FMC_PHASE(B, 1);
+    if (hit) {
       if (threadIdx.x == 0) mc.overlap = 1;
       __syncthreads();
       return 0;
@@ -1544,6 +1578,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       if (CA.resident) listed = list_near_guests(B, rs, p, mc.slot, B.ev.rmx[p]);
       else listed = list_near_guests(B, gsites, p, mc.slot, B.ev.rmx[p]);
     }
+    FMC_PHASE_SYNC(B, 2);
     scan_framework<F32, NS>(S, B.ev, p, ns, B.si, A, ovd, sfp, st);
     bool done = false;
     if constexpr (F32 && GN == 1) {
@@ -1563,12 +1598,15 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       scan_guests<F32, GN, NS>(S, B.H, CA, chain, B.ev, p, ns, mc.g, mc.slot, B.ev.rmx[p], B.si, A,
                                ovd, sfp, st);
     __syncthreads();
+    FMC_PHASE(B, 3);
   };
   scan_position(0, acc0, sf0);
   if (npos == 2) scan_position(1, acc1, sf1);
   build_powers<F32>(S, B.ev, npos, ns);
   __syncthreads();
+  FMC_PHASE(B, 4);
   kspace<F32, GN, NS>(B, CA, chain, mc.kind == 2, acc0, acc1, st);
+  FMC_PHASE_SYNC(B, 5);
   // block totals: out[p * nper + j], j = e2fw, vdwfw, recip, mixfw,
   // e2g[GN], vdwg[GN], mixg[GN]
   constexpr int nper = PosAcc<F32, GN>::kN;
@@ -1576,6 +1614,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
                                             (sf0 ? 1 : 0) | (sf1 ? 2 : 0), B.ev.red_i);
   int sfa = sfl & 1;
   int sfb = (sfl >> 1) & 1;
+  FMC_PHASE(B, 6);
   if (B.ev.csize > 1) {  // totals over the cluster
     if (threadIdx.x == 0) {
       B.ev.out[2 * nper] = sfa;
@@ -1584,6 +1623,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
     cluster_exchange(B, 2 * nper + 2, st);
     sfa = B.ev.out[2 * nper] > 0.5;
     sfb = B.ev.out[2 * nper + 1] > 0.5;
+    FMC_PHASE(B, 7);
   }
   if (threadIdx.x == 0) {
     const double *R = B.ev.out;
@@ -1630,6 +1670,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
     if (!isfinite(mc.estep)) st |= kStNonFinite;
   }
   __syncthreads();
+  FMC_PHASE(B, 8);
   return 1;
 }
 
@@ -1981,6 +2022,7 @@ __device__ void stats_production(const SysDev &S, ChainHdr &H, int production, i
       double w[8] = {aN, E, EN, N2, E2, NF, calc_qst(E, aN, N2, EN, S.temp),
                      calc_cv(E2, E, aN, N2, EN, S.temp)};
       for (int q = 0; q < 8; ++q) H.wacc[i][q] += rc * w[q];
+      H.wsq[i] += rc * (aN * aN);
       for (int q = 0; q < 6; ++q) H.chainstats[i][q] = 0.0;
     }
     H.windows++;

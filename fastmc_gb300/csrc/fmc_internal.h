@@ -91,6 +91,7 @@ struct System {
 
 // host_setup.cpp
 void load_system(const std::string &dir, System &s);
+void upload_system(const fmc_system_desc &d, System &s);
 inline int loc2(int i, int j) {
   int a = i > j ? i : j, b = i > j ? j : i;
   return (a * (a - 1)) / 2 + b;

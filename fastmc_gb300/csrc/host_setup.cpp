@@ -896,9 +896,10 @@ void finish_control(System &s) {
   s.statvolm = s.volm * 1e-30;
 }
 
+void build_derived(System &s);
+
 // erfcgen (ewald.f:1-30), lrcorrect's per-pair tail constants
-// (vdw_terms.f:548-645), framework type counts, k-vector list
-// (ewald.f:151-315) and excluding_ewald_charges (gcmc.f:2662-2761).
+// (vdw_terms.f:548-645), then build_derived.
 void build_tables(System &s) {
   const double a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741;
   const double a4 = -1.453152027, a5 = 1.061405429, pp = 0.3275911;
@@ -930,6 +931,15 @@ void build_tables(System &s) {
       if (i != j) e *= 2.0;
       s.steadd[iv] = e;
     }
+  build_derived(s);
+}
+
+// Framework type counts, k-vector list (ewald.f:151-315) and
+// excluding_ewald_charges (gcmc.f:2662-2761): what follows from the cell,
+// the molecules and the Ewald parameters alone.
+void build_derived(System &s) {
+  const double a1 = 0.254829592, a2 = -0.284496736, a3 = 1.421413741;
+  const double a4 = -1.453152027, a5 = 1.061405429, pp = 0.3275911;
   const MolType &fw = s.mol[s.fw_mol];
   s.n_fw = fw.nummols * fw.natoms;
   s.numtyp_fw.assign(s.ntpatm + 1, 0);
@@ -939,6 +949,11 @@ void build_tables(System &s) {
     if (fw.frz[a]) s.numfrz_fw[fw.ltp[a]] += fw.nummols;
   }
   // k vectors in the half space, reference loop order
+  s.kl.clear();
+  s.km.clear();
+  s.kn.clear();
+  s.rksq.clear();
+  s.akk.clear();
   double det[10];
   cell_props(s.rcell, det);
   double twopi = 2.0 * kPi;
@@ -1007,6 +1022,173 @@ void build_tables(System &s) {
 }
 
 }  // namespace
+
+// The system from a host's start-up arrays (fmc_upload_system): the fields
+// fmc_system_load fills from the input files, taken from the descriptor,
+// then the parts that follow from them (build_derived).
+void upload_system(const fmc_system_desc &d, System &s) {
+  auto need = [](bool ok, const char *what) {
+    if (!ok) raise(FMC_ERR_ARG, std::string("fmc_upload_system: ") + what);
+  };
+  need(d.imcon >= 1 && d.imcon <= 3, "imcon must be 1, 2 or 3");
+  need(d.maxmls >= 2 && d.maxmls <= FMC_MAX_MOLTYPES, "maxmls out of range");
+  need(d.ntpguest >= 1 && d.ntpguest <= FMC_MAX_GUEST_TYPES, "ntpguest out of range");
+  need(d.ntpatm >= 1 && d.ntpatm <= 16, "ntpatm out of range");
+  need(d.mxegrd >= 8 && d.ntpvdw >= 1, "table sizes out of range");
+  need(d.erc && d.vvv && d.ltpvdw && d.prmvdw && d.lstvdw && d.steadd, "null table");
+  need(d.numatoms && d.nummols && d.is_guest && d.ltype && d.charge && d.mass && d.frozen,
+       "null molecule array");
+  need(d.guest_tmpl && d.fugacity && d.delr && d.disp_ratio && d.tran_ratio && d.rota_ratio &&
+           d.move_freq, "null guest array");
+  need(d.rcut > 0.0 && d.alpha > 0.0 && d.temp > 0.0 && d.engunit > 0.0 && d.epsq > 0.0,
+       "non-positive rcut, alpha, temperature, engunit or epsq");
+  need(d.drewd > 0.0 && d.dlrpot > 0.0, "non-positive table spacing");
+  for (int i = 0; i < 3; ++i) need(d.kmax[i] >= 1, "kmax below 1");
+  s = System();
+  s.imcon = d.imcon;
+  for (int i = 0; i < 9; ++i) s.cell[i] = d.cell[i];
+  cell_props(s.cell, s.celprp);
+  s.volm = s.celprp[9];
+  need(s.volm > 0.0, "cell has no volume");
+  invert3(s.cell, s.rcell);
+  if (s.imcon == 2 || s.imcon == 1)
+    for (int i : {1, 2, 3, 5, 6, 7})
+      if (std::fabs(s.cell[i]) > 1e-10) raise(FMC_ERR_INPUT, "cell is not orthorhombic (error 410)");
+  s.engunit = d.engunit;
+  s.temp = d.temp;
+  s.rcut = s.rvdw = d.rcut;
+  s.alpha = d.alpha;
+  s.epsq = s.eps = d.epsq;
+  for (int i = 0; i < 3; ++i) s.kmax[i] = d.kmax[i];
+  s.overlap_sq = d.overlap * d.overlap;
+  s.surftol = d.surftol;
+  s.eqsteps = d.eqsteps;
+  s.nwindsteps = std::max(1, d.nwindsteps);
+  s.minchk = std::max(1, d.minchk);
+  s.laccsample = d.laccsample != 0;
+  // tables, 1-based as the reference keeps them
+  s.ntpatm = d.ntpatm;
+  s.mxatyp = d.ntpatm;
+  s.mxegrd = d.mxegrd;
+  s.drewd = d.drewd;
+  s.dlrpot = d.dlrpot;
+  s.erc.assign(s.mxegrd + 3, 0.0);
+  for (int i = 1; i <= s.mxegrd; ++i) s.erc[i] = d.erc[i - 1];
+  const int npair = s.ntpatm * (s.ntpatm + 1) / 2;
+  s.ntpvdw = d.ntpvdw;
+  s.maxvdw = std::max(s.ntpvdw, npair);
+  s.ltpvdw.assign(s.maxvdw + 2, -1);
+  s.lstvdw.assign(s.maxvdw + 2, 0);
+  s.prmvdw.assign(s.maxvdw + 2, std::array<double, 6>{0, 0, 0, 0, 0, 0});
+  s.vvv.assign(s.maxvdw + 2, std::vector<double>(s.mxegrd + 3, 0.0));
+  for (int k = 1; k <= s.ntpvdw; ++k) {
+    need(d.ltpvdw[k - 1] == 1 || d.ltpvdw[k - 1] == 2, "ltpvdw: only 12-6 (1) and lj (2) are supported");
+    s.ltpvdw[k] = d.ltpvdw[k - 1];
+    s.prmvdw[k][1] = d.prmvdw[k - 1];
+    s.prmvdw[k][2] = d.prmvdw[s.ntpvdw + k - 1];
+    for (int i = 1; i <= s.mxegrd; ++i) s.vvv[k][i] = d.vvv[(size_t)(k - 1) * s.mxegrd + (i - 1)];
+  }
+  s.steadd.assign(npair + 1, 0.0);
+  for (int p = 1; p <= npair; ++p) {
+    need(d.lstvdw[p - 1] >= 1 && d.lstvdw[p - 1] <= s.ntpvdw + 1, "lstvdw entry out of range");
+    s.lstvdw[p] = d.lstvdw[p - 1];
+    s.steadd[p] = d.steadd[p - 1];
+  }
+  // molecule types
+  s.maxmls = d.maxmls;
+  s.mol.assign(s.maxmls + 1, MolType());
+  s.locguest.assign(1, 0);
+  s.locfram.assign(1, 0);
+  s.guest_tmpl.assign(1, {});
+  s.unqatm.assign(s.ntpatm + 1, "");
+  size_t site = 0, fwxyz = 0, tmpl = 0;
+  for (int m = 1; m <= s.maxmls; ++m) {
+    MolType &mt = s.mol[m];
+    mt.natoms = d.numatoms[m - 1];
+    mt.nummols = d.nummols[m - 1];
+    mt.guest = d.is_guest[m - 1] != 0;
+    need(mt.natoms >= 1 && mt.nummols >= 0, "molecule sizes out of range");
+    mt.site.assign(mt.natoms, "");
+    mt.wght.assign(mt.natoms, 0.0);
+    mt.chg.assign(mt.natoms, 0.0);
+    mt.frz.assign(mt.natoms, 0);
+    mt.ltp.assign(mt.natoms, 0);
+    for (int a = 0; a < mt.natoms; ++a, ++site) {
+      mt.ltp[a] = d.ltype[site];
+      need(mt.ltp[a] >= 1 && mt.ltp[a] <= s.ntpatm, "ltype out of range");
+      mt.chg[a] = d.charge[site];
+      mt.wght[a] = d.mass[site];
+      mt.frz[a] = d.frozen[site] ? 1 : 0;
+    }
+    if (mt.guest) {
+      need(mt.nummols == 0, "guests are created on the device (nummols of a guest type must be 0)");
+      need(mt.natoms <= FMC_MAX_SITES, "guest has too many sites");
+      s.locguest.push_back(m);
+      ++s.ntpguest;
+      s.guest_tmpl.push_back(std::vector<double>(d.guest_tmpl + tmpl, d.guest_tmpl + tmpl + 3 * mt.natoms));
+      tmpl += 3 * mt.natoms;
+    } else {
+      s.locfram.push_back(m);
+      ++s.ntpfram;
+      need(d.fw_xyz != nullptr, "null framework coordinates");
+      const size_t n = 3 * (size_t)mt.nummols * mt.natoms;
+      mt.xyz.assign(d.fw_xyz + fwxyz, d.fw_xyz + fwxyz + n);
+      fwxyz += n;
+      for (int a = 0; a < mt.natoms; ++a)
+        if (!mt.frz[a]) raise(FMC_ERR_INPUT, "non-frozen framework atoms are not supported");
+    }
+  }
+  if (s.ntpfram != 1) raise(FMC_ERR_INPUT, "exactly one framework molecule type is supported");
+  need(s.ntpguest == d.ntpguest, "ntpguest differs from the guest molecule types");
+  s.fw_mol = s.locfram[1];
+  s.sumchg = 0.0;
+  for (int it = 1; it <= s.maxmls; ++it)
+    for (int l = 0; l < s.mol[it].natoms; ++l) s.sumchg += double(s.mol[it].nummols) * s.mol[it].chg[l];
+  // run control per guest type
+  const int G = s.ntpguest;
+  s.gstfuga.assign(G + 1, 0.0);
+  s.gstpress.assign(G + 1, 0.0);
+  s.gstmolfract.assign(G + 1, 0.0);
+  s.delr.assign(G + 1, 0.0);
+  s.disp_ratio.assign(G + 1, 0.0);
+  s.tran_ratio.assign(G + 1, 0.0);
+  s.rota_ratio.assign(G + 1, 0.0);
+  s.guest_insert.assign(G + 1, 0);
+  for (auto *v : {&s.mcinsf, &s.mcdelf, &s.mcdisf, &s.mcjmpf, &s.mcswpf, &s.mctraf, &s.mcrotf, &s.mcswif})
+    v->assign(G + 1, 0.0f);
+  s.nprob.assign(G + 1, 0);
+  s.lprobeng.assign(G + 1, 0);
+  for (int g = 1; g <= G; ++g) {
+    s.gstfuga[g] = s.gstpress[g] = d.fugacity[g - 1];
+    s.delr[g] = d.delr[g - 1];
+    s.disp_ratio[g] = d.disp_ratio[g - 1];
+    s.tran_ratio[g] = d.tran_ratio[g - 1];
+    s.rota_ratio[g] = d.rota_ratio[g - 1];
+    s.guest_insert[g] = d.create ? d.create[g - 1] : 0;
+    const float *f = d.move_freq + 8 * (g - 1);
+    s.mcinsf[g] = f[0];
+    s.mcdelf[g] = f[1];
+    s.mcdisf[g] = f[2];
+    s.mcjmpf[g] = f[3];
+    s.mcswpf[g] = f[4];
+    s.mctraf[g] = f[5];
+    s.mcrotf[g] = f[6];
+    s.mcswif[g] = f[7];
+    for (int k = 1; k < 8; ++k) need(f[k] >= f[k - 1], "move thresholds must be cumulative");
+    if (s.mcswpf[g] > s.mcjmpf[g] && G < 2) raise(FMC_ERR_INPUT, "swap moves need two guest types");
+    if (s.mcswif[g] > s.mcrotf[g] && G >= 3)
+      raise(FMC_ERR_INPUT, "switch moves with three or more guest types are not supported");
+  }
+  for (int i = 0; i < 9; ++i) s.ucell[i] = s.cell[i];  // no probability grids
+  invert3(s.ucell, s.rucell);
+  s.beta = 1.0 / (kKboltz * s.temp);
+  s.statvolm = s.volm * 1e-30;
+  build_derived(s);
+  if (s.newld != d.newld)
+    raise(FMC_ERR_INPUT, "fmc_upload_system: the host's newld (" + std::to_string(d.newld) +
+                             ") differs from the k-vectors of cell, kmax and alpha (" +
+                             std::to_string(s.newld) + ")");
+}
 
 void load_system(const std::string &dir, System &s) {
   scan_inputs(dir, s);

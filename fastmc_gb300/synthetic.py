@@ -60,14 +60,18 @@ class UnitCell:
     sigma: np.ndarray      # (4,) A
 
 
-def make_unit_cell(seed: int) -> UnitCell:
+def make_unit_cell(seed: int, natoms: int = ATOMS_PER_UNIT) -> UnitCell:
     """One 12.8 A unit cell: uniform positions with a 1.8 A periodic minimum
-    separation (rejection sampling), 48 atoms of each of 4 types."""
+    separation (rejection sampling), natoms / 4 atoms of each of 4 types
+    (192 for the benchmark frameworks; fewer gives an open framework for
+    tests that need accepted moves)."""
+    if natoms % N_FW_TYPES:
+        raise ValueError("natoms must be a multiple of the 4 framework types")
     rng = np.random.Generator(np.random.PCG64(seed))
-    pos = np.empty((ATOMS_PER_UNIT, 3))
+    pos = np.empty((natoms, 3))
     n = 0
     tries = 0
-    while n < ATOMS_PER_UNIT:
+    while n < natoms:
         tries += 1
         if tries > 1_000_000:
             raise RuntimeError("could not place framework atoms")
@@ -79,11 +83,11 @@ def make_unit_cell(seed: int) -> UnitCell:
                 continue
         pos[n] = p
         n += 1
-    types = np.repeat(np.arange(N_FW_TYPES), ATOMS_PER_UNIT // N_FW_TYPES)
+    types = np.repeat(np.arange(N_FW_TYPES), natoms // N_FW_TYPES)
     rng.shuffle(types)
     eps = rng.uniform(0.02, 0.10, size=N_FW_TYPES)
     sigma = rng.uniform(2.5, 3.8, size=N_FW_TYPES)
-    q = rng.normal(0.0, 0.4, size=ATOMS_PER_UNIT)
+    q = rng.normal(0.0, 0.4, size=natoms)
     q = q - q.mean()
     q = np.round(q, 10)
     q[-1] -= q.sum()  # exact zero in the written precision
@@ -167,7 +171,7 @@ def field_text(spec: GcmcSpec, uc: UnitCell) -> str:
         lines.append("finish")
     lines.append("Framework")
     lines.append(f"NUMMOLS {spec.ntile ** 3}")
-    lines.append(f"ATOMS {ATOMS_PER_UNIT}")
+    lines.append(f"ATOMS {len(uc.types)}")
     for t, q in zip(uc.types, uc.charges):
         lines.append(f"{FW_NAMES[t]:<8s}{20.0:14.6f}{q:20.12f}      1      1")
     lines.append("finish")
@@ -192,7 +196,7 @@ def field_text(spec: GcmcSpec, uc: UnitCell) -> str:
 def config_text(spec: GcmcSpec, uc: UnitCell) -> str:
     n = spec.ntile
     L = spec.box
-    natoms = ATOMS_PER_UNIT * n ** 3
+    natoms = len(uc.types) * n ** 3
     out = [spec.title, f"{0:10d}{2:10d}{natoms:10d}"]
     out.append(f"{L:20.12f}{0.0:20.12f}{0.0:20.12f}")
     out.append(f"{0.0:20.12f}{L:20.12f}{0.0:20.12f}")
@@ -202,7 +206,7 @@ def config_text(spec: GcmcSpec, uc: UnitCell) -> str:
         for iy in range(n):
             for iz in range(n):
                 off = np.array([ix, iy, iz], dtype=float) * UNIT_CELL
-                for a in range(ATOMS_PER_UNIT):
+                for a in range(len(uc.types)):
                     k += 1
                     p = uc.xyz[a] + off
                     out.append(f"{FW_NAMES[uc.types[a]]:<8s}{k:10d}")

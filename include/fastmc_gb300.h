@@ -109,6 +109,65 @@ typedef struct {
 
 int fmc_system_get_info(const fmc_system *sys, fmc_system_info *info);
 
+/* The same system from a host that has done the reference's start-up itself
+ * (gcmc.f:203-590) and holds its module arrays: the Fortran host's drop-in
+ * for fmc_system_load, so the library does not read the input files again.
+ * Each field names the reference variable it carries.  Arrays are 0-based
+ * copies of the 1-based Fortran ones (element i-1 holds x(i)); 2-D arrays
+ * are column-major, as Fortran stores them.  The library enumerates the
+ * k-vectors itself from cell, kmax and alpha (ewald.f:151-315) and refuses
+ * the system (FMC_ERR_INPUT) when their count differs from the host's newld;
+ * everything else, the tables included, is taken as given.  Guests are
+ * created on the device (create molecules), so guest molecule types carry
+ * nummols 0.  Replaces the host's hand-over of its start-up state; the
+ * reference has no such call because its energy routines read the module
+ * arrays directly (utility_pack.f:1-204, ewald_module.f, vdw_module.f). */
+typedef struct {
+  int imcon;               /* imcon: 1 cubic, 2 orthorhombic, 3 parallelepiped */
+  double cell[9];          /* cell(1..9) */
+  double engunit;          /* engunit (418.4 for UNITS kcal) */
+  double temp;             /* temp (K) */
+  double rcut;             /* rcut (A) */
+  double alpha;            /* alpha, the Ewald convergence parameter (1/A) */
+  int kmax[3];             /* kmax1, kmax2, kmax3 */
+  int newld;               /* the host's number of k-vectors */
+  double epsq;             /* epsq, relative dielectric constant */
+  double overlap;          /* overlap distance (A), before the host squares it */
+  double surftol;          /* surftol */
+  int eqsteps, nwindsteps, minchk, laccsample; /* main-loop control */
+  int ntpatm;              /* unique atom types */
+  int mxegrd;              /* table points */
+  double drewd;            /* erc grid spacing (A) */
+  double dlrpot;           /* vvv grid spacing (A) */
+  const double *erc;       /* erc(1..mxegrd), erfcgen's table */
+  int ntpvdw;              /* van der Waals table rows */
+  const double *vvv;       /* vvv(1..mxegrd, 1..ntpvdw), forgen's tables */
+  const int *ltpvdw;       /* ltpvdw(1..ntpvdw): 1 = 12-6, 2 = lj */
+  const double *prmvdw;    /* prmvdw(1..ntpvdw, 1..2) after define_van_der_waals */
+  const int *lstvdw;       /* lstvdw(1..ntpatm*(ntpatm+1)/2): table row per type pair */
+  const double *steadd;    /* steadd(1..ntpatm*(ntpatm+1)/2): lrcorrect's tail terms */
+  int maxmls;              /* molecule types */
+  const int *numatoms;     /* sites per molecule, per molecule type */
+  const int *nummols;      /* molecules per type (framework copies; 0 for guests) */
+  const int *is_guest;     /* 1 for the &guest molecule types */
+  const int *ltype;        /* site atom types 1..ntpatm, type after type */
+  const double *charge;    /* site charges, same layout */
+  const double *mass;      /* site masses, same layout */
+  const int *frozen;       /* site freeze flags, same layout */
+  const double *fw_xyz;    /* framework coordinates x,y,z per atom (molxxx/yyy/zzz) */
+  int ntpguest;            /* guest types (the &guest types in order) */
+  const double *guest_tmpl;/* guestx/y/z: each guest type's centred template */
+  const double *fugacity;  /* gstfuga(1..ntpguest), Pa */
+  const double *delr;      /* initial displacement size per guest type (A) */
+  const double *disp_ratio, *tran_ratio, *rota_ratio; /* acceptance targets */
+  const float *move_freq;  /* 8 cumulative REAL*4 thresholds per guest type, in
+                              the order mcinsf mcdelf mcdisf mcjmpf mcswpf mctraf
+                              mcrotf mcswif (as gcmc.f:341-386 leaves them) */
+  const int *create;       /* guest_insert per guest type, or NULL */
+} fmc_system_desc;
+
+int fmc_upload_system(const fmc_system_desc *desc, fmc_system **out);
+
 /* Override the fugacity (Pa) of guest type iguest (1-based) before creating
  * chains; used to build isotherms from one set of files. */
 int fmc_system_set_fugacity(fmc_system *sys, int iguest, double pascal);
@@ -250,6 +309,16 @@ typedef struct {
   int64_t prodcount;
   int64_t windows;
   int64_t device_ns;       /* device time of this chain's launches so far */
+  double guest_avg_n[FMC_MAX_GUEST_TYPES]; /* <N> of each guest type */
+  double guest_se_n[FMC_MAX_GUEST_TYPES];  /* its "standard error" as the
+                              reference prints it: the weighted standard
+                              deviation of the window averages */
+  /* SM clock cycles of the move loop per phase (0 proposal, 1 overlap test,
+   * 2 neighbour segments, 3 pair terms, 4 power tables, 5 k-space, 6 block
+   * reduction, 7 cluster exchange, 8 epilogue, 9 decision, 10 commit,
+   * 11 statistics); zero unless the library was built with
+   * FMC_PHASE_TIMERS */
+  int64_t phase_cycles[16];
 } fmc_chain_stats;
 
 /* One entry of the optional per-move log (parity tests). */

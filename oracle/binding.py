@@ -70,6 +70,7 @@ def load() -> C.CDLL:
             "orc_get_erc": (i, [vp, dp, i]),
             "orc_get_vvv": (i, [vp, i, dp, i]),
             "orc_set_prefilter": (None, [vp, i]),
+            "orc_get_array": (i, [vp, C.c_char_p, dp, i]),
             "orc_save_state": (i, [vp]),
             "orc_restore_state": (i, [vp]),
         }
@@ -123,6 +124,17 @@ class Oracle:
 
     def set_prefilter(self, on: bool):
         self.lib.orc_set_prefilter(self._h, int(on))
+
+    def array(self, name: str):
+        """A set-up array of the upload descriptor by field name."""
+        import numpy as np
+        n = self.lib.orc_get_array(self._h, name.encode(), None, 0)
+        if n < 0:
+            raise KeyError(name)
+        out = np.zeros(max(1, n))
+        self._ck(self.lib.orc_get_array(self._h, name.encode(),
+                                        out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
+        return out[:n]
 
     def save_state(self):
         self._ck(self.lib.orc_save_state(self._h))

@@ -3724,6 +3724,100 @@ int orc_create_molecules(orc_sim *h, int iguest, int nguests) {
 
 void orc_set_prefilter(orc_sim *h, int on) { h->s.prefilter_inserts = on != 0; }
 
+// The set-up arrays the library's fmc_upload_system takes, by the name of
+// its descriptor field, as doubles (0-based copies of the 1-based arrays,
+// 2-D arrays column-major): the oracle stands in for a host that has done
+// the reference's start-up.  Returns the element count (out == NULL: the
+// count only), -count when cap is too small, -1 for an unknown name.
+int orc_get_array(const orc_sim *h, const char *name, double *out, int cap) {
+  const Sim &s = h->s;
+  std::vector<double> v;
+  const std::string n = name ? name : "";
+  const int G = s.ntpguest;
+  auto per_site = [&](auto get) {
+    for (int m = 1; m <= s.maxmls; ++m)
+      for (int a = 1; a <= s.mol[m].natoms; ++a) v.push_back(get(s.mol[m], a));
+  };
+  if (n == "imcon") v = {double(s.imcon)};
+  else if (n == "cell") v.assign(s.cell, s.cell + 9);
+  else if (n == "engunit") v = {s.engunit};
+  else if (n == "temp") v = {s.temp};
+  else if (n == "rcut") v = {s.rcut};
+  else if (n == "alpha") v = {s.alpha};
+  else if (n == "kmax") v = {double(s.kmax1), double(s.kmax2), double(s.kmax3)};
+  else if (n == "newld") v = {double(s.newld)};
+  else if (n == "epsq") v = {s.epsq};
+  else if (n == "overlap") v = {std::sqrt(s.overlap)};
+  else if (n == "surftol") v = {s.surftol};
+  else if (n == "eqsteps") v = {double(s.eqsteps)};
+  else if (n == "nwindsteps") v = {double(s.nwindsteps)};
+  else if (n == "minchk") v = {double(s.minchk)};
+  else if (n == "laccsample") v = {s.laccsample ? 1.0 : 0.0};
+  else if (n == "ntpatm") v = {double(s.ntpatm)};
+  else if (n == "mxegrd") v = {double(s.mxegrd)};
+  else if (n == "drewd") v = {s.drewd};
+  else if (n == "dlrpot") v = {s.dlrpot};
+  else if (n == "erc") v.assign(s.erc.begin() + 1, s.erc.begin() + 1 + s.mxegrd);
+  else if (n == "ntpvdw") v = {double(s.ntpvdw)};
+  else if (n == "vvv") {
+    for (int k = 1; k <= s.ntpvdw; ++k)
+      for (int i = 1; i <= s.mxegrd; ++i) v.push_back(s.vvv[k][i]);
+  } else if (n == "ltpvdw") {
+    for (int k = 1; k <= s.ntpvdw; ++k) v.push_back(s.ltpvdw[k]);
+  } else if (n == "prmvdw") {
+    for (int c = 1; c <= 2; ++c)
+      for (int k = 1; k <= s.ntpvdw; ++k) v.push_back(s.prmvdw[k][c]);
+  } else if (n == "lstvdw" || n == "steadd") {
+    const int np = s.ntpatm * (s.ntpatm + 1) / 2;
+    for (int p = 1; p <= np; ++p) v.push_back(n == "lstvdw" ? double(s.lstvdw[p]) : s.steadd[p]);
+  } else if (n == "maxmls") v = {double(s.maxmls)};
+  else if (n == "numatoms" || n == "nummols" || n == "is_guest") {
+    for (int m = 1; m <= s.maxmls; ++m)
+      v.push_back(n == "numatoms" ? s.mol[m].natoms
+                  : n == "nummols" ? s.mol[m].nummols : (s.mol[m].guest ? 1 : 0));
+  } else if (n == "ltype") per_site([](const MolType &m, int a) { return double(m.ltp[a]); });
+  else if (n == "charge") per_site([](const MolType &m, int a) { return m.chg[a]; });
+  else if (n == "mass") per_site([](const MolType &m, int a) { return m.wght[a]; });
+  else if (n == "frozen") per_site([](const MolType &m, int a) { return double(m.frz[a]); });
+  else if (n == "fw_xyz") {
+    for (int m = 1; m <= s.maxmls; ++m)
+      if (!s.mol[m].guest)
+        for (int i = 1; i <= s.mol[m].nummols * s.mol[m].natoms; ++i) {
+          v.push_back(s.mol[m].mx[i]);
+          v.push_back(s.mol[m].my[i]);
+          v.push_back(s.mol[m].mz[i]);
+        }
+  } else if (n == "ntpguest") v = {double(G)};
+  else if (n == "guest_tmpl") {
+    for (int g = 1; g <= G; ++g)
+      for (int i = 1; i <= s.mol[s.locguest[g]].natoms; ++i) {
+        v.push_back(s.guestx[g][i]);
+        v.push_back(s.guesty[g][i]);
+        v.push_back(s.guestz[g][i]);
+      }
+  } else if (n == "fugacity" || n == "delr" || n == "disp_ratio" || n == "tran_ratio" ||
+             n == "rota_ratio") {
+    const std::vector<double> &a = n == "fugacity" ? s.gstfuga : n == "delr" ? s.delr
+                                   : n == "disp_ratio" ? s.disp_ratio
+                                   : n == "tran_ratio" ? s.tran_ratio : s.rota_ratio;
+    for (int g = 1; g <= G; ++g) v.push_back(a[g]);
+  } else if (n == "move_freq") {
+    for (int g = 1; g <= G; ++g)
+      for (const auto *a : {&s.mcinsf, &s.mcdelf, &s.mcdisf, &s.mcjmpf, &s.mcswpf, &s.mctraf,
+                            &s.mcrotf, &s.mcswif})
+        v.push_back((*a)[g]);
+  } else if (n == "create") {
+    for (int g = 1; g <= G; ++g) v.push_back(s.guest_insert[g]);
+  } else {
+    return -1;
+  }
+  const int cnt = (int)v.size();
+  if (!out) return cnt;  // size query
+  if (cap < cnt) return -cnt;
+  for (int i = 0; i < cnt; ++i) out[i] = v[i];
+  return cnt;
+}
+
 int orc_save_state(orc_sim *h) {
   return guarded([&] {
     h->saved = std::make_unique<Sim>(h->s);

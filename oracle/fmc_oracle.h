@@ -111,6 +111,12 @@ int orc_create_molecules(orc_sim *s, int iguest, int nguests);
  * generator's sequence are the same with it on or off. */
 void orc_set_prefilter(orc_sim *s, int on);
 
+/* The set-up arrays of fmc_upload_system's descriptor (fmc_system_desc),
+ * by field name, as doubles: the oracle playing the Fortran host that has
+ * done the reference's start-up.  Returns the element count (out == NULL:
+ * the count only), -count when cap is too small, -1 for an unknown name. */
+int orc_get_array(const orc_sim *s, const char *name, double *out, int cap);
+
 /* Keep a copy of the whole simulation state (coordinates, S(k), energies,
  * counters, generator) and put it back: replays of one state. 0 or -1. */
 int orc_save_state(orc_sim *s);

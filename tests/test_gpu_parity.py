@@ -466,3 +466,121 @@ def test_gpu_swap_pending_refuses_other_moves(fmc_lib, inputs_dir):
     assert np.array_equal(p.sk(), s0)
     with pytest.raises(fmc_lib.FmcError):
         L.check(L.load().fmc_swap_finish(p._h, 0))
+
+
+def _calf20_positions(o, n, seed, iguest=1):
+    """Trial positions of a guest inside CALF-20's parallelepiped cell (random
+    fractional centre and orientation) that the oracle finds free of overlap."""
+    cell = np.array(o.array("cell")).reshape(3, 3)
+    tm = np.array(o.array("guest_tmpl"))[:9].reshape(3, 3) if iguest == 1 else None
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(20000):
+        th = rng.uniform(0, 2 * math.pi)
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        c, s = math.cos(th), math.sin(th)
+        K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+        R = np.eye(3) + s * K + (1 - c) * K @ K
+        xyz = tm @ R.T + rng.uniform(0, 1, 3) @ cell
+        if not o.insertion_energy(iguest, xyz)["overlap"]:
+            out.append(xyz)
+            if len(out) == n:
+                break
+    return out
+
+
+def test_gpu_calf20_per_move_fp64(fmc_lib, oracle_lib):
+    """The per-move C ABI on the reference's own test system (CALF-20,
+    parallelepiped cell, imcon 3, two guest types) against the oracle:
+    insertions, deletions, displacements and the committed S(k), FP64."""
+    o = oracle_lib.Oracle(CALF20)
+    sysm = fmc_lib.System.load(CALF20)
+    assert sysm.info().imcon == 3
+    plain = fmc_lib.PlainEngine(sysm, fmc_lib.FMC_PREC_FP64, 64)
+    maxmls = sysm.info().maxmls
+    pos = _calf20_positions(o, 16, seed=3)
+    assert len(pos) >= 12
+    inserted = 0
+    for xyz in pos:
+        ref = o.insertion_energy(1, xyz)
+        _cmp(plain.insertion(1, xyz), ref, maxmls)
+        ok = not ref["overlap"]
+        assert plain.commit(0.0) == ok
+        o.apply_move(1, 1, 0, xyz, ok)
+        inserted += ok
+        if inserted == 10:
+            break
+    assert inserted >= 8
+    assert np.allclose(plain.coords(1), o.coords(o.locguest(1)), rtol=0, atol=1e-12)
+    for c in range(1, inserted + 1):
+        _cmp(plain.deletion(1, c), o.deletion_energy(1, c), maxmls)
+    rng = np.random.default_rng(8)
+    nd = 0
+    for _ in range(40):
+        c = int(rng.integers(1, inserted + 1))
+        th = rng.uniform(0, 0.8)
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        abcq = [*rng.uniform(-0.4, 0.4, 3), math.cos(th / 2), *(math.sin(th / 2) * ax)]
+        ref = o.displace_energy(1, c, abcq)
+        _cmp(plain.displace(1, c, abcq), ref, maxmls, keys=("estep",))
+        nd += not ref["overlap"]
+    assert nd >= 10
+    plain.deletion(1, 2)
+    plain.commit(0.0)
+    o.apply_move(2, 1, 2, None, True)
+    sg, so = plain.sk(), o.sk()
+    assert np.allclose(sg, so, rtol=1e-10, atol=1e-10 * np.abs(so).max())
+
+
+def test_gpu_calf20_chain_fp64(fmc_lib, oracle_lib):
+    """A device-resident FP64 chain on CALF-20 with the test's CONTROL (CO2
+    and N2, insert / delete / displace, probability grids) follows the
+    oracle move by move on the parallelepiped cell."""
+    n = 3000
+    o = oracle_lib.Oracle(CALF20)
+    o.seed(12345)
+    ref = o.run(n)
+    b = fmc_lib.Batch([fmc_lib.System.load(CALF20)], [{"seed": 12345}],
+                      precision=fmc_lib.FMC_PREC_FP64, guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    nacc = nfull = 0
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.iguest, g.choice, g.overlap, g.accepted) == \
+               (r.move, r.iguest, r.choice, r.overlap, r.accepted), i
+        assert g.rande == r.rande, i
+        if not r.overlap:
+            assert close(g.estep, r.estep, scale=1e-6), (i, g.estep, r.estep)
+            nfull += 1
+        nacc += r.accepted
+    assert nacc >= 50 and nfull >= 200
+    st = b.stats()[0]
+    assert st.nummols == o.nummols(o.locguest(1))
+
+
+def test_gpu_window_statistics_two_guests_fp64(fmc_lib, oracle_lib, inputs_dir):
+    """Per guest type <N> and the reference's "standard error" (the weighted
+    standard deviation of the window averages, gcmc.f:1218-1241) from the
+    device chain's windows equal the oracle's."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=10,
+                               move_mix=(("insert", 0.1), ("displace", 0.3), ("jump", 0.3),
+                                         ("rotate", 0.3)))
+    spec.overlap = 1.0
+    spec.second_guest = True
+    spec.create2 = 8
+    spec.steps = 100  # 100-move windows
+    d = inputs_dir(spec, "gpu_two_guests_windows")
+    n = 400
+    o, _ = _two_guest_oracle(oracle_lib, d, n)
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 7}], precision=fmc_lib.FMC_PREC_FP64,
+                      guest_capacity=64)
+    b.run(n)
+    st = b.stats()[0]
+    assert st.windows == 4
+    for g in (1, 2):
+        ref = o.stats(g)
+        assert close(st.guest_avg_n[g - 1], ref[0], rel=1e-12, scale=1e-12), (g, st.guest_avg_n[g - 1], ref[0])
+        assert close(st.guest_se_n[g - 1], ref[29], rel=1e-9, scale=1e-9), (g, st.guest_se_n[g - 1], ref[29])

@@ -189,3 +189,51 @@ def test_reference_isotherm_inputs_load(fmc_lib, tmp_path):
         assert info.ntpguest == 2 and info.imcon == 3
         p, _, _ = control_numbers(ctl)
         assert abs(sum(info.fugacity[:2]) - p * 1e5) < 1e-6 * p * 1e5
+
+
+UPLOAD_FIELDS = ("imcon", "cell", "engunit", "temp", "rcut", "alpha", "kmax", "newld", "epsq",
+                 "overlap", "surftol", "eqsteps", "nwindsteps", "minchk", "laccsample", "ntpatm",
+                 "mxegrd", "drewd", "dlrpot", "erc", "ntpvdw", "vvv", "ltpvdw", "prmvdw", "lstvdw",
+                 "steadd", "maxmls", "numatoms", "nummols", "is_guest", "ltype", "charge", "mass",
+                 "frozen", "fw_xyz", "ntpguest", "guest_tmpl", "fugacity", "delr", "disp_ratio",
+                 "tran_ratio", "rota_ratio", "move_freq", "create")
+
+
+def host_arrays(oracle_lib, d):
+    """The start-up arrays of a host that read the inputs in `d` itself (the
+    oracle plays that host), by fmc_system_desc field name."""
+    o = oracle_lib.Oracle(d)
+    return {k: o.array(k) for k in UPLOAD_FIELDS}
+
+
+@pytest.mark.parametrize("which", ["synthetic", "calf20"])
+def test_upload_system_matches_load(fmc_lib, oracle_lib, inputs_dir, which):
+    """fmc_upload_system from a host's arrays gives the system
+    fmc_system_load builds from the files (orthorhombic and parallelepiped
+    cells)."""
+    from conftest import CALF20
+    d = CALF20 if which == "calf20" else inputs_dir(
+        syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=10), "upload")
+    a = fmc_lib.System.load(d).info()
+    b = fmc_lib.System.upload(host_arrays(oracle_lib, d)).info()
+    for name, _ in a._fields_:
+        va, vb = getattr(a, name), getattr(b, name)
+        if hasattr(va, "__len__"):
+            va, vb = list(va), list(vb)
+        if name in ("mcsteps",):
+            continue  # a run length the descriptor does not carry
+        assert va == vb, (name, va, vb)
+
+
+def test_upload_system_refuses_inconsistent_arrays(fmc_lib, oracle_lib, inputs_dir):
+    from fastmc_gb300 import _lib as L
+    d = inputs_dir(syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0), "upload_bad")
+    arr = host_arrays(oracle_lib, d)
+    bad = dict(arr, newld=arr["newld"] + 1)
+    with pytest.raises(fmc_lib.FmcError) as e:
+        fmc_lib.System.upload(bad)
+    assert e.value.code == L.FMC_ERR_INPUT and "newld" in str(e.value)
+    bad = dict(arr, lstvdw=np.full_like(arr["lstvdw"], 99))
+    with pytest.raises(fmc_lib.FmcError) as e:
+        fmc_lib.System.upload(bad)
+    assert e.value.code == L.FMC_ERR_ARG
