@@ -77,9 +77,10 @@ def algorithmic_flops_per_eval(cutoff: float, nk: int) -> float:
 
 
 def trial_evals(st) -> int:
-    """Energy evaluations of the trial moves in a chain's counters."""
+    """Energy evaluations of the trial moves in a chain's counters (a swap
+    is a deletion and an insertion)."""
     a = st.attempts
-    return int(a[0] + a[1] + 2 * (a[2] + a[3] + a[4] + a[5]))
+    return int(a[0] + a[1] + 2 * (a[2] + a[3] + a[4] + a[5] + a[6]))
 
 
 def workload(tmp: str):
@@ -312,7 +313,7 @@ def reduce_over_ranks(dist, device, max_vals, sum_vals):
     return [float(x) for x in t.tolist()], [float(x) for x in e.tolist()]
 
 
-def plain_paths(F, batch, systems, specs, snap_stats, moves, clusters):
+def plain_paths(F, batch, systems, dirs, specs, snap_stats, moves, clusters):
     """The single-chain GPU paths on the same workload and states:
     - "device": every chain run alone (the others paused), from its
       pre-loaded state, on the cluster size that is fastest for a lone chain
@@ -354,47 +355,104 @@ def plain_paths(F, batch, systems, specs, snap_stats, moves, clusters):
                      "workload": "the same 64 chains and states, one chain at a time (FP32, "
                                  "device-resident), cluster per framework " +
                                  str([best[f] for f in range(len(systems))])}
-    rng = np.random.default_rng(1)
-    tot_ev, tot_s = 0, 0.0
+    out["per_move_abi"] = per_move_abi(F, batch, systems, dirs, specs)
+    return out
+
+
+def per_move_abi(F, batch, systems, dirs, specs, seconds=1.0):
+    """The drop-in path: one C-ABI call per trial move and one per commit,
+    driven from the host through ctypes the way a Fortran host calls it
+    (FP64; insert / delete / displace / rotate in equal shares, the draws
+    made ahead with numpy), on chain 8 of each framework loaded with that
+    chain's pre-loaded molecules, for about `seconds` each.  Beside it the
+    CPU oracle on one core runs the same moves with the same decisions
+    (energy routine, then the commit), the serial host path the drop-in
+    replaces.  Both in trial-move evaluations per second."""
+    import ctypes as C
+    import numpy as np
+    from fastmc_gb300 import _lib as L
+    from oracle.binding import Oracle
+    lib = L.load()
+    res = L.MoveResult()
+    acc = C.c_int()
+    dp = C.POINTER(C.c_double)
+    tot = {"gpu_ev": 0, "gpu_s": 0.0, "cpu_ev": 0, "cpu_s": 0.0}
     for f in range(len(systems)):
         c = [i for i, s in enumerate(specs) if s["system"] == f][8]
         x, m = batch.coords(c)
-        L = systems[f].info().cell[0]
+        mols = x[:9 * m].reshape(m, 3, 3)
+        L_box = systems[f].info().cell[0]
         p = F.PlainEngine(systems[f], F.FMC_PREC_FP64, 1024)
-        for mol in x[:9 * m].reshape(m, 3, 3):
+        for mol in mols:
             p.insertion(1, mol)
             p.commit(0.0)
         nm = p.nummols(1)
-        t0 = time.perf_counter()
+        rng = np.random.default_rng(1 + f)
+        nplan = 20000
+        kinds = rng.integers(0, 4, nplan)
+        u = rng.random(nplan)
+        rande = rng.random(nplan)
+        ax = rng.normal(size=(nplan, 3))
+        ax /= np.linalg.norm(ax, axis=1)[:, None]
+        ins = np.ascontiguousarray(np.einsum("i,nj->nij", np.array([0.0, 1.16, -1.16]), ax) +
+                                   rng.uniform(0, L_box, (nplan, 1, 3)))
+        th = rng.uniform(0, math.pi / 3, nplan)
+        abcq = np.zeros((nplan, 7))
+        abcq[:, :3] = rng.uniform(-0.25, 0.25, (nplan, 3))
+        abcq[kinds == 3, :3] = 0.0  # rotation: no shift
+        abcq[:, 3] = np.cos(th / 2)
+        abcq[:, 4:] = np.sin(th / 2)[:, None] * ax
+        done = []  # (kind, choice, accepted) to replay on the CPU
         evals = 0
-        while time.perf_counter() - t0 < 1.0:
-            k = int(rng.integers(4)) if nm else 0
-            if k == 0:
-                ax = rng.normal(size=3)
-                ax /= np.linalg.norm(ax)
-                p.insertion(1, np.outer([0.0, 1.16, -1.16], ax) + rng.uniform(0, L, 3))
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < seconds and k < nplan:
+            kd = int(kinds[k]) if nm else 0
+            ch = 1 + int(u[k] * nm) if nm else 0
+            if kd == 0:
+                lib.fmc_insertion(p._h, 1, ins[k].ctypes.data_as(dp), C.byref(res))
                 evals += 1
-            elif k == 1:
-                p.deletion(1, int(rng.integers(1, nm + 1)))
+            elif kd == 1:
+                lib.fmc_deletion(p._h, 1, ch, C.byref(res))
                 evals += 1
             else:
-                th = rng.uniform(0, math.pi / 3)
-                ax = rng.normal(size=3)
-                ax /= np.linalg.norm(ax)
-                sh = rng.uniform(-0.25, 0.25, 3) if k == 2 else np.zeros(3)
-                p.displace(1, int(rng.integers(1, nm + 1)),
-                           [*sh, math.cos(th / 2), *(math.sin(th / 2) * ax)])
+                lib.fmc_displace(p._h, 1, ch, abcq[k].ctypes.data_as(dp), C.byref(res))
                 evals += 2
-            p.commit(float(rng.random()))
-            nm = p.nummols(1)
-        tot_s += time.perf_counter() - t0
-        tot_ev += evals
+            lib.fmc_metropolis_commit(p._h, float(rande[k]), C.byref(acc))
+            done.append((kd, ch, acc.value))
+            nm += acc.value if kd == 0 else (-acc.value if kd == 1 else 0)
+            k += 1
+        tot["gpu_s"] += time.perf_counter() - t0
+        tot["gpu_ev"] += evals
         p.close()
-    out["per_move_abi"] = {"value": tot_ev / tot_s, "unit": UNIT,
-                           "workload": "chain 8 of each framework, its pre-loaded molecules, FP64, "
-                                       "host-driven per-move C ABI (insert/delete/displace/rotate), "
-                                       "wall time"}
-    return out
+        # the same moves and decisions on the oracle, one core
+        o = Oracle(dirs[f])
+        for mol in mols:
+            o.apply_move(1, 1, 0, mol, True)
+        t0 = time.perf_counter()
+        cev = 0
+        for k, (kd, ch, a) in enumerate(done[:2000]):
+            if kd == 0:
+                o.insertion_energy(1, ins[k])
+                o.apply_move(1, 1, 0, ins[k], bool(a))
+                cev += 1
+            elif kd == 1:
+                o.deletion_energy(1, ch)
+                o.apply_move(2, 1, ch, None, bool(a))
+                cev += 1
+            else:
+                o.displace_energy(1, ch, abcq[k])
+                o.apply_move(3, 1, ch, abcq[k], bool(a))
+                cev += 2
+        tot["cpu_s"] += time.perf_counter() - t0
+        tot["cpu_ev"] += cev
+        o.close()
+    gpu = tot["gpu_ev"] / tot["gpu_s"]
+    cpu = tot["cpu_ev"] / tot["cpu_s"]
+    return {"value": gpu, "unit": UNIT, "oracle_1core_same_moves": cpu, "ratio_to_1core": gpu / cpu,
+            "workload": "chain 8 of each framework with its pre-loaded molecules, FP64, one C-ABI "
+                        "call per move and one per commit from the host (ctypes), wall time; the "
+                        "oracle replays the first 2000 of those moves with the same decisions"}
 
 
 def config5_widom(F, tmp):
@@ -593,7 +651,7 @@ def run_ours(args, rank, world, local_rank):
             "cpu_baseline_1core": cpu1,
         }
         if not args.no_plain:
-            out["plain_single_chain"] = plain_paths(F, batch, systems, specs, snap, args.moves,
+            out["plain_single_chain"] = plain_paths(F, batch, systems, dirs, specs, snap, args.moves,
                                                     per_chain)
         if args.widom:
             out["config5_widom"] = config5_widom(F, tmp)

@@ -25,7 +25,8 @@ MAX_MOLTYPES = 8
 MAX_GUEST_TYPES = 4
 MAX_SITES = 8
 
-MOVE_NAMES = {1: "insert", 2: "delete", 3: "displace", 4: "translate", 5: "rotate", 6: "jump"}
+MOVE_NAMES = {1: "insert", 2: "delete", 3: "displace", 4: "translate", 5: "rotate", 6: "jump",
+              7: "swap"}
 
 
 class SystemInfo(C.Structure):
@@ -88,7 +89,7 @@ class ChainSpec(C.Structure):
 
 class ChainStats(C.Structure):
     _fields_ = [("moves", C.c_int64), ("evals", C.c_int64), ("overlap_exits", C.c_int64),
-                ("attempts", C.c_int64 * 6), ("accepts", C.c_int64 * 6),
+                ("attempts", C.c_int64 * 8), ("accepts", C.c_int64 * 8),
                 ("nummols", C.c_int), ("status", C.c_int), ("energy", C.c_double),
                 ("avg_n", C.c_double), ("avg_e", C.c_double), ("avg_en", C.c_double),
                 ("avg_n2", C.c_double), ("avg_e2", C.c_double), ("avg_nf", C.c_double),
@@ -144,6 +145,7 @@ SIGNATURES = {
     "fmc_batch_get_stats": (C.c_int, [vp, C.POINTER(ChainStats)]),
     "fmc_batch_get_log": (C.c_int, [vp, C.c_int, C.POINTER(MoveLog), C.c_int, ip]),
     "fmc_batch_get_coords": (C.c_int, [vp, C.c_int, dp, C.c_int, ip]),
+    "fmc_batch_get_coords_type": (C.c_int, [vp, C.c_int, C.c_int, dp, C.c_int, ip]),
     "fmc_batch_get_sk": (C.c_int, [vp, C.c_int, dp, C.c_int]),
     "fmc_batch_last_timing": (C.c_int, [vp, dp, i64p, i64p]),
     "fmc_batch_cycle_bytes": (C.c_int, [vp, i64p, i64p]),

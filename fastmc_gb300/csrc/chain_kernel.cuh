@@ -142,6 +142,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (threadIdx.x == 32) run_deferred<F32, GN>(B);
       propose(B, CA, chain, kPropMC, 0);
       FMC_PHASE(B, 0);
+      if (B.mc.kind == 7) {  // mc_swap: evaluation, decision, commit or rollback, statistics
+        swap_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);
+        if (B.S.prob_nsub > 0 && CA.grid && B.H.production) store_prob(B, CA, chain);
+        __syncthreads();
+        continue;
+      }
       int full = 0;
       if (B.mc.kind != 0) full = evaluate_any<F32, GN>(B, CA, chain, st);
       if (threadIdx.x == 0) {
@@ -215,7 +221,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       B.mc.evaluated = 1;
       B.mc.accepted = 0;
       (void)full;
-      gctx[chain] = B.mc;
     }
   } else if (mode == kModeWidom) {
     double hsum = 0.0;
@@ -241,17 +246,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       wj.partial[3 * blockIdx.x + 2] = (double)ntot;
     }
   } else if (mode == kModeCommit) {
+    // nmoves carries the host's decision (0 or 1), or -1 for energy_eval
+    // on the device with the rande in gctx
     if (threadIdx.x == 0) {
       B.mc = gctx[chain];
       if (B.mc.forced) B.mc.accepted = B.mc.overlap ? 0 : 1;  // accept_move called directly
+      else if (nmoves >= 0) B.mc.accepted = nmoves;
       else decide(B, false);
     }
     __syncthreads();
     commit(B, CA, chain, st);
-    if (threadIdx.x == 0) {
-      B.mc.evaluated = 0;
-      gctx[chain] = B.mc;
-    }
+    if (threadIdx.x == 0) B.mc.evaluated = 0;
   }
   if (st) atomicOr(&B.flags[0], st);
   __syncthreads();
@@ -289,6 +294,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (threadIdx.x == 0) {
     B.H.status |= B.flags[0];
     B.H.dev_ns += (long long)(global_ns() - t_start);
+    if ((mode == kModeEval || mode == kModeCommit) && rank == 0) {
+      B.mc.dev_status = B.H.status;  // read back with the move: no separate status read
+      gctx[chain] = B.mc;
+    }
   }
   __syncthreads();
   if (rank == 0) block_copy(hdrs + chain, &B.H);

@@ -197,7 +197,7 @@ struct ChainHdr {
   double wsq[kMaxG];       // sum over windows of weight x <N>_window^2 (standard error)
   long long windows;
   long long moves, evals, overlap_exits;
-  long long attempts[6], accepts[6];  // insert, delete, displace, translate, rotate, jump
+  long long attempts[8], accepts[8];  // insert, delete, displace, translate, rotate, jump, swap, switch
   long long log_n;
   int system;
   int pad1;
@@ -242,6 +242,8 @@ struct ChainArrays {
                     // there and an accepted move flips ChainHdr::skb
   double2 *snew;    // [chain][nkmax] scratch s(k) of the evaluated position
   double2 *sold;    // [chain][nkmax] scratch s(k) of the old position
+  double2 *sksave;  // [chain][2][nkmax] FP64 path, systems with swap moves: the two
+                    // guest types' S(k) before a swap, for its rejection (else null)
   const float4 *trig;  // [kTrigN] sin(2 pi k/kTrigN) hi, lo, cos(2 pi k/kTrigN) hi, lo
   double *grid;        // [chain][subgrid][bin] probability grids (null: none)
   size_t grid_stride;  // doubles per chain
@@ -300,6 +302,7 @@ struct MoveCtx {
   int evaluated;
   int npos;           // 1 or 2 positions evaluated
   int forced;         // commit mode: accept without a decision (a swap's halves)
+  int dev_status;     // per-move ABI: the chain's status word after the launch
   double pos[2][kMaxS][3];   // [0] = new / inserted / deleted, [1] = old (displace)
   double estep;
   double rande;

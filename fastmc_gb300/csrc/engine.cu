@@ -663,7 +663,7 @@ struct Chains {
   DBuf<double> gpos;
   DBuf<float4> ghi, glo;
   DBuf<int> ord, freel;
-  DBuf<double2> sk, snew, sold;
+  DBuf<double2> sk, snew, sold, sksave;
   DBuf<float4> skdf, skdf2;
   DBuf<float4> trig;  // sin/cos(2 pi k / kTrigN) hi/lo pairs
   DBuf<double> grid;  // probability grids [chain][subgrid][bin]
@@ -906,6 +906,13 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   C.sold.alloc((size_t)nchains * nkmax);
   C.snew.zero();
   C.sold.zero();
+  {  // FP64 chains with swap moves keep the two guest types' S(k) for a rejection
+    bool swaps = false;
+    for (int i = 0; i < nsys; ++i)
+      for (int g = 1; g <= systems[i]->ntpguest; ++g)
+        if (systems[i]->mcswpf[g] > systems[i]->mcjmpf[g]) swaps = true;
+    if (swaps && precision == FMC_PREC_FP64) C.sksave.alloc((size_t)nchains * 2 * nkmax);
+  }
   C.skdf.alloc((size_t)nchains * kMaxG * nkmax);
   C.skdf.zero();
   if (precision == FMC_PREC_FP32) {
@@ -950,6 +957,7 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   CA.skdf = C.skdf.p;
   CA.snew = C.snew.p;
   CA.sold = C.sold.p;
+  CA.sksave = C.sksave.p;
   CA.skdf2 = C.skdf2.p;
   FMC_CUDA(cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking));
   FMC_CUDA(cudaEventCreate(&C.ev0));
@@ -981,7 +989,7 @@ void fill_stats(const Chains &C, fmc_chain_stats *out) {
     o.moves = h.moves;
     o.evals = h.evals;
     o.overlap_exits = h.overlap_exits;
-    for (int i = 0; i < 6; ++i) {
+    for (int i = 0; i < 8; ++i) {
       o.attempts[i] = h.attempts[i];
       o.accepts[i] = h.accepts[i];
     }
@@ -1147,7 +1155,23 @@ struct fmc_plain {
   fmc_system_info info{};
   int has_move = 0;
   std::unique_ptr<ChainSnapshot> swap_saved;  // set while a swap awaits fmc_swap_finish
+  // pinned host copies of the move record (one copy each way per evaluation)
+  MoveCtx *pin_in = nullptr, *pin_out = nullptr;
+  MoveCtx last{};                // the last evaluated move, for the host's decision
+  int nummols[kMaxG] = {};       // host mirror of the guest counts (energy_eval's N)
+  int swap_nummols[kMaxG] = {};  // the mirror before a pending swap
+  ~fmc_plain() {
+    if (pin_in) cudaFreeHost(pin_in);
+    if (pin_out) cudaFreeHost(pin_out);
+  }
 };
+
+// The per-move ABI runs its commit kernels asynchronously; everything that
+// reads the engine's device state on another stream or on the host waits
+// for them first.
+static void settle(const fmc_plain *h) {
+  FMC_CUDA(cudaStreamSynchronize(h->C.stream));
+}
 
 struct fmc_batch {
   Chains C;
@@ -1387,6 +1411,8 @@ int fmc_plain_create(const fmc_system *sys, int precision, int guest_capacity, f
     fmc_chain_spec spec{0, -1.0, 1, 0};
     init_chains(h->C, &sp, 1, &spec, 1, precision, guest_capacity);
     h->C.CA.resident = 0;  // one move per launch: guests stay in global memory
+    FMC_CUDA(cudaMallocHost(&h->pin_in, sizeof(MoveCtx)));
+    FMC_CUDA(cudaMallocHost(&h->pin_out, sizeof(MoveCtx)));
     *out = h.release();
     return FMC_OK;
   });
@@ -1400,6 +1426,7 @@ int fmc_plain_destroy(fmc_plain *h) {
 int fmc_full_ewald(fmc_plain *h, double *out4) {
   return guard([&] {
     if (!h || !out4) raise(FMC_ERR_ARG, "null argument");
+    settle(h);
     Chains &C = h->C;
     C.normalize_sk();
     const System &s = *C.hsys[0];
@@ -1481,12 +1508,21 @@ static int plain_eval(fmc_plain *h, MoveCtx &mc, fmc_move_result *res, bool gues
   if (h->swap_saved) raise(FMC_ERR_STATE, "a swap awaits fmc_swap_finish");
   const System &s = *C.hsys[0];
   mc.evaluated = 0;
-  FMC_CUDA(cudaMemcpyAsync(C.ctx.p, &mc, sizeof(MoveCtx), cudaMemcpyHostToDevice, C.stream));
+  // the move up, one launch (after any commit still queued), the move back
+  // with the chain's status word, one synchronisation
+  *h->pin_in = mc;
+  FMC_CUDA(cudaMemcpyAsync(C.ctx.p, h->pin_in, sizeof(MoveCtx), cudaMemcpyHostToDevice, C.stream));
   C.launch(kModeEval, 0);
-  MoveCtx out;
-  FMC_CUDA(cudaMemcpyAsync(&out, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost, C.stream));
+  FMC_CUDA(cudaMemcpyAsync(h->pin_out, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost, C.stream));
   C.sync();
-  C.check_status();
+  const MoveCtx &out = *h->pin_out;
+  if (out.dev_status) {
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "the chain raised device status 0x%x (see fmc_batch status bits)",
+                  out.dev_status);
+    raise(FMC_ERR_DEVICE, buf);
+  }
+  h->last = out;
   h->has_move = 1;
   if (res) {
     std::memset(res, 0, sizeof *res);
@@ -1500,7 +1536,7 @@ static int plain_eval(fmc_plain *h, MoveCtx &mc, fmc_move_result *res, bool gues
     res->overlap = out.overlap;
     res->surface = out.surf_new;
     res->surface_old = out.surf_old;
-    res->status = C.host_hdr[0].status;
+    res->status = out.dev_status;
     for (int i = 0; i < out.ns && i < FMC_MAX_SITES; ++i)
       for (int d = 0; d < 3; ++d) res->newxyz[3 * i + d] = out.pos[0][i][d];
   }
@@ -1582,21 +1618,47 @@ int fmc_displace(fmc_plain *h, int iguest, int choice, const double *abcq, fmc_m
   });
 }
 
+// energy_eval (utility_pack.f:3637-3693) for the last evaluated move, on the
+// host as the reference runs it, FP64: with N the guest count before the
+// move, insert V f / ((N+1) kB T) e^{-beta dE}, delete N kB T / (V f)
+// e^{-beta dE} (1 when f is zero), displace e^{-beta dE}, the exponent
+// clamped at +-700; accepted when rande < test.  A displacement with
+// estep < 0 is accepted without rande (gcmc.f:1879-1886); an overlapping
+// insertion or displacement is rejected.
+static int host_energy_eval(const fmc_plain *h, double rande) {
+  const MoveCtx &m = h->last;
+  const System &s = *h->C.hsys[0];
+  if (m.kind == 0) return 0;
+  if ((m.kind == 1 || m.kind >= 3) && m.overlap) return 0;
+  if (m.kind >= 3 && m.estep < 0.0) return 1;
+  const int g = m.g;
+  const double eng = m.kind == 2 ? -m.estep : m.estep;
+  const double ipress = s.gstfuga[g + 1];
+  const int ing = h->nummols[g];
+  double test = 0.0;
+  if (-s.beta * eng > 700.0) test = std::exp(700.0);
+  else if (s.beta * eng > 700.0) test = std::exp(-700.0);
+  else if (m.kind >= 3) test = std::exp(-1.0 * s.beta * eng);
+  else if (m.kind == 1)
+    test = s.statvolm * ipress / ((double(ing) + 1.0) * fmc::kBoltz * s.temp) * std::exp(-1.0 * s.beta * eng);
+  else if (std::fabs(ipress) < 1.0e-7) test = 1.0;
+  else test = double(ing) * fmc::kBoltz * s.temp / (s.statvolm * ipress) * std::exp(-1.0 * s.beta * eng);
+  return rande < test ? 1 : 0;
+}
+
 int fmc_metropolis_commit(fmc_plain *h, double rande, int *accepted) {
   return guard([&] {
     if (!h) raise(FMC_ERR_ARG, "null argument");
     if (!h->has_move) raise(FMC_ERR_STATE, "no evaluated move to commit");
     Chains &C = h->C;
-    MoveCtx mc;
-    FMC_CUDA(cudaMemcpy(&mc, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost));
-    mc.rande = rande;
-    FMC_CUDA(cudaMemcpyAsync(C.ctx.p, &mc, sizeof(MoveCtx), cudaMemcpyHostToDevice, C.stream));
-    C.launch(kModeCommit, 0);
-    FMC_CUDA(cudaMemcpyAsync(&mc, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost, C.stream));
-    C.sync();
-    C.check_status();
+    // decided here; accept_move (or nothing) queued on the engine's stream,
+    // without waiting: the next evaluation runs after it
+    const int acc = host_energy_eval(h, rande);
+    C.launch(kModeCommit, acc);
     h->has_move = 0;
-    if (accepted) *accepted = mc.accepted;
+    if (acc && h->last.kind == 1) h->nummols[h->last.g]++;
+    if (acc && h->last.kind == 2) h->nummols[h->last.g]--;
+    if (accepted) *accepted = acc;
     return FMC_OK;
   });
 }
@@ -1608,12 +1670,15 @@ static int chain_coords(const Chains &C, int chain, int iguest, double *xyz, int
 static void forced_commit(fmc_plain *h) {
   Chains &C = h->C;
   MoveCtx mc;
-  FMC_CUDA(cudaMemcpy(&mc, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost));
+  FMC_CUDA(cudaMemcpyAsync(&mc, C.ctx.p, sizeof(MoveCtx), cudaMemcpyDeviceToHost, C.stream));
+  C.sync();
   mc.forced = 1;
   FMC_CUDA(cudaMemcpyAsync(C.ctx.p, &mc, sizeof(MoveCtx), cudaMemcpyHostToDevice, C.stream));
-  C.launch(kModeCommit, 0);
+  C.launch(kModeCommit, -1);
   C.sync();
   C.check_status();
+  if (!mc.overlap && mc.kind == 1) h->nummols[mc.g]++;
+  if (mc.kind == 2) h->nummols[mc.g]--;
   h->has_move = 0;
 }
 
@@ -1622,8 +1687,10 @@ int fmc_swap(fmc_plain *h, int iguest, int choice, int jguest, const double *q4,
   return guard([&] {
     if (!h || !q4) raise(FMC_ERR_ARG, "null argument");
     if (h->swap_saved) raise(FMC_ERR_STATE, "a swap awaits fmc_swap_finish");
+    settle(h);
     Chains &C = h->C;
     const System &s = *C.hsys[0];
+    std::memcpy(h->swap_nummols, h->nummols, sizeof h->nummols);
     if (iguest < 1 || iguest > s.ntpguest || jguest < 1 || jguest > s.ntpguest || jguest == iguest)
       raise(FMC_ERR_ARG, "bad guest index");
     const MolType &mi = s.mol[s.locguest[iguest]], &mj = s.mol[s.locguest[jguest]];
@@ -1711,7 +1778,10 @@ int fmc_swap_finish(fmc_plain *h, int accepted) {
   return guard([&] {
     if (!h) raise(FMC_ERR_ARG, "null argument");
     if (!h->swap_saved) raise(FMC_ERR_STATE, "no swap to finish");
-    if (!accepted) restore_state(h->C, *h->swap_saved);
+    if (!accepted) {
+      restore_state(h->C, *h->swap_saved);
+      std::memcpy(h->nummols, h->swap_nummols, sizeof h->nummols);
+    }
     h->swap_saved.reset();
     return FMC_OK;
   });
@@ -1720,6 +1790,7 @@ int fmc_swap_finish(fmc_plain *h, int accepted) {
 int fmc_plain_get_nummols(const fmc_plain *h, int iguest, int *n) {
   return guard([&] {
     if (!h || !n) raise(FMC_ERR_ARG, "null argument");
+    settle(h);
     ChainHdr hd;
     FMC_CUDA(cudaMemcpy(&hd, h->C.hdr.p, sizeof hd, cudaMemcpyDeviceToHost));
     if (iguest < 1 || iguest > kMaxG) raise(FMC_ERR_ARG, "bad guest index");
@@ -1756,6 +1827,7 @@ static int chain_coords(const Chains &C, int chain, int iguest, double *xyz, int
 int fmc_plain_get_coords(const fmc_plain *h, int iguest, double *xyz, int cap) {
   return guard([&] {
     if (!h || !xyz) raise(FMC_ERR_ARG, "null argument");
+    settle(h);
     return chain_coords(h->C, 0, iguest, xyz, cap, nullptr);
   });
 }
@@ -1807,6 +1879,7 @@ static int chain_sk(Chains &C, int chain, double *out, int cap) {
 int fmc_plain_get_sk(const fmc_plain *h, double *sk, int cap) {
   return guard([&] {
     if (!h || !sk) raise(FMC_ERR_ARG, "null argument");
+    settle(h);
     // the buffer normalisation does not change what the handle holds
     return chain_sk(const_cast<fmc_plain *>(h)->C, 0, sk, cap);
   });
@@ -1815,6 +1888,7 @@ int fmc_plain_get_sk(const fmc_plain *h, double *sk, int cap) {
 int fmc_plain_get_energy(const fmc_plain *h, double *energy, int cap) {
   return guard([&] {
     if (!h || !energy) raise(FMC_ERR_ARG, "null argument");
+    settle(h);
     ChainHdr hd;
     FMC_CUDA(cudaMemcpy(&hd, h->C.hdr.p, sizeof hd, cudaMemcpyDeviceToHost));
     for (int m = 1; m <= h->C.maxmls && m <= cap; ++m) energy[m - 1] = hd.energy[m];
@@ -1829,10 +1903,6 @@ int fmc_batch_create(const fmc_system *const *systems, int nsys, const fmc_chain
     if (!systems || !out) raise(FMC_ERR_ARG, "null argument");
     std::vector<const System *> sp;
     for (int i = 0; i < nsys; ++i) sp.push_back(systems[i] ? &systems[i]->s : nullptr);
-    for (const System *q : sp)
-      for (int g = 1; q && g <= q->ntpguest; ++g)
-        if (q->mcswpf[g] > q->mcjmpf[g])
-          raise(FMC_ERR_INPUT, "swap moves run through fmc_swap, not in device-resident chains");
     auto b = std::make_unique<fmc_batch>();
     init_chains(b->C, sp.data(), nsys, chains, nchains, precision, guest_capacity);
     // device-side pre-loading uses the system's insert0; per-chain counts
@@ -1993,6 +2063,17 @@ int fmc_batch_get_coords(fmc_batch *b, int chain, double *xyz, int cap, int *n) 
     if (!b || !xyz) raise(FMC_ERR_ARG, "null argument");
     if (chain < 0 || chain >= b->C.nchains) raise(FMC_ERR_ARG, "bad chain index");
     return chain_coords(b->C, chain, 1, xyz, cap, n);
+  });
+}
+
+int fmc_batch_get_coords_type(fmc_batch *b, int chain, int iguest, double *xyz, int cap, int *n) {
+  return guard([&] {
+    if (!b || !xyz) raise(FMC_ERR_ARG, "null argument");
+    if (chain < 0 || chain >= b->C.nchains) raise(FMC_ERR_ARG, "bad chain index");
+    ChainHdr hd;
+    FMC_CUDA(cudaMemcpy(&hd, b->C.hdr.p + chain, sizeof hd, cudaMemcpyDeviceToHost));
+    if (iguest < 1 || iguest > b->C.hsys[hd.system]->ntpguest) raise(FMC_ERR_ARG, "bad guest type");
+    return chain_coords(b->C, chain, iguest, xyz, cap, n);
   });
 }
 

@@ -81,6 +81,17 @@ struct BlockShared {
     double chgtmp;
     double delE[kMaxM + 1];
   } dfr;
+  // a swap move in flight (swap_move): the partner type, the new molecule's
+  // sites, the energy changes, and the state a rejection puts back
+  struct Swap {
+    int gj, overlap, accepted;
+    double estepi, estepj, rande;
+    double pos[kMaxS][3];
+    int nummols[kMaxG], nslots[kMaxG], nfree[kMaxG], skb[kMaxG];
+    double energy[kMaxM + 1], chgsum_mol[kMaxM + 1], surfacemols[kMaxM + 1];
+    int numtyp[kMaxT + 1], numfrz[kMaxT + 1];
+    int numtyp_mol[kMaxM + 1][kMaxT + 1], numfrz_mol[kMaxM + 1][kMaxT + 1];
+  } swp;
   float draws[8];
   float stepf[4];    // FP32 path: shift half-width and half-angle / pi scale, hi/lo
   float4 trig[kTrigN];  // FP32 path: the quaternion table (copied per launch)
@@ -260,11 +271,11 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   if (randmov < G.mcinsf) kind = 1;
   else if (randmov < G.mcdelf) kind = 2;
   else if (randmov < G.mcdisf) kind = 3;
-  else if (randmov < G.mcjmpf) kind = 6;  // jump (chains with swap moves are refused at creation)
-  else if (randmov < G.mcswpf) kind = 3;
+  else if (randmov < G.mcjmpf) kind = 6;  // jump
+  else if (randmov < G.mcswpf) kind = 7;  // swap
   else if (randmov < G.mctraf) kind = 4;
   else if (randmov < G.mcrotf) kind = 5;
-  else if (randmov < G.mcswif) kind = 7;  // switch
+  else if (randmov < G.mcswif) kind = 8;  // switch
   else kind = 3;
   // adaptive step sizes (gcmc.f:859-900); the updates themselves (FP64) are
   // out of line, the tests here are integer compares
@@ -273,7 +284,7 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
                      (H.rota_count[g] >= 1 && H.rota_mod[g] == 0)))
     adapt_steps<F32>(H, G, g);
   if (nmols == 0) kind = 1;
-  if (kind == 7) {
+  if (kind == 8) {
     // mc_switch (gcmc.f:2041-2267) returns before any draw unless two other
     // guest types hold molecules, which set-up rules out (at most two guest
     // types with switch moves): no move, and `accepted` keeps its value
@@ -292,6 +303,15 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   } else if (kind == 2) {
     H.del_count[g]++;
     mc.choice = pick1(dc.next(), nmols);
+  } else if (kind == 7) {
+    // mc_swap (gcmc.f:2269-2452): the molecule (floor(duni n + 1)), the
+    // partner guest type among the others, then random_rot with the
+    // displacement angle (utility_pack.f:3526-3563); run by swap_move
+    mc.choice = pick1(dc.next(), nmols);
+    const int jg = pick1(dc.next(), S.ntpguest - 1);  // 1-based among the others
+    B.swp.gj = jg < g + 1 ? jg - 1 : jg;
+    for (int i = 3; i < 7; ++i) B.draws[i] = dc.next();
+    B.geo[7] = H.rotangle;
   } else if (kind == 6) {
     // mc_jump (gcmc.f:1937-2039): the molecule, then random_jump's point
     // (utility_pack.f:3359-3380) and random_rot with angle 2 pi
@@ -395,7 +415,7 @@ __device__ void geometry_warp(BlockShared<F32> &B, const ChainArrays &CA, int ch
   const SysDev &S = B.S;
   MoveCtx &mc = B.mc;
   const int lane = threadIdx.x & 31;
-  if (mc.kind == 0) return;
+  if (mc.kind == 0 || mc.kind == 7) return;  // a swap builds its positions in swap_move
   const GuestType &G = S.g[mc.g];
   const int ns = G.ns;
   const bool mine = lane < 3 * ns;
@@ -538,7 +558,7 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
   EvalSmem<F32> &ev = B.ev;
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  if (mc.kind == 0) return;
+  if (mc.kind == 0 || mc.kind == 7) return;  // a swap builds its positions in swap_move
   const GuestType &G = S.g[mc.g];
   const int ns = G.ns;
   const bool mine = lane < 3 * ns;
@@ -2044,6 +2064,227 @@ __device__ void run_deferred(BlockShared<F32> &B) {
     bookkeep<F32>(B.S, B.H, D.g, D.n_old, D.kind, D.delE, D.chgtmp, D.surf_new, D.surf_old);
   stats_production<F32>(B.S, B.H, D.production, D.accepted);
   D.pending = 0;
+}
+
+// mc_swap (gcmc.f:2269-2452) inside a device-resident chain, all threads:
+// the chosen molecule of guest type g is deleted and the deletion committed
+// (accept_move), a molecule of the partner type gj is built from its
+// template at the deleted molecule's centre of mass, rotated about it by the
+// drawn quaternion, inserted and committed, and the pair is decided by the
+// reference's two tests (volume in cubic angstroms as written there; the
+// second number is drawn only when the first test passes, neither when the
+// insertion overlaps).  A rejection puts back what the reference's
+// reject_move restores (mc_moves.f:646-669): coordinates, molecule order,
+// S(k), counts, charges, surface tally and energies -- but not the system
+// charge sumchg, which keeps the two commits as in the reference.  The
+// reference also commits an overlapping insertion before undoing it; here
+// it is not committed, which leaves the same state.
+template <bool F32, int GN>
+__device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain, int &st,
+                          LogRec *logs, int logcap, int rank) {
+  SysDev &S = B.S;
+  ChainHdr &H = B.H;
+  MoveCtx &mc = B.mc;
+  auto &W = B.swp;
+  const int gi = mc.g, gj = W.gj, choice = mc.choice, slot_i = mc.slot;
+  const GuestType &Gi = S.g[gi], &Gj = S.g[gj];
+  if (threadIdx.x == 0) {
+    for (int g = 0; g < kMaxG; ++g) {
+      W.nummols[g] = H.nummols[g];
+      W.nslots[g] = H.nslots[g];
+      W.nfree[g] = H.nfree[g];
+      W.skb[g] = H.skb[g];
+    }
+    for (int m = 0; m <= kMaxM; ++m) {
+      W.energy[m] = H.energy[m];
+      W.chgsum_mol[m] = H.chgsum_mol[m];
+      W.surfacemols[m] = H.surfacemols[m];
+      for (int t = 0; t <= kMaxT; ++t) {
+        W.numtyp_mol[m][t] = H.numtyp_mol[m][t];
+        W.numfrz_mol[m][t] = H.numfrz_mol[m][t];
+      }
+    }
+    for (int t = 0; t <= kMaxT; ++t) {
+      W.numtyp[t] = H.numtyp[t];
+      W.numfrz[t] = H.numfrz[t];
+    }
+    // centre of mass of the chosen molecule (com, utility_pack.f:3565-3596)
+    const double *src = CA.gpos + gslot_base(CA, chain, gi, slot_i) * 3;
+    double w = 0.0, c[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < Gi.ns; ++k) {
+      w += Gi.mass[k];
+      for (int d = 0; d < 3; ++d) c[d] += src[3 * k + d] * Gi.mass[k];
+    }
+    for (int d = 0; d < 3; ++d) c[d] /= w;
+    // the partner's template at c, rotated about c (rotation,
+    // utility_pack.f:3480-3524): (t + c) - c as the reference forms it
+    double q[4];
+    draw_quaternion(B.draws, B.geo[7], q);
+    for (int i = 0; i < Gj.ns; ++i) {
+      double v[3];
+      for (int d = 0; d < 3; ++d) v[d] = (Gj.tmpl[i][d] + c[d]) - c[d];
+      for (int d = 0; d < 3; ++d) {
+        double row[3];
+        qrow(q, d, row);
+        W.pos[i][d] = (row[0] * v[0] + row[1] * v[1] + row[2] * v[2]) + c[d];
+      }
+    }
+    // the deletion first (forced commit: delE of every molecule type now)
+    mc.kind = 2;
+    mc.npos = 1;
+    mc.ns = Gi.ns;
+    B.flags[3] = F32 ? 1 : 0;
+    B.flags[4] = 0;
+  }
+  __syncthreads();
+  if constexpr (!F32) {  // both types' S(k), this CTA's share, for a rejection
+    int kb, ke;
+    share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
+    const double2 *ski = CA.sk + ((size_t)chain * kMaxG + gi) * CA.nkmax;
+    const double2 *skj = CA.sk + ((size_t)chain * kMaxG + gj) * CA.nkmax;
+    double2 *sv = CA.sksave + (size_t)chain * 2 * CA.nkmax;
+    for (int k = kb + threadIdx.x; k < ke; k += kThreads) {
+      sv[k] = ski[k];
+      sv[CA.nkmax + k] = skj[k];
+    }
+  }
+  if (threadIdx.x < 32) {
+    if constexpr (F32) geometry_f32(B, CA, chain);
+    else geometry_warp(B, CA, chain, kPropMC);
+  }
+  __syncthreads();
+  evaluate_any<F32, GN>(B, CA, chain, st);
+  if (threadIdx.x == 0) {
+    W.estepi = -mc.estep;
+    mc.accepted = 1;
+  }
+  __syncthreads();
+  commit(B, CA, chain, st, false);
+  // the partner molecule
+  if (threadIdx.x == 0) {
+    mc.kind = 1;
+    mc.g = gj;
+    mc.ns = Gj.ns;
+    mc.npos = 1;
+    mc.slot = -1;
+    mc.choice = 0;
+    mc.overlap = 0;
+    mc.estep = 0.0;
+    mc.surf_new = mc.surf_old = 0;
+    for (int i = 0; i < Gj.ns; ++i)
+      for (int d = 0; d < 3; ++d) mc.pos[0][i][d] = W.pos[i][d];
+    B.flags[3] = 0;  // FP64 positions
+    B.flags[4] = 0;
+  }
+  __syncthreads();
+  const int full_j = evaluate_any<F32, GN>(B, CA, chain, st);
+  if (threadIdx.x == 0) {
+    W.estepj = mc.estep;
+    W.overlap = mc.overlap;
+    mc.accepted = mc.overlap ? 0 : 1;
+  }
+  __syncthreads();
+  commit(B, CA, chain, st, false);
+  if (threadIdx.x == 0) {  // the reference's two tests (gcmc.f:2371-2411)
+    int acc = 0;
+    double r0 = -1.0;
+    if (!W.overlap) {
+      r0 = (double)draw_f(H);
+      const int jn = H.nummols[gj], in = H.nummols[gi] + 1;
+      const double testi = double(in) * kBoltz * S.temp / (S.volm * H.fuga[gi]) *
+                           exp(-1.0 * S.beta * W.estepi);
+      const double testj = S.volm * H.fuga[gj] / (double(jn) * kBoltz * S.temp) *
+                           exp(-1.0 * S.beta * W.estepj);
+      if (r0 < testi) acc = (double)draw_f(H) < testj;
+    }
+    W.accepted = acc;
+    W.rande = r0;
+  }
+  __syncthreads();
+  if (!W.accepted) {
+    if (threadIdx.x == 0) {
+      for (int g = 0; g < kMaxG; ++g) {
+        H.nummols[g] = W.nummols[g];
+        H.nslots[g] = W.nslots[g];
+        H.nfree[g] = W.nfree[g];
+        H.skb[g] = W.skb[g];  // FP32: the buffers the evaluations left untouched
+      }
+      for (int m = 0; m <= kMaxM; ++m) {
+        H.energy[m] = W.energy[m];
+        H.chgsum_mol[m] = W.chgsum_mol[m];
+        H.surfacemols[m] = W.surfacemols[m];
+        for (int t = 0; t <= kMaxT; ++t) {
+          H.numtyp_mol[m][t] = W.numtyp_mol[m][t];
+          H.numfrz_mol[m][t] = W.numfrz_mol[m][t];
+        }
+      }
+      for (int t = 0; t <= kMaxT; ++t) {
+        H.numtyp[t] = W.numtyp[t];
+        H.numfrz[t] = W.numfrz[t];
+      }
+    }
+    if constexpr (!F32) {
+      int kb, ke;
+      share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
+      double2 *ski = CA.sk + ((size_t)chain * kMaxG + gi) * CA.nkmax;
+      double2 *skj = CA.sk + ((size_t)chain * kMaxG + gj) * CA.nkmax;
+      const double2 *sv = CA.sksave + (size_t)chain * 2 * CA.nkmax;
+      for (int k = kb + threadIdx.x; k < ke; k += kThreads) {
+        ski[k] = sv[k];
+        skj[k] = sv[CA.nkmax + k];
+      }
+    }
+    if (rank == 0) {
+      // the deleted molecule back into the order list at its place
+      // (accept_move shifted the later ones down, mc_moves.f:574-590)
+      int *ord = CA.ord + ((size_t)chain * kMaxG + gi) * CA.cap;
+      const int n = W.nummols[gi], c0 = choice - 1;
+      constexpr int kPer = 8;  // capacity <= 4096 = 8 * kThreads
+      int vals[kPer];
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) {
+        const int i = c0 + threadIdx.x + j * kThreads;
+        if (i < n - 1) vals[j] = ord[i];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) {
+        const int i = c0 + threadIdx.x + j * kThreads;
+        if (i < n - 1) ord[i + 1] = vals[j];
+      }
+      if (threadIdx.x == 0) ord[c0] = slot_i;
+    }
+    __syncthreads();
+    cluster_commit_sync(B, st);
+  }
+  if (threadIdx.x == 0) {
+    const int acc = W.accepted;
+    H.last_accepted = acc;
+    H.attempts[6]++;
+    if (acc) H.accepts[6]++;
+    H.moves++;
+    H.evals += 1 + (full_j ? 1 : 0);
+    if (W.overlap) H.overlap_exits++;
+    if (logcap > 0 && H.log_n < logcap) {
+      if (rank == 0) {
+        LogRec &L = logs[(size_t)chain * logcap + H.log_n];
+        L.move = 7;
+        L.iguest = gi + 1;
+        L.choice = choice;
+        L.overlap = W.overlap;
+        L.accepted = acc;
+        L.estep = W.estepi + W.estepj;
+        L.rande = W.rande;
+        for (int s = 0; s < 3 && s < Gj.ns; ++s)
+          for (int d = 0; d < 3; ++d) L.newxyz[3 * s + d] = W.pos[s][d];
+        L.nmols_after = H.nummols[gi];
+      }
+      H.log_n++;
+    }
+    mc.g = gi;  // the move's guest type, for what follows
+    stats_production<F32>(S, H, H.production, acc);
+  }
+  __syncthreads();
 }
 
 // equitable_bin (utility_pack.f:2407-2519) into one subgrid with atomics:

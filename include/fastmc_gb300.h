@@ -50,6 +50,7 @@ extern "C" {
 #define FMC_MOVE_TRANSLATE 4 /* "move translate" */
 #define FMC_MOVE_ROTATE 5    /* "move rotate" */
 #define FMC_MOVE_JUMP 6      /* "move jump" (mc_jump, gcmc.f:1937-2039) */
+#define FMC_MOVE_SWAP 7      /* "move swap" (mc_swap, gcmc.f:2269-2452) */
 
 #define FMC_MAX_MOLTYPES 8
 #define FMC_MAX_GUEST_TYPES 4
@@ -300,8 +301,9 @@ typedef struct {
   int64_t moves;           /* trial moves done */
   int64_t evals;           /* completed energy evaluations (no overlap exit) */
   int64_t overlap_exits;   /* positions rejected by the overlap test */
-  int64_t attempts[6];     /* insert, delete, displace, translate, rotate, jump */
-  int64_t accepts[6];
+  int64_t attempts[8];     /* insert, delete, displace, translate, rotate, jump,
+                              swap, switch (an acting one) */
+  int64_t accepts[8];
   int nummols;
   int status;              /* device status word */
   double energy;           /* energy(guest mol), FIELD unit */
@@ -362,6 +364,8 @@ int fmc_batch_get_stats(fmc_batch *b, fmc_chain_stats *stats);
 int fmc_batch_get_log(fmc_batch *b, int chain, fmc_move_log *log, int cap,
                       int *n);
 int fmc_batch_get_coords(fmc_batch *b, int chain, double *xyz, int cap, int *n);
+/* The same for guest type iguest (1-based); fmc_batch_get_coords is type 1. */
+int fmc_batch_get_coords_type(fmc_batch *b, int chain, int iguest, double *xyz, int cap, int *n);
 int fmc_batch_get_sk(fmc_batch *b, int chain, double *sk, int cap);
 
 /* Checkpoint / restart of every chain's device state: state records

@@ -15,14 +15,10 @@ and applies that band; it also reports the band with se = 0:
     python oracle/isotherm.py [--seed S] [--workers W] [--out results.json]
 
 With --device the ten points run instead as ten device-resident chains of
-the CUDA library in one batch (FP64: the CALF-20 cell is a parallelepiped,
-which the FP32 path refuses), and their CO2 and N2 averages and standard
-errors (from the chains' window statistics) are checked the same way.
-Device-resident chains refuse swap moves, so their CONTROL files drop the
-"move swap" line: with these inputs the reference accepts no swap (its test
-with the volume in cubic angstroms), and switch never acts with two guest
-types, so both are moves that change nothing and the equilibrium averages
-are the same.
+the CUDA library in one batch, from the same CONTROL files with all six
+moves (FP64: the CALF-20 cell is a parallelepiped, which the FP32 path
+refuses), and their CO2 and N2 averages and standard errors (from the
+chains' window statistics) are checked the same way.
 
     python oracle/isotherm.py --device [--seed S] [--moves N] [--out results.json]
 """
@@ -90,8 +86,7 @@ def run_device(seed: int, moves: int):
         os.makedirs(d)
         for f in ("CONFIG", "FIELD"):
             shutil.copy(os.path.join(GOLD, "calf20", f), d)
-        with open(ctl) as fi, open(os.path.join(d, "CONTROL"), "w") as fo:
-            fo.writelines(l for l in fi if not l.strip().lower().startswith("move swap"))
+        shutil.copy(ctl, os.path.join(d, "CONTROL"))
         systems.append(F.System.load(d))
         rows.append({"point": name, "pressure_bar": p, "moves": moves or eq + steps})
     b = F.Batch(systems, [{"system": i, "seed": seed + i} for i in range(len(names))],

@@ -394,8 +394,6 @@ def test_gpu_swap_per_move(fmc_lib, oracle_lib, inputs_dir, prec):
     o.create_molecules(2, 6)
     p = fmc_lib.PlainEngine(fmc_lib.System.load(d),
                             fmc_lib.FMC_PREC_FP64 if prec == "fp64" else fmc_lib.FMC_PREC_FP32, 64)
-    with pytest.raises(fmc_lib.FmcError):
-        fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 1}])
     moved = 0.0  # sum of |energy change| committed: the scale of the running energies' error
     for g, ns in ((1, 3), (2, 2)):
         for m in o.coords(o.locguest(g)).reshape(-1, ns, 3):
@@ -584,3 +582,100 @@ def test_gpu_window_statistics_two_guests_fp64(fmc_lib, oracle_lib, inputs_dir):
         ref = o.stats(g)
         assert close(st.guest_avg_n[g - 1], ref[0], rel=1e-12, scale=1e-12), (g, st.guest_avg_n[g - 1], ref[0])
         assert close(st.guest_se_n[g - 1], ref[29], rel=1e-9, scale=1e-9), (g, st.guest_se_n[g - 1], ref[29])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_gpu_chain_swaps_follow_oracle(fmc_lib, oracle_lib, inputs_dir, prec):
+    """Swap moves inside device-resident chains (mc_swap, gcmc.f:2269-2452):
+    the chain follows the oracle move by move -- the swapped molecule, the
+    partner type and orientation drawn, both tests with the second number
+    drawn only when the first passes, and rejections that put the state
+    back (about 300 of them; with the reference's tests, whose volume is in
+    cubic angstroms, a swap is accepted only when the deletion releases
+    more than about 69 kT and the partner fits where it left, which does not
+    happen here).  FP64: every decision, estep (deletion plus insertion) to
+    1e-9, and at the end both guest types' coordinates and S(k).  FP32:
+    until the first decision at a threshold, estep to 2e-6 of
+    max(|estep|, 1)."""
+    d = _swap_dir(inputs_dir)
+    n = 600
+    o = oracle_lib.Oracle(d)
+    o.seed(5)
+    o.create_molecules(1, 8)
+    o.create_molecules(2, 6)
+    ref = o.run(n)
+    p = fmc_lib.FMC_PREC_FP64 if prec == "fp64" else fmc_lib.FMC_PREC_FP32
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 5}], precision=p, guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    swaps = [r for r in ref if r.move == 7]
+    assert len(swaps) >= 100
+    nsw = 0
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.iguest, g.choice) == (r.move, r.iguest, r.choice), i
+        if prec == "fp32" and (g.overlap != r.overlap or g.accepted != r.accepted):
+            break
+        assert (g.overlap, g.accepted) == (r.overlap, r.accepted), i
+        if prec == "fp64":
+            assert g.rande == r.rande, i
+            assert g.nmols_after == r.nmols_after, i
+        if not r.overlap:
+            tol = 1e-9 if prec == "fp64" else 2e-6
+            assert abs(g.estep - r.estep) <= tol * max(abs(r.estep), 1.0), (i, g.estep, r.estep)
+        nsw += r.move == 7
+    assert nsw >= 50
+    if prec == "fp64":
+        st = b.stats()[0]
+        assert st.attempts[6] == len(swaps) and st.accepts[6] == sum(r.accepted for r in swaps)
+        for gg in (1, 2):
+            m = o.locguest(gg)
+            x, cnt = _batch_coords(b, gg)
+            assert cnt == o.nummols(m)
+            assert np.allclose(x, o.coords(m), rtol=0, atol=1e-9)
+        info = b.systems[0].info()
+        so = o.sk()
+        assert np.allclose(b.sk(0, info.newld, info.maxmls), so, rtol=0, atol=1e-9 * np.abs(so).max())
+
+
+def _batch_coords(b, iguest):
+    """Site coordinates of one guest type of chain 0 (molecule order)."""
+    import ctypes as C
+    from fastmc_gb300 import _lib as L
+    out = np.zeros(1 << 14)
+    n = C.c_int()
+    L.check(L.load().fmc_batch_get_coords_type(b._h, 0, iguest, out.ctypes.data_as(L.dp), out.size,
+                                               C.byref(n)))
+    ns = b.systems[0].info().guest_nsites[iguest - 1]
+    return out[:3 * ns * n.value].reshape(-1, 3), n.value
+
+
+def test_gpu_reference_all_moves_control_fp64(fmc_lib, oracle_lib):
+    """The reference's own test input with all six moves (CALF-20, CO2 and
+    N2, insert / delete / displace / swap / switch / jump in equal shares)
+    in a device-resident FP64 chain, move by move against the oracle."""
+    import os
+    import shutil
+    import tempfile
+    n = 3000
+    with tempfile.TemporaryDirectory() as d:
+        for f in ("CONFIG", "FIELD"):
+            shutil.copy(os.path.join(CALF20, f), d)
+        shutil.copy(os.path.join(CALF20, "CONTROL_all_moves"), os.path.join(d, "CONTROL"))
+        o = oracle_lib.Oracle(d)
+        o.seed(31)
+        ref = o.run(n)
+        b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 31}],
+                          precision=fmc_lib.FMC_PREC_FP64, guest_capacity=64)
+        b.set_log(n)
+        b.run(n)
+        got = b.log(0, n)
+    kinds = set()
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.iguest, g.choice, g.overlap, g.accepted) == \
+               (r.move, r.iguest, r.choice, r.overlap, r.accepted), i
+        assert g.rande == r.rande, i
+        if not r.overlap and r.move != 0:
+            assert close(g.estep, r.estep, scale=1e-6), (i, g.estep, r.estep)
+        kinds.add(r.move)
+    assert {1, 2, 3, 6, 7}.issubset(kinds)
