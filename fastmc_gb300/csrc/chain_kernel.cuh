@@ -44,6 +44,7 @@ __device__ void widom_propose(BlockShared<F32> &B, const WidomJob &wj, int t) {
     mc.surf_new = mc.surf_old = 0;
     B.flags[3] = 0;  // FP64 positions: the evaluation converts them
     B.flags[4] = 1;  // no delE of other molecule types
+    B.flags[6] = 0;
   }
   if (lane < 3 * ns) {
     const int s = lane / 3, d = lane % 3;
@@ -137,10 +138,27 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (threadIdx.x == 0) B.tmark = clock64();
 #endif
   if (mode == kModeMoves) {
+    // speculative rounds of up to kspec proposals where they apply; kspec
+    // doubles after a round of exits only and halves after a round whose
+    // first proposal passed (every thread computes the same value)
+    const bool spec = speculation_applies(B, CA);
+    int kspec = 2;
     for (int it = 0; it < nmoves; ++it) {
       // the previous move's FP64 bookkeeping overlaps this proposal
       if (threadIdx.x == 32) run_deferred<F32, GN>(B);
-      propose(B, CA, chain, kPropMC, 0);
+      if (spec) {
+        const int kwin = min(kspec, nmoves - it);
+        const int exits = spec_round(B, CA, chain, kwin, logs, logcap, rank);
+        it += exits;
+        if (!B.spec_have) kspec = min(2 * kspec, kMaxSpec);
+        else if (exits == 0) kspec = max(1, kspec / 2);
+        if (!B.spec_have) {
+          --it;  // the loop's increment counts no further move
+          continue;
+        }
+      } else {
+        propose(B, CA, chain, kPropMC, 0);
+      }
       FMC_PHASE(B, 0);
       if (B.mc.kind == 7) {  // mc_swap: evaluation, decision, commit or rollback, statistics
         swap_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);

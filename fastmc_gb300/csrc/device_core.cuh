@@ -46,7 +46,7 @@ constexpr int kStBadChoice = 16;   // molecule index out of range
 constexpr int kStKmax = 32;        // kmax beyond the shared tables
 constexpr int kStWait = 64;        // a bounded wait on an asynchronous copy ran out
 constexpr int kStDraws = 128;      // generator buffer empty (internal error)
-constexpr int kRBuf = 64;          // generator outputs drawn ahead per chain
+constexpr int kRBuf = 256;         // generator outputs drawn ahead per chain (power of two)
 
 constexpr double kPi = 3.141592653589793;
 constexpr double kSqrPi = 1.7724538509055159;

@@ -62,6 +62,8 @@ struct LogRec {  // mirrors fmc_move_log
   double newxyz[9];
 };
 
+constexpr int kMaxSpec = 8;  // proposals of one speculative round
+
 template <bool F32>
 struct BlockShared {
   // FP32 batches of one guest type: every guest site in molecule order as
@@ -92,13 +94,28 @@ struct BlockShared {
     int numtyp[kMaxT + 1], numfrz[kMaxT + 1];
     int numtyp_mol[kMaxM + 1][kMaxT + 1], numfrz_mol[kMaxM + 1][kMaxT + 1];
   } swp;
+  // speculative proposals (spec_round): each one's selection, first-pass
+  // positions and overlap outcome, and the selection state after it
+  struct SelState {
+    long long gcmccount, ins, del, disp, tran, rota, jump;
+    int minchk_left, production, disp_mod, tran_mod, rota_mod, rhead, ravail, status;
+    double delrdisp, tran_delr, rotangle, rota_rotangle;
+    float sh_disp[2], sh_tran[2], rho_rot[2][2];
+  };
+  struct Spec {
+    int kind, choice, slot, npos, flag2, flag5, production, testable, hit;
+    float draws[7], stepf[4];
+    float phi[2][kMaxS][3], plo[2][kMaxS][3];
+    SelState sel;
+  } spec[kMaxSpec];
+  int spec_n, spec_exits, spec_have;
   float draws[8];
   float stepf[4];    // FP32 path: shift half-width and half-angle / pi scale, hi/lo
   float4 trig[kTrigN];  // FP32 path: the quaternion table (copied per launch)
   double geo[12];    // a, b, c, q1..q4, rotation angle, com/frac scratch
   double vtmp[3];
   int flags[8];     // 0 status, 1 slot, 2 "translate" (q = 0), 3 FP32 geometry, 4 delE deferred,
-                    // 5 switch no-op
+                    // 5 switch no-op, 6 overlap test already passed (speculative round)
   // cluster exchange (chains on more than one CTA): per-CTA partial totals,
   // double-buffered, and the flags the peers raise in this CTA's memory
   double xv[2][40];
@@ -548,31 +565,31 @@ __device__ __forceinline__ void quat_f32(const float *dr, float scale, float *q)
 // construction in plain FP32 arithmetic on hi/lo positions (good to about
 // 1e-7 A), for the overlap test that ends most trial moves.  A move that
 // passes it gets its positions again from refine_geometry at double-float
-// precision before its energy is evaluated.  One lane per site coordinate;
-// orthorhombic cells.  Also fills the site constants and the bounds of each
-// position (their 1e-3 A margin covers the refinement).
+// precision before its energy is evaluated.  One warp, one lane per site
+// coordinate; orthorhombic cells.  Writes position 0 (new) and, for moves
+// of an existing molecule, position 1 (old) into phi/plo; the bounds of
+// each position carry a 1e-3 A margin that covers the refinement.
 template <bool F32>
-__device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
+__device__ void geometry_f32_core(const BlockShared<F32> &B, const ChainArrays &CA, int chain,
+                                  int kind, int g, int slot, const float *draws, const float *stepf,
+                                  int flag2, float (*phi)[kMaxS][3], float (*plo)[kMaxS][3]) {
   const SysDev &S = B.S;
-  MoveCtx &mc = B.mc;
-  EvalSmem<F32> &ev = B.ev;
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  if (mc.kind == 0 || mc.kind == 7) return;  // a swap builds its positions in swap_move
-  const GuestType &G = S.g[mc.g];
+  const GuestType &G = S.g[g];
   const int ns = G.ns;
   const bool mine = lane < 3 * ns;
   const int s = mine ? lane / 3 : 0;
   const int d = lane % 3;
   const float Lh = S.boxh[d], Ll = S.boxl[d];
   float ph = 0.f, pl = 0.f, e;
-  if (mc.kind == 1) {
+  if (kind == 1) {
     float q[4], row[3];
-    quat_f32(B.draws, 1.0f, q);
+    quat_f32(draws, 1.0f, q);
     qrow(q, d, row);
     const float *t = G.tmplf[s];
     const float v = row[0] * t[0] + row[1] * t[1] + row[2] * t[2];
-    const float u = B.draws[d];
+    const float u = draws[d];
     const float ch = __fmul_rn(u, Lh);
     const float cl = fmaf(u, Lh, -ch) + u * Ll;
     two_sum_f(ch, v, ph, e);
@@ -580,32 +597,32 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
   } else {
     float oh = 0.f, ol = 0.f;
     if (mine && CA.resident) {
-      oh = reinterpret_cast<const float *>(&B.grh[mc.slot * ns + s])[d];
-      ol = reinterpret_cast<const float *>(&B.grl[mc.slot * ns + s])[d];
+      oh = reinterpret_cast<const float *>(&B.grh[slot * ns + s])[d];
+      ol = reinterpret_cast<const float *>(&B.grl[slot * ns + s])[d];
     } else if (mine) {
-      const size_t b = gslot_base(CA, chain, mc.g, mc.slot) + s;
+      const size_t b = gslot_base(CA, chain, g, slot) + s;
       oh = reinterpret_cast<const float *>(CA.ghi + b)[d];
       ol = reinterpret_cast<const float *>(CA.glo + b)[d];
     }
-    if (mc.kind == 2) {
+    if (kind == 2) {
       ph = oh;
       pl = ol;
     } else {
       if (mine) {
-        ev.phi[1][s][d] = oh;
-        ev.plo[1][s][d] = ol;
+        phi[1][s][d] = oh;
+        plo[1][s][d] = ol;
       }
       // centre of mass of the old molecule, relative to site 0 (jump only)
       const float p0h = __shfl_sync(full, oh, d), p0l = __shfl_sync(full, ol, d);
       float sh = 0.f;
-      if (mc.kind == 6) {  // jump: the old centre of mass to the drawn point
+      if (kind == 6) {  // jump: the old centre of mass to the drawn point
         const float off = mine ? ((oh - p0h) + (ol - p0l)) * G.wf[s] : 0.f;
         float cof = 0.f;
         for (int s2 = 0; s2 < ns; ++s2) cof += __shfl_sync(full, off, 3 * s2 + d);
-        const float u = B.draws[d];
+        const float u = draws[d];
         sh = (__fmul_rn(u, Lh) - p0h) + ((fmaf(u, Lh, -__fmul_rn(u, Lh)) + u * Ll) - p0l) - cof;
-      } else if (mc.kind != 5) {
-        sh = __fmul_rn(2.0f * B.draws[d] - 1.0f, B.stepf[0]);
+      } else if (kind != 5) {
+        sh = __fmul_rn(2.0f * draws[d] - 1.0f, stepf[0]);
       }
       two_sum_f(oh, sh, ph, e);
       pl = ol + e;
@@ -628,10 +645,10 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
         cmh = t;
         cml += e - k * Ll;
       }
-      if (mc.kind == 6 || B.draws[3] >= 0.0f) {  // rotation about the wrapped centre
+      if (kind == 6 || draws[3] >= 0.0f) {  // rotation about the wrapped centre
         float q[4] = {0.f, 0.f, 0.f, 0.f};  // "move translate": q = 0, Q = -I
-        if (mc.kind == 6) quat_f32(B.draws, 1.0f, q);
-        else if (!B.flags[2]) quat_f32(B.draws, B.stepf[2], q);
+        if (kind == 6) quat_f32(draws, 1.0f, q);
+        else if (!flag2) quat_f32(draws, stepf[2], q);
         const float x = (ph - cmh) + (pl - cml);
         const float x0 = __shfl_sync(full, x, 3 * s), x1 = __shfl_sync(full, x, 3 * s + 1),
                     x2 = __shfl_sync(full, x, 3 * s + 2);
@@ -644,9 +661,18 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
     }
   }
   if (mine) {
-    ev.phi[0][s][d] = ph;
-    ev.plo[0][s][d] = pl;
+    phi[0][s][d] = ph;
+    plo[0][s][d] = pl;
   }
+}
+
+// The site constants of the moving guest type and the bounds of the
+// evaluated positions (warp 0).
+template <bool F32>
+__device__ void site_constants_and_bounds(BlockShared<F32> &B) {
+  const MoveCtx &mc = B.mc;
+  const GuestType &G = B.S.g[mc.g];
+  const int lane = threadIdx.x & 31, ns = G.ns;
   if (B.si_g != mc.g) {  // site constants of the moving guest type
     if (lane < ns) {
       SiteInfo &si = B.si[lane];
@@ -664,6 +690,18 @@ __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int cha
   }
   __syncwarp();
   position_bounds(B, lane);
+}
+
+// FP32 path, moves drawn on the device: the first-pass geometry of the move
+// in mc (warp 0), then the site constants and position bounds.
+template <bool F32>
+__device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
+  MoveCtx &mc = B.mc;
+  if (mc.kind == 0 || mc.kind == 7) return;  // a swap builds its positions in swap_move
+  geometry_f32_core(B, CA, chain, mc.kind, mc.g, mc.slot, B.draws, B.stepf, B.flags[2], B.ev.phi,
+                    B.ev.plo);
+  __syncwarp();
+  site_constants_and_bounds(B);
 }
 
 // Double-float quaternion: the half angle pi * rho, rho = r * scale (scale
@@ -814,6 +852,7 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       mc.accepted = 0;
       mc.surf_new = mc.surf_old = 0;
       B.flags[5] = 0;
+      B.flags[6] = 0;
       if (mode == kPropMC) {
         select_move(B, CA, chain);
       } else if (mode == kPropInsert) {
@@ -1568,12 +1607,14 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
     __syncthreads();
   }
   if (mc.kind == 1 || mc.kind >= 3) {
-    const int hit = overlap_check(B, CA, chain);
-    FMC_PHASE(B, 1);
-    if (hit) {
-      if (threadIdx.x == 0) mc.overlap = 1;
-      __syncthreads();
-      return 0;
+    if (!B.flags[6]) {  // flags[6]: a speculative round found this position clear already
+      const int hit = overlap_check(B, CA, chain);
+      FMC_PHASE(B, 1);
+      if (hit) {
+        if (threadIdx.x == 0) mc.overlap = 1;
+        __syncthreads();
+        return 0;
+      }
     }
     if constexpr (F32) {
       // FP32 first-pass geometry: warp 0 refines it; the positions are
@@ -2066,6 +2107,303 @@ __device__ void run_deferred(BlockShared<F32> &B) {
   D.pending = 0;
 }
 
+// ------------------------------------------------- speculative proposals
+// Most trial moves of a dense framework end on the overlap test, change no
+// state and consume a fixed number of generator draws (the Metropolis
+// number is drawn only after the test passes, gcmc.f:1732).  So the next
+// moves of a chain can be proposed ahead and their overlap tests run
+// together: the proposals up to the first that passes (or that has no
+// overlap test: a deletion, a switch that does nothing) are the chain's
+// next moves exactly as the one-at-a-time loop would make them.  The ones
+// before it are completed as overlap exits; the selections after it are
+// undone (counters, step sizes, generator position).  FP32 chains of one
+// guest type with cell lists and resident guests, no probability grids.
+
+// The selection state select_move changes (one guest type).
+template <bool F32>
+__device__ __forceinline__ void save_selection(const BlockShared<F32> &B,
+                                               typename BlockShared<F32>::SelState &s) {
+  const ChainHdr &H = B.H;
+  s.gcmccount = H.gcmccount;
+  s.ins = H.ins_count[0];
+  s.del = H.del_count[0];
+  s.disp = H.disp_count[0];
+  s.tran = H.tran_count[0];
+  s.rota = H.rota_count[0];
+  s.jump = H.jump_count[0];
+  s.minchk_left = H.minchk_left;
+  s.production = H.production;
+  s.disp_mod = H.disp_mod[0];
+  s.tran_mod = H.tran_mod[0];
+  s.rota_mod = H.rota_mod[0];
+  s.rhead = H.rhead;
+  s.ravail = H.ravail;
+  s.status = H.status;
+  s.delrdisp = H.delrdisp[0];
+  s.tran_delr = H.tran_delr[0];
+  s.rotangle = H.rotangle;
+  s.rota_rotangle = H.rota_rotangle;
+  for (int i = 0; i < 2; ++i) {
+    s.sh_disp[i] = H.sh_disp[0][i];
+    s.sh_tran[i] = H.sh_tran[0][i];
+    s.rho_rot[0][i] = H.rho_rot[0][i];
+    s.rho_rot[1][i] = H.rho_rot[1][i];
+  }
+}
+
+template <bool F32>
+__device__ __forceinline__ void load_selection(BlockShared<F32> &B,
+                                               const typename BlockShared<F32>::SelState &s) {
+  ChainHdr &H = B.H;
+  H.gcmccount = s.gcmccount;
+  H.ins_count[0] = s.ins;
+  H.del_count[0] = s.del;
+  H.disp_count[0] = s.disp;
+  H.tran_count[0] = s.tran;
+  H.rota_count[0] = s.rota;
+  H.jump_count[0] = s.jump;
+  H.minchk_left = s.minchk_left;
+  H.production = s.production;
+  H.disp_mod[0] = s.disp_mod;
+  H.tran_mod[0] = s.tran_mod;
+  H.rota_mod[0] = s.rota_mod;
+  H.rhead = s.rhead;
+  H.ravail = s.ravail;
+  H.status = s.status;
+  H.delrdisp[0] = s.delrdisp;
+  H.tran_delr[0] = s.tran_delr;
+  H.rotangle = s.rotangle;
+  H.rota_rotangle = s.rota_rotangle;
+  for (int i = 0; i < 2; ++i) {
+    H.sh_disp[0][i] = s.sh_disp[i];
+    H.sh_tran[0][i] = s.sh_tran[i];
+    H.rho_rot[0][i] = s.rho_rot[0][i];
+    H.rho_rot[1][i] = s.rho_rot[1][i];
+  }
+}
+
+// True when a chain can run speculative rounds (all threads agree).
+template <bool F32>
+__device__ __forceinline__ bool speculation_applies(const BlockShared<F32> &B, const ChainArrays &CA) {
+  const SysDev &S = B.S;
+  if (!F32 || !CA.resident || !S.use_cells || S.ntpguest != 1) return false;
+  if (S.prob_nsub > 0 && CA.grid) return false;
+  const float mincs = fminf(S.cszf[0], fminf(S.cszf[1], S.cszf[2]));
+  return mincs >= sqrtf(S.overlap_sqf) + 0.01f;  // the 27 neighbour cells cover the test
+}
+
+// Overlap tests of the testable proposals of a round, all threads: every
+// site against the 27 neighbour cells (padded slots) and every resident
+// guest molecule, the arithmetic of overlap_check.  Sets spec[j].hit.
+template <bool F32>
+__device__ void overlap_batch(BlockShared<F32> &B, int n) {
+  const SysDev &S = B.S;
+  const int ns = S.g[0].ns, lp = S.cpad_log2;
+  const int per = (ns * 27) << lp;
+  for (int t = threadIdx.x; t < n * per; t += kThreads) {
+    const int jp = t / per, r = t - jp * per;
+    auto &P = B.spec[jp];
+    if (!P.testable || *(volatile int *)&P.hit) continue;
+    const int j = r & ((1 << lp) - 1);
+    const int sc = r >> lp;
+    const int s = sc / 27, c = sc - 27 * s;
+    const int o3[3] = {c / 9 - 1, (c / 3) % 3 - 1, c % 3 - 1};
+    int im[3], iw[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      int ic = (int)floorf(P.phi[0][s][d] * S.rcszf[d]) + o3[d];
+      int k = 0;
+      if (ic < 0) k = -1;
+      else if (ic >= S.nc[d]) k = 1;
+      if (ic - k * S.nc[d] < 0 || ic - k * S.nc[d] >= S.nc[d]) k = image_of(ic, S.nc[d]);
+      im[d] = k;
+      iw[d] = ic - k * S.nc[d];
+    }
+    const size_t a = ((size_t)((iw[0] * S.nc[1] + iw[1]) * S.nc[2] + iw[2]) << lp) + j;
+    const float4 H4 = __ldg(S.cpad_hi + a), L4 = __ldg(S.cpad_lo + a);
+    float ah[3] = {H4.x, H4.y, H4.z}, al[3] = {L4.x, L4.y, L4.z};
+    float r2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (im[d] != 0) {
+        float h, e;
+        two_sum_f(ah[d], float(im[d]) * S.boxh[d], h, e);
+        ah[d] = h;
+        al[d] = al[d] + (e + float(im[d]) * S.boxl[d]);
+      }
+      float dd = (P.phi[0][s][d] - ah[d]) + (P.plo[0][s][d] - al[d]);
+      r2 = fmaf(dd, dd, r2);
+    }
+    if (r2 < S.overlap_sqf) P.hit = 1;
+  }
+  // resident guests, one (proposal, molecule) per item
+  const GuestType &G = S.g[0];
+  const int n2 = B.H.nummols[0];
+  const float pre = sqrtf(S.overlap_sqf) + 2.0f * (float)G.rmax + 2.0f * (float)G.rmax + 0.01f;
+  const float pre2 = pre * pre;
+  for (int t = threadIdx.x; t < n * n2; t += kThreads) {
+    const int jp = t / n2, i = t - jp * n2;
+    auto &P = B.spec[jp];
+    if (!P.testable || *(volatile int *)&P.hit) continue;
+    if (P.kind != 1 && i == P.slot) continue;  // the moving molecule itself
+    const float4 q0 = B.grh[i * ns];
+    float dx = P.phi[0][0][0] - q0.x, dy = P.phi[0][0][1] - q0.y, dz = P.phi[0][0][2] - q0.z;
+    dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
+    dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
+    dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+    int hit = 0;
+    for (int b = 0; b < ns; ++b) {
+      const float4 qh = B.grh[i * ns + b], ql = B.grl[i * ns + b];
+      for (int s = 0; s < ns; ++s) {
+        float ex = mi_diff32(P.phi[0][s][0], P.plo[0][s][0], qh.x, ql.x, S.boxh[0], S.boxl[0], S.rboxf[0]);
+        float ey = mi_diff32(P.phi[0][s][1], P.plo[0][s][1], qh.y, ql.y, S.boxh[1], S.boxl[1], S.rboxf[1]);
+        float ez = mi_diff32(P.phi[0][s][2], P.plo[0][s][2], qh.z, ql.z, S.boxh[2], S.boxl[2], S.rboxf[2]);
+        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < S.overlap_sqf) hit = 1;
+      }
+    }
+    if (hit) P.hit = 1;
+  }
+}
+
+// One speculative round of up to kwin proposals (all threads; ends with a
+// barrier).  The overlap exits among them are completed here (counters,
+// production statistics, log); the first proposal that is not one is left
+// in mc / draws / ev as propose() leaves a move (spec_have = 1), with
+// flags[6] set when its overlap test has passed.  Returns the exits.
+template <bool F32>
+__device__ int spec_round(BlockShared<F32> &B, const ChainArrays &CA, int chain, int kwin,
+                          LogRec *logs, int logcap, int rank) {
+  SysDev &S = B.S;
+  ChainHdr &H = B.H;
+  MoveCtx &mc = B.mc;
+  if (threadIdx.x < 32) {
+    // draws for kwin proposals (at most 11 each) and the chosen one's
+    // Metropolis number, within the ring
+    const int need = 11 * kwin + 5;
+    while (H.ravail < need) refill_draws(H);
+    if (threadIdx.x == 0) {
+      int n = 0;
+      for (int j = 0; j < kwin; ++j) {
+        mc.rande = -1.0;
+        mc.estep = 0.0;
+        mc.overlap = 0;
+        mc.accepted = 0;
+        mc.surf_new = mc.surf_old = 0;
+        B.flags[5] = 0;
+        select_move(B, CA, chain);
+        if (mc.kind == 2 || (mc.kind >= 3 && mc.kind != 7)) {
+          if (mc.choice < 1 || mc.choice > H.nummols[0]) {
+            H.status |= kStBadChoice;
+            mc.kind = 0;
+          } else {
+            mc.slot = mc.choice - 1;  // resident guests: molecule i in slot i
+          }
+        }
+        auto &P = B.spec[j];
+        P.kind = mc.kind;
+        P.choice = mc.choice;
+        P.slot = mc.slot;
+        P.npos = mc.npos;
+        P.flag2 = B.flags[2];
+        P.flag5 = B.flags[5];
+        P.production = H.production;
+        for (int i = 0; i < 7; ++i) P.draws[i] = B.draws[i];
+        for (int i = 0; i < 4; ++i) P.stepf[i] = B.stepf[i];
+        P.testable = mc.kind == 1 || (mc.kind >= 3 && mc.kind <= 6);
+        P.hit = 0;
+        save_selection(B, P.sel);
+        ++n;
+        if (!P.testable) break;  // a deletion or a no-op: no test, it is this round's move
+      }
+      B.spec_n = n;
+    }
+  }
+  __syncthreads();
+  const int n = B.spec_n;
+  {  // first-pass positions, warp j for proposal j
+    const int w = threadIdx.x >> 5;
+    if (w < n) {
+      auto &P = B.spec[w];
+      if (P.kind != 0)
+        geometry_f32_core(B, CA, chain, P.kind, 0, P.slot, P.draws, P.stepf, P.flag2, P.phi, P.plo);
+    }
+  }
+  __syncthreads();
+  overlap_batch(B, n);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int j = 0;
+    const GuestType &G = S.g[0];
+    while (j < n && B.spec[j].testable && B.spec[j].hit) {  // overlap exits
+      const auto &P = B.spec[j];
+      H.last_accepted = 0;
+      H.attempts[P.kind - 1]++;
+      H.moves++;
+      H.overlap_exits++;
+      if (logcap > 0 && H.log_n < logcap) {
+        if (rank == 0) {
+          LogRec &L = logs[(size_t)chain * logcap + H.log_n];
+          L.move = P.kind;
+          L.iguest = 1;
+          L.choice = P.choice;
+          L.overlap = 1;
+          L.accepted = 0;
+          L.estep = 0.0;
+          L.rande = -1.0;
+          for (int s = 0; s < 3 && s < G.ns; ++s)
+            for (int d = 0; d < 3; ++d)
+              L.newxyz[3 * s + d] = (double)P.phi[0][s][d] + (double)P.plo[0][s][d];
+          L.nmols_after = H.nummols[0];
+        }
+        H.log_n++;
+      }
+      stats_production<F32>(S, H, P.production, 0);
+      ++j;
+    }
+    B.spec_exits = j;
+    B.spec_have = j < n;
+    if (j < n) {  // the round's move: its selection state, the later ones undone
+      const auto &P = B.spec[j];
+      load_selection(B, P.sel);
+      mc.kind = P.kind;
+      mc.g = 0;
+      mc.ns = G.ns;
+      mc.choice = P.choice;
+      mc.slot = P.slot;
+      mc.npos = P.npos;
+      mc.rande = -1.0;
+      mc.estep = 0.0;
+      mc.overlap = 0;
+      mc.accepted = 0;
+      mc.surf_new = mc.surf_old = 0;
+      for (int i = 0; i < 7; ++i) B.draws[i] = P.draws[i];
+      for (int i = 0; i < 4; ++i) B.stepf[i] = P.stepf[i];
+      B.flags[2] = P.flag2;
+      B.flags[5] = P.flag5;
+      B.flags[3] = 1;  // FP32 first-pass geometry, refined after the test
+      B.flags[4] = 1;  // delE of the other molecule types only if accepted
+      B.flags[6] = P.testable;
+    }
+  }
+  __syncthreads();
+  if (B.spec_have && threadIdx.x < 32) {
+    const auto &P = B.spec[B.spec_exits];
+    const int lane = threadIdx.x, ns = S.g[0].ns;
+    if (P.kind != 0 && lane < 3 * ns) {
+      const int s = lane / 3, d = lane % 3;
+      for (int p = 0; p < P.npos; ++p) {
+        B.ev.phi[p][s][d] = P.phi[p][s][d];
+        B.ev.plo[p][s][d] = P.plo[p][s][d];
+      }
+    }
+    __syncwarp();
+    if (P.kind != 0) site_constants_and_bounds(B);
+  }
+  __syncthreads();
+  return B.spec_exits;
+}
+
 // mc_swap (gcmc.f:2269-2452) inside a device-resident chain, all threads:
 // the chosen molecule of guest type g is deleted and the deletion committed
 // (accept_move), a molecule of the partner type gj is built from its
@@ -2135,6 +2473,7 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
     mc.ns = Gi.ns;
     B.flags[3] = F32 ? 1 : 0;
     B.flags[4] = 0;
+    B.flags[6] = 0;
   }
   __syncthreads();
   if constexpr (!F32) {  // both types' S(k), this CTA's share, for a rejection
@@ -2175,6 +2514,7 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
       for (int d = 0; d < 3; ++d) mc.pos[0][i][d] = W.pos[i][d];
     B.flags[3] = 0;  // FP64 positions
     B.flags[4] = 0;
+    B.flags[6] = 0;
   }
   __syncthreads();
   const int full_j = evaluate_any<F32, GN>(B, CA, chain, st);
