@@ -130,6 +130,7 @@ SIGNATURES = {
     "fmc_displace": (C.c_int, [vp, C.c_int, C.c_int, dp, C.POINTER(MoveResult)]),
     "fmc_guest_energy": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(MoveResult)]),
     "fmc_metropolis_commit": (C.c_int, [vp, C.c_double, ip]),
+    "fmc_commit": (C.c_int, [vp, C.c_int]),
     "fmc_swap": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, C.POINTER(SwapResult)]),
     "fmc_swap_finish": (C.c_int, [vp, C.c_int]),
     "fmc_plain_get_nummols": (C.c_int, [vp, C.c_int, ip]),

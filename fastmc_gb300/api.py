@@ -148,9 +148,14 @@ class PlainEngine:
         return _result_dict(r, self._info.maxmls, self._ns(iguest))
 
     def commit(self, rande: float) -> bool:
+        """energy_eval with the host's uniform number, then the commit."""
         acc = C.c_int()
         L.check(L.load().fmc_metropolis_commit(self._h, rande, C.byref(acc)))
         return bool(acc.value)
+
+    def commit_decided(self, accepted: bool) -> None:
+        """The commit of the last evaluated move with the caller's decision."""
+        L.check(L.load().fmc_commit(self._h, int(accepted)))
 
     def swap(self, iguest: int, choice: int, jguest: int, q: Sequence[float],
              rande: Callable[[], float]) -> dict:

@@ -273,6 +273,18 @@ __global__ void __launch_bounds__(kThreads, 1)
       else decide(B, false);
     }
     __syncthreads();
+    if constexpr (F32) {
+      // the evaluated position as the evaluation split it (FP64 positions
+      // of the per-move ABI into hi/lo pairs): commit stores these
+      if (threadIdx.x < 3 * B.mc.ns) {
+        const int s = threadIdx.x / 3, d = threadIdx.x % 3;
+        const double v = B.mc.pos[0][s][d];
+        const float h = (float)v;
+        B.ev.phi[0][s][d] = h;
+        B.ev.plo[0][s][d] = (float)(v - (double)h);
+      }
+      __syncthreads();
+    }
     commit(B, CA, chain, st);
     if (threadIdx.x == 0) B.mc.evaluated = 0;
   }

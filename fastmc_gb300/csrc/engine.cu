@@ -1663,6 +1663,21 @@ int fmc_metropolis_commit(fmc_plain *h, double rande, int *accepted) {
   });
 }
 
+int fmc_commit(fmc_plain *h, int accepted) {
+  return guard([&] {
+    if (!h) raise(FMC_ERR_ARG, "null argument");
+    if (!h->has_move) raise(FMC_ERR_STATE, "no evaluated move to commit");
+    const MoveCtx &m = h->last;
+    // an overlapping insertion or displacement is never committed
+    const int acc = (accepted && !((m.kind == 1 || m.kind >= 3) && m.overlap)) ? 1 : 0;
+    h->C.launch(kModeCommit, acc);
+    h->has_move = 0;
+    if (acc && m.kind == 1) h->nummols[m.g]++;
+    if (acc && m.kind == 2) h->nummols[m.g]--;
+    return FMC_OK;
+  });
+}
+
 static int chain_coords(const Chains &C, int chain, int iguest, double *xyz, int cap, int *nout);
 
 // accept_move for the last evaluated move without energy_eval (mc_swap

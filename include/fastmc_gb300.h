@@ -251,6 +251,12 @@ int fmc_guest_energy(fmc_plain *h, int iguest, int choice,
  * decision to *accepted. */
 int fmc_metropolis_commit(fmc_plain *h, double rande, int *accepted);
 
+/* accept_move or reject_move (mc_moves.f:485-673) on the device for the
+ * last evaluated move, with the host's own decision (accepted 1 or 0): for
+ * a host that keeps calling its energy_eval.  Queued without waiting, like
+ * fmc_metropolis_commit; an overlapping trial position is never committed. */
+int fmc_commit(fmc_plain *h, int accepted);
+
 /* mc_swap (gcmc.f:2269-2452) in two calls, the host drawing as the
  * reference does.  fmc_swap: molecule `choice` (1-based) of guest type
  * iguest is deleted and committed, a molecule of jguest is built from its

@@ -596,7 +596,7 @@ def test_gpu_chain_swaps_follow_oracle(fmc_lib, oracle_lib, inputs_dir, prec):
     happen here).  FP64: every decision, estep (deletion plus insertion) to
     1e-9, and at the end both guest types' coordinates and S(k).  FP32:
     until the first decision at a threshold, estep to 2e-6 of
-    max(|estep|, 1)."""
+    max(|estep|, 1), 1e-5 for the swaps themselves."""
     d = _swap_dir(inputs_dir)
     n = 600
     o = oracle_lib.Oracle(d)
@@ -621,7 +621,9 @@ def test_gpu_chain_swaps_follow_oracle(fmc_lib, oracle_lib, inputs_dir, prec):
             assert g.rande == r.rande, i
             assert g.nmols_after == r.nmols_after, i
         if not r.overlap:
-            tol = 1e-9 if prec == "fp64" else 2e-6
+            # FP32: a swap adds two energies that, for pre-loaded molecules on
+            # the LJ wall, reach 1e5 kcal/mol; measured within 4e-6 of them
+            tol = 1e-9 if prec == "fp64" else (1e-5 if r.move == 7 else 2e-6)
             assert abs(g.estep - r.estep) <= tol * max(abs(r.estep), 1.0), (i, g.estep, r.estep)
         nsw += r.move == 7
     assert nsw >= 50
@@ -674,8 +676,39 @@ def test_gpu_reference_all_moves_control_fp64(fmc_lib, oracle_lib):
     for i, (g, r) in enumerate(zip(got, ref)):
         assert (g.move, g.iguest, g.choice, g.overlap, g.accepted) == \
                (r.move, r.iguest, r.choice, r.overlap, r.accepted), i
-        assert g.rande == r.rande, i
+        if r.move != 0:  # a switch that does nothing draws nothing (logged -1 / 0)
+            assert g.rande == r.rande, i
         if not r.overlap and r.move != 0:
             assert close(g.estep, r.estep, scale=1e-6), (i, g.estep, r.estep)
         kinds.add(r.move)
     assert {1, 2, 3, 6, 7}.issubset(kinds)
+
+
+def test_gpu_commit_with_host_decision(fmc_lib, oracle_lib, small):
+    """fmc_commit: the host decides (here at random) and the device commits
+    accordingly; the oracle given the same decisions ends in the same state
+    (coordinates, S(k), energy)."""
+    o = oracle_lib.Oracle(small)
+    plain = fmc_lib.PlainEngine(fmc_lib.System.load(small), fmc_lib.FMC_PREC_FP64, 64)
+    rng = np.random.default_rng(12)
+    pos = _free_positions(o, 12, seed=9)
+    n = 0
+    for xyz in pos:
+        acc = bool(rng.random() < 0.7)
+        r = plain.insertion(1, xyz)
+        ov = o.insertion_energy(1, xyz)["overlap"]
+        assert r["overlap"] == ov
+        plain.commit_decided(acc)
+        o.apply_move(1, 1, 0, xyz, acc and not ov)
+        n += acc and not ov
+    for _ in range(6):
+        c = int(rng.integers(1, n + 1))
+        acc = bool(rng.random() < 0.5)
+        plain.deletion(1, c)
+        plain.commit_decided(acc)
+        o.apply_move(2, 1, c, None, acc)
+        n -= acc
+    assert plain.nummols(1) == o.nummols(o.locguest(1)) == n
+    assert np.allclose(plain.coords(1), o.coords(o.locguest(1)), rtol=0, atol=1e-12)
+    so = o.sk()
+    assert np.allclose(plain.sk(), so, rtol=0, atol=1e-10 * np.abs(so).max())
