@@ -290,12 +290,13 @@ def measured_peak_hbm():
 
 
 def profiled_traffic():
-    """DRAM bytes (read + write) per chain-kernel launch of this workload,
-    from the committed ncu summary, if present."""
+    """DRAM bytes (read + write) of one step's chain-kernel launches (the
+    unit `achieved` is quoted in) of this workload, from the committed ncu
+    summary, if present."""
     p = os.path.join(ROOT, "profiles", "chain_kernel_config3.json")
     try:
         with open(p) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+            return json.load(f).get("dram_bytes_per_step")
     except Exception:
         return None
 

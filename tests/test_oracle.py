@@ -472,6 +472,26 @@ def test_isotherm_fixtures_match_reference_keys():
     assert len(seen) == 10
 
 
+@pytest.mark.parametrize("name", ["isotherm_oracle.json", "isotherm_device.json"])
+def test_recorded_isotherm_passes_reference_band(name):
+    """The recorded isotherm runs (the oracle on CPU; FP64 device-resident
+    chains on a GB300 with the ten CONTROL files unchanged, swap and switch
+    included) re-checked against run_test.py's criterion from the published
+    uptakes: both guests' averages within [0.8 (avg - se), 1.2 (avg + se)]
+    at all ten pressures, with the reference's run length."""
+    with open(os.path.join(GOLDEN, name)) as f:
+        rec = json.load(f)
+    ref = {float(k): v for k, v in golden()["isotherm_avg_guests"].items()}
+    assert len(rec["rows"]) == 10
+    for r in rec["rows"]:
+        k = min(ref, key=lambda v: abs(v - r["pressure_bar"]))
+        assert abs(k - r["pressure_bar"]) < 1e-5
+        co2, n2 = ref[k]
+        assert r.get("status", 0) == 0 and r["moves"] == 1250000
+        for avg, se, v in ((r["avg_co2"], r["se_co2"], co2), (r["avg_n2"], r["se_n2"], n2)):
+            assert 0.8 * (avg - se) <= v <= 1.2 * (avg + se), (r["point"], avg, se, v)
+
+
 def test_preload_prefilter_changes_nothing(oracle_lib, inputs_dir):
     """insert_guests' framework pre-test skips only trial positions that
     insertion() rejects anyway: with it on and off the same molecules are
