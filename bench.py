@@ -78,9 +78,9 @@ def algorithmic_flops_per_eval(cutoff: float, nk: int) -> float:
 
 def trial_evals(st) -> int:
     """Energy evaluations of the trial moves in a chain's counters (a swap
-    is a deletion and an insertion)."""
+    is a deletion and an insertion, an acting switch two of each)."""
     a = st.attempts
-    return int(a[0] + a[1] + 2 * (a[2] + a[3] + a[4] + a[5] + a[6]))
+    return int(a[0] + a[1] + 2 * (a[2] + a[3] + a[4] + a[5] + a[6]) + 4 * a[7])
 
 
 def workload(tmp: str):
@@ -537,6 +537,8 @@ def run_ours(args, rank, world, local_rank):
     infos = [s.info() for s in systems]
     batch = F.Batch(systems, specs, precision=F.FMC_PREC_FP32, guest_capacity=1024)
     batch.snapshot()  # the pre-loaded state every step starts from
+    if args.speculate:
+        batch.set_speculation(args.speculate)
     # CTAs per chain, from timed trial cycles (the chains' state is restored
     # afterwards); set-up, outside the timing
     if args.chain_clusters:
@@ -629,6 +631,7 @@ def run_ours(args, rank, world, local_rank):
                        "molecules_at_step_start": {"total": sum(loads), "max": max(loads),
                                                    "mean": sum(loads) / n},
                        "same_config": True,
+                       "speculative_proposals": args.speculate,
                        "l2": "flushed (256 MB write) before every timed step"},
             "trial_moves_per_s": moves / (dev_ms / 1000.0),
             "full_evals_per_s": full / (dev_ms / 1000.0),
@@ -702,6 +705,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
     ap.add_argument("--widom", action="store_true", help="also time config 5's 1e7 Widom trials")
+    ap.add_argument("--speculate", type=int, default=0,
+                    help="speculative proposals per round at most (2..8; 0: off)")
     ap.add_argument("--chain-clusters", default="", help="CTAs per chain, one value per chain")
     ap.add_argument("--clusters", default="", help="CTAs per chain per framework, e.g. 1,2,2,4 "
                     "(default: autotuned)")

@@ -269,6 +269,10 @@ class Batch:
         L.check(L.load().fmc_batch_get_sk(self._h, chain, out.ctypes.data_as(L.dp), out.size))
         return out.reshape(nk, maxmls + 1, 2)
 
+    def set_speculation(self, kmax: int):
+        """Speculative proposals per round at most (2..8; 0 or 1: off)."""
+        L.check(L.load().fmc_batch_set_speculation(self._h, int(kmax)))
+
     def set_cluster(self, sizes):
         """CTAs per chain for the chains of each system (1..8)."""
         a = (C.c_int * len(sizes))(*[int(v) for v in sizes])

@@ -142,6 +142,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // doubles after a round of exits only and halves after a round whose
     // first proposal passed (every thread computes the same value)
     const bool spec = speculation_applies(B, CA);
+    const int kcap = min(CA.spec_max, kMaxSpec);
     int kspec = 2;
     for (int it = 0; it < nmoves; ++it) {
       // the previous move's FP64 bookkeeping overlaps this proposal
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int kwin = min(kspec, nmoves - it);
         const int exits = spec_round(B, CA, chain, kwin, logs, logcap, rank);
         it += exits;
-        if (!B.spec_have) kspec = min(2 * kspec, kMaxSpec);
+        if (!B.spec_have) kspec = min(2 * kspec, kcap);
         else if (exits == 0) kspec = max(1, kspec / 2);
         if (!B.spec_have) {
           --it;  // the loop's increment counts no further move
@@ -160,8 +161,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         propose(B, CA, chain, kPropMC, 0);
       }
       FMC_PHASE(B, 0);
-      if (B.mc.kind == 7) {  // mc_swap: evaluation, decision, commit or rollback, statistics
-        swap_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);
+      if (B.mc.kind >= 7) {  // mc_swap / the acting mc_switch: evaluations, decision, commits or rollback, statistics
+        if (B.mc.kind == 7) swap_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);
+        else switch_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);
         if (B.S.prob_nsub > 0 && CA.grid && B.H.production) store_prob(B, CA, chain);
         __syncthreads();
         continue;

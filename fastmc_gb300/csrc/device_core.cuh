@@ -250,6 +250,7 @@ struct ChainArrays {
   int cap;          // molecules per guest type
   int nkmax;
   int resident;     // FP32 batches of one guest type: guests held in shared memory
+  int spec_max;     // proposals per speculative round at most (below 2: none)
 };
 
 // Entries of the sine/cosine table of the double-float quaternions (one

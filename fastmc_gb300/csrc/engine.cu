@@ -906,12 +906,16 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   C.sold.alloc((size_t)nchains * nkmax);
   C.snew.zero();
   C.sold.zero();
-  {  // FP64 chains with swap moves keep the two guest types' S(k) for a rejection
-    bool swaps = false;
+  {  // the two guest types' S(k) for a rejection: FP64 chains with swap
+    // moves, and chains whose switch moves can act (three or more guest
+    // types; both precisions, FP32 entries are 16-byte hi/lo pairs too)
+    bool swaps = false, switches = false;
     for (int i = 0; i < nsys; ++i)
-      for (int g = 1; g <= systems[i]->ntpguest; ++g)
+      for (int g = 1; g <= systems[i]->ntpguest; ++g) {
         if (systems[i]->mcswpf[g] > systems[i]->mcjmpf[g]) swaps = true;
-    if (swaps && precision == FMC_PREC_FP64) C.sksave.alloc((size_t)nchains * 2 * nkmax);
+        if (systems[i]->mcswif[g] > systems[i]->mcrotf[g] && systems[i]->ntpguest >= 3) switches = true;
+      }
+    if ((swaps && precision == FMC_PREC_FP64) || switches) C.sksave.alloc((size_t)nchains * 2 * nkmax);
   }
   C.skdf.alloc((size_t)nchains * kMaxG * nkmax);
   C.skdf.zero();
@@ -974,6 +978,7 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   // capacity x sites within the shared array); the per-move ABI keeps them
   // in global memory (its launches are single moves)
   CA.resident = (precision == FMC_PREC_FP32 && ngmax == 1 && cap * nsmax <= kGuestSmem) ? 1 : 0;
+  CA.spec_max = 0;  // speculative rounds off unless asked for (fmc_batch_set_speculation)
   cudaError_t e;
   if (precision == FMC_PREC_FP32 && C.gn == 1) e = set_chain_smem<true, 1>(C.smem);
   else if (precision == FMC_PREC_FP32) e = set_chain_smem<true, kMaxG>(C.smem);
@@ -2434,6 +2439,21 @@ int fmc_batch_set_cluster(fmc_batch *b, const int *csize, int nsys) {
     Chains &C = b->C;
     if (nsys != (int)C.sys.size()) raise(FMC_ERR_ARG, "one cluster size per system is required");
     C.set_clusters(std::vector<int>(csize, csize + nsys));
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_set_speculation(fmc_batch *b, int kmax) {
+  return guard([&] {
+    if (!b) raise(FMC_ERR_ARG, "null batch");
+    if (kmax < 0 || kmax > kMaxSpec) raise(FMC_ERR_ARG, "kmax must be 0..8");
+    Chains &C = b->C;
+    C.CA.spec_max = kmax;
+    if (C.graph) {  // the launches captured the old value
+      cudaGraphExecDestroy(C.graph);
+      C.graph = nullptr;
+    }
+    C.graph_moves = -1;
     return FMC_OK;
   });
 }

@@ -32,7 +32,9 @@ namespace fmcdev {
 // Phases: 0 proposal, 1 overlap test, 2 neighbour segments and near-guest
 // list, 3 framework and guest pair terms, 4 power tables, 5 k-space,
 // 6 block reduction, 7 cluster exchange, 8 epilogue, 9 decision and log,
-// 10 commit, 11 statistics.
+// 10 commit, 11 statistics; speculative rounds: 12 draws and selections,
+// 13 first-pass positions, 14 batched overlap tests, 15 exits and the
+// round's move.
 #ifdef FMC_PHASE_TIMERS
 #define FMC_PHASE(B, n)                                     \
   do {                                                      \
@@ -83,8 +85,11 @@ struct BlockShared {
     double chgtmp;
     double delE[kMaxM + 1];
   } dfr;
-  // a swap move in flight (swap_move): the partner type, the new molecule's
-  // sites, the energy changes, and the state a rejection puts back
+  // a swap or switch move in flight (swap_move, switch_move): the partner
+  // type, the new molecule's sites, the energy changes, and the state a
+  // rejection puts back; a switch also keeps the partner molecule, both
+  // molecules' centres, their sites relative to them and their coordinates
+  // before the move (index 0 the chosen molecule, 1 the partner)
   struct Swap {
     int gj, overlap, accepted;
     double estepi, estepj, rande;
@@ -93,6 +98,9 @@ struct BlockShared {
     double energy[kMaxM + 1], chgsum_mol[kMaxM + 1], surfacemols[kMaxM + 1];
     int numtyp[kMaxT + 1], numfrz[kMaxT + 1];
     int numtyp_mol[kMaxM + 1][kMaxT + 1], numfrz_mol[kMaxM + 1][kMaxT + 1];
+    int jchoice, slot_j;
+    double cen[2][3], rel[2][kMaxS][3], opos[2][kMaxS][3];
+    float4 ohi[2][kMaxS], olo[2][kMaxS];
   } swp;
   // speculative proposals (spec_round): each one's selection, first-pass
   // positions and overlap outcome, and the selection state after it
@@ -301,12 +309,16 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
                      (H.rota_count[g] >= 1 && H.rota_mod[g] == 0)))
     adapt_steps<F32>(H, G, g);
   if (nmols == 0) kind = 1;
+  int nsw = 0, swg[kMaxG];  // switch_chosen_guest: the other types holding molecules
   if (kind == 8) {
     // mc_switch (gcmc.f:2041-2267) returns before any draw unless two other
-    // guest types hold molecules, which set-up rules out (at most two guest
-    // types with switch moves): no move, and `accepted` keeps its value
-    B.flags[5] = 1;
-    kind = 0;
+    // guest types hold molecules: then no move, and `accepted` keeps its value
+    for (int i = 0; i < S.ntpguest; ++i)
+      if (H.nummols[i] > 0 && i != g) swg[nsw++] = i;
+    if (nsw < 2) {
+      B.flags[5] = 1;
+      kind = 0;
+    }
   }
   mc.kind = kind;
   mc.g = g;
@@ -329,6 +341,12 @@ __device__ void select_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
     B.swp.gj = jg < g + 1 ? jg - 1 : jg;
     for (int i = 3; i < 7; ++i) B.draws[i] = dc.next();
     B.geo[7] = H.rotangle;
+  } else if (kind == 8) {
+    // the acting mc_switch (gcmc.f:2096-2107): the partner type among the
+    // others holding molecules, then a molecule of each; run by switch_move
+    B.swp.gj = swg[pick1(dc.next(), nsw) - 1];
+    mc.choice = pick1(dc.next(), nmols);
+    B.swp.jchoice = pick1(dc.next(), H.nummols[B.swp.gj]);
   } else if (kind == 6) {
     // mc_jump (gcmc.f:1937-2039): the molecule, then random_jump's point
     // (utility_pack.f:3359-3380) and random_rot with angle 2 pi
@@ -432,7 +450,7 @@ __device__ void geometry_warp(BlockShared<F32> &B, const ChainArrays &CA, int ch
   const SysDev &S = B.S;
   MoveCtx &mc = B.mc;
   const int lane = threadIdx.x & 31;
-  if (mc.kind == 0 || mc.kind == 7) return;  // a swap builds its positions in swap_move
+  if (mc.kind == 0 || mc.kind >= 7) return;  // swap_move / switch_move build their positions
   const GuestType &G = S.g[mc.g];
   const int ns = G.ns;
   const bool mine = lane < 3 * ns;
@@ -697,7 +715,7 @@ __device__ void site_constants_and_bounds(BlockShared<F32> &B) {
 template <bool F32>
 __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   MoveCtx &mc = B.mc;
-  if (mc.kind == 0 || mc.kind == 7) return;  // a swap builds its positions in swap_move
+  if (mc.kind == 0 || mc.kind >= 7) return;  // swap_move / switch_move build their positions
   geometry_f32_core(B, CA, chain, mc.kind, mc.g, mc.slot, B.draws, B.stepf, B.flags[2], B.ev.phi,
                     B.ev.plo);
   __syncwarp();
@@ -2186,7 +2204,7 @@ __device__ __forceinline__ void load_selection(BlockShared<F32> &B,
 template <bool F32>
 __device__ __forceinline__ bool speculation_applies(const BlockShared<F32> &B, const ChainArrays &CA) {
   const SysDev &S = B.S;
-  if (!F32 || !CA.resident || !S.use_cells || S.ntpguest != 1) return false;
+  if (!F32 || CA.spec_max < 2 || !CA.resident || !S.use_cells || S.ntpguest != 1) return false;
   if (S.prob_nsub > 0 && CA.grid) return false;
   const float mincs = fminf(S.cszf[0], fminf(S.cszf[1], S.cszf[2]));
   return mincs >= sqrtf(S.overlap_sqf) + 0.01f;  // the 27 neighbour cells cover the test
@@ -2320,6 +2338,7 @@ __device__ int spec_round(BlockShared<F32> &B, const ChainArrays &CA, int chain,
     }
   }
   __syncthreads();
+  FMC_PHASE(B, 12);
   const int n = B.spec_n;
   {  // first-pass positions, warp j for proposal j
     const int w = threadIdx.x >> 5;
@@ -2330,8 +2349,10 @@ __device__ int spec_round(BlockShared<F32> &B, const ChainArrays &CA, int chain,
     }
   }
   __syncthreads();
+  FMC_PHASE(B, 13);
   overlap_batch(B, n);
   __syncthreads();
+  FMC_PHASE(B, 14);
   if (threadIdx.x == 0) {
     int j = 0;
     const GuestType &G = S.g[0];
@@ -2401,7 +2422,117 @@ __device__ int spec_round(BlockShared<F32> &B, const ChainArrays &CA, int chain,
     if (P.kind != 0) site_constants_and_bounds(B);
   }
   __syncthreads();
+  FMC_PHASE(B, 15);
   return B.spec_exits;
+}
+
+// Thread 0: the chain's counts, energies, charges, surface tallies and
+// site-type counters, kept for a swap or switch that may be rejected, and
+// put back.
+template <bool F32>
+__device__ void save_counts(BlockShared<F32> &B) {
+  const ChainHdr &H = B.H;
+  auto &W = B.swp;
+  for (int g = 0; g < kMaxG; ++g) {
+    W.nummols[g] = H.nummols[g];
+    W.nslots[g] = H.nslots[g];
+    W.nfree[g] = H.nfree[g];
+    W.skb[g] = H.skb[g];
+  }
+  for (int m = 0; m <= kMaxM; ++m) {
+    W.energy[m] = H.energy[m];
+    W.chgsum_mol[m] = H.chgsum_mol[m];
+    W.surfacemols[m] = H.surfacemols[m];
+    for (int t = 0; t <= kMaxT; ++t) {
+      W.numtyp_mol[m][t] = H.numtyp_mol[m][t];
+      W.numfrz_mol[m][t] = H.numfrz_mol[m][t];
+    }
+  }
+  for (int t = 0; t <= kMaxT; ++t) {
+    W.numtyp[t] = H.numtyp[t];
+    W.numfrz[t] = H.numfrz[t];
+  }
+}
+
+template <bool F32>
+__device__ void restore_counts(BlockShared<F32> &B) {
+  ChainHdr &H = B.H;
+  const auto &W = B.swp;
+  for (int g = 0; g < kMaxG; ++g) {
+    H.nummols[g] = W.nummols[g];
+    H.nslots[g] = W.nslots[g];
+    H.nfree[g] = W.nfree[g];
+    H.skb[g] = W.skb[g];  // FP32: the buffers current before the move
+  }
+  for (int m = 0; m <= kMaxM; ++m) {
+    H.energy[m] = W.energy[m];
+    H.chgsum_mol[m] = W.chgsum_mol[m];
+    H.surfacemols[m] = W.surfacemols[m];
+    for (int t = 0; t <= kMaxT; ++t) {
+      H.numtyp_mol[m][t] = W.numtyp_mol[m][t];
+      H.numfrz_mol[m][t] = W.numfrz_mol[m][t];
+    }
+  }
+  for (int t = 0; t <= kMaxT; ++t) {
+    H.numtyp[t] = W.numtyp[t];
+    H.numfrz[t] = W.numfrz[t];
+  }
+}
+
+// All threads of rank 0's CTA: a deleted molecule's slot back into its
+// type's order list at entry choice-1, the later entries shifted up (the
+// deletion shifted them down, mc_moves.f:574-590); n is the count before
+// the deletion.  Entry n-1, if in use, is overwritten.
+__device__ inline void reinsert_order(const ChainArrays &CA, int chain, int g, int choice, int slot,
+                               int n) {
+  int *ord = CA.ord + ((size_t)chain * kMaxG + g) * CA.cap;
+  const int c0 = choice - 1;
+  constexpr int kPer = 8;  // capacity <= 4096 = 8 * kThreads
+  int vals[kPer];
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int i = c0 + threadIdx.x + j * kThreads;
+    if (i < n - 1) vals[j] = ord[i];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int i = c0 + threadIdx.x + j * kThreads;
+    if (i < n - 1) ord[i + 1] = vals[j];
+  }
+  if (threadIdx.x == 0) ord[c0] = slot;
+  __syncthreads();
+}
+
+// This CTA's share of two guest types' S(k): the current buffers into the
+// chain's save area (save) or the save area back into the buffers given
+// by skb (restore).  FP32 entries are hi/lo float4, FP64 double2; both are
+// 16 bytes, the save area is typed double2.
+template <bool F32>
+__device__ void sk_pair_copy(BlockShared<F32> &B, const ChainArrays &CA, int chain, int ga, int gb,
+                             const int *skb, bool save) {
+  const SysDev &S = B.S;
+  int kb, ke;
+  share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
+  const int gs[2] = {ga, gb};
+  for (int m = 0; m < 2; ++m) {
+    const size_t o = ((size_t)chain * kMaxG + gs[m]) * CA.nkmax;
+    double2 *sv = CA.sksave + ((size_t)chain * 2 + m) * CA.nkmax;
+    if constexpr (F32) {
+      float4 *sk = (skb[gs[m]] ? CA.skdf2 : CA.skdf) + o;
+      float4 *sv4 = reinterpret_cast<float4 *>(sv);
+      for (int k = kb + threadIdx.x; k < ke; k += kThreads) {
+        if (save) sv4[k] = sk[k];
+        else sk[k] = sv4[k];
+      }
+    } else {
+      double2 *sk = CA.sk + o;
+      for (int k = kb + threadIdx.x; k < ke; k += kThreads) {
+        if (save) sv[k] = sk[k];
+        else sk[k] = sv[k];
+      }
+    }
+  }
 }
 
 // mc_swap (gcmc.f:2269-2452) inside a device-resident chain, all threads:
@@ -2427,25 +2558,7 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
   const int gi = mc.g, gj = W.gj, choice = mc.choice, slot_i = mc.slot;
   const GuestType &Gi = S.g[gi], &Gj = S.g[gj];
   if (threadIdx.x == 0) {
-    for (int g = 0; g < kMaxG; ++g) {
-      W.nummols[g] = H.nummols[g];
-      W.nslots[g] = H.nslots[g];
-      W.nfree[g] = H.nfree[g];
-      W.skb[g] = H.skb[g];
-    }
-    for (int m = 0; m <= kMaxM; ++m) {
-      W.energy[m] = H.energy[m];
-      W.chgsum_mol[m] = H.chgsum_mol[m];
-      W.surfacemols[m] = H.surfacemols[m];
-      for (int t = 0; t <= kMaxT; ++t) {
-        W.numtyp_mol[m][t] = H.numtyp_mol[m][t];
-        W.numfrz_mol[m][t] = H.numfrz_mol[m][t];
-      }
-    }
-    for (int t = 0; t <= kMaxT; ++t) {
-      W.numtyp[t] = H.numtyp[t];
-      W.numfrz[t] = H.numfrz[t];
-    }
+    save_counts(B);
     // centre of mass of the chosen molecule (com, utility_pack.f:3565-3596)
     const double *src = CA.gpos + gslot_base(CA, chain, gi, slot_i) * 3;
     double w = 0.0, c[3] = {0.0, 0.0, 0.0};
@@ -2476,17 +2589,9 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
     B.flags[6] = 0;
   }
   __syncthreads();
-  if constexpr (!F32) {  // both types' S(k), this CTA's share, for a rejection
-    int kb, ke;
-    share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
-    const double2 *ski = CA.sk + ((size_t)chain * kMaxG + gi) * CA.nkmax;
-    const double2 *skj = CA.sk + ((size_t)chain * kMaxG + gj) * CA.nkmax;
-    double2 *sv = CA.sksave + (size_t)chain * 2 * CA.nkmax;
-    for (int k = kb + threadIdx.x; k < ke; k += kThreads) {
-      sv[k] = ski[k];
-      sv[CA.nkmax + k] = skj[k];
-    }
-  }
+  // FP64: both types' S(k), this CTA's share, for a rejection (FP32: the
+  // buffers the two evaluations do not write keep it)
+  if constexpr (!F32) sk_pair_copy(B, CA, chain, gi, gj, H.skb, true);
   if (threadIdx.x < 32) {
     if constexpr (F32) geometry_f32(B, CA, chain);
     else geometry_warp(B, CA, chain, kPropMC);
@@ -2542,58 +2647,10 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
   }
   __syncthreads();
   if (!W.accepted) {
-    if (threadIdx.x == 0) {
-      for (int g = 0; g < kMaxG; ++g) {
-        H.nummols[g] = W.nummols[g];
-        H.nslots[g] = W.nslots[g];
-        H.nfree[g] = W.nfree[g];
-        H.skb[g] = W.skb[g];  // FP32: the buffers the evaluations left untouched
-      }
-      for (int m = 0; m <= kMaxM; ++m) {
-        H.energy[m] = W.energy[m];
-        H.chgsum_mol[m] = W.chgsum_mol[m];
-        H.surfacemols[m] = W.surfacemols[m];
-        for (int t = 0; t <= kMaxT; ++t) {
-          H.numtyp_mol[m][t] = W.numtyp_mol[m][t];
-          H.numfrz_mol[m][t] = W.numfrz_mol[m][t];
-        }
-      }
-      for (int t = 0; t <= kMaxT; ++t) {
-        H.numtyp[t] = W.numtyp[t];
-        H.numfrz[t] = W.numfrz[t];
-      }
-    }
-    if constexpr (!F32) {
-      int kb, ke;
-      share_of(S.nk, B.ev.rank, B.ev.csize, kb, ke);
-      double2 *ski = CA.sk + ((size_t)chain * kMaxG + gi) * CA.nkmax;
-      double2 *skj = CA.sk + ((size_t)chain * kMaxG + gj) * CA.nkmax;
-      const double2 *sv = CA.sksave + (size_t)chain * 2 * CA.nkmax;
-      for (int k = kb + threadIdx.x; k < ke; k += kThreads) {
-        ski[k] = sv[k];
-        skj[k] = sv[CA.nkmax + k];
-      }
-    }
-    if (rank == 0) {
-      // the deleted molecule back into the order list at its place
-      // (accept_move shifted the later ones down, mc_moves.f:574-590)
-      int *ord = CA.ord + ((size_t)chain * kMaxG + gi) * CA.cap;
-      const int n = W.nummols[gi], c0 = choice - 1;
-      constexpr int kPer = 8;  // capacity <= 4096 = 8 * kThreads
-      int vals[kPer];
-#pragma unroll
-      for (int j = 0; j < kPer; ++j) {
-        const int i = c0 + threadIdx.x + j * kThreads;
-        if (i < n - 1) vals[j] = ord[i];
-      }
-      __syncthreads();
-#pragma unroll
-      for (int j = 0; j < kPer; ++j) {
-        const int i = c0 + threadIdx.x + j * kThreads;
-        if (i < n - 1) ord[i + 1] = vals[j];
-      }
-      if (threadIdx.x == 0) ord[c0] = slot_i;
-    }
+    if (threadIdx.x == 0) restore_counts(B);  // FP32: skb back to the buffers left untouched
+    if constexpr (!F32) sk_pair_copy(B, CA, chain, gi, gj, W.skb, false);
+    // the deleted molecule back into the order list at its place
+    if (rank == 0) reinsert_order(CA, chain, gi, choice, slot_i, W.nummols[gi]);
     __syncthreads();
     cluster_commit_sync(B, st);
   }
@@ -2617,6 +2674,195 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
         L.rande = W.rande;
         for (int s = 0; s < 3 && s < Gj.ns; ++s)
           for (int d = 0; d < 3; ++d) L.newxyz[3 * s + d] = W.pos[s][d];
+        L.nmols_after = H.nummols[gi];
+      }
+      H.log_n++;
+    }
+    mc.g = gi;  // the move's guest type, for what follows
+    stats_production<F32>(S, H, H.production, acc);
+  }
+  __syncthreads();
+}
+
+// The acting mc_switch (gcmc.f:2096-2267) inside a device-resident chain,
+// all threads: molecule ichoice of type gi and molecule jchoice of type gj
+// exchange centres of mass, each keeping its orientation.  As the
+// reference runs it: both deletions evaluated and committed (accept_move),
+// the partner inserted at the first molecule's centre and committed, then
+// the first molecule at the partner's centre, evaluated and committed.  An
+// insertion that overlaps is committed too, as the reference does: it stops
+// before its structure factor, so accept_move adds the one the partner's
+// deletion left (FP64: the scratch s(k); FP32: the S(k) buffer that
+// deletion did not write) and delE cleared, and the next insertion is
+// evaluated against that state.  Decided as a displacement on estepi +
+// estepj, with no number drawn when the sum is negative, and vetoed by any
+// overlap.  A rejection puts back counts, energies, charges, surface
+// tallies, both types' S(k), both molecules' coordinates and the order
+// lists; the system charge keeps the four commits, which cancel.
+template <bool F32, int GN>
+__device__ void switch_move(BlockShared<F32> &B, const ChainArrays &CA, int chain, int &st,
+                            LogRec *logs, int logcap, int rank) {
+  SysDev &S = B.S;
+  ChainHdr &H = B.H;
+  MoveCtx &mc = B.mc;
+  auto &W = B.swp;
+  const int gi = mc.g, gj = W.gj, ichoice = mc.choice, jchoice = W.jchoice, slot_i = mc.slot;
+  const GuestType &Gi = S.g[gi], &Gj = S.g[gj];
+  if (threadIdx.x == 0) {
+    save_counts(B);
+    W.overlap = 0;
+    W.slot_j = CA.ord[((size_t)chain * kMaxG + gj) * CA.cap + (jchoice - 1)];
+    // both molecules' centres of mass (com, utility_pack.f:3565-3596), their
+    // sites relative to them (gcmc.f:2140-2153) and their coordinates
+    const int gs[2] = {gi, gj}, slots[2] = {slot_i, W.slot_j};
+    for (int m = 0; m < 2; ++m) {
+      const GuestType &G = S.g[gs[m]];
+      const size_t b = gslot_base(CA, chain, gs[m], slots[m]);
+      const double *src = CA.gpos + b * 3;
+      double w = 0.0, c[3] = {0.0, 0.0, 0.0};
+      for (int k = 0; k < G.ns; ++k) {
+        w += G.mass[k];
+        for (int d = 0; d < 3; ++d) c[d] += src[3 * k + d] * G.mass[k];
+      }
+      for (int d = 0; d < 3; ++d) W.cen[m][d] = c[d] / w;
+      for (int k = 0; k < G.ns; ++k) {
+        for (int d = 0; d < 3; ++d) {
+          W.opos[m][k][d] = src[3 * k + d];
+          W.rel[m][k][d] = src[3 * k + d] - W.cen[m][d];
+        }
+        W.ohi[m][k] = CA.ghi[b + k];
+        W.olo[m][k] = CA.glo[b + k];
+      }
+    }
+    mc.kind = 2;  // the first deletion (choice, slot as proposed)
+    mc.npos = 1;
+    mc.ns = Gi.ns;
+    B.flags[3] = F32 ? 1 : 0;
+    B.flags[4] = 0;  // delE of every molecule type now: the commit is forced
+    B.flags[6] = 0;
+  }
+  __syncthreads();
+  sk_pair_copy(B, CA, chain, gi, gj, H.skb, true);  // this CTA's share, for a rejection
+  int nfull = 0;
+  // step: evaluate the move in mc (positions from the geometry for a
+  // deletion, given in mc.pos for an insertion) and commit it, forced
+  auto half = [&](double &acc_estep, bool del) {
+    if (del && threadIdx.x < 32) {
+      if constexpr (F32) geometry_f32(B, CA, chain);
+      else geometry_warp(B, CA, chain, kPropMC);
+    }
+    __syncthreads();
+    nfull += evaluate_any<F32, GN>(B, CA, chain, st);
+    if (threadIdx.x == 0) {
+      if (del) {
+        acc_estep = -mc.estep;
+      } else if (mc.overlap) {
+        W.overlap = 1;  // insertion cleared delE before its overlap exit; estep stays 0
+        for (int m = 0; m <= kMaxM; ++m) mc.delE[m] = 0.0;
+      } else {
+        acc_estep += mc.estep;
+      }
+      mc.accepted = 1;
+    }
+    __syncthreads();
+    commit(B, CA, chain, st, false);
+  };
+  half(W.estepi, true);
+  if (threadIdx.x == 0) {  // the partner's deletion
+    mc.kind = 2;
+    mc.g = gj;
+    mc.ns = Gj.ns;
+    mc.npos = 1;
+    mc.choice = jchoice;
+    mc.slot = W.slot_j;
+    mc.overlap = 0;
+    mc.estep = 0.0;
+    mc.accepted = 0;
+    mc.surf_new = mc.surf_old = 0;
+    B.flags[3] = F32 ? 1 : 0;
+  }
+  half(W.estepj, true);
+  // the partner at the first molecule's centre, then the first molecule at
+  // the partner's (gcmc.f:2185-2214)
+  for (int m = 1; m >= 0; --m) {
+    if (threadIdx.x == 0) {
+      const GuestType &G = m ? Gj : Gi;
+      mc.kind = 1;
+      mc.g = m ? gj : gi;
+      mc.ns = G.ns;
+      mc.npos = 1;
+      mc.slot = -1;
+      mc.choice = 0;
+      mc.overlap = 0;
+      mc.estep = 0.0;
+      mc.accepted = 0;
+      mc.surf_new = mc.surf_old = 0;
+      for (int k = 0; k < G.ns; ++k)
+        for (int d = 0; d < 3; ++d) mc.pos[0][k][d] = W.rel[m][k][d] + W.cen[1 - m][d];
+      B.flags[3] = 0;  // FP64 positions
+    }
+    half(m ? W.estepj : W.estepi, false);
+  }
+  if (threadIdx.x == 0) {  // gcmc.f:2218-2229
+    const double e = W.estepi + W.estepj;
+    int acc = 1;
+    double r0 = -1.0;
+    if (!(e < 0.0)) {
+      r0 = (double)draw_f(H);
+      double test;
+      if (-S.beta * e > 700.0) test = exp(700.0);
+      else if (S.beta * e > 700.0) test = exp(-700.0);
+      else test = exp(-1.0 * S.beta * e);
+      acc = r0 < test;
+    }
+    if (W.overlap) acc = 0;
+    W.accepted = acc;
+    W.rande = r0;
+  }
+  __syncthreads();
+  if (!W.accepted) {
+    if (threadIdx.x == 0) restore_counts(B);
+    sk_pair_copy(B, CA, chain, gi, gj, W.skb, false);
+    if (rank == 0) {
+      // order lists: each molecule back at its entry (its re-insertion took
+      // the slot its deletion freed and sits at the end), and its coordinates
+      reinsert_order(CA, chain, gi, ichoice, slot_i, W.nummols[gi]);
+      reinsert_order(CA, chain, gj, jchoice, W.slot_j, W.nummols[gj]);
+      const int t = threadIdx.x;
+      if (t < 2 * kMaxS) {
+        const int m = t / kMaxS, k = t % kMaxS;
+        const GuestType &G = m ? Gj : Gi;
+        if (k < G.ns) {
+          const size_t b = gslot_base(CA, chain, m ? gj : gi, m ? W.slot_j : slot_i) + k;
+          for (int d = 0; d < 3; ++d) CA.gpos[b * 3 + d] = W.opos[m][k][d];
+          CA.ghi[b] = W.ohi[m][k];
+          CA.glo[b] = W.olo[m][k];
+        }
+      }
+    }
+    __syncthreads();
+    cluster_commit_sync(B, st);
+  }
+  if (threadIdx.x == 0) {
+    const int acc = W.accepted;
+    H.last_accepted = acc;
+    H.attempts[7]++;
+    if (acc) H.accepts[7]++;
+    H.moves++;
+    H.evals += nfull;
+    if (W.overlap) H.overlap_exits++;
+    if (logcap > 0 && H.log_n < logcap) {
+      if (rank == 0) {
+        LogRec &L = logs[(size_t)chain * logcap + H.log_n];
+        L.move = 8;
+        L.iguest = gi + 1;
+        L.choice = ichoice;
+        L.overlap = W.overlap;
+        L.accepted = acc;
+        L.estep = W.estepi + W.estepj;
+        L.rande = W.rande;
+        for (int k = 0; k < 3 && k < Gi.ns; ++k)
+          for (int d = 0; d < 3; ++d) L.newxyz[3 * k + d] = W.rel[0][k][d] + W.cen[1][d];
         L.nmols_after = H.nummols[gi];
       }
       H.log_n++;

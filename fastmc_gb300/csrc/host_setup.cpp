@@ -884,13 +884,9 @@ void finish_control(System &s) {
     s.mctraf[i] = s.mcswpf[i] + (s.mctraf[i] / nrm);
     s.mcrotf[i] = s.mctraf[i] + (s.mcrotf[i] / nrm);
     s.mcswif[i] = s.mcrotf[i] + (s.mcswif[i] / nrm);
-    // swap needs a partner type (device-resident chains refuse it; it runs
-    // through the per-move fmc_swap); switch only as the move that returns
-    // without acting (fewer than two other loaded guest types, which holds
-    // for every move when the system has at most two guest types)
+    // swap needs a partner type; switch acts only with three or more guest
+    // types (it returns without a draw unless two other types hold molecules)
     if (s.mcswpf[i] > s.mcjmpf[i] && G < 2) raise(FMC_ERR_INPUT, "swap moves need two guest types");
-    if (s.mcswif[i] > s.mcrotf[i] && G >= 3)
-      raise(FMC_ERR_INPUT, "switch moves with three or more guest types are not supported");
   }
   s.beta = 1.0 / (kKboltz * s.temp);
   s.statvolm = s.volm * 1e-30;
@@ -1176,8 +1172,6 @@ void upload_system(const fmc_system_desc &d, System &s) {
     s.mcswif[g] = f[7];
     for (int k = 1; k < 8; ++k) need(f[k] >= f[k - 1], "move thresholds must be cumulative");
     if (s.mcswpf[g] > s.mcjmpf[g] && G < 2) raise(FMC_ERR_INPUT, "swap moves need two guest types");
-    if (s.mcswif[g] > s.mcrotf[g] && G >= 3)
-      raise(FMC_ERR_INPUT, "switch moves with three or more guest types are not supported");
   }
   for (int i = 0; i < 9; ++i) s.ucell[i] = s.cell[i];  // no probability grids
   invert3(s.ucell, s.rucell);

@@ -459,6 +459,15 @@ int fmc_batch_set_cluster(fmc_batch *b, const int *csize, int nsys);
  * it gets a size again); at least one chain must stay active. */
 int fmc_batch_set_chain_cluster(fmc_batch *b, const int *csize, int nchains);
 int fmc_batch_get_chain_cluster(const fmc_batch *b, int *csize, int nchains);
+/* Speculative proposals in FP32 batches of one guest type with resident
+ * guests: up to kmax (2..8) moves are drawn ahead, their overlap tests run
+ * as one block-wide pass, the leading overlap exits are completed together
+ * and the draws of the proposals after the first one that passes are
+ * undone, so the chains' moves, draws and decisions are those of the
+ * sequential loop.  0 or 1: off (the default).  No reference counterpart:
+ * the reference runs one move at a time (gcmc.f:704-1164). */
+int fmc_batch_set_speculation(fmc_batch *b, int kmax);
+
 int fmc_batch_get_cluster(const fmc_batch *b, int *csize, int nsys);
 
 /* Autotuner: picks the cluster size of every system by timing trial cycles

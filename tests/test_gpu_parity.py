@@ -584,20 +584,75 @@ def test_gpu_window_statistics_two_guests_fp64(fmc_lib, oracle_lib, inputs_dir):
         assert close(st.guest_se_n[g - 1], ref[29], rel=1e-9, scale=1e-9), (g, st.guest_se_n[g - 1], ref[29])
 
 
+def _open_dir(tmp_path, name, mix, ntypes):
+    """An open framework (48 atoms per 12.8 A cell), 1.5 A overlap distance,
+    CO2 plus the two-site dipolar guest (and the three-site linear one):
+    8 / 6 (/ 6) molecules pre-loaded, none of them on the LJ wall."""
+    spec = syn.small_test_spec(seed=4, kmax=6, pressure_bar=5.0, create=8, move_mix=mix)
+    spec.overlap = 1.5
+    spec.second_guest = True
+    spec.create2 = 6
+    if ntypes == 3:
+        spec.third_guest = True
+        spec.create3 = 6
+    d = str(tmp_path / name)
+    syn.write_inputs(d, spec, uc=syn.make_unit_cell(4, natoms=48))
+    return d
+
+
+def _follow(got, ref, prec, kinds, tol_kind):
+    """Move-by-move comparison of a device chain's log with the oracle's:
+    move, guest type and molecule always; FP64 every decision, rande and
+    count, estep to 1e-9; FP32 until the first decision that differs (a
+    decision at the threshold), estep to 2e-6 of max(|estep|, 1), moves of
+    the given kinds to tol_kind of max(|estep|, 100) (they add energies of
+    several molecules).  The given kinds' estep is compared also when they
+    overlapped.  Returns the number of the given kinds compared."""
+    nk = 0
+    for i, (g, r) in enumerate(zip(got, ref)):
+        assert (g.move, g.iguest, g.choice) == (r.move, r.iguest, r.choice), i
+        if prec == "fp32" and (g.overlap != r.overlap or g.accepted != r.accepted):
+            break
+        assert (g.overlap, g.accepted) == (r.overlap, r.accepted), i
+        if prec == "fp64":
+            assert g.rande == r.rande, i
+            assert g.nmols_after == r.nmols_after, i
+        if r.move in kinds:
+            tol = 1e-9 * max(abs(r.estep), 1.0) if prec == "fp64" else tol_kind * max(abs(r.estep), 100.0)
+            assert abs(g.estep - r.estep) <= tol, (i, g.estep, r.estep)
+            nk += 1
+        elif not r.overlap:
+            tol = 1e-9 if prec == "fp64" else 2e-6
+            assert abs(g.estep - r.estep) <= tol * max(abs(r.estep), 1.0), (i, g.estep, r.estep)
+    return nk
+
+
+def _final_state(b, o, types):
+    """FP64 chain 0 against the oracle at the end: every guest type's count
+    and coordinates in molecule order, and S(k)."""
+    for gg in types:
+        m = o.locguest(gg)
+        x, cnt = _batch_coords(b, gg)
+        assert cnt == o.nummols(m)
+        assert np.allclose(x, o.coords(m), rtol=0, atol=1e-9)
+    info = b.systems[0].info()
+    so = o.sk()
+    assert np.allclose(b.sk(0, info.newld, info.maxmls), so, rtol=0, atol=1e-9 * np.abs(so).max())
+
+
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_gpu_chain_swaps_follow_oracle(fmc_lib, oracle_lib, inputs_dir, prec):
+def test_gpu_chain_swaps_follow_oracle(fmc_lib, oracle_lib, tmp_path, prec):
     """Swap moves inside device-resident chains (mc_swap, gcmc.f:2269-2452):
     the chain follows the oracle move by move -- the swapped molecule, the
     partner type and orientation drawn, both tests with the second number
-    drawn only when the first passes, and rejections that put the state
-    back (about 300 of them; with the reference's tests, whose volume is in
-    cubic angstroms, a swap is accepted only when the deletion releases
-    more than about 69 kT and the partner fits where it left, which does not
-    happen here).  FP64: every decision, estep (deletion plus insertion) to
-    1e-9, and at the end both guest types' coordinates and S(k).  FP32:
-    until the first decision at a threshold, estep to 2e-6 of
-    max(|estep|, 1), 1e-5 for the swaps themselves."""
-    d = _swap_dir(inputs_dir)
+    drawn only when the first passes, acceptances (3 here; with the
+    reference's tests, whose volume is in cubic angstroms, a swap is
+    accepted only when the deletion releases more than about 69 kT) and
+    about 300 rejections that put the state back.  FP64: every decision,
+    estep (deletion plus insertion) to 1e-9, and at the end both guest
+    types' coordinates and S(k).  FP32: until the first decision at a
+    threshold, swaps' estep to 1e-5 of max(|estep|, 100 kcal/mol)."""
+    d = _open_dir(tmp_path, "swap", (("insert", 0.2), ("displace", 0.3), ("swap", 0.5)), 2)
     n = 600
     o = oracle_lib.Oracle(d)
     o.seed(5)
@@ -610,34 +665,50 @@ def test_gpu_chain_swaps_follow_oracle(fmc_lib, oracle_lib, inputs_dir, prec):
     b.run(n)
     got = b.log(0, n)
     swaps = [r for r in ref if r.move == 7]
-    assert len(swaps) >= 100
-    nsw = 0
-    for i, (g, r) in enumerate(zip(got, ref)):
-        assert (g.move, g.iguest, g.choice) == (r.move, r.iguest, r.choice), i
-        if prec == "fp32" and (g.overlap != r.overlap or g.accepted != r.accepted):
-            break
-        assert (g.overlap, g.accepted) == (r.overlap, r.accepted), i
-        if prec == "fp64":
-            assert g.rande == r.rande, i
-            assert g.nmols_after == r.nmols_after, i
-        if not r.overlap:
-            # FP32: a swap adds two energies that, for pre-loaded molecules on
-            # the LJ wall, reach 1e5 kcal/mol; measured within 4e-6 of them
-            tol = 1e-9 if prec == "fp64" else (1e-5 if r.move == 7 else 2e-6)
-            assert abs(g.estep - r.estep) <= tol * max(abs(r.estep), 1.0), (i, g.estep, r.estep)
-        nsw += r.move == 7
+    assert len(swaps) >= 250 and sum(r.accepted for r in swaps) >= 2
+    nsw = _follow(got, ref, prec, (7,), 1e-5)
     assert nsw >= 50
     if prec == "fp64":
         st = b.stats()[0]
         assert st.attempts[6] == len(swaps) and st.accepts[6] == sum(r.accepted for r in swaps)
-        for gg in (1, 2):
-            m = o.locguest(gg)
-            x, cnt = _batch_coords(b, gg)
-            assert cnt == o.nummols(m)
-            assert np.allclose(x, o.coords(m), rtol=0, atol=1e-9)
-        info = b.systems[0].info()
-        so = o.sk()
-        assert np.allclose(b.sk(0, info.newld, info.maxmls), so, rtol=0, atol=1e-9 * np.abs(so).max())
+        _final_state(b, o, (1, 2))
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_gpu_chain_switch_follows_oracle(fmc_lib, oracle_lib, tmp_path, prec):
+    """The acting mc_switch (gcmc.f:2041-2267) inside device-resident chains
+    with three guest types: a molecule and one of another type that holds
+    molecules exchange centres of mass, both deletions and both insertions
+    committed before the decision (also an insertion that overlaps, whose
+    commit adds the structure factor the partner's deletion left, as the
+    reference's accept_move does; the second insertion is evaluated against
+    that state, so estep and whether a number is drawn follow it), decided
+    as a displacement on estepi + estepj, rejections putting everything
+    back.  About 490 switches: 18 accepted, 71 with an overlap, 440 with a
+    number drawn.  FP64: every decision, rande and count, estep to 1e-9
+    (overlapping switches included), and at the end all three types'
+    coordinates and S(k).  FP32: until the first decision at a threshold,
+    switches' estep to 1e-5 of max(|estep|, 100 kcal/mol)."""
+    d = _open_dir(tmp_path, "switch", (("displace", 0.4), ("switch", 0.6)), 3)
+    n = 800
+    o = oracle_lib.Oracle(d)
+    o.seed(5)
+    for gg, k in ((1, 8), (2, 6), (3, 6)):
+        o.create_molecules(gg, k)
+    ref = o.run(n)
+    p = fmc_lib.FMC_PREC_FP64 if prec == "fp64" else fmc_lib.FMC_PREC_FP32
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 5}], precision=p, guest_capacity=64)
+    b.set_log(n)
+    b.run(n)
+    got = b.log(0, n)
+    sw = [r for r in ref if r.move == 8]
+    assert len(sw) >= 400 and sum(r.accepted for r in sw) >= 10 and sum(r.overlap for r in sw) >= 30
+    nsw = _follow(got, ref, prec, (8,), 1e-5)
+    assert nsw >= 50
+    if prec == "fp64":
+        st = b.stats()[0]
+        assert st.attempts[7] == len(sw) and st.accepts[7] == sum(r.accepted for r in sw)
+        _final_state(b, o, (1, 2, 3))
 
 
 def _batch_coords(b, iguest):

@@ -169,3 +169,30 @@ def test_fp32_structure_factor_does_not_drift(fmc_lib, oracle_lib, tmp_path):
     errs = [r["sk_rel_err"] for r in report]
     assert max(errs) < 1e-5
     assert errs[2] < 4.0 * max(errs[0], 1e-9)  # no growth with the number of moves
+
+
+def test_speculation_changes_nothing(fmc_lib, tmp_path):
+    """Speculative rounds (fmc_batch_set_speculation) draw proposals ahead,
+    test their overlaps together and undo the draws after the first one
+    that passes: the chains' moves, decisions and energies are bit for bit
+    those of the sequential loop, on one CTA and on a cluster, with every
+    round size."""
+    spec = syn.small_test_spec(seed=5, kmax=8, ntile=3, pressure_bar=5.0, create=60)
+    d = str(tmp_path / "spec")
+    syn.write_inputs(d, spec)
+    sysm = fmc_lib.System.load(d)
+    b = fmc_lib.Batch([sysm], [{"seed": 3}, {"seed": 4}, {"seed": 5}],
+                      precision=fmc_lib.FMC_PREC_FP32, guest_capacity=256)
+    b.set_chain_cluster([1, 2, 1])
+    b.snapshot()
+    runs = []
+    for k in (0, 2, 5, 8):
+        b.restore()
+        b.set_speculation(k)
+        b.set_log(400)
+        b.run(400)
+        runs.append((_logs(b, 400), [(s.nummols, s.energy, s.moves, s.overlap_exits, tuple(s.accepts))
+                                     for s in b.stats()]))
+    assert sum(r[2] for r in runs[0][0][0]) >= 100  # overlap exits to batch
+    for r in runs[1:]:
+        assert r == runs[0]

@@ -109,9 +109,8 @@ def test_probability_inputs(fmc_lib, tmp_path):
 
 
 def test_swap_and_switch_set_up(fmc_lib, tmp_path):
-    """Swap needs a partner type; switch loads with up to two guest types
-    (where mc_switch never acts) and is refused with three; three guest
-    types without switch load."""
+    """Swap needs a partner type (refused with one guest type); switch loads
+    with any number of guest types (it acts from three on)."""
     import fastmc_gb300._lib as L
 
     def spec(mix, ntypes):
@@ -121,8 +120,9 @@ def test_swap_and_switch_set_up(fmc_lib, tmp_path):
         return s
     for mix, ntypes, ok in (((("insert", 0.5), ("switch", 0.5)), 1, True),
                             ((("insert", 0.5), ("switch", 0.5)), 2, True),
-                            ((("insert", 0.5), ("switch", 0.5)), 3, False),
+                            ((("insert", 0.5), ("switch", 0.5)), 3, True),
                             ((("insert", 0.5), ("displace", 0.5)), 3, True),
+                            ((("insert", 0.5), ("swap", 0.5)), 1, False),
                             ((("insert", 0.5), ("swap", 0.5)), 2, True)):
         d = tmp_path / f"s{len(list(tmp_path.iterdir()))}"
         syn.write_inputs(str(d), spec(mix, ntypes))
@@ -131,7 +131,7 @@ def test_swap_and_switch_set_up(fmc_lib, tmp_path):
         else:
             with pytest.raises(L.FmcError) as e:
                 fmc_lib.System.load(str(d))
-            assert "switch" in str(e.value)
+            assert "swap" in str(e.value)
 
 
 def test_peng_robinson_fugacity(fmc_lib, oracle_lib, tmp_path):
