@@ -152,6 +152,8 @@ SIGNATURES = {
     "fmc_batch_cycle_bytes": (C.c_int, [vp, i64p, i64p]),
     "fmc_batch_set_cluster": (C.c_int, [vp, ip, C.c_int]),
     "fmc_batch_set_speculation": (C.c_int, [vp, C.c_int]),
+    "fmc_batch_write_revive": (C.c_int, [vp, C.c_int, C.c_char_p]),
+    "fmc_batch_read_revive": (C.c_int, [vp, C.c_int, C.c_char_p]),
     "fmc_batch_get_cluster": (C.c_int, [vp, ip, C.c_int]),
     "fmc_batch_autotune": (C.c_int, [vp, C.c_int, ip, C.c_int]),
     "fmc_batch_save": (C.c_int, [vp, C.c_char_p]),

@@ -269,6 +269,14 @@ class Batch:
         L.check(L.load().fmc_batch_get_sk(self._h, chain, out.ctypes.data_as(L.dp), out.size))
         return out.reshape(nk, maxmls + 1, 2)
 
+    def write_revive(self, chain: int, directory: str):
+        """The reference's REVIVE and REVCON for one chain, into directory."""
+        L.check(L.load().fmc_batch_write_revive(self._h, chain, directory.encode()))
+
+    def read_revive(self, chain: int, directory: str):
+        """Restart one chain from directory/REVIVE as the reference does."""
+        L.check(L.load().fmc_batch_read_revive(self._h, chain, directory.encode()))
+
     def set_speculation(self, kmax: int):
         """Speculative proposals per round at most (2..8; 0 or 1: off)."""
         L.check(L.load().fmc_batch_set_speculation(self._h, int(kmax)))

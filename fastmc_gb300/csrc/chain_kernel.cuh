@@ -21,6 +21,7 @@ constexpr int kModeCreate = 1;  // "create molecules" pre-loading
 constexpr int kModeEval = 2;    // evaluate the move in gctx (per-move ABI)
 constexpr int kModeCommit = 3;  // decide with gctx.rande and commit
 constexpr int kModeWidom = 4;   // test insertions of a WidomJob (no state change)
+constexpr int kModeLoad = 5;    // insert a WidomJob's positions into chain wj.chain (restart)
 
 // Warp 0: trial t of a Widom job as an external insertion (FP64 positions).
 template <bool F32>
@@ -90,8 +91,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   BlockShared<F32> &B = *reinterpret_cast<BlockShared<F32> *>(dyn);
   const unsigned long long t_start = global_ns();
   const int rank = csize > 1 ? (int)cluster_rank() : 0;
-  const int chain = mode == kModeWidom ? wj.chain
-                    : (chain_ids ? chain_ids[blockIdx.x / csize] : (int)blockIdx.x / csize);
+  const int chain = (mode == kModeWidom || mode == kModeLoad)
+                        ? wj.chain
+                        : (chain_ids ? chain_ids[blockIdx.x / csize] : (int)blockIdx.x / csize);
   block_copy(&B.H, hdrs + chain);
   __syncthreads();
   block_copy(&B.S, systems + B.H.system);
@@ -223,10 +225,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         propose(B, CA, chain, kPropInsert, g);
-        evaluate_any<F32, GN>(B, CA, chain, st);
+        evaluate_rare<F32, GN>(B, CA, chain, st);
         if (threadIdx.x == 0) B.mc.accepted = B.mc.overlap ? 0 : 1;
         __syncthreads();
-        commit(B, CA, chain, st);
+        commit_rare(B, CA, chain, st);
         __syncthreads();
         ++iter;
       }
@@ -264,6 +266,23 @@ __global__ void __launch_bounds__(kThreads, 1)
       wj.partial[3 * blockIdx.x] = hsum;
       wj.partial[3 * blockIdx.x + 1] = (double)nok;
       wj.partial[3 * blockIdx.x + 2] = (double)ntot;
+    }
+  } else if (mode == kModeLoad) {
+    // molecules read from a restart file, in order: each inserted where it
+    // is, whatever it overlaps (revread loads them as they are), and
+    // committed with the energy changes of every molecule type
+    for (int t = 0; t < wj.ntrial; ++t) {
+      if (threadIdx.x < 32) widom_propose(B, wj, t);
+      if (threadIdx.x == 0) {
+        B.flags[4] = 0;
+        B.flags[6] = 1;  // no overlap test
+      }
+      __syncthreads();
+      evaluate_rare<F32, GN>(B, CA, chain, st);
+      if (threadIdx.x == 0) B.mc.accepted = 1;
+      __syncthreads();
+      commit_rare(B, CA, chain, st);
+      __syncthreads();
     }
   } else if (mode == kModeCommit) {
     // nmoves carries the host's decision (0 or 1), or -1 for energy_eval

@@ -46,6 +46,7 @@ constexpr int kStBadChoice = 16;   // molecule index out of range
 constexpr int kStKmax = 32;        // kmax beyond the shared tables
 constexpr int kStWait = 64;        // a bounded wait on an asynchronous copy ran out
 constexpr int kStDraws = 128;      // generator buffer empty (internal error)
+constexpr int kStIndex = 256;      // a guest slot or position out of range (access skipped)
 constexpr int kRBuf = 256;         // generator outputs drawn ahead per chain (power of two)
 
 constexpr double kPi = 3.141592653589793;
@@ -322,53 +323,12 @@ struct Acc {  // per-position partial sums
   double mix[kMaxM + 1];
 };
 
-// ------------------------------------------ bulk copies and mbarriers
-// One-dimensional bulk asynchronous copies global -> shared that complete
-// on an mbarrier (transaction count), and bounded waits on it.
-constexpr int kKT = kThreads;       // k-vectors per staged tile
-constexpr int kWaitLimit = 1 << 22; // try_wait polls before a wait gives up
+// ------------------------------------------------- padding, waits
+constexpr int kKT = kThreads;       // k-vector arrays are padded to multiples of this
+constexpr int kWaitLimit = 1 << 22; // polls before a bounded wait gives up
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_fence_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
-                                         unsigned long long *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Wait for the given phase parity; false if it did not complete in time.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
-  for (int it = 0; it < kWaitLimit; ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-// Order this thread's generic-proxy global writes before later bulk copies
-// that read the same data.
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async;" ::: "memory");
 }
 
 // ------------------------------------------------- thread-block clusters

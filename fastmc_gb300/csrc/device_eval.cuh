@@ -466,6 +466,10 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
       share_of(n2, sm.rank, sm.csize, i0, i1);
       for (int i = i0 + threadIdx.x; i < i1; i += kThreads) {
         int slot = ord[i];
+        if ((unsigned)slot >= (unsigned)CA.cap) {  // a damaged order list: skipped, reported
+          st |= kStIndex;
+          continue;
+        }
         if (g2 == self_g && slot == self_slot) continue;
         float4 q0 = gh[(size_t)slot * kMaxS];
         float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y,
@@ -512,6 +516,10 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
       share_of(n2, sm.rank, sm.csize, i0, i1);
       for (int i = i0 + threadIdx.x; i < i1; i += kThreads) {
         int slot = ord[i];
+        if ((unsigned)slot >= (unsigned)CA.cap) {  // a damaged order list: skipped, reported
+          st |= kStIndex;
+          continue;
+        }
         if (g2 == self_g && slot == self_slot) continue;
         size_t base = (((size_t)chain * kMaxG + g2) * CA.cap + slot) * kMaxS;
         const double *q0 = CA.gpos + base * 3;

@@ -136,6 +136,7 @@ constexpr int kModeCreate = 1;
 constexpr int kModeEval = 2;
 constexpr int kModeCommit = 3;
 constexpr int kModeWidom = 4;
+constexpr int kModeLoad = 5;
 
 // ----------------------------------------------------- device allocations
 // Every cudaMalloc / cudaFree the library makes goes through DBuf and is
@@ -840,7 +841,8 @@ struct Chains {
         std::snprintf(buf, sizeof buf,
                       "chain %d raised device status 0x%x (1 table range, 2 segment overflow, "
                       "4 capacity, 8 non-finite, 16 bad molecule index, 32 kmax, "
-                      "64 copy wait timed out, 128 generator buffer empty)",
+                      "64 copy wait timed out, 128 generator buffer empty, "
+                      "256 guest slot or position out of range)",
                       c, host_hdr[c].status);
         raise(FMC_ERR_DEVICE, buf);
       }
@@ -2296,6 +2298,296 @@ int fmc_batch_restore(fmc_batch *b) {
     if (!b) raise(FMC_ERR_ARG, "null batch");
     if (!b->snap) raise(FMC_ERR_STATE, "no snapshot taken (fmc_batch_snapshot)");
     restore_state(b->C, *b->snap);  // the saved records select the first S(k) buffer
+    return FMC_OK;
+  });
+}
+
+// ------------------------------------------------------ REVIVE / REVCON
+// The reference's restart files (revive, utility_pack.f:2299-2344; revread,
+// gcmc.f:447-474).  REVIVE is a Fortran unformatted sequential file: each
+// record is its byte count (4 bytes), the data, and the count again, as
+// gfortran writes it; integers and logicals are 4 bytes, reals 8, in the
+// host's byte order.  REVCON is the formatted configuration revive writes
+// beside it, in CONFIG's layout.
+
+static void frec_write(std::FILE *f, const void *p, size_t bytes) {
+  if (bytes > 0x7fffffffu) raise(FMC_ERR_CAPACITY, "REVIVE record too large");
+  const uint32_t n = (uint32_t)bytes;
+  if (std::fwrite(&n, 4, 1, f) != 1 || (bytes && std::fwrite(p, 1, bytes, f) != bytes) ||
+      std::fwrite(&n, 4, 1, f) != 1)
+    raise(FMC_ERR_ARG, "REVIVE write failed");
+}
+
+static std::vector<char> frec_read(std::FILE *f, size_t want, const char *what) {
+  uint32_t n = 0, m = 0;
+  if (std::fread(&n, 4, 1, f) != 1) raise(FMC_ERR_INPUT, std::string("REVIVE truncated at ") + what);
+  if (n != want) raise(FMC_ERR_INPUT, std::string("REVIVE record ") + what + " has the wrong length");
+  std::vector<char> v(n);
+  if ((n && std::fread(v.data(), 1, n, f) != n) || std::fread(&m, 4, 1, f) != 1 || m != n)
+    raise(FMC_ERR_INPUT, std::string("REVIVE record ") + what + " is damaged");
+  return v;
+}
+
+// Fortran edit descriptors of revive's formats, gfortran's output.
+static std::string fort_e(double v, int w, int d) {  // Ew.d: 0.ddddE+xx
+  char buf[64];
+  int ex = 0;
+  std::string digits(d, '0');
+  if (v != 0.0) {
+    std::snprintf(buf, sizeof buf, "%.*e", d - 1, std::fabs(v));  // m.mmmme+xx
+    std::string t(buf);
+    const size_t e = t.find('e');
+    digits = t.substr(0, 1) + t.substr(2, e - 2);
+    ex = std::atoi(t.c_str() + e + 1) + 1;
+  }
+  std::string out = std::string(std::signbit(v) ? "-" : "") + "0." + digits;
+  char eb[16];
+  if (std::abs(ex) <= 99) std::snprintf(eb, sizeof eb, "E%c%02d", ex < 0 ? '-' : '+', std::abs(ex));
+  else std::snprintf(eb, sizeof eb, "%c%03d", ex < 0 ? '-' : '+', std::abs(ex));
+  out += eb;
+  if ((int)out.size() > w) return std::string(w, '*');
+  return std::string(w - out.size(), ' ') + out;
+}
+
+static std::string fort_f(double v, int w, int d) {  // Fw.d
+  char buf[128];
+  std::snprintf(buf, sizeof buf, "%*.*f", w, d, v);
+  std::string out(buf);
+  if ((int)out.size() > w) return std::string(w, '*');
+  return out;
+}
+
+static std::string fort_g(double v, int w, int d) {  // Gw.d, 4 trailing blanks in F form
+  const double a = std::fabs(v);
+  if (a == 0.0) return fort_f(v, w - 4, d - 1) + "    ";
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%.*e", d - 1, a);  // rounded to d significant digits
+  const int x = std::atoi(std::strchr(buf, 'e') + 1);
+  const int s = x + 1;  // digits before the decimal point of the rounded value
+  if (x < -1 || s > d) return fort_e(v, w, d);
+  return fort_f(v, w - 4, d - s) + "    ";
+}
+
+// The chain's guest molecule types in the reference's order, with their
+// site coordinates in molecule order (molxxx/molyyy/molzzz).
+struct ReviveState {
+  std::vector<int> nummols;                      // [mol 1..maxmls]
+  std::vector<std::vector<double>> x, y, z;      // [mol][site]
+};
+
+int fmc_batch_write_revive(fmc_batch *b, int chain, const char *dir) {
+  return guard([&] {
+    if (!b || !dir) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (chain < 0 || chain >= C.nchains) raise(FMC_ERR_ARG, "bad chain index");
+    C.sync();
+    C.pull_headers();
+    const ChainHdr &h = C.host_hdr[chain];
+    const System &s = *C.hsys[h.system];
+    const int M = s.maxmls, G = s.ntpguest;
+    ReviveState st;
+    st.nummols.assign(M + 1, 0);
+    st.x.resize(M + 1);
+    st.y.resize(M + 1);
+    st.z.resize(M + 1);
+    for (int m = 1; m <= M; ++m) {
+      const MolType &mt = s.mol[m];
+      std::vector<double> xyz;
+      if (mt.guest) {
+        int g = 0;
+        for (int i = 1; i <= G; ++i)
+          if (s.locguest[i] == m) g = i;
+        xyz.assign((size_t)3 * mt.natoms * std::max(1, h.nummols[g - 1]), 0.0);
+        int n = 0;
+        chain_coords(C, chain, g, xyz.data(), (int)xyz.size(), &n);
+        st.nummols[m] = n;
+        xyz.resize((size_t)3 * mt.natoms * n);
+      } else {
+        st.nummols[m] = mt.nummols;
+        xyz = mt.xyz;
+      }
+      for (size_t i = 0; i < xyz.size() / 3; ++i) {
+        st.x[m].push_back(xyz[3 * i]);
+        st.y[m].push_back(xyz[3 * i + 1]);
+        st.z[m].push_back(xyz[3 * i + 2]);
+      }
+    }
+    int totatm = 0;
+    for (int m = 1; m <= M; ++m) totatm += st.nummols[m] * s.mol[m].natoms;
+    // chainstats(1 .. 16 ntpguest + 1): the production count and the open
+    // window's sums (gcmc.f:1052-1077), with the moves an FP32 chain has not
+    // yet added; the end-of-run averages (istat+7 .. istat+16) are zero
+    // while a run goes on
+    std::vector<double> cs((size_t)16 * G + 1, 0.0);
+    cs[0] = double(h.prodcount);
+    for (int i = 0; i < G; ++i) {
+      const int mol = s.locguest[i + 1];
+      const double pend = double(h.pend);
+      const double dm = double((float)h.nummols[i]), e = h.energy[mol];
+      const double sm = double((float)h.surfacemols[mol]);
+      const double add[6] = {pend * dm, pend * e, pend * (e * dm), pend * (dm * dm), pend * (e * e),
+                             pend * sm};
+      for (int q = 0; q < 6; ++q) cs[1 + 16 * i + q] = h.chainstats[i][q] + add[q];
+    }
+    const std::string d(dir);
+    {  // REVCON (utility_pack.f:2316-2326): guests first, then the framework (condense)
+      std::unique_ptr<std::FILE, int (*)(std::FILE *)> f(std::fopen((d + "/REVCON").c_str(), "w"),
+                                                          &std::fclose);
+      if (!f) raise(FMC_ERR_ARG, "cannot open " + d + "/REVCON");
+      std::string title = s.cfgname;
+      title.resize(80, ' ');
+      for (char &c : title)
+        if ((unsigned char)c < 32) c = ' ';
+      const int mol0 = s.locguest[1];
+      std::string out = title + "\n" + "         0";  // levcfg 0
+      char ib[32];
+      std::snprintf(ib, sizeof ib, "%10d", s.imcon);
+      out += ib + fort_e(h.energy[mol0], 20, 10) + "\n";
+      if (s.imcon > 0)
+        for (int r = 0; r < 3; ++r)
+          out += fort_f(s.cell[3 * r], 20, 12) + fort_f(s.cell[3 * r + 1], 20, 12) +
+                 fort_f(s.cell[3 * r + 2], 20, 12) + "\n";
+      int idx = 0;
+      auto emit = [&](int m) {
+        const MolType &mt = s.mol[m];
+        for (int k = 0; k < st.nummols[m] * mt.natoms; ++k) {
+          std::string nm = mt.site[k % mt.natoms];
+          nm.resize(8, ' ');
+          std::snprintf(ib, sizeof ib, "%10d", ++idx);
+          out += nm + ib + "\n" + fort_g(st.x[m][k], 20, 10) + fort_g(st.y[m][k], 20, 10) +
+                 fort_g(st.z[m][k], 20, 10) + "\n";
+        }
+      };
+      for (int g = 1; g <= G; ++g) emit(s.locguest[g]);
+      for (int k = 1; k <= s.ntpfram; ++k) emit(s.locfram[k]);
+      if (std::fwrite(out.data(), 1, out.size(), f.get()) != out.size())
+        raise(FMC_ERR_ARG, "REVCON write failed");
+    }
+    {  // REVIVE (utility_pack.f:2328-2341)
+      std::unique_ptr<std::FILE, int (*)(std::FILE *)> f(std::fopen((d + "/REVIVE").c_str(), "wb"),
+                                                          &std::fclose);
+      if (!f) raise(FMC_ERR_ARG, "cannot open " + d + "/REVIVE");
+      const int32_t prod = h.production ? 1 : 0;
+      frec_write(f.get(), &prod, 4);
+      std::vector<int32_t> nm(st.nummols.begin() + 1, st.nummols.end());
+      frec_write(f.get(), nm.data(), 4 * nm.size());
+      frec_write(f.get(), cs.data(), 8 * cs.size());
+      const int32_t na = totatm;
+      frec_write(f.get(), &na, 4);
+      for (int m = 1; m <= M; ++m) {
+        frec_write(f.get(), st.x[m].data(), 8 * st.x[m].size());
+        frec_write(f.get(), st.y[m].data(), 8 * st.y[m].size());
+        frec_write(f.get(), st.z[m].data(), 8 * st.z[m].size());
+      }
+      // energy(i), i = 1..ntpguest, indexed by molecule type as written
+      std::vector<double> en(G);
+      for (int i = 1; i <= G; ++i) en[i - 1] = h.energy[i];
+      frec_write(f.get(), en.data(), 8 * en.size());
+    }
+    return FMC_OK;
+  });
+}
+
+int fmc_batch_read_revive(fmc_batch *b, int chain, const char *dir) {
+  return guard([&] {
+    if (!b || !dir) raise(FMC_ERR_ARG, "null argument");
+    Chains &C = b->C;
+    if (chain < 0 || chain >= C.nchains) raise(FMC_ERR_ARG, "bad chain index");
+    C.sync();
+    C.normalize_sk();
+    C.pull_headers();
+    const ChainHdr cur = C.host_hdr[chain];
+    const System &s = *C.hsys[cur.system];
+    const int M = s.maxmls, G = s.ntpguest;
+    std::unique_ptr<std::FILE, int (*)(std::FILE *)> f(
+        std::fopen((std::string(dir) + "/REVIVE").c_str(), "rb"), &std::fclose);
+    if (!f) raise(FMC_ERR_ARG, std::string("cannot open ") + dir + "/REVIVE");
+    // everything is read and checked before the chain changes
+    int32_t prod = 0, na = 0;
+    std::memcpy(&prod, frec_read(f.get(), 4, "production").data(), 4);
+    std::vector<int32_t> nm(M);
+    std::memcpy(nm.data(), frec_read(f.get(), 4 * (size_t)M, "nummols").data(), 4 * (size_t)M);
+    std::vector<double> cs((size_t)16 * G + 1);
+    std::memcpy(cs.data(), frec_read(f.get(), 8 * cs.size(), "chainstats").data(), 8 * cs.size());
+    std::memcpy(&na, frec_read(f.get(), 4, "natms").data(), 4);
+    int tot = 0;
+    for (int m = 1; m <= M; ++m) {
+      if (nm[m - 1] < 0) raise(FMC_ERR_INPUT, "REVIVE holds a negative molecule count");
+      tot += nm[m - 1] * s.mol[m].natoms;
+    }
+    if (na != tot) raise(FMC_ERR_INPUT, "REVIVE's atom count does not match its molecule counts");
+    std::vector<std::vector<double>> xyz(M + 1);
+    for (int m = 1; m <= M; ++m) {
+      const MolType &mt = s.mol[m];
+      const size_t n = (size_t)nm[m - 1] * mt.natoms;
+      if (!mt.guest && nm[m - 1] != mt.nummols)
+        raise(FMC_ERR_INPUT, "REVIVE's framework differs from this system's");
+      if (mt.guest && nm[m - 1] > C.CA.cap) raise(FMC_ERR_CAPACITY, "REVIVE exceeds the guest capacity");
+      std::vector<double> c[3];
+      const char *nmx[3] = {"molxxx", "molyyy", "molzzz"};
+      for (int d = 0; d < 3; ++d) {
+        c[d].resize(n);
+        if (n) std::memcpy(c[d].data(), frec_read(f.get(), 8 * n, nmx[d]).data(), 8 * n);
+        else frec_read(f.get(), 0, nmx[d]);
+      }
+      xyz[m].resize(3 * n);
+      for (size_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) xyz[m][3 * i + d] = c[d][i];
+      if (!mt.guest)  // the framework is the system's (frozen; its tables are built)
+        for (size_t i = 0; i < 3 * n; ++i)
+          if (std::fabs(xyz[m][i] - mt.xyz[i]) > 1e-9)
+            raise(FMC_ERR_INPUT, "REVIVE's framework differs from this system's");
+    }
+    frec_read(f.get(), 8 * (size_t)G, "energy");  // single_point recomputes the energies
+    // a new chain record as the start-up leaves it (production from
+    // eqsteps, gcmc.f:450-465, 600), keeping the chain's generator, pressure,
+    // log and device time; the open window's sums from the file
+    ChainHdr h = initial_header(s, cur.system, 0, nullptr);
+    std::memcpy(h.u, cur.u, sizeof h.u);
+    h.c = cur.c;
+    h.cd = cur.cd;
+    h.cm = cur.cm;
+    h.ir = cur.ir;
+    h.jr = cur.jr;
+    std::memcpy(h.rbuf, cur.rbuf, sizeof h.rbuf);
+    h.rhead = cur.rhead;
+    h.ravail = cur.ravail;
+    std::memcpy(h.fuga, cur.fuga, sizeof h.fuga);
+    h.log_n = cur.log_n;
+    h.dev_ns = cur.dev_ns;
+    FMC_CUDA(cudaMemcpy(C.hdr.p + chain, &h, sizeof h, cudaMemcpyHostToDevice));
+    const size_t so = (size_t)chain * kMaxG * C.CA.nkmax;
+    if (C.sk.p) FMC_CUDA(cudaMemset(C.sk.p + so, 0, sizeof(double2) * kMaxG * C.CA.nkmax));
+    if (C.skdf.p) FMC_CUDA(cudaMemset(C.skdf.p + so, 0, sizeof(float4) * kMaxG * C.CA.nkmax));
+    if (C.skdf2.p) FMC_CUDA(cudaMemset(C.skdf2.p + so, 0, sizeof(float4) * kMaxG * C.CA.nkmax));
+    if (C.grid.p)  // probability grids start again with the run
+      FMC_CUDA(cudaMemset(C.grid.p + (size_t)chain * C.CA.grid_stride, 0,
+                          sizeof(double) * C.CA.grid_stride));
+    // the molecules, each type in order, inserted where they are
+    for (int g = 1; g <= G; ++g) {
+      const int m = s.locguest[g];
+      const int n = nm[m - 1];
+      if (n == 0) continue;
+      DBuf<double> in;
+      in.upload(xyz[m]);
+      WidomJob wj{};
+      wj.chain = chain;
+      wj.iguest = g - 1;
+      wj.ntrial = n;
+      wj.nstep = 1;
+      wj.ng[0] = wj.ng[1] = wj.ng[2] = 1;
+      wj.xyz_in = in.p;
+      FMC_CUDA(C.launch_one(1, 1, nullptr, C.stream, kModeLoad, 0, wj));
+      C.sync();
+    }
+    C.headers_stale = true;
+    C.pull_headers();
+    ChainHdr &hn = C.host_hdr[chain];
+    if (hn.status) raise(FMC_ERR_DEVICE, "loading the REVIVE molecules raised a device status");
+    for (int i = 0; i < G; ++i)
+      for (int q = 0; q < 6; ++q) hn.chainstats[i][q] = cs[1 + 16 * i + q];
+    FMC_CUDA(cudaMemcpy(C.hdr.p + chain, &hn, sizeof hn, cudaMemcpyHostToDevice));
+    (void)prod;  // revread's production flag gives way to eqsteps at start-up
     return FMC_OK;
   });
 }

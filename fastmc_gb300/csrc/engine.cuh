@@ -123,7 +123,8 @@ struct BlockShared {
   double geo[12];    // a, b, c, q1..q4, rotation angle, com/frac scratch
   double vtmp[3];
   int flags[8];     // 0 status, 1 slot, 2 "translate" (q = 0), 3 FP32 geometry, 4 delE deferred,
-                    // 5 switch no-op, 6 overlap test already passed (speculative round)
+                    // 5 switch no-op, 6 overlap test already passed (speculative round),
+                    // 7 positions out of range (position_bounds)
   // cluster exchange (chains on more than one CTA): per-CTA partial totals,
   // double-buffered, and the flags the peers raise in this CTA's memory
   double xv[2][40];
@@ -564,6 +565,10 @@ __device__ __forceinline__ void position_bounds(BlockShared<F32> &B, int lane) {
   }
   if (act) B.ev.cen[p][d] = c;
   if (act && d == 0) B.ev.rmx[p] = sqrtf(rm2) + 1e-3f;
+  // positions that are not finite or far outside any cell (a damaged
+  // state): the evaluation refuses them before any index is formed
+  const unsigned bad = __ballot_sync(full, act && !(fabsf(c) < 1.0e6f && rm2 < 1.0e4f));
+  if (lane == 0) B.flags[7] = bad ? 1 : 0;
 }
 
 // FP32 quaternion of random_ins / random_rot: half angle pi * r * scale
@@ -906,6 +911,10 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
         } else {
           mc.slot = (F32 && CA.resident) ? mc.choice - 1
                                          : CA.ord[((size_t)chain * kMaxG + mc.g) * CA.cap + (mc.choice - 1)];
+          if ((unsigned)mc.slot >= (unsigned)CA.cap) {  // a damaged order list
+            B.H.status |= kStIndex;
+            mc.kind = 0;
+          }
         }
       }
     }
@@ -1071,6 +1080,10 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
       float pre2 = pre * pre;
       for (int i = threadIdx.x; i < n2 && !hit; i += kThreads) {
         int slot = ord[i];
+        if ((unsigned)slot >= (unsigned)CA.cap) {
+          atomicOr(&B.flags[0], kStIndex);
+          continue;
+        }
         if (g2 == mc.g && slot == mc.slot) continue;
         float4 q0 = gh[(size_t)slot * kMaxS];
         float dx = ev.phi[0][0][0] - q0.x, dy = ev.phi[0][0][1] - q0.y, dz = ev.phi[0][0][2] - q0.z;
@@ -1091,6 +1104,10 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
     } else {
       for (int i = threadIdx.x; i < n2 && !hit; i += kThreads) {
         int slot = ord[i];
+        if ((unsigned)slot >= (unsigned)CA.cap) {
+          atomicOr(&B.flags[0], kStIndex);
+          continue;
+        }
         if (g2 == mc.g && slot == mc.slot) continue;
         const double *q = CA.gpos + gslot_base(CA, chain, g2, slot) * 3;
         if (S.use_cells) {
@@ -1624,6 +1641,15 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
     if (threadIdx.x < 32) position_bounds(B, threadIdx.x);  // conservative (FP32)
     __syncthreads();
   }
+  if (B.flags[7]) {  // positions out of range: no evaluation, reported
+    if (threadIdx.x == 0) {
+      mc.overlap = 1;
+      mc.estep = 0.0;
+    }
+    st |= kStIndex;
+    __syncthreads();
+    return 0;
+  }
   if (mc.kind == 1 || mc.kind >= 3) {
     if (!B.flags[6]) {  // flags[6]: a speculative round found this position clear already
       const int hit = overlap_check(B, CA, chain);
@@ -1761,6 +1787,15 @@ __device__ __forceinline__ int evaluate_any(BlockShared<F32> &B, const ChainArra
     if (B.mc.ns == 3) return evaluate<F32, GN, 3>(B, CA, chain, st);
   }
   return evaluate<F32, GN, 0>(B, CA, chain, st);
+}
+
+// The same, called rather than inlined: for the moves and modes that run
+// seldom (pre-loading, restart loading, swap and switch halves), so that the
+// kernel holds one more copy of the evaluation instead of one per call site.
+template <bool F32, int GN>
+__device__ __noinline__ int evaluate_rare(BlockShared<F32> &B, const ChainArrays &CA, int chain,
+                                          int &st) {
+  return evaluate_any<F32, GN>(B, CA, chain, st);
 }
 
 // ----------------------------------------------------------------- decide
@@ -1940,6 +1975,10 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
         st |= kStCapacity;
         slot = -1;
       }
+      if (slot >= CA.cap || slot < -1) {  // a damaged free list
+        st |= kStIndex;
+        slot = -1;
+      }
       if (slot >= 0 && B.ev.rank == 0) ord[H.nummols[g]] = slot;
     }
     B.flags[1] = slot;
@@ -2019,6 +2058,14 @@ __device__ void commit(BlockShared<F32> &B, const ChainArrays &CA, int chain, in
   }
   __syncthreads();
   if (!res) cluster_commit_sync(B, st);  // resident guests: every CTA updated its own copy
+}
+
+// commit, called rather than inlined, for the seldom-run paths (as
+// evaluate_rare).
+template <bool F32>
+__device__ __noinline__ void commit_rare(BlockShared<F32> &B, const ChainArrays &CA, int chain,
+                                         int &st) {
+  commit(B, CA, chain, st, false);
 }
 
 __device__ inline double calc_qst(double E, double N, double N2, double EN, double T) {
@@ -2597,13 +2644,13 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
     else geometry_warp(B, CA, chain, kPropMC);
   }
   __syncthreads();
-  evaluate_any<F32, GN>(B, CA, chain, st);
+  evaluate_rare<F32, GN>(B, CA, chain, st);
   if (threadIdx.x == 0) {
     W.estepi = -mc.estep;
     mc.accepted = 1;
   }
   __syncthreads();
-  commit(B, CA, chain, st, false);
+  commit_rare(B, CA, chain, st);
   // the partner molecule
   if (threadIdx.x == 0) {
     mc.kind = 1;
@@ -2622,14 +2669,14 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
     B.flags[6] = 0;
   }
   __syncthreads();
-  const int full_j = evaluate_any<F32, GN>(B, CA, chain, st);
+  const int full_j = evaluate_rare<F32, GN>(B, CA, chain, st);
   if (threadIdx.x == 0) {
     W.estepj = mc.estep;
     W.overlap = mc.overlap;
     mc.accepted = mc.overlap ? 0 : 1;
   }
   __syncthreads();
-  commit(B, CA, chain, st, false);
+  commit_rare(B, CA, chain, st);
   if (threadIdx.x == 0) {  // the reference's two tests (gcmc.f:2371-2411)
     int acc = 0;
     double r0 = -1.0;
@@ -2752,7 +2799,7 @@ __device__ void switch_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
       else geometry_warp(B, CA, chain, kPropMC);
     }
     __syncthreads();
-    nfull += evaluate_any<F32, GN>(B, CA, chain, st);
+    nfull += evaluate_rare<F32, GN>(B, CA, chain, st);
     if (threadIdx.x == 0) {
       if (del) {
         acc_estep = -mc.estep;
@@ -2765,7 +2812,7 @@ __device__ void switch_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
       mc.accepted = 1;
     }
     __syncthreads();
-    commit(B, CA, chain, st, false);
+    commit_rare(B, CA, chain, st);
   };
   half(W.estepi, true);
   if (threadIdx.x == 0) {  // the partner's deletion

@@ -87,6 +87,7 @@ struct System {
   std::vector<double> ewald3en;  // [mol]
   int fw_mol = 0;                // the single framework molecule type
   int n_fw = 0;                  // framework atoms
+  std::string cfgname = std::string(80, ' ');  // CONFIG title (REVCON's first record)
 };
 
 // host_setup.cpp

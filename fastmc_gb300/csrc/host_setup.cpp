@@ -556,6 +556,7 @@ void read_config(const std::string &dir, System &s) {
   Record r;
   Reader f(join(dir, "CONFIG"));
   f.need(r);
+  s.cfgname.assign(r.c, r.c + 80);  // cfgname, the title record's first 80 characters
   f.need(r);
   int levcfg = int_of(r);
   for (int row = 0; row < 3; ++row) {

@@ -388,6 +388,28 @@ int fmc_batch_load(fmc_batch *b, const char *path);
  * positions, system indices) before any of it reaches the device; a
  * rejected file (FMC_ERR_INPUT) leaves the batch unchanged. */
 
+/* The reference's restart files for one chain (revive,
+ * utility_pack.f:2299-2344), written into the existing directory dir:
+ * REVIVE, Fortran unformatted sequential records as gfortran writes them
+ * (the production flag, nummols of every molecule type, chainstats(1 ..
+ * 16 ntpguest + 1) -- the production count and the open window's sums --,
+ * the atom count, each molecule type's x, y and z site coordinates, and
+ * energy(1 .. ntpguest)); and REVCON, the configuration in CONFIG's layout
+ * (guests first, then the framework, as condense orders them).  A
+ * reference run restarts from REVIVE with revread (gcmc.f:447-474). */
+int fmc_batch_write_revive(fmc_batch *b, int chain, const char *dir);
+
+/* Restart one chain from dir/REVIVE, as the reference does after revread
+ * (gcmc.f:447-474) and its start-up: the guest molecules of the file are
+ * inserted where they are (no overlap test) and the energies, S(k),
+ * counts and charges follow from them; the open window's sums come from
+ * the file; the production flag, counters, step sizes, windows and
+ * probability grids start again; the chain keeps its generator and
+ * pressure.  The framework in the file must be this system's, and the
+ * counts must fit the batch's capacity (FMC_ERR_INPUT / FMC_ERR_CAPACITY;
+ * nothing is changed then). */
+int fmc_batch_read_revive(fmc_batch *b, int chain, const char *dir);
+
 /* The same state copy kept in device memory: fmc_batch_snapshot copies
  * every chain's state, fmc_batch_restore puts that copy back (any number
  * of times), so that cycles can be replayed from one state -- e.g. timed
