@@ -604,10 +604,12 @@ def _follow(got, ref, prec, kinds, tol_kind):
     """Move-by-move comparison of a device chain's log with the oracle's:
     move, guest type and molecule always; FP64 every decision, rande and
     count, estep to 1e-9; FP32 until the first decision that differs (a
-    decision at the threshold), estep to 2e-6 of max(|estep|, 1), moves of
-    the given kinds to tol_kind of max(|estep|, 100) (they add energies of
-    several molecules).  The given kinds' estep is compared also when they
-    overlapped.  Returns the number of the given kinds compared."""
+    decision at the threshold), estep to 2e-6 of max(|estep|, 30 kcal/mol)
+    (the FP32 error follows the moving molecule's energies, not their
+    difference; measured at most 5.4e-5 kcal/mol on identical states), moves
+    of the given kinds to tol_kind of max(|estep|, 100) (they add energies
+    of several molecules).  The given kinds' estep is compared also when
+    they overlapped.  Returns the number of the given kinds compared."""
     nk = 0
     for i, (g, r) in enumerate(zip(got, ref)):
         assert (g.move, g.iguest, g.choice) == (r.move, r.iguest, r.choice), i
@@ -622,8 +624,8 @@ def _follow(got, ref, prec, kinds, tol_kind):
             assert abs(g.estep - r.estep) <= tol, (i, g.estep, r.estep)
             nk += 1
         elif not r.overlap:
-            tol = 1e-9 if prec == "fp64" else 2e-6
-            assert abs(g.estep - r.estep) <= tol * max(abs(r.estep), 1.0), (i, g.estep, r.estep)
+            tol = 1e-9 * max(abs(r.estep), 1.0) if prec == "fp64" else 2e-6 * max(abs(r.estep), 30.0)
+            assert abs(g.estep - r.estep) <= tol, (i, g.estep, r.estep)
     return nk
 
 

@@ -79,12 +79,13 @@ def test_revive_round_trip(fmc_lib, oracle_lib, sysdir, tmp_path, prec):
     o = oracle_lib.Oracle(sysdir)
     mol = o.locguest(1)
     fw = [m for m in range(1, info.maxmls + 1) if m != mol][0]
-    natoms = {mol: 3, fw: o.coords(fw).size // 3}
+    nfw = o.nummols(fw)  # the framework: nfw molecules (tiles of the unit cell)
+    natoms = {mol: 3, fw: o.coords(fw).shape[0] // nfw}
     st = b.stats()[0]
     prod, nm, cs, natms, xyz, en = parse_revive(os.path.join(d, "REVIVE"), info.maxmls, natoms, 1)
     x, n = b.coords(0)
-    assert nm[mol - 1] == n == st.nummols and nm[fw - 1] == 1
-    assert natms == 3 * n + natoms[fw]
+    assert nm[mol - 1] == n == st.nummols and nm[fw - 1] == nfw
+    assert natms == 3 * n + nfw * natoms[fw]
     assert np.array_equal(xyz[mol], x[:9 * n])
     assert np.array_equal(xyz[fw], o.coords(fw).reshape(-1))
     assert prod in (0, 1)
@@ -135,8 +136,8 @@ def test_revive_from_the_oracle(fmc_lib, oracle_lib, sysdir, tmp_path):
     fw = [m for m in range(1, info.maxmls + 1) if m != mol][0]
     n = o.nummols(mol)
     recs = [struct.pack("<i", 0),
-            struct.pack(f"<{info.maxmls}i", *[n if m == mol else 1 for m in range(1, info.maxmls + 1)]),
-            np.zeros(17).tobytes(), struct.pack("<i", 3 * n + o.coords(fw).size // 3)]
+            struct.pack(f"<{info.maxmls}i", *[o.nummols(m) for m in range(1, info.maxmls + 1)]),
+            np.zeros(17).tobytes(), struct.pack("<i", 3 * n + o.coords(fw).shape[0])]
     for m in range(1, info.maxmls + 1):
         c = o.coords(m).reshape(-1, 3)
         recs += [np.ascontiguousarray(c[:, d]).tobytes() for d in range(3)]
@@ -173,13 +174,16 @@ def test_revive_rejects_damaged_file(fmc_lib, sysdir, tmp_path):
     bad[2] = bad[2][:-8]  # chainstats one value short
     cases.append((bad, L.FMC_ERR_INPUT))
     info = sysm.info()
+    mol = info.guest_mol[0]
+    fw = [m for m in range(1, info.maxmls + 1) if m != mol][0]
     nm = list(struct.unpack(f"<{info.maxmls}i", recs[1]))
-    big = [1000 if v != 1 else v for v in nm]  # guest count above the capacity
+    big = list(nm)
+    big[mol - 1] = 1000  # guest count above the capacity
     bad = list(recs)
     bad[1] = struct.pack(f"<{info.maxmls}i", *big)
     cases.append((bad, None))
     bad = list(recs)
-    fwi = 4 + 3 * nm.index(1)
+    fwi = 4 + 3 * (fw - 1)
     arr = np.frombuffer(recs[fwi], dtype="<f8").copy()
     arr[0] += 0.5
     bad[fwi] = arr.tobytes()
