@@ -119,6 +119,9 @@ struct SysDev {
   double rcsz[3];          // 1 / csz
   double rbox[3];          // 1 / L, the reference's aaa = 1/cell (images)
   float boxh[3], boxl[3];  // L as a float hi/lo pair
+  // parallelepiped cells (imcon 3), FP32 path: cell and its inverse as
+  // float hi/lo pairs, the reference's layout (cell[0..2] the first edge)
+  float cellh[9], celll[9], rcellh[9], rcelll[9];
   float rboxf[3], rcszf[3], cszf[3];
   float rboxf_lo[3];       // 1/L - rboxf
   float overlap_sqf, rc2f, rdrewdf, rdlrpotf;

@@ -236,6 +236,70 @@ __device__ __forceinline__ void mi_diff_df(float ph, float pl, float qh, float q
   dl = e + (al - ql);
 }
 
+// Parallelepiped cells (imcon 3): the minimum image of p - q for points as
+// float hi/lo pairs.  images (utility_pack.f:1697-1902, imcon 3) takes the
+// fractional difference s = rcell d, removes nint(s) and goes back through
+// the cell; here the same image, the integer cell translation n =
+// nint(rcell d), is taken off as d - cell n with the cell edges as hi/lo
+// pairs and exact products, so the difference keeps the accuracy of its
+// hi/lo inputs (the FP32 rounding of rcell d only matters for points half
+// a cell apart, far beyond any cutoff).
+__device__ __forceinline__ void mi_tric_df(const SysDev &S, const float *ph, const float *pl,
+                                           const float *qh, const float *ql, float *dh,
+                                           float *dl) {
+  float d0[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) d0[j] = (ph[j] - qh[j]) + (pl[j] - ql[j]);
+  float n[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    n[k] = rintf(fmaf(S.rcellh[k], d0[0], fmaf(S.rcellh[k + 3], d0[1], S.rcellh[k + 6] * d0[2])));
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    float th = 0.f, tl = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (n[k] != 0.f) {
+        const float c = S.cellh[j + 3 * k];
+        const float p = n[k] * c;
+        const float pe = fmaf(n[k], c, -p) + n[k] * S.celll[j + 3 * k];
+        float s, e;
+        two_sum_f(th, p, s, e);
+        th = s;
+        tl += e + pe;
+      }
+    }
+    float s1, e1, s2, e2;
+    two_sum_f(ph[j], -qh[j], s1, e1);
+    two_sum_f(s1, -th, s2, e2);
+    dh[j] = s2;
+    dl[j] = (e1 + e2) + ((pl[j] - ql[j]) - tl);
+  }
+}
+
+// Plain FP32 minimum image of a difference vector in a parallelepiped cell
+// (prefilters: accurate to about 1e-6 A), r^2.
+__device__ __forceinline__ float tric_r2_f32(const SysDev &S, float dx, float dy, float dz) {
+  float n[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    n[k] = rintf(fmaf(S.rcellh[k], dx, fmaf(S.rcellh[k + 3], dy, S.rcellh[k + 6] * dz)));
+  const float *c = S.cellh;
+  dx -= fmaf(c[0], n[0], fmaf(c[3], n[1], c[6] * n[2]));
+  dy -= fmaf(c[1], n[0], fmaf(c[4], n[1], c[7] * n[2]));
+  dz -= fmaf(c[2], n[0], fmaf(c[5], n[1], c[8] * n[2]));
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// The same as one float per axis, and r^2.
+__device__ __forceinline__ float mi_tric_r2(const SysDev &S, const float *ph, const float *pl,
+                                            const float *qh, const float *ql) {
+  float dh[3], dl[3];
+  mi_tric_df(S, ph, pl, qh, ql, dh, dl);
+  const float x = dh[0] + dl[0], y = dh[1] + dl[1], z = dh[2] + dl[2];
+  return fmaf(x, x, fmaf(y, y, z * z));
+}
+
 __device__ __forceinline__ int image_of(int ic, int n) {
   return (ic >= 0) ? ic / n : -((-ic + n - 1) / n);
 }
@@ -249,12 +313,14 @@ __device__ __forceinline__ int image_of(int ic, int n) {
 template <bool F32>
 __device__ void build_segments(const SysDev &S, EvalSmem<F32> &sm, const float *c, float R,
                                int &st) {
-  if (!S.use_cells) {
+  if (!S.use_cells) {  // every framework atom, this CTA's share of a cluster
     if (threadIdx.x == 0) {
-      sm.seg_start[0] = 0;
+      int a0, a1;
+      share_of(S.nfw, sm.rank, sm.csize, a0, a1);
+      sm.seg_start[0] = a0;
       sm.seg_shift[0] = (2) | (2 << 4) | (2 << 8);
       sm.seg_pref[0] = 0;
-      sm.seg_pref[1] = S.nfw;
+      sm.seg_pref[1] = a1 - a0;
       sm.nslots = 1;
     }
     __syncthreads();
@@ -390,6 +456,34 @@ __device__ __forceinline__ void scan_framework(const SysDev &S, EvalSmem<F32> &s
     }
     acc.e2fw.add(e2);
     acc.vdwfw.add(vdw);
+  } else if (!S.use_cells) {
+    // parallelepiped cell: every atom of this CTA's share, minimum image
+    // through the cell translation (mi_tric_df)
+    float vdw = 0.0f;
+    int cnt = 0;
+    const int a0 = sm.seg_start[0];
+    for (int t = t0 + threadIdx.x; t < total; t += kThreads) {
+      const int a = a0 + t;
+      const float4 H = __ldg(S.fwhi + a), Lo = __ldg(S.fwlo + a);
+      const int tb = __ldg(S.fwtype + a);
+      const float ah[3] = {H.x, H.y, H.z}, al[3] = {Lo.x, Lo.y, Lo.z};
+#pragma unroll
+      for (int k = 0; k < (NS > 0 ? NS : ns); ++k) {
+        float dh[3], dl[3];
+        mi_tric_df(S, sm.phi[pos][k], sm.plo[pos][k], ah, al, dh, dl);
+        const float dx = dh[0] + dl[0], dy = dh[1] + dl[1], dz = dh[2] + dl[2];
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const bool near = vdw_is_near(S, si[k], tb, r2);
+        pair_term32(S, si[k], H.w, Lo.w, tb, 1, r2, acc.e2fw, vdw, ov, sf, st, near);
+        if (near) acc.vdwfw.add_df(vdw_near_df(S, si[k], tb, dh, dl, st));
+      }
+      if (++cnt == 8) {
+        acc.vdwfw.add(vdw);
+        vdw = 0.0f;
+        cnt = 0;
+      }
+    }
+    acc.vdwfw.add(vdw);
   } else {
     float vdw = 0.0f;
     int cnt = 0;
@@ -474,10 +568,14 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
         float4 q0 = gh[(size_t)slot * kMaxS];
         float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y,
               dz = sm.phi[pos][0][2] - q0.z;
-        dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
-        dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
-        dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+        if (S.use_cells) {
+          dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
+          dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
+          dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+          if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+        } else if (tric_r2_f32(S, dx, dy, dz) > pre2) {
+          continue;
+        }
         float vdw = 0.f;
         for (int b = 0; b < G2.ns; ++b) {
           float4 qh = gh[(size_t)slot * kMaxS + b];
@@ -485,24 +583,34 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
           int tb = G2.type[b];
 #pragma unroll
           for (int k = 0; k < (NS > 0 ? NS : ns); ++k) {
-            float ex = mi_diff32(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
-                                 S.boxl[0], S.rboxf[0]);
-            float ey = mi_diff32(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
-                                 S.boxl[1], S.rboxf[1]);
-            float ez = mi_diff32(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2],
-                                 S.boxl[2], S.rboxf[2]);
+            float dh[3], dl[3], ex, ey, ez;
+            if (S.use_cells) {
+              ex = mi_diff32(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
+                             S.boxl[0], S.rboxf[0]);
+              ey = mi_diff32(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
+                             S.boxl[1], S.rboxf[1]);
+              ez = mi_diff32(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2],
+                             S.boxl[2], S.rboxf[2]);
+            } else {  // parallelepiped cell
+              const float qa[3] = {qh.x, qh.y, qh.z}, qb[3] = {ql.x, ql.y, ql.z};
+              mi_tric_df(S, sm.phi[pos][k], sm.plo[pos][k], qa, qb, dh, dl);
+              ex = dh[0] + dl[0];
+              ey = dh[1] + dl[1];
+              ez = dh[2] + dl[2];
+            }
             float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
             const bool near = vdw_is_near(S, si[k], tb, r2);
             pair_term32(S, si[k], qh.w, ql.w, tb, G2.frz[b], r2, acc.e2g[g2], vdw, ov, sf, st,
                         near);
             if (near) {
-              float dh[3], dl[3];
-              mi_diff_df(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0], S.boxl[0],
-                         S.rboxf[0], dh[0], dl[0]);
-              mi_diff_df(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1], S.boxl[1],
-                         S.rboxf[1], dh[1], dl[1]);
-              mi_diff_df(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2], S.boxl[2],
-                         S.rboxf[2], dh[2], dl[2]);
+              if (S.use_cells) {
+                mi_diff_df(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
+                           S.boxl[0], S.rboxf[0], dh[0], dl[0]);
+                mi_diff_df(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
+                           S.boxl[1], S.rboxf[1], dh[1], dl[1]);
+                mi_diff_df(sm.phi[pos][k][2], sm.plo[pos][k][2], qh.z, ql.z, S.boxh[2],
+                           S.boxl[2], S.rboxf[2], dh[2], dl[2]);
+              }
               acc.vdwg[g2].add_df(vdw_near_df(S, si[k], tb, dh, dl, st));
             }
           }
@@ -581,10 +689,27 @@ __device__ void build_powers(const SysDev &S, EvalSmem<F32> &sm, int npos, int n
     int nf = npos * ns * 3;
     if (threadIdx.x < nf) {
       int pos = threadIdx.x / (ns * 3), rem = threadIdx.x % (ns * 3), s = rem / 3, d = rem % 3;
-      const float xh = sm.phi[pos][s][d], xl = sm.plo[pos][s][d];
-      const float rh = S.rboxf[d], rl = S.rboxf_lo[d];
-      const float fh = xh * rh;
-      const float fe = fmaf(xh, rh, -fh) + fmaf(xh, rl, xl * rh);
+      float fh, fe;
+      if (S.use_cells) {
+        const float xh = sm.phi[pos][s][d], xl = sm.plo[pos][s][d];
+        const float rh = S.rboxf[d], rl = S.rboxf_lo[d];
+        fh = xh * rh;
+        fe = fmaf(xh, rh, -fh) + fmaf(xh, rl, xl * rh);
+      } else {  // parallelepiped: rcell row d times the position, double-float
+        fh = 0.f;
+        fe = 0.f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float xh = sm.phi[pos][s][j], xl = sm.plo[pos][s][j];
+          const float rh = S.rcellh[d + 3 * j], rl = S.rcelll[d + 3 * j];
+          const float p = xh * rh;
+          const float pe = fmaf(xh, rh, -p) + fmaf(xh, rl, xl * rh);
+          float t, e;
+          two_sum_f(fh, p, t, e);
+          fh = t;
+          fe += e + pe;
+        }
+      }
       float s0, e0, hi, lo;
       two_sum_f(fh, -floorf(fh), s0, e0);
       two_sum_f(s0, e0 + fe, hi, lo);

@@ -229,6 +229,10 @@ void build_device_system(const System &s, DevSystem &D) {
   for (int i = 0; i < 9; ++i) {
     d.cell[i] = s.cell[i];
     d.rcell[i] = s.rcell[i];
+    d.cellh[i] = (float)s.cell[i];
+    d.celll[i] = (float)(s.cell[i] - (double)d.cellh[i]);
+    d.rcellh[i] = (float)s.rcell[i];
+    d.rcelll[i] = (float)(s.rcell[i] - (double)d.rcellh[i]);
   }
   d.box[0] = s.cell[0];
   d.box[1] = s.cell[4];
@@ -861,8 +865,6 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   int nkmax = 1, maxmls = 1;
   for (int i = 0; i < nsys; ++i) {
     if (!systems[i]) raise(FMC_ERR_ARG, "null system");
-    if (precision == FMC_PREC_FP32 && systems[i]->imcon == 3)
-      raise(FMC_ERR_INPUT, "the FP32 path supports orthorhombic cells (imcon 1, 2)");
     auto D = std::make_unique<DevSystem>();
     build_device_system(*systems[i], *D);
     nkmax = std::max(nkmax, std::max(1, (systems[i]->newld + kKT - 1) / kKT) * kKT);
@@ -979,7 +981,10 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
   // guests resident in shared memory during a launch (FP32, one guest type,
   // capacity x sites within the shared array); the per-move ABI keeps them
   // in global memory (its launches are single moves)
-  CA.resident = (precision == FMC_PREC_FP32 && ngmax == 1 && cap * nsmax <= kGuestSmem) ? 1 : 0;
+  bool tric = false;  // parallelepiped cells take the global guest arrays
+  for (int i = 0; i < nsys; ++i) tric = tric || systems[i]->imcon == 3;
+  CA.resident =
+      (precision == FMC_PREC_FP32 && ngmax == 1 && cap * nsmax <= kGuestSmem && !tric) ? 1 : 0;
   CA.spec_max = 0;  // speculative rounds off unless asked for (fmc_batch_set_speculation)
   cudaError_t e;
   if (precision == FMC_PREC_FP32 && C.gn == 1) e = set_chain_smem<true, 1>(C.smem);

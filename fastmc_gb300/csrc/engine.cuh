@@ -584,6 +584,30 @@ __device__ __forceinline__ void quat_f32(const float *dr, float scale, float *q)
   q[3] = sn * (b3 * rn);
 }
 
+// Parallelepiped cell, FP32 path: coordinate d of cell . u (u fractional,
+// three values) as a hi/lo pair, exact products summed without loss.
+__device__ __forceinline__ void cart_tric(const SysDev &S, const float *u, int d, float &h,
+                                          float &l) {
+  h = 0.f;
+  l = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float c = S.cellh[d + 3 * k];
+    const float p = u[k] * c;
+    const float pe = fmaf(u[k], c, -p) + u[k] * S.celll[d + 3 * k];
+    float t, e;
+    two_sum_f(h, p, t, e);
+    h = t;
+    l += e + pe;
+  }
+}
+
+// Coordinate d of cell . n for whole cell translations n (a hi/lo pair).
+__device__ __forceinline__ void cell_shift(const SysDev &S, const float *n, int d, float &h,
+                                           float &l) {
+  cart_tric(S, n, d, h, l);
+}
+
 // FP32 path, moves drawn on the device, first pass: geometry_warp's
 // construction in plain FP32 arithmetic on hi/lo positions (good to about
 // 1e-7 A), for the overlap test that ends most trial moves.  A move that
@@ -613,8 +637,13 @@ __device__ void geometry_f32_core(const BlockShared<F32> &B, const ChainArrays &
     const float *t = G.tmplf[s];
     const float v = row[0] * t[0] + row[1] * t[1] + row[2] * t[2];
     const float u = draws[d];
-    const float ch = __fmul_rn(u, Lh);
-    const float cl = fmaf(u, Lh, -ch) + u * Ll;
+    float ch, cl;
+    if (S.use_cells) {
+      ch = __fmul_rn(u, Lh);
+      cl = fmaf(u, Lh, -ch) + u * Ll;
+    } else {
+      cart_tric(S, draws, d, ch, cl);
+    }
     two_sum_f(ch, v, ph, e);
     pl = cl + e;
   } else {
@@ -643,7 +672,14 @@ __device__ void geometry_f32_core(const BlockShared<F32> &B, const ChainArrays &
         float cof = 0.f;
         for (int s2 = 0; s2 < ns; ++s2) cof += __shfl_sync(full, off, 3 * s2 + d);
         const float u = draws[d];
-        sh = (__fmul_rn(u, Lh) - p0h) + ((fmaf(u, Lh, -__fmul_rn(u, Lh)) + u * Ll) - p0l) - cof;
+        float ch, cl;
+        if (S.use_cells) {
+          ch = __fmul_rn(u, Lh);
+          cl = fmaf(u, Lh, -ch) + u * Ll;
+        } else {
+          cart_tric(S, draws, d, ch, cl);
+        }
+        sh = (ch - p0h) + (cl - p0l) - cof;
       } else if (kind != 5) {
         sh = __fmul_rn(2.0f * draws[d] - 1.0f, stepf[0]);
       }
@@ -658,15 +694,34 @@ __device__ void geometry_f32_core(const BlockShared<F32> &B, const ChainArrays &
       two_sum_f(s0h, cof, cmh, e);
       cml = s0l + e;
       // wrap the centre into the cell by whole edges (translate)
-      const float k = floorf((cmh + cml) * S.rboxf[d]);
-      if (k != 0.0f) {
-        float t;
-        two_sum_f(ph, -k * Lh, t, e);
-        ph = t;
-        pl += e - k * Ll;
-        two_sum_f(cmh, -k * Lh, t, e);
-        cmh = t;
-        cml += e - k * Ll;
+      if (S.use_cells) {
+        const float k = floorf((cmh + cml) * S.rboxf[d]);
+        if (k != 0.0f) {
+          float t;
+          two_sum_f(ph, -k * Lh, t, e);
+          ph = t;
+          pl += e - k * Ll;
+          two_sum_f(cmh, -k * Lh, t, e);
+          cmh = t;
+          cml += e - k * Ll;
+        }
+      } else {  // parallelepiped: whole cell translations of the fractional centre
+        float c3[3], n[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) c3[j] = __shfl_sync(full, cmh + cml, j);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          n[k] = floorf(fmaf(S.rcellh[k], c3[0], fmaf(S.rcellh[k + 3], c3[1], S.rcellh[k + 6] * c3[2])));
+        if (n[0] != 0.f || n[1] != 0.f || n[2] != 0.f) {
+          float th, tl, t;
+          cell_shift(S, n, d, th, tl);
+          two_sum_f(ph, -th, t, e);
+          ph = t;
+          pl += e - tl;
+          two_sum_f(cmh, -th, t, e);
+          cmh = t;
+          cml += e - tl;
+        }
       }
       if (kind == 6 || draws[3] >= 0.0f) {  // rotation about the wrapped centre
         float q[4] = {0.f, 0.f, 0.f, 0.f};  // "move translate": q = 0, Q = -I
@@ -815,7 +870,12 @@ __device__ __noinline__ void refine_geometry(BlockShared<F32> &B, const ChainArr
     quat_df(B.draws, free_rot ? F2{1.0f, 0.0f} : F2{B.stepf[2], B.stepf[3]}, B.trig, q);
   F2 row[3];
   if (rot) qrow_df(q, d, row);
-  auto cart = [&]() {  // the drawn point u * L, u = draws[d]
+  auto cart = [&]() {  // the drawn point u * L (cell . u), u = draws[0..2]
+    if (!S.use_cells) {
+      float h, l;
+      cart_tric(S, B.draws, d, h, l);
+      return f2_norm(h, l);
+    }
     const float u = B.draws[d];
     const float ch = __fmul_rn(u, L.h);
     return f2_norm(ch, fmaf(u, L.h, -ch) + __fmul_rn(u, L.l));
@@ -847,11 +907,28 @@ __device__ __noinline__ void refine_geometry(BlockShared<F32> &B, const ChainArr
     }
     p = f2_add(o, a);
     F2 c = com(p);
-    const float k = floorf(c.h * S.rboxf[d]);  // wrap the centre into the cell
-    if (k != 0.0f) {
-      const F2 kL = f2_mulf(L, k);
-      p = f2_sub(p, kL);
-      c = f2_sub(c, kL);
+    if (S.use_cells) {
+      const float k = floorf(c.h * S.rboxf[d]);  // wrap the centre into the cell
+      if (k != 0.0f) {
+        const F2 kL = f2_mulf(L, k);
+        p = f2_sub(p, kL);
+        c = f2_sub(c, kL);
+      }
+    } else {  // parallelepiped: whole cell translations of the fractional centre
+      const unsigned full = 0xffffffffu;
+      float c3[3], n[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) c3[j] = __shfl_sync(full, c.h + c.l, j);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        n[k] = floorf(fmaf(S.rcellh[k], c3[0], fmaf(S.rcellh[k + 3], c3[1], S.rcellh[k + 6] * c3[2])));
+      if (n[0] != 0.f || n[1] != 0.f || n[2] != 0.f) {
+        float th, tl;
+        cell_shift(S, n, d, th, tl);
+        const F2 t = f2_norm(th, tl);
+        p = f2_sub(p, t);
+        c = f2_sub(c, t);
+      }
     }
     if (rot) p = f2_add(c, rotate(f2_sub(p, c)));
   }
@@ -1024,6 +1101,13 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
         }
       }
     }
+  } else if (F32) {  // parallelepiped cell, FP32 path: every framework atom
+    for (int t = threadIdx.x; t < ns * S.nfw && !hit; t += kThreads) {
+      const int s = t / S.nfw, a = t % S.nfw;
+      const float4 H = __ldg(S.fwhi + a), L = __ldg(S.fwlo + a);
+      const float ah[3] = {H.x, H.y, H.z}, al[3] = {L.x, L.y, L.z};
+      if (mi_tric_r2(S, ev.phi[0][s], ev.plo[0][s], ah, al) < S.overlap_sqf) hit = 1;
+    }
   } else {
     for (int t = threadIdx.x; t < ns * S.nfw && !hit; t += kThreads) {
       int s = t / S.nfw, a = t % S.nfw;
@@ -1087,17 +1171,28 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
         if (g2 == mc.g && slot == mc.slot) continue;
         float4 q0 = gh[(size_t)slot * kMaxS];
         float dx = ev.phi[0][0][0] - q0.x, dy = ev.phi[0][0][1] - q0.y, dz = ev.phi[0][0][2] - q0.z;
-        dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
-        dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
-        dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
-        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+        if (S.use_cells) {
+          dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
+          dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
+          dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+          if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
+        } else if (tric_r2_f32(S, dx, dy, dz) > pre2) {
+          continue;
+        }
         for (int b = 0; b < G2.ns; ++b) {
           float4 qh = gh[(size_t)slot * kMaxS + b], ql = gl[(size_t)slot * kMaxS + b];
           for (int s = 0; s < ns; ++s) {
-            float ex = mi_diff32(ev.phi[0][s][0], ev.plo[0][s][0], qh.x, ql.x, S.boxh[0], S.boxl[0], S.rboxf[0]);
-            float ey = mi_diff32(ev.phi[0][s][1], ev.plo[0][s][1], qh.y, ql.y, S.boxh[1], S.boxl[1], S.rboxf[1]);
-            float ez = mi_diff32(ev.phi[0][s][2], ev.plo[0][s][2], qh.z, ql.z, S.boxh[2], S.boxl[2], S.rboxf[2]);
-            if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < S.overlap_sqf) hit = 1;
+            float r2;
+            if (S.use_cells) {
+              float ex = mi_diff32(ev.phi[0][s][0], ev.plo[0][s][0], qh.x, ql.x, S.boxh[0], S.boxl[0], S.rboxf[0]);
+              float ey = mi_diff32(ev.phi[0][s][1], ev.plo[0][s][1], qh.y, ql.y, S.boxh[1], S.boxl[1], S.rboxf[1]);
+              float ez = mi_diff32(ev.phi[0][s][2], ev.plo[0][s][2], qh.z, ql.z, S.boxh[2], S.boxl[2], S.rboxf[2]);
+              r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+            } else {
+              const float qa[3] = {qh.x, qh.y, qh.z}, qb[3] = {ql.x, ql.y, ql.z};
+              r2 = mi_tric_r2(S, ev.phi[0][s], ev.plo[0][s], qa, qb);
+            }
+            if (r2 < S.overlap_sqf) hit = 1;
           }
         }
       }
@@ -1681,7 +1776,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
                              CA.ord + (size_t)chain * kMaxG * CA.cap};
     if constexpr (F32 && GN == 1) {
       if (CA.resident) listed = list_near_guests(B, rs, p, mc.slot, B.ev.rmx[p]);
-      else listed = list_near_guests(B, gsites, p, mc.slot, B.ev.rmx[p]);
+      else if (S.use_cells) listed = list_near_guests(B, gsites, p, mc.slot, B.ev.rmx[p]);
     }
     FMC_PHASE_SYNC(B, 2);
     scan_framework<F32, NS>(S, B.ev, p, ns, B.si, A, ovd, sfp, st);

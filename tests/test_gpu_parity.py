@@ -532,16 +532,19 @@ def test_gpu_calf20_per_move_fp64(fmc_lib, oracle_lib):
     assert np.allclose(sg, so, rtol=1e-10, atol=1e-10 * np.abs(so).max())
 
 
-def test_gpu_calf20_chain_fp64(fmc_lib, oracle_lib):
+@pytest.mark.parametrize("csize", [1, 2])
+def test_gpu_calf20_chain_fp64(fmc_lib, oracle_lib, csize):
     """A device-resident FP64 chain on CALF-20 with the test's CONTROL (CO2
     and N2, insert / delete / displace, probability grids) follows the
-    oracle move by move on the parallelepiped cell."""
+    oracle move by move on the parallelepiped cell, on one CTA and on a
+    2-CTA cluster (each CTA scans its share of the framework atoms)."""
     n = 3000
     o = oracle_lib.Oracle(CALF20)
     o.seed(12345)
     ref = o.run(n)
     b = fmc_lib.Batch([fmc_lib.System.load(CALF20)], [{"seed": 12345}],
                       precision=fmc_lib.FMC_PREC_FP64, guest_capacity=64)
+    b.set_cluster([csize])
     b.set_log(n)
     b.run(n)
     got = b.log(0, n)
@@ -557,6 +560,89 @@ def test_gpu_calf20_chain_fp64(fmc_lib, oracle_lib):
     assert nacc >= 50 and nfull >= 200
     st = b.stats()[0]
     assert st.nummols == o.nummols(o.locguest(1))
+
+
+def test_gpu_calf20_per_move_fp32(fmc_lib, oracle_lib):
+    """The FP32 path on CALF-20's parallelepiped cell (minimum images through
+    whole cell translations taken off in hi/lo pairs, fractional coordinates
+    in double-float): insertion, deletion and displacement estep against the
+    oracle to 1e-6 of max(|estep|, the molecule's energy, 1 kcal/mol), the
+    same overlap outcomes, and S(k) after the commits."""
+    o = oracle_lib.Oracle(CALF20)
+    sysm = fmc_lib.System.load(CALF20)
+    plain = fmc_lib.PlainEngine(sysm, fmc_lib.FMC_PREC_FP32, 64)
+    pos = _calf20_positions(o, 16, seed=3)
+    inserted = 0
+    for xyz in pos:
+        ref = o.insertion_energy(1, xyz)
+        got = plain.insertion(1, xyz)
+        assert got["overlap"] == ref["overlap"]
+        if not ref["overlap"]:
+            assert abs(got["estep"] - ref["estep"]) <= 1e-6 * max(abs(ref["estep"]), 1.0)
+        ok = not ref["overlap"]
+        assert plain.commit(0.0) == ok
+        o.apply_move(1, 1, 0, xyz, ok)
+        inserted += ok
+        if inserted == 10:
+            break
+    assert inserted >= 8
+    eown = {}
+    for c in range(1, inserted + 1):
+        ref = o.deletion_energy(1, c)
+        eown[c] = abs(ref["estep"])
+        got = plain.deletion(1, c)
+        assert abs(got["estep"] - ref["estep"]) <= 1e-6 * max(abs(ref["estep"]), 1.0)
+    rng = np.random.default_rng(8)
+    nd = 0
+    for _ in range(40):
+        c = int(rng.integers(1, inserted + 1))
+        th = rng.uniform(0, 0.8)
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        abcq = [*rng.uniform(-0.4, 0.4, 3), math.cos(th / 2), *(math.sin(th / 2) * ax)]
+        ref = o.displace_energy(1, c, abcq)
+        got = plain.displace(1, c, abcq)
+        assert got["overlap"] == ref["overlap"]
+        if not ref["overlap"]:
+            tol = 1e-6 * max(abs(ref["estep"]), eown[c], 1.0)
+            assert abs(got["estep"] - ref["estep"]) <= tol, (c, got["estep"], ref["estep"])
+            nd += 1
+    assert nd >= 10
+    plain.deletion(1, 2)
+    plain.commit(0.0)
+    o.apply_move(2, 1, 2, None, True)
+    sg, so = plain.sk(), o.sk()
+    assert np.allclose(sg, so, rtol=0, atol=2e-6 * np.abs(so).max())
+
+
+@pytest.mark.parametrize("csize", [1, 2])
+def test_gpu_calf20_all_moves_fp32(fmc_lib, oracle_lib, csize):
+    """The reference's own test input unchanged (CALF-20, parallelepiped
+    cell; CO2 and N2; insert / delete / displace / swap / switch / jump) in
+    a batched FP32 chain, on one CTA and on a 2-CTA cluster: the chain
+    follows the oracle move by move until its first decision at a
+    threshold (estep to 2e-6 of max(|estep|, 30 kcal/mol), swaps to 1e-5
+    of max(|estep|, 100)), over at least 500 moves."""
+    import shutil
+    import tempfile
+    n = 3000
+    with tempfile.TemporaryDirectory() as d:
+        for f in ("CONFIG", "FIELD"):
+            shutil.copy(os.path.join(CALF20, f), d)
+        shutil.copy(os.path.join(CALF20, "CONTROL_all_moves"), os.path.join(d, "CONTROL"))
+        o = oracle_lib.Oracle(d)
+        o.seed(31)
+        ref = o.run(n)
+        b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 31}],
+                          precision=fmc_lib.FMC_PREC_FP32, guest_capacity=64)
+        b.set_cluster([csize])
+        b.set_log(n)
+        b.run(n)
+        got = b.log(0, n)
+    assert all(s.status == 0 for s in b.stats())
+    _, ncmp = _follow(got, ref, "fp32", (7,), 1e-5)
+    kinds = {r.move for r in ref[:ncmp]}
+    assert ncmp >= 500 and {1, 2, 3, 6, 7} <= kinds, (ncmp, kinds)
 
 
 def test_gpu_window_statistics_two_guests_fp64(fmc_lib, oracle_lib, inputs_dir):
@@ -609,12 +695,15 @@ def _follow(got, ref, prec, kinds, tol_kind):
     difference; measured at most 5.4e-5 kcal/mol on identical states), moves
     of the given kinds to tol_kind of max(|estep|, 100) (they add energies
     of several molecules).  The given kinds' estep is compared also when
-    they overlapped.  Returns the number of the given kinds compared."""
+    they overlapped.  Returns the number of the given kinds compared and
+    the number of moves compared."""
     nk = 0
+    ncmp = 0
     for i, (g, r) in enumerate(zip(got, ref)):
         assert (g.move, g.iguest, g.choice) == (r.move, r.iguest, r.choice), i
         if prec == "fp32" and (g.overlap != r.overlap or g.accepted != r.accepted):
             break
+        ncmp += 1
         assert (g.overlap, g.accepted) == (r.overlap, r.accepted), i
         if prec == "fp64":
             assert g.rande == r.rande, i
@@ -626,7 +715,7 @@ def _follow(got, ref, prec, kinds, tol_kind):
         elif not r.overlap:
             tol = 1e-9 * max(abs(r.estep), 1.0) if prec == "fp64" else 2e-6 * max(abs(r.estep), 30.0)
             assert abs(g.estep - r.estep) <= tol, (i, g.estep, r.estep)
-    return nk
+    return nk, ncmp
 
 
 def _final_state(b, o, types):
@@ -668,7 +757,7 @@ def test_gpu_chain_swaps_follow_oracle(fmc_lib, oracle_lib, tmp_path, prec):
     got = b.log(0, n)
     swaps = [r for r in ref if r.move == 7]
     assert len(swaps) >= 250 and sum(r.accepted for r in swaps) >= 2
-    nsw = _follow(got, ref, prec, (7,), 1e-5)
+    nsw, _ = _follow(got, ref, prec, (7,), 1e-5)
     assert nsw >= 50
     if prec == "fp64":
         st = b.stats()[0]
@@ -705,7 +794,7 @@ def test_gpu_chain_switch_follows_oracle(fmc_lib, oracle_lib, tmp_path, prec):
     got = b.log(0, n)
     sw = [r for r in ref if r.move == 8]
     assert len(sw) >= 400 and sum(r.accepted for r in sw) >= 10 and sum(r.overlap for r in sw) >= 30
-    nsw = _follow(got, ref, prec, (8,), 1e-5)
+    nsw, _ = _follow(got, ref, prec, (8,), 1e-5)
     assert nsw >= 50
     if prec == "fp64":
         st = b.stats()[0]
