@@ -686,6 +686,8 @@ def profile_case(args):
     prec = F.FMC_PREC_FP64 if args.fp64 else F.FMC_PREC_FP32
     b = F.Batch([sysm], specs, precision=prec, guest_capacity=1024)
     b.set_cluster([args.cluster])
+    if args.speculate and not args.fp64:
+        b.set_speculation(args.speculate)
     for it in range(args.launches):
         st = b.run(args.moves)
         ms, ev, mv = b.last_timing()
@@ -705,8 +707,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
     ap.add_argument("--widom", action="store_true", help="also time config 5's 1e7 Widom trials")
-    ap.add_argument("--speculate", type=int, default=0,
-                    help="speculative proposals per round at most (2..8; 0: off)")
+    ap.add_argument("--speculate", type=int, default=8,
+                    help="speculative proposals per round at most (2..8; 0: off); the chains' "
+                         "moves are the same either way")
     ap.add_argument("--chain-clusters", default="", help="CTAs per chain, one value per chain")
     ap.add_argument("--clusters", default="", help="CTAs per chain per framework, e.g. 1,2,2,4 "
                     "(default: autotuned)")
