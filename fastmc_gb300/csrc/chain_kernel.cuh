@@ -143,7 +143,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     // speculative rounds of up to kspec proposals where they apply; kspec
     // doubles after a round of exits only and halves after a round whose
     // first proposal passed (every thread computes the same value)
-    const bool spec = speculation_applies(B, CA);
+    // (one guest type only: compiled into the single-type kernel alone)
+    const bool spec = GN == 1 && speculation_applies(B, CA);
     const int kcap = min(CA.spec_max, kMaxSpec);
     int kspec = 2;
     for (int it = 0; it < nmoves; ++it) {
@@ -151,7 +152,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (threadIdx.x == 32) run_deferred<F32, GN>(B);
       if (spec) {
         const int kwin = min(kspec, nmoves - it);
-        const int exits = spec_round(B, CA, chain, kwin, logs, logcap, rank);
+        int exits = 0;
+        if constexpr (GN == 1)
+          exits = spec_round<F32, kTricOk<F32, GN>>(B, CA, chain, kwin, logs, logcap, rank);
         it += exits;
         if (!B.spec_have) kspec = min(2 * kspec, kcap);
         else if (exits == 0) kspec = max(1, kspec / 2);
@@ -160,12 +163,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           continue;
         }
       } else {
-        propose(B, CA, chain, kPropMC, 0);
+        propose<F32, kTricOk<F32, GN>>(B, CA, chain, kPropMC, 0);
       }
       FMC_PHASE(B, 0);
       if (B.mc.kind >= 7) {  // mc_swap / the acting mc_switch: evaluations, decision, commits or rollback, statistics
-        if (B.mc.kind == 7) swap_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);
-        else switch_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);
+        // (two or more guest types: not compiled into the single-type kernel,
+        // whose systems cannot draw them)
+        if constexpr (GN > 1) {
+          if (B.mc.kind == 7) swap_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);
+          else switch_move<F32, GN>(B, CA, chain, st, logs, logcap, rank);
+        } else {
+          st |= kStBadChoice;
+        }
         if (B.S.prob_nsub > 0 && CA.grid && B.H.production) store_prob(B, CA, chain);
         __syncthreads();
         continue;
@@ -224,7 +233,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           st |= kStCapacity;
           break;
         }
-        propose(B, CA, chain, kPropInsert, g);
+        propose<F32, kTricOk<F32, GN>>(B, CA, chain, kPropInsert, g);
         evaluate_rare<F32, GN>(B, CA, chain, st);
         if (threadIdx.x == 0) B.mc.accepted = B.mc.overlap ? 0 : 1;
         __syncthreads();
@@ -236,7 +245,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (mode == kModeEval) {
     if (threadIdx.x == 0) B.mc = gctx[chain];
     __syncthreads();
-    propose(B, CA, chain, kPropExternal, 0);
+    propose<F32, kTricOk<F32, GN>>(B, CA, chain, kPropExternal, 0);
     int full = 0;
     if (B.mc.kind != 0) full = evaluate_any<F32, GN>(B, CA, chain, st);
     if (threadIdx.x == 0) {

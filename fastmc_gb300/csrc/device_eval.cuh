@@ -417,7 +417,7 @@ __device__ __forceinline__ int find_slot(const int *pref, int n, int t) {
 
 // Scan the framework for position `pos` (ns sites).
 // NS > 0: the site count is a compile-time constant (site loops unroll).
-template <bool F32, int NS, class PA>
+template <bool F32, int NS, bool TRIC, class PA>
 __device__ __forceinline__ void scan_framework(const SysDev &S, EvalSmem<F32> &sm, int pos,
                                                int ns_rt, const SiteInfo *si, PA &acc, int &ov,
                                                int &sf, int &st) {
@@ -456,7 +456,7 @@ __device__ __forceinline__ void scan_framework(const SysDev &S, EvalSmem<F32> &s
     }
     acc.e2fw.add(e2);
     acc.vdwfw.add(vdw);
-  } else if (!S.use_cells) {
+  } else if (TRIC && !S.use_cells) {
     // parallelepiped cell: every atom of this CTA's share, minimum image
     // through the cell translation (mi_tric_df)
     float vdw = 0.0f;
@@ -553,6 +553,8 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
     const int *ord = CA.ord + ((size_t)chain * kMaxG + g2) * CA.cap;
     float pre = (float)S.rcut + 2.0f * rmax_self + 2.0f * (float)G2.rmax + 0.01f;
     if constexpr (F32) {
+      // parallelepiped cells only in the multi-type FP32 kernel
+      const bool tric = GN > 1 && !S.use_cells;
       const float4 *gh = CA.ghi + ((size_t)chain * kMaxG + g2) * CA.cap * kMaxS;
       const float4 *gl = CA.glo + ((size_t)chain * kMaxG + g2) * CA.cap * kMaxS;
       float pre2 = pre * pre;
@@ -568,7 +570,7 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
         float4 q0 = gh[(size_t)slot * kMaxS];
         float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y,
               dz = sm.phi[pos][0][2] - q0.z;
-        if (S.use_cells) {
+        if (!tric) {
           dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
           dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
           dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
@@ -584,7 +586,7 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
 #pragma unroll
           for (int k = 0; k < (NS > 0 ? NS : ns); ++k) {
             float dh[3], dl[3], ex, ey, ez;
-            if (S.use_cells) {
+            if (!tric) {
               ex = mi_diff32(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
                              S.boxl[0], S.rboxf[0]);
               ey = mi_diff32(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
@@ -603,7 +605,7 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
             pair_term32(S, si[k], qh.w, ql.w, tb, G2.frz[b], r2, acc.e2g[g2], vdw, ov, sf, st,
                         near);
             if (near) {
-              if (S.use_cells) {
+              if (!tric) {
                 mi_diff_df(sm.phi[pos][k][0], sm.plo[pos][k][0], qh.x, ql.x, S.boxh[0],
                            S.boxl[0], S.rboxf[0], dh[0], dl[0]);
                 mi_diff_df(sm.phi[pos][k][1], sm.plo[pos][k][1], qh.y, ql.y, S.boxh[1],
@@ -679,7 +681,7 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
 // directly for each power j).  FP64 path: sincospi of the reduced phase.
 // FP32 path: the fractional coordinate is split into a float hi/lo pair
 // and j*s is reduced exactly with an FMA before sincospif.
-template <bool F32>
+template <bool F32, bool TRIC>
 __device__ void build_powers(const SysDev &S, EvalSmem<F32> &sm, int npos, int ns) {
   int k1 = S.kmax[0], k2 = S.kmax[1], k3 = S.kmax[2];
   if constexpr (F32) {
@@ -690,7 +692,7 @@ __device__ void build_powers(const SysDev &S, EvalSmem<F32> &sm, int npos, int n
     if (threadIdx.x < nf) {
       int pos = threadIdx.x / (ns * 3), rem = threadIdx.x % (ns * 3), s = rem / 3, d = rem % 3;
       float fh, fe;
-      if (S.use_cells) {
+      if (!TRIC || S.use_cells) {
         const float xh = sm.phi[pos][s][d], xl = sm.plo[pos][s][d];
         const float rh = S.rboxf[d], rl = S.rboxf_lo[d];
         fh = xh * rh;

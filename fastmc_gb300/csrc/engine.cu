@@ -977,12 +977,14 @@ void init_chains(Chains &C, const System *const *systems, int nsys, const fmc_ch
     for (int g = 1; g <= systems[i]->ntpguest; ++g)
       nsmax = std::max(nsmax, systems[i]->mol[systems[i]->locguest[g]].natoms);
   }
-  C.gn = (precision == FMC_PREC_FP32 && ngmax == 1) ? 1 : kMaxG;
+  // parallelepiped cells run on the multi-type FP32 kernel (the single-type
+  // one is built for orthorhombic cells only) with the global guest arrays
+  bool tric = false;
+  for (int i = 0; i < nsys; ++i) tric = tric || systems[i]->imcon == 3;
+  C.gn = (precision == FMC_PREC_FP32 && ngmax == 1 && !tric) ? 1 : kMaxG;
   // guests resident in shared memory during a launch (FP32, one guest type,
   // capacity x sites within the shared array); the per-move ABI keeps them
   // in global memory (its launches are single moves)
-  bool tric = false;  // parallelepiped cells take the global guest arrays
-  for (int i = 0; i < nsys; ++i) tric = tric || systems[i]->imcon == 3;
   CA.resident =
       (precision == FMC_PREC_FP32 && ngmax == 1 && cap * nsmax <= kGuestSmem && !tric) ? 1 : 0;
   CA.spec_max = 0;  // speculative rounds off unless asked for (fmc_batch_set_speculation)

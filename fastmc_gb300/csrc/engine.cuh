@@ -66,6 +66,12 @@ struct LogRec {  // mirrors fmc_move_log
 
 constexpr int kMaxSpec = 8;  // proposals of one speculative round
 
+// Parallelepiped cells (imcon 3) are compiled into the FP64 kernel and the
+// multi-type FP32 kernel; the single-type FP32 kernel (orthorhombic batches)
+// carries no code for them, which keeps its registers for the hot loop.
+template <bool F32, int GN>
+constexpr bool kTricOk = !F32 || GN > 1;
+
 template <bool F32>
 struct BlockShared {
   // FP32 batches of one guest type: every guest site in molecule order as
@@ -616,7 +622,7 @@ __device__ __forceinline__ void cell_shift(const SysDev &S, const float *n, int 
 // coordinate; orthorhombic cells.  Writes position 0 (new) and, for moves
 // of an existing molecule, position 1 (old) into phi/plo; the bounds of
 // each position carry a 1e-3 A margin that covers the refinement.
-template <bool F32>
+template <bool F32, bool TRIC>
 __device__ void geometry_f32_core(const BlockShared<F32> &B, const ChainArrays &CA, int chain,
                                   int kind, int g, int slot, const float *draws, const float *stepf,
                                   int flag2, float (*phi)[kMaxS][3], float (*plo)[kMaxS][3]) {
@@ -638,7 +644,7 @@ __device__ void geometry_f32_core(const BlockShared<F32> &B, const ChainArrays &
     const float v = row[0] * t[0] + row[1] * t[1] + row[2] * t[2];
     const float u = draws[d];
     float ch, cl;
-    if (S.use_cells) {
+    if (!TRIC || S.use_cells) {
       ch = __fmul_rn(u, Lh);
       cl = fmaf(u, Lh, -ch) + u * Ll;
     } else {
@@ -673,7 +679,7 @@ __device__ void geometry_f32_core(const BlockShared<F32> &B, const ChainArrays &
         for (int s2 = 0; s2 < ns; ++s2) cof += __shfl_sync(full, off, 3 * s2 + d);
         const float u = draws[d];
         float ch, cl;
-        if (S.use_cells) {
+        if (!TRIC || S.use_cells) {
           ch = __fmul_rn(u, Lh);
           cl = fmaf(u, Lh, -ch) + u * Ll;
         } else {
@@ -694,7 +700,7 @@ __device__ void geometry_f32_core(const BlockShared<F32> &B, const ChainArrays &
       two_sum_f(s0h, cof, cmh, e);
       cml = s0l + e;
       // wrap the centre into the cell by whole edges (translate)
-      if (S.use_cells) {
+      if (!TRIC || S.use_cells) {
         const float k = floorf((cmh + cml) * S.rboxf[d]);
         if (k != 0.0f) {
           float t;
@@ -772,11 +778,11 @@ __device__ void site_constants_and_bounds(BlockShared<F32> &B) {
 
 // FP32 path, moves drawn on the device: the first-pass geometry of the move
 // in mc (warp 0), then the site constants and position bounds.
-template <bool F32>
+template <bool F32, bool TRIC>
 __device__ void geometry_f32(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   MoveCtx &mc = B.mc;
   if (mc.kind == 0 || mc.kind >= 7) return;  // swap_move / switch_move build their positions
-  geometry_f32_core(B, CA, chain, mc.kind, mc.g, mc.slot, B.draws, B.stepf, B.flags[2], B.ev.phi,
+  geometry_f32_core<F32, TRIC>(B, CA, chain, mc.kind, mc.g, mc.slot, B.draws, B.stepf, B.flags[2], B.ev.phi,
                     B.ev.plo);
   __syncwarp();
   site_constants_and_bounds(B);
@@ -851,7 +857,7 @@ __device__ __forceinline__ void qrow_df(const F2 *q, int d, F2 *row) {
 // relative; this one moves it by ~1e-12.  Warp 0, one lane per site
 // coordinate; the draws, old positions (phi/plo[1]) and step sizes are the
 // first pass's.
-template <bool F32>
+template <bool F32, bool TRIC>
 __device__ __noinline__ void refine_geometry(BlockShared<F32> &B, const ChainArrays &CA) {
   const SysDev &S = B.S;
   const MoveCtx &mc = B.mc;
@@ -871,7 +877,7 @@ __device__ __noinline__ void refine_geometry(BlockShared<F32> &B, const ChainArr
   F2 row[3];
   if (rot) qrow_df(q, d, row);
   auto cart = [&]() {  // the drawn point u * L (cell . u), u = draws[0..2]
-    if (!S.use_cells) {
+    if (TRIC && !S.use_cells) {
       float h, l;
       cart_tric(S, B.draws, d, h, l);
       return f2_norm(h, l);
@@ -907,7 +913,7 @@ __device__ __noinline__ void refine_geometry(BlockShared<F32> &B, const ChainArr
     }
     p = f2_add(o, a);
     F2 c = com(p);
-    if (S.use_cells) {
+    if (!TRIC || S.use_cells) {
       const float k = floorf(c.h * S.rboxf[d]);  // wrap the centre into the cell
       if (k != 0.0f) {
         const F2 kL = f2_mulf(L, k);
@@ -939,7 +945,7 @@ __device__ __noinline__ void refine_geometry(BlockShared<F32> &B, const ChainArr
 }
 
 // Warp 0 proposal for all modes; ends with a block barrier.
-template <bool F32>
+template <bool F32, bool TRIC>
 __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, int mode, int g_forced) {
   if (threadIdx.x < 32) {
     // at least 16 draws in the buffer: a move takes at most 11
@@ -1000,7 +1006,7 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       B.flags[4] = mode == kPropMC ? 1 : 0;  // delE of other molecule types only if accepted
     }
     __syncwarp();
-    if (F32 && mode != kPropExternal) geometry_f32(B, CA, chain);
+    if (F32 && mode != kPropExternal) geometry_f32<F32, TRIC>(B, CA, chain);
     else geometry_warp(B, CA, chain, mode);
   }
   __syncthreads();
@@ -1010,7 +1016,7 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
 // Any framework or guest site within the overlap distance of any site of
 // position 0: the test that lets an insertion or displacement exit before
 // the full sums (insertion / guest_energy, mc_moves.f:217-225, 347-355).
-template <bool F32>
+template <bool F32, bool TRIC>
 __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   const SysDev &S = B.S;
   const MoveCtx &mc = B.mc;
@@ -1101,7 +1107,7 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
         }
       }
     }
-  } else if (F32) {  // parallelepiped cell, FP32 path: every framework atom
+  } else if (F32 && TRIC) {  // parallelepiped cell, FP32 path: every framework atom
     for (int t = threadIdx.x; t < ns * S.nfw && !hit; t += kThreads) {
       const int s = t / S.nfw, a = t % S.nfw;
       const float4 H = __ldg(S.fwhi + a), L = __ldg(S.fwlo + a);
@@ -1171,7 +1177,7 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
         if (g2 == mc.g && slot == mc.slot) continue;
         float4 q0 = gh[(size_t)slot * kMaxS];
         float dx = ev.phi[0][0][0] - q0.x, dy = ev.phi[0][0][1] - q0.y, dz = ev.phi[0][0][2] - q0.z;
-        if (S.use_cells) {
+        if (!TRIC || S.use_cells) {
           dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
           dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
           dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
@@ -1183,7 +1189,7 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
           float4 qh = gh[(size_t)slot * kMaxS + b], ql = gl[(size_t)slot * kMaxS + b];
           for (int s = 0; s < ns; ++s) {
             float r2;
-            if (S.use_cells) {
+            if (!TRIC || S.use_cells) {
               float ex = mi_diff32(ev.phi[0][s][0], ev.plo[0][s][0], qh.x, ql.x, S.boxh[0], S.boxl[0], S.rboxf[0]);
               float ey = mi_diff32(ev.phi[0][s][1], ev.plo[0][s][1], qh.y, ql.y, S.boxh[1], S.boxl[1], S.rboxf[1]);
               float ez = mi_diff32(ev.phi[0][s][2], ev.plo[0][s][2], qh.z, ql.z, S.boxh[2], S.boxl[2], S.rboxf[2]);
@@ -1747,7 +1753,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
   }
   if (mc.kind == 1 || mc.kind >= 3) {
     if (!B.flags[6]) {  // flags[6]: a speculative round found this position clear already
-      const int hit = overlap_check(B, CA, chain);
+      const int hit = overlap_check<F32, kTricOk<F32, GN>>(B, CA, chain);
       FMC_PHASE(B, 1);
       if (hit) {
         if (threadIdx.x == 0) mc.overlap = 1;
@@ -1758,7 +1764,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
     if constexpr (F32) {
       // FP32 first-pass geometry: warp 0 refines it; the positions are
       // next read after build_segments' barriers
-      if (B.flags[3] && threadIdx.x < 32) refine_geometry(B, CA);
+      if (B.flags[3] && threadIdx.x < 32) refine_geometry<F32, kTricOk<F32, GN>>(B, CA);
     }
   }
   PosAcc<F32, GN> acc0, acc1;
@@ -1779,7 +1785,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
       else if (S.use_cells) listed = list_near_guests(B, gsites, p, mc.slot, B.ev.rmx[p]);
     }
     FMC_PHASE_SYNC(B, 2);
-    scan_framework<F32, NS>(S, B.ev, p, ns, B.si, A, ovd, sfp, st);
+    scan_framework<F32, NS, kTricOk<F32, GN>>(S, B.ev, p, ns, B.si, A, ovd, sfp, st);
     bool done = false;
     if constexpr (F32 && GN == 1) {
       if (listed) {
@@ -1802,7 +1808,7 @@ __device__ int evaluate(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
   };
   scan_position(0, acc0, sf0);
   if (npos == 2) scan_position(1, acc1, sf1);
-  build_powers<F32>(S, B.ev, npos, ns);
+  build_powers<F32, kTricOk<F32, GN>>(S, B.ev, npos, ns);
   __syncthreads();
   FMC_PHASE(B, 4);
   kspace<F32, GN, NS>(B, CA, chain, mc.kind == 2, acc0, acc1, st);
@@ -2431,7 +2437,7 @@ __device__ void overlap_batch(BlockShared<F32> &B, int n) {
 // production statistics, log); the first proposal that is not one is left
 // in mc / draws / ev as propose() leaves a move (spec_have = 1), with
 // flags[6] set when its overlap test has passed.  Returns the exits.
-template <bool F32>
+template <bool F32, bool TRIC>
 __device__ int spec_round(BlockShared<F32> &B, const ChainArrays &CA, int chain, int kwin,
                           LogRec *logs, int logcap, int rank) {
   SysDev &S = B.S;
@@ -2487,7 +2493,8 @@ __device__ int spec_round(BlockShared<F32> &B, const ChainArrays &CA, int chain,
     if (w < n) {
       auto &P = B.spec[w];
       if (P.kind != 0)
-        geometry_f32_core(B, CA, chain, P.kind, 0, P.slot, P.draws, P.stepf, P.flag2, P.phi, P.plo);
+        geometry_f32_core<F32, TRIC>(B, CA, chain, P.kind, 0, P.slot, P.draws, P.stepf, P.flag2, P.phi,
+                                     P.plo);
     }
   }
   __syncthreads();
@@ -2735,7 +2742,7 @@ __device__ void swap_move(BlockShared<F32> &B, const ChainArrays &CA, int chain,
   // buffers the two evaluations do not write keep it)
   if constexpr (!F32) sk_pair_copy(B, CA, chain, gi, gj, H.skb, true);
   if (threadIdx.x < 32) {
-    if constexpr (F32) geometry_f32(B, CA, chain);
+    if constexpr (F32) geometry_f32<F32, kTricOk<F32, GN>>(B, CA, chain);
     else geometry_warp(B, CA, chain, kPropMC);
   }
   __syncthreads();
@@ -2890,7 +2897,7 @@ __device__ void switch_move(BlockShared<F32> &B, const ChainArrays &CA, int chai
   // deletion, given in mc.pos for an insertion) and commit it, forced
   auto half = [&](double &acc_estep, bool del) {
     if (del && threadIdx.x < 32) {
-      if constexpr (F32) geometry_f32(B, CA, chain);
+      if constexpr (F32) geometry_f32<F32, kTricOk<F32, GN>>(B, CA, chain);
       else geometry_warp(B, CA, chain, kPropMC);
     }
     __syncthreads();
