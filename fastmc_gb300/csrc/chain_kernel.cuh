@@ -175,7 +175,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         } else {
           st |= kStBadChoice;
         }
-        if (B.S.prob_nsub > 0 && CA.grid && B.H.production) store_prob(B, CA, chain);
+        if (B.S.prob_nsub > 0 && CA.grid && B.H.production) {
+          store_prob(B, CA, chain);
+          if (B.swp.accepted) store_enprob(B, CA, chain, B.mc.g);
+        }
         __syncthreads();
         continue;
       }
@@ -220,7 +223,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       __syncthreads();
       // probability grids after every production move (gcmc.f:1129-1130)
-      if (B.S.prob_nsub > 0 && CA.grid && B.dfr.production) store_prob(B, CA, chain);
+      if (B.S.prob_nsub > 0 && CA.grid && B.dfr.production) {
+        store_prob(B, CA, chain);
+        if (B.mc.accepted) store_enprob(B, CA, chain, B.mc.g);
+      }
       FMC_PHASE_SYNC(B, 11);
     }
     if (threadIdx.x == 32) run_deferred<F32, GN>(B);
@@ -268,6 +274,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         if (wj.estep_out) wj.estep_out[t] = B.mc.overlap ? 0.0 : B.mc.estep;
         if (wj.overlap_out) wj.overlap_out[t] = B.mc.overlap;
+        // the energy probability grid of widom_grid's test insertions
+        // (gcmc.f:2529-2532; not for positions given by the caller)
+        if (!B.mc.overlap && !wj.xyz_in && CA.grid && B.S.prob_nsub > 0) {
+          const double e = B.mc.estep;
+          store_enprob(B, CA, chain, wj.iguest, &e);
+        }
       }
       __syncthreads();
     }

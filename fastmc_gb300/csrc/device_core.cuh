@@ -159,6 +159,8 @@ struct SysDev {
   int ngrid[3];
   double rucell[9];        // inverse of the unit (folding) cell
   int prob_nitem[kMaxG], prob_item0[kMaxG];
+  int prob_eng_sub[kMaxG];         // energy grids: the energy-sum subgrid (the count is the
+                                   // next one), -1 without
   short prob_sub[kMaxProbItems];   // 0-based subgrid
   short prob_site[kMaxProbItems];  // 0: centre of mass, else 1-based site
   // guests

@@ -456,6 +456,7 @@ void build_device_system(const System &s, DevSystem &D) {
     for (int ig = 1; ig <= s.ntpguest; ++ig) {
       d.prob_item0[ig - 1] = nit;
       d.prob_nitem[ig - 1] = 0;
+      d.prob_eng_sub[ig - 1] = -1;
       if (!s.lprob) continue;
       int np = s.nprob[ig];
       if (s.lprobeng[ig]) np -= 2;
@@ -474,7 +475,10 @@ void build_device_system(const System &s, DevSystem &D) {
         }
       }
       itprob += np;
-      if (s.lprobeng[ig]) itprob += 2;
+      if (s.lprobeng[ig]) {  // the guest type's last two grids (storeenprob)
+        itprob += 2;
+        d.prob_eng_sub[ig - 1] = itprob - 2;
+      }
     }
   }
   // framework S(k) (K4)

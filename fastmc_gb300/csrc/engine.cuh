@@ -3113,6 +3113,49 @@ __device__ inline void equitable_bin_dev(double *g, const int *ng, double fa, do
   atomicAdd(g + aridx + bridx + cridx, (ar * br * cr) * val);
 }
 
+// storeenprob (utility_pack.f:550-618) as the main loop calls it after an
+// accepted production move (gcmc.f:1131-1134): with the main program's
+// randchoice and guest_toten, which no move routine sets (theirs are their
+// own variables), so molecule 0 -- newx as the move left it -- and energy 0.
+// The centre of mass of the move's last positions (the guest type's site
+// count and masses), folded into the unit cell, adds 1 to the guest type's
+// count grid; the energy grid gains 0 and is left alone.  Thread 0 of rank
+// 0.  newx is position 0 of the last evaluation: the inserted, deleted or
+// moved molecule, a swap's partner over the deleted molecule's later sites,
+// a switch's first molecule at its new centre, and for a switch that did
+// nothing the previous move's.  widom_grid (gcmc.f:2529-2532) calls it with
+// a test insertion's estep: `energy` adds that to the energy grid too.
+template <bool F32>
+__device__ void store_enprob(BlockShared<F32> &B, const ChainArrays &CA, int chain, int g,
+                             const double *energy = nullptr) {
+  const SysDev &S = B.S;
+  if (threadIdx.x != 0 || B.ev.rank != 0 || S.prob_eng_sub[g] < 0) return;
+  const GuestType &G = S.g[g];
+  double c[3] = {0.0, 0.0, 0.0}, w = 0.0;
+  for (int k = 0; k < G.ns; ++k) {
+    const double m = G.mass[k];
+    w += m;
+    for (int d = 0; d < 3; ++d) {
+      const double x = F32 ? (double)B.ev.phi[0][k][d] + (double)B.ev.plo[0][k][d] : B.mc.pos[0][k][d];
+      c[d] += x * m;
+    }
+  }
+  for (int d = 0; d < 3; ++d) c[d] /= w;
+  const double *r = S.rucell;  // frac2
+  double fx = c[0] * r[0] + c[1] * r[3] + c[2] * r[6];
+  double fy = c[0] * r[1] + c[1] * r[4] + c[2] * r[7];
+  double fz = c[0] * r[2] + c[1] * r[5] + c[2] * r[8];
+  fx -= floor(fx);
+  fy -= floor(fy);
+  fz -= floor(fz);
+  double *grid = CA.grid + (size_t)chain * CA.grid_stride;
+  if (energy)
+    equitable_bin_dev(grid + (size_t)S.prob_eng_sub[g] * S.prob_gridsize, S.ngrid, fx, fy, fz,
+                      *energy);
+  equitable_bin_dev(grid + (size_t)(S.prob_eng_sub[g] + 1) * S.prob_gridsize, S.ngrid, fx, fy, fz,
+                    1.0);
+}
+
 // storeprob (utility_pack.f:621-687), all threads after a production move:
 // every molecule's centre of mass or listed sites, folded into the unit
 // cell, binned with weight 1.  One work item per (molecule, item); the CTAs

@@ -807,8 +807,6 @@ void finish_control(System &s) {
       const double gd = s.celprp[d] / std::ceil(s.celprp[d] / s.gridfactor[d] / s.griddim) / s.gridfactor[d];
       s.ngrid[d] = (int)std::ceil(s.celprp[d] / (gd * s.gridfactor[d]));
     }
-    for (int i = 1; i <= G; ++i)
-      if (s.lprobeng[i]) raise(FMC_ERR_INPUT, "energy probability grids are not supported");
   }
   bool lfract = false, lpress = true;
   double fsum = 0.0, nofract = 0.0, psum = 0.0;

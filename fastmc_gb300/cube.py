@@ -63,3 +63,35 @@ def write_prob_cube(path: str, grid: np.ndarray, prodcount: int, ucell: Sequence
         out.append("".join(line))
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")
+
+
+def write_energy_cube(path: str, energy: np.ndarray, count: np.ndarray, cell: Sequence[float],
+                      atoms: Iterable[Tuple[int, float, float, float]] = ()) -> None:
+    """Write a guest type's energy probability grid in the layout of the
+    reference's writeenprob (utility_pack.f:689-778): the energy sums over
+    the counts of the guest type's last two grids (0 where nothing was
+    counted), the voxel vectors as the cell rows over the grid counts as
+    writeenprob writes them (in A, not converted), framework atoms in bohr."""
+    e = np.asarray(energy, dtype=np.float64)
+    c = np.asarray(count, dtype=np.float64)
+    na, nb, nc = e.shape
+    atoms = list(atoms)
+    out = ["Energy histogram cube file", "outer loop a, middle loop b, inner loop c",
+           f"{len(atoms):6d}{0.0:12.6f}{0.0:12.6f}{0.0:12.6f}"]
+    for n, row in zip((na, nb, nc), (cell[0:3], cell[3:6], cell[6:9])):
+        out.append(f"{n:6d}" + "".join(f"{v / n:12.6f}" for v in row))
+    for z, x, y, w in atoms:
+        out.append(f"{int(z):6d}{0.0:12.6f}{x * ANGS2BOHR:12.6f}{y * ANGS2BOHR:12.6f}{w * ANGS2BOHR:12.6f}")
+    line, ip = [], 0
+    flat_e, flat_c = e.reshape(-1), c.reshape(-1)
+    for j in range(1, flat_e.size + 1):
+        ip += 1
+        v = flat_e[j - 1] / flat_c[j - 1] if flat_c[j - 1] > 0.0 else 0.0
+        line.append(fortran_e15_6(float(v)))
+        if j % nc == 0 or ip == 6:
+            out.append("".join(line))
+            line, ip = [], 0
+    if line:
+        out.append("".join(line))
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")

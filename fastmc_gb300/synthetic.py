@@ -239,7 +239,10 @@ def control_text(spec: GcmcSpec) -> str:
     if spec.probability:
         lines.append(f"  probability {len(spec.probability)}")
         for sites in spec.probability:
-            lines.append("  " + " ".join(str(int(v)) for v in [len(sites), *sites]))
+            if isinstance(sites, str):  # "energy": the energy probability grids
+                lines.append("  " + sites)
+            else:
+                lines.append("  " + " ".join(str(int(v)) for v in [len(sites), *sites]))
     lines.append("&end")
     if spec.second_guest:
         lines.append("&guest 2")

@@ -63,6 +63,7 @@ def load() -> C.CDLL:
             "orc_stats": (None, [vp, i, dp]),
             "orc_prob_info": (i, [vp, C.POINTER(C.c_int)]),
             "orc_prob_grid": (i, [vp, i, dp, i]),
+            "orc_store_energy": (i, [vp, i, dp, d]),
             "orc_prodcount": (C.c_longlong, [vp]),
             "orc_swap": (i, [vp, i, i, i, dp, dp, dp]),
             "orc_fugacity": (d, [vp, i]),
@@ -226,6 +227,13 @@ class Oracle:
         out = np.zeros(na * nb * nc)
         self._ck(self.lib.orc_prob_grid(self._h, sub, out.ctypes.data_as(C.POINTER(C.c_double)), out.size))
         return out.reshape(na, nb, nc)
+
+    def store_energy(self, iguest: int, xyz, energy: float) -> None:
+        """storeenprob of given site coordinates and energy (a Widom trial)."""
+        import numpy as np
+        a = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(-1))
+        self._ck(self.lib.orc_store_energy(self._h, iguest, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                           float(energy)))
 
     def fugacity(self, iguest: int) -> float:
         """gstfuga(iguest) in Pa."""

@@ -441,6 +441,7 @@ struct Sim {
   // statistics
   bool production = false;
   bool last_accepted = false;  // the main loop's `accepted` (not reset per move)
+  int cur_iguest = 1;          // the main loop's iguest (the move's guest type)
   long long gcmccount = 0, prodcount = 0, rollcount = 0, cycle_step = 0;
   int minchk = 1;
   std::vector<double> chainstats;
@@ -537,6 +538,7 @@ struct Sim {
   } fwgrid;
   bool fw_overlap_certain(int natms);
   void production_stats(bool accepted);
+  void storeenprob(int iguest, double energy);
   void setup_grid();
   void equitable_bin(double fa, double fb, double fc, int sub, double val);
   void storeprob();
@@ -2095,8 +2097,6 @@ void Sim::read_all(const std::string &dir) {
   tran_ratio.assign(ntpguest + 1, 0.5);
   rota_ratio.assign(ntpguest + 1, 0.5);
   readcontrol(dir);
-  for (int i = 1; i <= ntpguest; ++i)
-    if (lprobeng[i]) fail("oracle: energy probability grids (storeenprob) are not restated");
   overlap = overlap * overlap;
   fugacity();
   normalise_moves();
@@ -3231,6 +3231,11 @@ void Sim::production_stats(bool accepted) {
   last_accepted = accepted;
   if (!production) return;
   if (lprob) storeprob();  // gcmc.f:1129-1130, every production move
+  // gcmc.f:1131-1134: storeenprob(iguest, randchoice, ..., guest_toten) with
+  // the main program's randchoice and guest_toten, which no routine sets
+  // (the move routines' variables of those names are their own): molecule
+  // 0, so newx as the move left it, and energy 0
+  if (lprob && lprobeng[cur_iguest] && accepted) storeenprob(cur_iguest, 0.0);
   if (!((laccsample && accepted) || !laccsample)) return;
   ++prodcount;
   ++rollcount;
@@ -3442,6 +3447,30 @@ void Sim::storeprob() {
   }
 }
 
+// storeenprob (utility_pack.f:550-618) with imol 0: the centre of mass of
+// newx (the guest type's site count and masses), folded into the unit cell,
+// binned into the guest type's last two grids: the energy into the first,
+// a count into the second.
+void Sim::storeenprob(int iguest, double energy) {
+  const int m0 = locguest[iguest];
+  double cx, cy, cz;
+  com(mol[m0].natoms, m0, cx, cy, cz);
+  const double *rc = rucell;  // frac2
+  const double sx = cx * rc[0] + cy * rc[3] + cz * rc[6];
+  const double sy = cx * rc[1] + cy * rc[4] + cz * rc[7];
+  const double sz = cx * rc[2] + cy * rc[5] + cz * rc[8];
+  cx = sx - std::floor(sx);
+  cy = sy - std::floor(sy);
+  cz = sz - std::floor(sz);
+  int itprob = 0;
+  for (int j = 1; j <= ntpguest; ++j) {
+    itprob += nprob[j];
+    if (j == iguest) break;
+  }
+  equitable_bin(cx, cy, cz, itprob - 1, energy);
+  equitable_bin(cx, cy, cz, itprob, 1.0);
+}
+
 // One iteration of the main loop (gcmc.f:704-1164), moves ins/del/dis/tra/rot.
 void Sim::step(orc_move_log *lg) {
   ++cycle_step;
@@ -3502,6 +3531,7 @@ void Sim::step(orc_move_log *lg) {
     std::memset(lg, 0, sizeof(*lg));
     lg->iguest = iguest;
   }
+  cur_iguest = iguest;
   if (insert) {
     mc_insert(iguest, lg);
   } else if (del) {
@@ -3967,6 +3997,24 @@ int orc_prob_grid(const orc_sim *h, int sub, double *out, int n) {
     if (!s.lprob || sub < 1 || sub > s.ntprob || n < s.gridsize) fail("oracle: bad probability grid request");
     std::copy(s.grid.begin() + (size_t)(sub - 1) * s.gridsize,
               s.grid.begin() + (size_t)sub * s.gridsize, out);
+    return 0;
+  });
+}
+
+// storeenprob (utility_pack.f:550-618) of given site coordinates and
+// energy, as widom_grid calls it for a test insertion (gcmc.f:2529-2532).
+int orc_store_energy(orc_sim *h, int iguest, const double *xyz, double energy) {
+  return guarded([&] {
+    Sim &s = h->s;
+    if (!s.lprob || iguest < 1 || iguest > s.ntpguest || !s.lprobeng[iguest])
+      fail("oracle: no energy probability grid for this guest type");
+    const int n = s.mol[s.locguest[iguest]].natoms;
+    for (int a = 1; a <= n; ++a) {
+      s.newx[a] = xyz[3 * (a - 1)];
+      s.newy[a] = xyz[3 * (a - 1) + 1];
+      s.newz[a] = xyz[3 * (a - 1) + 2];
+    }
+    s.storeenprob(iguest, energy);
     return 0;
   });
 }

@@ -158,6 +158,9 @@ void orc_stats(const orc_sim *s, int iguest, double *out);
  * doubles, bin order a outer, b middle, c inner */
 int orc_prob_info(const orc_sim *s, int *out4);
 int orc_prob_grid(const orc_sim *s, int sub, double *out, int n);
+/* storeenprob of given site coordinates (natms x 3) and energy, as
+ * widom_grid calls it for a test insertion */
+int orc_store_energy(orc_sim *s, int iguest, const double *xyz, double energy);
 long long orc_prodcount(const orc_sim *s);
 
 /* MZT generator alone (for RNG parity tests): seed like orc_seed on a

@@ -81,3 +81,67 @@ def test_prob_grid_untouched_by_autotune_and_checkpoint(fmc_lib, inputs_dir, tmp
     b.load(path)
     for c in range(2):
         assert np.array_equal(b.prob_grid(c), before[c])
+
+
+def _energy_dir(tmp_path):
+    """One guest type with a centre-of-mass grid and the energy grids (an
+    'e' line, storeenprob) on an open framework (48 atoms per cell)."""
+    spec = syn.small_test_spec(seed=4, kmax=5, pressure_bar=5.0, create=10,
+                               move_mix=(("insert", 0.2), ("delete", 0.2), ("displace", 0.6)))
+    spec.overlap = 1.5
+    spec.probability = [[0], "energy"]
+    spec.grid_spacing = 0.8
+    d = str(tmp_path / "egrid")
+    syn.write_inputs(d, spec, uc=syn.make_unit_cell(4, natoms=48))
+    return d
+
+
+@pytest.mark.parametrize("prec,csize,n", [("fp64", 1, 400), ("fp64", 2, 400), ("fp32", 1, 200)])
+def test_energy_grids_follow_oracle(fmc_lib, oracle_lib, tmp_path, prec, csize, n):
+    """The energy grids as the main loop fills them (storeenprob with the
+    main program's guest_toten, 0, and molecule 0: a count at the centre of
+    the accepted move's last positions, nothing in the energy grid) next to
+    the centre-of-mass grid, against the oracle's three grids; FP32 over a
+    run whose decisions are the oracle's."""
+    d = _energy_dir(tmp_path)
+    o = oracle_lib.Oracle(d)
+    o.seed(3)
+    o.create_molecules(1, 10)
+    logs = o.run(n)
+    ref = np.stack([o.prob_grid(k + 1) for k in range(3)])
+    p = fmc_lib.FMC_PREC_FP64 if prec == "fp64" else fmc_lib.FMC_PREC_FP32
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 3}], precision=p, guest_capacity=64)
+    b.set_cluster([csize])
+    b.set_log(n)
+    b.run(n)
+    got_logs = b.log(0, n)
+    assert [(g.move, g.choice, g.accepted) for g in got_logs] == \
+           [(r.move, r.choice, r.accepted) for r in logs]
+    assert b.prob_info(0)[1] == 3
+    got = b.prob_grid(0)
+    assert sum(r.accepted for r in logs) >= 30
+    assert np.all(got[1] == 0.0) and got[2].sum() > 0
+    tol = 1e-10 if prec == "fp64" else 1e-7
+    assert np.allclose(got, ref, rtol=tol, atol=tol)
+
+
+def test_widom_energy_grid(fmc_lib, oracle_lib, tmp_path):
+    """widom_grid's test insertions fill the energy grids with their energies
+    and counts (gcmc.f:2529-2532): the device grids gain what the oracle's
+    storeenprob bins for the same trials (positions and energies the device
+    reports); the centre-of-mass grid is left alone."""
+    d = _energy_dir(tmp_path)
+    b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 3}], precision=fmc_lib.FMC_PREC_FP64,
+                      guest_capacity=64)
+    before = b.prob_grid(0)
+    (henry, nok, ntot), est, ovl, xyz = b.widom_grid(0, (6, 6, 6), 2, seed=7, details=True)
+    after = b.prob_grid(0)
+    assert nok >= 50
+    o = oracle_lib.Oracle(d)
+    for t in np.flatnonzero(ovl == 0):
+        o.store_energy(1, xyz[t], est[t])
+    ref = np.stack([o.prob_grid(k + 1) for k in range(3)])
+    diff = after - before
+    assert np.all(diff[0] == 0.0)
+    assert np.allclose(diff[1:], ref[1:], rtol=1e-10, atol=1e-10 * np.abs(ref[1]).max())
+    assert np.isclose(diff[2].sum(), nok, rtol=1e-12)

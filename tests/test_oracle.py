@@ -492,6 +492,32 @@ def test_recorded_isotherm_passes_reference_band(name):
             assert 0.8 * (avg - se) <= v <= 1.2 * (avg + se), (r["point"], avg, se, v)
 
 
+def test_energy_grids_as_the_main_loop_fills_them(oracle_lib, tmp_path):
+    """storeenprob from the main loop (gcmc.f:1131-1134) gets the main
+    program's guest_toten, which stays 0, and molecule 0: every accepted
+    production move adds a count at the centre of mass of the move's last
+    positions (weight 1 spread over 8 voxels) and nothing to the energy
+    grid.  The grids follow the site grid in the guest type's block."""
+    spec = syn.small_test_spec(seed=4, kmax=5, pressure_bar=5.0, create=10,
+                               move_mix=(("insert", 0.2), ("delete", 0.2), ("displace", 0.6)))
+    spec.overlap = 1.5
+    spec.probability = [[0], "energy"]
+    spec.grid_spacing = 0.8
+    d = str(tmp_path / "energy_grid")
+    syn.write_inputs(d, spec, uc=syn.make_unit_cell(4, natoms=48))  # an open framework
+    o = oracle_lib.Oracle(d)
+    o.seed(3)
+    o.create_molecules(1, 10)
+    logs = o.run(400)
+    assert o.prob_info()[3] == 3
+    site, energy, count = (o.prob_grid(k) for k in (1, 2, 3))
+    nacc = sum(1 for r in logs if r.accepted)
+    assert nacc >= 50
+    assert np.all(energy == 0.0)
+    assert count.sum() == pytest.approx(nacc, rel=1e-12)
+    assert site.sum() == pytest.approx(sum(r.nmols_after for r in logs), rel=1e-12)
+
+
 def test_preload_prefilter_changes_nothing(oracle_lib, inputs_dir):
     """insert_guests' framework pre-test skips only trial positions that
     insertion() rejects anyway: with it on and off the same molecules are
