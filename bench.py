@@ -474,6 +474,61 @@ def config5_widom(F, tmp):
             "workload": "config5: 102.4 A, 98304 atoms, 2000 CO2, cutoff 14 A, kmax 20, FP32"}
 
 
+def sampled_energy_adjoint(F, tmp, nsnap=4096):
+    """The sampled energy and its adjoint over a batch of frozen snapshots of
+    the 51.2 A framework (12288 atoms, cutoff 12.5 A, alpha 0.24, kmax 12):
+    8 FP32 chains pre-loaded with 400 CO2 and run 2000 moves each give the
+    states; snapshot q keeps the first N_q (uniform 50-400) molecules of a
+    random order of state q mod 8.  One call (fmc_adjoint_eval_batch, FP32
+    pair terms and phases, FP64 sums) returns every snapshot's energy,
+    dE/d(guest coordinates) (3N x FP32) and dE/d(eps, sigma, lambda) of the 4
+    framework types; the FP64 call on the same batch gives the reference
+    gradient.  Host wall time around the call, inputs on the device."""
+    import numpy as np
+    import torch
+    from fastmc_gb300 import synthetic as syn
+    from fastmc_gb300.adjoint import Adjoint
+    d = os.path.join(tmp, "snapshots51")
+    syn.write_inputs(d, syn.config2())
+    sysm = F.System.load(d)
+    b = F.Batch([sysm], [{"seed": 40 + c} for c in range(8)], precision=F.FMC_PREC_FP32,
+                guest_capacity=512)
+    b.run(2000)
+    states = []
+    for c in range(8):
+        x, n = b.coords(c)
+        states.append(x[:9 * n].reshape(n, 3, 3))
+    rng = np.random.default_rng(11)
+    nm = rng.integers(50, 401, size=nsnap)
+    parts = []
+    for q in range(nsnap):
+        st = states[q % 8]
+        parts.append(st[rng.permutation(len(st))[:nm[q]]])
+    nm = [len(p_) for p_ in parts]
+    x = torch.tensor(np.concatenate(parts), dtype=torch.float64, device="cuda")
+    adj = Adjoint(sysm)
+    p0 = adj.base_params()
+    adj.evaluate_batch(x, nm, p0, "fp32")  # warm-up
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e32, g32, p32 = adj.evaluate_batch(x, nm, p0, "fp32")
+        times.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    e64, g64, p64 = adj.evaluate_batch(x, nm, p0, "fp64")
+    t64 = time.perf_counter() - t0
+    g64n, g32n = g64.cpu().numpy(), g32.cpu().numpy()
+    s = min(times)
+    return {"value": nsnap / s, "unit": "snapshots/s", "snapshots": nsnap,
+            "guest_molecules": int(sum(nm)), "seconds_fp32": s, "seconds_fp64": t64,
+            "max_rel_energy_err_fp32": float(np.max(np.abs(e32 - e64) / np.abs(e64))),
+            "max_site_grad_err_fp32_rel_to_max": float(np.abs(g32n - g64n).max() / np.abs(g64n).max()),
+            "max_param_grad_rel_err_fp32": float(np.max(np.abs(p32 - p64)) / np.abs(p64).max()),
+            "workload": "4096 snapshots, 51.2 A, 12288 framework atoms, 50-400 CO2, cutoff 12.5 A, "
+                        "kmax 12, FP32 terms"}
+
+
 # ------------------------------------------------------------------ arms
 def run_reference(args, rank, world):
     if rank != 0:
@@ -659,6 +714,8 @@ def run_ours(args, rank, world, local_rank):
                                                     per_chain)
         if args.widom:
             out["config5_widom"] = config5_widom(F, tmp)
+        if args.adjoint:
+            out["sampled_energy_adjoint"] = sampled_energy_adjoint(F, tmp)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -707,6 +764,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
     ap.add_argument("--widom", action="store_true", help="also time config 5's 1e7 Widom trials")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="also time the sampled-energy adjoint of 4096 snapshots (51.2 A box)")
     ap.add_argument("--speculate", type=int, default=8,
                     help="speculative proposals per round at most (2..8; 0: off); the chains' "
                          "moves are the same either way")

@@ -166,6 +166,7 @@ SIGNATURES = {
     "fmc_adjoint_create": (C.c_int, [vp, C.POINTER(vp)]),
     "fmc_adjoint_info": (C.c_int, [vp, ip, ip, dp]),
     "fmc_adjoint_eval": (C.c_int, [vp, C.c_int, vp, dp, dp, vp, dp]),
+    "fmc_adjoint_eval_batch": (C.c_int, [vp, C.c_int, ip, vp, dp, C.c_int, dp, vp, dp]),
     "fmc_adjoint_destroy": (C.c_int, [vp]),
     "fmc_batch_get_chain_cluster": (C.c_int, [vp, ip, C.c_int]),
     "fmc_batch_prob_grid": (C.c_int, [vp, C.c_int, C.c_int, dp, C.c_int64]),

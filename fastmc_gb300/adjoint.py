@@ -63,6 +63,35 @@ class Adjoint:
                                           C.byref(e), C.c_void_p(gx.data_ptr()), gp.ctypes.data_as(L.dp)))
         return e.value, gx, gp.reshape(self.ntype, 3)
 
+    def evaluate_batch(self, xyz, nmol, params, precision: str = "fp32"):
+        """The sampled energy of a batch of snapshots and its adjoint
+        (fmc_adjoint_eval_batch): xyz a CUDA float64 tensor (sum(nmol),
+        nsite, 3) holding every snapshot's molecules one after the other,
+        nmol the molecule count of each snapshot.  Returns energies (S,)
+        numpy, dE/dxyz as a CUDA float32 tensor shaped like xyz, and
+        dE/dparams (S, ntype, 3) numpy."""
+        import torch
+        if not (xyz.is_cuda and xyz.dtype == torch.float64):
+            raise TypeError("xyz must be a CUDA float64 tensor")
+        x = xyz.contiguous()
+        nm = np.ascontiguousarray(np.asarray(nmol, dtype=np.int32).reshape(-1))
+        if x.shape[1:] != (self.nsite, 3) or x.shape[0] != int(nm.sum()):
+            raise ValueError("xyz must have shape (sum(nmol), %d, 3)" % self.nsite)
+        p = np.ascontiguousarray(np.asarray(params.detach().cpu() if hasattr(params, "detach") else params,
+                                            dtype=np.float64).reshape(-1))
+        if p.size != 3 * self.ntype:
+            raise ValueError("params must have shape (%d, 3)" % self.ntype)
+        prec = L.FMC_PREC_FP32 if precision == "fp32" else L.FMC_PREC_FP64
+        gx = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+        e = np.zeros(max(1, nm.size))
+        gp = np.zeros(max(1, nm.size) * 3 * self.ntype)
+        torch.cuda.synchronize(x.device)
+        L.check(L.load().fmc_adjoint_eval_batch(
+            self._h, int(nm.size), nm.ctypes.data_as(L.ip), C.c_void_p(x.data_ptr()),
+            p.ctypes.data_as(L.dp), prec, e.ctypes.data_as(L.dp), C.c_void_p(gx.data_ptr()),
+            gp.ctypes.data_as(L.dp)))
+        return e[:nm.size], gx, gp[:nm.size * 3 * self.ntype].reshape(nm.size, self.ntype, 3)
+
     def close(self) -> None:
         if self._h:
             L.load().fmc_adjoint_destroy(self._h)
@@ -98,6 +127,36 @@ def _function():
 def guest_framework_energy(adj: Adjoint, xyz, params):
     """Differentiable E (kcal/mol): torch autograd through the adjoint."""
     return _function().apply(adj, xyz, params)
+
+
+def _batch_function():
+    import torch
+
+    class SampledEnergy(torch.autograd.Function):
+        """E_q(xyz, params) of a batch of snapshots (the chains' sampled
+        energy) with the batched adjoint as its backward."""
+
+        @staticmethod
+        def forward(ctx, adj, xyz, nmol, params, precision):
+            e, gx, gp = adj.evaluate_batch(xyz, nmol, params, precision)
+            ctx.save_for_backward(gx, torch.as_tensor(gp, dtype=params.dtype, device=params.device))
+            ctx.snap = torch.as_tensor(np.repeat(np.arange(len(e)), np.asarray(nmol)), device=xyz.device)
+            return torch.as_tensor(e, dtype=torch.float64, device=params.device)
+
+        @staticmethod
+        def backward(ctx, grad):
+            gx, gp = ctx.saved_tensors
+            gm = grad.to(gx.device, torch.float64)[ctx.snap].view(-1, 1, 1)
+            gxyz = gm * gx.to(torch.float64)
+            gpar = (grad.to(gp.device).view(-1, 1, 1) * gp).sum(dim=0)
+            return None, gxyz, None, gpar, None
+
+    return SampledEnergy
+
+
+def sampled_energy(adj: Adjoint, xyz, nmol, params, precision: str = "fp32"):
+    """Differentiable energies (kcal/mol) of a batch of snapshots."""
+    return _batch_function().apply(adj, xyz, nmol, params, precision)
 
 
 def uptake_sensitivity(n, de_dtheta, beta: float):

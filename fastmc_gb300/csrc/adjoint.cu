@@ -16,6 +16,7 @@
 // the type-t atoms at their FIELD charges.  Orthorhombic cells; FP64.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -249,6 +250,337 @@ __global__ void adj_recip_site_kernel(AdjConst c, const int4 *__restrict__ klmn,
   gxyz[3 * i + 2] += gz * c.rengunit;
 }
 
+
+// ------------------------------------------------ the sampled Hamiltonian
+// Batched snapshots, the energy the chains sample: the guests' real-space
+// erfc Coulomb and Lennard-Jones terms from the reference's tables (erc and
+// vvv with the 3-point interpolation, ewald.f:703-715, vdw_terms.f:441-453)
+// against the framework and against the other molecules, the reciprocal sum
+// of the guests against the framework and each other without each
+// molecule's own term, and the guest-framework Lennard-Jones tail
+// (lrcorrect, vdw_terms.f:470-645).  Framework type t's (eps_t, sigma_t)
+// move its pairs' parameters from the FIELD's values as Lorentz-Berthelot
+// mixing does (eps x sqrt(eps_t / eps_t0), sigma + (sigma_t - sigma_t0)/2),
+// so the tables at the base parameters are the system's own; lambda_t
+// scales the type's charges.  Pair terms in T (float or double), sums in
+// FP64.
+
+constexpr int kHT = 256;  // threads per block, Hamiltonian kernels
+
+struct HamConst {
+  double L[3], rL[3];
+  double rc2, chg_r4e, rengunit, krecip, rdrewd, rdlrpot;
+  int mxegrd, tabstride, nfw, ns, ntype, nk, nc[3];
+  double chgea[kMaxASite], qs[kMaxASite];
+  int gg_row[kMaxASite][kMaxASite];  // guest-guest LJ table row, -1 without
+  double eps_t[kMaxAType];           // eps_t of the call (FIELD unit), for dE/deps
+  double lam[kMaxAType];
+};
+
+// The 3-point interpolation and its derivative in r.
+template <class T>
+__device__ __forceinline__ T interp_d(const T *tab, T r, T rd, int mx, T &dv) {
+  const T t = r * rd;
+  const int l = int(t);
+  if (l < 1 || l + 2 > mx + 2) {
+    dv = T(0);
+    return T(0);
+  }
+  const T p = t - T(l);
+  const T v0 = tab[l], v1 = tab[l + 1], v2 = tab[l + 2];
+  const T t1 = v0 + (v1 - v0) * p;
+  const T t2 = v1 + (v2 - v1) * (p - T(1));
+  // d/dp of t1 + (t2 - t1) p / 2, then d/dr = rd d/dp
+  dv = ((v1 - v0) + (t2 - t1) * T(0.5) + p * T(0.5) * ((v2 - v1) - (v1 - v0))) * rd;
+  return t1 + (t2 - t1) * p * T(0.5);
+}
+
+// Real space, one block per molecule of the batch: its sites against the
+// framework atoms of the 27 neighbour cells (cells at least rc wide, or
+// every atom when the box holds fewer than three) and against every site
+// of the snapshot's other molecules (each pair's energy halved: the other
+// molecule's block sees it too).  The energy and dE/d(eps, sigma, lambda)
+// per type go to the snapshot's sums; the molecule's site gradients are
+// stored (FP64).  T: the type of the pair terms.
+template <class T>
+__global__ void __launch_bounds__(kHT) ham_real_kernel(
+    HamConst c, const double4 *__restrict__ fw, const int *__restrict__ fwt,
+    const int *__restrict__ cstart, const double *__restrict__ xyz, const int *__restrict__ mol_snap,
+    const int *__restrict__ snap_mol0, const int *__restrict__ snap_nmol, const T *__restrict__ erc,
+    const T *__restrict__ vt, const T *__restrict__ ds, const T *__restrict__ vgg, double *g64,
+    double *esnap, double *psnap) {
+  constexpr int NV = 1 + 3 * kMaxAType;
+  __shared__ double sh[(kHT / 32) * NV];
+  __shared__ int cell_id[27], cell_pref[28];
+  __shared__ double site[kMaxASite][3];
+  const int m = blockIdx.x, snap = mol_snap[m], ns = c.ns;
+  if (threadIdx.x < 3 * ns) site[threadIdx.x / 3][threadIdx.x % 3] = xyz[(size_t)m * ns * 3 + threadIdx.x];
+  double v[NV];
+  for (int q = 0; q < NV; ++q) v[q] = 0.0;
+  double g[kMaxASite][3];
+  for (int s = 0; s < kMaxASite; ++s) g[s][0] = g[s][1] = g[s][2] = 0.0;
+  __syncthreads();
+  const T rd = (T)c.rdrewd, rdl = (T)c.rdlrpot;
+  const bool cells = c.nc[0] >= 3 && c.nc[1] >= 3 && c.nc[2] >= 3;
+  for (int s = 0; s < ns; ++s) {
+    int total = c.nfw;  // candidate framework atoms of site s
+    if (cells) {
+      if (threadIdx.x < 27) {
+        int ic[3], w[3];
+        for (int d = 0; d < 3; ++d) {
+          double f = site[s][d] * c.rL[d];
+          f -= floor(f);
+          ic[d] = min(c.nc[d] - 1, (int)(f * c.nc[d]));
+        }
+        const int o[3] = {(int)threadIdx.x / 9 - 1, ((int)threadIdx.x / 3) % 3 - 1, (int)threadIdx.x % 3 - 1};
+        for (int d = 0; d < 3; ++d) w[d] = (ic[d] + o[d] + c.nc[d]) % c.nc[d];
+        cell_id[threadIdx.x] = (w[0] * c.nc[1] + w[1]) * c.nc[2] + w[2];
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        cell_pref[0] = 0;
+        for (int q = 0; q < 27; ++q)
+          cell_pref[q + 1] = cell_pref[q] + cstart[cell_id[q] + 1] - cstart[cell_id[q]];
+      }
+      __syncthreads();
+      total = cell_pref[27];
+    }
+    const T ca = (T)c.chgea[s];
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      int j = t;
+      if (cells) {
+        int q = 0;
+        while (cell_pref[q + 1] <= t) ++q;
+        j = cstart[cell_id[q]] + (t - cell_pref[q]);
+      }
+      const double4 a = fw[j];
+      double dx = site[s][0] - a.x, dy = site[s][1] - a.y, dz = site[s][2] - a.z;
+      dx -= c.L[0] * rint(dx * c.rL[0]);
+      dy -= c.L[1] * rint(dy * c.rL[1]);
+      dz -= c.L[2] * rint(dz * c.rL[2]);
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 >= c.rc2) continue;
+      const int ty = fwt[j];
+      const T r = (T)sqrt(r2);
+      T de, dvv, dsd;
+      const T ev = interp_d(erc, r, rd, c.mxegrd, de);
+      const size_t row = ((size_t)s * c.ntype + ty) * c.tabstride;
+      const T lj = interp_d(vt + row, r, rdl, c.mxegrd, dvv);
+      const T dsig = interp_d(ds + row, r, rdl, c.mxegrd, dsd);
+      const T qq = ca * (T)a.w;
+      const T lam = (T)c.lam[ty];
+      const double dedr = (double)(lam * qq * de) + (double)dvv;
+      const double rr = 1.0 / sqrt(r2);
+      g[s][0] += dedr * dx * rr;
+      g[s][1] += dedr * dy * rr;
+      g[s][2] += dedr * dz * rr;
+      v[0] += (double)(lam * qq * ev) + (double)lj;
+      if (c.eps_t[ty] > 0.0) v[1 + 3 * ty] += (double)lj / (2.0 * c.eps_t[ty]);
+      v[1 + 3 * ty + 1] += (double)dsig;
+      v[1 + 3 * ty + 2] += (double)(qq * ev);
+    }
+    __syncthreads();
+  }
+  // the snapshot's other molecules
+  const int m0 = snap_mol0[snap], nm = snap_nmol[snap];
+  for (int t = threadIdx.x; t < nm * ns * ns; t += blockDim.x) {
+    const int mm = m0 + t / (ns * ns);
+    if (mm == m) continue;
+    const int s = (t / ns) % ns, s2 = t % ns;
+    const double *q = xyz + ((size_t)mm * ns + s2) * 3;
+    double dx = site[s][0] - q[0], dy = site[s][1] - q[1], dz = site[s][2] - q[2];
+    dx -= c.L[0] * rint(dx * c.rL[0]);
+    dy -= c.L[1] * rint(dy * c.rL[1]);
+    dz -= c.L[2] * rint(dz * c.rL[2]);
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 >= c.rc2) continue;
+    const T r = (T)sqrt(r2);
+    T de, dvv = T(0), lj = T(0);
+    const T ev = interp_d(erc, r, rd, c.mxegrd, de);
+    const int rowi = c.gg_row[s][s2];
+    if (rowi >= 0) lj = interp_d(vgg + (size_t)rowi * c.tabstride, r, rdl, c.mxegrd, dvv);
+    const T qq = (T)c.chgea[s] * (T)c.qs[s2];
+    const double dedr = (double)(qq * de) + (double)dvv;
+    const double rr = 1.0 / sqrt(r2);
+    g[s][0] += dedr * dx * rr;
+    g[s][1] += dedr * dy * rr;
+    g[s][2] += dedr * dz * rr;
+    v[0] += 0.5 * ((double)(qq * ev) + (double)lj);
+  }
+  // sums: the snapshot's energy and parameter gradients, the sites' gradients
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const int nv = 1 + 3 * c.ntype;
+  for (int i = 0; i < nv; ++i) {
+    double x = v[i];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[wq * NV + i] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double t = 0.0;
+    for (int k = 0; k < kHT / 32; ++k) t += sh[k * NV + threadIdx.x];
+    t *= c.rengunit;
+    if (t != 0.0) atomicAdd(threadIdx.x == 0 ? esnap + snap : psnap + (size_t)snap * 3 * c.ntype + threadIdx.x - 1, t);
+  }
+  __syncthreads();
+  for (int i = 0; i < 3 * ns; ++i) {
+    double x = g[i / 3][i % 3];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[wq * NV + (i % NV)] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int k = 0; k < kHT / 32; ++k) t += sh[k * NV + (i % NV)];
+      g64[(size_t)m * ns * 3 + i] = t * c.rengunit;
+    }
+    __syncthreads();
+  }
+}
+
+// Per-site fractional coordinates x / L as float hi/lo pairs, reduced to
+// [0, 1) (the phases only need them modulo 1).
+__global__ void ham_frac_kernel(HamConst c, const double *xyz, int nsite, float2 *fr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * nsite) return;
+  double f = xyz[i] * c.rL[i % 3];
+  f -= floor(f);
+  const float h = (float)f;
+  fr[i] = make_float2(h, (float)(f - (double)h));
+}
+
+// e^{i 2 pi (l fx + m fy + n fz)} of one site: FP64, or in FP32 with the
+// products j * f formed exactly (FMA residuals) and reduced before sincospif.
+template <class T>
+__device__ __forceinline__ void ham_phase(const int4 l, const double *xyz, const float2 *fr, double rLx,
+                                          double rLy, double rLz, T &cs, T &sn) {
+  if constexpr (sizeof(T) == 8) {
+    double f = (double)l.x * (xyz[0] * rLx) + (double)l.y * (xyz[1] * rLy) + (double)l.z * (xyz[2] * rLz);
+    f -= rint(f);
+    sincospi(2.0 * f, &sn, &cs);
+  } else {
+    float hs = 0.f, ls = 0.f;
+    const int lk[3] = {l.x, l.y, l.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float j = (float)lk[d];
+      const float p = j * fr[d].x;
+      const float pe = fmaf(j, fr[d].x, -p) + j * fr[d].y;
+      const float t = hs + p;
+      const float bp = t - hs;
+      ls += ((hs - (t - bp)) + (p - bp)) + pe;
+      hs = t;
+    }
+    float x = (hs - rintf(hs)) + ls;
+    sincospif(2.0f * x, &sn, &cs);
+  }
+}
+
+// The guests' structure factor of every snapshot (block x), k per thread: S_g, and
+// the reciprocal energy K a_k [2 Re(S_g conj(S_fw)) + |S_g|^2 - sum_m |s_m|^2]
+// with S_fw = sum_t lambda_t S_t, dE/dlambda_t = K a_k 2 Re(S_g conj(S_t)).
+template <class T>
+__global__ void __launch_bounds__(kHT) ham_sk_kernel(HamConst c, const int4 *__restrict__ klmn,
+                                                     const double *__restrict__ akk,
+                                                     const double2 *__restrict__ skt,
+                                                     const double *__restrict__ xyz,
+                                                     const float2 *__restrict__ fr,
+                                                     const int *__restrict__ snap_mol0,
+                                                     const int *__restrict__ snap_nmol, double2 *sg,
+                                                     double *esnap, double *psnap) {
+  constexpr int NV = 1 + 3 * kMaxAType;
+  __shared__ double sh[(kHT / 32) * NV];
+  const int k = blockIdx.y * kHT + threadIdx.x, snap = blockIdx.x, ns = c.ns;
+  double v[NV];
+  for (int q = 0; q < NV; ++q) v[q] = 0.0;
+  if (k < c.nk) {
+    const int4 l = klmn[k];
+    double Sr = 0.0, Si = 0.0, self = 0.0;
+    const int m0 = snap_mol0[snap], nm = snap_nmol[snap];
+    for (int mm = m0; mm < m0 + nm; ++mm) {
+      double sr = 0.0, si = 0.0;
+      for (int s = 0; s < ns; ++s) {
+        const size_t i = (size_t)mm * ns + s;
+        T cs, sn;
+        ham_phase<T>(l, xyz + 3 * i, fr + 3 * i, c.rL[0], c.rL[1], c.rL[2], cs, sn);
+        sr += c.qs[s] * (double)cs;
+        si += c.qs[s] * (double)sn;
+      }
+      Sr += sr;
+      Si += si;
+      self += sr * sr + si * si;
+    }
+    double Fr = 0.0, Fi = 0.0;
+    const double f = c.krecip * akk[k] * c.rengunit;
+    for (int t = 0; t < c.ntype; ++t) {
+      const double2 st = skt[(size_t)t * c.nk + k];
+      Fr += c.lam[t] * st.x;
+      Fi += c.lam[t] * st.y;
+      v[1 + 3 * t + 2] = 2.0 * f * (Sr * st.x + Si * st.y);
+    }
+    v[0] = f * (2.0 * (Sr * Fr + Si * Fi) + (Sr * Sr + Si * Si) - self);
+    sg[(size_t)snap * c.nk + k] = make_double2(Sr + Fr, Si + Fi);  // S_g + S_fw
+  }
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const int nv = 1 + 3 * c.ntype;
+  for (int i = 0; i < nv; ++i) {
+    double x = v[i];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[wq * NV + i] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double t = 0.0;
+    for (int q = 0; q < kHT / 32; ++q) t += sh[q * NV + threadIdx.x];
+    if (t != 0.0) atomicAdd(threadIdx.x == 0 ? esnap + snap : psnap + (size_t)snap * 3 * c.ntype + threadIdx.x - 1, t);
+  }
+}
+
+// Reciprocal site gradients, one thread per molecule (its sites' phases
+// give its own s_m): dE/dr_i = -2 K q_i sum_k a_k k Im(e^{i phi_i} conj(W)),
+// W = S_fw + S_g - s_m; added to the real-space gradients and stored as
+// float (3N x FP32).
+template <class T>
+__global__ void ham_recip_grad_kernel(HamConst c, const int4 *__restrict__ klmn,
+                                      const double *__restrict__ akk, const double2 *__restrict__ sg,
+                                      const double *__restrict__ xyz, const float2 *__restrict__ fr,
+                                      const int *__restrict__ mol_snap, int nmol_total,
+                                      const double *__restrict__ g64, float *gout) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmol_total) return;
+  const int ns = c.ns, snap = mol_snap[m];
+  double g[kMaxASite][3];
+  for (int s = 0; s < kMaxASite; ++s) g[s][0] = g[s][1] = g[s][2] = 0.0;
+  for (int k = 0; k < c.nk; ++k) {
+    const int4 l = klmn[k];
+    double cs[kMaxASite], sn[kMaxASite], sr = 0.0, si = 0.0;
+    for (int s = 0; s < ns; ++s) {
+      const size_t i = (size_t)m * ns + s;
+      T a, b;
+      ham_phase<T>(l, xyz + 3 * i, fr + 3 * i, c.rL[0], c.rL[1], c.rL[2], a, b);
+      cs[s] = (double)a;
+      sn[s] = (double)b;
+      sr += c.qs[s] * cs[s];
+      si += c.qs[s] * sn[s];
+    }
+    const double2 w0 = sg[(size_t)snap * c.nk + k];
+    const double wr = w0.x - sr, wi = w0.y - si;
+    const double f = -2.0 * c.krecip * akk[k];
+    const double kx = 2.0 * kPi * l.x * c.rL[0], ky = 2.0 * kPi * l.y * c.rL[1],
+                 kz = 2.0 * kPi * l.z * c.rL[2];
+    for (int s = 0; s < ns; ++s) {
+      const double w = f * c.qs[s] * (sn[s] * wr - cs[s] * wi);
+      g[s][0] += w * kx;
+      g[s][1] += w * ky;
+      g[s][2] += w * kz;
+    }
+  }
+  for (int s = 0; s < ns; ++s)
+    for (int d = 0; d < 3; ++d) {
+      const size_t i = ((size_t)m * ns + s) * 3 + d;
+      gout[i] = (float)(g64[i] + g[s][d] * c.rengunit);
+    }
+}
+
 }  // namespace
 
 struct fmc_adjoint {
@@ -260,6 +592,15 @@ struct fmc_adjoint {
   ABuf<double2> skt, sfw;
   ABuf<double> acc;
   std::vector<int> type_of_field;  // framework type index -> FIELD unique type
+  // the sampled Hamiltonian (fmc_adjoint_eval_batch)
+  HamConst h{};
+  ABuf<double4> hfw;   // framework atoms sorted by cell
+  ABuf<int> hfwt, hcstart;
+  ABuf<double> erc64, vgg64;
+  ABuf<float> erc32, vgg32;
+  std::vector<double> eps0, sig0;  // [site][type] the FIELD's pair parameters (internal unit, A)
+  std::vector<double> ntyp;        // framework atoms per type
+  double volm = 0, rcut = 0, engunit = 1, dlrpot = 0;
 };
 
 extern "C" {
@@ -336,6 +677,94 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
       FMC_ACUDA(cudaGetLastError());
       FMC_ACUDA(cudaDeviceSynchronize());
     }
+    // the sampled Hamiltonian: tables, framework cells, pair parameters
+    HamConst &h = a->h;
+    for (int d = 0; d < 3; ++d) {
+      h.L[d] = c.L[d];
+      h.rL[d] = c.rL[d];
+      h.nc[d] = std::max(1, (int)std::floor(c.L[d] / s.rcut));
+    }
+    h.rc2 = c.rc2;
+    h.rengunit = c.rengunit;
+    h.krecip = c.krecip;
+    h.rdrewd = 1.0 / s.drewd;
+    h.rdlrpot = 1.0 / s.dlrpot;
+    h.mxegrd = s.mxegrd;
+    h.tabstride = s.mxegrd + 3;
+    h.nfw = c.nfw;
+    h.ns = c.ns;
+    h.ntype = c.ntype;
+    h.nk = c.nk;
+    for (int i = 0; i < gm.natoms; ++i) {
+      h.qs[i] = gm.chg[i];
+      h.chgea[i] = gm.chg[i] / s.epsq * fmc::kR4pie0;  // ewald.f:688 (chgea)
+    }
+    a->volm = s.volm;
+    a->rcut = s.rcut;
+    a->engunit = s.engunit;
+    a->dlrpot = s.dlrpot;
+    for (int i = 0; i < gm.natoms; ++i)
+      for (int k = 0; k < c.ntype; ++k)
+        if (gm.ltp[i] == a->type_of_field[k])
+          raise(FMC_ERR_INPUT, "the adjoint needs guest and framework atom types apart");
+    a->eps0.assign((size_t)c.ns * c.ntype, 0.0);
+    a->sig0.assign((size_t)c.ns * c.ntype, 0.0);
+    for (int i = 0; i < c.ns; ++i)
+      for (int k = 0; k < c.ntype; ++k) {
+        const int iv = s.lstvdw[fmc::loc2(gm.ltp[i], a->type_of_field[k])];
+        if (iv < 1 || iv > s.ntpvdw || s.ltpvdw[iv] != 2)
+          raise(FMC_ERR_INPUT, "the adjoint needs a 12-6 LJ pair for every guest site and framework type");
+        a->eps0[(size_t)i * c.ntype + k] = s.prmvdw[iv][1];
+        a->sig0[(size_t)i * c.ntype + k] = s.prmvdw[iv][2];
+      }
+    a->ntyp.assign(c.ntype, 0.0);
+    for (int j = 0; j < c.nfw; ++j) a->ntyp[fwt[j]] += 1.0;
+    const size_t ts = (size_t)h.tabstride;
+    std::vector<double> erc(ts, 0.0);
+    for (int i = 1; i <= s.mxegrd; ++i) erc[i] = s.erc[i];
+    a->erc64.upload(erc);
+    a->erc32.upload(std::vector<float>(erc.begin(), erc.end()));
+    std::vector<double> vgg;
+    for (int i = 0; i < c.ns; ++i)
+      for (int j = 0; j < c.ns; ++j) {
+        const int iv = s.lstvdw[fmc::loc2(gm.ltp[i], gm.ltp[j])];
+        h.gg_row[i][j] = -1;
+        if (iv >= 1 && iv <= s.ntpvdw) {
+          h.gg_row[i][j] = (int)(vgg.size() / ts);
+          for (size_t q = 0; q < ts; ++q) vgg.push_back(q >= 1 && (int)q <= s.mxegrd ? s.vvv[iv][q] : 0.0);
+        }
+      }
+    if (vgg.empty()) vgg.assign(ts, 0.0);
+    a->vgg64.upload(vgg);
+    a->vgg32.upload(std::vector<float>(vgg.begin(), vgg.end()));
+    {  // framework atoms by cell (z fastest)
+      std::vector<int> cell(c.nfw), order(c.nfw);
+      for (int j = 0; j < c.nfw; ++j) {
+        int ic[3];
+        const double p3[3] = {fw[j].x, fw[j].y, fw[j].z};
+        for (int d = 0; d < 3; ++d) {
+          double f = p3[d] * h.rL[d];
+          f -= std::floor(f);
+          ic[d] = std::min(h.nc[d] - 1, (int)(f * h.nc[d]));
+        }
+        cell[j] = (ic[0] * h.nc[1] + ic[1]) * h.nc[2] + ic[2];
+        order[j] = j;
+      }
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cell[x] < cell[y]; });
+      const int ncell = h.nc[0] * h.nc[1] * h.nc[2];
+      std::vector<int> cs(ncell + 1, 0);
+      for (int j = 0; j < c.nfw; ++j) cs[cell[j] + 1]++;
+      for (int q = 0; q < ncell; ++q) cs[q + 1] += cs[q];
+      std::vector<double4> sf(c.nfw);
+      std::vector<int> st(c.nfw);
+      for (int j = 0; j < c.nfw; ++j) {
+        sf[j] = fw[order[j]];
+        st[j] = fwt[order[j]];
+      }
+      a->hfw.upload(sf);
+      a->hfwt.upload(st);
+      a->hcstart.upload(cs);
+    }
     *out = hold.release();
     return FMC_OK;
   });
@@ -386,6 +815,136 @@ int fmc_adjoint_eval(fmc_adjoint *a, int nmol, const double *xyz, const double *
     *energy = acc[0];
     for (int t = 0; t < c.ntype; ++t)
       for (int q = 0; q < 3; ++q) gparams[3 * t + q] = acc[1 + 3 * t + q];
+    return FMC_OK;
+  });
+}
+
+int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const double *xyz,
+                           const double *params, int precision, double *energy, float *gxyz,
+                           double *gparams) {
+  return aguard([&] {
+    if (!a || (nsnap > 0 && (!nmol || !xyz || !params || !energy || !gxyz || !gparams)))
+      raise(FMC_ERR_ARG, "null argument");
+    if (nsnap < 0) raise(FMC_ERR_ARG, "negative snapshot count");
+    if (precision != FMC_PREC_FP32 && precision != FMC_PREC_FP64) raise(FMC_ERR_ARG, "bad precision");
+    HamConst h = a->h;
+    const int T = h.ntype, ns = h.ns;
+    for (int t = 0; t < T; ++t) {
+      if (!(params[3 * t] >= 0.0) || !(params[3 * t + 1] > 0.0))
+        raise(FMC_ERR_ARG, "epsilon >= 0 and sigma > 0 required");
+      h.eps_t[t] = params[3 * t];
+      h.lam[t] = params[3 * t + 2];
+    }
+    std::vector<int> mol_snap, mol0(std::max(1, nsnap)), nm(std::max(1, nsnap));
+    long long total = 0;
+    for (int q = 0; q < nsnap; ++q) {
+      if (nmol[q] < 0) raise(FMC_ERR_ARG, "negative molecule count");
+      mol0[q] = (int)total;
+      nm[q] = nmol[q];
+      total += nmol[q];
+      if (total * ns > (1LL << 26)) raise(FMC_ERR_CAPACITY, "too many guest sites in one batch");
+      for (int i = 0; i < nmol[q]; ++i) mol_snap.push_back(q);
+    }
+    // the guest-framework tables at these parameters (forgen's expression,
+    // vdw_terms.f:181-234, with Lorentz-Berthelot moves of the FIELD's pair
+    // values) and their sigma derivatives
+    const size_t ts = (size_t)h.tabstride;
+    std::vector<double> vt((size_t)ns * T * ts, 0.0), ds((size_t)ns * T * ts, 0.0);
+    std::vector<double> pe((size_t)ns * T), ps((size_t)ns * T);
+    for (int i = 0; i < ns; ++i)
+      for (int t = 0; t < T; ++t) {
+        const size_t o = (size_t)i * T + t;
+        const double e0t = a->c.par[t][0], s0t = a->c.par[t][1];
+        const double eps = a->eps0[o] * (e0t > 0.0 ? std::sqrt(params[3 * t] / e0t) : 0.0);
+        const double sig = a->sig0[o] + 0.5 * (params[3 * t + 1] - s0t);
+        pe[o] = eps;
+        ps[o] = sig;
+        for (int q = 1; q <= h.mxegrd; ++q) {
+          const double rr = double(q) * a->dlrpot;
+          const double sr6 = std::pow(sig / rr, 6);
+          vt[o * ts + q] = 4.0 * eps * sr6 * (sr6 - 1.0);
+          ds[o * ts + q] = 0.5 * 4.0 * eps * (12.0 * sr6 * sr6 - 6.0 * sr6) / sig;
+        }
+      }
+    ABuf<int> dms, dm0, dnm;
+    ABuf<double> e_d, p_d, g64, vt64, ds64;
+    ABuf<float> vt32, ds32;
+    ABuf<float2> fr;
+    ABuf<double2> sg;
+    dms.upload(mol_snap.empty() ? std::vector<int>{0} : mol_snap);
+    dm0.upload(mol0);
+    dnm.upload(nm);
+    e_d.upload(std::vector<double>(std::max(1, nsnap), 0.0));
+    p_d.upload(std::vector<double>((size_t)std::max(1, nsnap) * 3 * T, 0.0));
+    g64.alloc((size_t)std::max(1LL, total) * ns * 3);
+    if (precision == FMC_PREC_FP64) {
+      vt64.upload(vt);
+      ds64.upload(ds);
+    } else {
+      vt32.upload(std::vector<float>(vt.begin(), vt.end()));
+      ds32.upload(std::vector<float>(ds.begin(), ds.end()));
+    }
+    fr.alloc((size_t)std::max(1LL, total) * ns * 3);
+    sg.alloc((size_t)std::max(1, nsnap) * std::max(1, h.nk));
+    if (total > 0) {
+      const int nsite = (int)(total * ns);
+      ham_frac_kernel<<<(3 * nsite + 255) / 256, 256>>>(h, xyz, nsite, fr.p);
+      FMC_ACUDA(cudaGetLastError());
+      if (precision == FMC_PREC_FP64) {
+        ham_real_kernel<double><<<(unsigned)total, kHT>>>(h, a->hfw.p, a->hfwt.p, a->hcstart.p, xyz, dms.p,
+                                                           dm0.p, dnm.p, a->erc64.p, vt64.p, ds64.p,
+                                                           a->vgg64.p, g64.p, e_d.p, p_d.p);
+      } else {
+        ham_real_kernel<float><<<(unsigned)total, kHT>>>(h, a->hfw.p, a->hfwt.p, a->hcstart.p, xyz, dms.p,
+                                                          dm0.p, dnm.p, a->erc32.p, vt32.p, ds32.p,
+                                                          a->vgg32.p, g64.p, e_d.p, p_d.p);
+      }
+      FMC_ACUDA(cudaGetLastError());
+      if (h.nk > 0) {
+        dim3 grid(nsnap, (h.nk + kHT - 1) / kHT);  // snapshots along x (up to 2^31 - 1)
+        if (precision == FMC_PREC_FP64)
+          ham_sk_kernel<double><<<grid, kHT>>>(h, a->klmn.p, a->akk.p, a->skt.p, xyz, fr.p, dm0.p, dnm.p,
+                                               sg.p, e_d.p, p_d.p);
+        else
+          ham_sk_kernel<float><<<grid, kHT>>>(h, a->klmn.p, a->akk.p, a->skt.p, xyz, fr.p, dm0.p, dnm.p,
+                                              sg.p, e_d.p, p_d.p);
+        FMC_ACUDA(cudaGetLastError());
+      }
+      const unsigned gb = (unsigned)((total + 127) / 128);
+      if (precision == FMC_PREC_FP64)
+        ham_recip_grad_kernel<double><<<gb, 128>>>(h, a->klmn.p, a->akk.p, sg.p, xyz, fr.p, dms.p,
+                                                  (int)total, g64.p, gxyz);
+      else
+        ham_recip_grad_kernel<float><<<gb, 128>>>(h, a->klmn.p, a->akk.p, sg.p, xyz, fr.p, dms.p,
+                                                 (int)total, g64.p, gxyz);
+      FMC_ACUDA(cudaGetLastError());
+    }
+    FMC_ACUDA(cudaDeviceSynchronize());
+    std::vector<double> e(std::max(1, nsnap)), gp((size_t)std::max(1, nsnap) * 3 * T);
+    FMC_ACUDA(cudaMemcpy(e.data(), e_d.p, e.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    FMC_ACUDA(cudaMemcpy(gp.data(), p_d.p, gp.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    // the guest-framework Lennard-Jones tail (lrcorrect, vdw_terms.f:470-645):
+    // 2 pi / V n_a n_t eadd per site and framework type, eadd = 2 x 4 eps
+    // (sigma^12 / (9 rc^9) - sigma^6 / (3 rc^3)) for unlike types
+    const double rc = a->rcut, twopi = 2.0 * fmc::kPi;
+    for (int q = 0; q < nsnap; ++q) {
+      const double N = double(nmol[q]);
+      for (int i = 0; i < ns; ++i)
+        for (int t = 0; t < T; ++t) {
+          const size_t o = (size_t)i * T + t;
+          const double eps = pe[o], sig = ps[o];
+          const double pre = twopi / a->volm * N * a->ntyp[t] / a->engunit;
+          const double eadd = 2.0 * 4.0 * eps * (std::pow(sig, 12) / (9.0 * std::pow(rc, 9)) -
+                                                 std::pow(sig, 6) / (3.0 * std::pow(rc, 3)));
+          const double dsig = 2.0 * 4.0 * eps * (12.0 * std::pow(sig, 11) / (9.0 * std::pow(rc, 9)) -
+                                                 6.0 * std::pow(sig, 5) / (3.0 * std::pow(rc, 3)));
+          e[q] += pre * eadd;
+          if (params[3 * t] > 0.0) gp[(size_t)q * 3 * T + 3 * t] += pre * eadd / (2.0 * params[3 * t]);
+          gp[(size_t)q * 3 * T + 3 * t + 1] += pre * dsig * 0.5;
+        }
+      energy[q] = e[q];
+      for (int j = 0; j < 3 * T; ++j) gparams[(size_t)q * 3 * T + j] = gp[(size_t)q * 3 * T + j];
+    }
     return FMC_OK;
   });
 }

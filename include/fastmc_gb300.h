@@ -448,6 +448,7 @@ int fmc_widom_positions(fmc_batch *b, int chain, int iguest, int npos, const dou
 int fmc_batch_prob_info(fmc_batch *b, int chain, int *ngrid, int *nsub);
 int fmc_batch_prob_grid(fmc_batch *b, int chain, int sub, double *out, int64_t n);
 
+
 /* Adjoint of the guest-framework interaction energy (no counterpart in the
  * reference).  For a snapshot of nmol guest molecules (one guest type; site
  * coordinates xyz, nmol x natoms x 3 doubles in DEVICE memory, A):
@@ -467,6 +468,27 @@ int fmc_adjoint_info(const fmc_adjoint *a, int *ntype, int *nsite, double *base)
 int fmc_adjoint_eval(fmc_adjoint *a, int nmol, const double *xyz, const double *params,
                      double *energy, double *gxyz, double *gparams);
 int fmc_adjoint_destroy(fmc_adjoint *a);
+
+/* The energy the chains sample, for a batch of frozen snapshots, and its
+ * adjoint.  Per snapshot q (nmol[q] molecules of the system's guest type;
+ * xyz: device pointer to every snapshot's site coordinates one after the
+ * other, FP64): E_q = the guests' real-space erfc Coulomb and Lennard-Jones
+ * terms from the reference's tables (erc, vvv, 3-point interpolation,
+ * ewald.f:703-715, vdw_terms.f:441-453) against the framework and the
+ * other molecules, the reciprocal sum of the guests with the framework and
+ * with each other without each molecule's own term, and the
+ * guest-framework Lennard-Jones tail (lrcorrect, vdw_terms.f:470-645), in
+ * kcal/mol: the sampled energy up to terms that depend only on the
+ * molecule count.  params (host, ntype x 3): framework type t's (eps_t,
+ * sigma_t, lambda_t); its pairs' parameters move from the FIELD's values
+ * as Lorentz-Berthelot mixing does and lambda_t scales its charges.
+ * Out: energy[q] (host), gxyz (device, float, 3 per site: dE/dxyz),
+ * gparams[q][t][3] (host).  precision: FMC_PREC_FP64 (pair terms and
+ * phases in FP64) or FMC_PREC_FP32 (in FP32, sums in FP64).  Orthorhombic
+ * cells, one guest type.  No counterpart in the reference. */
+int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const double *xyz,
+                           const double *params, int precision, double *energy, float *gxyz,
+                           double *gparams);
 
 /* Thread-block clusters: the chains of system i run on clusters of
  * csize[i] CTAs (1..8; default 1).  Each CTA of a cluster takes a share of

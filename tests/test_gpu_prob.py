@@ -119,7 +119,7 @@ def test_energy_grids_follow_oracle(fmc_lib, oracle_lib, tmp_path, prec, csize, 
            [(r.move, r.choice, r.accepted) for r in logs]
     assert b.prob_info(0)[1] == 3
     got = b.prob_grid(0)
-    assert sum(r.accepted for r in logs) >= 30
+    assert sum(r.accepted for r in logs) >= n // 10
     assert np.all(got[1] == 0.0) and got[2].sum() > 0
     tol = 1e-10 if prec == "fp64" else 1e-7
     assert np.allclose(got, ref, rtol=tol, atol=tol)
@@ -129,12 +129,17 @@ def test_widom_energy_grid(fmc_lib, oracle_lib, tmp_path):
     """widom_grid's test insertions fill the energy grids with their energies
     and counts (gcmc.f:2529-2532): the device grids gain what the oracle's
     storeenprob bins for the same trials (positions and energies the device
-    reports); the centre-of-mass grid is left alone."""
+    reports); the centre-of-mass grid is left alone.  The trial grid has 7
+    points a side, so that no centre falls exactly on an inner edge of the
+    probability grid's bins (2 cells of 16 bins a side against k / 7): there
+    the reference's equitable binning moves by a whole bin with the last
+    bit of the centre, which the device's fused multiply-adds and the
+    host's rounding set differently."""
     d = _energy_dir(tmp_path)
     b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 3}], precision=fmc_lib.FMC_PREC_FP64,
                       guest_capacity=64)
     before = b.prob_grid(0)
-    (henry, nok, ntot), est, ovl, xyz = b.widom_grid(0, (6, 6, 6), 2, seed=7, details=True)
+    (henry, nok, ntot), est, ovl, xyz = b.widom_grid(0, (7, 7, 7), 2, seed=7, details=True)
     after = b.prob_grid(0)
     assert nok >= 50
     o = oracle_lib.Oracle(d)
