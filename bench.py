@@ -51,7 +51,7 @@ UNIT = "evals/s"
 RHO = 192.0 / 12.8 ** 3       # framework atoms per A^3
 GUEST_REACH = 1.16            # C-O distance of the CO2 guest
 NSITE = 3                     # CO2 sites
-WORKLOAD = ("config3 batched isotherm: 64 chains = 16 pressures 0.002-1 bar x 4 frameworks "
+WORKLOAD = ("batched isotherm: 64 chains = 16 pressures 0.002-1 bar x 4 frameworks "
             "25.6/38.4/51.2/64.0 A, CO2, FP32 terms with double-float sums and S(k); every step "
             "replays the same cycle from the pre-loaded state")
 
@@ -85,7 +85,7 @@ def trial_evals(st) -> int:
 
 def workload(tmp: str):
     from fastmc_gb300 import synthetic as syn
-    chains = syn.config3_chains()
+    chains = syn.isotherm_chains()
     dirs = []
     for f in range(4):
         spec = [c for c in chains if c.fw_seed == f + 1][0]
@@ -293,7 +293,7 @@ def profiled_traffic():
     """DRAM bytes (read + write) of one step's chain-kernel launches (the
     unit `achieved` is quoted in) of this workload, from the committed ncu
     summary, if present."""
-    p = os.path.join(ROOT, "profiles", "chain_kernel_config3.json")
+    p = os.path.join(ROOT, "profiles", "chain_kernel_isotherm64.json")
     try:
         with open(p) as f:
             return json.load(f).get("dram_bytes_per_step")
@@ -456,13 +456,13 @@ def per_move_abi(F, batch, systems, dirs, specs, seconds=1.0):
                         "oracle replays the first 2000 of those moves with the same decisions"}
 
 
-def config5_widom(F, tmp):
-    """Config 5's test insertions: 1e7 Widom trials (a 100^3 grid x 10
+def widom_102A(F, tmp):
+    """Test insertions into the large framework: 1e7 Widom trials (a 100^3 grid x 10
     orientations, one launch) against the 102.4 A framework (98304 atoms,
     cutoff 14 A, kmax 20) with 2000 CO2 loaded, FP32 terms."""
     from fastmc_gb300 import synthetic as syn
-    d = os.path.join(tmp, "config5")
-    syn.write_inputs(d, syn.config5())
+    d = os.path.join(tmp, "widom102")
+    syn.write_inputs(d, syn.widom_102A())
     sysm = F.System.load(d)
     b = F.Batch([sysm], [{"seed": 5}], precision=F.FMC_PREC_FP32, guest_capacity=2048)
     b.widom_grid(0, (10, 10, 10), 1, seed=1)  # warm-up
@@ -471,7 +471,7 @@ def config5_widom(F, tmp):
     s = time.perf_counter() - t0
     return {"value": ntot / s, "unit": "trial insertions/s", "trials": ntot,
             "non_overlapping": nok, "henry": h, "seconds": s,
-            "workload": "config5: 102.4 A, 98304 atoms, 2000 CO2, cutoff 14 A, kmax 20, FP32"}
+            "workload": "102.4 A, 98304 atoms, 2000 CO2, cutoff 14 A, kmax 20, FP32"}
 
 
 def sampled_energy_adjoint(F, tmp, nsnap=4096):
@@ -489,7 +489,7 @@ def sampled_energy_adjoint(F, tmp, nsnap=4096):
     from fastmc_gb300 import synthetic as syn
     from fastmc_gb300.adjoint import Adjoint
     d = os.path.join(tmp, "snapshots51")
-    syn.write_inputs(d, syn.config2())
+    syn.write_inputs(d, syn.single_chain_51A())
     sysm = F.System.load(d)
     b = F.Batch([sysm], [{"seed": 40 + c} for c in range(8)], precision=F.FMC_PREC_FP32,
                 guest_capacity=512)
@@ -713,7 +713,7 @@ def run_ours(args, rank, world, local_rank):
             out["plain_single_chain"] = plain_paths(F, batch, systems, dirs, specs, snap, args.moves,
                                                     per_chain)
         if args.widom:
-            out["config5_widom"] = config5_widom(F, tmp)
+            out["widom_102A"] = widom_102A(F, tmp)
         if args.adjoint:
             out["sampled_energy_adjoint"] = sampled_energy_adjoint(F, tmp)
         print(json.dumps(out), flush=True)
@@ -732,7 +732,7 @@ def profile_case(args):
     from fastmc_gb300 import build
     from fastmc_gb300 import synthetic as syn
     build.build()
-    chains = syn.config3_chains()
+    chains = syn.isotherm_chains()
     sel = [(i, c) for i, c in enumerate(chains) if c.fw_seed == args.framework]
     sel = sel[args.first:args.first + args.chains]
     d = os.path.join(tempfile.mkdtemp(), "fw")
@@ -763,7 +763,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
-    ap.add_argument("--widom", action="store_true", help="also time config 5's 1e7 Widom trials")
+    ap.add_argument("--widom", action="store_true", help="also time 1e7 Widom trials against the 102.4 A framework")
     ap.add_argument("--adjoint", action="store_true",
                     help="also time the sampled-energy adjoint of 4096 snapshots (51.2 A box)")
     ap.add_argument("--speculate", type=int, default=8,

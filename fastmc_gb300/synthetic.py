@@ -276,29 +276,29 @@ def write_inputs(directory: str, spec: GcmcSpec, uc: Optional[UnitCell] = None) 
     return directory
 
 
-# --------------------------------------------------------------- the configs
-def config1() -> GcmcSpec:
+# ------------------------------------------------- the benchmark workloads
+def single_chain_25A() -> GcmcSpec:
     """Plain FP64 single chain: 2x2x2 tiling (25.6 A, 1536 atoms),
     alpha 0.26, kmax 7, T 293 K, P 0.1 bar, equal move mix, seed 1."""
     return GcmcSpec(ntile=2, fw_seed=1, alpha=0.26, kmax=7, pressure_bar=0.1,
-                    steps=100000, title="config1 25.6A 1536 atoms")
+                    steps=100000, title="single chain 25.6A 1536 atoms")
 
 
-def config2() -> GcmcSpec:
+def single_chain_51A() -> GcmcSpec:
     """Larger single chain: 4x4x4 tiling (51.2 A, 12288 atoms), 400 CO2
     pre-loaded at random non-overlapping positions, alpha 0.24, kmax 12."""
     return GcmcSpec(ntile=4, fw_seed=2, alpha=0.24, kmax=12, pressure_bar=0.1,
                     steps=1000000, create_molecules=400,
-                    title="config2 51.2A 12288 atoms")
+                    title="single chain 51.2A 12288 atoms")
 
 
-CONFIG3_TILES = (2, 3, 4, 5)
-CONFIG3_KMAX = (7, 10, 12, 18)
-CONFIG3_ALPHA = 0.24
-CONFIG3_PRESSURES = tuple(float(p) for p in np.logspace(np.log10(0.002), 0.0, 16))
+ISOTHERM_TILES = (2, 3, 4, 5)
+ISOTHERM_KMAX = (7, 10, 12, 18)
+ISOTHERM_ALPHA = 0.24
+ISOTHERM_PRESSURES = tuple(float(p) for p in np.logspace(np.log10(0.002), 0.0, 16))
 
 
-def config3_chains() -> List[GcmcSpec]:
+def isotherm_chains() -> List[GcmcSpec]:
     """Batched isotherm: 16 pressures log-spaced 0.002-1.0 bar x 4 frameworks
     (edges 25.6/38.4/51.2/64.0 A, framework seeds 1..4, kmax 7/10/12/18).
     The 64.0 A box holds 24000 atoms at the tiled density (5^3 unit cells).
@@ -306,24 +306,24 @@ def config3_chains() -> List[GcmcSpec]:
     floor(f_c * Nmax) guests, Nmax = 800 (L/64)^3 and
     f_c = ((7 c + 3 f) mod 16) / 15."""
     out = []
-    for f, (nt, km) in enumerate(zip(CONFIG3_TILES, CONFIG3_KMAX)):
+    for f, (nt, km) in enumerate(zip(ISOTHERM_TILES, ISOTHERM_KMAX)):
         L = UNIT_CELL * nt
         nmax = 800.0 * (L / 64.0) ** 3
-        for c, p in enumerate(CONFIG3_PRESSURES):
+        for c, p in enumerate(ISOTHERM_PRESSURES):
             frac = ((7 * c + 3 * f) % 16) / 15.0
-            out.append(GcmcSpec(ntile=nt, fw_seed=f + 1, alpha=CONFIG3_ALPHA,
+            out.append(GcmcSpec(ntile=nt, fw_seed=f + 1, alpha=ISOTHERM_ALPHA,
                                 kmax=km, pressure_bar=p, steps=1000000,
                                 create_molecules=int(frac * nmax),
-                                title=f"config3 fw{f + 1} {L:.1f}A P={p:.4g}bar"))
+                                title=f"isotherm fw{f + 1} {L:.1f}A P={p:.4g}bar"))
     return out
 
 
-def config5() -> GcmcSpec:
+def widom_102A() -> GcmcSpec:
     """Large framework: 8x8x8 tiling (102.4 A, 98304 atoms), 2000 CO2,
     cutoff 14 A, alpha 0.22, kmax 20."""
     return GcmcSpec(ntile=8, fw_seed=5, alpha=0.22, kmax=20, cutoff=14.0,
                     pressure_bar=0.1, steps=10000000, create_molecules=2000,
-                    title="config5 102.4A 98304 atoms")
+                    title="widom 102.4A 98304 atoms")
 
 
 def small_test_spec(seed: int = 7, kmax: int = 5, ntile: int = 2,

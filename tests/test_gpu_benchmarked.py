@@ -13,7 +13,7 @@ exact set-up is checked:
   energy before the move, 1 kcal/mol);
 - an FP64 chain on a 4-CTA cluster of the 64 A / kmax 18 framework matches
   the oracle to 1e-9 with identical decisions;
-- config 1 (25.6 A, kmax 7, alpha 0.26, 0.1 bar, seed 1): an FP64 device
+- the single 25.6 A chain (kmax 7, alpha 0.26, 0.1 bar, seed 1): an FP64 device
   chain makes the same decisions as the oracle for 1e5 moves.  The chain
   starts empty and, at 0.1 bar in this pore-free framework, stays empty:
   all 1e5 moves are insertions, about 300 of them free of overlap (full
@@ -34,9 +34,9 @@ MOVES = 256
 
 
 @pytest.fixture(scope="module")
-def config3(tmp_path_factory):
-    base = tmp_path_factory.mktemp("config3")
-    chains = syn.config3_chains()
+def isotherm(tmp_path_factory):
+    base = tmp_path_factory.mktemp("isotherm")
+    chains = syn.isotherm_chains()
     dirs = []
     for f in range(4):
         spec = [c for c in chains if c.fw_seed == f + 1][0]
@@ -55,8 +55,8 @@ def _oracle_runs(jobs):
         return pool.map(replay.chain_moves, jobs)
 
 
-def test_config3_fp32_clusters_follow_oracle(fmc_lib, oracle_lib, config3):
-    dirs, specs = config3
+def test_isotherm_fp32_clusters_follow_oracle(fmc_lib, oracle_lib, isotherm):
+    dirs, specs = isotherm
     systems = [fmc_lib.System.load(d) for d in dirs]
     b = fmc_lib.Batch(systems, specs, precision=fmc_lib.FMC_PREC_FP32, guest_capacity=1024)
     b.set_cluster(BENCH_CLUSTERS)
@@ -91,8 +91,8 @@ def test_config3_fp32_clusters_follow_oracle(fmc_lib, oracle_lib, config3):
     assert nfull >= 2000 and nchk >= 0.8 * len(specs) * MOVES
 
 
-def test_fp64_cluster4_64A_kmax18_matches_oracle(fmc_lib, oracle_lib, config3):
-    dirs, specs = config3
+def test_fp64_cluster4_64A_kmax18_matches_oracle(fmc_lib, oracle_lib, isotherm):
+    dirs, specs = isotherm
     chain = [s for s in specs if s["system"] == 3 and 80 <= s["create_molecules"] <= 400][0]
     sysm = fmc_lib.System.load(dirs[3])
     b = fmc_lib.Batch([sysm], [{**chain, "system": 0}], precision=fmc_lib.FMC_PREC_FP64,
@@ -114,10 +114,10 @@ def test_fp64_cluster4_64A_kmax18_matches_oracle(fmc_lib, oracle_lib, config3):
     assert nfull >= 50
 
 
-def test_config1_fp64_1e5_moves(fmc_lib, oracle_lib, tmp_path):
+def test_single_chain_25A_fp64_1e5_moves(fmc_lib, oracle_lib, tmp_path):
     n = 100000
-    d = str(tmp_path / "config1")
-    syn.write_inputs(d, syn.config1())
+    d = str(tmp_path / "single25")
+    syn.write_inputs(d, syn.single_chain_25A())
     o = oracle_lib.Oracle(d)
     o.seed(1)
     ref = o.run(n)

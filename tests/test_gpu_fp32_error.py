@@ -78,12 +78,12 @@ def _errors(o, eng, n, box, ntrial, seed):
     return out, mism
 
 
-@pytest.mark.parametrize("case", ["config1", "config2_100"])
+@pytest.mark.parametrize("case", ["25A", "51A_100"])
 def test_fp32_delta_e_error(fmc_lib, oracle_lib, inputs_dir, case):
-    if case == "config1":
-        spec, ncreate, box = syn.config1(), 20, 25.6
+    if case == "25A":
+        spec, ncreate, box = syn.single_chain_25A(), 20, 25.6
     else:
-        spec, ncreate, box = syn.config2(), 100, 51.2
+        spec, ncreate, box = syn.single_chain_51A(), 100, 51.2
     d = inputs_dir(spec, "fp32err_" + case)
     o, eng, n = _state(oracle_lib, fmc_lib, d, ncreate, seed=5)
     assert n == ncreate

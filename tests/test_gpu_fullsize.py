@@ -35,8 +35,8 @@ def _random_molecule(rng, box):
     return np.outer(TMPL, ax) + rng.uniform(0, box, 3)
 
 
-def test_config2_full_size_per_move(fmc_lib, oracle_lib, inputs_dir):
-    d = inputs_dir(syn.config2(), "full_config2")
+def test_51A_full_size_per_move(fmc_lib, oracle_lib, inputs_dir):
+    d = inputs_dir(syn.single_chain_51A(), "full_51A")
     _, xyz = _loaded(fmc_lib, d, 400)
     o = oracle_lib.Oracle(d)
     sysm = fmc_lib.System.load(d)
@@ -87,8 +87,8 @@ def test_config2_full_size_per_move(fmc_lib, oracle_lib, inputs_dir):
     assert ndis >= 5
 
 
-def test_config5_full_size_widom(fmc_lib, oracle_lib, inputs_dir):
-    d = inputs_dir(syn.config5(), "full_config5")
+def test_102A_full_size_widom(fmc_lib, oracle_lib, inputs_dir):
+    d = inputs_dir(syn.widom_102A(), "full_102A")
     b, xyz = _loaded(fmc_lib, d, 2000)
     o = oracle_lib.Oracle(d)
     for m in xyz:

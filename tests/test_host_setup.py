@@ -29,12 +29,12 @@ def test_library_exports_every_header_symbol(fmc_lib):
     assert lib.fmc_version().startswith(b"fastmc_gb300")
 
 
-@pytest.mark.parametrize("which", ["calf20", "config1", "small"])
+@pytest.mark.parametrize("which", ["calf20", "single25", "small"])
 def test_setup_matches_oracle(fmc_lib, oracle_lib, inputs_dir, which):
     if which == "calf20":
         d = CALF20
-    elif which == "config1":
-        d = inputs_dir(syn.config1(), "cfg1")
+    elif which == "single25":
+        d = inputs_dir(syn.single_chain_25A(), "cfg1")
     else:
         d = inputs_dir(syn.small_test_spec(seed=9, kmax=6, create=5), "small9")
     s = fmc_lib.System.load(d)
@@ -50,7 +50,7 @@ def test_setup_matches_oracle(fmc_lib, oracle_lib, inputs_dir, which):
 
 
 def test_tables_match_oracle(fmc_lib, oracle_lib, inputs_dir):
-    d = inputs_dir(syn.config1(), "cfg1")
+    d = inputs_dir(syn.single_chain_25A(), "cfg1")
     orc = oracle_lib.Oracle(d)
     out = np.zeros(2000)
     n = orc.lib.orc_get_erc(orc._h, out.ctypes.data_as(C.POINTER(C.c_double)), 2000)
@@ -84,7 +84,7 @@ def test_synthetic_framework_properties():
     assert np.bincount(uc.types).tolist() == [48, 48, 48, 48]
     assert np.all((uc.eps >= 0.02) & (uc.eps <= 0.10))
     assert np.all((uc.sigma >= 2.5) & (uc.sigma <= 3.8))
-    chains = syn.config3_chains()
+    chains = syn.isotherm_chains()
     assert len(chains) == 64
     assert sorted({round(c.box, 6) for c in chains}) == [25.6, 38.4, 51.2, 64.0]
 
