@@ -477,9 +477,10 @@ def widom_102A(F, tmp):
 def sampled_energy_adjoint(F, tmp, nsnap=4096):
     """The sampled energy and its adjoint over a batch of frozen snapshots of
     the 51.2 A framework (12288 atoms, cutoff 12.5 A, alpha 0.24, kmax 12):
-    8 FP32 chains pre-loaded with 400 CO2 and run 2000 moves each give the
-    states; snapshot q keeps the first N_q (uniform 50-400) molecules of a
-    random order of state q mod 8.  One call (fmc_adjoint_eval_batch, FP32
+    8 FP32 chains pre-loaded with 400 CO2 and run 100 moves each give the
+    states (at 0.1 bar a longer run empties them); snapshot q keeps N_q
+    (uniform 50-400, at most the state's count) molecules of a random order
+    of state q mod 8.  One call (fmc_adjoint_eval_batch, FP32
     pair terms and phases, FP64 sums) returns every snapshot's energy,
     dE/d(guest coordinates) (3N x FP32) and dE/d(eps, sigma, lambda) of the 4
     framework types; the FP64 call on the same batch gives the reference
@@ -493,7 +494,7 @@ def sampled_energy_adjoint(F, tmp, nsnap=4096):
     sysm = F.System.load(d)
     b = F.Batch([sysm], [{"seed": 40 + c} for c in range(8)], precision=F.FMC_PREC_FP32,
                 guest_capacity=512)
-    b.run(2000)
+    b.run(100)
     states = []
     for c in range(8):
         x, n = b.coords(c)

@@ -83,13 +83,14 @@ class Adjoint:
             raise ValueError("params must have shape (%d, 3)" % self.ntype)
         prec = L.FMC_PREC_FP32 if precision == "fp32" else L.FMC_PREC_FP64
         gx = torch.empty(x.shape, dtype=torch.float32, device=x.device)
+        xp = C.c_void_p(x.data_ptr()) if x.numel() else None
+        gxp = C.c_void_p(gx.data_ptr()) if gx.numel() else None
         e = np.zeros(max(1, nm.size))
         gp = np.zeros(max(1, nm.size) * 3 * self.ntype)
         torch.cuda.synchronize(x.device)
         L.check(L.load().fmc_adjoint_eval_batch(
-            self._h, int(nm.size), nm.ctypes.data_as(L.ip), C.c_void_p(x.data_ptr()),
-            p.ctypes.data_as(L.dp), prec, e.ctypes.data_as(L.dp), C.c_void_p(gx.data_ptr()),
-            gp.ctypes.data_as(L.dp)))
+            self._h, int(nm.size), nm.ctypes.data_as(L.ip), xp, p.ctypes.data_as(L.dp), prec,
+            e.ctypes.data_as(L.dp), gxp, gp.ctypes.data_as(L.dp)))
         return e[:nm.size], gx, gp[:nm.size * 3 * self.ntype].reshape(nm.size, self.ntype, 3)
 
     def close(self) -> None:

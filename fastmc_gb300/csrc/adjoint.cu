@@ -256,9 +256,13 @@ __global__ void adj_recip_site_kernel(AdjConst c, const int4 *__restrict__ klmn,
 // erfc Coulomb and Lennard-Jones terms from the reference's tables (erc and
 // vvv with the 3-point interpolation, ewald.f:703-715, vdw_terms.f:441-453)
 // against the framework and against the other molecules, the reciprocal sum
-// of the guests against the framework and each other without each
-// molecule's own term, and the guest-framework Lennard-Jones tail
-// (lrcorrect, vdw_terms.f:470-645).  Framework type t's (eps_t, sigma_t)
+// of the guests against the framework and the guests (each molecule's own
+// |s_m|^2 included), and the guest-framework Lennard-Jones tail (lrcorrect,
+// vdw_terms.f:470-645).  Left out are the terms that no coordinate or
+// parameter moves: a constant per molecule (the excluded intramolecular
+// pairs, ewald3, and the Ewald self energy), the framework's own energy
+// (it does move with lambda, but equally in every snapshot) and the
+// guest-guest tail.  Framework type t's (eps_t, sigma_t)
 // move its pairs' parameters from the FIELD's values as Lorentz-Berthelot
 // mixing does (eps x sqrt(eps_t / eps_t0), sigma + (sigma_t - sigma_t0)/2),
 // so the tables at the base parameters are the system's own; lambda_t
@@ -476,8 +480,10 @@ __device__ __forceinline__ void ham_phase(const int4 l, const double *xyz, const
 }
 
 // The guests' structure factor of every snapshot (block x), k per thread: S_g, and
-// the reciprocal energy K a_k [2 Re(S_g conj(S_fw)) + |S_g|^2 - sum_m |s_m|^2]
-// with S_fw = sum_t lambda_t S_t, dE/dlambda_t = K a_k 2 Re(S_g conj(S_t)).
+// the reciprocal energy K a_k [2 Re(S_g conj(S_fw)) + |S_g|^2] with S_fw =
+// sum_t lambda_t S_t, dE/dlambda_t = K a_k 2 Re(S_g conj(S_t)).  |S_g|^2
+// keeps each molecule's own |s_m|^2: it depends on the orientation (a
+// finite k set), and the reference's insertion energy carries it.
 template <class T>
 __global__ void __launch_bounds__(kHT) ham_sk_kernel(HamConst c, const int4 *__restrict__ klmn,
                                                      const double *__restrict__ akk,
@@ -494,20 +500,19 @@ __global__ void __launch_bounds__(kHT) ham_sk_kernel(HamConst c, const int4 *__r
   for (int q = 0; q < NV; ++q) v[q] = 0.0;
   if (k < c.nk) {
     const int4 l = klmn[k];
-    double Sr = 0.0, Si = 0.0, self = 0.0;
+    double Sr = 0.0, Si = 0.0;
     const int m0 = snap_mol0[snap], nm = snap_nmol[snap];
     for (int mm = m0; mm < m0 + nm; ++mm) {
-      double sr = 0.0, si = 0.0;
+      T sr = T(0), si = T(0);  // one molecule in T, the snapshot's sum in FP64
       for (int s = 0; s < ns; ++s) {
         const size_t i = (size_t)mm * ns + s;
         T cs, sn;
         ham_phase<T>(l, xyz + 3 * i, fr + 3 * i, c.rL[0], c.rL[1], c.rL[2], cs, sn);
-        sr += c.qs[s] * (double)cs;
-        si += c.qs[s] * (double)sn;
+        sr += (T)c.qs[s] * cs;
+        si += (T)c.qs[s] * sn;
       }
-      Sr += sr;
-      Si += si;
-      self += sr * sr + si * si;
+      Sr += (double)sr;
+      Si += (double)si;
     }
     double Fr = 0.0, Fi = 0.0;
     const double f = c.krecip * akk[k] * c.rengunit;
@@ -517,7 +522,7 @@ __global__ void __launch_bounds__(kHT) ham_sk_kernel(HamConst c, const int4 *__r
       Fi += c.lam[t] * st.y;
       v[1 + 3 * t + 2] = 2.0 * f * (Sr * st.x + Si * st.y);
     }
-    v[0] = f * (2.0 * (Sr * Fr + Si * Fi) + (Sr * Sr + Si * Si) - self);
+    v[0] = f * (2.0 * (Sr * Fr + Si * Fi) + (Sr * Sr + Si * Si));
     sg[(size_t)snap * c.nk + k] = make_double2(Sr + Fr, Si + Fi);  // S_g + S_fw
   }
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
@@ -535,10 +540,9 @@ __global__ void __launch_bounds__(kHT) ham_sk_kernel(HamConst c, const int4 *__r
   }
 }
 
-// Reciprocal site gradients, one thread per molecule (its sites' phases
-// give its own s_m): dE/dr_i = -2 K q_i sum_k a_k k Im(e^{i phi_i} conj(W)),
-// W = S_fw + S_g - s_m; added to the real-space gradients and stored as
-// float (3N x FP32).
+// Reciprocal site gradients, one thread per molecule: dE/dr_i = -2 K q_i
+// sum_k a_k k Im(e^{i phi_i} conj(W)), W = S_fw + S_g; added to the
+// real-space gradients and stored as float (3N x FP32).
 template <class T>
 __global__ void ham_recip_grad_kernel(HamConst c, const int4 *__restrict__ klmn,
                                       const double *__restrict__ akk, const double2 *__restrict__ sg,
@@ -552,18 +556,16 @@ __global__ void ham_recip_grad_kernel(HamConst c, const int4 *__restrict__ klmn,
   for (int s = 0; s < kMaxASite; ++s) g[s][0] = g[s][1] = g[s][2] = 0.0;
   for (int k = 0; k < c.nk; ++k) {
     const int4 l = klmn[k];
-    double cs[kMaxASite], sn[kMaxASite], sr = 0.0, si = 0.0;
+    double cs[kMaxASite], sn[kMaxASite];
     for (int s = 0; s < ns; ++s) {
       const size_t i = (size_t)m * ns + s;
       T a, b;
       ham_phase<T>(l, xyz + 3 * i, fr + 3 * i, c.rL[0], c.rL[1], c.rL[2], a, b);
       cs[s] = (double)a;
       sn[s] = (double)b;
-      sr += c.qs[s] * cs[s];
-      si += c.qs[s] * sn[s];
     }
     const double2 w0 = sg[(size_t)snap * c.nk + k];
-    const double wr = w0.x - sr, wi = w0.y - si;
+    const double wr = w0.x, wi = w0.y;
     const double f = -2.0 * c.krecip * akk[k];
     const double kx = 2.0 * kPi * l.x * c.rL[0], ky = 2.0 * kPi * l.y * c.rL[1],
                  kz = 2.0 * kPi * l.z * c.rL[2];
@@ -823,8 +825,7 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
                            const double *params, int precision, double *energy, float *gxyz,
                            double *gparams) {
   return aguard([&] {
-    if (!a || (nsnap > 0 && (!nmol || !xyz || !params || !energy || !gxyz || !gparams)))
-      raise(FMC_ERR_ARG, "null argument");
+    if (!a || (nsnap > 0 && (!nmol || !params || !energy || !gparams))) raise(FMC_ERR_ARG, "null argument");
     if (nsnap < 0) raise(FMC_ERR_ARG, "negative snapshot count");
     if (precision != FMC_PREC_FP32 && precision != FMC_PREC_FP64) raise(FMC_ERR_ARG, "bad precision");
     HamConst h = a->h;
@@ -845,6 +846,7 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
       if (total * ns > (1LL << 26)) raise(FMC_ERR_CAPACITY, "too many guest sites in one batch");
       for (int i = 0; i < nmol[q]; ++i) mol_snap.push_back(q);
     }
+    if (total > 0 && (!xyz || !gxyz)) raise(FMC_ERR_ARG, "null argument");
     // the guest-framework tables at these parameters (forgen's expression,
     // vdw_terms.f:181-234, with Lorentz-Berthelot moves of the FIELD's pair
     // values) and their sigma derivatives

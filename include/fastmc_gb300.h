@@ -476,10 +476,12 @@ int fmc_adjoint_destroy(fmc_adjoint *a);
  * terms from the reference's tables (erc, vvv, 3-point interpolation,
  * ewald.f:703-715, vdw_terms.f:441-453) against the framework and the
  * other molecules, the reciprocal sum of the guests with the framework and
- * with each other without each molecule's own term, and the
- * guest-framework Lennard-Jones tail (lrcorrect, vdw_terms.f:470-645), in
- * kcal/mol: the sampled energy up to terms that depend only on the
- * molecule count.  params (host, ntype x 3): framework type t's (eps_t,
+ * with each other (each molecule's own |s_m|^2 included: it turns with the
+ * molecule), and the guest-framework Lennard-Jones tail (lrcorrect,
+ * vdw_terms.f:470-645), in kcal/mol: the sampled energy up to terms that
+ * depend only on the molecule count (the framework's own energy also on
+ * lambda, equally in every snapshot).  xyz and gxyz may be null when every
+ * snapshot is empty.  params (host, ntype x 3): framework type t's (eps_t,
  * sigma_t, lambda_t); its pairs' parameters move from the FIELD's values
  * as Lorentz-Berthelot mixing does and lambda_t scales its charges.
  * Out: energy[q] (host), gxyz (device, float, 3 per site: dE/dxyz),

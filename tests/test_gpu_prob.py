@@ -1,6 +1,8 @@
 """Probability grids (storeprob, utility_pack.f:621-687) accumulated on the
 device after every production move, against the oracle's grids for the
 same chain."""
+import os
+
 import numpy as np
 import pytest
 
@@ -93,6 +95,18 @@ def _energy_dir(tmp_path):
     spec.grid_spacing = 0.8
     d = str(tmp_path / "egrid")
     syn.write_inputs(d, spec, uc=syn.make_unit_cell(4, natoms=48))
+    # the guest's sites moved off its centre (the reference's set-up leaves
+    # half of that offset in the template): test insertions at grid points
+    # then have their centres off the cell's faces, where the binning wraps
+    # and the last bit of the centre picks the bins
+    path = os.path.join(d, "FIELD")
+    lines = open(path).read().split("\n")
+    i0 = next(i for i, l in enumerate(lines) if l.startswith("&guest CO2"))
+    for i in range(i0 + 3, i0 + 6):
+        w = lines[i].split()
+        x, y, z = float(w[3]) + 0.4, float(w[4]) + 0.3, float(w[5]) + 0.2
+        lines[i] = f"{w[0]:<8s}{float(w[1]):14.6f}{float(w[2]):14.6f}{x:14.6f}{y:14.6f}{z:14.6f}"
+    open(path, "w").write("\n".join(lines))
     return d
 
 
@@ -129,12 +143,12 @@ def test_widom_energy_grid(fmc_lib, oracle_lib, tmp_path):
     """widom_grid's test insertions fill the energy grids with their energies
     and counts (gcmc.f:2529-2532): the device grids gain what the oracle's
     storeenprob bins for the same trials (positions and energies the device
-    reports); the centre-of-mass grid is left alone.  The trial grid has 7
-    points a side, so that no centre falls exactly on an inner edge of the
-    probability grid's bins (2 cells of 16 bins a side against k / 7): there
-    the reference's equitable binning moves by a whole bin with the last
-    bit of the centre, which the device's fused multiply-adds and the
-    host's rounding set differently."""
+    reports); the centre-of-mass grid is left alone.  No centre sits exactly on
+    a bin edge (the guest's centre is off its rotation origin, and the grid
+    has 7 points a side against 16 bins a cell): there the reference's
+    equitable binning moves by a whole bin with the last bit of the centre,
+    which the device's fused multiply-adds and the host's rounding set
+    differently."""
     d = _energy_dir(tmp_path)
     b = fmc_lib.Batch([fmc_lib.System.load(d)], [{"seed": 3}], precision=fmc_lib.FMC_PREC_FP64,
                       guest_capacity=64)

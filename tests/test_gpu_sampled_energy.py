@@ -137,6 +137,12 @@ def test_fp32_against_fp64_and_single_snapshots(batch):
         assert torch.allclose(g1, g64[o:o + n])
         assert np.allclose(pp1[0], p64[q], rtol=1e-10, atol=1e-10 * np.abs(p64[q]).max())
         o += n
+    # empty snapshots: nothing but zeros, also between others
+    e0, g0, pz = adj.evaluate_batch(x[:0], [0, 0], p0, "fp64")
+    assert np.all(e0 == 0.0) and np.all(pz == 0.0) and g0.numel() == 0
+    e2, g2, p2 = adj.evaluate_batch(x[:nm[0]], [0, nm[0], 0], p0, "fp64")
+    assert e2[0] == 0.0 and e2[2] == 0.0 and math.isclose(e2[1], e64[0], rel_tol=1e-12, abs_tol=1e-9)
+    assert torch.allclose(g2, g64[:nm[0]])
 
 
 def test_autograd_over_a_batch(batch):
