@@ -526,8 +526,8 @@ def sampled_energy_adjoint(F, tmp, nsnap=4096):
             "max_rel_energy_err_fp32": float(np.max(np.abs(e32 - e64) / np.abs(e64))),
             "max_site_grad_err_fp32_rel_to_max": float(np.abs(g32n - g64n).max() / np.abs(g64n).max()),
             "max_param_grad_rel_err_fp32": float(np.max(np.abs(p32 - p64)) / np.abs(p64).max()),
-            "workload": "4096 snapshots, 51.2 A, 12288 framework atoms, 50-400 CO2, cutoff 12.5 A, "
-                        "kmax 12, FP32 terms"}
+            "workload": f"{nsnap} snapshots, 51.2 A, 12288 framework atoms, 50-400 CO2, "
+                        "cutoff 12.5 A, kmax 12, FP32 terms"}
 
 
 # ------------------------------------------------------------------ arms
@@ -716,7 +716,7 @@ def run_ours(args, rank, world, local_rank):
         if args.widom:
             out["widom_102A"] = widom_102A(F, tmp)
         if args.adjoint:
-            out["sampled_energy_adjoint"] = sampled_energy_adjoint(F, tmp)
+            out["sampled_energy_adjoint"] = sampled_energy_adjoint(F, tmp, args.snapshots)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -767,6 +767,9 @@ def main():
     ap.add_argument("--widom", action="store_true", help="also time 1e7 Widom trials against the 102.4 A framework")
     ap.add_argument("--adjoint", action="store_true",
                     help="also time the sampled-energy adjoint of 4096 snapshots (51.2 A box)")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="time only the sampled-energy adjoint and print its JSON line")
+    ap.add_argument("--snapshots", type=int, default=4096, help="snapshots of the adjoint batch")
     ap.add_argument("--speculate", type=int, default=8,
                     help="speculative proposals per round at most (2..8; 0: off); the chains' "
                          "moves are the same either way")
@@ -784,6 +787,11 @@ def main():
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args)
+        return
+    if args.adjoint_only:
+        import fastmc_gb300 as F
+        with tempfile.TemporaryDirectory() as tmp:
+            print(json.dumps(sampled_energy_adjoint(F, tmp, args.snapshots)), flush=True)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
