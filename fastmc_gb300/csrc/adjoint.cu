@@ -267,13 +267,17 @@ __global__ void adj_recip_site_kernel(AdjConst c, const int4 *__restrict__ klmn,
 // mixing does (eps x sqrt(eps_t / eps_t0), sigma + (sigma_t - sigma_t0)/2),
 // so the tables at the base parameters are the system's own; lambda_t
 // scales the type's charges.  Pair terms in T (float or double), sums in
-// FP64.
+// FP64.  In float, a pair's separation is formed from hi/lo float pairs of
+// the two positions (the minimum image taken off exactly), so it carries
+// the relative error of one float rounding, as the trial-move path's.
 
 constexpr int kHT = 256;  // threads per block, Hamiltonian kernels
+constexpr int kHW = kHT / 32;
 
 struct HamConst {
   double L[3], rL[3];
-  double rc2, chg_r4e, rengunit, krecip, rdrewd, rdlrpot;
+  float Lh[3], Ll[3], rLf[3];
+  double rc2, rengunit, krecip, rdrewd, rdlrpot;
   int mxegrd, tabstride, nfw, ns, ntype, nk, nc[3];
   double chgea[kMaxASite], qs[kMaxASite];
   int gg_row[kMaxASite][kMaxASite];  // guest-guest LJ table row, -1 without
@@ -281,12 +285,24 @@ struct HamConst {
   double lam[kMaxAType];
 };
 
-// The 3-point interpolation and its derivative in r.
+// The 3-point interpolation, and with interp_d its derivative in r.
+template <class T>
+__device__ __forceinline__ T interp(const T *tab, T r, T rd, int mx) {
+  const T t = r * rd;
+  const int l = int(t);
+  if (l < 1 || l > mx) return T(0);
+  const T p = t - T(l);
+  const T v0 = tab[l], v1 = tab[l + 1], v2 = tab[l + 2];
+  const T t1 = v0 + (v1 - v0) * p;
+  const T t2 = v1 + (v2 - v1) * (p - T(1));
+  return t1 + (t2 - t1) * p * T(0.5);
+}
+
 template <class T>
 __device__ __forceinline__ T interp_d(const T *tab, T r, T rd, int mx, T &dv) {
   const T t = r * rd;
   const int l = int(t);
-  if (l < 1 || l + 2 > mx + 2) {
+  if (l < 1 || l > mx) {
     dv = T(0);
     return T(0);
   }
@@ -299,157 +315,272 @@ __device__ __forceinline__ T interp_d(const T *tab, T r, T rd, int mx, T &dv) {
   return t1 + (t2 - t1) * p * T(0.5);
 }
 
-// Real space, one block per molecule of the batch: its sites against the
-// framework atoms of the 27 neighbour cells (cells at least rc wide, or
-// every atom when the box holds fewer than three) and against every site
-// of the snapshot's other molecules (each pair's energy halved: the other
-// molecule's block sees it too).  The energy and dE/d(eps, sigma, lambda)
-// per type go to the snapshot's sums; the molecule's site gradients are
-// stored (FP64).  T: the type of the pair terms.
+template <class T>
+__device__ __forceinline__ T warp_sum(T x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+__device__ __forceinline__ void split_hl(double x, float &h, float &l) {
+  h = (float)x;
+  l = (float)(x - (double)h);
+}
+
+// a - b to the nearest image along one axis, a and b as hi/lo float pairs
+// in [0, L): the hi difference with its exact rounding error (two-sum),
+// the image taken off the hi part (exact: it is within a factor two of the
+// cell edge), then the low parts.
+__device__ __forceinline__ float mi_hl(float ah, float al, float bh, float bl, float Lh, float Ll,
+                                       float rL) {
+  const float t = ah - bh;
+  const float bb = t - ah;
+  const float e = (ah - (t - bb)) + (-bh - bb);
+  const float n = rintf(t * rL);
+  return (t - n * Lh) + ((e + (al - bl)) - n * Ll);
+}
+
+// Real space, one block per molecule of the batch.  Framework: the atoms
+// are sorted by (cell, type); a warp takes one (site, neighbour cell, type)
+// entry at a time -- the site shifted by the cell's image, one table row,
+// the type's sums -- its lanes the entry's atoms, and adds the warp's sums
+// to its own shared accumulators.  Cells at least rc wide, or with fewer
+// than three a side every cell with the nearest image per pair.  Guests:
+// threads over the snapshot's other molecules, each pair's energy halved
+// (the other molecule's block sees it too).  The molecule's site gradients
+// are stored (FP64); the snapshot's energy and dE/d(eps, sigma, lambda) per
+// type are added to its sums.  T: the type of the pair terms.
 template <class T>
 __global__ void __launch_bounds__(kHT) ham_real_kernel(
-    HamConst c, const double4 *__restrict__ fw, const int *__restrict__ fwt,
-    const int *__restrict__ cstart, const double *__restrict__ xyz, const int *__restrict__ mol_snap,
+    HamConst c, const double4 *__restrict__ fw, const float4 *__restrict__ fwh,
+    const float4 *__restrict__ fwl, const int *__restrict__ cstart, const double *__restrict__ xyz,
+    const float2 *__restrict__ cw, const int *__restrict__ mol_snap,
     const int *__restrict__ snap_mol0, const int *__restrict__ snap_nmol, const T *__restrict__ erc,
     const T *__restrict__ vt, const T *__restrict__ ds, const T *__restrict__ vgg, double *g64,
     double *esnap, double *psnap) {
-  constexpr int NV = 1 + 3 * kMaxAType;
-  __shared__ double sh[(kHT / 32) * NV];
-  __shared__ int cell_id[27], cell_pref[28];
-  __shared__ double site[kMaxASite][3];
-  const int m = blockIdx.x, snap = mol_snap[m], ns = c.ns;
-  if (threadIdx.x < 3 * ns) site[threadIdx.x / 3][threadIdx.x % 3] = xyz[(size_t)m * ns * 3 + threadIdx.x];
-  double v[NV];
-  for (int q = 0; q < NV; ++q) v[q] = 0.0;
-  double g[kMaxASite][3];
-  for (int s = 0; s < kMaxASite; ++s) g[s][0] = g[s][1] = g[s][2] = 0.0;
+  constexpr bool F32 = sizeof(T) == 4;
+  __shared__ double acc_p[kHW][kMaxAType][3];  // per warp and type: LJ, dLJ/dsigma, Coulomb / lambda
+  __shared__ double acc_g[kHW][kMaxASite][3];  // per warp: site gradients
+  __shared__ double acc_e[kHW];                // per warp: guest-guest energy
+  __shared__ double site[kMaxASite][3];        // the molecule's sites, wrapped into the cell
+  __shared__ double spos[kMaxASite][27][3];    // a site less a neighbour cell's image
+  __shared__ int cell_of[kMaxASite][27];
+  const int m = blockIdx.x, snap = mol_snap[m], ns = c.ns, T_ = c.ntype;
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < kHW * kMaxAType * 3; i += kHT) (&acc_p[0][0][0])[i] = 0.0;
+  for (int i = threadIdx.x; i < kHW * kMaxASite * 3; i += kHT) (&acc_g[0][0][0])[i] = 0.0;
+  if (threadIdx.x < kHW) acc_e[threadIdx.x] = 0.0;
+  if (threadIdx.x < 3 * ns) {
+    const int d = threadIdx.x % 3;
+    const double x = xyz[(size_t)m * ns * 3 + threadIdx.x];
+    site[threadIdx.x / 3][d] = x - c.L[d] * floor(x * c.rL[d]);
+  }
   __syncthreads();
-  const T rd = (T)c.rdrewd, rdl = (T)c.rdlrpot;
   const bool cells = c.nc[0] >= 3 && c.nc[1] >= 3 && c.nc[2] >= 3;
-  for (int s = 0; s < ns; ++s) {
-    int total = c.nfw;  // candidate framework atoms of site s
-    if (cells) {
-      if (threadIdx.x < 27) {
-        int ic[3], w[3];
-        for (int d = 0; d < 3; ++d) {
-          double f = site[s][d] * c.rL[d];
-          f -= floor(f);
-          ic[d] = min(c.nc[d] - 1, (int)(f * c.nc[d]));
+  if (cells) {
+    for (int p = threadIdx.x; p < ns * 27; p += kHT) {
+      const int s = p / 27, q = p % 27;
+      const int o[3] = {q / 9 - 1, (q / 3) % 3 - 1, q % 3 - 1};
+      int w[3];
+      for (int d = 0; d < 3; ++d) {
+        const int ic = min(c.nc[d] - 1, (int)(site[s][d] * c.rL[d] * c.nc[d]));
+        w[d] = ic + o[d];
+        double shift = 0.0;
+        if (w[d] < 0) {
+          w[d] += c.nc[d];
+          shift = -c.L[d];
+        } else if (w[d] >= c.nc[d]) {
+          w[d] -= c.nc[d];
+          shift = c.L[d];
         }
-        const int o[3] = {(int)threadIdx.x / 9 - 1, ((int)threadIdx.x / 3) % 3 - 1, (int)threadIdx.x % 3 - 1};
-        for (int d = 0; d < 3; ++d) w[d] = (ic[d] + o[d] + c.nc[d]) % c.nc[d];
-        cell_id[threadIdx.x] = (w[0] * c.nc[1] + w[1]) * c.nc[2] + w[2];
+        spos[s][q][d] = site[s][d] - shift;
       }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        cell_pref[0] = 0;
-        for (int q = 0; q < 27; ++q)
-          cell_pref[q + 1] = cell_pref[q] + cstart[cell_id[q] + 1] - cstart[cell_id[q]];
-      }
-      __syncthreads();
-      total = cell_pref[27];
+      cell_of[s][q] = (w[0] * c.nc[1] + w[1]) * c.nc[2] + w[2];
     }
-    const T ca = (T)c.chgea[s];
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      int j = t;
-      if (cells) {
-        int q = 0;
-        while (cell_pref[q + 1] <= t) ++q;
-        j = cstart[cell_id[q]] + (t - cell_pref[q]);
+  }
+  __syncthreads();
+  const T rd = (T)c.rdrewd, rdl = (T)c.rdlrpot, rc2 = (T)c.rc2;
+  const int ncell = c.nc[0] * c.nc[1] * c.nc[2];
+  const int nslot = cells ? 27 : ncell;
+  const int ne = ns * nslot * T_;
+  for (int e = wq; e < ne; e += kHW) {  // one (site, cell, type) entry per warp
+    const int t = e % T_, sq = e / T_, s = sq / nslot, q = sq % nslot;
+    const int cell = cells ? cell_of[s][q] : q;
+    const int j0 = cstart[cell * T_ + t], j1 = cstart[cell * T_ + t + 1];
+    if (j0 == j1) continue;
+    const T *row = vt + ((size_t)s * T_ + t) * c.tabstride;
+    const T *drow = ds + ((size_t)s * T_ + t) * c.tabstride;
+    const T ca = (T)c.chgea[s], lam = (T)c.lam[t];
+    double px = cells ? spos[s][q][0] : site[s][0], py = cells ? spos[s][q][1] : site[s][1],
+           pz = cells ? spos[s][q][2] : site[s][2];
+    float xh, xl, yh, yl, zh, zl;
+    split_hl(px, xh, xl);
+    split_hl(py, yh, yl);
+    split_hl(pz, zh, zl);
+    T plj = 0, pds = 0, pco = 0, gx = 0, gy = 0, gz = 0;
+    for (int j = j0 + lane; j < j1; j += 32) {
+      T dx, dy, dz, qa;
+      if (F32 && cells) {
+        const float4 ah = fwh[j], al = fwl[j];
+        dx = (T)((xh - ah.x) + (xl - al.x));
+        dy = (T)((yh - ah.y) + (yl - al.y));
+        dz = (T)((zh - ah.z) + (zl - al.z));
+        qa = (T)ah.w;
+      } else {
+        const double4 a = fw[j];
+        double ex = px - a.x, ey = py - a.y, ez = pz - a.z;
+        if (!cells) {
+          ex -= c.L[0] * rint(ex * c.rL[0]);
+          ey -= c.L[1] * rint(ey * c.rL[1]);
+          ez -= c.L[2] * rint(ez * c.rL[2]);
+        }
+        dx = (T)ex;
+        dy = (T)ey;
+        dz = (T)ez;
+        qa = (T)a.w;
       }
-      const double4 a = fw[j];
-      double dx = site[s][0] - a.x, dy = site[s][1] - a.y, dz = site[s][2] - a.z;
-      dx -= c.L[0] * rint(dx * c.rL[0]);
-      dy -= c.L[1] * rint(dy * c.rL[1]);
-      dz -= c.L[2] * rint(dz * c.rL[2]);
-      const double r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 >= c.rc2) continue;
-      const int ty = fwt[j];
-      const T r = (T)sqrt(r2);
-      T de, dvv, dsd;
+      const T r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 >= rc2) continue;
+      const T r = sqrt(r2);
+      T de, dvv;
       const T ev = interp_d(erc, r, rd, c.mxegrd, de);
-      const size_t row = ((size_t)s * c.ntype + ty) * c.tabstride;
-      const T lj = interp_d(vt + row, r, rdl, c.mxegrd, dvv);
-      const T dsig = interp_d(ds + row, r, rdl, c.mxegrd, dsd);
-      const T qq = ca * (T)a.w;
-      const T lam = (T)c.lam[ty];
-      const double dedr = (double)(lam * qq * de) + (double)dvv;
-      const double rr = 1.0 / sqrt(r2);
-      g[s][0] += dedr * dx * rr;
-      g[s][1] += dedr * dy * rr;
-      g[s][2] += dedr * dz * rr;
-      v[0] += (double)(lam * qq * ev) + (double)lj;
-      if (c.eps_t[ty] > 0.0) v[1 + 3 * ty] += (double)lj / (2.0 * c.eps_t[ty]);
-      v[1 + 3 * ty + 1] += (double)dsig;
-      v[1 + 3 * ty + 2] += (double)(qq * ev);
+      const T lj = interp_d(row, r, rdl, c.mxegrd, dvv);
+      const T dsig = interp(drow, r, rdl, c.mxegrd);
+      const T qq = ca * qa;
+      const T f = (lam * qq * de + dvv) / r;
+      gx += f * dx;
+      gy += f * dy;
+      gz += f * dz;
+      plj += lj;
+      pds += dsig;
+      pco += qq * ev;
     }
-    __syncthreads();
+    plj = warp_sum(plj);
+    pds = warp_sum(pds);
+    pco = warp_sum(pco);
+    gx = warp_sum(gx);
+    gy = warp_sum(gy);
+    gz = warp_sum(gz);
+    if (lane == 0) {
+      acc_p[wq][t][0] += (double)plj;
+      acc_p[wq][t][1] += (double)pds;
+      acc_p[wq][t][2] += (double)pco;
+      acc_g[wq][s][0] += (double)gx;
+      acc_g[wq][s][1] += (double)gy;
+      acc_g[wq][s][2] += (double)gz;
+    }
   }
   // the snapshot's other molecules
-  const int m0 = snap_mol0[snap], nm = snap_nmol[snap];
-  for (int t = threadIdx.x; t < nm * ns * ns; t += blockDim.x) {
-    const int mm = m0 + t / (ns * ns);
-    if (mm == m) continue;
-    const int s = (t / ns) % ns, s2 = t % ns;
-    const double *q = xyz + ((size_t)mm * ns + s2) * 3;
-    double dx = site[s][0] - q[0], dy = site[s][1] - q[1], dz = site[s][2] - q[2];
-    dx -= c.L[0] * rint(dx * c.rL[0]);
-    dy -= c.L[1] * rint(dy * c.rL[1]);
-    dz -= c.L[2] * rint(dz * c.rL[2]);
-    const double r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 >= c.rc2) continue;
-    const T r = (T)sqrt(r2);
-    T de, dvv = T(0), lj = T(0);
-    const T ev = interp_d(erc, r, rd, c.mxegrd, de);
-    const int rowi = c.gg_row[s][s2];
-    if (rowi >= 0) lj = interp_d(vgg + (size_t)rowi * c.tabstride, r, rdl, c.mxegrd, dvv);
-    const T qq = (T)c.chgea[s] * (T)c.qs[s2];
-    const double dedr = (double)(qq * de) + (double)dvv;
-    const double rr = 1.0 / sqrt(r2);
-    g[s][0] += dedr * dx * rr;
-    g[s][1] += dedr * dy * rr;
-    g[s][2] += dedr * dz * rr;
-    v[0] += 0.5 * ((double)(qq * ev) + (double)lj);
-  }
-  // sums: the snapshot's energy and parameter gradients, the sites' gradients
-  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-  const int nv = 1 + 3 * c.ntype;
-  for (int i = 0; i < nv; ++i) {
-    double x = v[i];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[wq * NV + i] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x < nv) {
-    double t = 0.0;
-    for (int k = 0; k < kHT / 32; ++k) t += sh[k * NV + threadIdx.x];
-    t *= c.rengunit;
-    if (t != 0.0) atomicAdd(threadIdx.x == 0 ? esnap + snap : psnap + (size_t)snap * 3 * c.ntype + threadIdx.x - 1, t);
-  }
-  __syncthreads();
-  for (int i = 0; i < 3 * ns; ++i) {
-    double x = g[i / 3][i % 3];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[wq * NV + (i % NV)] = x;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int k = 0; k < kHT / 32; ++k) t += sh[k * NV + (i % NV)];
-      g64[(size_t)m * ns * 3 + i] = t * c.rengunit;
+  {
+    const int m0 = snap_mol0[snap], nm = snap_nmol[snap];
+    float sh[kMaxASite][3], sl[kMaxASite][3];
+#pragma unroll
+    for (int s = 0; s < kMaxASite; ++s)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float2 v = s < ns ? cw[((size_t)m * ns + s) * 3 + d] : make_float2(0.f, 0.f);
+        sh[s][d] = v.x;
+        sl[s][d] = v.y;
+      }
+    T pg[kMaxASite][3], pe = 0;
+#pragma unroll
+    for (int s = 0; s < kMaxASite; ++s) pg[s][0] = pg[s][1] = pg[s][2] = 0;
+    for (int mm = m0 + threadIdx.x; mm < m0 + nm; mm += kHT) {
+      if (mm == m) continue;
+#pragma unroll
+      for (int s = 0; s < kMaxASite; ++s) {
+        if (s >= ns) break;
+        T gx = 0, gy = 0, gz = 0;
+        for (int s2 = 0; s2 < ns; ++s2) {
+          const size_t i2 = (size_t)mm * ns + s2;
+          T dx, dy, dz;
+          if (F32) {
+            const float2 qx = cw[3 * i2], qy = cw[3 * i2 + 1], qz = cw[3 * i2 + 2];
+            dx = (T)mi_hl(sh[s][0], sl[s][0], qx.x, qx.y, c.Lh[0], c.Ll[0], c.rLf[0]);
+            dy = (T)mi_hl(sh[s][1], sl[s][1], qy.x, qy.y, c.Lh[1], c.Ll[1], c.rLf[1]);
+            dz = (T)mi_hl(sh[s][2], sl[s][2], qz.x, qz.y, c.Lh[2], c.Ll[2], c.rLf[2]);
+          } else {
+            double ex = site[s][0] - xyz[3 * i2], ey = site[s][1] - xyz[3 * i2 + 1],
+                   ez = site[s][2] - xyz[3 * i2 + 2];
+            ex -= c.L[0] * rint(ex * c.rL[0]);
+            ey -= c.L[1] * rint(ey * c.rL[1]);
+            ez -= c.L[2] * rint(ez * c.rL[2]);
+            dx = (T)ex;
+            dy = (T)ey;
+            dz = (T)ez;
+          }
+          const T r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 >= rc2) continue;
+          const T r = sqrt(r2);
+          T de, dvv = T(0), lj = T(0);
+          const T ev = interp_d(erc, r, rd, c.mxegrd, de);
+          const int rowi = c.gg_row[s][s2];
+          if (rowi >= 0) lj = interp_d(vgg + (size_t)rowi * c.tabstride, r, rdl, c.mxegrd, dvv);
+          const T qq = (T)c.chgea[s] * (T)c.qs[s2];
+          const T f = (qq * de + dvv) / r;
+          gx += f * dx;
+          gy += f * dy;
+          gz += f * dz;
+          pe += T(0.5) * (qq * ev + lj);
+        }
+        pg[s][0] += gx;
+        pg[s][1] += gy;
+        pg[s][2] += gz;
+      }
     }
-    __syncthreads();
+    pe = warp_sum(pe);
+    if (lane == 0) acc_e[wq] += (double)pe;
+#pragma unroll
+    for (int s = 0; s < kMaxASite; ++s) {
+      if (s >= ns) break;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const T x = warp_sum(pg[s][d]);
+        if (lane == 0) acc_g[wq][s][d] += (double)x;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 3 * ns) {
+    const int s = threadIdx.x / 3, d = threadIdx.x % 3;
+    double g = 0.0;
+    for (int w = 0; w < kHW; ++w) g += acc_g[w][s][d];
+    g64[(size_t)m * ns * 3 + threadIdx.x] = g * c.rengunit;
+  }
+  if (threadIdx.x < T_) {  // dE/d(eps, sigma, lambda) of type t
+    const int t = threadIdx.x;
+    double lj = 0.0, dsg = 0.0, co = 0.0;
+    for (int w = 0; w < kHW; ++w) {
+      lj += acc_p[w][t][0];
+      dsg += acc_p[w][t][1];
+      co += acc_p[w][t][2];
+    }
+    double *p = psnap + (size_t)snap * 3 * T_ + 3 * t;
+    if (c.eps_t[t] > 0.0 && lj != 0.0) atomicAdd(p, lj / (2.0 * c.eps_t[t]) * c.rengunit);
+    if (dsg != 0.0) atomicAdd(p + 1, dsg * c.rengunit);
+    if (co != 0.0) atomicAdd(p + 2, co * c.rengunit);
+  }
+  if (threadIdx.x == 0) {
+    double e = 0.0;
+    for (int w = 0; w < kHW; ++w) e += acc_e[w];
+    for (int t = 0; t < T_; ++t)
+      for (int w = 0; w < kHW; ++w) e += c.lam[t] * acc_p[w][t][2] + acc_p[w][t][0];
+    if (e != 0.0) atomicAdd(esnap + snap, e * c.rengunit);
   }
 }
 
-// Per-site fractional coordinates x / L as float hi/lo pairs, reduced to
-// [0, 1) (the phases only need them modulo 1).
-__global__ void ham_frac_kernel(HamConst c, const double *xyz, int nsite, float2 *fr) {
+// Per site: fractional coordinates x / L reduced to [0, 1) and the
+// Cartesian position wrapped into [0, L), both as float hi/lo pairs.
+__global__ void ham_frac_kernel(HamConst c, const double *xyz, int nsite, float2 *fr, float2 *cw) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * nsite) return;
-  double f = xyz[i] * c.rL[i % 3];
+  const int d = i % 3;
+  double f = xyz[i] * c.rL[d];
   f -= floor(f);
-  const float h = (float)f;
-  fr[i] = make_float2(h, (float)(f - (double)h));
+  float h, l;
+  split_hl(f, h, l);
+  fr[i] = make_float2(h, l);
+  split_hl(xyz[i] - c.L[d] * floor(xyz[i] * c.rL[d]), h, l);
+  cw[i] = make_float2(h, l);
 }
 
 // e^{i 2 pi (l fx + m fy + n fz)} of one site: FP64, or in FP32 with the
@@ -541,11 +672,12 @@ __global__ void __launch_bounds__(kHT) ham_sk_kernel(HamConst c, const int4 *__r
 }
 
 // Reciprocal site gradients, one thread per molecule: dE/dr_i = -2 K q_i
-// sum_k a_k k Im(e^{i phi_i} conj(W)), W = S_fw + S_g; added to the
-// real-space gradients and stored as float (3N x FP32).
+// sum_k a_k k Im(e^{i phi_i} conj(W)), W = S_fw + S_g, with kv[k] = (k,
+// -2 K a_k); in T, summed in T over runs of 32 k-vectors and those in
+// FP64; added to the real-space gradients and stored as float (3N x FP32).
 template <class T>
 __global__ void ham_recip_grad_kernel(HamConst c, const int4 *__restrict__ klmn,
-                                      const double *__restrict__ akk, const double2 *__restrict__ sg,
+                                      const double4 *__restrict__ kv, const double2 *__restrict__ sg,
                                       const double *__restrict__ xyz, const float2 *__restrict__ fr,
                                       const int *__restrict__ mol_snap, int nmol_total,
                                       const double *__restrict__ g64, float *gout) {
@@ -553,34 +685,50 @@ __global__ void ham_recip_grad_kernel(HamConst c, const int4 *__restrict__ klmn,
   if (m >= nmol_total) return;
   const int ns = c.ns, snap = mol_snap[m];
   double g[kMaxASite][3];
-  for (int s = 0; s < kMaxASite; ++s) g[s][0] = g[s][1] = g[s][2] = 0.0;
+  T gc[kMaxASite][3];
+  T qs[kMaxASite];
+#pragma unroll
+  for (int s = 0; s < kMaxASite; ++s) {
+    g[s][0] = g[s][1] = g[s][2] = 0.0;
+    gc[s][0] = gc[s][1] = gc[s][2] = T(0);
+    qs[s] = s < ns ? (T)c.qs[s] : T(0);
+  }
+  const double2 *w = sg + (size_t)snap * c.nk;
   for (int k = 0; k < c.nk; ++k) {
     const int4 l = klmn[k];
-    double cs[kMaxASite], sn[kMaxASite];
-    for (int s = 0; s < ns; ++s) {
+    const double4 kk = kv[k];
+    const double2 w0 = w[k];
+    const T wr = (T)w0.x, wi = (T)w0.y, f = (T)kk.w, kx = (T)kk.x, ky = (T)kk.y, kz = (T)kk.z;
+#pragma unroll
+    for (int s = 0; s < kMaxASite; ++s) {
+      if (s >= ns) break;
       const size_t i = (size_t)m * ns + s;
-      T a, b;
-      ham_phase<T>(l, xyz + 3 * i, fr + 3 * i, c.rL[0], c.rL[1], c.rL[2], a, b);
-      cs[s] = (double)a;
-      sn[s] = (double)b;
+      T cs, sn;
+      ham_phase<T>(l, xyz + 3 * i, fr + 3 * i, c.rL[0], c.rL[1], c.rL[2], cs, sn);
+      const T a = f * qs[s] * (sn * wr - cs * wi);
+      gc[s][0] += a * kx;
+      gc[s][1] += a * ky;
+      gc[s][2] += a * kz;
     }
-    const double2 w0 = sg[(size_t)snap * c.nk + k];
-    const double wr = w0.x, wi = w0.y;
-    const double f = -2.0 * c.krecip * akk[k];
-    const double kx = 2.0 * kPi * l.x * c.rL[0], ky = 2.0 * kPi * l.y * c.rL[1],
-                 kz = 2.0 * kPi * l.z * c.rL[2];
-    for (int s = 0; s < ns; ++s) {
-      const double w = f * c.qs[s] * (sn[s] * wr - cs[s] * wi);
-      g[s][0] += w * kx;
-      g[s][1] += w * ky;
-      g[s][2] += w * kz;
+    if ((k & 31) == 31 || k == c.nk - 1) {
+#pragma unroll
+      for (int s = 0; s < kMaxASite; ++s)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          g[s][d] += (double)gc[s][d];
+          gc[s][d] = T(0);
+        }
     }
   }
-  for (int s = 0; s < ns; ++s)
+#pragma unroll
+  for (int s = 0; s < kMaxASite; ++s) {
+    if (s >= ns) break;
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
       const size_t i = ((size_t)m * ns + s) * 3 + d;
       gout[i] = (float)(g64[i] + g[s][d] * c.rengunit);
     }
+  }
 }
 
 }  // namespace
@@ -596,8 +744,10 @@ struct fmc_adjoint {
   std::vector<int> type_of_field;  // framework type index -> FIELD unique type
   // the sampled Hamiltonian (fmc_adjoint_eval_batch)
   HamConst h{};
-  ABuf<double4> hfw;   // framework atoms sorted by cell
-  ABuf<int> hfwt, hcstart;
+  ABuf<double4> hfw;         // framework atoms sorted by (cell, type), wrapped into the cell, charge
+  ABuf<float4> hfwh, hfwl;   // the same positions as float hi/lo pairs (hi carries the charge)
+  ABuf<int> hcstart;         // [cell * ntype + type] first atom, ncell * ntype + 1 entries
+  ABuf<double4> kv;          // per k-vector: (k, -2 krecip a_k)
   ABuf<double> erc64, vgg64;
   ABuf<float> erc32, vgg32;
   std::vector<double> eps0, sig0;  // [site][type] the FIELD's pair parameters (internal unit, A)
@@ -684,8 +834,13 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
     for (int d = 0; d < 3; ++d) {
       h.L[d] = c.L[d];
       h.rL[d] = c.rL[d];
+      h.Lh[d] = (float)c.L[d];
+      h.Ll[d] = (float)(c.L[d] - (double)h.Lh[d]);
+      h.rLf[d] = (float)c.rL[d];
       h.nc[d] = std::max(1, (int)std::floor(c.L[d] / s.rcut));
     }
+    if (2.0 * s.rcut > std::min(c.L[0], std::min(c.L[1], c.L[2])))
+      raise(FMC_ERR_INPUT, "the adjoint needs the cutoff below half the cell");
     h.rc2 = c.rc2;
     h.rengunit = c.rengunit;
     h.krecip = c.krecip;
@@ -739,33 +894,46 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
     if (vgg.empty()) vgg.assign(ts, 0.0);
     a->vgg64.upload(vgg);
     a->vgg32.upload(std::vector<float>(vgg.begin(), vgg.end()));
-    {  // framework atoms by cell (z fastest)
-      std::vector<int> cell(c.nfw), order(c.nfw);
+    {  // framework atoms wrapped into the cell and sorted by (cell, type), cells z fastest
+      const int T = c.ntype;
+      std::vector<double4> wf(c.nfw);
+      std::vector<int> key(c.nfw), order(c.nfw);
       for (int j = 0; j < c.nfw; ++j) {
+        double p3[3] = {fw[j].x, fw[j].y, fw[j].z};
         int ic[3];
-        const double p3[3] = {fw[j].x, fw[j].y, fw[j].z};
         for (int d = 0; d < 3; ++d) {
-          double f = p3[d] * h.rL[d];
-          f -= std::floor(f);
-          ic[d] = std::min(h.nc[d] - 1, (int)(f * h.nc[d]));
+          p3[d] -= h.L[d] * std::floor(p3[d] * h.rL[d]);
+          ic[d] = std::min(h.nc[d] - 1, (int)(p3[d] * h.rL[d] * h.nc[d]));
         }
-        cell[j] = (ic[0] * h.nc[1] + ic[1]) * h.nc[2] + ic[2];
+        wf[j] = make_double4(p3[0], p3[1], p3[2], fw[j].w);
+        key[j] = ((ic[0] * h.nc[1] + ic[1]) * h.nc[2] + ic[2]) * T + fwt[j];
         order[j] = j;
       }
-      std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cell[x] < cell[y]; });
-      const int ncell = h.nc[0] * h.nc[1] * h.nc[2];
-      std::vector<int> cs(ncell + 1, 0);
-      for (int j = 0; j < c.nfw; ++j) cs[cell[j] + 1]++;
-      for (int q = 0; q < ncell; ++q) cs[q + 1] += cs[q];
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
+      const int nkey = h.nc[0] * h.nc[1] * h.nc[2] * T;
+      std::vector<int> cs(nkey + 1, 0);
+      for (int j = 0; j < c.nfw; ++j) cs[key[j] + 1]++;
+      for (int q = 0; q < nkey; ++q) cs[q + 1] += cs[q];
       std::vector<double4> sf(c.nfw);
-      std::vector<int> st(c.nfw);
+      std::vector<float4> hi(c.nfw), lo(c.nfw);
       for (int j = 0; j < c.nfw; ++j) {
-        sf[j] = fw[order[j]];
-        st[j] = fwt[order[j]];
+        const double4 a = wf[order[j]];
+        sf[j] = a;
+        const float hx = (float)a.x, hy = (float)a.y, hz = (float)a.z;
+        hi[j] = make_float4(hx, hy, hz, (float)a.w);
+        lo[j] = make_float4((float)(a.x - hx), (float)(a.y - hy), (float)(a.z - hz), 0.f);
       }
       a->hfw.upload(sf);
-      a->hfwt.upload(st);
+      a->hfwh.upload(hi);
+      a->hfwl.upload(lo);
       a->hcstart.upload(cs);
+    }
+    {
+      std::vector<double4> kv(std::max(1, c.nk));
+      for (int k = 0; k < c.nk; ++k)
+        kv[k] = make_double4(2.0 * fmc::kPi * s.kl[k] * c.rL[0], 2.0 * fmc::kPi * s.km[k] * c.rL[1],
+                             2.0 * fmc::kPi * s.kn[k] * c.rL[2], -2.0 * c.krecip * s.akk[k]);
+      a->kv.upload(kv);
     }
     *out = hold.release();
     return FMC_OK;
@@ -871,7 +1039,7 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
     ABuf<int> dms, dm0, dnm;
     ABuf<double> e_d, p_d, g64, vt64, ds64;
     ABuf<float> vt32, ds32;
-    ABuf<float2> fr;
+    ABuf<float2> fr, cw;
     ABuf<double2> sg;
     dms.upload(mol_snap.empty() ? std::vector<int>{0} : mol_snap);
     dm0.upload(mol0);
@@ -887,19 +1055,20 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
       ds32.upload(std::vector<float>(ds.begin(), ds.end()));
     }
     fr.alloc((size_t)std::max(1LL, total) * ns * 3);
+    cw.alloc((size_t)std::max(1LL, total) * ns * 3);
     sg.alloc((size_t)std::max(1, nsnap) * std::max(1, h.nk));
     if (total > 0) {
       const int nsite = (int)(total * ns);
-      ham_frac_kernel<<<(3 * nsite + 255) / 256, 256>>>(h, xyz, nsite, fr.p);
+      ham_frac_kernel<<<(3 * nsite + 255) / 256, 256>>>(h, xyz, nsite, fr.p, cw.p);
       FMC_ACUDA(cudaGetLastError());
       if (precision == FMC_PREC_FP64) {
-        ham_real_kernel<double><<<(unsigned)total, kHT>>>(h, a->hfw.p, a->hfwt.p, a->hcstart.p, xyz, dms.p,
-                                                           dm0.p, dnm.p, a->erc64.p, vt64.p, ds64.p,
-                                                           a->vgg64.p, g64.p, e_d.p, p_d.p);
+        ham_real_kernel<double><<<(unsigned)total, kHT>>>(
+            h, a->hfw.p, a->hfwh.p, a->hfwl.p, a->hcstart.p, xyz, cw.p, dms.p, dm0.p, dnm.p, a->erc64.p,
+            vt64.p, ds64.p, a->vgg64.p, g64.p, e_d.p, p_d.p);
       } else {
-        ham_real_kernel<float><<<(unsigned)total, kHT>>>(h, a->hfw.p, a->hfwt.p, a->hcstart.p, xyz, dms.p,
-                                                          dm0.p, dnm.p, a->erc32.p, vt32.p, ds32.p,
-                                                          a->vgg32.p, g64.p, e_d.p, p_d.p);
+        ham_real_kernel<float><<<(unsigned)total, kHT>>>(
+            h, a->hfw.p, a->hfwh.p, a->hfwl.p, a->hcstart.p, xyz, cw.p, dms.p, dm0.p, dnm.p, a->erc32.p,
+            vt32.p, ds32.p, a->vgg32.p, g64.p, e_d.p, p_d.p);
       }
       FMC_ACUDA(cudaGetLastError());
       if (h.nk > 0) {
@@ -914,10 +1083,10 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
       }
       const unsigned gb = (unsigned)((total + 127) / 128);
       if (precision == FMC_PREC_FP64)
-        ham_recip_grad_kernel<double><<<gb, 128>>>(h, a->klmn.p, a->akk.p, sg.p, xyz, fr.p, dms.p,
+        ham_recip_grad_kernel<double><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, xyz, fr.p, dms.p,
                                                   (int)total, g64.p, gxyz);
       else
-        ham_recip_grad_kernel<float><<<gb, 128>>>(h, a->klmn.p, a->akk.p, sg.p, xyz, fr.p, dms.p,
+        ham_recip_grad_kernel<float><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, xyz, fr.p, dms.p,
                                                  (int)total, g64.p, gxyz);
       FMC_ACUDA(cudaGetLastError());
     }
