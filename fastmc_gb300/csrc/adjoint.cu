@@ -285,13 +285,19 @@ struct HamConst {
   double lam[kMaxAType];
 };
 
-// The 3-point interpolation, and with interp_d its derivative in r.
+// Table position of r: node l and fraction p of the 3-point interpolation
+// (false outside the table).
 template <class T>
-__device__ __forceinline__ T interp(const T *tab, T r, T rd, int mx) {
+__device__ __forceinline__ bool tab_pos(T r, T rd, int mx, int &l, T &p) {
   const T t = r * rd;
-  const int l = int(t);
-  if (l < 1 || l > mx) return T(0);
-  const T p = t - T(l);
+  l = int(t);
+  p = t - T(l);
+  return l >= 1 && l <= mx;
+}
+
+// The 3-point interpolation at (l, p), and with interp_d its derivative in r.
+template <class T>
+__device__ __forceinline__ T interp(const T *tab, int l, T p) {
   const T v0 = tab[l], v1 = tab[l + 1], v2 = tab[l + 2];
   const T t1 = v0 + (v1 - v0) * p;
   const T t2 = v1 + (v2 - v1) * (p - T(1));
@@ -299,14 +305,7 @@ __device__ __forceinline__ T interp(const T *tab, T r, T rd, int mx) {
 }
 
 template <class T>
-__device__ __forceinline__ T interp_d(const T *tab, T r, T rd, int mx, T &dv) {
-  const T t = r * rd;
-  const int l = int(t);
-  if (l < 1 || l > mx) {
-    dv = T(0);
-    return T(0);
-  }
-  const T p = t - T(l);
+__device__ __forceinline__ T interp_d(const T *tab, int l, T p, T rd, T &dv) {
   const T v0 = tab[l], v1 = tab[l + 1], v2 = tab[l + 2];
   const T t1 = v0 + (v1 - v0) * p;
   const T t2 = v1 + (v2 - v1) * (p - T(1));
@@ -314,6 +313,12 @@ __device__ __forceinline__ T interp_d(const T *tab, T r, T rd, int mx, T &dv) {
   dv = ((v1 - v0) + (t2 - t1) * T(0.5) + p * T(0.5) * ((v2 - v1) - (v1 - v0))) * rd;
   return t1 + (t2 - t1) * p * T(0.5);
 }
+
+// The interpolant's slope steps at the table's nodes, so the node a pair
+// falls on decides its gradient to within that step.  In float, a pair
+// within the rounding of r of a node is placed again from its separation
+// in FP64, as the FP64 terms place it.
+__device__ __forceinline__ bool near_node(float p) { return p < 2e-3f || p > 1.f - 2e-3f; }
 
 template <class T>
 __device__ __forceinline__ T warp_sum(T x) {
@@ -339,16 +344,54 @@ __device__ __forceinline__ float mi_hl(float ah, float al, float bh, float bl, f
   return (t - n * Lh) + ((e + (al - bl)) - n * Ll);
 }
 
+// One pair's terms: the erfc Coulomb and LJ energies, the LJ sigma
+// derivative (framework pairs) and dE/dr / r.  r64 gives the FP64
+// separation when a float r lies next to a table node.
+template <class T, bool FW, class R64>
+__device__ __forceinline__ bool pair_terms(const HamConst &c, T r2, const T *erc, const T *row,
+                                           const T *drow, T rd, T rdl, T qq, T lam, R64 &&r64,
+                                           T &ev, T &lj, T &dsig, T &f) {
+  const T r = sqrt(r2);
+  int le, lv;
+  T pe, pv;
+  bool ine = tab_pos(r, rd, c.mxegrd, le, pe);
+  bool inv = tab_pos(r, rdl, c.mxegrd, lv, pv);
+  if (sizeof(T) == 4 && (near_node((float)pe) || near_node((float)pv))) {
+    const double rr = r64();
+    double te = rr * c.rdrewd, tv = rr * c.rdlrpot;
+    le = int(te);
+    lv = int(tv);
+    pe = (T)(te - le);
+    pv = (T)(tv - lv);
+    ine = le >= 1 && le <= c.mxegrd;
+    inv = lv >= 1 && lv <= c.mxegrd;
+  }
+  T de = T(0), dvv = T(0);
+  ev = ine ? interp_d(erc, le, pe, rd, de) : T(0);
+  lj = T(0);
+  dsig = T(0);
+  if (row && inv) {
+    lj = interp_d(row, lv, pv, rdl, dvv);
+    if (FW) dsig = interp(drow, lv, pv);
+  }
+  f = (lam * qq * de + dvv) / r;
+  return true;
+}
+
 // Real space, one block per molecule of the batch.  Framework: the atoms
-// are sorted by (cell, type); a warp takes one (site, neighbour cell, type)
-// entry at a time -- the site shifted by the cell's image, one table row,
-// the type's sums -- its lanes the entry's atoms, and adds the warp's sums
-// to its own shared accumulators.  Cells at least rc wide, or with fewer
-// than three a side every cell with the nearest image per pair.  Guests:
-// threads over the snapshot's other molecules, each pair's energy halved
-// (the other molecule's block sees it too).  The molecule's site gradients
-// are stored (FP64); the snapshot's energy and dE/d(eps, sigma, lambda) per
-// type are added to its sums.  T: the type of the pair terms.
+// are sorted by (cell, type); a warp takes one (site, type, run of
+// neighbour cells) item at a time: its lanes walk the run's atoms as one
+// list, each lane stepping from cell to cell (the site shifted by the
+// cell's image), with one table row and the type's sums per item, which
+// the warp adds to its own shared accumulators.  Cells at least rc wide,
+// or with fewer than three a side every cell with the nearest image per
+// pair.  Guests: threads over the snapshot's other molecules, each pair's
+// energy halved (the other molecule's block sees it too).  The molecule's
+// site gradients are stored (FP64); the snapshot's energy and dE/d(eps,
+// sigma, lambda) per type are added to its sums.  T: the type of the pair
+// terms.
+constexpr int kRun = 9;  // neighbour cells per item (one x-slab of the 27)
+
 template <class T>
 __global__ void __launch_bounds__(kHT) ham_real_kernel(
     HamConst c, const double4 *__restrict__ fw, const float4 *__restrict__ fwh,
@@ -363,6 +406,7 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
   __shared__ double acc_e[kHW];                // per warp: guest-guest energy
   __shared__ double site[kMaxASite][3];        // the molecule's sites, wrapped into the cell
   __shared__ double spos[kMaxASite][27][3];    // a site less a neighbour cell's image
+  __shared__ float spf[kMaxASite][27][6];      // the same as float hi/lo pairs
   __shared__ int cell_of[kMaxASite][27];
   const int m = blockIdx.x, snap = mol_snap[m], ns = c.ns, T_ = c.ntype;
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
@@ -393,6 +437,7 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
           shift = c.L[d];
         }
         spos[s][q][d] = site[s][d] - shift;
+        split_hl(spos[s][q][d], spf[s][q][2 * d], spf[s][q][2 * d + 1]);
       }
       cell_of[s][q] = (w[0] * c.nc[1] + w[1]) * c.nc[2] + w[2];
     }
@@ -401,23 +446,63 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
   const T rd = (T)c.rdrewd, rdl = (T)c.rdlrpot, rc2 = (T)c.rc2;
   const int ncell = c.nc[0] * c.nc[1] * c.nc[2];
   const int nslot = cells ? 27 : ncell;
-  const int ne = ns * nslot * T_;
-  for (int e = wq; e < ne; e += kHW) {  // one (site, cell, type) entry per warp
-    const int t = e % T_, sq = e / T_, s = sq / nslot, q = sq % nslot;
-    const int cell = cells ? cell_of[s][q] : q;
-    const int j0 = cstart[cell * T_ + t], j1 = cstart[cell * T_ + t + 1];
-    if (j0 == j1) continue;
+  const int run = cells ? kRun : 32;
+  const int nrun = (nslot + run - 1) / run;
+  const int nitem = ns * T_ * nrun;
+  for (int it = wq; it < nitem; it += kHW) {  // one (site, type, run of cells) item per warp
+    const int r0 = it % nrun, t = (it / nrun) % T_, s = it / (nrun * T_);
+    const int q0 = r0 * run, nq = min(run, nslot - q0);
+    // lane k < nq: cell q0 + k of the run, its atoms of type t
+    int first = 0, cnt = 0;
+    if (lane < nq) {
+      const int cell = cells ? cell_of[s][q0 + lane] : q0 + lane;
+      first = cstart[cell * T_ + t];
+      cnt = cstart[cell * T_ + t + 1] - first;
+    }
+    int incl = cnt;  // inclusive scan of the counts over the run
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) continue;
+    const int joff = first - (incl - cnt);  // atom index = list index + joff of its cell
     const T *row = vt + ((size_t)s * T_ + t) * c.tabstride;
     const T *drow = ds + ((size_t)s * T_ + t) * c.tabstride;
     const T ca = (T)c.chgea[s], lam = (T)c.lam[t];
-    double px = cells ? spos[s][q][0] : site[s][0], py = cells ? spos[s][q][1] : site[s][1],
-           pz = cells ? spos[s][q][2] : site[s][2];
-    float xh, xl, yh, yl, zh, zl;
-    split_hl(px, xh, xl);
-    split_hl(py, yh, yl);
-    split_hl(pz, zh, zl);
     T plj = 0, pds = 0, pco = 0, gx = 0, gy = 0, gz = 0;
-    for (int j = j0 + lane; j < j1; j += 32) {
+    int k = -1, end = 0, off = 0;  // this lane's cell in the run, its list end and offset
+    double px = site[s][0], py = site[s][1], pz = site[s][2];
+    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
+    for (int base = 0; base < total; base += 32) {
+      const int idx = base + lane;
+      const bool act = idx < total;
+      while (__any_sync(0xffffffffu, act && idx >= end)) {  // step to the cell holding idx
+        const int nk = k + 1;
+        const int ne = __shfl_sync(0xffffffffu, incl, nk & 31);
+        const int no = __shfl_sync(0xffffffffu, joff, nk & 31);
+        if (act && idx >= end) {
+          k = nk;
+          end = ne;
+          off = no;
+          if (cells) {  // the site shifted by this cell's image
+            const int q = q0 + k;
+            px = spos[s][q][0];
+            py = spos[s][q][1];
+            pz = spos[s][q][2];
+            if (F32) {
+              xh = spf[s][q][0];
+              xl = spf[s][q][1];
+              yh = spf[s][q][2];
+              yl = spf[s][q][3];
+              zh = spf[s][q][4];
+              zl = spf[s][q][5];
+            }
+          }
+        }
+      }
+      if (!act) continue;
+      const int j = idx + off;
       T dx, dy, dz, qa;
       if (F32 && cells) {
         const float4 ah = fwh[j], al = fwl[j];
@@ -440,19 +525,25 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
       }
       const T r2 = dx * dx + dy * dy + dz * dz;
       if (r2 >= rc2) continue;
-      const T r = sqrt(r2);
-      T de, dvv;
-      const T ev = interp_d(erc, r, rd, c.mxegrd, de);
-      const T lj = interp_d(row, r, rdl, c.mxegrd, dvv);
-      const T dsig = interp(drow, r, rdl, c.mxegrd);
-      const T qq = ca * qa;
-      const T f = (lam * qq * de + dvv) / r;
+      T ev, lj, dsig, f;
+      pair_terms<T, true>(c, r2, erc, row, drow, rd, rdl, ca * qa, lam,
+                          [&]() {
+                            const double4 a = fw[j];
+                            double ex = px - a.x, ey = py - a.y, ez = pz - a.z;
+                            if (!cells) {
+                              ex -= c.L[0] * rint(ex * c.rL[0]);
+                              ey -= c.L[1] * rint(ey * c.rL[1]);
+                              ez -= c.L[2] * rint(ez * c.rL[2]);
+                            }
+                            return sqrt(ex * ex + ey * ey + ez * ez);
+                          },
+                          ev, lj, dsig, f);
       gx += f * dx;
       gy += f * dy;
       gz += f * dz;
       plj += lj;
       pds += dsig;
-      pco += qq * ev;
+      pco += ca * qa * ev;
     }
     plj = warp_sum(plj);
     pds = warp_sum(pds);
@@ -469,35 +560,29 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
       acc_g[wq][s][2] += (double)gz;
     }
   }
-  // the snapshot's other molecules
+  // the snapshot's other molecules, one site of this molecule at a time
   {
     const int m0 = snap_mol0[snap], nm = snap_nmol[snap];
-    float sh[kMaxASite][3], sl[kMaxASite][3];
-#pragma unroll
-    for (int s = 0; s < kMaxASite; ++s)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const float2 v = s < ns ? cw[((size_t)m * ns + s) * 3 + d] : make_float2(0.f, 0.f);
-        sh[s][d] = v.x;
-        sl[s][d] = v.y;
-      }
-    T pg[kMaxASite][3], pe = 0;
-#pragma unroll
-    for (int s = 0; s < kMaxASite; ++s) pg[s][0] = pg[s][1] = pg[s][2] = 0;
-    for (int mm = m0 + threadIdx.x; mm < m0 + nm; mm += kHT) {
-      if (mm == m) continue;
-#pragma unroll
-      for (int s = 0; s < kMaxASite; ++s) {
-        if (s >= ns) break;
-        T gx = 0, gy = 0, gz = 0;
+    T pe = 0;
+    for (int s = 0; s < ns; ++s) {
+      float sh[3] = {0.f, 0.f, 0.f}, sl[3] = {0.f, 0.f, 0.f};
+      if (F32)
+        for (int d = 0; d < 3; ++d) {
+          const float2 v = cw[((size_t)m * ns + s) * 3 + d];
+          sh[d] = v.x;
+          sl[d] = v.y;
+        }
+      T gx = 0, gy = 0, gz = 0;
+      for (int mm = m0 + threadIdx.x; mm < m0 + nm; mm += kHT) {
+        if (mm == m) continue;
         for (int s2 = 0; s2 < ns; ++s2) {
           const size_t i2 = (size_t)mm * ns + s2;
           T dx, dy, dz;
           if (F32) {
             const float2 qx = cw[3 * i2], qy = cw[3 * i2 + 1], qz = cw[3 * i2 + 2];
-            dx = (T)mi_hl(sh[s][0], sl[s][0], qx.x, qx.y, c.Lh[0], c.Ll[0], c.rLf[0]);
-            dy = (T)mi_hl(sh[s][1], sl[s][1], qy.x, qy.y, c.Lh[1], c.Ll[1], c.rLf[1]);
-            dz = (T)mi_hl(sh[s][2], sl[s][2], qz.x, qz.y, c.Lh[2], c.Ll[2], c.rLf[2]);
+            dx = (T)mi_hl(sh[0], sl[0], qx.x, qx.y, c.Lh[0], c.Ll[0], c.rLf[0]);
+            dy = (T)mi_hl(sh[1], sl[1], qy.x, qy.y, c.Lh[1], c.Ll[1], c.rLf[1]);
+            dz = (T)mi_hl(sh[2], sl[2], qz.x, qz.y, c.Lh[2], c.Ll[2], c.rLf[2]);
           } else {
             double ex = site[s][0] - xyz[3 * i2], ey = site[s][1] - xyz[3 * i2 + 1],
                    ez = site[s][2] - xyz[3 * i2 + 2];
@@ -510,34 +595,37 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
           }
           const T r2 = dx * dx + dy * dy + dz * dz;
           if (r2 >= rc2) continue;
-          const T r = sqrt(r2);
-          T de, dvv = T(0), lj = T(0);
-          const T ev = interp_d(erc, r, rd, c.mxegrd, de);
           const int rowi = c.gg_row[s][s2];
-          if (rowi >= 0) lj = interp_d(vgg + (size_t)rowi * c.tabstride, r, rdl, c.mxegrd, dvv);
           const T qq = (T)c.chgea[s] * (T)c.qs[s2];
-          const T f = (qq * de + dvv) / r;
+          T ev, lj, dsig, f;
+          pair_terms<T, false>(c, r2, erc, rowi >= 0 ? vgg + (size_t)rowi * c.tabstride : nullptr,
+                               nullptr, rd, rdl, qq, T(1),
+                               [&]() {
+                                 double ex = site[s][0] - xyz[3 * i2], ey = site[s][1] - xyz[3 * i2 + 1],
+                                        ez = site[s][2] - xyz[3 * i2 + 2];
+                                 ex -= c.L[0] * rint(ex * c.rL[0]);
+                                 ey -= c.L[1] * rint(ey * c.rL[1]);
+                                 ez -= c.L[2] * rint(ez * c.rL[2]);
+                                 return sqrt(ex * ex + ey * ey + ez * ez);
+                               },
+                               ev, lj, dsig, f);
           gx += f * dx;
           gy += f * dy;
           gz += f * dz;
           pe += T(0.5) * (qq * ev + lj);
         }
-        pg[s][0] += gx;
-        pg[s][1] += gy;
-        pg[s][2] += gz;
+      }
+      gx = warp_sum(gx);
+      gy = warp_sum(gy);
+      gz = warp_sum(gz);
+      if (lane == 0) {
+        acc_g[wq][s][0] += (double)gx;
+        acc_g[wq][s][1] += (double)gy;
+        acc_g[wq][s][2] += (double)gz;
       }
     }
     pe = warp_sum(pe);
     if (lane == 0) acc_e[wq] += (double)pe;
-#pragma unroll
-    for (int s = 0; s < kMaxASite; ++s) {
-      if (s >= ns) break;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const T x = warp_sum(pg[s][d]);
-        if (lane == 0) acc_g[wq][s][d] += (double)x;
-      }
-    }
   }
   __syncthreads();
   if (threadIdx.x < 3 * ns) {
