@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -279,6 +280,7 @@ struct HamConst {
   float Lh[3], Ll[3], rLf[3];
   double rc2, rengunit, krecip, rdrewd, rdlrpot;
   int mxegrd, tabstride, nfw, ns, ntype, nk, nc[3];
+  int kmin[3], kext[3];  // per axis: the smallest k index and the count of indices
   double chgea[kMaxASite], qs[kMaxASite];
   int gg_row[kMaxASite][kMaxASite];  // guest-guest LJ table row, -1 without
   double eps_t[kMaxAType];           // eps_t of the call (FIELD unit), for dE/deps
@@ -759,6 +761,185 @@ __global__ void __launch_bounds__(kHT) ham_sk_kernel(HamConst c, const int4 *__r
   }
 }
 
+// e^{i 2 pi j f} for one axis, f a hi/lo fraction in [0, 1): j f formed
+// exactly (FMA residual) and reduced before sincospif.
+__device__ __forceinline__ float2 axis_phase(int j, float2 f) {
+  const float jf = (float)j;
+  const float p = jf * f.x;
+  const float pe = fmaf(jf, f.x, -p) + jf * f.y;
+  const float x = (p - rintf(p)) + pe;
+  float sn, cs;
+  sincospif(2.0f * x, &sn, &cs);
+  return make_float2(cs, sn);
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// The guests' structure factor in FP32 (block: one snapshot and 256
+// k-vectors): the snapshot's sites in runs of whole molecules, each run's
+// per-axis phase tables e^{i 2 pi j f_d} built once in shared memory, so a
+// thread's phase at k = (l, m, n) is the product of three table entries.
+// Molecule sums in float, the snapshot's in FP64; then as ham_sk_kernel.
+constexpr int kSkRun = 64;  // sites per table run at most
+
+__global__ void __launch_bounds__(kHT) ham_sk32_kernel(HamConst c, const int4 *__restrict__ klmn,
+                                                       const double *__restrict__ akk,
+                                                       const double2 *__restrict__ skt,
+                                                       const float2 *__restrict__ fr,
+                                                       const int *__restrict__ snap_mol0,
+                                                       const int *__restrict__ snap_nmol, double2 *sg,
+                                                       double *esnap, double *psnap) {
+  extern __shared__ float2 ptab[];  // [site of the run][KX + KY + KZ]
+  constexpr int NV = 1 + 3 * kMaxAType;
+  __shared__ double sh[(kHT / 32) * NV];
+  const int KX = c.kext[0], KY = c.kext[1], KW = c.kext[0] + c.kext[1] + c.kext[2];
+  const int k = blockIdx.y * kHT + threadIdx.x, snap = blockIdx.x, ns = c.ns;
+  int ix = 0, iy = 0, iz = 0;
+  if (k < c.nk) {
+    const int4 l = klmn[k];
+    ix = l.x - c.kmin[0];
+    iy = KX + l.y - c.kmin[1];
+    iz = KX + KY + l.z - c.kmin[2];
+  }
+  float qs[kMaxASite];
+#pragma unroll
+  for (int s = 0; s < kMaxASite; ++s) qs[s] = s < ns ? (float)c.qs[s] : 0.f;
+  const int m0 = snap_mol0[snap], nm = snap_nmol[snap];
+  const int mrun = max(1, kSkRun / ns);  // molecules per run
+  double Sr = 0.0, Si = 0.0;
+  for (int r0 = 0; r0 < nm; r0 += mrun) {
+    const int nr = min(mrun, nm - r0), nsite = nr * ns;
+    const size_t site0 = (size_t)(m0 + r0) * ns;
+    __syncthreads();
+    for (int e = threadIdx.x; e < nsite * KW; e += kHT) {
+      const int si = e / KW, w = e % KW;
+      const int d = w < KX ? 0 : (w < KX + KY ? 1 : 2);
+      const int j = d == 0 ? w + c.kmin[0] : (d == 1 ? w - KX + c.kmin[1] : w - KX - KY + c.kmin[2]);
+      ptab[e] = axis_phase(j, fr[(site0 + si) * 3 + d]);
+    }
+    __syncthreads();
+    if (k < c.nk)
+      for (int mm = 0; mm < nr; ++mm) {
+        float sr = 0.f, si = 0.f;
+#pragma unroll
+        for (int s = 0; s < kMaxASite; ++s) {
+          if (s >= ns) break;
+          const float2 *t = ptab + (mm * ns + s) * KW;
+          const float2 e = cmul(cmul(t[ix], t[iy]), t[iz]);
+          sr += qs[s] * e.x;
+          si += qs[s] * e.y;
+        }
+        Sr += (double)sr;
+        Si += (double)si;
+      }
+  }
+  // the reciprocal energy and dE/dlambda_t, reduced over the block
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const double f = k < c.nk ? c.krecip * akk[k] * c.rengunit : 0.0;
+  double Fr = 0.0, Fi = 0.0;
+  for (int t = 0; t < c.ntype; ++t) {
+    double dl = 0.0;
+    if (k < c.nk) {
+      const double2 st = skt[(size_t)t * c.nk + k];
+      Fr += c.lam[t] * st.x;
+      Fi += c.lam[t] * st.y;
+      dl = 2.0 * f * (Sr * st.x + Si * st.y);
+    }
+    dl = warp_sum(dl);
+    if (lane == 0) sh[wq * NV + 1 + t] = dl;
+  }
+  double e = 0.0;
+  if (k < c.nk) {
+    e = f * (2.0 * (Sr * Fr + Si * Fi) + (Sr * Sr + Si * Si));
+    sg[(size_t)snap * c.nk + k] = make_double2(Sr + Fr, Si + Fi);  // S_g + S_fw
+  }
+  e = warp_sum(e);
+  if (lane == 0) sh[wq * NV] = e;
+  __syncthreads();
+  if (threadIdx.x <= c.ntype) {
+    double t = 0.0;
+    for (int q = 0; q < kHT / 32; ++q) t += sh[q * NV + threadIdx.x];
+    if (t != 0.0)
+      atomicAdd(threadIdx.x == 0 ? esnap + snap : psnap + (size_t)snap * 3 * c.ntype + 3 * (threadIdx.x - 1) + 2, t);
+  }
+}
+
+inline size_t ham_sk32_smem(const HamConst &h) {
+  return sizeof(float2) * (size_t)std::max(1, kSkRun / h.ns) * h.ns * (h.kext[0] + h.kext[1] + h.kext[2]);
+}
+
+// Reciprocal site gradients in FP32, one thread per molecule, k in the
+// list's order: along a row of n (same l and m, n one more) a site's phase
+// steps by e^{i 2 pi f_z}; it is formed anew at each row's start and after
+// every 8 steps.  Otherwise as ham_recip_grad_kernel.
+template <int NS>
+__global__ void ham_recip_grad32_kernel(HamConst c, const int4 *__restrict__ klmn,
+                                        const double4 *__restrict__ kv, const double2 *__restrict__ sg,
+                                        const float2 *__restrict__ fr, const int *__restrict__ mol_snap,
+                                        int nmol_total, const double *__restrict__ g64, float *gout) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmol_total) return;
+  const int ns = c.ns, snap = mol_snap[m];
+  double g[NS][3];
+  float gc[NS][3], qs[NS];
+  float2 ph[NS], ez[NS];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    g[s][0] = g[s][1] = g[s][2] = 0.0;
+    gc[s][0] = gc[s][1] = gc[s][2] = 0.f;
+    qs[s] = s < ns ? (float)c.qs[s] : 0.f;
+    ez[s] = s < ns ? axis_phase(1, fr[((size_t)m * ns + s) * 3 + 2]) : make_float2(1.f, 0.f);
+    ph[s] = make_float2(1.f, 0.f);
+  }
+  const double2 *w = sg + (size_t)snap * c.nk;
+  int4 prev = make_int4(INT_MIN, 0, 0, 0);
+  int steps = 0;
+  for (int k = 0; k < c.nk; ++k) {
+    const int4 l = klmn[k];
+    const bool step = l.x == prev.x && l.y == prev.y && l.z == prev.z + 1 && steps < 8;
+    steps = step ? steps + 1 : 0;
+    prev = l;
+    const double4 kk = kv[k];
+    const double2 w0 = w[k];
+    const float wr = (float)w0.x, wi = (float)w0.y, f = (float)kk.w, kx = (float)kk.x,
+                ky = (float)kk.y, kz = (float)kk.z;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      if (NS == kMaxASite && s >= ns) break;
+      if (step) {
+        ph[s] = cmul(ph[s], ez[s]);
+      } else {
+        const float2 *q = fr + ((size_t)m * ns + s) * 3;
+        ph[s] = cmul(cmul(axis_phase(l.x, q[0]), axis_phase(l.y, q[1])), axis_phase(l.z, q[2]));
+      }
+      const float a = f * qs[s] * (ph[s].y * wr - ph[s].x * wi);
+      gc[s][0] += a * kx;
+      gc[s][1] += a * ky;
+      gc[s][2] += a * kz;
+    }
+    if ((k & 31) == 31 || k == c.nk - 1) {
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          g[s][d] += (double)gc[s][d];
+          gc[s][d] = 0.f;
+        }
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    if (NS == kMaxASite && s >= ns) break;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const size_t i = ((size_t)m * ns + s) * 3 + d;
+      gout[i] = (float)(g64[i] + g[s][d] * c.rengunit);
+    }
+  }
+}
+
 // Reciprocal site gradients, one thread per molecule: dE/dr_i = -2 K q_i
 // sum_k a_k k Im(e^{i phi_i} conj(W)), W = S_fw + S_g, with kv[k] = (k,
 // -2 K a_k); in T, summed in T over runs of 32 k-vectors and those in
@@ -936,6 +1117,20 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
     h.rdlrpot = 1.0 / s.dlrpot;
     h.mxegrd = s.mxegrd;
     h.tabstride = s.mxegrd + 3;
+    {
+      int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+      for (int k = 0; k < s.newld; ++k) {
+        const int v[3] = {s.kl[k], s.km[k], s.kn[k]};
+        for (int d = 0; d < 3; ++d) {
+          lo[d] = std::min(lo[d], v[d]);
+          hi[d] = std::max(hi[d], v[d]);
+        }
+      }
+      for (int d = 0; d < 3; ++d) {
+        h.kmin[d] = lo[d];
+        h.kext[d] = hi[d] - lo[d] + 1;
+      }
+    }
     h.nfw = c.nfw;
     h.ns = c.ns;
     h.ntype = c.ntype;
@@ -1164,18 +1359,24 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
         if (precision == FMC_PREC_FP64)
           ham_sk_kernel<double><<<grid, kHT>>>(h, a->klmn.p, a->akk.p, a->skt.p, xyz, fr.p, dm0.p, dnm.p,
                                                sg.p, e_d.p, p_d.p);
-        else
-          ham_sk_kernel<float><<<grid, kHT>>>(h, a->klmn.p, a->akk.p, a->skt.p, xyz, fr.p, dm0.p, dnm.p,
-                                              sg.p, e_d.p, p_d.p);
+        else {
+          FMC_ACUDA(cudaFuncSetAttribute(ham_sk32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)ham_sk32_smem(h)));
+          ham_sk32_kernel<<<grid, kHT, ham_sk32_smem(h)>>>(h, a->klmn.p, a->akk.p, a->skt.p, fr.p, dm0.p,
+                                                           dnm.p, sg.p, e_d.p, p_d.p);
+        }
         FMC_ACUDA(cudaGetLastError());
       }
       const unsigned gb = (unsigned)((total + 127) / 128);
       if (precision == FMC_PREC_FP64)
         ham_recip_grad_kernel<double><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, xyz, fr.p, dms.p,
                                                   (int)total, g64.p, gxyz);
+      else if (ns == 3)  // three-site guests (CO2) with their site loops unrolled
+        ham_recip_grad32_kernel<3><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, fr.p, dms.p, (int)total,
+                                                g64.p, gxyz);
       else
-        ham_recip_grad_kernel<float><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, xyz, fr.p, dms.p,
-                                                 (int)total, g64.p, gxyz);
+        ham_recip_grad32_kernel<kMaxASite><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, fr.p, dms.p,
+                                                        (int)total, g64.p, gxyz);
       FMC_ACUDA(cudaGetLastError());
     }
     FMC_ACUDA(cudaDeviceSynchronize());
