@@ -713,9 +713,9 @@ def run_ours(args, rank, world, local_rank):
         if not args.no_plain:
             out["plain_single_chain"] = plain_paths(F, batch, systems, dirs, specs, snap, args.moves,
                                                     per_chain)
-        if args.widom:
+        if not args.no_widom:
             out["widom_102A"] = widom_102A(F, tmp)
-        if args.adjoint:
+        if not args.no_adjoint:
             out["sampled_energy_adjoint"] = sampled_energy_adjoint(F, tmp, args.snapshots)
         print(json.dumps(out), flush=True)
     if dist:
@@ -764,9 +764,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="one CTA per chain")
     ap.add_argument("--no-plain", action="store_true", help="skip the single-chain comparison")
-    ap.add_argument("--widom", action="store_true", help="also time 1e7 Widom trials against the 102.4 A framework")
-    ap.add_argument("--adjoint", action="store_true",
-                    help="also time the sampled-energy adjoint of 4096 snapshots (51.2 A box)")
+    ap.add_argument("--no-widom", action="store_true",
+                    help="skip timing 1e7 Widom trials against the 102.4 A framework")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip timing the sampled-energy adjoint of 4096 snapshots (51.2 A box)")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="time only the sampled-energy adjoint and print its JSON line")
     ap.add_argument("--snapshots", type=int, default=4096, help="snapshots of the adjoint batch")
