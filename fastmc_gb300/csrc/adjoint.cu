@@ -288,12 +288,20 @@ struct HamConst {
 };
 
 // Table position of r: node l and fraction p of the 3-point interpolation
-// (false outside the table).
+// (false outside the table).  In float, floor(t) comes from adding 2^23
+// rounded down (exact for 0 <= t < 2^23) and its bits, with no conversion
+// instruction (those issue to the FP64 pipe, which this part has little of).
 template <class T>
 __device__ __forceinline__ bool tab_pos(T r, T rd, int mx, int &l, T &p) {
   const T t = r * rd;
-  l = int(t);
-  p = t - T(l);
+  if constexpr (sizeof(T) == 4) {
+    const float tt = __fadd_rd(t, 8388608.0f);
+    l = __float_as_int(tt) - 0x4B000000;
+    p = t - (tt - 8388608.0f);
+  } else {
+    l = int(t);
+    p = t - T(l);
+  }
   return l >= 1 && l <= mx;
 }
 
@@ -410,7 +418,11 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
   __shared__ double spos[kMaxASite][27][3];    // a site less a neighbour cell's image
   __shared__ float spf[kMaxASite][27][6];      // the same as float hi/lo pairs
   __shared__ int cell_of[kMaxASite][27];
+  __shared__ T qprod[kMaxASite][kMaxASite];  // chgea_s q_s2 of guest site pairs
   const int m = blockIdx.x, snap = mol_snap[m], ns = c.ns, T_ = c.ntype;
+  if (threadIdx.x < kMaxASite * kMaxASite)
+    qprod[threadIdx.x / kMaxASite][threadIdx.x % kMaxASite] =
+        (T)c.chgea[threadIdx.x / kMaxASite] * (T)c.qs[threadIdx.x % kMaxASite];
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kHW * kMaxAType * 3; i += kHT) (&acc_p[0][0][0])[i] = 0.0;
   for (int i = threadIdx.x; i < kHW * kMaxASite * 3; i += kHT) (&acc_g[0][0][0])[i] = 0.0;
@@ -598,7 +610,7 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
           const T r2 = dx * dx + dy * dy + dz * dz;
           if (r2 >= rc2) continue;
           const int rowi = c.gg_row[s][s2];
-          const T qq = (T)c.chgea[s] * (T)c.qs[s2];
+          const T qq = qprod[s][s2];
           T ev, lj, dsig, f;
           pair_terms<T, false>(c, r2, erc, rowi >= 0 ? vgg + (size_t)rowi * c.tabstride : nullptr,
                                nullptr, rd, rdl, qq, T(1),
@@ -763,8 +775,7 @@ __global__ void __launch_bounds__(kHT) ham_sk_kernel(HamConst c, const int4 *__r
 
 // e^{i 2 pi j f} for one axis, f a hi/lo fraction in [0, 1): j f formed
 // exactly (FMA residual) and reduced before sincospif.
-__device__ __forceinline__ float2 axis_phase(int j, float2 f) {
-  const float jf = (float)j;
+__device__ __forceinline__ float2 axis_phase(float jf, float2 f) {
   const float p = jf * f.x;
   const float pe = fmaf(jf, f.x, -p) + jf * f.y;
   const float x = (p - rintf(p)) + pe;
@@ -790,7 +801,7 @@ __global__ void __launch_bounds__(kHT) ham_sk32_kernel(HamConst c, const int4 *_
                                                        const float2 *__restrict__ fr,
                                                        const int *__restrict__ snap_mol0,
                                                        const int *__restrict__ snap_nmol, double2 *sg,
-                                                       double *esnap, double *psnap) {
+                                                       float2 *sgf, double *esnap, double *psnap) {
   extern __shared__ float2 ptab[];  // [site of the run][KX + KY + KZ]
   constexpr int NV = 1 + 3 * kMaxAType;
   __shared__ double sh[(kHT / 32) * NV];
@@ -817,23 +828,24 @@ __global__ void __launch_bounds__(kHT) ham_sk32_kernel(HamConst c, const int4 *_
       const int si = e / KW, w = e % KW;
       const int d = w < KX ? 0 : (w < KX + KY ? 1 : 2);
       const int j = d == 0 ? w + c.kmin[0] : (d == 1 ? w - KX + c.kmin[1] : w - KX - KY + c.kmin[2]);
-      ptab[e] = axis_phase(j, fr[(site0 + si) * 3 + d]);
+      ptab[e] = axis_phase((float)j, fr[(site0 + si) * 3 + d]);
     }
     __syncthreads();
-    if (k < c.nk)
+    if (k < c.nk) {
+      float rr = 0.f, ri = 0.f;  // the run's sum in float, the snapshot's in FP64
       for (int mm = 0; mm < nr; ++mm) {
-        float sr = 0.f, si = 0.f;
 #pragma unroll
         for (int s = 0; s < kMaxASite; ++s) {
           if (s >= ns) break;
           const float2 *t = ptab + (mm * ns + s) * KW;
           const float2 e = cmul(cmul(t[ix], t[iy]), t[iz]);
-          sr += qs[s] * e.x;
-          si += qs[s] * e.y;
+          rr += qs[s] * e.x;
+          ri += qs[s] * e.y;
         }
-        Sr += (double)sr;
-        Si += (double)si;
       }
+      Sr += (double)rr;
+      Si += (double)ri;
+    }
   }
   // the reciprocal energy and dE/dlambda_t, reduced over the block
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
@@ -854,6 +866,7 @@ __global__ void __launch_bounds__(kHT) ham_sk32_kernel(HamConst c, const int4 *_
   if (k < c.nk) {
     e = f * (2.0 * (Sr * Fr + Si * Fi) + (Sr * Sr + Si * Si));
     sg[(size_t)snap * c.nk + k] = make_double2(Sr + Fr, Si + Fi);  // S_g + S_fw
+    sgf[(size_t)snap * c.nk + k] = make_float2((float)(Sr + Fr), (float)(Si + Fi));
   }
   e = warp_sum(e);
   if (lane == 0) sh[wq * NV] = e;
@@ -876,9 +889,10 @@ inline size_t ham_sk32_smem(const HamConst &h) {
 // every 8 steps.  Otherwise as ham_recip_grad_kernel.
 template <int NS>
 __global__ void ham_recip_grad32_kernel(HamConst c, const int4 *__restrict__ klmn,
-                                        const double4 *__restrict__ kv, const double2 *__restrict__ sg,
-                                        const float2 *__restrict__ fr, const int *__restrict__ mol_snap,
-                                        int nmol_total, const double *__restrict__ g64, float *gout) {
+                                        const float4 *__restrict__ klf, const float4 *__restrict__ kv,
+                                        const float2 *__restrict__ sg, const float2 *__restrict__ fr,
+                                        const int *__restrict__ mol_snap, int nmol_total,
+                                        const double *__restrict__ g64, float *gout) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= nmol_total) return;
   const int ns = c.ns, snap = mol_snap[m];
@@ -890,10 +904,10 @@ __global__ void ham_recip_grad32_kernel(HamConst c, const int4 *__restrict__ klm
     g[s][0] = g[s][1] = g[s][2] = 0.0;
     gc[s][0] = gc[s][1] = gc[s][2] = 0.f;
     qs[s] = s < ns ? (float)c.qs[s] : 0.f;
-    ez[s] = s < ns ? axis_phase(1, fr[((size_t)m * ns + s) * 3 + 2]) : make_float2(1.f, 0.f);
+    ez[s] = s < ns ? axis_phase(1.f, fr[((size_t)m * ns + s) * 3 + 2]) : make_float2(1.f, 0.f);
     ph[s] = make_float2(1.f, 0.f);
   }
-  const double2 *w = sg + (size_t)snap * c.nk;
+  const float2 *w = sg + (size_t)snap * c.nk;
   int4 prev = make_int4(INT_MIN, 0, 0, 0);
   int steps = 0;
   for (int k = 0; k < c.nk; ++k) {
@@ -901,10 +915,11 @@ __global__ void ham_recip_grad32_kernel(HamConst c, const int4 *__restrict__ klm
     const bool step = l.x == prev.x && l.y == prev.y && l.z == prev.z + 1 && steps < 8;
     steps = step ? steps + 1 : 0;
     prev = l;
-    const double4 kk = kv[k];
-    const double2 w0 = w[k];
-    const float wr = (float)w0.x, wi = (float)w0.y, f = (float)kk.w, kx = (float)kk.x,
-                ky = (float)kk.y, kz = (float)kk.z;
+    const float4 kk = kv[k];
+    const float2 w0 = w[k];
+    const float wr = w0.x, wi = w0.y, f = kk.w, kx = kk.x, ky = kk.y, kz = kk.z;
+    float4 lf = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!step) lf = klf[k];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
       if (NS == kMaxASite && s >= ns) break;
@@ -912,7 +927,7 @@ __global__ void ham_recip_grad32_kernel(HamConst c, const int4 *__restrict__ klm
         ph[s] = cmul(ph[s], ez[s]);
       } else {
         const float2 *q = fr + ((size_t)m * ns + s) * 3;
-        ph[s] = cmul(cmul(axis_phase(l.x, q[0]), axis_phase(l.y, q[1])), axis_phase(l.z, q[2]));
+        ph[s] = cmul(cmul(axis_phase(lf.x, q[0]), axis_phase(lf.y, q[1])), axis_phase(lf.z, q[2]));
       }
       const float a = f * qs[s] * (ph[s].y * wr - ph[s].x * wi);
       gc[s][0] += a * kx;
@@ -1017,6 +1032,7 @@ struct fmc_adjoint {
   ABuf<float4> hfwh, hfwl;   // the same positions as float hi/lo pairs (hi carries the charge)
   ABuf<int> hcstart;         // [cell * ntype + type] first atom, ncell * ntype + 1 entries
   ABuf<double4> kv;          // per k-vector: (k, -2 krecip a_k)
+  ABuf<float4> kv32, klf;    // the same in float, and (l, m, n) as floats
   ABuf<double> erc64, vgg64;
   ABuf<float> erc32, vgg32;
   std::vector<double> eps0, sig0;  // [site][type] the FIELD's pair parameters (internal unit, A)
@@ -1217,6 +1233,14 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
         kv[k] = make_double4(2.0 * fmc::kPi * s.kl[k] * c.rL[0], 2.0 * fmc::kPi * s.km[k] * c.rL[1],
                              2.0 * fmc::kPi * s.kn[k] * c.rL[2], -2.0 * c.krecip * s.akk[k]);
       a->kv.upload(kv);
+      std::vector<float4> kv32(kv.size()), klf(kv.size());
+      for (size_t k = 0; k < kv.size(); ++k) {
+        kv32[k] = make_float4((float)kv[k].x, (float)kv[k].y, (float)kv[k].z, (float)kv[k].w);
+        klf[k] = k < (size_t)c.nk ? make_float4((float)s.kl[k], (float)s.km[k], (float)s.kn[k], 0.f)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      a->kv32.upload(kv32);
+      a->klf.upload(klf);
     }
     *out = hold.release();
     return FMC_OK;
@@ -1322,7 +1346,7 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
     ABuf<int> dms, dm0, dnm;
     ABuf<double> e_d, p_d, g64, vt64, ds64;
     ABuf<float> vt32, ds32;
-    ABuf<float2> fr, cw;
+    ABuf<float2> fr, cw, sgf;
     ABuf<double2> sg;
     dms.upload(mol_snap.empty() ? std::vector<int>{0} : mol_snap);
     dm0.upload(mol0);
@@ -1340,6 +1364,7 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
     fr.alloc((size_t)std::max(1LL, total) * ns * 3);
     cw.alloc((size_t)std::max(1LL, total) * ns * 3);
     sg.alloc((size_t)std::max(1, nsnap) * std::max(1, h.nk));
+    if (precision == FMC_PREC_FP32) sgf.alloc((size_t)std::max(1, nsnap) * std::max(1, h.nk));
     if (total > 0) {
       const int nsite = (int)(total * ns);
       ham_frac_kernel<<<(3 * nsite + 255) / 256, 256>>>(h, xyz, nsite, fr.p, cw.p);
@@ -1363,7 +1388,7 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
           FMC_ACUDA(cudaFuncSetAttribute(ham_sk32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)ham_sk32_smem(h)));
           ham_sk32_kernel<<<grid, kHT, ham_sk32_smem(h)>>>(h, a->klmn.p, a->akk.p, a->skt.p, fr.p, dm0.p,
-                                                           dnm.p, sg.p, e_d.p, p_d.p);
+                                                           dnm.p, sg.p, sgf.p, e_d.p, p_d.p);
         }
         FMC_ACUDA(cudaGetLastError());
       }
@@ -1372,11 +1397,11 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
         ham_recip_grad_kernel<double><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, xyz, fr.p, dms.p,
                                                   (int)total, g64.p, gxyz);
       else if (ns == 3)  // three-site guests (CO2) with their site loops unrolled
-        ham_recip_grad32_kernel<3><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, fr.p, dms.p, (int)total,
-                                                g64.p, gxyz);
+        ham_recip_grad32_kernel<3><<<gb, 128>>>(h, a->klmn.p, a->klf.p, a->kv32.p, sgf.p, fr.p, dms.p,
+                                                (int)total, g64.p, gxyz);
       else
-        ham_recip_grad32_kernel<kMaxASite><<<gb, 128>>>(h, a->klmn.p, a->kv.p, sg.p, fr.p, dms.p,
-                                                        (int)total, g64.p, gxyz);
+        ham_recip_grad32_kernel<kMaxASite><<<gb, 128>>>(h, a->klmn.p, a->klf.p, a->kv32.p, sgf.p, fr.p,
+                                                        dms.p, (int)total, g64.p, gxyz);
       FMC_ACUDA(cudaGetLastError());
     }
     FMC_ACUDA(cudaDeviceSynchronize());
