@@ -419,6 +419,8 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
   __shared__ float spf[kMaxASite][27][6];      // the same as float hi/lo pairs
   __shared__ int cell_of[kMaxASite][27];
   __shared__ T qprod[kMaxASite][kMaxASite];  // chgea_s q_s2 of guest site pairs
+  __shared__ T qv[kHW][4][64];                // per warp: queued pairs (separation, charge)
+  __shared__ int qc[kHW][64];                 // and (atom index << 5 | cell of the run)
   const int m = blockIdx.x, snap = mol_snap[m], ns = c.ns, T_ = c.ntype;
   if (threadIdx.x < kMaxASite * kMaxASite)
     qprod[threadIdx.x / kMaxASite][threadIdx.x % kMaxASite] =
@@ -485,6 +487,40 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
     const T *drow = ds + ((size_t)s * T_ + t) * c.tabstride;
     const T ca = (T)c.chgea[s], lam = (T)c.lam[t];
     T plj = 0, pds = 0, pco = 0, gx = 0, gy = 0, gz = 0;
+    // pairs within the cutoff wait in the warp's queue; 32 at a time, one
+    // per lane, take the table terms (the cutoff test passes for about one
+    // candidate in seven)
+    auto run_pairs = [&](int n) {
+      __syncwarp();
+      if (lane < n) {
+        const int code = qc[wq][lane], j = code >> 5, kq = code & 31;
+        const T dx = qv[wq][0][lane], dy = qv[wq][1][lane], dz = qv[wq][2][lane], qa = qv[wq][3][lane];
+        T ev, lj, dsig, f;
+        pair_terms<T, true>(c, dx * dx + dy * dy + dz * dz, erc, row, drow, rd, rdl, ca * qa, lam,
+                            [&]() {
+                              const double4 a = fw[j];
+                              const int q = q0 + kq;
+                              double ex = (cells ? spos[s][q][0] : site[s][0]) - a.x;
+                              double ey = (cells ? spos[s][q][1] : site[s][1]) - a.y;
+                              double ez = (cells ? spos[s][q][2] : site[s][2]) - a.z;
+                              if (!cells) {
+                                ex -= c.L[0] * rint(ex * c.rL[0]);
+                                ey -= c.L[1] * rint(ey * c.rL[1]);
+                                ez -= c.L[2] * rint(ez * c.rL[2]);
+                              }
+                              return sqrt(ex * ex + ey * ey + ez * ez);
+                            },
+                            ev, lj, dsig, f);
+        gx += f * dx;
+        gy += f * dy;
+        gz += f * dz;
+        plj += lj;
+        pds += dsig;
+        pco += ca * qa * ev;
+      }
+      __syncwarp();
+    };
+    int qn = 0;  // queued pairs (warp-uniform)
     int k = -1, end = 0, off = 0;  // this lane's cell in the run, its list end and offset
     double px = site[s][0], py = site[s][1], pz = site[s][2];
     float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
@@ -515,50 +551,50 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
           }
         }
       }
-      if (!act) continue;
       const int j = idx + off;
-      T dx, dy, dz, qa;
-      if (F32 && cells) {
-        const float4 ah = fwh[j], al = fwl[j];
-        dx = (T)((xh - ah.x) + (xl - al.x));
-        dy = (T)((yh - ah.y) + (yl - al.y));
-        dz = (T)((zh - ah.z) + (zl - al.z));
-        qa = (T)ah.w;
-      } else {
-        const double4 a = fw[j];
-        double ex = px - a.x, ey = py - a.y, ez = pz - a.z;
-        if (!cells) {
-          ex -= c.L[0] * rint(ex * c.rL[0]);
-          ey -= c.L[1] * rint(ey * c.rL[1]);
-          ez -= c.L[2] * rint(ez * c.rL[2]);
+      T dx = T(0), dy = T(0), dz = T(0), qa = T(0);
+      if (act) {
+        if (F32 && cells) {
+          const float4 ah = fwh[j], al = fwl[j];
+          dx = (T)((xh - ah.x) + (xl - al.x));
+          dy = (T)((yh - ah.y) + (yl - al.y));
+          dz = (T)((zh - ah.z) + (zl - al.z));
+          qa = (T)ah.w;
+        } else {
+          const double4 a = fw[j];
+          double ex = px - a.x, ey = py - a.y, ez = pz - a.z;
+          if (!cells) {
+            ex -= c.L[0] * rint(ex * c.rL[0]);
+            ey -= c.L[1] * rint(ey * c.rL[1]);
+            ez -= c.L[2] * rint(ez * c.rL[2]);
+          }
+          dx = (T)ex;
+          dy = (T)ey;
+          dz = (T)ez;
+          qa = (T)a.w;
         }
-        dx = (T)ex;
-        dy = (T)ey;
-        dz = (T)ez;
-        qa = (T)a.w;
       }
-      const T r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 >= rc2) continue;
-      T ev, lj, dsig, f;
-      pair_terms<T, true>(c, r2, erc, row, drow, rd, rdl, ca * qa, lam,
-                          [&]() {
-                            const double4 a = fw[j];
-                            double ex = px - a.x, ey = py - a.y, ez = pz - a.z;
-                            if (!cells) {
-                              ex -= c.L[0] * rint(ex * c.rL[0]);
-                              ey -= c.L[1] * rint(ey * c.rL[1]);
-                              ez -= c.L[2] * rint(ez * c.rL[2]);
-                            }
-                            return sqrt(ex * ex + ey * ey + ez * ez);
-                          },
-                          ev, lj, dsig, f);
-      gx += f * dx;
-      gy += f * dy;
-      gz += f * dz;
-      plj += lj;
-      pds += dsig;
-      pco += ca * qa * ev;
+      const bool in = act && dx * dx + dy * dy + dz * dz < rc2;
+      const unsigned bm = __ballot_sync(0xffffffffu, in);
+      if (in) {
+        const int pos = qn + __popc(bm & ((1u << lane) - 1u));
+        qv[wq][0][pos] = dx;
+        qv[wq][1][pos] = dy;
+        qv[wq][2][pos] = dz;
+        qv[wq][3][pos] = qa;
+        qc[wq][pos] = (j << 5) | k;
+      }
+      qn += __popc(bm);
+      if (qn >= 32) {
+        run_pairs(32);
+        if (lane < qn - 32) {
+          for (int d = 0; d < 4; ++d) qv[wq][d][lane] = qv[wq][d][32 + lane];
+          qc[wq][lane] = qc[wq][32 + lane];
+        }
+        qn -= 32;
+      }
     }
+    if (qn > 0) run_pairs(qn);
     plj = warp_sum(plj);
     pds = warp_sum(pds);
     pco = warp_sum(pco);
@@ -574,7 +610,8 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
       acc_g[wq][s][2] += (double)gz;
     }
   }
-  // the snapshot's other molecules, one site of this molecule at a time
+  // the snapshot's other molecules, one site of this molecule at a time;
+  // pairs within the cutoff queued per warp as for the framework
   {
     const int m0 = snap_mol0[snap], nm = snap_nmol[snap];
     T pe = 0;
@@ -587,33 +624,18 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
           sl[d] = v.y;
         }
       T gx = 0, gy = 0, gz = 0;
-      for (int mm = m0 + threadIdx.x; mm < m0 + nm; mm += kHT) {
-        if (mm == m) continue;
-        for (int s2 = 0; s2 < ns; ++s2) {
-          const size_t i2 = (size_t)mm * ns + s2;
-          T dx, dy, dz;
-          if (F32) {
-            const float2 qx = cw[3 * i2], qy = cw[3 * i2 + 1], qz = cw[3 * i2 + 2];
-            dx = (T)mi_hl(sh[0], sl[0], qx.x, qx.y, c.Lh[0], c.Ll[0], c.rLf[0]);
-            dy = (T)mi_hl(sh[1], sl[1], qy.x, qy.y, c.Lh[1], c.Ll[1], c.rLf[1]);
-            dz = (T)mi_hl(sh[2], sl[2], qz.x, qz.y, c.Lh[2], c.Ll[2], c.rLf[2]);
-          } else {
-            double ex = site[s][0] - xyz[3 * i2], ey = site[s][1] - xyz[3 * i2 + 1],
-                   ez = site[s][2] - xyz[3 * i2 + 2];
-            ex -= c.L[0] * rint(ex * c.rL[0]);
-            ey -= c.L[1] * rint(ey * c.rL[1]);
-            ez -= c.L[2] * rint(ez * c.rL[2]);
-            dx = (T)ex;
-            dy = (T)ey;
-            dz = (T)ez;
-          }
-          const T r2 = dx * dx + dy * dy + dz * dz;
-          if (r2 >= rc2) continue;
+      auto run_pairs = [&](int n) {
+        __syncwarp();
+        if (lane < n) {
+          const int code = qc[wq][lane], s2 = code & 7;
+          const size_t i2 = (size_t)(code >> 3) * ns + s2;
+          const T dx = qv[wq][0][lane], dy = qv[wq][1][lane], dz = qv[wq][2][lane];
           const int rowi = c.gg_row[s][s2];
           const T qq = qprod[s][s2];
           T ev, lj, dsig, f;
-          pair_terms<T, false>(c, r2, erc, rowi >= 0 ? vgg + (size_t)rowi * c.tabstride : nullptr,
-                               nullptr, rd, rdl, qq, T(1),
+          pair_terms<T, false>(c, dx * dx + dy * dy + dz * dz, erc,
+                               rowi >= 0 ? vgg + (size_t)rowi * c.tabstride : nullptr, nullptr, rd, rdl, qq,
+                               T(1),
                                [&]() {
                                  double ex = site[s][0] - xyz[3 * i2], ey = site[s][1] - xyz[3 * i2 + 1],
                                         ez = site[s][2] - xyz[3 * i2 + 2];
@@ -628,7 +650,53 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
           gz += f * dz;
           pe += T(0.5) * (qq * ev + lj);
         }
+        __syncwarp();
+      };
+      int qn = 0;
+      for (int mb = m0 + 32 * wq; mb < m0 + nm; mb += kHT) {
+        const int mm = mb + lane;
+        const bool act = mm < m0 + nm && mm != m;
+        for (int s2 = 0; s2 < ns; ++s2) {
+          const size_t i2 = (size_t)mm * ns + s2;
+          T dx = T(0), dy = T(0), dz = T(0);
+          if (act) {
+            if (F32) {
+              const float2 qx = cw[3 * i2], qy = cw[3 * i2 + 1], qz = cw[3 * i2 + 2];
+              dx = (T)mi_hl(sh[0], sl[0], qx.x, qx.y, c.Lh[0], c.Ll[0], c.rLf[0]);
+              dy = (T)mi_hl(sh[1], sl[1], qy.x, qy.y, c.Lh[1], c.Ll[1], c.rLf[1]);
+              dz = (T)mi_hl(sh[2], sl[2], qz.x, qz.y, c.Lh[2], c.Ll[2], c.rLf[2]);
+            } else {
+              double ex = site[s][0] - xyz[3 * i2], ey = site[s][1] - xyz[3 * i2 + 1],
+                     ez = site[s][2] - xyz[3 * i2 + 2];
+              ex -= c.L[0] * rint(ex * c.rL[0]);
+              ey -= c.L[1] * rint(ey * c.rL[1]);
+              ez -= c.L[2] * rint(ez * c.rL[2]);
+              dx = (T)ex;
+              dy = (T)ey;
+              dz = (T)ez;
+            }
+          }
+          const bool in = act && dx * dx + dy * dy + dz * dz < rc2;
+          const unsigned bm = __ballot_sync(0xffffffffu, in);
+          if (in) {
+            const int pos = qn + __popc(bm & ((1u << lane) - 1u));
+            qv[wq][0][pos] = dx;
+            qv[wq][1][pos] = dy;
+            qv[wq][2][pos] = dz;
+            qc[wq][pos] = (mm << 3) | s2;
+          }
+          qn += __popc(bm);
+          if (qn >= 32) {
+            run_pairs(32);
+            if (lane < qn - 32) {
+              for (int d = 0; d < 3; ++d) qv[wq][d][lane] = qv[wq][d][32 + lane];
+              qc[wq][lane] = qc[wq][32 + lane];
+            }
+            qn -= 32;
+          }
+        }
       }
+      if (qn > 0) run_pairs(qn);
       gx = warp_sum(gx);
       gy = warp_sum(gy);
       gz = warp_sum(gz);
