@@ -285,6 +285,30 @@ struct HamConst {
   int gg_row[kMaxASite][kMaxASite];  // guest-guest LJ table row, -1 without
   double eps_t[kMaxAType];           // eps_t of the call (FIELD unit), for dE/deps
   double lam[kMaxAType];
+  // float copies for the FP32 kernels (no conversion instructions there)
+  float rdrewdf, rdlrpotf, rc2f, ncf[3];
+  float chgeaf[kMaxASite], qsf[kMaxASite], lamf[kMaxAType];
+};
+
+template <class T>
+struct HamT;  // the call's constants in the pair type
+template <>
+struct HamT<float> {
+  static __device__ __forceinline__ float rd(const HamConst &c) { return c.rdrewdf; }
+  static __device__ __forceinline__ float rdl(const HamConst &c) { return c.rdlrpotf; }
+  static __device__ __forceinline__ float rc2(const HamConst &c) { return c.rc2f; }
+  static __device__ __forceinline__ float chgea(const HamConst &c, int s) { return c.chgeaf[s]; }
+  static __device__ __forceinline__ float qs(const HamConst &c, int s) { return c.qsf[s]; }
+  static __device__ __forceinline__ float lam(const HamConst &c, int t) { return c.lamf[t]; }
+};
+template <>
+struct HamT<double> {
+  static __device__ __forceinline__ double rd(const HamConst &c) { return c.rdrewd; }
+  static __device__ __forceinline__ double rdl(const HamConst &c) { return c.rdlrpot; }
+  static __device__ __forceinline__ double rc2(const HamConst &c) { return c.rc2; }
+  static __device__ __forceinline__ double chgea(const HamConst &c, int s) { return c.chgea[s]; }
+  static __device__ __forceinline__ double qs(const HamConst &c, int s) { return c.qs[s]; }
+  static __device__ __forceinline__ double lam(const HamConst &c, int t) { return c.lam[t]; }
 };
 
 // Table position of r: node l and fraction p of the 3-point interpolation
@@ -411,24 +435,26 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
     const T *__restrict__ vt, const T *__restrict__ ds, const T *__restrict__ vgg, double *g64,
     double *esnap, double *psnap) {
   constexpr bool F32 = sizeof(T) == 4;
-  __shared__ double acc_p[kHW][kMaxAType][3];  // per warp and type: LJ, dLJ/dsigma, Coulomb / lambda
-  __shared__ double acc_g[kHW][kMaxASite][3];  // per warp: site gradients
-  __shared__ double acc_e[kHW];                // per warp: guest-guest energy
-  __shared__ double site[kMaxASite][3];        // the molecule's sites, wrapped into the cell
-  __shared__ double spos[kMaxASite][27][3];    // a site less a neighbour cell's image
-  __shared__ float spf[kMaxASite][27][6];      // the same as float hi/lo pairs
+  __shared__ T acc_p[kHW][kMaxAType][3];  // per warp and type: LJ, dLJ/dsigma, Coulomb / lambda
+  __shared__ T acc_g[kHW][kMaxASite][3];  // per warp: site gradients
+  __shared__ T acc_e[kHW];                // per warp: guest-guest energy
+  __shared__ double site[kMaxASite][3];   // the molecule's sites, wrapped into the cell
+  __shared__ double spos[kMaxASite][27][3];  // FP64 terms: a site less a neighbour cell's image
+  __shared__ float spf[kMaxASite][27][6];    // FP32 terms: the same as float hi/lo pairs
+  __shared__ signed char sgn[kMaxASite][27][3];  // the image: site - sgn L
   __shared__ int cell_of[kMaxASite][27];
   __shared__ T qprod[kMaxASite][kMaxASite];  // chgea_s q_s2 of guest site pairs
-  __shared__ T qv[kHW][4][64];                // per warp: queued pairs (separation, charge)
-  __shared__ int qc[kHW][64];                 // and (atom index << 5 | cell of the run)
+  __shared__ T qv[kHW][4][64];               // per warp: queued pairs (separation, charge)
+  __shared__ int qc[kHW][64];                // and (atom index << 5 | cell of the run)
+  using H = HamT<T>;
   const int m = blockIdx.x, snap = mol_snap[m], ns = c.ns, T_ = c.ntype;
   if (threadIdx.x < kMaxASite * kMaxASite)
     qprod[threadIdx.x / kMaxASite][threadIdx.x % kMaxASite] =
-        (T)c.chgea[threadIdx.x / kMaxASite] * (T)c.qs[threadIdx.x % kMaxASite];
+        H::chgea(c, threadIdx.x / kMaxASite) * H::qs(c, threadIdx.x % kMaxASite);
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < kHW * kMaxAType * 3; i += kHT) (&acc_p[0][0][0])[i] = 0.0;
-  for (int i = threadIdx.x; i < kHW * kMaxASite * 3; i += kHT) (&acc_g[0][0][0])[i] = 0.0;
-  if (threadIdx.x < kHW) acc_e[threadIdx.x] = 0.0;
+  for (int i = threadIdx.x; i < kHW * kMaxAType * 3; i += kHT) (&acc_p[0][0][0])[i] = T(0);
+  for (int i = threadIdx.x; i < kHW * kMaxASite * 3; i += kHT) (&acc_g[0][0][0])[i] = T(0);
+  if (threadIdx.x < kHW) acc_e[threadIdx.x] = T(0);
   if (threadIdx.x < 3 * ns) {
     const int d = threadIdx.x % 3;
     const double x = xyz[(size_t)m * ns * 3 + threadIdx.x];
@@ -442,24 +468,43 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
       const int o[3] = {q / 9 - 1, (q / 3) % 3 - 1, q % 3 - 1};
       int w[3];
       for (int d = 0; d < 3; ++d) {
-        const int ic = min(c.nc[d] - 1, (int)(site[s][d] * c.rL[d] * c.nc[d]));
+        int ic;
+        float h = 0.f, l = 0.f;
+        if (F32) {  // from the wrapped site's hi/lo pair, in float
+          const float2 v = cw[((size_t)m * ns + s) * 3 + d];
+          h = v.x;
+          l = v.y;
+          ic = min(c.nc[d] - 1, __float2int_rz(h * c.rLf[d] * c.ncf[d]));
+        } else {
+          ic = min(c.nc[d] - 1, (int)(site[s][d] * c.rL[d] * c.nc[d]));
+        }
         w[d] = ic + o[d];
-        double shift = 0.0;
+        int sg = 0;
         if (w[d] < 0) {
           w[d] += c.nc[d];
-          shift = -c.L[d];
+          sg = -1;
         } else if (w[d] >= c.nc[d]) {
           w[d] -= c.nc[d];
-          shift = c.L[d];
+          sg = 1;
         }
-        spos[s][q][d] = site[s][d] - shift;
-        split_hl(spos[s][q][d], spf[s][q][2 * d], spf[s][q][2 * d + 1]);
+        sgn[s][q][d] = (signed char)sg;
+        if (F32) {  // (h + l) - sg L as a hi/lo pair: two-sum of the hi parts, then the low parts
+          const float bh = -sg * c.Lh[d], bl = -sg * c.Ll[d];
+          const float t = h + bh, bb = t - h;
+          const float e = (h - (t - bb)) + (bh - bb);
+          const float lo = e + (l + bl);
+          const float hi = t + lo;
+          spf[s][q][2 * d] = hi;
+          spf[s][q][2 * d + 1] = lo - (hi - t);
+        } else {
+          spos[s][q][d] = site[s][d] - sg * c.L[d];
+        }
       }
       cell_of[s][q] = (w[0] * c.nc[1] + w[1]) * c.nc[2] + w[2];
     }
   }
   __syncthreads();
-  const T rd = (T)c.rdrewd, rdl = (T)c.rdlrpot, rc2 = (T)c.rc2;
+  const T rd = H::rd(c), rdl = H::rdl(c), rc2 = H::rc2(c);
   const int ncell = c.nc[0] * c.nc[1] * c.nc[2];
   const int nslot = cells ? 27 : ncell;
   const int run = cells ? kRun : 32;
@@ -485,7 +530,7 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
     const int joff = first - (incl - cnt);  // atom index = list index + joff of its cell
     const T *row = vt + ((size_t)s * T_ + t) * c.tabstride;
     const T *drow = ds + ((size_t)s * T_ + t) * c.tabstride;
-    const T ca = (T)c.chgea[s], lam = (T)c.lam[t];
+    const T ca = H::chgea(c, s), lam = H::lam(c, t);
     T plj = 0, pds = 0, pco = 0, gx = 0, gy = 0, gz = 0;
     // pairs within the cutoff wait in the warp's queue; 32 at a time, one
     // per lane, take the table terms (the cutoff test passes for about one
@@ -500,9 +545,12 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
                             [&]() {
                               const double4 a = fw[j];
                               const int q = q0 + kq;
-                              double ex = (cells ? spos[s][q][0] : site[s][0]) - a.x;
-                              double ey = (cells ? spos[s][q][1] : site[s][1]) - a.y;
-                              double ez = (cells ? spos[s][q][2] : site[s][2]) - a.z;
+                              double ex = site[s][0] - a.x, ey = site[s][1] - a.y, ez = site[s][2] - a.z;
+                              if (cells) {
+                                ex -= sgn[s][q][0] * c.L[0];
+                                ey -= sgn[s][q][1] * c.L[1];
+                                ez -= sgn[s][q][2] * c.L[2];
+                              }
                               if (!cells) {
                                 ex -= c.L[0] * rint(ex * c.rL[0]);
                                 ey -= c.L[1] * rint(ey * c.rL[1]);
@@ -537,9 +585,6 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
           off = no;
           if (cells) {  // the site shifted by this cell's image
             const int q = q0 + k;
-            px = spos[s][q][0];
-            py = spos[s][q][1];
-            pz = spos[s][q][2];
             if (F32) {
               xh = spf[s][q][0];
               xl = spf[s][q][1];
@@ -547,6 +592,10 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
               yl = spf[s][q][3];
               zh = spf[s][q][4];
               zl = spf[s][q][5];
+            } else {
+              px = spos[s][q][0];
+              py = spos[s][q][1];
+              pz = spos[s][q][2];
             }
           }
         }
@@ -602,12 +651,12 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
     gy = warp_sum(gy);
     gz = warp_sum(gz);
     if (lane == 0) {
-      acc_p[wq][t][0] += (double)plj;
-      acc_p[wq][t][1] += (double)pds;
-      acc_p[wq][t][2] += (double)pco;
-      acc_g[wq][s][0] += (double)gx;
-      acc_g[wq][s][1] += (double)gy;
-      acc_g[wq][s][2] += (double)gz;
+      acc_p[wq][t][0] += plj;
+      acc_p[wq][t][1] += pds;
+      acc_p[wq][t][2] += pco;
+      acc_g[wq][s][0] += gx;
+      acc_g[wq][s][1] += gy;
+      acc_g[wq][s][2] += gz;
     }
   }
   // the snapshot's other molecules, one site of this molecule at a time;
@@ -701,40 +750,42 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
       gy = warp_sum(gy);
       gz = warp_sum(gz);
       if (lane == 0) {
-        acc_g[wq][s][0] += (double)gx;
-        acc_g[wq][s][1] += (double)gy;
-        acc_g[wq][s][2] += (double)gz;
+        acc_g[wq][s][0] += gx;
+        acc_g[wq][s][1] += gy;
+        acc_g[wq][s][2] += gz;
       }
     }
     pe = warp_sum(pe);
-    if (lane == 0) acc_e[wq] += (double)pe;
+    if (lane == 0) acc_e[wq] += pe;
   }
   __syncthreads();
+  // the warps' sums in FP64: site gradients, and per type dE/d(eps, sigma,
+  // lambda) and the energy (warp 0; the types are at most 16)
   if (threadIdx.x < 3 * ns) {
     const int s = threadIdx.x / 3, d = threadIdx.x % 3;
     double g = 0.0;
-    for (int w = 0; w < kHW; ++w) g += acc_g[w][s][d];
+    for (int w = 0; w < kHW; ++w) g += (double)acc_g[w][s][d];
     g64[(size_t)m * ns * 3 + threadIdx.x] = g * c.rengunit;
   }
-  if (threadIdx.x < T_) {  // dE/d(eps, sigma, lambda) of type t
-    const int t = threadIdx.x;
-    double lj = 0.0, dsg = 0.0, co = 0.0;
-    for (int w = 0; w < kHW; ++w) {
-      lj += acc_p[w][t][0];
-      dsg += acc_p[w][t][1];
-      co += acc_p[w][t][2];
-    }
-    double *p = psnap + (size_t)snap * 3 * T_ + 3 * t;
-    if (c.eps_t[t] > 0.0 && lj != 0.0) atomicAdd(p, lj / (2.0 * c.eps_t[t]) * c.rengunit);
-    if (dsg != 0.0) atomicAdd(p + 1, dsg * c.rengunit);
-    if (co != 0.0) atomicAdd(p + 2, co * c.rengunit);
-  }
-  if (threadIdx.x == 0) {
+  if (wq == 0) {
     double e = 0.0;
-    for (int w = 0; w < kHW; ++w) e += acc_e[w];
-    for (int t = 0; t < T_; ++t)
-      for (int w = 0; w < kHW; ++w) e += c.lam[t] * acc_p[w][t][2] + acc_p[w][t][0];
-    if (e != 0.0) atomicAdd(esnap + snap, e * c.rengunit);
+    if (lane < T_) {
+      const int t = lane;
+      double lj = 0.0, dsg = 0.0, co = 0.0;
+      for (int w = 0; w < kHW; ++w) {
+        lj += (double)acc_p[w][t][0];
+        dsg += (double)acc_p[w][t][1];
+        co += (double)acc_p[w][t][2];
+      }
+      double *p = psnap + (size_t)snap * 3 * T_ + 3 * t;
+      if (c.eps_t[t] > 0.0 && lj != 0.0) atomicAdd(p, lj / (2.0 * c.eps_t[t]) * c.rengunit);
+      if (dsg != 0.0) atomicAdd(p + 1, dsg * c.rengunit);
+      if (co != 0.0) atomicAdd(p + 2, co * c.rengunit);
+      e = c.lam[t] * co + lj;
+    }
+    if (lane < kHW) e += (double)acc_e[lane];
+    e = warp_sum(e);
+    if (lane == 0 && e != 0.0) atomicAdd(esnap + snap, e * c.rengunit);
   }
 }
 
@@ -1201,6 +1252,10 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
     h.rdlrpot = 1.0 / s.dlrpot;
     h.mxegrd = s.mxegrd;
     h.tabstride = s.mxegrd + 3;
+    h.rdrewdf = (float)h.rdrewd;
+    h.rdlrpotf = (float)h.rdlrpot;
+    h.rc2f = (float)h.rc2;
+    for (int d = 0; d < 3; ++d) h.ncf[d] = (float)h.nc[d];
     {
       int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
       for (int k = 0; k < s.newld; ++k) {
@@ -1222,6 +1277,8 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
     for (int i = 0; i < gm.natoms; ++i) {
       h.qs[i] = gm.chg[i];
       h.chgea[i] = gm.chg[i] / s.epsq * fmc::kR4pie0;  // ewald.f:688 (chgea)
+      h.qsf[i] = (float)h.qs[i];
+      h.chgeaf[i] = (float)h.chgea[i];
     }
     a->volm = s.volm;
     a->rcut = s.rcut;
@@ -1378,6 +1435,7 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
         raise(FMC_ERR_ARG, "epsilon >= 0 and sigma > 0 required");
       h.eps_t[t] = params[3 * t];
       h.lam[t] = params[3 * t + 2];
+      h.lamf[t] = (float)h.lam[t];
     }
     std::vector<int> mol_snap, mol0(std::max(1, nsnap)), nm(std::max(1, nsnap));
     long long total = 0;
