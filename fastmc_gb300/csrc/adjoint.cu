@@ -69,7 +69,7 @@ struct ABuf {
   void upload(const std::vector<T> &v) {
     if (p) cudaFree(p);
     p = nullptr;
-    n = v.size();
+    n = cap = v.size();
     if (n) {
       FMC_ACUDA(cudaMalloc(&p, n * sizeof(T)));
       FMC_ACUDA(cudaMemcpy(p, v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
@@ -78,9 +78,20 @@ struct ABuf {
   void alloc(size_t count) {
     if (p) cudaFree(p);
     p = nullptr;
-    n = count;
+    n = cap = count;
     if (n) FMC_ACUDA(cudaMalloc(&p, n * sizeof(T)));
   }
+  // grow-only: reallocate only when count exceeds what is held
+  void reserve(size_t count) {
+    count = std::max<size_t>(count, 1);
+    if (count > cap) alloc(count);
+    n = count;
+  }
+  void put(const std::vector<T> &v) {
+    reserve(v.size());
+    if (!v.empty()) FMC_ACUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  }
+  size_t cap = 0;
 };
 
 constexpr int kAT = 256;       // threads per block
@@ -1157,6 +1168,14 @@ struct fmc_adjoint {
   std::vector<double> eps0, sig0;  // [site][type] the FIELD's pair parameters (internal unit, A)
   std::vector<double> ntyp;        // framework atoms per type
   double volm = 0, rcut = 0, engunit = 1, dlrpot = 0;
+  // per-call buffers, kept between calls and grown when a batch needs more
+  struct Scratch {
+    ABuf<int> dms, dm0, dnm;
+    ABuf<double> e_d, p_d, g64, vt64, ds64;
+    ABuf<float> vt32, ds32;
+    ABuf<float2> fr, cw, sgf;
+    ABuf<double2> sg;
+  } w;
 };
 
 extern "C" {
@@ -1469,28 +1488,31 @@ int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const dou
           ds[o * ts + q] = 0.5 * 4.0 * eps * (12.0 * sr6 * sr6 - 6.0 * sr6) / sig;
         }
       }
-    ABuf<int> dms, dm0, dnm;
-    ABuf<double> e_d, p_d, g64, vt64, ds64;
-    ABuf<float> vt32, ds32;
-    ABuf<float2> fr, cw, sgf;
-    ABuf<double2> sg;
-    dms.upload(mol_snap.empty() ? std::vector<int>{0} : mol_snap);
-    dm0.upload(mol0);
-    dnm.upload(nm);
-    e_d.upload(std::vector<double>(std::max(1, nsnap), 0.0));
-    p_d.upload(std::vector<double>((size_t)std::max(1, nsnap) * 3 * T, 0.0));
-    g64.alloc((size_t)std::max(1LL, total) * ns * 3);
+    auto &W = a->w;
+    auto &dms = W.dms, &dm0 = W.dm0, &dnm = W.dnm;
+    auto &e_d = W.e_d, &p_d = W.p_d, &g64 = W.g64, &vt64 = W.vt64, &ds64 = W.ds64;
+    auto &vt32 = W.vt32, &ds32 = W.ds32;
+    auto &fr = W.fr, &cw = W.cw, &sgf = W.sgf;
+    auto &sg = W.sg;
+    dms.put(mol_snap.empty() ? std::vector<int>{0} : mol_snap);
+    dm0.put(mol0);
+    dnm.put(nm);
+    e_d.reserve(std::max(1, nsnap));
+    p_d.reserve((size_t)std::max(1, nsnap) * 3 * T);
+    FMC_ACUDA(cudaMemset(e_d.p, 0, e_d.n * sizeof(double)));
+    FMC_ACUDA(cudaMemset(p_d.p, 0, p_d.n * sizeof(double)));
+    g64.reserve((size_t)std::max(1LL, total) * ns * 3);
     if (precision == FMC_PREC_FP64) {
-      vt64.upload(vt);
-      ds64.upload(ds);
+      vt64.put(vt);
+      ds64.put(ds);
     } else {
-      vt32.upload(std::vector<float>(vt.begin(), vt.end()));
-      ds32.upload(std::vector<float>(ds.begin(), ds.end()));
+      vt32.put(std::vector<float>(vt.begin(), vt.end()));
+      ds32.put(std::vector<float>(ds.begin(), ds.end()));
     }
-    fr.alloc((size_t)std::max(1LL, total) * ns * 3);
-    cw.alloc((size_t)std::max(1LL, total) * ns * 3);
-    sg.alloc((size_t)std::max(1, nsnap) * std::max(1, h.nk));
-    if (precision == FMC_PREC_FP32) sgf.alloc((size_t)std::max(1, nsnap) * std::max(1, h.nk));
+    fr.reserve((size_t)std::max(1LL, total) * ns * 3);
+    cw.reserve((size_t)std::max(1LL, total) * ns * 3);
+    sg.reserve((size_t)std::max(1, nsnap) * std::max(1, h.nk));
+    if (precision == FMC_PREC_FP32) sgf.reserve((size_t)std::max(1, nsnap) * std::max(1, h.nk));
     if (total > 0) {
       const int nsite = (int)(total * ns);
       ham_frac_kernel<<<(3 * nsite + 255) / 256, 256>>>(h, xyz, nsite, fr.p, cw.p);
