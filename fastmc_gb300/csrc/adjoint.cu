@@ -297,7 +297,7 @@ struct HamConst {
   double eps_t[kMaxAType];           // eps_t of the call (FIELD unit), for dE/deps
   double lam[kMaxAType];
   // float copies for the FP32 kernels (no conversion instructions there)
-  float rdrewdf, rdlrpotf, rc2f, ncf[3];
+  float rdrewdf, rdlrpotf, rc2f, ncf[3], wf[3], rwf[3];  // wf: cell widths, rwf = 1 / wf
   float chgeaf[kMaxASite], qsf[kMaxASite], lamf[kMaxAType];
 };
 
@@ -424,18 +424,28 @@ __device__ __forceinline__ bool pair_terms(const HamConst &c, T r2, const T *erc
 }
 
 // Real space, one block per molecule of the batch.  Framework: the atoms
-// are sorted by (cell, type); a warp takes one (site, type, run of
-// neighbour cells) item at a time: its lanes walk the run's atoms as one
-// list, each lane stepping from cell to cell (the site shifted by the
-// cell's image), with one table row and the type's sums per item, which
-// the warp adds to its own shared accumulators.  Cells at least rc wide,
-// or with fewer than three a side every cell with the nearest image per
-// pair.  Guests: threads over the snapshot's other molecules, each pair's
-// energy halved (the other molecule's block sees it too).  The molecule's
-// site gradients are stored (FP64); the snapshot's energy and dE/d(eps,
-// sigma, lambda) per type are added to its sums.  T: the type of the pair
-// terms.
-constexpr int kRun = 9;  // neighbour cells per item (one x-slab of the 27)
+// are sorted by (type, cell), cells at least rc/2 wide, so that for one
+// type the cells of a z-column are one run of atoms.  A warp takes one
+// (site, type, half of the 5 x 5 neighbour columns) item at a time; each
+// lane sets up one column: skipped when the column lies farther than rc
+// from the site in the xy-plane, else the z-cells within the sphere's
+// chord, as one run or two where the column wraps in z, each with the
+// image the site is shifted by.  The lanes then walk the item's runs as
+// one list (each lane stepping from run to run), queue the pairs within
+// the cutoff, and evaluate them 32 at a time with one table row and the
+// type's sums, which the warp adds to its own shared accumulators.  With
+// fewer than five cells a side, one cell holds every atom and each pair
+// takes the nearest image.  Guests: threads over the snapshot's other
+// molecules, each pair's energy halved (the other molecule's block sees
+// it too).  The molecule's site gradients are stored (FP64); the
+// snapshot's energy and dE/d(eps, sigma, lambda) per type are added to its
+// sums.  T: the type of the pair terms.
+constexpr int kColR = 2;                      // neighbour columns each side
+constexpr int kNCol = (2 * kColR + 1) * (2 * kColR + 1);
+constexpr int kColHalf = (kNCol + 1) / 2;     // columns per item (13, 12)
+// cells a side for the column search: a z-chord with its margin spans at
+// most 2 kColR + 2 cells, which must not wrap onto itself
+constexpr int kFineMin = 2 * kColR + 2;
 
 template <class T>
 __global__ void __launch_bounds__(kHT) ham_real_kernel(
@@ -450,13 +460,13 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
   __shared__ T acc_g[kHW][kMaxASite][3];  // per warp: site gradients
   __shared__ T acc_e[kHW];                // per warp: guest-guest energy
   __shared__ double site[kMaxASite][3];   // the molecule's sites, wrapped into the cell
-  __shared__ double spos[kMaxASite][27][3];  // FP64 terms: a site less a neighbour cell's image
-  __shared__ float spf[kMaxASite][27][6];    // FP32 terms: the same as float hi/lo pairs
-  __shared__ signed char sgn[kMaxASite][27][3];  // the image: site - sgn L
-  __shared__ int cell_of[kMaxASite][27];
+  __shared__ float sitef[kMaxASite][6];   // the same as float hi/lo pairs
+  __shared__ int sitecell[kMaxASite][3];  // their cells
+  __shared__ float rpos[kHW][64][6];      // per warp and run: the shifted site as float hi/lo pairs
+  __shared__ signed char rsg[kHW][64][3]; // and the image: site - rsg L
   __shared__ T qprod[kMaxASite][kMaxASite];  // chgea_s q_s2 of guest site pairs
   __shared__ T qv[kHW][4][64];               // per warp: queued pairs (separation, charge)
-  __shared__ int qc[kHW][64];                // and (atom index << 5 | cell of the run)
+  __shared__ int qc[kHW][64];                // and (atom index << 6 | run)
   using H = HamT<T>;
   const int m = blockIdx.x, snap = mol_snap[m], ns = c.ns, T_ = c.ntype;
   if (threadIdx.x < kMaxASite * kMaxASite)
@@ -469,100 +479,116 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
   if (threadIdx.x < 3 * ns) {
     const int d = threadIdx.x % 3;
     const double x = xyz[(size_t)m * ns * 3 + threadIdx.x];
-    site[threadIdx.x / 3][d] = x - c.L[d] * floor(x * c.rL[d]);
+    const double w = x - c.L[d] * floor(x * c.rL[d]);
+    site[threadIdx.x / 3][d] = w;
+    sitecell[threadIdx.x / 3][d] = min(c.nc[d] - 1, (int)(w * c.rL[d] * c.nc[d]));
+    split_hl(w, sitef[threadIdx.x / 3][2 * d], sitef[threadIdx.x / 3][2 * d + 1]);
   }
   __syncthreads();
-  const bool cells = c.nc[0] >= 3 && c.nc[1] >= 3 && c.nc[2] >= 3;
-  if (cells) {
-    for (int p = threadIdx.x; p < ns * 27; p += kHT) {
-      const int s = p / 27, q = p % 27;
-      const int o[3] = {q / 9 - 1, (q / 3) % 3 - 1, q % 3 - 1};
-      int w[3];
-      for (int d = 0; d < 3; ++d) {
-        int ic;
-        float h = 0.f, l = 0.f;
-        if (F32) {  // from the wrapped site's hi/lo pair, in float
-          const float2 v = cw[((size_t)m * ns + s) * 3 + d];
-          h = v.x;
-          l = v.y;
-          ic = min(c.nc[d] - 1, __float2int_rz(h * c.rLf[d] * c.ncf[d]));
-        } else {
-          ic = min(c.nc[d] - 1, (int)(site[s][d] * c.rL[d] * c.nc[d]));
-        }
-        w[d] = ic + o[d];
-        int sg = 0;
-        if (w[d] < 0) {
-          w[d] += c.nc[d];
-          sg = -1;
-        } else if (w[d] >= c.nc[d]) {
-          w[d] -= c.nc[d];
-          sg = 1;
-        }
-        sgn[s][q][d] = (signed char)sg;
-        if (F32) {  // (h + l) - sg L as a hi/lo pair: two-sum of the hi parts, then the low parts
-          const float bh = -sg * c.Lh[d], bl = -sg * c.Ll[d];
-          const float t = h + bh, bb = t - h;
-          const float e = (h - (t - bb)) + (bh - bb);
-          const float lo = e + (l + bl);
-          const float hi = t + lo;
-          spf[s][q][2 * d] = hi;
-          spf[s][q][2 * d + 1] = lo - (hi - t);
-        } else {
-          spos[s][q][d] = site[s][d] - sg * c.L[d];
-        }
-      }
-      cell_of[s][q] = (w[0] * c.nc[1] + w[1]) * c.nc[2] + w[2];
-    }
-  }
-  __syncthreads();
+  const bool fine = c.nc[0] >= kFineMin && c.nc[1] >= kFineMin && c.nc[2] >= kFineMin;
   const T rd = H::rd(c), rdl = H::rdl(c), rc2 = H::rc2(c);
   const int ncell = c.nc[0] * c.nc[1] * c.nc[2];
-  const int nslot = cells ? 27 : ncell;
-  const int run = cells ? kRun : 32;
-  const int nrun = (nslot + run - 1) / run;
-  const int nitem = ns * T_ * nrun;
-  for (int it = wq; it < nitem; it += kHW) {  // one (site, type, run of cells) item per warp
-    const int r0 = it % nrun, t = (it / nrun) % T_, s = it / (nrun * T_);
-    const int q0 = r0 * run, nq = min(run, nslot - q0);
-    // lane k < nq: cell q0 + k of the run, its atoms of type t
-    int first = 0, cnt = 0;
-    if (lane < nq) {
-      const int cell = cells ? cell_of[s][q0 + lane] : q0 + lane;
-      first = cstart[cell * T_ + t];
-      cnt = cstart[cell * T_ + t + 1] - first;
+  const int nitem = ns * T_ * (fine ? 2 : 1);
+  for (int it = wq; it < nitem; it += kHW) {  // one (site, type, half of the columns) item per warp
+    const int half = fine ? it % 2 : 0, st = fine ? it / 2 : it;
+    const int t = st % T_, s = st / T_;
+    // lane k: column c0 + k (fine) or, lane 0, the one cell (brute force);
+    // up to two runs: (first atom, count) each
+    int f1 = 0, n1 = 0, f2 = 0, n2 = 0;
+    if (fine) {
+      const int col = half * kColHalf + lane;
+      if (lane < (half ? kNCol - kColHalf : kColHalf)) {
+        const int dx = col / (2 * kColR + 1) - kColR, dy = col % (2 * kColR + 1) - kColR;
+        const int icx = sitecell[s][0] + dx, icy = sitecell[s][1] + dy;
+        // distance in the xy-plane from the site to the column (unwrapped
+        // frame), in float with a margin: a column kept needlessly only
+        // adds candidates the cutoff test drops
+        const float sx = sitef[s][0], sy = sitef[s][2], sz = sitef[s][4];
+        const float ex = fmaxf(0.f, fmaxf((float)icx * c.wf[0] - sx, sx - (float)(icx + 1) * c.wf[0]));
+        const float ey = fmaxf(0.f, fmaxf((float)icy * c.wf[1] - sy, sy - (float)(icy + 1) * c.wf[1]));
+        const float d2 = ex * ex + ey * ey;
+        if (d2 < c.rc2f + 1e-2f) {
+          const float zh = sqrtf(fmaxf(c.rc2f - d2, 0.f)) + 1e-2f;
+          int iz0 = (int)floorf((sz - zh) * c.rwf[2]), iz1 = (int)floorf((sz + zh) * c.rwf[2]);
+          iz1 = min(iz1, iz0 + c.nc[2] - 1);
+          int ix = icx, iy = icy, sgx = 0, sgy = 0;
+          if (ix < 0) { ix += c.nc[0]; sgx = -1; } else if (ix >= c.nc[0]) { ix -= c.nc[0]; sgx = 1; }
+          if (iy < 0) { iy += c.nc[1]; sgy = -1; } else if (iy >= c.nc[1]) { iy -= c.nc[1]; sgy = 1; }
+          const int cb = (ix * c.nc[1] + iy) * c.nc[2], tb = t * ncell;
+          // run 1: the cells inside [0, nz); run 2: the part that wraps
+          const int a0 = max(iz0, 0), a1 = min(iz1, c.nc[2] - 1);
+          int b0 = 0, b1 = -1, sgz = 0;
+          if (iz0 < 0) {
+            b0 = iz0 + c.nc[2];
+            b1 = c.nc[2] - 1;
+            sgz = -1;
+          } else if (iz1 >= c.nc[2]) {
+            b0 = 0;
+            b1 = iz1 - c.nc[2];
+            sgz = 1;
+          }
+          if (a0 <= a1) {
+            f1 = cstart[tb + cb + a0];
+            n1 = cstart[tb + cb + a1 + 1] - f1;
+          }
+          if (b0 <= b1) {
+            f2 = cstart[tb + cb + b0];
+            n2 = cstart[tb + cb + b1 + 1] - f2;
+          }
+          const int sg[2][3] = {{sgx, sgy, 0}, {sgx, sgy, sgz}};
+          for (int r = 0; r < 2; ++r) {
+            for (int d = 0; d < 3; ++d) {
+              rsg[wq][2 * lane + r][d] = (signed char)sg[r][d];
+              // (h + l) - sg L as a hi/lo pair: two-sum of the hi parts, then the lows
+              const float h = sitef[s][2 * d], l = sitef[s][2 * d + 1];
+              const float bh = -(float)sg[r][d] * c.Lh[d], bl = -(float)sg[r][d] * c.Ll[d];
+              const float t0 = h + bh, bb = t0 - h;
+              const float e = (h - (t0 - bb)) + (bh - bb);
+              const float lo = e + (l + bl);
+              const float hi = t0 + lo;
+              rpos[wq][2 * lane + r][2 * d] = hi;
+              rpos[wq][2 * lane + r][2 * d + 1] = lo - (hi - t0);
+            }
+          }
+        }
+      }
+    } else if (lane == 0) {
+      f1 = cstart[t * ncell];
+      n1 = cstart[t * ncell + ncell] - f1;
+      for (int d = 0; d < 3; ++d) {
+        rsg[wq][0][d] = 0;
+        rpos[wq][0][2 * d] = sitef[s][2 * d];
+        rpos[wq][0][2 * d + 1] = sitef[s][2 * d + 1];
+      }
     }
-    int incl = cnt;  // inclusive scan of the counts over the run
+    const int cnt = n1 + n2;
+    int incl = cnt;  // inclusive scan of the lanes' counts
     for (int o = 1; o < 32; o <<= 1) {
       const int v = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += v;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
     if (total == 0) continue;
-    const int joff = first - (incl - cnt);  // atom index = list index + joff of its cell
     const T *row = vt + ((size_t)s * T_ + t) * c.tabstride;
     const T *drow = ds + ((size_t)s * T_ + t) * c.tabstride;
     const T ca = H::chgea(c, s), lam = H::lam(c, t);
     T plj = 0, pds = 0, pco = 0, gx = 0, gy = 0, gz = 0;
     // pairs within the cutoff wait in the warp's queue; 32 at a time, one
-    // per lane, take the table terms (the cutoff test passes for about one
-    // candidate in seven)
+    // per lane, take the table terms
     auto run_pairs = [&](int n) {
       __syncwarp();
       if (lane < n) {
-        const int code = qc[wq][lane], j = code >> 5, kq = code & 31;
+        const int code = qc[wq][lane], j = code >> 6, rr = code & 63;
         const T dx = qv[wq][0][lane], dy = qv[wq][1][lane], dz = qv[wq][2][lane], qa = qv[wq][3][lane];
         T ev, lj, dsig, f;
         pair_terms<T, true>(c, dx * dx + dy * dy + dz * dz, erc, row, drow, rd, rdl, ca * qa, lam,
                             [&]() {
                               const double4 a = fw[j];
-                              const int q = q0 + kq;
-                              double ex = site[s][0] - a.x, ey = site[s][1] - a.y, ez = site[s][2] - a.z;
-                              if (cells) {
-                                ex -= sgn[s][q][0] * c.L[0];
-                                ey -= sgn[s][q][1] * c.L[1];
-                                ez -= sgn[s][q][2] * c.L[2];
-                              }
-                              if (!cells) {
+                              double ex = site[s][0] - rsg[wq][rr][0] * c.L[0] - a.x;
+                              double ey = site[s][1] - rsg[wq][rr][1] * c.L[1] - a.y;
+                              double ez = site[s][2] - rsg[wq][rr][2] * c.L[2] - a.z;
+                              if (!fine) {
                                 ex -= c.L[0] * rint(ex * c.rL[0]);
                                 ey -= c.L[1] * rint(ey * c.rL[1]);
                                 ez -= c.L[2] * rint(ez * c.rL[2]);
@@ -579,42 +605,54 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
       }
       __syncwarp();
     };
-    int qn = 0;  // queued pairs (warp-uniform)
-    int k = -1, end = 0, off = 0;  // this lane's cell in the run, its list end and offset
-    double px = site[s][0], py = site[s][1], pz = site[s][2];
+    int qn = 0;                    // queued pairs (warp-uniform)
+    int k = -1, end = 0, mid = 0;  // this lane's column, its list end and the end of its first run
+    int o1 = 0, o2 = 0;            // atom index = list index + offset, per run
+    int rr = 0;                    // the run (2 k + 0 or 1)
     float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
+    double px = 0.0, py = 0.0, pz = 0.0;
+    const int excl = incl - cnt;
     for (int base = 0; base < total; base += 32) {
       const int idx = base + lane;
       const bool act = idx < total;
-      while (__any_sync(0xffffffffu, act && idx >= end)) {  // step to the cell holding idx
+      while (__any_sync(0xffffffffu, act && idx >= end)) {  // step to the column holding idx
         const int nk = k + 1;
         const int ne = __shfl_sync(0xffffffffu, incl, nk & 31);
-        const int no = __shfl_sync(0xffffffffu, joff, nk & 31);
+        const int nx = __shfl_sync(0xffffffffu, excl, nk & 31);
+        const int nn1 = __shfl_sync(0xffffffffu, n1, nk & 31);
+        const int nf1 = __shfl_sync(0xffffffffu, f1, nk & 31);
+        const int nf2 = __shfl_sync(0xffffffffu, f2, nk & 31);
         if (act && idx >= end) {
           k = nk;
           end = ne;
-          off = no;
-          if (cells) {  // the site shifted by this cell's image
-            const int q = q0 + k;
-            if (F32) {
-              xh = spf[s][q][0];
-              xl = spf[s][q][1];
-              yh = spf[s][q][2];
-              yl = spf[s][q][3];
-              zh = spf[s][q][4];
-              zl = spf[s][q][5];
-            } else {
-              px = spos[s][q][0];
-              py = spos[s][q][1];
-              pz = spos[s][q][2];
-            }
+          mid = nx + nn1;
+          o1 = nf1 - nx;
+          o2 = nf2 - mid;
+        }
+      }
+      int j = 0;
+      if (act) {
+        const int r = idx < mid ? 0 : 1;
+        j = idx + (r == 0 ? o1 : o2);
+        const int nr = 2 * k + r;
+        if (nr != rr || base == 0) {  // the site shifted by this run's image
+          rr = nr;
+          xh = rpos[wq][rr][0];
+          xl = rpos[wq][rr][1];
+          yh = rpos[wq][rr][2];
+          yl = rpos[wq][rr][3];
+          zh = rpos[wq][rr][4];
+          zl = rpos[wq][rr][5];
+          if (!F32 || !fine) {
+            px = site[s][0] - rsg[wq][rr][0] * c.L[0];
+            py = site[s][1] - rsg[wq][rr][1] * c.L[1];
+            pz = site[s][2] - rsg[wq][rr][2] * c.L[2];
           }
         }
       }
-      const int j = idx + off;
       T dx = T(0), dy = T(0), dz = T(0), qa = T(0);
       if (act) {
-        if (F32 && cells) {
+        if (F32 && fine) {
           const float4 ah = fwh[j], al = fwl[j];
           dx = (T)((xh - ah.x) + (xl - al.x));
           dy = (T)((yh - ah.y) + (yl - al.y));
@@ -623,7 +661,7 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
         } else {
           const double4 a = fw[j];
           double ex = px - a.x, ey = py - a.y, ez = pz - a.z;
-          if (!cells) {
+          if (!fine) {
             ex -= c.L[0] * rint(ex * c.rL[0]);
             ey -= c.L[1] * rint(ey * c.rL[1]);
             ez -= c.L[2] * rint(ez * c.rL[2]);
@@ -642,7 +680,7 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
         qv[wq][1][pos] = dy;
         qv[wq][2][pos] = dz;
         qv[wq][3][pos] = qa;
-        qc[wq][pos] = (j << 5) | k;
+        qc[wq][pos] = (j << 6) | rr;
       }
       qn += __popc(bm);
       if (qn >= 32) {
@@ -669,6 +707,7 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
       acc_g[wq][s][1] += gy;
       acc_g[wq][s][2] += gz;
     }
+    __syncwarp();
   }
   // the snapshot's other molecules, one site of this molecule at a time;
   // pairs within the cutoff queued per warp as for the framework
@@ -1160,7 +1199,7 @@ struct fmc_adjoint {
   HamConst h{};
   ABuf<double4> hfw;         // framework atoms sorted by (cell, type), wrapped into the cell, charge
   ABuf<float4> hfwh, hfwl;   // the same positions as float hi/lo pairs (hi carries the charge)
-  ABuf<int> hcstart;         // [cell * ntype + type] first atom, ncell * ntype + 1 entries
+  ABuf<int> hcstart;         // [type * ncell + cell] first atom, ntype * ncell + 1 entries
   ABuf<double4> kv;          // per k-vector: (k, -2 krecip a_k)
   ABuf<float4> kv32, klf;    // the same in float, and (l, m, n) as floats
   ABuf<double> erc64, vgg64;
@@ -1237,6 +1276,7 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
         fwt.push_back(idx[fwm.ltp[i]]);
       }
     c.nfw = (int)fw.size();
+    if (c.nfw >= (1 << 25)) raise(FMC_ERR_CAPACITY, "the adjoint takes fewer than 2^25 framework atoms");
     a->fw.upload(fw);
     a->fwt.upload(fwt);
     std::vector<int4> kl(s.newld);
@@ -1260,7 +1300,13 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
       h.Lh[d] = (float)c.L[d];
       h.Ll[d] = (float)(c.L[d] - (double)h.Lh[d]);
       h.rLf[d] = (float)c.rL[d];
-      h.nc[d] = std::max(1, (int)std::floor(c.L[d] / s.rcut));
+      h.nc[d] = (int)std::floor(c.L[d] / (0.5 * s.rcut));  // cells at least rc / 2 wide
+    }
+    if (h.nc[0] < kFineMin || h.nc[1] < kFineMin || h.nc[2] < kFineMin)
+      h.nc[0] = h.nc[1] = h.nc[2] = 1;  // small cells: one cell, every atom, nearest image per pair
+    for (int d = 0; d < 3; ++d) {
+      h.wf[d] = (float)(c.L[d] / h.nc[d]);
+      h.rwf[d] = (float)(h.nc[d] / c.L[d]);
     }
     if (2.0 * s.rcut > std::min(c.L[0], std::min(c.L[1], c.L[2])))
       raise(FMC_ERR_INPUT, "the adjoint needs the cutoff below half the cell");
@@ -1337,7 +1383,7 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
     if (vgg.empty()) vgg.assign(ts, 0.0);
     a->vgg64.upload(vgg);
     a->vgg32.upload(std::vector<float>(vgg.begin(), vgg.end()));
-    {  // framework atoms wrapped into the cell and sorted by (cell, type), cells z fastest
+    {  // framework atoms wrapped into the cell and sorted by (type, cell), cells z fastest
       const int T = c.ntype;
       std::vector<double4> wf(c.nfw);
       std::vector<int> key(c.nfw), order(c.nfw);
@@ -1349,7 +1395,7 @@ int fmc_adjoint_create(const fmc_system *sys, fmc_adjoint **out) {
           ic[d] = std::min(h.nc[d] - 1, (int)(p3[d] * h.rL[d] * h.nc[d]));
         }
         wf[j] = make_double4(p3[0], p3[1], p3[2], fw[j].w);
-        key[j] = ((ic[0] * h.nc[1] + ic[1]) * h.nc[2] + ic[2]) * T + fwt[j];
+        key[j] = fwt[j] * (h.nc[0] * h.nc[1] * h.nc[2]) + (ic[0] * h.nc[1] + ic[1]) * h.nc[2] + ic[2];
         order[j] = j;
       }
       std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
