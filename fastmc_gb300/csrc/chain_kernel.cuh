@@ -22,6 +22,28 @@ constexpr int kModeEval = 2;    // evaluate the move in gctx (per-move ABI)
 constexpr int kModeCommit = 3;  // decide with gctx.rande and commit
 constexpr int kModeWidom = 4;   // test insertions of a WidomJob (no state change)
 constexpr int kModeLoad = 5;    // insert a WidomJob's positions into chain wj.chain (restart)
+// Widom screen: margin (A^2) on the overlap distance squared, far above the
+// error of a float trial geometry (~1e-5 A in a 100 A cell)
+constexpr float kScreenMargin = 1e-3f;
+
+// Coordinate d of site s of trial t of a Widom job (FP64): the caller's
+// position, or a grid point (1-based fractions) and a random orientation
+// (random_rot with angle 2 pi, rotation about the origin).
+__device__ __forceinline__ double widom_site(const SysDev &S, const GuestType &G, const WidomJob &wj,
+                                             int t, int s, int d) {
+  if (wj.xyz_in) return wj.xyz_in[((size_t)t * G.ns + s) * 3 + d];
+  const int gi = t / wj.nstep;
+  const int i = gi / (wj.ng[1] * wj.ng[2]) + 1, j = (gi / wj.ng[2]) % wj.ng[1] + 1, k = gi % wj.ng[2] + 1;
+  const double f[3] = {double(i) / wj.ng[0], double(j) / wj.ng[1], double(k) / wj.ng[2]};
+  float dr[7];
+  for (int q = 3; q < 7; ++q) dr[q] = hash_uniform(wj.seed, 4ull * (unsigned long long)t + (q - 3));
+  double qt[4], row[3];
+  draw_quaternion(dr, 2.0 * kPi, qt);
+  qrow(qt, d, row);
+  const double *tp = G.tmpl[s];
+  return row[0] * tp[0] + row[1] * tp[1] + row[2] * tp[2] + S.cell[d] * f[0] + S.cell[3 + d] * f[1] +
+         S.cell[6 + d] * f[2];
+}
 
 // Warp 0: trial t of a Widom job as an external insertion (FP64 positions).
 template <bool F32>
@@ -49,27 +71,75 @@ __device__ void widom_propose(BlockShared<F32> &B, const WidomJob &wj, int t) {
   }
   if (lane < 3 * ns) {
     const int s = lane / 3, d = lane % 3;
-    double v;
-    if (wj.xyz_in) {
-      v = wj.xyz_in[((size_t)t * ns + s) * 3 + d];
-    } else {
-      // grid point (1-based fractions) and a random orientation
-      // (random_rot with angle 2 pi, rotation about the origin)
-      const int gi = t / wj.nstep;
-      const int i = gi / (wj.ng[1] * wj.ng[2]) + 1, j = (gi / wj.ng[2]) % wj.ng[1] + 1,
-                k = gi % wj.ng[2] + 1;
-      const double f[3] = {double(i) / wj.ng[0], double(j) / wj.ng[1], double(k) / wj.ng[2]};
-      float dr[7];
-      for (int q = 3; q < 7; ++q) dr[q] = hash_uniform(wj.seed, 4ull * (unsigned long long)t + (q - 3));
-      double qt[4], row[3];
-      draw_quaternion(dr, 2.0 * kPi, qt);
-      qrow(qt, d, row);
-      const double *tp = G.tmpl[s];
-      v = row[0] * tp[0] + row[1] * tp[1] + row[2] * tp[2] + S.cell[d] * f[0] + S.cell[3 + d] * f[1] +
-          S.cell[6 + d] * f[2];
-    }
+    const double v = widom_site(S, G, wj, t, s, d);
     mc.pos[0][s][d] = v;
     if (wj.xyz_out) wj.xyz_out[((size_t)t * ns + s) * 3 + d] = v;
+  }
+}
+
+// Widom jobs on the FP32 path: warp w screens trial t0 + w against the
+// framework (27 neighbour cells) in float and either records it as an
+// overlap or leaves it in wsc.list for the full evaluation.  Out of line,
+// so the screen's registers stay out of the move loop's allocation.
+template <bool F32>
+__device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &wj, int t0) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const GuestType &G = B.S.g[wj.iguest];
+  const int ns = G.ns, lp = B.S.cpad_log2;
+  const int t = t0 + warp;
+  if (lane == 0) B.wsc.list[warp] = -1;
+  if (t < wj.ntrial) {
+    bool sane = true;
+    if (lane < 3 * ns) {
+      const int s = lane / 3, d = lane % 3;
+      float v;
+      if (wj.xyz_in) {
+        v = (float)wj.xyz_in[((size_t)t * ns + s) * 3 + d];
+      } else {
+        const int gi = t / wj.nstep;
+        const int i = gi / (wj.ng[1] * wj.ng[2]) + 1, j = (gi / wj.ng[2]) % wj.ng[1] + 1,
+                  k = gi % wj.ng[2] + 1;
+        const float f[3] = {(float)i / (float)wj.ng[0], (float)j / (float)wj.ng[1],
+                            (float)k / (float)wj.ng[2]};
+        float dr[7], q[4], row[3];
+        for (int r = 3; r < 7; ++r)
+          dr[r] = hash_uniform(wj.seed, 4ull * (unsigned long long)t + (r - 3));
+        quat_f32(dr, 1.0f, q);  // random_rot with angle 2 pi
+        qrow(q, d, row);
+        const float *tp = B.wsc.tmpl[s], *cl = B.wsc.cell;
+        v = row[0] * tp[0] + row[1] * tp[1] + row[2] * tp[2] + cl[d] * f[0] + cl[3 + d] * f[1] +
+            cl[6 + d] * f[2];
+      }
+      B.wsc.pos[warp][s][d] = v;
+      sane = fabsf(v) < 1.0e6f;  // NaN fails too
+    }
+    sane = __all_sync(0xffffffffu, sane);
+    __syncwarp();
+    bool hit = false;
+    if (sane) {
+      const float lim = B.S.overlap_sqf - kScreenMargin, zero[3] = {0.f, 0.f, 0.f};
+      const int nitem = (ns * 27) << lp;
+      for (int it = lane; it < nitem; it += 32) {
+        const int j = it & ((1 << lp) - 1), sc = it >> lp;
+        const int s = sc / 27, c = sc - 27 * s;
+        if (overlap_r2_27(B.S, B.wsc.pos[warp][s], zero, c, j) < lim) hit = true;
+      }
+    }
+    hit = __any_sync(0xffffffffu, hit);
+    if (lane == 0) {
+      if (hit) {
+        if (wj.estep_out) wj.estep_out[t] = 0.0;
+        if (wj.overlap_out) wj.overlap_out[t] = 1;
+        atomicAdd(&B.wsc.nscreened, 1);
+      } else {
+        B.wsc.list[warp] = t;
+      }
+    }
+    // the trial's positions as the full evaluation forms them
+    if (hit && wj.xyz_out && lane < 3 * ns) {
+      const int s = lane / 3, d = lane % 3;
+      wj.xyz_out[((size_t)t * ns + s) * 3 + d] = widom_site(B.S, G, wj, t, s, d);
+    }
   }
 }
 
@@ -262,7 +332,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (mode == kModeWidom) {
     double hsum = 0.0;
     long long nok = 0, ntot = 0;
-    for (int t = blockIdx.x; t < wj.ntrial; t += gridDim.x) {
+    // one trial through the full evaluation (the block)
+    auto full_trial = [&](int t) {
       if (threadIdx.x < 32) widom_propose(B, wj, t);
       __syncthreads();
       evaluate_any<F32, GN>(B, CA, chain, st);
@@ -282,7 +353,39 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       __syncthreads();
+    };
+    bool screened = false;
+    if constexpr (F32 && !kTricOk<F32, GN>) screened = overlap_27(B.S);
+    // Most test insertions end at the overlap test.  On the FP32 path with
+    // 27-cell overlap tests, each warp first screens one trial against the
+    // framework in float (widom_screen: a slot counts only when r^2 is
+    // below the overlap distance squared by a margin well above the float
+    // geometry's error), so a trial it marks overlapping overlaps in the
+    // full test too; the others go through the full evaluation, in trial
+    // order, so the Henry sum is the same every run.
+    const GuestType &G = B.S.g[wj.iguest];
+    const int ns = G.ns;
+    if (threadIdx.x == 0) B.wsc.nscreened = 0;
+    if (threadIdx.x < 9) B.wsc.cell[threadIdx.x] = (float)B.S.cell[threadIdx.x];
+    if (threadIdx.x >= 32 && threadIdx.x < 32 + 3 * ns)
+      B.wsc.tmpl[(threadIdx.x - 32) / 3][(threadIdx.x - 32) % 3] =
+          (float)G.tmpl[(threadIdx.x - 32) / 3][(threadIdx.x - 32) % 3];
+    __syncthreads();
+    for (int t0 = blockIdx.x * kWarps; t0 < wj.ntrial; t0 += gridDim.x * kWarps) {
+      if (screened) {
+        widom_screen(B, wj, t0);
+      } else if ((threadIdx.x & 31) == 0) {
+        const int t = t0 + (threadIdx.x >> 5);
+        B.wsc.list[threadIdx.x >> 5] = t < wj.ntrial ? t : -1;
+      }
+      __syncthreads();
+      for (int q = 0; q < kWarps; ++q) {
+        const int tq = B.wsc.list[q];
+        if (tq >= 0) full_trial(tq);
+      }
+      __syncthreads();
     }
+    if (threadIdx.x == 0) ntot += B.wsc.nscreened;
     if (threadIdx.x == 0) {
       wj.partial[3 * blockIdx.x] = hsum;
       wj.partial[3 * blockIdx.x + 1] = (double)nok;

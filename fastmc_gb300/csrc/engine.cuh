@@ -123,6 +123,13 @@ struct BlockShared {
     SelState sel;
   } spec[kMaxSpec];
   int spec_n, spec_exits, spec_have;
+  // Widom jobs: each warp's trial, screened against the framework
+  struct WidomScreen {
+    float pos[kWarps][kMaxS][3];  // the trial's sites in FP32
+    float cell[9], tmpl[kMaxS][3];  // the cell vectors and the guest's sites in float
+    int list[kWarps];             // per warp: its trial when the screen left it, else -1
+    int nscreened;
+  } wsc;
   float draws[8];
   float stepf[4];    // FP32 path: shift half-width and half-angle / pi scale, hi/lo
   float4 trig[kTrigN];  // FP32 path: the quaternion table (copied per launch)
@@ -1016,6 +1023,49 @@ __device__ void propose(BlockShared<F32> &B, const ChainArrays &CA, int chain, i
 // Any framework or guest site within the overlap distance of any site of
 // position 0: the test that lets an insertion or displacement exit before
 // the full sums (insertion / guest_energy, mc_moves.f:217-225, 347-355).
+// r^2 of one work item of the FP32 overlap test over 27 neighbour cells:
+// a site position as a hi/lo pair, neighbour cell c (0..26) of the cell
+// holding it and padded slot j of that cell (an empty slot lies far away).
+__device__ __forceinline__ float overlap_r2_27(const SysDev &S, const float *ph, const float *pl, int c,
+                                               int j) {
+  const int lp = S.cpad_log2;
+  const int o3[3] = {c / 9 - 1, (c / 3) % 3 - 1, c % 3 - 1};
+  int im[3], iw[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int ic = (int)floorf(ph[d] * S.rcszf[d]) + o3[d];
+    int k = 0;
+    if (ic < 0) k = -1;
+    else if (ic >= S.nc[d]) k = 1;
+    if (ic - k * S.nc[d] < 0 || ic - k * S.nc[d] >= S.nc[d]) k = image_of(ic, S.nc[d]);
+    im[d] = k;
+    iw[d] = ic - k * S.nc[d];
+  }
+  const size_t a = ((size_t)((iw[0] * S.nc[1] + iw[1]) * S.nc[2] + iw[2]) << lp) + j;
+  const float4 H = __ldg(S.cpad_hi + a), L = __ldg(S.cpad_lo + a);
+  float ah[3] = {H.x, H.y, H.z}, al[3] = {L.x, L.y, L.z};
+  float r2 = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (im[d] != 0) {
+      float h, e;
+      two_sum_f(ah[d], float(im[d]) * S.boxh[d], h, e);
+      ah[d] = h;
+      al[d] = al[d] + (e + float(im[d]) * S.boxl[d]);
+    }
+    float dd = (ph[d] - ah[d]) + (pl[d] - al[d]);
+    r2 = fmaf(dd, dd, r2);
+  }
+  return r2;
+}
+
+// The FP32 overlap test takes 27 neighbour cells (cells at least the
+// overlap distance wide).
+__device__ __forceinline__ bool overlap_27(const SysDev &S) {
+  const float mincs = fminf(S.cszf[0], fminf(S.cszf[1], S.cszf[2]));
+  return S.use_cells && mincs >= sqrtf(S.overlap_sqf) + 0.01f;
+}
+
 template <bool F32, bool TRIC>
 __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int chain) {
   const SysDev &S = B.S;
@@ -1039,34 +1089,7 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
         const int j = t & ((1 << lp) - 1);
         const int sc = t >> lp;
         const int s = sc / 27, c = sc - 27 * s;
-        const int o3[3] = {c / 9 - 1, (c / 3) % 3 - 1, c % 3 - 1};
-        int im[3], iw[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          int ic = (int)floorf(ev.phi[0][s][d] * S.rcszf[d]) + o3[d];
-          int k = 0;
-          if (ic < 0) k = -1;
-          else if (ic >= S.nc[d]) k = 1;
-          if (ic - k * S.nc[d] < 0 || ic - k * S.nc[d] >= S.nc[d]) k = image_of(ic, S.nc[d]);
-          im[d] = k;
-          iw[d] = ic - k * S.nc[d];
-        }
-        const size_t a = ((size_t)((iw[0] * S.nc[1] + iw[1]) * S.nc[2] + iw[2]) << lp) + j;
-        const float4 H = __ldg(S.cpad_hi + a), L = __ldg(S.cpad_lo + a);
-        float ah[3] = {H.x, H.y, H.z}, al[3] = {L.x, L.y, L.z};
-        float r2 = 0.f;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          if (im[d] != 0) {
-            float h, e;
-            two_sum_f(ah[d], float(im[d]) * S.boxh[d], h, e);
-            ah[d] = h;
-            al[d] = al[d] + (e + float(im[d]) * S.boxl[d]);
-          }
-          float dd = (ev.phi[0][s][d] - ah[d]) + (ev.plo[0][s][d] - al[d]);
-          r2 = fmaf(dd, dd, r2);
-        }
-        if (r2 < S.overlap_sqf) hit = 1;
+        if (overlap_r2_27(S, ev.phi[0][s], ev.plo[0][s], c, j) < S.overlap_sqf) hit = 1;
       }
     } else
     for (int t = threadIdx.x; t < ns * per_site && !hit; t += kThreads) {
