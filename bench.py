@@ -456,10 +456,12 @@ def per_move_abi(F, batch, systems, dirs, specs, seconds=1.0):
                         "oracle replays the first 2000 of those moves with the same decisions"}
 
 
-def widom_102A(F, tmp):
+def widom_102A(F, tmp, gcmc_moves=4096):
     """Test insertions into the large framework: 1e7 Widom trials (a 100^3 grid x 10
     orientations, one launch) against the 102.4 A framework (98304 atoms,
-    cutoff 14 A, kmax 20) with 2000 CO2 loaded, FP32 terms."""
+    cutoff 14 A, kmax 20) with 2000 CO2 loaded, FP32 terms; then GCMC moves
+    of that chain (its cluster autotuned, speculative rounds on): a sample
+    of gcmc_moves moves timed, rate per second."""
     from fastmc_gb300 import synthetic as syn
     d = os.path.join(tmp, "widom102")
     syn.write_inputs(d, syn.widom_102A())
@@ -469,8 +471,19 @@ def widom_102A(F, tmp):
     t0 = time.perf_counter()
     h, nok, ntot = b.widom_grid(0, (100, 100, 100), 10, seed=2)
     s = time.perf_counter() - t0
+    b.set_speculation(8)
+    b.autotune(256)
+    b.run(256)  # warm-up
+    st0 = b.stats()[0]
+    t0 = time.perf_counter()
+    b.run(gcmc_moves)
+    sm = time.perf_counter() - t0
+    st1 = b.stats()[0]
     return {"value": ntot / s, "unit": "trial insertions/s", "trials": ntot,
             "non_overlapping": nok, "henry": h, "seconds": s,
+            "gcmc": {"moves": gcmc_moves, "seconds": sm, "moves_per_s": gcmc_moves / sm,
+                     "evals_per_s": (trial_evals(st1) - trial_evals(st0)) / sm,
+                     "ctas": b.cluster()[0], "molecules": int(st1.nummols)},
             "workload": "102.4 A, 98304 atoms, 2000 CO2, cutoff 14 A, kmax 20, FP32"}
 
 
