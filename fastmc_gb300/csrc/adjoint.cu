@@ -1,6 +1,11 @@
-// adjoint.cu -- guest-framework interaction energy of a guest snapshot and
-// its adjoint: dE/d(guest site coordinates) and dE/d(epsilon, sigma, charge
-// scale) of every framework atom type.  No counterpart in the reference.
+// adjoint.cu -- energies of guest snapshots and their adjoints:
+// dE/d(guest site coordinates) and dE/d(epsilon, sigma, charge scale) of
+// every framework atom type.  No counterpart in the reference.  Two entry
+// points: fmc_adjoint_eval_batch, the energy the chains sample (the
+// reference's tables, guests with each other too) for a batch of
+// snapshots (the `ham_*` kernels, "the sampled Hamiltonian" below), and
+// fmc_adjoint_eval, the guest-framework energy of one snapshot with exact
+// erfc and analytic Lennard-Jones (the `adj_*` kernels), described here:
 //
 // E = sum over guest sites i and framework atoms j within the cutoff of
 //       q_i lambda_t q_j r4pie0/epsq erfc(alpha r)/r
