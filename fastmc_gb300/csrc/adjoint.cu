@@ -39,6 +39,7 @@ using fmc::Error;
 using fmc::raise;
 using fmcdev::kPi;
 using fmcdev::kSqrPi;
+using fmcdev::rint_image;
 
 #define FMC_ACUDA(x)                                                                \
   do {                                                                              \
@@ -384,13 +385,14 @@ __device__ __forceinline__ void split_hl(double x, float &h, float &l) {
 // a - b to the nearest image along one axis, a and b as hi/lo float pairs
 // in [0, L): the hi difference with its exact rounding error (two-sum),
 // the image taken off the hi part (exact: it is within a factor two of the
-// cell edge), then the low parts.
+// cell edge), then the low parts (|t / L| < 1: rint_image takes the
+// nearest integer by comparisons).
 __device__ __forceinline__ float mi_hl(float ah, float al, float bh, float bl, float Lh, float Ll,
                                        float rL) {
   const float t = ah - bh;
   const float bb = t - ah;
   const float e = (ah - (t - bb)) + (-bh - bb);
-  const float n = rintf(t * rL);
+  const float n = rint_image(t * rL);
   return (t - n * Lh) + ((e + (al - bl)) - n * Ll);
 }
 

@@ -646,6 +646,16 @@ __device__ inline int block_scan(int v, int &excl, int *scratch) {
 // A value held as an unevaluated sum hi + lo of two floats (about 48
 // significant bits).  Used for the FP32 path's accumulators and for its
 // running structure factor, so no FP64 instruction is needed there.
+// rint(x) for the minimum image of two points in or near one cell: with
+// |x| < 1.5 the result is -1, 0 or 1 (ties to even as rint: 0 at +-1/2),
+// taken by comparisons; a rounding instruction only otherwise (those issue
+// to the FP64 pipe, narrow on this part, and sit on the pair's dependency
+// chain).  The same value as rintf(x) except for the sign of a zero.
+__device__ __forceinline__ float rint_image(float x) {
+  if (fabsf(x) < 1.5f) return (x > 0.5f ? 1.f : 0.f) - (x < -0.5f ? 1.f : 0.f);
+  return rintf(x);
+}
+
 __device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) {
   s = a + b;
   float bb = s - a;

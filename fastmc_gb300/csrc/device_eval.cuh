@@ -210,7 +210,7 @@ __device__ __forceinline__ DF vdw_near_df(const SysDev &S, const SiteInfo &si, i
 __device__ __forceinline__ float mi_diff32(float ph, float pl, float qh, float ql, float Lh,
                                            float Ll, float rL) {
   float dh = ph - qh;
-  float k = rintf(dh * rL);
+  float k = rint_image(dh * rL);
   if (k != 0.0f) {
     float h, e;
     two_sum_f(ph, -k * Lh, h, e);
@@ -222,7 +222,7 @@ __device__ __forceinline__ float mi_diff32(float ph, float pl, float qh, float q
 // The same difference as a hi/lo pair (close pairs).
 __device__ __forceinline__ void mi_diff_df(float ph, float pl, float qh, float ql, float Lh,
                                            float Ll, float rL, float &dh, float &dl) {
-  float k = rintf((ph - qh) * rL);
+  float k = rint_image((ph - qh) * rL);
   float a = ph, al = pl;
   if (k != 0.0f) {
     float h, e;
@@ -571,9 +571,9 @@ __device__ __forceinline__ void scan_guests(const SysDev &S, const ChainHdr &H,
         float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y,
               dz = sm.phi[pos][0][2] - q0.z;
         if (!tric) {
-          dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
-          dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
-          dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+          dx -= S.boxh[0] * rint_image(dx * S.rboxf[0]);
+          dy -= S.boxh[1] * rint_image(dy * S.rboxf[1]);
+          dz -= S.boxh[2] * rint_image(dz * S.rboxf[2]);
           if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
         } else if (tric_r2_f32(S, dx, dy, dz) > pre2) {
           continue;

@@ -1166,9 +1166,9 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
       if (i == mc.slot) continue;
       const float4 q0 = B.grh[i * ns2];
       float dx = ev.phi[0][0][0] - q0.x, dy = ev.phi[0][0][1] - q0.y, dz = ev.phi[0][0][2] - q0.z;
-      dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
-      dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
-      dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+      dx -= S.boxh[0] * rint_image(dx * S.rboxf[0]);
+      dy -= S.boxh[1] * rint_image(dy * S.rboxf[1]);
+      dz -= S.boxh[2] * rint_image(dz * S.rboxf[2]);
       if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
       for (int b = 0; b < ns2; ++b) {
         const float4 qh = B.grh[i * ns2 + b], ql = B.grl[i * ns2 + b];
@@ -1201,9 +1201,9 @@ __device__ int overlap_check(BlockShared<F32> &B, const ChainArrays &CA, int cha
         float4 q0 = gh[(size_t)slot * kMaxS];
         float dx = ev.phi[0][0][0] - q0.x, dy = ev.phi[0][0][1] - q0.y, dz = ev.phi[0][0][2] - q0.z;
         if (!TRIC || S.use_cells) {
-          dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
-          dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
-          dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+          dx -= S.boxh[0] * rint_image(dx * S.rboxf[0]);
+          dy -= S.boxh[1] * rint_image(dy * S.rboxf[1]);
+          dz -= S.boxh[2] * rint_image(dz * S.rboxf[2]);
           if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
         } else if (tric_r2_f32(S, dx, dy, dz) > pre2) {
           continue;
@@ -1532,9 +1532,9 @@ __device__ __forceinline__ void scan_guests_resident(BlockShared<F32> &B, int po
     if (i == self_i) continue;
     const float4 q0 = B.grh[i * ns2];
     float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y, dz = sm.phi[pos][0][2] - q0.z;
-    dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
-    dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
-    dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+    dx -= S.boxh[0] * rint_image(dx * S.rboxf[0]);
+    dy -= S.boxh[1] * rint_image(dy * S.rboxf[1]);
+    dz -= S.boxh[2] * rint_image(dz * S.rboxf[2]);
     if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
     float vdw = 0.f;
 #pragma unroll
@@ -1615,9 +1615,9 @@ __device__ __forceinline__ bool list_near_guests(BlockShared<F32> &B, const Site
     if (i < i1 && !gs.is_self(i, self_slot)) {
       const float4 q0 = gs.hi(i, 0);
       float dx = sm.phi[pos][0][0] - q0.x, dy = sm.phi[pos][0][1] - q0.y, dz = sm.phi[pos][0][2] - q0.z;
-      dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
-      dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
-      dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+      dx -= S.boxh[0] * rint_image(dx * S.rboxf[0]);
+      dy -= S.boxh[1] * rint_image(dy * S.rboxf[1]);
+      dz -= S.boxh[2] * rint_image(dz * S.rboxf[2]);
       if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= pre2) {
         if (cnt == 0) m0 = i;
         else m1 = i;
@@ -2437,9 +2437,9 @@ __device__ void overlap_batch(BlockShared<F32> &B, int n) {
     if (P.kind != 1 && i == P.slot) continue;  // the moving molecule itself
     const float4 q0 = B.grh[i * ns];
     float dx = P.phi[0][0][0] - q0.x, dy = P.phi[0][0][1] - q0.y, dz = P.phi[0][0][2] - q0.z;
-    dx -= S.boxh[0] * rintf(dx * S.rboxf[0]);
-    dy -= S.boxh[1] * rintf(dy * S.rboxf[1]);
-    dz -= S.boxh[2] * rintf(dz * S.rboxf[2]);
+    dx -= S.boxh[0] * rint_image(dx * S.rboxf[0]);
+    dy -= S.boxh[1] * rint_image(dy * S.rboxf[1]);
+    dz -= S.boxh[2] * rint_image(dz * S.rboxf[2]);
     if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) > pre2) continue;
     int hit = 0;
     for (int b = 0; b < ns; ++b) {
