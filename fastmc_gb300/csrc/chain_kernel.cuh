@@ -119,10 +119,20 @@ __device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &w
     if (sane) {
       const float lim = B.S.overlap_sqf - kScreenMargin, zero[3] = {0.f, 0.f, 0.f};
       const int nitem = (ns * 27) << lp;
-      for (int it = lane; it < nitem; it += 32) {
-        const int j = it & ((1 << lp) - 1), sc = it >> lp;
-        const int s = sc / 27, c = sc - 27 * s;
-        if (overlap_r2_27(B.S, B.wsc.pos[warp][s], zero, c, j) < lim) hit = true;
+      // two slots per lane in flight, then stop at the first round that
+      // found one (an overlapping trial usually does within its first
+      // site's cells)
+      for (int base = 0; base < nitem; base += 64) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int it = base + 32 * u + lane;
+          if (it < nitem) {
+            const int j = it & ((1 << lp) - 1), sc = it >> lp;
+            const int s = sc / 27, c = sc - 27 * s;
+            if (overlap_r2_27(B.S, B.wsc.pos[warp][s], zero, c, j) < lim) hit = true;
+          }
+        }
+        if (__any_sync(0xffffffffu, hit)) break;
       }
     }
     hit = __any_sync(0xffffffffu, hit);
