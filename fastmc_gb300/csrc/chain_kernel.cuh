@@ -23,7 +23,8 @@ constexpr int kModeCommit = 3;  // decide with gctx.rande and commit
 constexpr int kModeWidom = 4;   // test insertions of a WidomJob (no state change)
 constexpr int kModeLoad = 5;    // insert a WidomJob's positions into chain wj.chain (restart)
 // Widom screen: margin (A^2) on the overlap distance squared, far above the
-// error of a float trial geometry (~1e-5 A in a 100 A cell)
+// error of a float trial geometry (~1e-5 A in a 100 A cell); trials per
+// warp between the block's barriers
 constexpr float kScreenMargin = 1e-3f;
 
 // Coordinate d of site s of trial t of a Widom job (FP64): the caller's
@@ -77,18 +78,22 @@ __device__ void widom_propose(BlockShared<F32> &B, const WidomJob &wj, int t) {
   }
 }
 
-// Widom jobs on the FP32 path: warp w screens trial t0 + w against the
-// framework (27 neighbour cells) in float and either records it as an
-// overlap or leaves it in wsc.list for the full evaluation.  Out of line,
-// so the screen's registers stay out of the move loop's allocation.
+// Widom jobs on the FP32 path: warp w screens trials t0 + k kWarps + w
+// (k < kScreenPer) against the framework (27 neighbour cells) in float and
+// records each either as an overlap or in wsc.list[k][w] for the full
+// evaluation.  Several trials per warp between the block's barriers, so a
+// warp whose trial needs the whole scan does not hold the others up.  Out
+// of line, so the screen's registers stay out of the move loop's
+// allocation.
 template <bool F32>
 __device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &wj, int t0) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const GuestType &G = B.S.g[wj.iguest];
   const int ns = G.ns, lp = B.S.cpad_log2;
-  const int t = t0 + warp;
-  if (lane == 0) B.wsc.list[warp] = -1;
-  if (t < wj.ntrial) {
+  for (int kk = 0; kk < kScreenPer; ++kk) {
+    const int t = t0 + kk * kWarps + warp;
+    if (lane == 0) B.wsc.list[kk][warp] = -1;
+    if (t >= wj.ntrial) continue;
     bool sane = true;
     if (lane < 3 * ns) {
       const int s = lane / 3, d = lane % 3;
@@ -142,7 +147,7 @@ __device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &w
         if (wj.overlap_out) wj.overlap_out[t] = 1;
         atomicAdd(&B.wsc.nscreened, 1);
       } else {
-        B.wsc.list[warp] = t;
+        B.wsc.list[kk][warp] = t;
       }
     }
     // the trial's positions as the full evaluation forms them
@@ -150,6 +155,7 @@ __device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &w
       const int s = lane / 3, d = lane % 3;
       wj.xyz_out[((size_t)t * ns + s) * 3 + d] = widom_site(B.S, G, wj, t, s, d);
     }
+    __syncwarp();  // the next trial's positions go where this one's were read
   }
 }
 
@@ -381,18 +387,22 @@ __global__ void __launch_bounds__(kThreads, 1)
       B.wsc.tmpl[(threadIdx.x - 32) / 3][(threadIdx.x - 32) % 3] =
           (float)G.tmpl[(threadIdx.x - 32) / 3][(threadIdx.x - 32) % 3];
     __syncthreads();
-    for (int t0 = blockIdx.x * kWarps; t0 < wj.ntrial; t0 += gridDim.x * kWarps) {
+    constexpr int kChunk = kWarps * kScreenPer;  // trials per block between barriers
+    for (int t0 = blockIdx.x * kChunk; t0 < wj.ntrial; t0 += gridDim.x * kChunk) {
       if (screened) {
         widom_screen(B, wj, t0);
       } else if ((threadIdx.x & 31) == 0) {
-        const int t = t0 + (threadIdx.x >> 5);
-        B.wsc.list[threadIdx.x >> 5] = t < wj.ntrial ? t : -1;
+        for (int kk = 0; kk < kScreenPer; ++kk) {
+          const int t = t0 + kk * kWarps + (threadIdx.x >> 5);
+          B.wsc.list[kk][threadIdx.x >> 5] = t < wj.ntrial ? t : -1;
+        }
       }
       __syncthreads();
-      for (int q = 0; q < kWarps; ++q) {
-        const int tq = B.wsc.list[q];
-        if (tq >= 0) full_trial(tq);
-      }
+      for (int kk = 0; kk < kScreenPer; ++kk)
+        for (int q = 0; q < kWarps; ++q) {
+          const int tq = B.wsc.list[kk][q];
+          if (tq >= 0) full_trial(tq);
+        }
       __syncthreads();
     }
     if (threadIdx.x == 0) ntot += B.wsc.nscreened;

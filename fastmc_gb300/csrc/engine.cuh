@@ -65,6 +65,7 @@ struct LogRec {  // mirrors fmc_move_log
 };
 
 constexpr int kMaxSpec = 8;  // proposals of one speculative round
+constexpr int kScreenPer = 8;  // Widom trials each warp screens between the block's barriers
 
 // Parallelepiped cells (imcon 3) are compiled into the FP64 kernel and the
 // multi-type FP32 kernel; the single-type FP32 kernel (orthorhombic batches)
@@ -127,7 +128,7 @@ struct BlockShared {
   struct WidomScreen {
     float pos[kWarps][kMaxS][3];  // the trial's sites in FP32
     float cell[9], tmpl[kMaxS][3];  // the cell vectors and the guest's sites in float
-    int list[kWarps];             // per warp: its trial when the screen left it, else -1
+    int list[kScreenPer][kWarps];  // per round and warp: the trial the screen left, else -1
     int nscreened;
   } wsc;
   float draws[8];
