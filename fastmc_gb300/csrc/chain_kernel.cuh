@@ -78,22 +78,30 @@ __device__ void widom_propose(BlockShared<F32> &B, const WidomJob &wj, int t) {
   }
 }
 
-// Widom jobs on the FP32 path: warp w screens trials t0 + k kWarps + w
-// (k < kScreenPer) against the framework (27 neighbour cells) in float and
-// records each either as an overlap or in wsc.list[k][w] for the full
-// evaluation.  Several trials per warp between the block's barriers, so a
-// warp whose trial needs the whole scan does not hold the others up.  Out
-// of line, so the screen's registers stay out of the move loop's
+// Trial of warp w in round k of chunk c of this block: blocks take every
+// gridDim-th group of kWarps trials, so the trials that need the full
+// evaluation spread over the blocks as the grid points do.
+__device__ __forceinline__ long long widom_trial(int c, int k, int w) {
+  return ((long long)(c * kScreenPer + k) * gridDim.x + blockIdx.x) * kWarps + w;
+}
+
+// Widom jobs on the FP32 path: warp w screens its trials of chunk c (one
+// per round k < kScreenPer) against the framework (27 neighbour cells) in
+// float and records each either as an overlap or in wsc.list[k][w] for the
+// full evaluation.  Several trials per warp between the block's barriers,
+// so a warp whose trial needs the whole scan does not hold the others up.
+// Out of line, so the screen's registers stay out of the move loop's
 // allocation.
 template <bool F32>
-__device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &wj, int t0) {
+__device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &wj, int chunk) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const GuestType &G = B.S.g[wj.iguest];
   const int ns = G.ns, lp = B.S.cpad_log2;
   for (int kk = 0; kk < kScreenPer; ++kk) {
-    const int t = t0 + kk * kWarps + warp;
+    const long long tl = widom_trial(chunk, kk, warp);
     if (lane == 0) B.wsc.list[kk][warp] = -1;
-    if (t >= wj.ntrial) continue;
+    if (tl >= wj.ntrial) continue;
+    const int t = (int)tl;
     bool sane = true;
     if (lane < 3 * ns) {
       const int s = lane / 3, d = lane % 3;
@@ -387,14 +395,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       B.wsc.tmpl[(threadIdx.x - 32) / 3][(threadIdx.x - 32) % 3] =
           (float)G.tmpl[(threadIdx.x - 32) / 3][(threadIdx.x - 32) % 3];
     __syncthreads();
-    constexpr int kChunk = kWarps * kScreenPer;  // trials per block between barriers
-    for (int t0 = blockIdx.x * kChunk; t0 < wj.ntrial; t0 += gridDim.x * kChunk) {
+    for (int c = 0; widom_trial(c, 0, 0) < wj.ntrial; ++c) {  // chunks of kScreenPer rounds
       if (screened) {
-        widom_screen(B, wj, t0);
+        widom_screen(B, wj, c);
       } else if ((threadIdx.x & 31) == 0) {
         for (int kk = 0; kk < kScreenPer; ++kk) {
-          const int t = t0 + kk * kWarps + (threadIdx.x >> 5);
-          B.wsc.list[kk][threadIdx.x >> 5] = t < wj.ntrial ? t : -1;
+          const long long t = widom_trial(c, kk, threadIdx.x >> 5);
+          B.wsc.list[kk][threadIdx.x >> 5] = t < wj.ntrial ? (int)t : -1;
         }
       }
       __syncthreads();
