@@ -65,7 +65,10 @@ struct LogRec {  // mirrors fmc_move_log
 };
 
 constexpr int kMaxSpec = 8;  // proposals of one speculative round
-constexpr int kScreenPer = 8;  // Widom trials each warp screens between the block's barriers
+// Widom trials each warp screens between the block's barriers (8 measured
+// no faster than 1 on the 102.4 A benchmark: the clear trials' full
+// evaluations set the pace)
+constexpr int kScreenPer = 1;
 
 // Parallelepiped cells (imcon 3) are compiled into the FP64 kernel and the
 // multi-type FP32 kernel; the single-type FP32 kernel (orthorhombic batches)
