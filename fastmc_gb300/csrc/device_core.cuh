@@ -796,11 +796,11 @@ __device__ int block_reduce_pos(const PosAcc<F32, GN> &a0, const PosAcc<F32, GN>
   // OR of the per-thread flag bits rides on the same barriers
   const int wf = __reduce_or_sync(0xffffffffu, (unsigned)flags);
   if (lane == 0) iscratch[w] = wf;
-  // every value reduced, the unused ones (zero) too: no branch between the
-  // values, so their shuffle rounds overlap instead of following one another
 #pragma unroll
   for (int i = 0; i < 2 * N; ++i) {
     const int p = i / N, j = i % N;
+    if (p >= npos) continue;
+    if (j >= 4 && (j - 4) % GN >= ng) continue;
     const auto x = warp_total(p == 0 ? a0.at(j) : a1.at(j));
     if (lane == 0) {
       if constexpr (F32) {
