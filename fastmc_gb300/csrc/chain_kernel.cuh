@@ -132,21 +132,17 @@ __device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &w
     if (sane) {
       const float lim = B.S.overlap_sqf - kScreenMargin, zero[3] = {0.f, 0.f, 0.f};
       const int nitem = (ns * 27) << lp;
-      // the sites' own cells first, then the face, edge and corner
-      // neighbours (cell c = 9 (dx+1) + 3 (dy+1) + dz+1), the sites
-      // interleaved; two slots per lane in flight, and a stop at the first
-      // round that found one: an overlapping trial usually does in its
-      // first round
-      constexpr unsigned char kOrder[27] = {13, 4,  10, 12, 14, 16, 22, 1,  3,  5,  7,  9,  11, 15,
-                                            17, 19, 21, 23, 25, 0,  2,  6,  8,  18, 20, 24, 26};
+      // two slots per lane in flight, then stop at the first round that
+      // found one (an overlapping trial usually does within its first
+      // site's cells)
       for (int base = 0; base < nitem; base += 64) {
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           const int it = base + 32 * u + lane;
           if (it < nitem) {
-            const int j = it & ((1 << lp) - 1), q = it >> lp;
-            const int r = q / ns, s = q - ns * r;
-            if (overlap_r2_27(B.S, B.wsc.pos[warp][s], zero, kOrder[r], j) < lim) hit = true;
+            const int j = it & ((1 << lp) - 1), sc = it >> lp;
+            const int s = sc / 27, c = sc - 27 * s;
+            if (overlap_r2_27(B.S, B.wsc.pos[warp][s], zero, c, j) < lim) hit = true;
           }
         }
         if (__any_sync(0xffffffffu, hit)) break;
