@@ -486,9 +486,12 @@ __global__ void __launch_bounds__(kHT) ham_real_kernel(
   if (threadIdx.x < 3 * ns) {
     const int d = threadIdx.x % 3;
     const double x = xyz[(size_t)m * ns * 3 + threadIdx.x];
-    const double w = x - c.L[d] * floor(x * c.rL[d]);
+    double w = x - c.L[d] * floor(x * c.rL[d]);
+    // a coordinate that is not finite, or so large that the wrap leaves the
+    // cell, gives a meaningless energy but no index outside the cell lists
+    if (!(w >= 0.0 && w <= c.L[d])) w = 0.0;
     site[threadIdx.x / 3][d] = w;
-    sitecell[threadIdx.x / 3][d] = min(c.nc[d] - 1, (int)(w * c.rL[d] * c.nc[d]));
+    sitecell[threadIdx.x / 3][d] = max(0, min(c.nc[d] - 1, (int)(w * c.rL[d] * c.nc[d])));
     split_hl(w, sitef[threadIdx.x / 3][2 * d], sitef[threadIdx.x / 3][2 * d + 1]);
   }
   __syncthreads();
