@@ -132,12 +132,12 @@ __device__ __noinline__ void widom_screen(BlockShared<F32> &B, const WidomJob &w
     if (sane) {
       const float lim = B.S.overlap_sqf - kScreenMargin, zero[3] = {0.f, 0.f, 0.f};
       const int nitem = (ns * 27) << lp;
-      // four slots per lane in flight, then stop at the first round that
+      // two slots per lane in flight, then stop at the first round that
       // found one (an overlapping trial usually does within its first
       // site's cells)
-      for (int base = 0; base < nitem; base += 128) {
+      for (int base = 0; base < nitem; base += 64) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < 2; ++u) {
           const int it = base + 32 * u + lane;
           if (it < nitem) {
             const int j = it & ((1 << lp) - 1), sc = it >> lp;
