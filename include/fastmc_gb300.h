@@ -487,7 +487,9 @@ int fmc_adjoint_destroy(fmc_adjoint *a);
  * Out: energy[q] (host), gxyz (device, float, 3 per site: dE/dxyz),
  * gparams[q][t][3] (host).  precision: FMC_PREC_FP64 (pair terms and
  * phases in FP64) or FMC_PREC_FP32 (in FP32, sums in FP64).  Orthorhombic
- * cells, one guest type.  No counterpart in the reference. */
+ * cells, one guest type.  The handle keeps its device buffers between
+ * calls (grown to the largest batch): one call at a time per handle.  No
+ * counterpart in the reference. */
 int fmc_adjoint_eval_batch(fmc_adjoint *a, int nsnap, const int *nmol, const double *xyz,
                            const double *params, int precision, double *energy, float *gxyz,
                            double *gparams);
